@@ -1,0 +1,342 @@
+"""ctypes binding of the C ABI declared in include/avbdg.h.
+
+The binding is generic over the symbol prefix: the GPU library exports ``avbdg_*``; test
+infrastructure builds other libraries that export the same world API under other prefixes and
+drives them through this same class.
+"""
+
+import ctypes as C
+
+import numpy as np
+
+OK = 0
+ERR_INVALID = -1
+ERR_CAPACITY = -2
+ERR_NONFINITE = -3
+ERR_TIMEOUT = -4
+ERR_CUDA = -5
+ERR_UNSUPPORTED = -6
+
+SHAPE_BOX = 0
+SHAPE_SPHERE = 1
+SHAPE_CYLINDER = 2
+
+
+class Params(C.Structure):
+    """avbdg_params: the public fields of avbd::Solver (src/avbd/solver.h:54-144)."""
+
+    _fields_ = [
+        ("dt", C.c_float),
+        ("gravity", C.c_float),
+        ("iterations", C.c_int),
+        ("alpha", C.c_float),
+        ("beta_lin", C.c_float),
+        ("beta_ang", C.c_float),
+        ("gamma", C.c_float),
+        ("newton_ratio", C.c_float),
+        ("stiffness_decay", C.c_float),
+        ("adaptive_beta", C.c_int),
+        ("adaptive_beta_error_floor", C.c_float),
+        ("convergence_threshold", C.c_float),
+        ("jacobi_relaxation", C.c_float),
+        ("contact_only_overflow", C.c_int),
+        ("stick_drift_heal", C.c_float),
+        ("max_penetration", C.c_float),
+        ("jacobian_rebuild_distance", C.c_float),
+        ("speculative_margin", C.c_float),
+        ("position_projection", C.c_int),
+        ("projection_iterations", C.c_int),
+        ("projection_beta", C.c_float),
+        ("projection_slop", C.c_float),
+        ("projection_max_correction", C.c_float),
+        ("contact_grace_ticks", C.c_int),
+        ("sleep_linear_threshold", C.c_float),
+        ("sleep_angular_threshold", C.c_float),
+        ("sleep_frames", C.c_int),
+        ("threads", C.c_int),
+    ]
+
+
+class BodyDesc(C.Structure):
+    """avbdg_body_desc: arguments of Rigid::Rigid plus post-construction fields."""
+
+    _fields_ = [
+        ("size", C.c_float * 3),
+        ("shape", C.c_int),
+        ("density", C.c_float),
+        ("friction", C.c_float),
+        ("position", C.c_float * 3),
+        ("orientation", C.c_float * 4),
+        ("velocity", C.c_float * 3),
+        ("angular_velocity", C.c_float * 3),
+        ("collision_layer", C.c_uint32),
+        ("collision_mask", C.c_uint32),
+        ("axis_lock_linear", C.c_uint32),
+        ("axis_lock_angular", C.c_uint32),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("bodies", C.c_int),
+        ("dynamic_bodies", C.c_int),
+        ("forces", C.c_int),
+        ("broad_pairs", C.c_int),
+        ("manifolds", C.c_int),
+        ("contacts", C.c_int),
+        ("colour_groups", C.c_int),
+        ("overflow_bodies", C.c_int),
+        ("update_bodies", C.c_int),
+        ("steps", C.c_int),
+        ("broad_ms", C.c_double),
+        ("graph_ms", C.c_double),
+        ("solve_ms", C.c_double),
+        ("finish_ms", C.c_double),
+        ("total_ms", C.c_double),
+    ]
+
+
+class AvbdError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"AVBD call failed ({code}): {message}")
+        self.code = code
+
+
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int32)
+_up = C.POINTER(C.c_uint64)
+_bp = C.POINTER(C.c_uint8)
+
+# name -> argtypes (after the handle where one is taken); all return int.
+_WORLD_FUNCS = {
+    "params_default": [C.POINTER(Params)],
+    "world_create": [C.POINTER(Params), C.c_int, C.c_int, C.POINTER(C.c_void_p)],
+    "world_destroy": [C.c_void_p],
+    "world_clear": [C.c_void_p],
+    "world_set_params": [C.c_void_p, C.POINTER(Params)],
+    "world_get_params": [C.c_void_p, C.POINTER(Params)],
+    "world_add_bodies": [C.c_void_p, C.c_int, C.POINTER(BodyDesc), C.POINTER(C.c_int)],
+    "world_add_joint": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, C.c_float, C.c_float, C.c_float,
+                        C.POINTER(C.c_int)],
+    "world_add_ignore_collision": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)],
+    "world_step": [C.c_void_p],
+    "world_step_interleaved": [C.c_void_p, C.c_int, C.c_int],
+    "world_step_n": [C.c_void_p, C.c_int],
+    "world_sync": [C.c_void_p],
+    "world_get_body_state": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp, _fp],
+    "world_set_body_state": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp, _fp],
+    "world_get_stats": [C.c_void_p, C.POINTER(Stats)],
+    "world_digest": [C.c_void_p, _up],
+    "world_dump_broadphase": [C.c_void_p, _up, _ip, C.c_int, _up, C.c_int, C.POINTER(C.c_int),
+                              C.POINTER(C.c_int)],
+    "world_dump_manifolds": [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _fp, _fp, _fp, _fp,
+                             C.POINTER(C.c_int)],
+    "world_dump_colours": [C.c_void_p, C.c_int, _bp, _ip, C.POINTER(C.c_int)],
+}
+
+
+def _ptr(a, ctype):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Api:
+    """The world API of one shared library, bound under `prefix` (e.g. "avbdg_")."""
+
+    def __init__(self, lib, prefix):
+        self.lib = lib
+        self.prefix = prefix
+        for name, argtypes in _WORLD_FUNCS.items():
+            fn = getattr(lib, prefix + name)
+            fn.argtypes = argtypes
+            fn.restype = C.c_int
+            setattr(self, name, fn)
+        err = getattr(lib, prefix + "last_error")
+        err.argtypes = []
+        err.restype = C.c_char_p
+        self._last_error = err
+
+    def check(self, rc):
+        if rc != OK:
+            raise AvbdError(rc, self._last_error().decode(errors="replace"))
+        return rc
+
+    def default_params(self):
+        p = Params()
+        self.check(self.params_default(C.byref(p)))
+        return p
+
+
+def make_body_descs(size, density, friction, position, orientation=None, velocity=None,
+                    angular_velocity=None):
+    """Pack per-body arrays (n x 3 / n x 4 / n) into an avbdg_body_desc array."""
+    size = np.asarray(size, np.float32).reshape(-1, 3)
+    n = size.shape[0]
+    density = np.broadcast_to(np.asarray(density, np.float32), (n,))
+    friction = np.broadcast_to(np.asarray(friction, np.float32), (n,))
+    position = np.asarray(position, np.float32).reshape(n, 3)
+    if orientation is None:
+        orientation = np.tile(np.array([0, 0, 0, 1], np.float32), (n, 1))
+    orientation = np.asarray(orientation, np.float32).reshape(n, 4)
+    velocity = np.zeros((n, 3), np.float32) if velocity is None else np.asarray(velocity, np.float32).reshape(n, 3)
+    if angular_velocity is None:
+        angular_velocity = np.zeros((n, 3), np.float32)
+    angular_velocity = np.asarray(angular_velocity, np.float32).reshape(n, 3)
+    descs = (BodyDesc * n)()
+    for i in range(n):
+        d = descs[i]
+        d.size[:] = size[i].tolist()
+        d.shape = SHAPE_BOX
+        d.density = float(density[i])
+        d.friction = float(friction[i])
+        d.position[:] = position[i].tolist()
+        d.orientation[:] = orientation[i].tolist()
+        d.velocity[:] = velocity[i].tolist()
+        d.angular_velocity[:] = angular_velocity[i].tolist()
+        d.collision_layer = 1
+        d.collision_mask = 1
+        d.axis_lock_linear = 0
+        d.axis_lock_angular = 0
+    return descs
+
+
+class World:
+    """One avbd::Solver behind the C ABI (any implementation bound by `Api`)."""
+
+    def __init__(self, api, params=None, max_bodies=0, max_forces=0):
+        self.api = api
+        p = api.default_params() if params is None else params
+        h = C.c_void_p()
+        api.check(api.world_create(C.byref(p), int(max_bodies), int(max_forces), C.byref(h)))
+        self.handle = h
+        self.n_bodies = 0
+
+    def close(self):
+        if self.handle:
+            self.api.world_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self):
+        p = Params()
+        self.api.check(self.api.world_get_params(self.handle, C.byref(p)))
+        return p
+
+    @params.setter
+    def params(self, p):
+        self.api.check(self.api.world_set_params(self.handle, C.byref(p)))
+
+    def add_bodies(self, descs):
+        n = len(descs)
+        ids = (C.c_int * n)()
+        self.api.check(self.api.world_add_bodies(self.handle, n, descs, ids))
+        self.n_bodies += n
+        return list(ids)
+
+    def add_joint(self, a, b, r_a, r_b, stiffness_lin=float("inf"), stiffness_ang=0.0,
+                  fracture=float("inf")):
+        ra = (C.c_float * 3)(*r_a)
+        rb = (C.c_float * 3)(*r_b)
+        out = C.c_int()
+        self.api.check(self.api.world_add_joint(self.handle, int(a), int(b), ra, rb,
+                                                float(stiffness_lin), float(stiffness_ang),
+                                                float(fracture), C.byref(out)))
+        return out.value
+
+    def add_ignore_collision(self, a, b):
+        out = C.c_int()
+        self.api.check(self.api.world_add_ignore_collision(self.handle, int(a), int(b), C.byref(out)))
+        return out.value
+
+    def step(self, n=1):
+        if n == 1:
+            self.api.check(self.api.world_step(self.handle))
+        else:
+            self.api.check(self.api.world_step_n(self.handle, int(n)))
+
+    def step_interleaved(self, substeps, rounds):
+        self.api.check(self.api.world_step_interleaved(self.handle, int(substeps), int(rounds)))
+
+    def sync(self):
+        self.api.check(self.api.world_sync(self.handle))
+
+    def state(self):
+        """(position n x 3, orientation n x 4, velocity n x 3, angular velocity n x 3), creation order."""
+        n = self.n_bodies
+        p = np.zeros((n, 3), np.float32)
+        q = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        w = np.zeros((n, 3), np.float32)
+        self.api.check(self.api.world_get_body_state(self.handle, 0, n, _ptr(p, C.c_float), _ptr(q, C.c_float),
+                                                     _ptr(v, C.c_float), _ptr(w, C.c_float)))
+        return p, q, v, w
+
+    def set_state(self, position=None, orientation=None, velocity=None, angular_velocity=None):
+        n = self.n_bodies
+
+        def arr(a, k):
+            return None if a is None else np.ascontiguousarray(np.asarray(a, np.float32).reshape(n, k))
+
+        p, q, v, w = arr(position, 3), arr(orientation, 4), arr(velocity, 3), arr(angular_velocity, 3)
+        self.api.check(self.api.world_set_body_state(self.handle, 0, n, _ptr(p, C.c_float), _ptr(q, C.c_float),
+                                                     _ptr(v, C.c_float), _ptr(w, C.c_float)))
+
+    def stats(self):
+        s = Stats()
+        self.api.check(self.api.world_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def digest(self):
+        out = C.c_uint64()
+        self.api.check(self.api.world_digest(self.handle, C.byref(out)))
+        return out.value
+
+    def broadphase(self):
+        nb, np_ = C.c_int(), C.c_int()
+        self.api.check(self.api.world_dump_broadphase(self.handle, None, None, 0, None, 0, C.byref(nb),
+                                                      C.byref(np_)))
+        codes = np.zeros(nb.value, np.uint64)
+        order = np.zeros(nb.value, np.int32)
+        pairs = np.zeros(np_.value, np.uint64)
+        self.api.check(self.api.world_dump_broadphase(self.handle, _ptr(codes, C.c_uint64), _ptr(order, C.c_int32),
+                                                      nb.value, _ptr(pairs, C.c_uint64), np_.value,
+                                                      C.byref(nb), C.byref(np_)))
+        return codes, order, pairs
+
+    def manifolds(self):
+        cnt = C.c_int()
+        self.api.check(self.api.world_dump_manifolds(self.handle, 0, None, None, None, None, None, None, None,
+                                                     None, C.byref(cnt)))
+        m = cnt.value
+        out = {
+            "body_a": np.zeros(m, np.int32),
+            "body_b": np.zeros(m, np.int32),
+            "count": np.zeros(m, np.int32),
+            "features": np.zeros((m, 8), np.int32),
+            "basis": np.zeros((m, 3, 3), np.float32),
+            "c0": np.zeros((m, 8, 3), np.float32),
+            "penalty": np.zeros((m, 8, 3), np.float32),
+            "lambda": np.zeros((m, 8, 3), np.float32),
+        }
+        self.api.check(self.api.world_dump_manifolds(
+            self.handle, m, _ptr(out["body_a"], C.c_int32), _ptr(out["body_b"], C.c_int32),
+            _ptr(out["count"], C.c_int32), _ptr(out["features"], C.c_int32), _ptr(out["basis"], C.c_float),
+            _ptr(out["c0"], C.c_float), _ptr(out["penalty"], C.c_float), _ptr(out["lambda"], C.c_float),
+            C.byref(cnt)))
+        return out
+
+    def colours(self):
+        cnt = C.c_int()
+        self.api.check(self.api.world_dump_colours(self.handle, 0, None, None, C.byref(cnt)))
+        col = np.zeros(cnt.value, np.uint8)
+        ids = np.zeros(cnt.value, np.int32)
+        self.api.check(self.api.world_dump_colours(self.handle, cnt.value, _ptr(col, C.c_uint8),
+                                                   _ptr(ids, C.c_int32), C.byref(cnt)))
+        return col, ids

@@ -1,0 +1,329 @@
+"""Scene builders: the reference test suite's pinned scenes and the seeded synthetic workloads.
+
+A scene is a plain description (creation-ordered body arrays, joints, solver overrides) that any
+implementation of the world API can instantiate, so the GPU library and its checkers receive
+bit-identical float32 inputs. Body creation order matters: the solver walks bodies in reverse
+creation order, and that order reaches the arithmetic.
+
+Pinned scenes restate the reference's test fixtures:
+  stack        test/core_test.cpp:391-399   (10-box stack, defaults, digest stack_300)
+  interleaved  test/core_test.cpp:404-414   (same stack, dt 1/120, stepInterleaved(2, 3))
+  mixed        test/core_test.cpp:612-631   (30-link soft-jointed chain + 40 boxes, mixed_240)
+Synthetic workloads (seeded, numpy PCG64) follow the benchmark configurations:
+  pyramid420   two 20-row walls of unit cubes on a 100 x 1 x 100 ground
+  pile         log-uniform box sizes and densities + a 32-link ball-jointed chain
+  lattice      64 x 64 x 16 unit cubes with 5 cm gaps and 2 cm jitter on a 500 m ground
+  batch        many independent small worlds (pyramids or piles), log-uniform sizes
+"""
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+F32 = np.float32
+INF = float("inf")
+
+
+@dataclass
+class Scene:
+    name: str
+    size: np.ndarray          # n x 3 full extents
+    density: np.ndarray       # n
+    friction: np.ndarray      # n
+    position: np.ndarray      # n x 3
+    orientation: np.ndarray   # n x 4 {x, y, z, w}
+    velocity: np.ndarray      # n x 3
+    joints: list = field(default_factory=list)   # (a, b, rA, rB, kLin, kAng, fracture)
+    params: dict = field(default_factory=dict)   # solver field overrides
+    steps: int = 0
+    substeps: int = 0          # > 1: stepInterleaved(substeps, rounds)
+    rounds: int = 0
+
+    @property
+    def n(self):
+        return int(self.size.shape[0])
+
+    @property
+    def dynamic(self):
+        return int(np.count_nonzero(self.density > 0))
+
+
+class _Builder:
+    def __init__(self):
+        self.size, self.density, self.friction, self.position, self.orientation = [], [], [], [], []
+        self.velocity = []
+        self.joints = []
+
+    def box(self, size, density, friction, position, orientation=(0, 0, 0, 1), velocity=(0, 0, 0)):
+        self.size.append(np.asarray(size, F32))
+        self.density.append(F32(density))
+        self.friction.append(F32(friction))
+        self.position.append(np.asarray(position, F32))
+        self.orientation.append(np.asarray(orientation, F32))
+        self.velocity.append(np.asarray(velocity, F32))
+        return len(self.size) - 1
+
+    def joint(self, a, b, ra, rb, k_lin=INF, k_ang=0.0, fracture=INF):
+        self.joints.append((a, b, tuple(float(x) for x in ra), tuple(float(x) for x in rb),
+                            float(k_lin), float(k_ang), float(fracture)))
+
+    def scene(self, name, **kw):
+        n = len(self.size)
+        return Scene(
+            name=name,
+            size=np.array(self.size, F32).reshape(n, 3),
+            density=np.array(self.density, F32).reshape(n),
+            friction=np.array(self.friction, F32).reshape(n),
+            position=np.array(self.position, F32).reshape(n, 3),
+            orientation=np.array(self.orientation, F32).reshape(n, 4),
+            velocity=np.array(self.velocity, F32).reshape(n, 3),
+            joints=list(self.joints),
+            **kw,
+        )
+
+
+def _f(x):
+    return F32(x)
+
+
+# ----------------------------------------------------------------------------------------------
+# Pinned scenes of the reference test suite
+# ----------------------------------------------------------------------------------------------
+
+def stack(steps=300):
+    """test/core_test.cpp:391-399: ground + 10 unit boxes at z = i * 1.5 + 1 (defaults)."""
+    b = _Builder()
+    b.box((100, 100, 1), 0.0, 0.5, (0, 0, 0))
+    for i in range(10):
+        b.box((1, 1, 1), 1.0, 0.5, (0, 0, _f(i) * _f(1.5) + _f(1.0)))
+    return b.scene("stack", steps=steps)
+
+
+def interleaved(steps=300):
+    """test/core_test.cpp:404-414: the stack at dt = 1/120 with stepInterleaved(2, 3)."""
+    s = stack(steps)
+    s.name = "interleaved"
+    s.params = {"dt": float(_f(1.0) / _f(120.0))}
+    s.substeps, s.rounds = 2, 3
+    return s
+
+
+def mixed(steps=240):
+    """test/core_test.cpp:612-631: 30-link chain (Joint 1000 / 250) + 40 free boxes."""
+    b = _Builder()
+    b.box((100, 100, 1), 0.0, 0.5, (0, 0, 0))
+    prev = None
+    for i in range(30):
+        link = b.box((1, 1, 1), 1.0, 0.5, (0, 0, _f(20.0) - _f(i) * _f(1.5)))
+        if prev is not None:
+            b.joint(prev, link, (0, 0, -0.5), (0, 0, 0.5), 1000.0, 250.0)
+        prev = link
+    for i in range(40):
+        b.box((1, 1, 1), 1.0, 0.5, (_f(5.0) + _f(i) * _f(1.2), 0, _f(3.0) + _f(i % 5)))
+    return b.scene("mixed", steps=steps)
+
+
+# Digests the reference suite pins for these scenes (tools/baseline/digests.txt:1-3).
+PINNED_DIGESTS = {
+    "stack": 0xFBAC4F08CB1C977C,
+    "interleaved": 0xB03ADEB37742850A,
+    "mixed": 0xFB3CA7A3162035C2,
+}
+
+
+def hard_chain(links=4, steps=300):
+    """test/core_test.cpp:271-300: static anchor + hard ball-jointed chain."""
+    b = _Builder()
+    prev = b.box((1, 1, 1), 0.0, 0.5, (0, 0, 10))
+    for i in range(links):
+        link = b.box((1, 1, 1), 1.0, 0.5, (0, 0, _f(9.0) - _f(i)))
+        b.joint(prev, link, (0, 0, -0.5), (0, 0, 0.5), INF, 0.0)
+        prev = link
+    return b.scene("hard_chain", steps=steps)
+
+
+# ----------------------------------------------------------------------------------------------
+# Synthetic workloads
+# ----------------------------------------------------------------------------------------------
+
+BENCH_PARAMS = {"gravity": -9.81, "iterations": 10, "dt": float(_f(1.0) / _f(60.0))}
+
+
+def pyramid420(steps=300, rows=20, spacing=1.01):
+    """Two parallel walls (y = -1.5 and +1.5) of `rows` rows (rows, rows-1, ..., 1 unit cubes,
+    1 kg, friction 0.5) on a static 100 x 1 x 100 ground whose top face is z = 0."""
+    b = _Builder()
+    b.box((100, 100, 1), 0.0, 0.5, (0, 0, -0.5))
+    for y in (-1.5, 1.5):
+        for r in range(rows):
+            count = rows - r
+            for k in range(count):
+                x = (_f(k) - _f(count - 1) * _f(0.5)) * _f(spacing)
+                b.box((1, 1, 1), 1.0, 0.5, (x, y, _f(0.5) + _f(r)))
+    return b.scene("pyramid420", params=dict(BENCH_PARAMS), steps=steps)
+
+
+def _random_quats(rng, n):
+    """Uniform random unit quaternions (Shoemake's method)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, c = np.sqrt(1.0 - u1), np.sqrt(u1)
+    q = np.stack([a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2),
+                  c * np.sin(2 * np.pi * u3), c * np.cos(2 * np.pi * u3)], axis=1)
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q.astype(F32)
+
+
+def _place_pile(rng, b, count, lo, hi, edge_range=(0.25, 2.0), density_range=(100.0, 1e4), friction=0.5):
+    """Boxes with log-uniform edges and densities, random orientations, placed without overlap by
+    rejection against bounding spheres inside the box [lo, hi]."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    sizes = np.exp(rng.uniform(math.log(edge_range[0]), math.log(edge_range[1]), (count, 3)))
+    dens = np.exp(rng.uniform(math.log(density_range[0]), math.log(density_range[1]), count))
+    quats = _random_quats(rng, count)
+    radii = 0.5 * np.linalg.norm(sizes, axis=1)
+    # Uniform grid hash on the largest diameter for the overlap rejection.
+    cell = 2.0 * radii.max()
+    grid = {}
+    centres = np.zeros((count, 3))
+    for i in range(count):
+        r = radii[i]
+        for _ in range(10000):
+            c = rng.uniform(lo + r, hi - r)
+            key = tuple((c // cell).astype(int))
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        for j in grid.get((key[0] + dx, key[1] + dy, key[2] + dz), ()):
+                            if np.sum((centres[j] - c) ** 2) < (radii[j] + r) ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                break
+        else:
+            raise RuntimeError("pile placement failed: volume too small")
+        centres[i] = c
+        grid.setdefault(key, []).append(i)
+        b.box(sizes[i].astype(F32), dens[i], friction, centres[i].astype(F32), quats[i])
+
+
+def pile(steps=600, count=1653, chain_links=32, seed=1):
+    """Mass-ratio pile: `count` boxes (edges log-uniform 0.25-2 m per axis, densities log-uniform
+    100-10^4 kg/m^3, uniform random orientations) placed without overlap in a 40 x 40 x 60 m volume
+    above a static 200 x 1 x 200 ground (top face z = 0), plus a `chain_links`-link chain of
+    0.2 x 0.2 x 1 m boxes hung by hard ball joints from a static anchor."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    b.box((200, 200, 1), 0.0, 0.5, (0, 0, -0.5))
+    _place_pile(rng, b, count, (-20.0, -20.0, 1.0), (20.0, 20.0, 61.0))
+    if chain_links > 0:
+        prev = b.box((0.2, 0.2, 1.0), 0.0, 0.5, (26.0, 0.0, 45.0))
+        for i in range(chain_links):
+            link = b.box((0.2, 0.2, 1.0), 1000.0, 0.5, (26.0, 0.0, _f(44.0) - _f(i)))
+            b.joint(prev, link, (0, 0, -0.5), (0, 0, 0.5), INF, 0.0)
+            prev = link
+    return b.scene("pile", params=dict(BENCH_PARAMS), steps=steps)
+
+
+def lattice(steps=240, nx=64, ny=64, nz=16, pitch=1.05, jitter=0.02, seed=3):
+    """Unit cubes (1 kg, friction 0.6) on an nx x ny x nz lattice with `pitch` spacing and uniform
+    +/- `jitter` per coordinate, above a static 500 x 1 x 500 ground (top face z = 0)."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    b.box((500, 500, 1), 0.0, 0.6, (0, 0, -0.5))
+    n = nx * ny * nz
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    pos = np.stack([(ix.ravel() - (nx - 1) * 0.5) * pitch,
+                    (iy.ravel() - (ny - 1) * 0.5) * pitch,
+                    0.5 + (pitch - 1.0) + iz.ravel() * pitch], axis=1)
+    pos += rng.uniform(-jitter, jitter, pos.shape)
+    pos = pos.astype(F32)
+    for i in range(n):
+        b.box((1, 1, 1), 1.0, 0.6, pos[i])
+    return b.scene("lattice", params=dict(BENCH_PARAMS), steps=steps)
+
+
+def small_world(rng, n_target):
+    """One world of the batched workload: a pyramid wall (rows 3-20) or a small pile, each with its
+    own static ground, about `n_target` dynamic bodies."""
+    b = _Builder()
+    b.box((60, 60, 1), 0.0, 0.5, (0, 0, -0.5))
+    if rng.random() < 0.5:
+        remaining = n_target
+        wall = 0
+        while remaining > 0:
+            rows = int(min(20, max(3, math.ceil((math.sqrt(8 * remaining + 1) - 1) / 2))))
+            y = _f(wall * 1.5)
+            placed = 0
+            for r in range(rows):
+                cnt = rows - r
+                for k in range(cnt):
+                    if placed >= remaining:
+                        break
+                    x = (_f(k) - _f(cnt - 1) * _f(0.5)) * _f(1.01)
+                    b.box((1, 1, 1), 1.0, 0.5, (x, y, _f(0.5) + _f(r)))
+                    placed += 1
+            remaining -= placed
+            wall += 1
+    else:
+        side = max(4.0, (n_target * 8.0) ** (1.0 / 3.0) * 1.6)
+        _place_pile(rng, b, n_target, (-side / 2, -side / 2, 1.0), (side / 2, side / 2, 1.0 + side))
+    return b.scene("world")
+
+
+def batch(worlds=4096, n_min=8, n_max=512, seed=7, steps=120):
+    """Independent worlds whose dynamic body counts are log-uniform in [n_min, n_max]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(worlds):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        w = small_world(rng, n)
+        w.params = dict(BENCH_PARAMS)
+        w.steps = steps
+        out.append(w)
+    return out
+
+
+# ----------------------------------------------------------------------------------------------
+# Instantiation
+# ----------------------------------------------------------------------------------------------
+
+def apply_params(p, overrides):
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def instantiate(api, scene, world_cls=None, params=None):
+    """Create a world on `api` holding `scene` (solver overrides applied before any body, since
+    bodies copy the solver's gravity at construction)."""
+    from . import capi
+
+    world_cls = world_cls or capi.World
+    p = api.default_params() if params is None else params
+    apply_params(p, scene.params)
+    w = world_cls(api, p, max_bodies=scene.n, max_forces=len(scene.joints))
+    descs = capi.make_body_descs(scene.size, scene.density, scene.friction, scene.position,
+                                 scene.orientation, scene.velocity)
+    w.add_bodies(descs)
+    for (a, b, ra, rb, kl, ka, fr) in scene.joints:
+        w.add_joint(a, b, ra, rb, kl, ka, fr)
+    return w
+
+
+def advance(world, scene, steps=None):
+    """Advance `world` by `steps` ticks of the scene's stepping mode."""
+    steps = scene.steps if steps is None else steps
+    if scene.substeps > 1:
+        for _ in range(steps):
+            world.step_interleaved(scene.substeps, scene.rounds)
+    elif steps > 0:
+        world.step(steps)

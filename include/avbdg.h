@@ -1,0 +1,218 @@
+/*
+ * avbdg.h - C ABI of the GB300 AVBD rigid-body time-step.
+ *
+ * This is the drop-in boundary for the CPU solver's step entry point. Every call maps onto
+ * one piece of the reference solver's public surface (src/avbd/solver.h:50-374 of
+ * godot-avbd); the citation next to each declaration names the reference interface it
+ * replaces. Plain C: opaque handles, POD structs, plain pointers and sizes, no exceptions
+ * across the boundary. Every call returns an int status (AVBDG_OK = 0, negative = error).
+ *
+ * Conventions (same as the reference core): metres, kilograms, seconds, +Z up, gravity along
+ * -Z, boxes described by full widths, quaternions stored {x, y, z, w}.
+ *
+ * Body and force identity. A body id is its creation index within the world (0, 1, 2, ...).
+ * The solver iterates bodies in *list order*, which is reverse creation order (the reference
+ * prepends every new Rigid to an intrusive list, src/avbd/rigid.cpp:29-30); forces likewise
+ * (src/avbd/force.cpp:19-21). State accessors take and return arrays in creation order.
+ *
+ * Threading. Calls on one world must be serialised by the caller (the reference Solver is
+ * not thread-safe per instance either). Different worlds may be driven from different host
+ * threads; each world owns its own CUDA stream.
+ */
+#ifndef AVBDG_H
+#define AVBDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define AVBDG_OK 0
+#define AVBDG_ERR_INVALID (-1)     /* bad handle, argument or index */
+#define AVBDG_ERR_CAPACITY (-2)    /* a fixed-capacity device buffer would overflow */
+#define AVBDG_ERR_NONFINITE (-3)   /* non-finite input state */
+#define AVBDG_ERR_TIMEOUT (-4)     /* a bounded device wait gave up */
+#define AVBDG_ERR_CUDA (-5)        /* CUDA runtime error (message via avbdg_last_error) */
+#define AVBDG_ERR_UNSUPPORTED (-6) /* a reference feature this build does not implement */
+
+/* Shapes (src/avbd/types.hpp:49-54). Only boxes are on the accelerated path. */
+#define AVBDG_SHAPE_BOX 0
+#define AVBDG_SHAPE_SPHERE 1
+#define AVBDG_SHAPE_CYLINDER 2
+
+/*
+ * Solver parameters: the public fields of avbd::Solver (src/avbd/solver.h:54-144) that
+ * shape a step. avbdg_params_default fills the reference defaults.
+ */
+typedef struct avbdg_params {
+    float dt;                     /* time step (s) */
+    float gravity;                /* signed magnitude along -Z; copied into each body at creation */
+    int iterations;               /* solver rounds per step */
+    float alpha;                  /* stabilisation, (0, 1] */
+    float beta_lin;               /* penalty ramp, linear rows */
+    float beta_ang;               /* penalty ramp, angular rows */
+    float gamma;                  /* warm-start decay */
+    float newton_ratio;           /* share of rounds running the primal */
+    float stiffness_decay;        /* penalty decay of dual-only rounds */
+    int adaptive_beta;            /* bool */
+    float adaptive_beta_error_floor;
+    float convergence_threshold;  /* 0 disables the early exit */
+    float jacobi_relaxation;      /* overflow (block-Jacobi) combine factor */
+    int contact_only_overflow;    /* bool */
+    float stick_drift_heal;
+    float max_penetration;
+    float jacobian_rebuild_distance;
+    float speculative_margin;
+    int position_projection;      /* bool */
+    int projection_iterations;
+    float projection_beta;
+    float projection_slop;
+    float projection_max_correction;
+    int contact_grace_ticks;
+    float sleep_linear_threshold;
+    float sleep_angular_threshold;
+    int sleep_frames;
+    int threads;                  /* CPU worker count of the reference; ignored on the GPU */
+} avbdg_params;
+
+/* Creation record of one body: the arguments of Rigid::Rigid (src/avbd/types.hpp:114-117)
+ * plus the public fields a host sets right after construction. */
+typedef struct avbdg_body_desc {
+    float size[3];                /* box: full extents */
+    int shape;                    /* AVBDG_SHAPE_* */
+    float density;                /* 0 = static body */
+    float friction;
+    float position[3];
+    float orientation[4];         /* {x, y, z, w}; identity = {0, 0, 0, 1} */
+    float velocity[3];
+    float angular_velocity[3];
+    uint32_t collision_layer;     /* Godot semantics; defaults 1/1 */
+    uint32_t collision_mask;
+    uint32_t axis_lock_linear;    /* bits 0..2 = x/y/z */
+    uint32_t axis_lock_angular;
+} avbdg_body_desc;
+
+/* Per-step counters and phase timings (src/avbd/solver.h:160-275). */
+typedef struct avbdg_stats {
+    int bodies;
+    int dynamic_bodies;           /* mass > 0 */
+    int forces;                   /* non-manifold forces alive (joints, ignores) */
+    int broad_pairs;              /* sorted unique candidate pairs (broadPhasePairCount) */
+    int manifolds;                /* live manifolds (manifoldCount) */
+    int contacts;                 /* contact points over live manifolds */
+    int colour_groups;            /* colourGroups */
+    int overflow_bodies;          /* overflowBodies */
+    int update_bodies;            /* bodies in the update set */
+    int steps;                    /* steps taken since creation */
+    /* last step, milliseconds: broad, graph (warm start + colouring + brake), solve, finish */
+    double broad_ms, graph_ms, solve_ms, finish_ms, total_ms;
+} avbdg_stats;
+
+/* ------------------------------------------------------------------------------------ */
+/* Library                                                                              */
+/* ------------------------------------------------------------------------------------ */
+
+/* Reference defaults of every Solver field (src/avbd/solver.h:54-144). */
+int avbdg_params_default(avbdg_params *out);
+
+/* Message of the last error on the calling thread ("" if none). Never NULL. */
+const char *avbdg_last_error(void);
+
+/* ------------------------------------------------------------------------------------ */
+/* Worlds (one avbd::Solver each)                                                       */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct avbdg_world avbdg_world;
+
+/* Solver::Solver (src/avbd/solver.cpp:21-23) with its fields assigned from `params`.
+ * `max_bodies` / `max_forces` size the device store; 0 picks a default that grows on demand. */
+int avbdg_world_create(const avbdg_params *params, int max_bodies, int max_forces,
+                       avbdg_world **out);
+/* Solver::~Solver (src/avbd/solver.cpp:25-28). */
+int avbdg_world_destroy(avbdg_world *world);
+/* Solver::clear (src/avbd/solver_step.cpp:29-40): removes every body, force and manifold. */
+int avbdg_world_clear(avbdg_world *world);
+
+/* Field assignment on a Solver (src/avbd/solver.h:54-144). Takes effect at the next step. */
+int avbdg_world_set_params(avbdg_world *world, const avbdg_params *params);
+int avbdg_world_get_params(const avbdg_world *world, avbdg_params *out);
+
+/* `count` x new Rigid(...) (src/avbd/rigid.cpp:22-72) in array order; body gravity is the
+ * world's current gravity. Writes the new ids to `out_ids` (may be NULL). */
+int avbdg_world_add_bodies(avbdg_world *world, int count, const avbdg_body_desc *descs,
+                           int *out_ids);
+
+/* new Joint(solver, a, b, rA, rB, stiffnessLin, stiffnessAng, fracture)
+ * (src/avbd/forces.hpp:58-87, src/avbd/joint.cpp:28-40). body_a = -1 anchors body_b to the
+ * world point rA. */
+int avbdg_world_add_joint(avbdg_world *world, int body_a, int body_b, const float r_a[3],
+                          const float r_b[3], float stiffness_lin, float stiffness_ang,
+                          float fracture, int *out_id);
+
+/* new IgnoreCollision(solver, a, b) (src/avbd/forces.hpp:103-113). */
+int avbdg_world_add_ignore_collision(avbdg_world *world, int body_a, int body_b, int *out_id);
+
+/* Solver::step (src/avbd/solver_step.cpp:44-75). Enqueued on the world's stream; the state
+ * accessors below synchronise. */
+int avbdg_world_step(avbdg_world *world);
+
+/* Solver::stepInterleaved (src/avbd/solver_step.cpp:109-160); `dt` must already be the
+ * substep dt, as in the reference. */
+int avbdg_world_step_interleaved(avbdg_world *world, int substeps, int rounds_per_substep);
+
+/* Run `count` plain steps back to back (one call, no host round trip between steps). */
+int avbdg_world_step_n(avbdg_world *world, int count);
+
+/* Wait for every queued step of this world. */
+int avbdg_world_sync(avbdg_world *world);
+
+/* Read bodies [first, first+count) in creation order: the Rigid public fields
+ * positionLin (3 floats), positionAng (4), velocityLin (3), velocityAng (3)
+ * (src/avbd/types.hpp:79-88). Any pointer may be NULL. */
+int avbdg_world_get_body_state(avbdg_world *world, int first, int count, float *position,
+                               float *orientation, float *velocity, float *angular_velocity);
+
+/* Write the same fields (host edits between steps, e.g. integrated external forces,
+ * src/server/avbd_physics_server3d.cpp:1503-1528). Any pointer may be NULL. */
+int avbdg_world_set_body_state(avbdg_world *world, int first, int count, const float *position,
+                               const float *orientation, const float *velocity,
+                               const float *angular_velocity);
+
+/* Counters and phase times of the last step. */
+int avbdg_world_get_stats(avbdg_world *world, avbdg_stats *out);
+
+/* FNV-1a digest over positionLin, positionAng, velocityLin, velocityAng of every body in list
+ * order: the reference test suite's state_digest (test/core_test.cpp:133-149). */
+int avbdg_world_digest(avbdg_world *world, uint64_t *out);
+
+/* ------------------------------------------------------------------------------------ */
+/* Parity dumps (the integer stages, for bit-exact comparison with the reference)        */
+/* ------------------------------------------------------------------------------------ */
+
+/* Broad phase of the last step: Morton codes over swept-AABB centres per list index
+ * (src/avbd/bvh_broadphase.cpp:19-36,70-85), the (code, index) sorted order (:87-96), and the
+ * sorted, de-duplicated candidate pair keys (min << 32 | max over list indices,
+ * src/avbd/solver_broadphase.cpp:124-137). Arrays may be NULL; counts are always written. */
+int avbdg_world_dump_broadphase(avbdg_world *world, uint64_t *codes, int32_t *order, int cap_bodies,
+                                uint64_t *pairs, int cap_pairs, int *n_bodies, int *n_pairs);
+
+/* Live manifolds in live order (src/avbd/manifold.hpp:92): body ids of A and B, contact
+ * count, eight feature keys per manifold (unused = 0), the 3x3 basis (row-major, normal first),
+ * and per contact C0, penalty and lambda (8 x 3 floats each). Arrays may be NULL. */
+int avbdg_world_dump_manifolds(avbdg_world *world, int cap, int32_t *body_a, int32_t *body_b,
+                               int32_t *contact_count, int32_t *features, float *basis,
+                               float *c0, float *penalty, float *lambda, int *count);
+
+/* Colouring of the last step (src/avbd/solver_solve.cpp:365-424): per update-set index, the
+ * colour (0..7, 8 = overflow) and the body id it refers to. */
+int avbdg_world_dump_colours(avbdg_world *world, int cap, uint8_t *colour, int32_t *body_id,
+                             int *count);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* AVBDG_H */
