@@ -1,0 +1,224 @@
+// C ABI (include/avbdg.h) over the host engine. Every entry point catches everything, records a
+// message for avbdg_last_error and returns a status code; nothing throws across the boundary.
+
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+
+#include "avbdg.h"
+#include "engine_host.hpp"
+
+struct avbdg_world {
+    avbdg::Engine engine;
+    avbdg_world(const avbdg_params &p, int nb, int nf) : engine(p, nb, nf, 1) { engine.addWorld(); }
+};
+
+namespace {
+
+thread_local std::string g_lastError;
+
+int record(int rc, const avbdg::Engine *e) {
+    if (rc != AVBDG_OK && e)
+        g_lastError = e->error();
+    return rc;
+}
+
+int failWith(int rc, const char *msg) {
+    g_lastError = msg;
+    return rc;
+}
+
+template <typename F>
+int guarded(avbdg_world *w, F &&fn) {
+    if (!w)
+        return failWith(AVBDG_ERR_INVALID, "null world");
+    try {
+        return record(fn(w->engine), &w->engine);
+    } catch (const std::bad_alloc &) {
+        return failWith(AVBDG_ERR_CAPACITY, "host allocation failed");
+    } catch (const std::exception &ex) {
+        return failWith(AVBDG_ERR_INVALID, ex.what());
+    } catch (...) {
+        return failWith(AVBDG_ERR_INVALID, "unknown error");
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+const char *avbdg_last_error(void) { return g_lastError.c_str(); }
+
+int avbdg_params_default(avbdg_params *p) {
+    if (!p)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 1.0f / 60.0f;
+    p->gravity = -10.0f;
+    p->iterations = 8;
+    p->alpha = 0.99f;
+    p->beta_lin = 10000.0f;
+    p->beta_ang = 100.0f;
+    p->gamma = 0.999f;
+    p->newton_ratio = 1.0f;
+    p->stiffness_decay = 1.0f;
+    p->adaptive_beta = 0;
+    p->adaptive_beta_error_floor = 1e-3f;
+    p->convergence_threshold = 0.0f;
+    p->jacobi_relaxation = 0.7f;
+    p->contact_only_overflow = 1;
+    p->stick_drift_heal = 0.002f;
+    p->max_penetration = 0.02f;
+    p->jacobian_rebuild_distance = 0.0f;
+    p->speculative_margin = 0.01f;
+    p->position_projection = 1;
+    p->projection_iterations = 4;
+    p->projection_beta = 1.0f;
+    p->projection_slop = 0.008f;
+    p->projection_max_correction = 0.0f;
+    p->contact_grace_ticks = 0;
+    p->sleep_linear_threshold = 0.1f;
+    p->sleep_angular_threshold = 0.139626f;
+    p->sleep_frames = 0;
+    p->threads = 0;
+    return AVBDG_OK;
+}
+
+int avbdg_world_create(const avbdg_params *params, int max_bodies, int max_forces, avbdg_world **out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    *out = nullptr;
+    avbdg_params p;
+    if (params)
+        p = *params;
+    else
+        avbdg_params_default(&p);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        return failWith(AVBDG_ERR_CUDA, "no CUDA device: the GPU step has no CPU fallback");
+    try {
+        avbdg_world *w = new avbdg_world(p, max_bodies, max_forces);
+        const int rc = w->engine.setParams(p);
+        if (rc != AVBDG_OK) {
+            g_lastError = w->engine.error();
+            delete w;
+            return rc;
+        }
+        *out = w;
+        return AVBDG_OK;
+    } catch (const std::bad_alloc &) {
+        return failWith(AVBDG_ERR_CAPACITY, "host allocation failed");
+    }
+}
+
+int avbdg_world_destroy(avbdg_world *w) {
+    delete w;
+    return AVBDG_OK;
+}
+
+int avbdg_world_clear(avbdg_world *w) {
+    return guarded(w, [](avbdg::Engine &e) {
+        e.clear();
+        e.addWorld();
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_world_set_params(avbdg_world *w, const avbdg_params *p) {
+    if (!p)
+        return failWith(AVBDG_ERR_INVALID, "null params");
+    return guarded(w, [p](avbdg::Engine &e) { return e.setParams(*p); });
+}
+
+int avbdg_world_get_params(const avbdg_world *w, avbdg_params *out) {
+    if (!w || !out)
+        return failWith(AVBDG_ERR_INVALID, "null argument");
+    *out = w->engine.params();
+    return AVBDG_OK;
+}
+
+int avbdg_world_add_bodies(avbdg_world *w, int count, const avbdg_body_desc *descs, int *ids) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.addBodies(0, count, descs, ids); });
+}
+
+int avbdg_world_add_joint(avbdg_world *w, int a, int b, const float r_a[3], const float r_b[3], float kl, float ka,
+                          float fr, int *id) {
+    return guarded(w, [=](avbdg::Engine &e) {
+        const int rc = e.addJoint(0, a, b, r_a, r_b, kl, ka, fr);
+        if (rc == AVBDG_OK && id)
+            *id = 0;
+        return rc;
+    });
+}
+
+int avbdg_world_add_ignore_collision(avbdg_world *w, int a, int b, int *id) {
+    return guarded(w, [=](avbdg::Engine &e) {
+        const int rc = e.addIgnore(0, a, b);
+        if (rc == AVBDG_OK && id)
+            *id = 0;
+        return rc;
+    });
+}
+
+int avbdg_world_step(avbdg_world *w) {
+    return guarded(w, [](avbdg::Engine &e) { return e.step(); });
+}
+
+int avbdg_world_step_interleaved(avbdg_world *w, int substeps, int rounds) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.stepInterleaved(substeps, rounds); });
+}
+
+int avbdg_world_step_n(avbdg_world *w, int count) {
+    return guarded(w, [=](avbdg::Engine &e) {
+        for (int i = 0; i < count; i++) {
+            const int rc = e.step();
+            if (rc != AVBDG_OK)
+                return rc;
+        }
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_world_sync(avbdg_world *w) {
+    return guarded(w, [](avbdg::Engine &e) { return e.sync(); });
+}
+
+int avbdg_world_get_body_state(avbdg_world *w, int first, int count, float *p, float *q, float *v, float *av) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.getState(0, first, count, p, q, v, av); });
+}
+
+int avbdg_world_set_body_state(avbdg_world *w, int first, int count, const float *p, const float *q,
+                               const float *v, const float *av) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.setState(0, first, count, p, q, v, av); });
+}
+
+int avbdg_world_get_stats(avbdg_world *w, avbdg_stats *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return guarded(w, [out](avbdg::Engine &e) { return e.stats(*out); });
+}
+
+int avbdg_world_digest(avbdg_world *w, uint64_t *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return guarded(w, [out](avbdg::Engine &e) { return e.digest(0, *out); });
+}
+
+int avbdg_world_dump_broadphase(avbdg_world *w, uint64_t *codes, int32_t *order, int capN, uint64_t *pairs,
+                                int capP, int *nB, int *nP) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.dumpBroadphase(codes, order, capN, pairs, capP, nB, nP); });
+}
+
+int avbdg_world_dump_manifolds(avbdg_world *w, int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_t *features,
+                               float *basis, float *c0, float *penalty, float *lambda, int *count) {
+    return guarded(w, [=](avbdg::Engine &e) {
+        return e.dumpManifolds(cap, ba, bb, nc, features, basis, c0, penalty, lambda, count);
+    });
+}
+
+int avbdg_world_dump_colours(avbdg_world *w, int cap, uint8_t *colour, int32_t *ids, int *count) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.dumpColours(cap, colour, ids, count); });
+}
+
+} // extern "C"

@@ -1,0 +1,831 @@
+// Host orchestration of the GB300 AVBD step: device store, capacity management and the phase
+// sequence of avbd::Solver::step / stepInterleaved (godot-avbd src/avbd/solver_step.cpp:44-160).
+
+#include "engine_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "kernels.cuh"
+#include "prims.cuh"
+
+namespace avbdg {
+
+namespace {
+
+// Rigid::Rigid for boxes (src/avbd/rigid.cpp:22-72); host compiled with -ffp-contract=off.
+void boxMassProperties(const avbdg_body_desc &b, float &mass, float moment[3], float &radius) {
+    const float sx = b.size[0], sy = b.size[1], sz = b.size[2];
+    mass = sx * sy * sz * b.density;
+    moment[0] = (sy * sy + sz * sz) / 12.0f * mass;
+    moment[1] = (sx * sx + sz * sz) / 12.0f * mass;
+    moment[2] = (sx * sx + sy * sy) / 12.0f * mass;
+    const float hx = sx * 0.5f, hy = sy * 0.5f, hz = sz * 0.5f;
+    const float px = hx * hx, py = hy * hy, pz = hz * hz;
+    float s = 0.0f;
+    s = s + px;
+    s = s + py;
+    s = s + pz;
+    radius = std::sqrt(s);
+}
+
+bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+constexpr int kRefitBudget = 16; // src/avbd/bvh_broadphase.hpp:40
+
+} // namespace
+
+Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int maxWorlds) : P(params) {
+    cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    for (auto &e : ev)
+        cudaEventCreate(&e);
+    const int nb = std::max(maxBodies, 64);
+    allocate(nb, std::max(1024, 8 * nb), std::max(maxForces, 16), std::max(4096, 16 * nb), std::max(maxWorlds, 1));
+}
+
+Engine::~Engine() {
+    if (stream)
+        cudaStreamSynchronize(stream);
+    releaseAll();
+    for (auto &e : ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (stream)
+        cudaStreamDestroy(stream);
+}
+
+int Engine::fail(int code, const std::string &msg) {
+    err = msg;
+    return code;
+}
+
+int Engine::cudaCheck(const char *where) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return fail(AVBDG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    return AVBDG_OK;
+}
+
+template <typename T>
+T *Engine::dalloc(size_t n) {
+    void *p = nullptr;
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    if (cudaMalloc(&p, bytes) != cudaSuccess)
+        return nullptr;
+    cudaMemsetAsync(p, 0, bytes, stream);
+    allocs.push_back(p);
+    return static_cast<T *>(p);
+}
+
+void Engine::releaseAll() {
+    for (void *p : allocs)
+        cudaFree(p);
+    allocs.clear();
+}
+
+void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
+    const Dev old = d;
+    std::vector<void *> oldAllocs;
+    oldAllocs.swap(allocs);
+    Dev n{};
+    n.NB = nb;
+    n.MM = mm;
+    n.FF = ff;
+    n.PP = pp;
+    n.WW = ww;
+    n.wBase = dalloc<int>(ww);
+    n.wCount = dalloc<int>(ww);
+    n.wMaxDepth = dalloc<int>(ww);
+    n.wStop = dalloc<int>(ww);
+    n.wBounds = dalloc<int>(6 * static_cast<size_t>(ww));
+    n.wActive = dalloc<int>(ww);
+    n.x = dalloc<float4>(nb);
+    n.q = dalloc<float4>(nb);
+    n.x0 = dalloc<float4>(nb);
+    n.q0 = dalloc<float4>(nb);
+    n.xi = dalloc<float4>(nb);
+    n.qi = dalloc<float4>(nb);
+    n.v = dalloc<float4>(nb);
+    n.w = dalloc<float4>(nb);
+    n.vprev = dalloc<float4>(nb);
+    n.size = dalloc<float4>(nb);
+    n.moment = dalloc<float4>(nb);
+    n.meta = dalloc<int4>(nb);
+    n.lpToBody = dalloc<int>(nb);
+    n.contactOnly = dalloc<uint8_t>(nb);
+    n.colour = dalloc<uint8_t>(nb);
+    n.aabbC = dalloc<float4>(nb);
+    n.aabbH = dalloc<float4>(nb);
+    n.codes = dalloc<uint64_t>(nb);
+    n.sortK = dalloc<uint64_t>(nb);
+    n.sortKAlt = dalloc<uint64_t>(nb);
+    n.sortV = dalloc<uint32_t>(nb);
+    n.sortVAlt = dalloc<uint32_t>(nb);
+    n.leafBody = dalloc<int>(nb);
+    n.nodeL = dalloc<int>(nb);
+    n.nodeR = dalloc<int>(nb);
+    n.nodeParent = dalloc<int>(nb);
+    n.leafParent = dalloc<int>(nb);
+    n.nodeFlag = dalloc<int>(nb);
+    n.nodeMin = dalloc<float4>(nb);
+    n.nodeMax = dalloc<float4>(nb);
+    n.pairStart = dalloc<int>(static_cast<size_t>(nb) + 1);
+    n.pairs = dalloc<uint64_t>(pp);
+    n.pairsTmp = dalloc<uint64_t>(pp);
+    const int flagsCap = std::max(pp, mm);
+    n.pairValid = dalloc<int>(flagsCap);
+    n.mActive = dalloc<int>(flagsCap);
+    for (ManifoldBuf *b : {&n.live, &n.stage}) {
+        b->ab = dalloc<int2>(mm);
+        b->b0 = dalloc<float4>(mm);
+        b->b1 = dalloc<float4>(mm);
+        b->b2 = dalloc<float4>(mm);
+        b->count = dalloc<int>(mm);
+        const size_t mc = static_cast<size_t>(mm) * kMaxContacts;
+        b->key = dalloc<int>(mc);
+        b->rA = dalloc<float4>(mc);
+        b->rB = dalloc<float4>(mc);
+        b->C0 = dalloc<float4>(mc);
+        b->k = dalloc<float4>(mc);
+        b->lam = dalloc<float4>(mc);
+    }
+    n.stamps = dalloc<float4>(static_cast<size_t>(mm) * 2 * kStampF4);
+    n.mSpec = dalloc<uint8_t>(mm);
+    n.mDone = dalloc<uint8_t>(mm);
+    n.specList = dalloc<int>(mm);
+    n.projLin = dalloc<float4>(2 * static_cast<size_t>(mm));
+    n.projAng = dalloc<float4>(2 * static_cast<size_t>(mm));
+    n.dLin = dalloc<float4>(nb);
+    n.dAng = dalloc<float4>(nb);
+    n.fAB = dalloc<int2>(ff);
+    n.fRA = dalloc<float4>(ff);
+    n.fRB = dalloc<float4>(ff);
+    n.fC0L = dalloc<float4>(ff);
+    n.fC0A = dalloc<float4>(ff);
+    n.fKL = dalloc<float4>(ff);
+    n.fKA = dalloc<float4>(ff);
+    n.fLL = dalloc<float4>(ff);
+    n.fLA = dalloc<float4>(ff);
+    n.fPar = dalloc<float4>(ff);
+    n.fKind = dalloc<int>(ff);
+    n.fBroken = dalloc<int>(ff);
+    n.fKeep = dalloc<int>(ff);
+    n.adjStart = dalloc<int>(static_cast<size_t>(nb) + 1);
+    n.adjFill = dalloc<int>(nb);
+    const size_t adjCap = 2 * (static_cast<size_t>(ff) + mm);
+    n.adjSeq = dalloc<uint32_t>(adjCap);
+    n.adjTmp = dalloc<uint32_t>(adjCap);
+    n.colourList = dalloc<int>(static_cast<size_t>(nb) * (kMaxColours + 1));
+    n.colourCount = dalloc<int>(kMaxColours + 1);
+    n.ctr = dalloc<int>(C_COUNT);
+    n.longList = dalloc<int>(static_cast<size_t>(std::max(nb, 1)) + 1);
+    const int scanCap = std::max({pp, mm, nb + 1, 2 * (ff + mm)}) + 1;
+    n.scanScratch = dalloc<char>(scanScratchBytes(scanCap));
+    n.radixScratch = dalloc<char>(radixScratchBytes(nb + 1));
+    n.barrier = dalloc<unsigned>(2);
+
+    if (old.NB > 0) {
+        // Carry the persistent state into the new store.
+        const auto cp = [this](void *dst, const void *src, size_t bytes) {
+            if (dst && src && bytes)
+                cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, stream);
+        };
+        const size_t nbCopy = static_cast<size_t>(std::min(old.NB, nb));
+        for (auto pr : {std::make_pair(n.x, old.x), std::make_pair(n.q, old.q), std::make_pair(n.x0, old.x0),
+                        std::make_pair(n.q0, old.q0), std::make_pair(n.xi, old.xi), std::make_pair(n.qi, old.qi),
+                        std::make_pair(n.v, old.v), std::make_pair(n.w, old.w), std::make_pair(n.vprev, old.vprev),
+                        std::make_pair(n.size, old.size), std::make_pair(n.moment, old.moment)})
+            cp(pr.first, pr.second, nbCopy * sizeof(float4));
+        cp(n.meta, old.meta, nbCopy * sizeof(int4));
+        cp(n.lpToBody, old.lpToBody, nbCopy * sizeof(int));
+        cp(n.codes, old.codes, nbCopy * sizeof(uint64_t));
+        cp(n.ctr, old.ctr, C_COUNT * sizeof(int));
+        cudaStreamSynchronize(stream);
+        int liveCount = 0;
+        cudaMemcpy(&liveCount, old.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToHost);
+        const size_t mCopy = static_cast<size_t>(std::min({liveCount, old.MM, mm}));
+        const ManifoldBuf &s = old.live;
+        const ManifoldBuf &t = n.live;
+        cp(t.ab, s.ab, mCopy * sizeof(int2));
+        cp(t.b0, s.b0, mCopy * sizeof(float4));
+        cp(t.b1, s.b1, mCopy * sizeof(float4));
+        cp(t.b2, s.b2, mCopy * sizeof(float4));
+        cp(t.count, s.count, mCopy * sizeof(int));
+        const size_t cCopy = mCopy * kMaxContacts;
+        cp(t.key, s.key, cCopy * sizeof(int));
+        for (auto pr : {std::make_pair(t.rA, s.rA), std::make_pair(t.rB, s.rB), std::make_pair(t.C0, s.C0),
+                        std::make_pair(t.k, s.k), std::make_pair(t.lam, s.lam)})
+            cp(pr.first, pr.second, cCopy * sizeof(float4));
+        const size_t fCopy = static_cast<size_t>(std::min(old.FF, ff));
+        cp(n.fAB, old.fAB, fCopy * sizeof(int2));
+        for (auto pr : {std::make_pair(n.fRA, old.fRA), std::make_pair(n.fRB, old.fRB), std::make_pair(n.fC0L, old.fC0L),
+                        std::make_pair(n.fC0A, old.fC0A), std::make_pair(n.fKL, old.fKL), std::make_pair(n.fKA, old.fKA),
+                        std::make_pair(n.fLL, old.fLL), std::make_pair(n.fLA, old.fLA), std::make_pair(n.fPar, old.fPar)})
+            cp(pr.first, pr.second, fCopy * sizeof(float4));
+        cp(n.fKind, old.fKind, fCopy * sizeof(int));
+        cp(n.fBroken, old.fBroken, fCopy * sizeof(int));
+        cudaStreamSynchronize(stream);
+        for (void *p : oldAllocs)
+            cudaFree(p);
+        treeValid = false;
+        adjValid = false;
+    }
+    d = n;
+    if (!wBase.empty()) {
+        cudaMemcpyAsync(d.wBase, wBase.data(), wBase.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d.wCount, wCount.data(), wCount.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
+    }
+    cudaStreamSynchronize(stream);
+}
+
+int Engine::ensureCapacity(int nb, int ff, int ww) {
+    if (nb <= d.NB && ff <= d.FF && ww <= d.WW)
+        return AVBDG_OK;
+    const int nnb = nb <= d.NB ? d.NB : std::max(nb, 2 * d.NB);
+    const int nff = ff <= d.FF ? d.FF : std::max(ff, 2 * d.FF);
+    const int nww = ww <= d.WW ? d.WW : std::max(ww, 2 * d.WW);
+    allocate(nnb, std::max(d.MM, 8 * nnb), nff, std::max(d.PP, 16 * nnb), nww);
+    return cudaCheck("grow");
+}
+
+int Engine::addWorld() {
+    if (ensureCapacity(nBodies, nForces, worlds() + 1))
+        return -1;
+    wBase.push_back(nBodies);
+    wCount.push_back(0);
+    const int w = worlds() - 1;
+    cudaMemcpyAsync(d.wBase + w, &wBase[w], sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.wCount + w, &wCount[w], sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+    return w;
+}
+
+int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outIds) {
+    if (w < 0 || w >= worlds() || count < 0 || (count > 0 && !descs))
+        return fail(AVBDG_ERR_INVALID, "bad world or body array");
+    if (w != worlds() - 1)
+        return fail(AVBDG_ERR_INVALID, "only the most recently created world can receive bodies");
+    for (int i = 0; i < count; i++) {
+        const avbdg_body_desc &b = descs[i];
+        if (b.shape != AVBDG_SHAPE_BOX)
+            return fail(AVBDG_ERR_UNSUPPORTED, "only box bodies run on the GPU path");
+        if (!finite3(b.size) || !finite3(b.position) || !finite3(b.velocity) || !finite3(b.angular_velocity) ||
+            !std::isfinite(b.density) || !std::isfinite(b.friction) || !std::isfinite(b.orientation[0]) ||
+            !std::isfinite(b.orientation[1]) || !std::isfinite(b.orientation[2]) || !std::isfinite(b.orientation[3]))
+            return fail(AVBDG_ERR_NONFINITE, "non-finite body description");
+    }
+    if (count == 0)
+        return AVBDG_OK;
+    int rc = ensureCapacity(nBodies + count, nForces, worlds());
+    if (rc)
+        return rc;
+    const int first = nBodies;
+    std::vector<float4> x(count), q(count), v(count), wv(count), sz(count), mo(count), zero4(count);
+    std::vector<int4> meta(count);
+    for (int i = 0; i < count; i++) {
+        const avbdg_body_desc &b = descs[i];
+        float mass, moment[3], radius;
+        boxMassProperties(b, mass, moment, radius);
+        x[i] = make_float4(b.position[0], b.position[1], b.position[2], mass);
+        q[i] = make_float4(b.orientation[0], b.orientation[1], b.orientation[2], b.orientation[3]);
+        v[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], P.gravity);
+        wv[i] = make_float4(b.angular_velocity[0], b.angular_velocity[1], b.angular_velocity[2], 0.0f);
+        sz[i] = make_float4(b.size[0], b.size[1], b.size[2], radius);
+        mo[i] = make_float4(moment[0], moment[1], moment[2], b.friction);
+        meta[i] = make_int4(w, static_cast<int>(b.collision_layer), static_cast<int>(b.collision_mask),
+                            static_cast<int>((b.axis_lock_linear & 0xff) | ((b.axis_lock_angular & 0xff) << 8)));
+        zero4[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
+        if (outIds)
+            outIds[i] = first - wBase[w] + i;
+        if (mass > 0.0f)
+            nDynamic++;
+    }
+    const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
+    cudaMemcpyAsync(d.x + first, x.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.q + first, q.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.v + first, v.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.vprev + first, zero4.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.w + first, wv.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.size + first, sz.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.moment + first, mo.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.meta + first, meta.data(), sizeof(int4) * static_cast<size_t>(count), cudaMemcpyHostToDevice,
+                    stream);
+    nBodies += count;
+    wCount[w] += count;
+    // The world's list order changed: rebuild its list-position map.
+    std::vector<int> lp(wCount[w]);
+    for (int i = 0; i < wCount[w]; i++)
+        lp[i] = wBase[w] + wCount[w] - 1 - i; // list position wBase + i holds body (base + count - 1 - i)
+    cudaMemcpyAsync(d.lpToBody + wBase[w], lp.data(), sizeof(int) * lp.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.wCount + w, &wCount[w], sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+    treeValid = false;
+    adjValid = false;
+    return cudaCheck("addBodies");
+}
+
+int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], float kLin, float kAng,
+                     float fracture) {
+    if (w < 0 || w >= worlds() || b < 0 || b >= wCount[w] || a < -1 || a >= wCount[w] || !rA || !rB)
+        return fail(AVBDG_ERR_INVALID, "bad body index");
+    int rc = ensureCapacity(nBodies, nForces + 1, worlds());
+    if (rc)
+        return rc;
+    const int ga = a >= 0 ? wBase[w] + a : -1;
+    const int gb = wBase[w] + b;
+    // torqueArm = length2((A ? A.size : 0) + B.size) (joint.cpp:38-39), from host copies of sizes.
+    float sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
+    if (ga >= 0)
+        cudaMemcpy(sa, d.size + ga, sizeof(float4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(sb, d.size + gb, sizeof(float4), cudaMemcpyDeviceToHost);
+    const float tx = sa[0] + sb[0], ty = sa[1] + sb[1], tz = sa[2] + sb[2];
+    const float px = tx * tx, py = ty * ty, pz = tz * tz;
+    float arm = 0.0f;
+    arm = arm + px;
+    arm = arm + py;
+    arm = arm + pz;
+    const int f = nForces;
+    const int2 ab = make_int2(ga, gb);
+    const float4 ra = make_float4(rA[0], rA[1], rA[2], 0.0f), rb = make_float4(rB[0], rB[1], rB[2], 0.0f);
+    const float4 zero = make_float4(0, 0, 0, 0);
+    const float4 par = make_float4(kLin, kAng, fracture, arm);
+    const int kind = 0, broken = 0;
+    cudaMemcpyAsync(d.fAB + f, &ab, sizeof(int2), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fRA + f, &ra, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fRB + f, &rb, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    for (float4 *arr : {d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA})
+        cudaMemcpyAsync(arr + f, &zero, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fPar + f, &par, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fKind + f, &kind, sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fBroken + f, &broken, sizeof(int), cudaMemcpyHostToDevice, stream);
+    nForces++;
+    cudaMemcpyAsync(d.ctr + C_FORCES, &nForces, sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+    adjValid = false;
+    return cudaCheck("addJoint");
+}
+
+int Engine::addIgnore(int w, int a, int b) {
+    if (w < 0 || w >= worlds() || a < 0 || b < 0 || a >= wCount[w] || b >= wCount[w])
+        return fail(AVBDG_ERR_INVALID, "bad body index");
+    int rc = ensureCapacity(nBodies, nForces + 1, worlds());
+    if (rc)
+        return rc;
+    const int f = nForces;
+    const int2 ab = make_int2(wBase[w] + a, wBase[w] + b);
+    const int kind = 1, broken = 0;
+    const float4 zero = make_float4(0, 0, 0, 0);
+    cudaMemcpyAsync(d.fAB + f, &ab, sizeof(int2), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fKind + f, &kind, sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fBroken + f, &broken, sizeof(int), cudaMemcpyHostToDevice, stream);
+    for (float4 *arr : {d.fRA, d.fRB, d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA, d.fPar})
+        cudaMemcpyAsync(arr + f, &zero, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    nForces++;
+    cudaMemcpyAsync(d.ctr + C_FORCES, &nForces, sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+    adjValid = false;
+    return cudaCheck("addIgnore");
+}
+
+void Engine::clear() {
+    cudaStreamSynchronize(stream);
+    wBase.clear();
+    wCount.clear();
+    nBodies = nDynamic = nForces = 0;
+    cudaMemsetAsync(d.ctr, 0, sizeof(int) * C_COUNT, stream);
+    cudaStreamSynchronize(stream);
+    treeValid = adjValid = false;
+    treeAge = 0;
+    steps = 0;
+}
+
+int Engine::setParams(const avbdg_params &p) {
+    if (p.iterations < 1 || !(p.dt > 0.0f))
+        return fail(AVBDG_ERR_INVALID, "iterations must be >= 1 and dt > 0");
+    if (p.contact_grace_ticks != 0 || p.sleep_frames != 0 || p.jacobian_rebuild_distance != 0.0f ||
+        p.convergence_threshold != 0.0f)
+        return fail(AVBDG_ERR_UNSUPPORTED,
+                    "contact grace, sleeping, the arm cache and the convergence probe are not on the GPU path");
+    P = p;
+    return AVBDG_OK;
+}
+
+StepParams Engine::stepParams(float collisionDt) const {
+    StepParams s{};
+    s.dt = P.dt;
+    s.dtSq = P.dt * P.dt;
+    s.collisionDt = collisionDt;
+    s.alpha = P.alpha;
+    s.oneMinusAlpha = 1 - P.alpha;
+    s.betaLin = P.beta_lin;
+    s.betaAng = P.beta_ang;
+    s.gamma = P.gamma;
+    s.stiffnessDecay = P.stiffness_decay;
+    s.jacobiRelax = P.jacobi_relaxation;
+    s.stickDriftHeal = P.stick_drift_heal;
+    s.maxPen = P.max_penetration;
+    s.specMargin = P.speculative_margin;
+    s.projBeta = P.projection_beta;
+    s.projSlop = P.projection_slop;
+    s.projMaxCorr = P.projection_max_correction;
+    s.adaptiveFloor = P.adaptive_beta_error_floor;
+    s.adaptiveBeta = P.adaptive_beta;
+    s.contactOnlyOverflow = P.contact_only_overflow;
+    s.projIters = P.projection_iterations;
+    return s;
+}
+
+bool Engine::needGreedy() const { return nForces > 0 || !P.contact_only_overflow; }
+
+// Solver::broadPhase (solver_broadphase.cpp:85-186).
+int Engine::broadPhase(const StepParams &sp) {
+    if (!adjValid)
+        launchAdjacency(d, nBodies, stream);
+    launchAabb(d, nBodies, sp, stream);
+    bool anyWorldTree = false;
+    for (int c : wCount)
+        anyWorldTree = anyWorldTree || c >= 2;
+    if (!anyWorldTree) {
+        cudaMemsetAsync(d.ctr + C_PAIRS, 0, sizeof(int), stream);
+        cudaMemcpyAsync(d.ctr + C_CAND, d.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToDevice, stream);
+        return AVBDG_OK;
+    }
+    // Rebuild from fresh Morton codes when the body set changed or after kRefitBudget refits
+    // (bvh_broadphase.cpp:186-203), so the code/order dumps follow the reference's schedule.
+    if (!treeValid || treeAge >= kRefitBudget) {
+        launchRebuildTree(d, nBodies, worlds(), stream);
+        treeValid = true;
+        treeAge = 0;
+    } else {
+        treeAge++;
+    }
+    launchRefit(d, nBodies, stream);
+    launchPairs(d, nBodies, stream);
+    launchFilterAcquire(d, stream);
+    return AVBDG_OK;
+}
+
+// warmstartForces + selectUpdateBodies (solver_solve.cpp:31-105, 263-424).
+int Engine::warmstartAndSelect(const StepParams &sp) {
+    launchForceInit(d, sp, nForces, stream);
+    launchManifoldInit(d, sp, stream);
+    launchManifoldCompact(d, stream);
+    launchAdjacency(d, nBodies, stream);
+    adjValid = true;
+    launchContactOnly(d, nBodies, stream);
+    launchColour(d, nBodies, needGreedy(), stream);
+    launchColourLists(d, nBodies, P.contact_only_overflow, stream);
+    return AVBDG_OK;
+}
+
+// Solver::projectContacts (solver_projection.cpp:67-281).
+void Engine::projectContacts(const StepParams &sp, bool positions, float window) {
+    launchProjActive(d, worlds(), stream);
+    if (sp.specMargin > 0.0f)
+        launchBrake(d, worlds(), window > 0.0f ? window : sp.collisionDt, stream);
+    if (positions && sp.projIters > 0)
+        launchProjection(d, nBodies, worlds(), sp, stream);
+}
+
+// Solver::runSubstep + iterateBody (solver_step.cpp:79-105, 195-316).
+void Engine::runSubstep(const StepParams &sp, int rounds) {
+    launchWarmstartBodies(d, nBodies, sp, stream);
+    const int newtonRounds =
+            std::clamp(static_cast<int>(std::ceil(P.newton_ratio * static_cast<float>(rounds))), 1, rounds);
+    const bool colours = needGreedy();
+    const bool inPlace = nForces == 0;
+    const int bodyCap = std::max(nDynamic, 1);
+    launchStamps(d, sp, false, stream);
+    for (int it = 0; it < rounds; it++) {
+        const bool newton = it < newtonRounds;
+        if (newton) {
+            if (colours) {
+                for (int c = 0; c < kMaxColours; c++)
+                    launchColourPass(d, c, bodyCap, sp, stream);
+                launchStamps(d, sp, true, stream);
+            }
+            launchOverflowSolve(d, bodyCap, sp, inPlace, stream);
+            if (!inPlace)
+                launchOverflowApply(d, bodyCap, sp, stream);
+        }
+        const bool nextNewton = it + 1 < newtonRounds;
+        launchDual(d, sp, nextNewton, newton ? 1.0f : P.stiffness_decay, stream);
+        launchForceDual(d, sp, nForces, stream);
+    }
+    launchFinishBodies(d, nBodies, sp, stream);
+}
+
+int Engine::finishStep() {
+    cudaMemcpyAsync(hostCtr, d.ctr, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("step");
+    int rc = cudaCheck("step");
+    if (rc)
+        return rc;
+    steps++;
+    nForces = hostCtr[C_FORCES];
+    if (hostCtr[C_ERRORS]) {
+        const int e = hostCtr[C_ERRORS];
+        cudaMemsetAsync(d.ctr + C_ERRORS, 0, sizeof(int), stream);
+        if (e & kErrBrakeTimeout)
+            return fail(AVBDG_ERR_TIMEOUT, "brake sweep: a bounded grid barrier gave up");
+        return fail(AVBDG_ERR_CAPACITY, "a device buffer overflowed this step (state is not trustworthy)");
+    }
+    // Keep headroom for the next step's pairs and manifolds.
+    if (hostCtr[C_PAIRS] * 2 > d.PP || hostCtr[C_CAND] * 2 > d.MM || hostCtr[C_ADJ] * 2 > 2 * (d.FF + d.MM)) {
+        allocate(d.NB, std::max(d.MM, 4 * hostCtr[C_CAND]), d.FF, std::max(d.PP, 4 * hostCtr[C_PAIRS]), d.WW);
+        return cudaCheck("grow");
+    }
+    return AVBDG_OK;
+}
+
+int Engine::step() {
+    if (nBodies == 0)
+        return AVBDG_OK;
+    const StepParams sp = stepParams(P.dt);
+    cudaEventRecord(ev[0], stream);
+    broadPhase(sp);
+    cudaEventRecord(ev[1], stream);
+    warmstartAndSelect(sp);
+    projectContacts(sp, false, 0.0f);
+    cudaEventRecord(ev[2], stream);
+    runSubstep(sp, P.iterations);
+    cudaEventRecord(ev[3], stream);
+    projectContacts(sp, P.position_projection != 0, 0.0f);
+    launchRebase(d, sp, stream);
+    cudaEventRecord(ev[4], stream);
+    timed = true;
+    return finishStep();
+}
+
+int Engine::stepInterleaved(int substeps, int roundsPerSubstep) {
+    if (substeps <= 1)
+        return step();
+    if (nBodies == 0)
+        return AVBDG_OK;
+    const StepParams sp = stepParams(P.dt * static_cast<float>(substeps));
+    cudaEventRecord(ev[0], stream);
+    broadPhase(sp);
+    cudaEventRecord(ev[1], stream);
+    warmstartAndSelect(sp);
+    cudaEventRecord(ev[2], stream);
+    const int rounds = roundsPerSubstep > 0 ? std::max(1, roundsPerSubstep)
+                                            : std::max(2, (P.iterations + substeps - 1) / substeps);
+    for (int sub = 0; sub < substeps; ++sub) {
+        if (sub > 0)
+            launchRebase(d, sp, stream);
+        projectContacts(sp, false, P.dt * static_cast<float>(substeps - sub));
+        runSubstep(sp, rounds);
+    }
+    cudaEventRecord(ev[3], stream);
+    projectContacts(sp, P.position_projection != 0, sp.collisionDt);
+    launchRebase(d, sp, stream);
+    cudaEventRecord(ev[4], stream);
+    timed = true;
+    return finishStep();
+}
+
+int Engine::sync() {
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("sync");
+    return AVBDG_OK;
+}
+
+int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {
+    if (w < 0 || w >= worlds() || first < 0 || count < 0 || first + count > wCount[w])
+        return fail(AVBDG_ERR_INVALID, "bad range");
+    if (count == 0)
+        return AVBDG_OK;
+    const int g0 = wBase[w] + first;
+    std::vector<float4> buf(count);
+    const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
+    const auto fetch = [&](const float4 *src, float *dst, int k) {
+        if (!dst)
+            return;
+        cudaMemcpyAsync(buf.data(), src + g0, b4, cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+        for (int i = 0; i < count; i++) {
+            dst[k * i + 0] = buf[i].x;
+            dst[k * i + 1] = buf[i].y;
+            dst[k * i + 2] = buf[i].z;
+            if (k == 4)
+                dst[k * i + 3] = buf[i].w;
+        }
+    };
+    fetch(d.x, pos, 3);
+    fetch(d.q, quat, 4);
+    fetch(d.v, vel, 3);
+    fetch(d.w, angVel, 3);
+    return cudaCheck("getState");
+}
+
+int Engine::setState(int w, int first, int count, const float *pos, const float *quat, const float *vel,
+                     const float *angVel) {
+    if (w < 0 || w >= worlds() || first < 0 || count < 0 || first + count > wCount[w])
+        return fail(AVBDG_ERR_INVALID, "bad range");
+    if (count == 0)
+        return AVBDG_OK;
+    const int g0 = wBase[w] + first;
+    std::vector<float4> buf(count);
+    const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
+    // Each field keeps its packed companion (mass in x.w, gravity in v.w).
+    const auto put = [&](float4 *dst, const float *src, int k) {
+        if (!src)
+            return;
+        cudaMemcpyAsync(buf.data(), dst + g0, b4, cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+        for (int i = 0; i < count; i++) {
+            buf[i].x = src[k * i + 0];
+            buf[i].y = src[k * i + 1];
+            buf[i].z = src[k * i + 2];
+            if (k == 4)
+                buf[i].w = src[k * i + 3];
+        }
+        cudaMemcpyAsync(dst + g0, buf.data(), b4, cudaMemcpyHostToDevice, stream);
+        cudaStreamSynchronize(stream);
+    };
+    put(d.x, pos, 3);
+    put(d.q, quat, 4);
+    put(d.v, vel, 3);
+    put(d.w, angVel, 3);
+    return cudaCheck("setState");
+}
+
+int Engine::stats(avbdg_stats &out) {
+    std::memset(&out, 0, sizeof(out));
+    sync();
+    cudaMemcpy(hostCtr, d.ctr, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost);
+    out.bodies = nBodies;
+    out.dynamic_bodies = nDynamic;
+    out.forces = hostCtr[C_FORCES];
+    out.broad_pairs = hostCtr[C_PAIRS];
+    out.manifolds = hostCtr[C_LIVE];
+    std::vector<int> counts(static_cast<size_t>(std::max(hostCtr[C_LIVE], 0)));
+    if (!counts.empty())
+        cudaMemcpy(counts.data(), d.live.count, sizeof(int) * counts.size(), cudaMemcpyDeviceToHost);
+    for (int c : counts)
+        out.contacts += c;
+    int cc[kMaxColours + 1] = {};
+    cudaMemcpy(cc, d.colourCount, sizeof(cc), cudaMemcpyDeviceToHost);
+    for (int c = 0; c < kMaxColours; c++)
+        if (cc[c] > 0)
+            out.colour_groups = c + 1;
+    out.overflow_bodies = cc[kMaxColours];
+    out.update_bodies = nDynamic;
+    out.steps = steps;
+    if (timed) {
+        float t[4] = {};
+        for (int i = 0; i < 4; i++)
+            cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]);
+        out.broad_ms = t[0];
+        out.graph_ms = t[1];
+        out.solve_ms = t[2];
+        out.finish_ms = t[3];
+        out.total_ms = t[0] + t[1] + t[2] + t[3];
+    }
+    return cudaCheck("stats");
+}
+
+int Engine::digest(int w, uint64_t &out) {
+    if (w < 0 || w >= worlds())
+        return fail(AVBDG_ERR_INVALID, "bad world");
+    const int n = wCount[w];
+    std::vector<float> p(3 * n), q(4 * n), v(3 * n), av(3 * n);
+    int rc = getState(w, 0, n, p.data(), q.data(), v.data(), av.data());
+    if (rc)
+        return rc;
+    uint64_t h = 1469598103934665603ull;
+    const auto mix = [&h](const void *ptr, size_t bytes) {
+        const unsigned char *c = static_cast<const unsigned char *>(ptr);
+        for (size_t i = 0; i < bytes; i++) {
+            h ^= c[i];
+            h *= 1099511628211ull;
+        }
+    };
+    for (int i = n - 1; i >= 0; i--) {
+        mix(&p[3 * i], 12);
+        mix(&q[4 * i], 16);
+        mix(&v[3 * i], 12);
+        mix(&av[3 * i], 12);
+    }
+    out = h;
+    return AVBDG_OK;
+}
+
+int Engine::dumpBroadphase(uint64_t *codes, int32_t *order, int capN, uint64_t *pairs, int capP, int *nB, int *nP) {
+    sync();
+    cudaMemcpy(hostCtr, d.ctr, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost);
+    const int n = nBodies;
+    const int np = hostCtr[C_PAIRS];
+    if (nB)
+        *nB = n;
+    if (nP)
+        *nP = np;
+    if ((codes || order) && n > 0) {
+        std::vector<uint64_t> c(n);
+        std::vector<int> l2b(n);
+        std::vector<uint32_t> sv(n);
+        cudaMemcpy(c.data(), d.codes, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(l2b.data(), d.lpToBody, sizeof(int) * n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(sv.data(), d.sortV, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost);
+        for (int i = 0; i < n && i < capN; i++) {
+            if (codes)
+                codes[i] = c[l2b[i]];
+            if (order)
+                order[i] = static_cast<int32_t>(sv[i]);
+        }
+    }
+    if (pairs && np > 0)
+        cudaMemcpy(pairs, d.pairs, sizeof(uint64_t) * std::min(np, capP), cudaMemcpyDeviceToHost);
+    return cudaCheck("dumpBroadphase");
+}
+
+int Engine::dumpManifolds(int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_t *features, float *basis,
+                          float *c0, float *penalty, float *lambda, int *count) {
+    sync();
+    cudaMemcpy(hostCtr, d.ctr, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost);
+    const int m = hostCtr[C_LIVE];
+    if (count)
+        *count = m;
+    const int k = std::min(m, cap);
+    if (k <= 0)
+        return AVBDG_OK;
+    std::vector<int2> ab(k);
+    std::vector<int> cnt(k), keys(static_cast<size_t>(k) * kMaxContacts);
+    std::vector<float4> b0(k), b1(k), b2(k);
+    std::vector<float4> C(static_cast<size_t>(k) * kMaxContacts), K(C.size()), Lm(C.size());
+    cudaMemcpy(ab.data(), d.live.ab, sizeof(int2) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(cnt.data(), d.live.count, sizeof(int) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(keys.data(), d.live.key, sizeof(int) * keys.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(b0.data(), d.live.b0, sizeof(float4) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b1.data(), d.live.b1, sizeof(float4) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b2.data(), d.live.b2, sizeof(float4) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(C.data(), d.live.C0, sizeof(float4) * C.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(K.data(), d.live.k, sizeof(float4) * C.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(Lm.data(), d.live.lam, sizeof(float4) * C.size(), cudaMemcpyDeviceToHost);
+    const int base = wBase.empty() ? 0 : wBase[0];
+    for (int i = 0; i < k; i++) {
+        if (ba)
+            ba[i] = ab[i].x - base;
+        if (bb)
+            bb[i] = ab[i].y - base;
+        if (nc)
+            nc[i] = cnt[i];
+        const float4 rows[3] = {b0[i], b1[i], b2[i]};
+        for (int r = 0; r < 3; r++)
+            if (basis) {
+                basis[9 * i + 3 * r + 0] = rows[r].x;
+                basis[9 * i + 3 * r + 1] = rows[r].y;
+                basis[9 * i + 3 * r + 2] = rows[r].z;
+            }
+        for (int j = 0; j < 8; j++) {
+            const bool on = j < cnt[i];
+            const size_t ci = static_cast<size_t>(i) * kMaxContacts + j;
+            if (features)
+                features[8 * i + j] = on ? keys[ci] : 0;
+            const float *cv = &C[ci].x, *kv = &K[ci].x, *lv = &Lm[ci].x;
+            for (int e = 0; e < 3; e++) {
+                if (c0)
+                    c0[24 * i + 3 * j + e] = on ? cv[e] : 0.0f;
+                if (penalty)
+                    penalty[24 * i + 3 * j + e] = on ? kv[e] : 0.0f;
+                if (lambda)
+                    lambda[24 * i + 3 * j + e] = on ? lv[e] : 0.0f;
+            }
+        }
+    }
+    return cudaCheck("dumpManifolds");
+}
+
+int Engine::dumpColours(int cap, uint8_t *colour, int32_t *bodyId, int *count) {
+    sync();
+    const int w = 0;
+    if (worlds() == 0) {
+        if (count)
+            *count = 0;
+        return AVBDG_OK;
+    }
+    const int n = wCount[w];
+    std::vector<float4> x(n);
+    std::vector<uint8_t> col(n);
+    cudaMemcpy(x.data(), d.x + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(col.data(), d.colour + wBase[w], n, cudaMemcpyDeviceToHost);
+    int u = 0;
+    for (int id = n - 1; id >= 0; id--) { // list order
+        if (!(x[id].w > 0.0f))
+            continue;
+        if (u < cap) {
+            if (colour)
+                colour[u] = col[id];
+            if (bodyId)
+                bodyId[u] = id;
+        }
+        u++;
+    }
+    if (count)
+        *count = u;
+    return cudaCheck("dumpColours");
+}
+
+} // namespace avbdg

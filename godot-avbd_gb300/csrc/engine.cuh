@@ -1,0 +1,137 @@
+// Device data layout and kernel entry points of the GB300 AVBD step.
+//
+// One Engine holds a SET of independent worlds (one for the plain avbdg_world API, thousands for
+// the batched API). Each world owns a contiguous range of body slots; manifolds, forces, pairs
+// and adjacency of all worlds live in shared arrays and never reference two worlds at once, so
+// every kernel runs over the whole set in one launch.
+//
+// HBM layout (SoA, 16-byte records so each body or contact field is one 128-bit load):
+//   bodies    x, q, x0, q0, xi, qi, v, w, vprev : float4   (x.w = mass, v.w = gravity)
+//             size (xyz, w = bounding radius), moment (xyz, w = friction), meta (int4)
+//   manifolds live order, dense: ab (int2), basis rows b0 (xyz, w = mu), b1, b2, count
+//   contacts  stride 8 per manifold: key, rA (w = adaptive beta scale), rB, C0, k, lam (w = stick)
+//   stamps    per (manifold, side) 7 float4: the Jacobi block contribution of that side
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dmath.cuh"
+
+namespace avbdg {
+
+constexpr int kMaxContacts = 8;
+constexpr int kMaxColours = 8;
+constexpr uint8_t kOverflowColour = 8;
+constexpr uint8_t kUncoloured = 255;
+constexpr int kStampF4 = 7; // float4 per (manifold, side) stamp
+
+constexpr float PENALTY_MIN = 1.0f;
+constexpr float PENALTY_MAX = 10000000000.0f;
+constexpr float ADAPTIVE_BETA_MAX = 64.0f;
+constexpr float COLLISION_MARGIN = 0.001f;
+constexpr float STICK_THRESH = 0.00001f;
+constexpr float CONTACT_RELEASE_GAP = 2.0e-3f;
+constexpr float kReleaseAbove = COLLISION_MARGIN + CONTACT_RELEASE_GAP;
+
+// Device counters (indices into Dev::ctr).
+enum Counter {
+    C_PAIRS = 0,      // candidate pairs this step
+    C_LIVE,           // live manifolds
+    C_CAND,           // live + newly acquired, before compaction
+    C_FORCES,         // live forces
+    C_ADJ,            // adjacency entries
+    C_LONG,           // long segments (segmented sort scratch)
+    C_SPEC,           // speculative manifolds (brake)
+    C_ERRORS,         // capacity / timeout bits (kErr*)
+    C_UNCOLOURED,     // colouring rounds
+    C_ONE,            // constant 1 (scan length helper)
+    C_TMP,
+    C_COUNT
+};
+
+constexpr int kErrPairs = 1;
+constexpr int kErrManifolds = 2;
+constexpr int kErrAdjacency = 4;
+constexpr int kErrBrakeTimeout = 8;
+constexpr int kErrColourTimeout = 16;
+
+// Solver fields a kernel reads (src/avbd/solver.h:54-144), with derived terms.
+struct StepParams {
+    float dt, dtSq, collisionDt;
+    float alpha, oneMinusAlpha, betaLin, betaAng, gamma;
+    float stiffnessDecay, jacobiRelax, stickDriftHeal, maxPen, specMargin;
+    float projBeta, projSlop, projMaxCorr, adaptiveFloor;
+    int adaptiveBeta, contactOnlyOverflow, projIters;
+};
+
+struct ManifoldBuf {
+    int2 *ab;          // global body indices (a = smaller list index)
+    float4 *b0, *b1, *b2;
+    int *count;
+    int *key;          // contacts: [m * 8 + k]
+    float4 *rA, *rB, *C0, *k, *lam;
+};
+
+struct Dev {
+    int NB, MM, FF, PP, WW; // capacities
+    // worlds
+    int *wBase, *wCount;    // body range
+    int *wMaxDepth;         // projection: max depth bits per world (positive floats)
+    int *wStop;             // projection: early-exit flag per world
+    int *wBounds;           // Morton scene bounds per world: lo xyz, hi xyz (ordered ints)
+    int *wActive;           // projection: movable manifolds per world (0 = skip the world)
+    // bodies
+    float4 *x, *q, *x0, *q0, *xi, *qi, *v, *w, *vprev;
+    float4 *size, *moment;
+    int4 *meta;             // x = world, y = layer, z = mask, w = lockLin | lockAng << 8
+    int *lpToBody;          // list position -> body
+    uint8_t *contactOnly, *colour;
+    float4 *aabbC, *aabbH;
+    // LBVH
+    uint64_t *codes;        // per body: Morton code of the last rebuild
+    uint64_t *sortK, *sortKAlt;
+    uint32_t *sortV, *sortVAlt;
+    int *leafBody;          // sorted position -> body
+    int *nodeL, *nodeR, *nodeParent, *leafParent, *nodeFlag;
+    float4 *nodeMin, *nodeMax;
+    // pairs
+    int *pairStart;         // per list position (+1)
+    uint64_t *pairs, *pairsTmp;
+    int *pairValid;         // then exclusive rank
+    // manifolds
+    ManifoldBuf live, stage;
+    int *mActive;           // then exclusive rank
+    float4 *stamps;
+    uint8_t *mSpec, *mDone; // brake
+    int *specList;
+    float4 *projLin, *projAng; // projection contributions per (manifold, side)
+    float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)
+    // forces (creation order; list order is descending index)
+    int2 *fAB;
+    float4 *fRA, *fRB, *fC0L, *fC0A, *fKL, *fKA, *fLL, *fLA, *fPar; // fPar: stiffLin, stiffAng, fracture, torqueArm
+    int *fKind, *fBroken, *fKeep;
+    // adjacency (dynamic bodies only): sequence numbers, forces first (list order) then manifolds
+    int *adjStart, *adjFill;
+    uint32_t *adjSeq, *adjTmp;
+    // colouring
+    int *colourList, *colourCount; // per colour c: bodies with colour c (c = 0..8)
+    // scratch
+    int *ctr;
+    int *longList;
+    void *scanScratch, *radixScratch;
+    unsigned *barrier;      // grid barrier of the cooperative brake (2 words)
+};
+
+// ---- device helpers shared by the kernel files ----
+
+__device__ __forceinline__ int bodyWorld(const Dev &d, int g) { return d.meta[g].x; }
+// List position of body g: the world's bodies in list order (reverse creation) occupy
+// [wBase, wBase + wCount).
+__device__ __forceinline__ int listPos(const Dev &d, int g) {
+    const int w = d.meta[g].x;
+    return 2 * d.wBase[w] + d.wCount[w] - 1 - g;
+}
+__device__ __forceinline__ bool isDynamic(const Dev &d, int g) { return d.x[g].w > 0.0f; }
+
+} // namespace avbdg

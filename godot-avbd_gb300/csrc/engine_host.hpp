@@ -1,0 +1,103 @@
+// Host orchestration of the GB300 AVBD step (C++ runtime under the C ABI).
+//
+// An Engine owns one CUDA stream and the device store of a set of worlds. `step()` enqueues the
+// phases of avbd::Solver::step (src/avbd/solver_step.cpp:44-75) for every world at once; all
+// counts stay on the device, so a step needs no host round trip except the capacity check at its
+// end and, when joints exist, the colouring rounds.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "avbdg.h"
+#include "engine.cuh"
+
+namespace avbdg {
+
+struct HostForce {
+    int kind; // 0 joint, 1 ignore
+    int a, b; // global body indices (-1 = world)
+    float rA[3], rB[3];
+    float stiffLin, stiffAng, fracture;
+};
+
+class Engine {
+public:
+    Engine(const avbdg_params &params, int maxBodies, int maxForces, int maxWorlds);
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    // Worlds. A new world's bodies occupy the next free slots; only the last world can grow.
+    int addWorld();
+    int addBodies(int world, int count, const avbdg_body_desc *descs, int *outIds);
+    int addJoint(int world, int a, int b, const float rA[3], const float rB[3], float kLin, float kAng,
+                 float fracture);
+    int addIgnore(int world, int a, int b);
+    void clear();
+
+    int setParams(const avbdg_params &p);
+    const avbdg_params &params() const { return P; }
+
+    // Enqueue one step of every world (Solver::step / Solver::stepInterleaved).
+    int step();
+    int stepInterleaved(int substeps, int rounds);
+    int sync();
+
+    int getState(int world, int first, int count, float *pos, float *quat, float *vel, float *angVel);
+    int setState(int world, int first, int count, const float *pos, const float *quat, const float *vel,
+                 const float *angVel);
+    int stats(avbdg_stats &out);
+    int digest(int world, uint64_t &out);
+    int dumpBroadphase(uint64_t *codes, int32_t *order, int capN, uint64_t *pairs, int capP, int *nB, int *nP);
+    int dumpManifolds(int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_t *features, float *basis, float *c0,
+                      float *penalty, float *lambda, int *count);
+    int dumpColours(int cap, uint8_t *colour, int32_t *bodyId, int *count);
+
+    int worlds() const { return static_cast<int>(wBase.size()); }
+    int worldBodies(int w) const { return wCount[w]; }
+    int bodies() const { return nBodies; }
+    int dynamicBodies() const { return nDynamic; }
+    cudaStream_t streamHandle() const { return stream; }
+    // Kernel launches of the last step (this library's kernels only).
+    int lastLaunches() const { return launches; }
+    const std::string &error() const { return err; }
+
+private:
+    avbdg_params P;
+    Dev d{};
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocs;
+    std::vector<int> wBase, wCount;
+    std::vector<HostForce> pendingForces; // added since the last upload
+    int nBodies = 0, nDynamic = 0, nForces = 0;
+    int treeAge = 0;
+    bool treeValid = false, adjValid = false, uploaded = false;
+    int steps = 0;
+    int launches = 0;
+    int hostCtr[C_COUNT] = {};
+    cudaEvent_t ev[5] = {};
+    bool timed = false;
+    std::string err;
+
+    int fail(int code, const std::string &msg);
+    int cudaCheck(const char *where);
+    void allocate(int nb, int mm, int ff, int pp, int ww);
+    void releaseAll();
+    template <typename T>
+    T *dalloc(size_t n);
+    int ensureCapacity(int nb, int ff, int ww);
+    int flushPending();
+    StepParams stepParams(float collisionDt) const;
+    int broadPhase(const StepParams &sp);
+    int warmstartAndSelect(const StepParams &sp);
+    void projectContacts(const StepParams &sp, bool positions, float window);
+    void runSubstep(const StepParams &sp, int rounds);
+    int finishStep();
+    bool needGreedy() const;
+};
+
+} // namespace avbdg

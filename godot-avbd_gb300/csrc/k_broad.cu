@@ -1,0 +1,451 @@
+// Broad phase: swept AABBs, Morton codes, Karras LBVH per world, refit, candidate pairs, exact
+// filter and manifold acquisition (godot-avbd src/avbd/solver_broadphase.cpp:85-186,
+// src/avbd/bvh_broadphase.cpp:19-292, src/avbd/rigid.cpp:83-106).
+//
+// The reference builds its tree by pairwise merging of Morton-sorted leaves and walks it
+// serially; the candidate set it produces is "every leaf pair whose closed swept AABBs overlap",
+// which does not depend on the tree's shape. Here each world gets a Karras radix tree over the
+// same (code, list index) order, every body walks it in parallel and emits its partners with a
+// larger list index, and per-body segments are sorted, so the sorted key list equals the
+// reference's sorted, de-duplicated sweepPairs bit for bit.
+
+#include "kernels.cuh"
+#include "prims.cuh"
+
+namespace avbdg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kStack = 128;
+
+__device__ __forceinline__ int orderedInt(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float orderedFloat(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+// Swept AABB (solver_broadphase.cpp:103-122) over the tight box bound (rigid.cpp:83-106).
+__global__ void aabbKernel(Dev d, int n, StepParams p) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0)
+        return;
+    const float4 x4 = d.x[g];
+    const float4 v4 = d.v[g];
+    const float4 s4 = d.size[g];
+    const m3 rot = qmat(asq(d.q[g]));
+    const f3 h = scale(xyz(s4), 0.5f);
+    const f3 tight{(fabsf(rot.c0.x) * h.x + fabsf(rot.c1.x) * h.y) + fabsf(rot.c2.x) * h.z,
+                   (fabsf(rot.c0.y) * h.x + fabsf(rot.c1.y) * h.y) + fabsf(rot.c2.y) * h.z,
+                   (fabsf(rot.c0.z) * h.x + fabsf(rot.c1.z) * h.y) + fabsf(rot.c2.z) * h.z};
+    const float cdt = p.collisionDt;
+    f3 disp = scale(xyz(v4), cdt);
+    if (x4.w > 0)
+        disp = add(disp, f3{0, 0, v4.w * cdt * cdt});
+    const float rotSweep = s4.w * length(xyz(d.w[g])) * cdt;
+    const float grow = rotSweep + p.specMargin;
+    const f3 c = add(xyz(x4), scale(disp, 0.5f));
+    const f3 half = add(add(tight, scale(vabs(disp), 0.5f)), f3{grow, grow, grow});
+    d.aabbC[g] = f4(c, 0.0f);
+    d.aabbH[g] = f4(half, 0.0f);
+}
+
+// ---- Morton codes (bvh_broadphase.cpp:19-36, 70-85) ----
+
+__global__ void boundsResetKernel(int *wBounds, int nWorlds) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nWorlds)
+        return;
+    for (int k = 0; k < 3; k++) {
+        wBounds[6 * w + k] = 0x7fffffff;          // lo (ordered)
+        wBounds[6 * w + 3 + k] = (int)0x80000000; // hi (ordered)
+    }
+}
+
+__global__ void boundsKernel(Dev d, int n, int *wBounds) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n)
+        return;
+    const int w = d.meta[g].x;
+    if (w < 0)
+        return;
+    const float4 c = d.aabbC[g];
+    atomicMin(&wBounds[6 * w + 0], orderedInt(c.x));
+    atomicMin(&wBounds[6 * w + 1], orderedInt(c.y));
+    atomicMin(&wBounds[6 * w + 2], orderedInt(c.z));
+    atomicMax(&wBounds[6 * w + 3], orderedInt(c.x));
+    atomicMax(&wBounds[6 * w + 4], orderedInt(c.y));
+    atomicMax(&wBounds[6 * w + 5], orderedInt(c.z));
+}
+
+__device__ __forceinline__ uint64_t expandBits21(uint32_t v) {
+    uint64_t x = v & 0x1fffffu;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10cfcfcfcfcfcfcfull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t quantise(float v, float lo, float scaleF) {
+    return static_cast<uint32_t>(sclamp((v - lo) * scaleF, 0.0f, 2097151.0f));
+}
+
+// Code per body; keys/values laid out by list position for the stable (code, list index) sort.
+__global__ void mortonKernel(Dev d, int n, const int *wBounds) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0)
+        return;
+    const int w = d.meta[g].x;
+    const float lox = orderedFloat(wBounds[6 * w + 0]), loy = orderedFloat(wBounds[6 * w + 1]),
+                loz = orderedFloat(wBounds[6 * w + 2]);
+    const float hix = orderedFloat(wBounds[6 * w + 3]), hiy = orderedFloat(wBounds[6 * w + 4]),
+                hiz = orderedFloat(wBounds[6 * w + 5]);
+    const f3 ext{hix - lox, hiy - loy, hiz - loz};
+    float e = ext.x;
+    if (e < ext.y)
+        e = ext.y;
+    if (e < ext.z)
+        e = ext.z;
+    if (e < 1.0e-6f)
+        e = 1.0e-6f;
+    const float sc = 2097151.0f / e;
+    const float4 c = d.aabbC[g];
+    // The reference quantises all three axes against lo.x (bvh_broadphase.cpp:85); kept.
+    const uint64_t code = expandBits21(quantise(c.x, lox, sc)) | (expandBits21(quantise(c.y, lox, sc)) << 1) |
+                          (expandBits21(quantise(c.z, lox, sc)) << 2);
+    d.codes[g] = code;
+    const int lp = listPos(d, g);
+    d.sortK[lp] = code;
+    d.sortV[lp] = static_cast<uint32_t>(lp);
+}
+
+// Slots without a body keep key ~0 and map to themselves in list-position space.
+__global__ void mortonResetKernel(Dev d, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    d.sortK[i] = ~0ull;
+    d.sortV[i] = static_cast<uint32_t>(i);
+}
+
+// Second key: the world's first slot (a free slot keys on its own position), so after the stable
+// sort world w's leaves occupy sorted positions [wBase, wBase + wCount).
+__global__ void worldKeyKernel(Dev d, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const int lp = static_cast<int>(d.sortV[i]);
+    const int g = d.lpToBody[lp];
+    d.sortK[i] = static_cast<uint64_t>(g >= 0 ? d.wBase[d.meta[g].x] : lp);
+}
+
+__global__ void leafKernel(Dev d, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    d.leafBody[i] = d.lpToBody[d.sortV[i]];
+}
+
+// Longest common prefix of the augmented keys (code, list position) within one world segment.
+__device__ __forceinline__ int deltaKey(const Dev &d, int s, int n, int i, int j) {
+    if (j < 0 || j >= n)
+        return -1;
+    const uint64_t ci = d.codes[d.leafBody[s + i]];
+    const uint64_t cj = d.codes[d.leafBody[s + j]];
+    if (ci != cj)
+        return __clzll(static_cast<long long>(ci ^ cj));
+    return 64 + __clz(static_cast<int>(d.sortV[s + i] ^ d.sortV[s + j]));
+}
+
+constexpr int kLeafBit = 0x40000000;
+
+// Karras (2012) radix tree: internal node i of a world spans a key range and splits at the
+// highest differing bit.
+__global__ void karrasKernel(Dev d, int n) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n)
+        return;
+    const int g = d.leafBody[p];
+    if (g < 0)
+        return;
+    const int w = d.meta[g].x;
+    const int s = d.wBase[w];
+    const int cnt = d.wCount[w];
+    const int i = p - s;
+    if (i == 0)
+        d.nodeParent[s] = -1;
+    if (cnt < 2 || i >= cnt - 1)
+        return;
+    const int dir = (deltaKey(d, s, cnt, i, i + 1) - deltaKey(d, s, cnt, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = deltaKey(d, s, cnt, i, i - dir);
+    int lmax = 2;
+    while (deltaKey(d, s, cnt, i, i + lmax * dir) > dmin)
+        lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (deltaKey(d, s, cnt, i, i + (l + t) * dir) > dmin)
+            l += t;
+    const int j = i + l * dir;
+    const int dnode = deltaKey(d, s, cnt, i, j);
+    int sp = 0;
+    for (int div = 2;; div <<= 1) {
+        const int t = (l + div - 1) / div;
+        if (deltaKey(d, s, cnt, i, i + (sp + t) * dir) > dnode)
+            sp += t;
+        if (t <= 1)
+            break;
+    }
+    const int gamma = i + sp * dir + (dir < 0 ? -1 : 0);
+    const int lo = i < j ? i : j;
+    const int hi = i < j ? j : i;
+    int left, right;
+    if (lo == gamma) {
+        left = kLeafBit | (s + gamma);
+        d.leafParent[s + gamma] = s + i;
+    } else {
+        left = s + gamma;
+        d.nodeParent[s + gamma] = s + i;
+    }
+    if (hi == gamma + 1) {
+        right = kLeafBit | (s + gamma + 1);
+        d.leafParent[s + gamma + 1] = s + i;
+    } else {
+        right = s + gamma + 1;
+        d.nodeParent[s + gamma + 1] = s + i;
+    }
+    d.nodeL[s + i] = left;
+    d.nodeR[s + i] = right;
+}
+
+__device__ __forceinline__ void childBounds(const Dev &d, int c, float4 &mn, float4 &mx) {
+    if (c & kLeafBit) {
+        const int b = d.leafBody[c & ~kLeafBit];
+        const float4 cc = d.aabbC[b];
+        const float4 hh = d.aabbH[b];
+        mn = make_float4(cc.x - hh.x, cc.y - hh.y, cc.z - hh.z, 0.0f);
+        mx = make_float4(cc.x + hh.x, cc.y + hh.y, cc.z + hh.z, 0.0f);
+    } else {
+        mn = __ldcg(&d.nodeMin[c]);
+        mx = __ldcg(&d.nodeMax[c]);
+    }
+}
+
+// Bottom-up refit: the second child to arrive at a node computes its bounds.
+__global__ void refitKernel(Dev d, int n) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n)
+        return;
+    const int g = d.leafBody[p];
+    if (g < 0)
+        return;
+    const int w = d.meta[g].x;
+    if (d.wCount[w] < 2)
+        return;
+    int node = d.leafParent[p];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&d.nodeFlag[node], 1) == 0)
+            return;
+        __threadfence();
+        float4 a0, a1, b0, b1;
+        childBounds(d, d.nodeL[node], a0, a1);
+        childBounds(d, d.nodeR[node], b0, b1);
+        __stcg(&d.nodeMin[node], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f));
+        __stcg(&d.nodeMax[node], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f));
+        node = d.nodeParent[node];
+    }
+}
+
+__device__ __forceinline__ bool overlapClosed(f3 aMin, f3 aMax, f3 bMin, f3 bMax) {
+    return !(bMin.x > aMax.x || bMin.y > aMax.y || bMin.z > aMax.z || aMin.x > bMax.x || aMin.y > bMax.y ||
+             aMin.z > bMax.z);
+}
+
+// Walk the world's tree with body g's box; emit partners with a larger list position.
+template <bool EMIT>
+__global__ void traverseKernel(Dev d, int n) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n)
+        return;
+    const int w = d.meta[g].x;
+    if (w < 0)
+        return;
+    const int cnt = d.wCount[w];
+    const int lpA = listPos(d, g);
+    int out = EMIT ? d.pairStart[lpA] : 0;
+    int found = 0;
+    if (cnt >= 2) {
+        const float4 c4 = d.aabbC[g], h4 = d.aabbH[g];
+        const f3 aMin{c4.x - h4.x, c4.y - h4.y, c4.z - h4.z};
+        const f3 aMax{c4.x + h4.x, c4.y + h4.y, c4.z + h4.z};
+        int stack[kStack];
+        int sp = 0;
+        stack[sp++] = d.wBase[w];
+        while (sp > 0) {
+            const int node = stack[--sp];
+            const int kids[2] = {d.nodeL[node], d.nodeR[node]};
+            for (int k = 0; k < 2; k++) {
+                const int c = kids[k];
+                if (c & kLeafBit) {
+                    const int b = d.leafBody[c & ~kLeafBit];
+                    const int lpB = listPos(d, b);
+                    if (lpB <= lpA)
+                        continue;
+                    const float4 bc = d.aabbC[b], bh = d.aabbH[b];
+                    const f3 bMin{bc.x - bh.x, bc.y - bh.y, bc.z - bh.z};
+                    const f3 bMax{bc.x + bh.x, bc.y + bh.y, bc.z + bh.z};
+                    if (overlapClosed(aMin, aMax, bMin, bMax)) {
+                        if (EMIT) {
+                            if (out < d.PP)
+                                d.pairs[out] = (static_cast<uint64_t>(lpA) << 32) | static_cast<uint32_t>(lpB);
+                            out++;
+                        }
+                        found++;
+                    }
+                } else {
+                    const float4 mn = d.nodeMin[c], mx = d.nodeMax[c];
+                    if (overlapClosed(aMin, aMax, f3{mn.x, mn.y, mn.z}, f3{mx.x, mx.y, mx.z})) {
+                        if (sp < kStack)
+                            stack[sp++] = c;
+                        else
+                            atomicOr(&d.ctr[C_ERRORS], kErrPairs);
+                    }
+                }
+            }
+        }
+    }
+    if (!EMIT)
+        d.pairStart[lpA] = found;
+}
+
+__global__ void pairTotalKernel(Dev d) {
+    int t = d.ctr[C_TMP];
+    if (t > d.PP) {
+        atomicOr(&d.ctr[C_ERRORS], kErrPairs);
+        t = d.PP;
+    }
+    d.ctr[C_PAIRS] = t;
+}
+
+// The other body of adjacency entry `seq` of body x, or -1.
+__device__ __forceinline__ int adjOther(const Dev &d, uint32_t seq, int x, int nForces) {
+    int a, b;
+    if (static_cast<int>(seq) < nForces) {
+        const int2 ab = d.fAB[nForces - 1 - static_cast<int>(seq)];
+        a = ab.x;
+        b = ab.y;
+    } else {
+        const int2 ab = d.live.ab[static_cast<int>(seq) - nForces];
+        a = ab.x;
+        b = ab.y;
+    }
+    if (a == x)
+        return b;
+    if (b == x)
+        return a;
+    return -1;
+}
+
+// pairOverlaps (solver_broadphase.cpp:30-65): bounds, layer/mask, not constrained, not both static.
+__global__ void filterKernel(Dev d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = d.ctr[C_PAIRS];
+    if (k >= np)
+        return;
+    const uint64_t key = d.pairs[k];
+    const int a = d.lpToBody[static_cast<int>(key >> 32)];
+    const int b = d.lpToBody[static_cast<int>(key & 0xffffffffu)];
+    const float4 ac = d.aabbC[a], ah = d.aabbH[a], bc = d.aabbC[b], bh = d.aabbH[b];
+    const bool bounds = overlapClosed(f3{ac.x - ah.x, ac.y - ah.y, ac.z - ah.z}, f3{ac.x + ah.x, ac.y + ah.y, ac.z + ah.z},
+                                      f3{bc.x - bh.x, bc.y - bh.y, bc.z - bh.z}, f3{bc.x + bh.x, bc.y + bh.y, bc.z + bh.z});
+    const int4 ma = d.meta[a], mb = d.meta[b];
+    const bool layers = ((static_cast<uint32_t>(ma.y) & static_cast<uint32_t>(mb.z)) != 0) ||
+                        ((static_cast<uint32_t>(mb.y) & static_cast<uint32_t>(ma.z)) != 0);
+    const bool dynA = d.x[a].w > 0.0f, dynB = d.x[b].w > 0.0f;
+    const bool bothStatic = !dynA && !dynB;
+    bool constrained = false;
+    if (!bothStatic) {
+        // The relation is symmetric; only dynamic bodies carry adjacency lists.
+        const int xb = dynA ? a : b;
+        const int yb = dynA ? b : a;
+        const int nf = d.ctr[C_FORCES];
+        for (int e = d.adjStart[xb]; e < d.adjStart[xb + 1]; e++)
+            if (adjOther(d, d.adjSeq[e], xb, nf) == yb) {
+                constrained = true;
+                break;
+            }
+    }
+    d.pairValid[k] = (bounds && layers && !constrained && !bothStatic) ? 1 : 0;
+}
+
+__global__ void acquireKernel(Dev d, const int *flags, const int *rank) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = d.ctr[C_PAIRS];
+    if (k >= np || !flags[k])
+        return;
+    const int m = d.ctr[C_LIVE] + rank[k];
+    if (m >= d.MM)
+        return;
+    const uint64_t key = d.pairs[k];
+    d.live.ab[m] = make_int2(d.lpToBody[static_cast<int>(key >> 32)], d.lpToBody[static_cast<int>(key & 0xffffffffu)]);
+    d.live.count[m] = 0;
+}
+
+__global__ void candTotalKernel(Dev d) {
+    int c = d.ctr[C_LIVE] + d.ctr[C_TMP];
+    if (c > d.MM) {
+        atomicOr(&d.ctr[C_ERRORS], kErrManifolds);
+        c = d.MM;
+    }
+    d.ctr[C_CAND] = c;
+}
+
+} // namespace
+
+static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
+
+void launchAabb(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
+    aabbKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+}
+
+void launchRebuildTree(const Dev &d, int n, int nWorlds, cudaStream_t s) {
+    boundsResetKernel<<<grid(nWorlds), kThreads, 0, s>>>(d.wBounds, nWorlds);
+    boundsKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
+    mortonResetKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    mortonKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
+    radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, n, nullptr, 0, 63, d.radixScratch, s);
+    if (nWorlds > 1) {
+        int bits = 1;
+        while ((1 << bits) < n + 1)
+            bits++;
+        worldKeyKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+        radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, n, nullptr, 0, bits, d.radixScratch, s);
+    }
+    leafKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    karrasKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+}
+
+void launchRefit(const Dev &d, int n, cudaStream_t s) {
+    cudaMemsetAsync(d.nodeFlag, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
+    refitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+}
+
+void launchPairs(const Dev &d, int n, cudaStream_t s) {
+    cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
+    traverseKernel<false><<<grid(n), kThreads, 0, s>>>(d, n);
+    scanExclusive(d.pairStart, d.pairStart, d.NB + 1, nullptr, d.ctr + C_TMP, d.scanScratch, s);
+    pairTotalKernel<<<1, 1, 0, s>>>(d);
+    traverseKernel<true><<<grid(n), kThreads, 0, s>>>(d, n);
+    segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, n, nullptr, d.longList, d.ctr + C_LONG, s);
+}
+
+void launchFilterAcquire(const Dev &d, cudaStream_t s) {
+    filterKernel<<<grid(d.PP), kThreads, 0, s>>>(d);
+    scanExclusive(d.pairValid, d.mActive, d.PP, d.ctr + C_PAIRS, d.ctr + C_TMP, d.scanScratch, s);
+    acquireKernel<<<grid(d.PP), kThreads, 0, s>>>(d, d.pairValid, d.mActive);
+    candTotalKernel<<<1, 1, 0, s>>>(d);
+}
+
+} // namespace avbdg

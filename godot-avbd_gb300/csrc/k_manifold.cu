@@ -1,0 +1,383 @@
+// Manifold store maintenance and the constraint adjacency (godot-avbd src/avbd/manifold.cpp,
+// src/avbd/solver_solve.cpp:31-105, src/avbd/joint.cpp:62-78).
+//
+// Live manifolds are kept densely in live order; a step appends the newly acquired ones, runs the
+// narrow phase and warm start for every candidate into a staging buffer, and compacts the
+// survivors back in order (the reference's stable compaction of `live`). Slot recycling is an
+// allocation detail of the reference that never reaches its arithmetic, so it has no equivalent.
+
+#include "kernels.cuh"
+#include "narrow.cuh"
+#include "prims.cuh"
+
+namespace avbdg {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// ---- adjacency (ForceAdjacency::build, manifold.cpp:123-166) ----
+// Entry sequence numbers: forces in list order (0 .. F-1, newest first), then manifolds in live
+// order (F + m). Only dynamic bodies carry lists: static bodies are never solved or coloured, and
+// a pair query always has a dynamic side.
+
+__global__ void adjCountKernel(Dev d) {
+    const int nf = d.ctr[C_FORCES];
+    const int nm = d.ctr[C_LIVE];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int2 ab;
+    if (i < nf)
+        ab = d.fAB[i];
+    else if (i - nf < nm)
+        ab = d.live.ab[i - nf];
+    else
+        return;
+    if (ab.x >= 0 && d.x[ab.x].w > 0.0f)
+        atomicAdd(&d.adjStart[ab.x], 1);
+    if (ab.y >= 0 && d.x[ab.y].w > 0.0f)
+        atomicAdd(&d.adjStart[ab.y], 1);
+}
+
+__global__ void adjFillKernel(Dev d) {
+    const int nf = d.ctr[C_FORCES];
+    const int nm = d.ctr[C_LIVE];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int2 ab;
+    uint32_t seq;
+    if (i < nf) {
+        ab = d.fAB[i];
+        seq = static_cast<uint32_t>(nf - 1 - i);
+    } else if (i - nf < nm) {
+        ab = d.live.ab[i - nf];
+        seq = static_cast<uint32_t>(i);
+    } else {
+        return;
+    }
+    if (ab.x >= 0 && d.x[ab.x].w > 0.0f)
+        d.adjSeq[d.adjStart[ab.x] + atomicAdd(&d.adjFill[ab.x], 1)] = seq;
+    if (ab.y >= 0 && d.x[ab.y].w > 0.0f)
+        d.adjSeq[d.adjStart[ab.y] + atomicAdd(&d.adjFill[ab.y], 1)] = seq;
+}
+
+__global__ void adjTotalKernel(Dev d) {
+    if (d.ctr[C_ADJ] > 2 * (d.FF + d.MM))
+        atomicOr(&d.ctr[C_ERRORS], kErrAdjacency);
+}
+
+// ---- manifold initialize (ManifoldStore::initialize, manifold.cpp:237-435) ----
+
+__device__ __forceinline__ void basisHessian(f3 b0, f3 b1, f3 b2, f3 k, float S[6]) {
+    const float b0x2 = b0.x * b0.x, b0y2 = b0.y * b0.y, b0z2 = b0.z * b0.z;
+    const float b0xy = b0.x * b0.y, b0xz = b0.x * b0.z, b0yz = b0.y * b0.z;
+    const float b1x2 = b1.x * b1.x, b1y2 = b1.y * b1.y, b1z2 = b1.z * b1.z;
+    const float b1xy = b1.x * b1.y, b1xz = b1.x * b1.z, b1yz = b1.y * b1.z;
+    const float b2x2 = b2.x * b2.x, b2y2 = b2.y * b2.y, b2z2 = b2.z * b2.z;
+    const float b2xy = b2.x * b2.y, b2xz = b2.x * b2.z, b2yz = b2.y * b2.z;
+    S[0] = k.x * b0x2 + k.y * b1x2 + k.z * b2x2;
+    S[1] = k.x * b0xy + k.y * b1xy + k.z * b2xy;
+    S[2] = k.x * b0xz + k.y * b1xz + k.z * b2xz;
+    S[3] = k.x * b0y2 + k.y * b1y2 + k.z * b2y2;
+    S[4] = k.x * b0yz + k.y * b1yz + k.z * b2yz;
+    S[5] = k.x * b0z2 + k.y * b1z2 + k.z * b2z2;
+}
+
+// mul(basis, v) with the basis stored as rows.
+__device__ __forceinline__ f3 basisMul(f3 r0, f3 r1, f3 r2, f3 v) {
+    return f3{(r0.x * v.x + r0.y * v.y) + r0.z * v.z, (r1.x * v.x + r1.y * v.y) + r1.z * v.z,
+              (r2.x * v.x + r2.y * v.y) + r2.z * v.z};
+}
+
+__global__ void manifoldInitKernel(Dev d, StepParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ctr[C_CAND])
+        return;
+    const ManifoldBuf L = d.live;
+    const ManifoldBuf S = d.stage;
+    const int2 ab = L.ab[i];
+    const int a = ab.x, b = ab.y;
+    const float4 xa4 = d.x[a], xb4 = d.x[b];
+    const bool awakeA = xa4.w > 0.0f, awakeB = xb4.w > 0.0f;
+    const int oldN = L.count[i];
+    const int base = i * kMaxContacts;
+    S.ab[i] = ab;
+    if (!awakeA && !awakeB) {
+        // Frozen: every input is parked, the state is kept verbatim.
+        S.b0[i] = L.b0[i];
+        S.b1[i] = L.b1[i];
+        S.b2[i] = L.b2[i];
+        S.count[i] = oldN;
+        for (int k = 0; k < oldN; k++) {
+            S.key[base + k] = L.key[base + k];
+            S.rA[base + k] = L.rA[base + k];
+            S.rB[base + k] = L.rB[base + k];
+            S.C0[base + k] = L.C0[base + k];
+            S.k[base + k] = L.k[base + k];
+            S.lam[base + k] = L.lam[base + k];
+        }
+        d.mActive[i] = 1;
+        return;
+    }
+    const f3 xa = xyz(xa4), xb = xyz(xb4);
+    const q4 qa = asq(d.q[a]), qb = asq(d.q[b]);
+    const float4 ma4 = d.moment[a], mb4 = d.moment[b];
+    const float mu = sqrtf(ma4.w * mb4.w);
+
+    // Speculative margin (Manifold::collide, collide.cpp:1100-1120).
+    float margin = p.specMargin;
+    if (margin > 0.0f) {
+        const float horizon = p.collisionDt;
+        const float4 va4 = d.v[a], vb4 = d.v[b];
+        const float gA = awakeA ? va4.w : 0.0f;
+        const float gB = awakeB ? vb4.w : 0.0f;
+        const f3 disp = add(scale(sub(xyz(va4), xyz(vb4)), horizon), f3{0, 0, (gA - gB) * horizon * horizon});
+        const float ra = d.size[a].w, rb = d.size[b].w;
+        margin += length(disp) + (ra * length(xyz(d.w[a])) + rb * length(xyz(d.w[b]))) * horizon;
+    }
+    NContact nc[kMaxContacts];
+    m3 basis = mcols(xyz(L.b0[i]), xyz(L.b1[i]), xyz(L.b2[i])); // rows kept when the SAT fails early
+    basis = transpose(basis);
+    const int n = collideBoxes(xa, qa, scale(xyz(d.size[a]), 0.5f), xb, qb, scale(xyz(d.size[b]), 0.5f), margin,
+                               nc, basis);
+    const f3 r0 = mrow(basis, 0), r1 = mrow(basis, 1), r2 = mrow(basis, 2);
+
+    f3 newK[kMaxContacts], newLam[kMaxContacts];
+    float newBeta[kMaxContacts], prevErr[kMaxContacts];
+    int newStick[kMaxContacts];
+    for (int c = 0; c < kMaxContacts; c++) {
+        newK[c] = f3{0, 0, 0};
+        newLam[c] = f3{0, 0, 0};
+        newStick[c] = 0;
+        newBeta[c] = 1.0f;
+        prevErr[c] = -1.0f;
+    }
+    for (int c = 0; c < n; c++) {
+        for (int j = 0; j < oldN; j++) {
+            if (nc[c].key != L.key[base + j])
+                continue;
+            const f3 newRA = nc[c].rA, newRB = nc[c].rB;
+            const float4 oRA = L.rA[base + j], oRB = L.rB[base + j];
+            const float4 oLam = L.lam[base + j];
+            nc[c].rA = xyz(oRA);
+            nc[c].rB = xyz(oRB);
+            prevErr[c] = smax(0.0f, COLLISION_MARGIN - L.C0[base + j].x);
+            newK[c] = xyz(L.k[base + j]);
+            newLam[c] = xyz(oLam);
+            const int oldStick = oLam.w != 0.0f;
+            newStick[c] = oldStick;
+            newBeta[c] = oRA.w;
+            if (!oldStick) {
+                nc[c].rA = newRA;
+                nc[c].rB = newRB;
+            } else {
+                const f3 oldA = add(xa, qrot(qa, xyz(oRA)));
+                const f3 oldB = add(xb, qrot(qb, xyz(oRB)));
+                const f3 nA = add(xa, qrot(qa, newRA));
+                const f3 nB = add(xb, qrot(qb, newRB));
+                const float drift = smax(length(sub(oldA, nA)), length(sub(oldB, nB)));
+                if (drift > p.stickDriftHeal) {
+                    nc[c].rA = newRA;
+                    nc[c].rB = newRB;
+                    newStick[c] = 0;
+                    newLam[c] = f3{newLam[c].x, 0.0f, 0.0f};
+                }
+            }
+            break;
+        }
+    }
+    S.b0[i] = f4(r0, mu);
+    S.b1[i] = f4(r1, 0.0f);
+    S.b2[i] = f4(r2, 0.0f);
+    S.count[i] = n;
+    for (int c = 0; c < n; c++) {
+        const f3 rA = nc[c].rA, rB = nc[c].rB;
+        const f3 pA = add(xa, qrot(qa, rA));
+        const f3 pB = add(xb, qrot(qb, rB));
+        f3 C0 = add(basisMul(r0, r1, r2, sub(pA, pB)), f3{COLLISION_MARGIN, 0, 0});
+        if (C0.x < -p.maxPen)
+            C0.x = -p.maxPen;
+        float beta = 1.0f;
+        if (p.adaptiveBeta && prevErr[c] >= 0.0f) {
+            const float err = smax(0.0f, COLLISION_MARGIN - C0.x);
+            const float fl = p.adaptiveFloor;
+            float sc = newBeta[c];
+            if (err <= fl)
+                sc = smax(sc * 0.5f, 1.0f);
+            else if (prevErr[c] <= fl)
+                sc = smin(sc * 2.0f, ADAPTIVE_BETA_MAX);
+            else if (err > 0.5f * prevErr[c])
+                sc = smin(sc * 2.0f, ADAPTIVE_BETA_MAX);
+            else if (err < 0.1f * prevErr[c])
+                sc = smax(sc * 0.5f, 1.0f);
+            beta = sc;
+        }
+        f3 lam = newLam[c];
+        int stick = newStick[c];
+        if (C0.x > kReleaseAbove) {
+            lam = f3{0, 0, 0};
+            stick = 0;
+        }
+        lam = scale(scale(lam, p.alpha), p.gamma);
+        const f3 k = lclampv(scale(newK[c], p.gamma), PENALTY_MIN, PENALTY_MAX);
+        S.key[base + c] = nc[c].key;
+        S.rA[base + c] = f4(rA, beta);
+        S.rB[base + c] = f4(rB, 0.0f);
+        S.C0[base + c] = f4(C0, 0.0f);
+        S.k[base + c] = f4(k, 0.0f);
+        S.lam[base + c] = f4(lam, stick ? 1.0f : 0.0f);
+    }
+    d.mActive[i] = n > 0 ? 1 : 0;
+}
+
+__global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.ctr[C_CAND] || !flags[i])
+        return;
+    const ManifoldBuf L = d.live;
+    const ManifoldBuf S = d.stage;
+    const int r = rank[i];
+    L.ab[r] = S.ab[i];
+    L.b0[r] = S.b0[i];
+    L.b1[r] = S.b1[i];
+    L.b2[r] = S.b2[i];
+    const int n = S.count[i];
+    L.count[r] = n;
+    for (int c = 0; c < n; c++) {
+        const int si = i * kMaxContacts + c, di = r * kMaxContacts + c;
+        L.key[di] = S.key[si];
+        L.rA[di] = S.rA[si];
+        L.rB[di] = S.rB[si];
+        L.C0[di] = S.C0[si];
+        L.k[di] = S.k[si];
+        L.lam[di] = S.lam[si];
+    }
+}
+
+// ---- rebase (ManifoldStore::rebase, manifold.cpp:448-461) ----
+__global__ void rebaseKernel(Dev d, StepParams p) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= d.ctr[C_LIVE])
+        return;
+    const ManifoldBuf L = d.live;
+    const int2 ab = L.ab[m];
+    const f3 xa = xyz(d.x[ab.x]), xb = xyz(d.x[ab.y]);
+    const q4 qa = asq(d.q[ab.x]), qb = asq(d.q[ab.y]);
+    const f3 r0 = xyz(L.b0[m]), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+    const int n = L.count[m];
+    for (int c = 0; c < n; c++) {
+        const int ci = m * kMaxContacts + c;
+        const f3 pA = add(xa, qrot(qa, xyz(L.rA[ci])));
+        const f3 pB = add(xb, qrot(qb, xyz(L.rB[ci])));
+        f3 C0 = add(basisMul(r0, r1, r2, sub(pA, pB)), f3{COLLISION_MARGIN, 0, 0});
+        if (C0.x < -p.maxPen)
+            C0.x = -p.maxPen;
+        L.C0[ci] = f4(C0, 0.0f);
+    }
+}
+
+// ---- forces: Joint::initialize (joint.cpp:62-78) and reaping of broken joints ----
+
+__device__ __forceinline__ f3 jointLinError(const Dev &d, int f) {
+    const int2 ab = d.fAB[f];
+    const f3 rA = xyz(d.fRA[f]), rB = xyz(d.fRB[f]);
+    const f3 pa = ab.x >= 0 ? add(xyz(d.x[ab.x]), qrot(asq(d.q[ab.x]), rA)) : rA;
+    return sub(pa, add(xyz(d.x[ab.y]), qrot(asq(d.q[ab.y]), rB)));
+}
+
+__device__ __forceinline__ f3 jointAngError(const Dev &d, int f) {
+    const int2 ab = d.fAB[f];
+    const q4 qa = ab.x >= 0 ? asq(d.q[ab.x]) : q4{0.0f, 0.0f, 0.0f, 1.0f};
+    return scale(qdiff(qa, asq(d.q[ab.y])), d.fPar[f].w);
+}
+
+__device__ __forceinline__ f3 warmPenalty(f3 k, float gamma, float stiffness) {
+    return f3{smin(sclamp(k.x * gamma, PENALTY_MIN, PENALTY_MAX), stiffness),
+              smin(sclamp(k.y * gamma, PENALTY_MIN, PENALTY_MAX), stiffness),
+              smin(sclamp(k.z * gamma, PENALTY_MIN, PENALTY_MAX), stiffness)};
+}
+
+__global__ void forceInitKernel(Dev d, StepParams p) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nf = d.ctr[C_FORCES];
+    if (f >= nf)
+        return;
+    if (d.fKind[f] != 0) { // IgnoreCollision: always active, no state
+        d.fKeep[f] = 1;
+        return;
+    }
+    const float4 par = d.fPar[f];
+    d.fC0L[f] = f4(jointLinError(d, f), 0.0f);
+    d.fC0A[f] = f4(jointAngError(d, f), 0.0f);
+    d.fLL[f] = f4(scale(scale(xyz(d.fLL[f]), p.alpha), p.gamma), 0.0f);
+    d.fLA[f] = f4(scale(scale(xyz(d.fLA[f]), p.alpha), p.gamma), 0.0f);
+    d.fKL[f] = f4(warmPenalty(xyz(d.fKL[f]), p.gamma, par.x), 0.0f);
+    d.fKA[f] = f4(warmPenalty(xyz(d.fKA[f]), p.gamma, par.y), 0.0f);
+    const int keep = d.fBroken[f] ? 0 : 1;
+    d.fKeep[f] = keep;
+    if (!keep)
+        atomicOr(&d.ctr[C_TMP], 1);
+}
+
+// Stable in-place compaction of the force list (reaping is rare; one thread walks it in order).
+__global__ void forceCompactKernel(Dev d) {
+    if (!d.ctr[C_TMP])
+        return;
+    const int nf = d.ctr[C_FORCES];
+    int w = 0;
+    for (int f = 0; f < nf; f++) {
+        if (!d.fKeep[f])
+            continue;
+        if (w != f) {
+            d.fAB[w] = d.fAB[f];
+            d.fRA[w] = d.fRA[f];
+            d.fRB[w] = d.fRB[f];
+            d.fC0L[w] = d.fC0L[f];
+            d.fC0A[w] = d.fC0A[f];
+            d.fKL[w] = d.fKL[f];
+            d.fKA[w] = d.fKA[f];
+            d.fLL[w] = d.fLL[f];
+            d.fLA[w] = d.fLA[f];
+            d.fPar[w] = d.fPar[f];
+            d.fKind[w] = d.fKind[f];
+            d.fBroken[w] = d.fBroken[f];
+        }
+        w++;
+    }
+    d.ctr[C_FORCES] = w;
+}
+
+} // namespace
+
+static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
+
+void launchAdjacency(const Dev &d, int nBodies, cudaStream_t s) {
+    cudaMemsetAsync(d.adjStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
+    cudaMemsetAsync(d.adjFill, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
+    adjCountKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
+    scanExclusive(d.adjStart, d.adjStart, nBodies + 1, nullptr, d.ctr + C_ADJ, d.scanScratch, s);
+    adjTotalKernel<<<1, 1, 0, s>>>(d);
+    adjFillKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
+    segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, nBodies, nullptr, d.longList, d.ctr + C_LONG, s);
+}
+
+void launchManifoldInit(const Dev &d, const StepParams &p, cudaStream_t s) {
+    manifoldInitKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+}
+
+void launchManifoldCompact(const Dev &d, cudaStream_t s) {
+    scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_CAND, d.ctr + C_LIVE, d.scanScratch, s);
+    manifoldCompactKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
+}
+
+void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s) {
+    rebaseKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+}
+
+void launchForceInit(const Dev &d, const StepParams &p, int nForces, cudaStream_t s) {
+    if (nForces <= 0)
+        return;
+    cudaMemsetAsync(d.ctr + C_TMP, 0, sizeof(int), s);
+    forceInitKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
+    forceCompactKernel<<<1, 1, 0, s>>>(d);
+}
+
+} // namespace avbdg

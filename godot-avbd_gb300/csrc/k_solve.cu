@@ -1,0 +1,918 @@
+// Update set, colouring and the substep (godot-avbd src/avbd/solver_solve.cpp,
+// src/avbd/solver_step.cpp:79-105,195-316, src/avbd/manifold.cpp:465-671, src/avbd/joint.cpp,
+// src/avbd/types.hpp:147-201, src/avbd/maths.h:156-343).
+//
+// Primal, block-Jacobi ("overflow") bodies: the reference computes each round's per-contact force
+// cache once per manifold (preCompute), then every overflow body stamps its incident manifolds
+// from that cache in adjacency order and solves its 6x6 block against the round's pose snapshot.
+// Here one kernel per manifold computes the dual update AND, from the same poses, the next
+// round's per-side block contributions ("stamps"); one kernel per body then sums its stamps in
+// adjacency order, solves the LDL^T in registers and applies the relaxed delta. Both steps keep
+// the reference's operation order, so the result is bit-identical.
+//
+// Coloured (Gauss-Seidel) bodies recompute their manifold terms from the current poses at every
+// touch; the reference's "first touch uses the dual's cache" rule yields the same floats.
+
+#include "kernels.cuh"
+#include "prims.cuh"
+
+namespace avbdg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kSolveThreads = 128;
+
+struct Blk {
+    m3 lin, ang, crs;
+    f3 rl, ra;
+};
+
+// Block::Block (types.hpp:157-172).
+__device__ __forceinline__ Blk makeBlock(float mass, f3 moment, float dtSq, f3 x, f3 xi, q4 q, q4 qi) {
+    Blk b;
+    const f3 mo = divs(f3{mass, mass, mass}, dtSq);
+    b.lin = mdiag(mo.x, mo.y, mo.z);
+    b.crs = mzero();
+    b.rl = cmul(mo, sub(x, xi));
+    const m3 rot = qmat(q);
+    const m3 iw = mul(rot, mul(mdiag(moment.x, moment.y, moment.z), transpose(rot)));
+    b.ang = mdivs(iw, dtSq);
+    b.ra = mul(b.ang, qdiff(q, qi));
+    return b;
+}
+
+// ---- 6x6 solves (maths.h:156-343) ----
+
+__device__ bool ldlt6(const float a[6][6], const float b[6], float x[6]) {
+    float l[6][6];
+    float dd[6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        float dj = a[j][j];
+#pragma unroll
+        for (int s = 0; s < j; s++)
+            dj -= l[j][s] * l[j][s] * dd[s];
+        if (!(dj > 1.0e-12f))
+            return false;
+        dd[j] = dj;
+        l[j][j] = 1.0f;
+#pragma unroll
+        for (int i = j + 1; i < 6; i++) {
+            float lij = a[i][j];
+#pragma unroll
+            for (int s = 0; s < j; s++)
+                lij -= l[i][s] * l[j][s] * dd[s];
+            l[i][j] = lij / dd[j];
+        }
+    }
+    float z[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        float v = b[i];
+#pragma unroll
+        for (int s = 0; s < i; s++)
+            v -= l[i][s] * z[s];
+        z[i] = v;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+        x[i] = z[i] / dd[i];
+#pragma unroll
+    for (int i = 5; i >= 0; i--) {
+        float v = x[i];
+#pragma unroll
+        for (int s = i + 1; s < 6; s++)
+            v -= l[s][i] * x[s];
+        x[i] = v;
+    }
+    float worst = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 6; i++)
+        worst = smax(worst, fabsf(x[i]));
+    return isfinite(worst) && worst < 1.0e1f;
+}
+
+__device__ __noinline__ bool ldlt6Pivoted(const float aIn[6][6], const float b[6], float x[6]) {
+    float a[6][6];
+    for (int r = 0; r < 6; r++)
+        for (int c = 0; c < 6; c++)
+            a[r][c] = aIn[r][c];
+    float dd[6] = {0, 0, 0, 0, 0, 0};
+    int t[6] = {0, 1, 2, 3, 4, 5};
+    bool foundZero = false;
+    for (int k = 0; k < 6; k++) {
+        int j = k;
+        float best = fabsf(a[k][k]);
+        for (int i = k + 1; i < 6; i++) {
+            const float cand = fabsf(a[i][i]);
+            if (cand > best) {
+                best = cand;
+                j = i;
+            }
+        }
+        t[k] = j;
+        if (j != k) {
+            for (int c = 0; c < 6; c++) {
+                const float tmp = a[k][c];
+                a[k][c] = a[j][c];
+                a[j][c] = tmp;
+            }
+            for (int r = 0; r < 6; r++) {
+                const float tmp = a[r][k];
+                a[r][k] = a[r][j];
+                a[r][j] = tmp;
+            }
+        }
+        if (k > 0) {
+            float temp[6] = {0, 0, 0, 0, 0, 0};
+            for (int i = 0; i < k; i++)
+                temp[i] = dd[i] * a[k][i];
+            float prod[6] = {0, 0, 0, 0, 0, 0};
+            for (int i = 0; i < k; i++)
+                prod[i] = a[k][i] * temp[i];
+            float dotv;
+            switch (k) {
+            case 1: dotv = prod[0]; break;
+            case 2: dotv = prod[0] + prod[1]; break;
+            case 3: dotv = (prod[0] + prod[1]) + prod[2]; break;
+            case 4: dotv = (prod[0] + prod[2]) + (prod[1] + prod[3]); break;
+            default: dotv = ((prod[0] + prod[2]) + (prod[1] + prod[3])) + prod[4]; break;
+            }
+            a[k][k] -= dotv;
+            for (int i = 0; i < k; i++) {
+                const float ti = temp[i];
+                for (int r = k + 1; r < 6; r++)
+                    a[r][k] -= a[r][i] * ti;
+            }
+        }
+        const float pivot = a[k][k];
+        const bool valid = fabsf(pivot) > 0.0f;
+        if (!valid) {
+            for (int r = k + 1; r < 6; r++)
+                if (a[r][k] != 0.0f)
+                    return false;
+            foundZero = true;
+        } else if (foundZero) {
+            return false;
+        }
+        if (valid)
+            for (int r = k + 1; r < 6; r++)
+                a[r][k] /= pivot;
+        dd[k] = pivot;
+    }
+    for (int i = 0; i < 6; i++)
+        x[i] = b[i];
+    for (int k = 0; k < 6; k++) {
+        const float tmp = x[k];
+        x[k] = x[t[k]];
+        x[t[k]] = tmp;
+    }
+    for (int jj = 0; jj < 5; jj++) {
+        const float v = x[jj];
+        if (v != 0.0f)
+            for (int i = jj + 1; i < 6; i++)
+                x[i] -= a[i][jj] * v;
+    }
+    const float tolerance = 1.17549435e-38f; // FLT_MIN
+    for (int i = 0; i < 6; i++)
+        x[i] = fabsf(dd[i]) > tolerance ? x[i] / dd[i] : 0.0f;
+    for (int jj = 5; jj >= 1; jj--) {
+        const float v = x[jj];
+        if (v != 0.0f)
+            for (int i = jj - 1; i >= 0; i--)
+                x[i] -= a[jj][i] * v;
+    }
+    for (int k = 5; k >= 0; k--) {
+        const float tmp = x[k];
+        x[k] = x[t[k]];
+        x[t[k]] = tmp;
+    }
+    float worst = 0.0f;
+    for (int i = 0; i < 6; i++)
+        worst = smax(worst, fabsf(x[i]));
+    return isfinite(worst) && worst < 1.0e1f;
+}
+
+// Block::solveDelta (types.hpp:176-197) with solve()'s fallback chain.
+__device__ __forceinline__ void solveBlock(const Blk &k, f3 &dl, f3 &da) {
+    float a[6][6];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            a[r][c] = mat(k.lin, c, r);
+            a[r + 3][c + 3] = mat(k.ang, c, r);
+            a[r + 3][c] = mat(k.crs, c, r);
+            a[r][c + 3] = mat(k.crs, r, c);
+        }
+    const float b[6] = {-k.rl.x, -k.rl.y, -k.rl.z, -k.ra.x, -k.ra.y, -k.ra.z};
+    float x[6];
+    if (ldlt6(a, b, x)) {
+        dl = f3{x[0], x[1], x[2]};
+        da = f3{x[3], x[4], x[5]};
+        return;
+    }
+    if (ldlt6Pivoted(a, b, x)) {
+        dl = f3{x[0], x[1], x[2]};
+        da = f3{x[3], x[4], x[5]};
+        return;
+    }
+    dl = f3{0, 0, 0};
+    da = f3{0, 0, 0};
+}
+
+// ---- contact terms (manifold.cpp:196-234, 465-570, 583-671) ----
+
+__device__ __forceinline__ void basisHessianD(f3 b0, f3 b1, f3 b2, f3 k, float S[6]) {
+    const float b0x2 = b0.x * b0.x, b0y2 = b0.y * b0.y, b0z2 = b0.z * b0.z;
+    const float b0xy = b0.x * b0.y, b0xz = b0.x * b0.z, b0yz = b0.y * b0.z;
+    const float b1x2 = b1.x * b1.x, b1y2 = b1.y * b1.y, b1z2 = b1.z * b1.z;
+    const float b1xy = b1.x * b1.y, b1xz = b1.x * b1.z, b1yz = b1.y * b1.z;
+    const float b2x2 = b2.x * b2.x, b2y2 = b2.y * b2.y, b2z2 = b2.z * b2.z;
+    const float b2xy = b2.x * b2.y, b2xz = b2.x * b2.z, b2yz = b2.y * b2.z;
+    S[0] = k.x * b0x2 + k.y * b1x2 + k.z * b2x2;
+    S[1] = k.x * b0xy + k.y * b1xy + k.z * b2xy;
+    S[2] = k.x * b0xz + k.y * b1xz + k.z * b2xz;
+    S[3] = k.x * b0y2 + k.y * b1y2 + k.z * b2y2;
+    S[4] = k.x * b0yz + k.y * b1yz + k.z * b2yz;
+    S[5] = k.x * b0z2 + k.y * b1z2 + k.z * b2z2;
+}
+
+__device__ __forceinline__ f3 basisMulD(f3 r0, f3 r1, f3 r2, f3 v) {
+    return f3{(r0.x * v.x + r0.y * v.y) + r0.z * v.z, (r1.x * v.x + r1.y * v.y) + r1.z * v.z,
+              (r2.x * v.x + r2.y * v.y) + r2.z * v.z};
+}
+
+struct Cone {
+    float bounds, scale;
+};
+
+__device__ __forceinline__ Cone clampForce(f3 &F, float mu) {
+    F.x = smin(F.x, 0.0f);
+    const float bounds = fabsf(F.x) * mu;
+    const float fs = length2d(F.y, F.z);
+    if (fs > bounds && fs > 0) {
+        F.y = F.y * (bounds / fs);
+        F.z = F.z * (bounds / fs);
+    }
+    return Cone{bounds, fs};
+}
+
+// Per-side accumulators of stampCached.
+struct SideAcc {
+    m3 ang, crs;
+    f3 rhsAng;
+};
+struct SharedAcc {
+    m3 lin;
+    f3 rhsLin;
+};
+
+__device__ __forceinline__ void stampContact(const float S[6], f3 r, f3 fw, SideAcc &acc) {
+    const float s00 = S[0], s01 = S[1], s02 = S[2], s11 = S[3], s12 = S[4], s22 = S[5];
+    const m3 Sm = mcols(f3{s00, s01, s02}, f3{s01, s11, s12}, f3{s02, s12, s22});
+    const m3 RS = mcols(cross(r, Sm.c0), cross(r, Sm.c1), cross(r, Sm.c2));
+    const float rx2 = r.x * r.x, ry2 = r.y * r.y, rz2 = r.z * r.z;
+    const float rxy = r.x * r.y, rxz = r.x * r.z, ryz = r.y * r.z;
+    const float h00 = s11 * rz2 - 2.0f * s12 * ryz + s22 * ry2;
+    const float h11 = s22 * rx2 - 2.0f * s02 * rxz + s00 * rz2;
+    const float h22 = s00 * ry2 - 2.0f * s01 * rxy + s11 * rx2;
+    const float h01 = s12 * rxz + s02 * ryz - s22 * rxy - s01 * rz2;
+    const float h02 = s12 * rxy + s01 * ryz - s11 * rxz - s02 * ry2;
+    const float h12 = s02 * rxy + s01 * rxz - s00 * ryz - s12 * rx2;
+    acc.ang = madd(acc.ang, mcols(f3{h00, h01, h02}, f3{h01, h11, h12}, f3{h02, h12, h22}));
+    acc.crs = madd(acc.crs, RS);
+    acc.rhsAng = add(acc.rhsAng, cross(r, fw));
+}
+
+__device__ __forceinline__ void stampShared(const float S[6], f3 fw, SharedAcc &acc) {
+    acc.lin = madd(acc.lin, mcols(f3{S[0], S[1], S[2]}, f3{S[1], S[3], S[4]}, f3{S[2], S[4], S[5]}));
+    acc.rhsLin = add(acc.rhsLin, fw);
+}
+
+__device__ __forceinline__ void zeroAcc(SideAcc &a) {
+    a.ang = mzero();
+    a.crs = mzero();
+    a.rhsAng = f3{0, 0, 0};
+}
+
+// Stamp record: lin (6 unique), rhsLin (signed), ang (6 unique), rhsAng (signed), cross (9).
+__device__ __forceinline__ void storeStamp(float4 *dst, const SharedAcc &sh, const SideAcc &sd, float side) {
+    const f3 rl = scale(sh.rhsLin, side);
+    const f3 ra = scale(sd.rhsAng, side);
+    dst[0] = make_float4(sh.lin.c0.x, sh.lin.c0.y, sh.lin.c0.z, sh.lin.c1.y);
+    dst[1] = make_float4(sh.lin.c1.z, sh.lin.c2.z, rl.x, rl.y);
+    dst[2] = make_float4(rl.z, sd.ang.c0.x, sd.ang.c0.y, sd.ang.c0.z);
+    dst[3] = make_float4(sd.ang.c1.y, sd.ang.c1.z, sd.ang.c2.z, ra.x);
+    dst[4] = make_float4(ra.y, ra.z, sd.crs.c0.x, sd.crs.c0.y);
+    dst[5] = make_float4(sd.crs.c0.z, sd.crs.c1.x, sd.crs.c1.y, sd.crs.c1.z);
+    dst[6] = make_float4(sd.crs.c2.x, sd.crs.c2.y, sd.crs.c2.z, 0.0f);
+}
+
+// block += stamp (full 3x3 adds, as the reference adds its accumulators).
+__device__ __forceinline__ void addStamp(Blk &b, const float4 *src) {
+    const float4 s0 = src[0], s1 = src[1], s2 = src[2], s3 = src[3], s4 = src[4], s5 = src[5], s6 = src[6];
+    const m3 lin = mcols(f3{s0.x, s0.y, s0.z}, f3{s0.y, s0.w, s1.x}, f3{s0.z, s1.x, s1.y});
+    const m3 ang = mcols(f3{s2.y, s2.z, s2.w}, f3{s2.z, s3.x, s3.y}, f3{s2.w, s3.y, s3.z});
+    const m3 crs = mcols(f3{s4.z, s4.w, s5.x}, f3{s5.y, s5.z, s5.w}, f3{s6.x, s6.y, s6.z});
+    b.lin = madd(b.lin, lin);
+    b.ang = madd(b.ang, ang);
+    b.crs = madd(b.crs, crs);
+    b.rl = add(b.rl, f3{s1.z, s1.w, s2.x});
+    b.ra = add(b.ra, f3{s3.w, s4.x, s4.y});
+}
+
+struct Pose {
+    f3 x, dLin, dAng;
+    q4 q;
+    m3 rot;
+};
+
+__device__ __forceinline__ Pose loadPose(const Dev &d, int g) {
+    Pose p;
+    const float4 x4 = d.x[g];
+    p.x = xyz(x4);
+    p.q = asq(d.q[g]);
+    p.dLin = sub(p.x, xyz(d.x0[g]));
+    p.dAng = qdiff(p.q, asq(d.q0[g]));
+    p.rot = qmat(p.q);
+    return p;
+}
+
+// Force the round's primal sees for contact c (preCompute, manifold.cpp:483-499).
+__device__ __forceinline__ f3 contactError(const StepParams &p, f3 C0, f3 bracket, f3 r0, f3 r1, f3 r2) {
+    const bool separated = p.specMargin > 0.0f && C0.x > kReleaseAbove;
+    return add(scale(C0, separated ? 1.0f : p.oneMinusAlpha), basisMulD(r0, r1, r2, bracket));
+}
+
+enum : int { kSideA = 1, kSideB = 2 };
+
+// Stamps of manifold m for the requested sides, from the current poses and penalties.
+__device__ void computeStamps(const Dev &d, const StepParams &p, int m, int sides) {
+    const ManifoldBuf L = d.live;
+    const int2 ab = L.ab[m];
+    const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
+    const float4 b04 = L.b0[m];
+    const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+    const float mu = b04.w;
+    const int n = L.count[m];
+    SharedAcc sh;
+    sh.lin = mzero();
+    sh.rhsLin = f3{0, 0, 0};
+    SideAcc sa, sb;
+    zeroAcc(sa);
+    zeroAcc(sb);
+    for (int c = 0; c < n; c++) {
+        const int ci = m * kMaxContacts + c;
+        const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
+        const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+        const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+        const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
+        const f3 k = xyz(L.k[ci]);
+        f3 F = add(cmul(k, C), xyz(L.lam[ci]));
+        clampForce(F, mu);
+        float S[6];
+        basisHessianD(r0, r1, r2, k, S);
+        const f3 fw = add(add(scale(r0, F.x), scale(r1, F.y)), scale(r2, F.z));
+        stampShared(S, fw, sh);
+        if (sides & kSideA)
+            stampContact(S, rAw, fw, sa);
+        if (sides & kSideB)
+            stampContact(S, rBw, fw, sb);
+    }
+    if (sides & kSideA)
+        storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
+    if (sides & kSideB)
+        storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
+}
+
+// Which sides of manifold m take stamps for the block-Jacobi solve, and whether a coloured body
+// touches it.
+__device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touchesColour) {
+    const bool dynA = d.x[ab.x].w > 0.0f, dynB = d.x[ab.y].w > 0.0f;
+    const uint8_t ca = dynA ? d.colour[ab.x] : kUncoloured;
+    const uint8_t cb = dynB ? d.colour[ab.y] : kUncoloured;
+    touchesColour = (dynA && ca < kOverflowColour) || (dynB && cb < kOverflowColour);
+    return ((dynA && ca == kOverflowColour) ? kSideA : 0) | ((dynB && cb == kOverflowColour) ? kSideB : 0);
+}
+
+__global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= d.ctr[C_LIVE])
+        return;
+    bool touches;
+    const int sides = overflowSides(d, d.live.ab[m], touches);
+    if (!sides || touches != (mixedOnly != 0))
+        return;
+    computeStamps(d, p, m, sides);
+}
+
+// Dual pass (ManifoldStore::updateDual) and, optionally, the next round's stamps.
+__global__ void dualKernel(Dev d, StepParams p, int stamps, float decay) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= d.ctr[C_LIVE])
+        return;
+    const ManifoldBuf L = d.live;
+    const int2 ab = L.ab[m];
+    if (!(d.x[ab.x].w > 0.0f) && !(d.x[ab.y].w > 0.0f))
+        return; // frozen
+    bool touches = false;
+    int sides = stamps ? overflowSides(d, ab, touches) : 0;
+    if (touches)
+        sides = 0; // recomputed after the colour passes
+    const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
+    const float4 b04 = L.b0[m];
+    const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+    const float mu = b04.w;
+    const int n = L.count[m];
+    SharedAcc sh;
+    sh.lin = mzero();
+    sh.rhsLin = f3{0, 0, 0};
+    SideAcc sa, sb;
+    zeroAcc(sa);
+    zeroAcc(sb);
+    for (int c = 0; c < n; c++) {
+        const int ci = m * kMaxContacts + c;
+        const float4 rA4 = L.rA[ci];
+        const f3 rAw = mul(A.rot, xyz(rA4));
+        const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+        const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+        const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
+        f3 k = xyz(L.k[ci]);
+        if (decay < 1.0f)
+            k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
+        const float4 lam4 = L.lam[ci];
+        float stick = lam4.w;
+        f3 F = add(cmul(k, C), xyz(lam4));
+        const Cone cone = clampForce(F, mu);
+        const f3 lam = F;
+        const float beta = p.betaLin * rA4.w;
+        if (F.x < 0)
+            k.x = smin(k.x + beta * fabsf(C.x), PENALTY_MAX);
+        if (cone.scale <= cone.bounds) {
+            k.y = smin(k.y + beta * fabsf(C.y), PENALTY_MAX);
+            k.z = smin(k.z + beta * fabsf(C.z), PENALTY_MAX);
+            stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
+        }
+        L.k[ci] = f4(k, 0.0f);
+        L.lam[ci] = f4(lam, stick);
+        if (sides) {
+            f3 Fn = add(cmul(k, C), lam);
+            clampForce(Fn, mu);
+            float S[6];
+            basisHessianD(r0, r1, r2, k, S);
+            const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
+            stampShared(S, fw, sh);
+            if (sides & kSideA)
+                stampContact(S, rAw, fw, sa);
+            if (sides & kSideB)
+                stampContact(S, rBw, fw, sb);
+        }
+    }
+    if (sides & kSideA)
+        storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
+    if (sides & kSideB)
+        storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
+}
+
+// ---- joints (joint.cpp:80-230) ----
+
+__device__ __forceinline__ f3 jointLin(const Dev &d, int f) {
+    const int2 ab = d.fAB[f];
+    const f3 rA = xyz(d.fRA[f]), rB = xyz(d.fRB[f]);
+    const f3 pa = ab.x >= 0 ? add(xyz(d.x[ab.x]), qrot(asq(d.q[ab.x]), rA)) : rA;
+    return sub(pa, add(xyz(d.x[ab.y]), qrot(asq(d.q[ab.y]), rB)));
+}
+
+__device__ __forceinline__ f3 jointAng(const Dev &d, int f) {
+    const int2 ab = d.fAB[f];
+    const q4 qa = ab.x >= 0 ? asq(d.q[ab.x]) : q4{0.0f, 0.0f, 0.0f, 1.0f};
+    return scale(qdiff(qa, asq(d.q[ab.y])), d.fPar[f].w);
+}
+
+__device__ __forceinline__ m3 geometricStiffness(int k, f3 v) {
+    const float vk = at(v, k);
+    m3 m = mdiag(-vk, -vk, -vk);
+    f3 ck = col(m, k);
+    ck = f3{ck.x + v.x, ck.y + v.y, ck.z + v.z};
+    if (k == 0)
+        m.c0 = ck;
+    else if (k == 1)
+        m.c1 = ck;
+    else
+        m.c2 = ck;
+    return m;
+}
+
+__device__ void jointStamp(const Dev &d, const StepParams &p, int f, int body, Blk &blk) {
+    if (d.fKind[f] != 0)
+        return;
+    const int2 ab = d.fAB[f];
+    const bool isA = body == ab.x;
+    const float4 par = d.fPar[f];
+    const f3 kl = xyz(d.fKL[f]);
+    if (length2(kl) > 0) {
+        const m3 K = mdiag(kl.x, kl.y, kl.z);
+        f3 C = jointLin(d, f);
+        if (isinf(par.x))
+            C = sub(C, scale(xyz(d.fC0L[f]), p.alpha));
+        const f3 F = add(mul(K, C), xyz(d.fLL[f]));
+        const m3 I = mdiag(1, 1, 1);
+        const m3 jLin = isA ? I : mneg(I);
+        f3 r;
+        if (isA)
+            r = neg(qrot(asq(d.q[ab.x]), xyz(d.fRA[f])));
+        else
+            r = qrot(asq(d.q[ab.y]), xyz(d.fRB[f]));
+        const m3 jAng = mcols(f3{0, r.z, -r.y}, f3{-r.z, 0, r.x}, f3{r.y, -r.x, 0});
+        const m3 jLinT = transpose(jLin);
+        const m3 jAngT = transpose(jAng);
+        const m3 jAngTk = mul(jAngT, K);
+        blk.lin = madd(blk.lin, mul(mul(jLinT, K), jLin));
+        blk.ang = madd(blk.ang, mul(jAngTk, jAng));
+        blk.crs = madd(blk.crs, mul(jAngTk, jLin));
+        const f3 rr = isA ? qrot(asq(d.q[ab.x]), xyz(d.fRA[f])) : neg(qrot(asq(d.q[ab.y]), xyz(d.fRB[f])));
+        const m3 H = madd(madd(mscale(geometricStiffness(0, rr), F.x), mscale(geometricStiffness(1, rr), F.y)),
+                          mscale(geometricStiffness(2, rr), F.z));
+        blk.ang = madd(blk.ang, mdiag(H.c0.x, H.c1.y, H.c2.z));
+        blk.rl = add(blk.rl, mul(jLinT, F));
+        blk.ra = add(blk.ra, mul(jAngT, F));
+    }
+    const f3 ka = xyz(d.fKA[f]);
+    if (length2(ka) > 0) {
+        const m3 K = mdiag(ka.x, ka.y, ka.z);
+        f3 C = jointAng(d, f);
+        if (isinf(par.y))
+            C = sub(C, scale(xyz(d.fC0A[f]), p.alpha));
+        const f3 F = add(mul(K, C), xyz(d.fLA[f]));
+        const m3 base = isA ? mdiag(1, 1, 1) : mcols(f3{0, 0, 0}, f3{0, -1, 0}, f3{0, 0, -1});
+        const m3 jAng = mscale(base, par.w);
+        blk.ang = madd(blk.ang, mul(mul(transpose(jAng), K), jAng));
+        blk.ra = add(blk.ra, mul(transpose(jAng), F));
+    }
+}
+
+__global__ void forceDualKernel(Dev d, StepParams p) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= d.ctr[C_FORCES] || d.fKind[f] != 0)
+        return;
+    const float4 par = d.fPar[f];
+    f3 kl = xyz(d.fKL[f]), ka = xyz(d.fKA[f]);
+    f3 ll = xyz(d.fLL[f]), la = xyz(d.fLA[f]);
+    if (length2(kl) > 0) {
+        const m3 K = mdiag(kl.x, kl.y, kl.z);
+        f3 C = jointLin(d, f);
+        if (isinf(par.x)) {
+            C = sub(C, scale(xyz(d.fC0L[f]), p.alpha));
+            ll = add(mul(K, C), ll);
+        }
+        const f3 cap = lminv(f3{par.x, par.x, par.x}, f3{PENALTY_MAX, PENALTY_MAX, PENALTY_MAX});
+        kl = lminv(add(kl, scale(vabs(C), p.betaLin)), cap);
+    }
+    if (length2(ka) > 0) {
+        const m3 K = mdiag(ka.x, ka.y, ka.z);
+        f3 C = jointAng(d, f);
+        if (isinf(par.y)) {
+            C = sub(C, scale(xyz(d.fC0A[f]), p.alpha));
+            la = add(mul(K, C), la);
+        }
+        const f3 cap = lminv(f3{par.y, par.y, par.y}, f3{PENALTY_MAX, PENALTY_MAX, PENALTY_MAX});
+        ka = lminv(add(ka, scale(vabs(C), p.betaAng)), cap);
+    }
+    if (length2(la) > par.z * par.z) {
+        kl = ka = ll = la = f3{0, 0, 0};
+        d.fBroken[f] = 1;
+    }
+    d.fKL[f] = f4(kl, 0.0f);
+    d.fKA[f] = f4(ka, 0.0f);
+    d.fLL[f] = f4(ll, 0.0f);
+    d.fLA[f] = f4(la, 0.0f);
+}
+
+// ---- per-body passes ----
+
+__device__ __forceinline__ int nForcesDev(const Dev &d) { return d.ctr[C_FORCES]; }
+
+// Assemble body g's block from its adjacency; manifold terms from stamps (Jacobi) or recomputed
+// from the current poses (Gauss-Seidel).
+template <bool RECOMPUTE>
+__device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk) {
+    const int nf = nForcesDev(d);
+    for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
+        const int seq = static_cast<int>(d.adjSeq[e]);
+        if (seq < nf) {
+            jointStamp(d, p, nf - 1 - seq, g, blk);
+            continue;
+        }
+        const int m = seq - nf;
+        const int side = d.live.ab[m].x == g ? 0 : 1;
+        if (RECOMPUTE) {
+            // Same floats as computeStamps for one side, summed straight into the block.
+            const ManifoldBuf L = d.live;
+            const int2 ab = L.ab[m];
+            const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
+            const float4 b04 = L.b0[m];
+            const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+            const int n = L.count[m];
+            SharedAcc sh;
+            sh.lin = mzero();
+            sh.rhsLin = f3{0, 0, 0};
+            SideAcc sd;
+            zeroAcc(sd);
+            for (int c = 0; c < n; c++) {
+                const int ci = m * kMaxContacts + c;
+                const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
+                const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+                const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+                const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
+                const f3 k = xyz(L.k[ci]);
+                f3 F = add(cmul(k, C), xyz(L.lam[ci]));
+                clampForce(F, b04.w);
+                float S[6];
+                basisHessianD(r0, r1, r2, k, S);
+                const f3 fw = add(add(scale(r0, F.x), scale(r1, F.y)), scale(r2, F.z));
+                stampShared(S, fw, sh);
+                stampContact(S, side == 0 ? rAw : rBw, fw, sd);
+            }
+            const float sgn = side == 0 ? 1.0f : -1.0f;
+            blk.lin = madd(blk.lin, sh.lin);
+            blk.ang = madd(blk.ang, sd.ang);
+            blk.crs = madd(blk.crs, sd.crs);
+            blk.rl = add(blk.rl, scale(sh.rhsLin, sgn));
+            blk.ra = add(blk.ra, scale(sd.rhsAng, sgn));
+        } else {
+            addStamp(blk, d.stamps + static_cast<size_t>(2 * m + side) * kStampF4);
+        }
+    }
+}
+
+__device__ __forceinline__ Blk bodyBlock(const Dev &d, const StepParams &p, int g) {
+    const float4 x4 = d.x[g];
+    return makeBlock(x4.w, xyz(d.moment[g]), p.dtSq, xyz(x4), xyz(d.xi[g]), asq(d.q[g]), asq(d.qi[g]));
+}
+
+__global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepParams p, int colour) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.colourCount[colour])
+        return;
+    const int g = d.colourList[colour * d.NB + k];
+    Blk blk = bodyBlock(d, p, g);
+    assemble<true>(d, p, g, blk);
+    f3 dl, da;
+    solveBlock(blk, dl, da);
+    const float4 x4 = d.x[g];
+    d.x[g] = f4(add(xyz(x4), dl), x4.w);
+    d.q[g] = f4(qintegrate(asq(d.q[g]), da));
+}
+
+__global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.colourCount[kOverflowColour])
+        return;
+    const int g = d.colourList[kOverflowColour * d.NB + k];
+    Blk blk = bodyBlock(d, p, g);
+    assemble<false>(d, p, g, blk);
+    f3 dl, da;
+    solveBlock(blk, dl, da);
+    if (inPlace) {
+        const float4 x4 = d.x[g];
+        d.x[g] = f4(add(xyz(x4), scale(dl, p.jacobiRelax)), x4.w);
+        d.q[g] = f4(qintegrate(asq(d.q[g]), scale(da, p.jacobiRelax)));
+    } else {
+        d.dLin[g] = f4(dl, 0.0f);
+        d.dAng[g] = f4(da, 0.0f);
+    }
+}
+
+__global__ void overflowApplyKernel(Dev d, StepParams p) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.colourCount[kOverflowColour])
+        return;
+    const int g = d.colourList[kOverflowColour * d.NB + k];
+    const float4 x4 = d.x[g];
+    d.x[g] = f4(add(xyz(x4), scale(xyz(d.dLin[g]), p.jacobiRelax)), x4.w);
+    d.q[g] = f4(qintegrate(asq(d.q[g]), scale(xyz(d.dAng[g]), p.jacobiRelax)));
+}
+
+__device__ __forceinline__ void maskLocked(int locks, f3 &v) {
+    if (locks) {
+        if (locks & 1)
+            v.x = 0.0f;
+        if (locks & 2)
+            v.y = 0.0f;
+        if (locks & 4)
+            v.z = 0.0f;
+    }
+}
+
+// Solver::warmstartBody (solver_solve.cpp:109-142).
+__global__ void warmstartKernel(Dev d, int n, StepParams p) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0)
+        return;
+    const int locks = d.meta[g].w;
+    const int lockLin = locks & 0xff, lockAng = (locks >> 8) & 0xff;
+    const float4 x4 = d.x[g];
+    const float4 v4 = d.v[g];
+    const float mass = x4.w;
+    f3 v = xyz(v4), w = xyz(d.w[g]);
+    maskLocked(lockLin, v);
+    maskLocked(lockAng, w);
+    const float dt = p.dt;
+    const float gr = (lockLin & 0x4) ? 0.0f : v4.w;
+    const f3 x = xyz(x4);
+    const q4 q = asq(d.q[g]);
+    f3 xi = add(x, scale(v, dt));
+    if (mass > 0)
+        xi = add(xi, scale(f3{0, 0, gr}, dt * dt));
+    const q4 qi = qintegrate(q, scale(w, dt));
+    const f3 accel = divs(sub(v, xyz(d.vprev[g])), dt);
+    const float accelExt = accel.z * copysignf(1.0f, gr);
+    float weight = sclamp(accelExt / fabsf(gr), 0.0f, 1.0f);
+    if (!isfinite(weight))
+        weight = 0.0f;
+    d.xi[g] = f4(xi, 0.0f);
+    d.qi[g] = f4(qi);
+    d.x0[g] = f4(x, 0.0f);
+    d.q0[g] = f4(q);
+    d.v[g] = f4(v, v4.w);
+    d.w[g] = f4(w, 0.0f);
+    if (mass > 0) {
+        d.x[g] = f4(add(add(x, scale(v, dt)), scale(f3{0, 0, gr}, weight * dt * dt)), mass);
+        d.q[g] = f4(qintegrate(q, scale(w, dt)));
+    }
+}
+
+// Solver::finishBody (solver_solve.cpp:146-176), idle sleep disabled.
+__global__ void finishKernel(Dev d, int n, StepParams p) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0)
+        return;
+    const int locks = d.meta[g].w;
+    const float4 x4 = d.x[g];
+    const float4 v4 = d.v[g];
+    d.vprev[g] = f4(xyz(v4), 0.0f);
+    f3 v = xyz(v4), w = xyz(d.w[g]);
+    if (x4.w > 0) {
+        v = divs(sub(xyz(x4), xyz(d.x0[g])), p.dt);
+        w = divs(qdiff(asq(d.q[g]), asq(d.q0[g])), p.dt);
+    }
+    maskLocked(locks & 0xff, v);
+    maskLocked((locks >> 8) & 0xff, w);
+    d.v[g] = f4(v, v4.w);
+    d.w[g] = f4(w, 0.0f);
+}
+
+// ---- update set and colouring (solver_solve.cpp:263-424) ----
+
+__global__ void contactOnlyInitKernel(Dev d, int n) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n)
+        return;
+    d.contactOnly[g] = 1;
+    d.colour[g] = (d.meta[g].x >= 0 && d.x[g].w > 0.0f) ? kUncoloured : kOverflowColour;
+}
+
+__global__ void contactOnlyMarkKernel(Dev d) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= d.ctr[C_FORCES])
+        return;
+    const int2 ab = d.fAB[f];
+    if (ab.x >= 0)
+        d.contactOnly[ab.x] = 0;
+    if (ab.y >= 0)
+        d.contactOnly[ab.y] = 0;
+}
+
+__device__ __forceinline__ int adjOtherSolve(const Dev &d, uint32_t seq, int x, int nf) {
+    int a, b;
+    if (static_cast<int>(seq) < nf) {
+        const int2 ab = d.fAB[nf - 1 - static_cast<int>(seq)];
+        a = ab.x;
+        b = ab.y;
+    } else {
+        const int2 ab = d.live.ab[static_cast<int>(seq) - nf];
+        a = ab.x;
+        b = ab.y;
+    }
+    if (a == x)
+        return b;
+    if (b == x)
+        return a;
+    return -1;
+}
+
+// One Jones-Plassmann round with list-order priority: a body is coloured once every earlier
+// (lower list position) neighbour in the update set is, with the smallest colour none of them
+// uses (the sequential greedy of colourGraph, reproduced exactly).
+__global__ void colourRoundKernel(Dev d, int n) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
+        return;
+    volatile uint8_t *col = d.colour;
+    if (col[g] != kUncoloured)
+        return;
+    const int nf = d.ctr[C_FORCES];
+    const int lpg = listPos(d, g);
+    unsigned used = 0;
+    for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
+        const int h = adjOtherSolve(d, d.adjSeq[e], g, nf);
+        if (h < 0 || !(d.x[h].w > 0.0f) || listPos(d, h) >= lpg)
+            continue;
+        const uint8_t c = col[h];
+        if (c == kUncoloured) {
+            atomicAdd(&d.ctr[C_UNCOLOURED], 1);
+            return;
+        }
+        if (c < kMaxColours)
+            used |= 1u << c;
+    }
+    uint8_t c = kOverflowColour;
+    for (int k = 0; k < kMaxColours; k++)
+        if (!(used & (1u << k))) {
+            c = static_cast<uint8_t>(k);
+            break;
+        }
+    col[g] = c;
+}
+
+__global__ void colourListKernel(Dev d, int n, int contactOnlyOverflow) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
+        return;
+    uint8_t c = d.colour[g];
+    if (contactOnlyOverflow && d.contactOnly[g])
+        c = kOverflowColour;
+    d.colour[g] = c;
+    const int slot = atomicAdd(&d.colourCount[c], 1);
+    d.colourList[c * d.NB + slot] = g;
+}
+
+} // namespace
+
+static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
+
+void launchContactOnly(const Dev &d, int n, cudaStream_t s) {
+    contactOnlyInitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    contactOnlyMarkKernel<<<grid(d.FF), kThreads, 0, s>>>(d);
+}
+
+void launchColour(const Dev &d, int n, bool needGreedy, cudaStream_t s) {
+    if (!needGreedy)
+        return;
+    // Rounds until no body is waiting; the host checks every 16 rounds.
+    for (int batch = 0; batch < 4096; batch++) {
+        for (int r = 0; r < 16; r++) {
+            cudaMemsetAsync(d.ctr + C_UNCOLOURED, 0, sizeof(int), s);
+            colourRoundKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+        }
+        int waiting = 0;
+        cudaMemcpyAsync(&waiting, d.ctr + C_UNCOLOURED, sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        if (waiting == 0)
+            return;
+    }
+}
+
+void launchColourLists(const Dev &d, int n, int contactOnlyOverflow, cudaStream_t s) {
+    cudaMemsetAsync(d.colourCount, 0, sizeof(int) * (kMaxColours + 1), s);
+    colourListKernel<<<grid(n), kThreads, 0, s>>>(d, n, contactOnlyOverflow);
+}
+
+void launchWarmstartBodies(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
+    warmstartKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+}
+
+void launchFinishBodies(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
+    finishKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+}
+
+void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s) {
+    stampsKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
+}
+
+void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &p, cudaStream_t s) {
+    colourPassKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
+}
+
+void launchOverflowSolve(const Dev &d, int capacity, const StepParams &p, bool inPlace, cudaStream_t s) {
+    overflowSolveKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p,
+                                                                                                    inPlace ? 1 : 0);
+}
+
+void launchOverflowApply(const Dev &d, int capacity, const StepParams &p, cudaStream_t s) {
+    overflowApplyKernel<<<grid(capacity), kThreads, 0, s>>>(d, p);
+}
+
+void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s) {
+    dualKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, stamps ? 1 : 0, decay);
+}
+
+void launchForceDual(const Dev &d, const StepParams &p, int nForces, cudaStream_t s) {
+    if (nForces <= 0)
+        return;
+    forceDualKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
+}
+
+} // namespace avbdg

@@ -1,0 +1,55 @@
+// Host-side launchers of the step's kernels (one function per kernel or kernel group).
+#pragma once
+
+#include "engine.cuh"
+
+namespace avbdg {
+
+// ---- broad phase (k_broad.cu) ----
+void launchAabb(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
+// Morton codes per body for the worlds listed as rebuilding (all worlds when `all`), then the
+// stable (world, code, list index) sort into leafBody and the Karras topology per world.
+void launchRebuildTree(const Dev &d, int nBodies, int nWorlds, cudaStream_t s);
+void launchRefit(const Dev &d, int nBodies, cudaStream_t s);
+// Candidate pairs: traversal count, scan, emit, per-segment sort. Leaves the count in C_PAIRS.
+void launchPairs(const Dev &d, int nBodies, cudaStream_t s);
+// Exact filter and acquisition of new manifolds after the live ones (C_CAND = C_LIVE + new).
+void launchFilterAcquire(const Dev &d, cudaStream_t s);
+
+// ---- manifolds and adjacency (k_manifold.cu) ----
+void launchAdjacency(const Dev &d, int nBodies, cudaStream_t s);
+void launchManifoldInit(const Dev &d, const StepParams &p, cudaStream_t s);
+void launchManifoldCompact(const Dev &d, cudaStream_t s);
+void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s);
+void launchForceInit(const Dev &d, const StepParams &p, int nForces, cudaStream_t s);
+
+// ---- update set and colouring (k_solve.cu) ----
+void launchContactOnly(const Dev &d, int nBodies, cudaStream_t s);
+// Greedy colouring of dynamic bodies in list order (when `needGreedy`), colours in d.colour.
+void launchColour(const Dev &d, int nBodies, bool needGreedy, cudaStream_t s);
+// Contact-only bodies to the overflow colour, then per-colour body lists and counts.
+void launchColourLists(const Dev &d, int nBodies, int contactOnlyOverflow, cudaStream_t s);
+
+// ---- substep (k_solve.cu) ----
+void launchWarmstartBodies(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
+void launchFinishBodies(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
+// Stamps (precompute) of manifolds touching the overflow set; `mixedOnly` restricts to those that
+// also touch a coloured body (recomputed after the colour passes).
+void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
+void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &p, cudaStream_t s);
+void launchOverflowSolve(const Dev &d, int capacity, const StepParams &p, bool inPlace, cudaStream_t s);
+void launchOverflowApply(const Dev &d, int capacity, const StepParams &p, cudaStream_t s);
+// Dual pass over live manifolds; with `stamps`, also the next round's stamps of manifolds whose
+// bodies are all overflow or static. `decay` < 1 scales penalties first (dual-only rounds).
+void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s);
+void launchForceDual(const Dev &d, const StepParams &p, int nForces, cudaStream_t s);
+
+// ---- projection (k_proj.cu) ----
+// projectionActive per world and the brake candidates (manifolds with an open gap).
+void launchProjActive(const Dev &d, int nWorlds, cudaStream_t s);
+void launchBrake(const Dev &d, int nWorlds, float window, cudaStream_t s);
+void launchProjection(const Dev &d, int nBodies, int nWorlds, const StepParams &p, cudaStream_t s);
+
+int brakeGridBlocks();
+
+} // namespace avbdg

@@ -1,0 +1,38 @@
+// Parallel primitives of the step: exclusive scan, stable LSD radix sort, segmented sort.
+//
+// Every primitive takes its element count from DEVICE memory and sizes its grid from a host
+// capacity, so a whole step can run without host round trips (and be captured in a graph).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace avbdg {
+
+// Scratch sizes the primitives need for `capacity` elements.
+size_t scanScratchBytes(int capacity);
+size_t radixScratchBytes(int capacity);
+
+// out[i] = sum(in[0..i)) for i < *d_n; *d_total = sum(in[0..*d_n)) (d_total may be null).
+// `in` and `out` may alias.
+void scanExclusive(const int *in, int *out, int capacity, const int *d_n, int *d_total, void *scratch,
+                   cudaStream_t stream);
+
+// Stable ascending sort of (keys, values) by key bits [beginBit, endBit) for *d_n elements.
+// Sorted data ends in keys/values; keysAlt/valuesAlt are the ping-pong buffers.
+void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_t *valuesAlt, int capacity,
+                    const int *d_n, int beginBit, int endBit, void *scratch, cudaStream_t stream);
+
+// Sorts each segment data[start[s] .. start[s+1]) ascending, for s < *d_segments. Segments up to 32
+// entries are sorted by one thread, up to 8192 by one block in shared memory, longer ones by a
+// tiled rank sort over several blocks through `tmp` (same capacity as `data`). Values must be
+// distinct within a segment. `longList` needs `segCapacity` ints, `longCount` one int.
+void segmentedSortU32(uint32_t *data, uint32_t *tmp, const int *start, int segCapacity, const int *d_segments,
+                      int *longList, int *longCount, cudaStream_t stream);
+void segmentedSortU64(uint64_t *data, uint64_t *tmp, const int *start, int segCapacity, const int *d_segments,
+                      int *longList, int *longCount, cudaStream_t stream);
+
+inline int divUp(int a, int b) { return (a + b - 1) / b; }
+
+} // namespace avbdg

@@ -478,7 +478,7 @@ int faceManifold(const Obb &A, const Obb &B, bool refIsA, int refAxis, V3 normal
     if (!count)
         return 0;
 
-    ContactSink sink{A, B, out};
+    ContactSink sink{A, B, out, 0, {}};
     int prefix = (refIsA ? kAxisFaceA : kAxisFaceB) << 24;
     prefix |= (refAxis & 0xFF) << 16;
     prefix |= (incAxis & 0xFF) << 8;
@@ -506,7 +506,7 @@ int edgeContact(const Obb &A, const Obb &B, int axisA, int axisB, V3 normalAB, C
     supportEdge(B, axisB, -normalAB, b0, b1);
     V3 xA, xB;
     closestOnSegments(a0, a1, b0, b1, xA, xB);
-    ContactSink sink{A, B, out};
+    ContactSink sink{A, B, out, 0, {}};
     const int key = (kAxisEdge << 24) | ((axisA & 0xFF) << 8) | (axisB & 0xFF);
     sink.add(xA, xB, key);
     if (!sink.count) {
@@ -579,6 +579,7 @@ int World::addBody(const avbdg_body_desc &d) {
                   (b.size.x * b.size.x + b.size.y * b.size.y) / 12.0f * b.mass};
     b.radius = std::sqrt(dot(b.size * 0.5f, b.size * 0.5f));
     bodies.push_back(b);
+    treeBodies = -1;
     return static_cast<int>(bodies.size()) - 1;
 }
 
@@ -1139,20 +1140,30 @@ void World::broadPhase() {
     if (ex < 1.0e-6f)
         ex = 1.0e-6f;
     const float scale = 2097151.0f / ex;
-    codes.resize(n);
-    for (int i = 0; i < n; i++) {
-        const V3 c = aabbCenter[i];
-        codes[i] = expandBits21(quantise(c.x, lo.x, scale)) | (expandBits21(quantise(c.y, lo.x, scale)) << 1) |
-                   (expandBits21(quantise(c.z, lo.x, scale)) << 2);
+    // The reference refreshes its codes and order only when it rebuilds the tree: the body set
+    // changed or 16 refits have passed (bvh_broadphase.cpp:186-203). The candidate set does not
+    // depend on the tree, so the oracle walks a fresh tree every step but keeps the reference's
+    // code/order schedule for the diagnostic dumps.
+    if (treeBodies != n || treeAge >= 16) {
+        codes.resize(n);
+        for (int i = 0; i < n; i++) {
+            const V3 c = aabbCenter[i];
+            codes[i] = expandBits21(quantise(c.x, lo.x, scale)) | (expandBits21(quantise(c.y, lo.x, scale)) << 1) |
+                       (expandBits21(quantise(c.z, lo.x, scale)) << 2);
+        }
+        order.resize(n);
+        for (int i = 0; i < n; i++)
+            order[i] = i;
+        std::sort(order.begin(), order.end(), [this](int a, int b) {
+            if (codes[a] != codes[b])
+                return codes[a] < codes[b];
+            return a < b;
+        });
+        treeBodies = n;
+        treeAge = 0;
+    } else {
+        treeAge++;
     }
-    order.resize(n);
-    for (int i = 0; i < n; i++)
-        order[i] = i;
-    std::sort(order.begin(), order.end(), [this](int a, int b) {
-        if (codes[a] != codes[b])
-            return codes[a] < codes[b];
-        return a < b;
-    });
 
     // Pairwise bottom-up merge of the sorted leaves, bounds by min/max of the children.
     std::vector<Node> nodes;

@@ -105,6 +105,7 @@ public:
     int colourCount = 0, overflowCount = 0;
 
     int addBody(const avbdg_body_desc &d);
+    void invalidateTree() { treeBodies = -1; }
     void addJoint(int a, int b, V3 rA, V3 rB, float kLin, float kAng, float fracture);
     void addIgnore(int a, int b);
     void step();
@@ -122,6 +123,7 @@ private:
     std::vector<Ref> adjRefs;
     std::vector<int> overflowOrder, colourBegins, colourOrder;
     std::vector<V3> aabbCenter, aabbHalf;
+    int treeBodies = -1, treeAge = 0; // code/order refresh schedule of the reference's LBVH
 
     void buildAdjacency();
     int otherBody(const Ref &r, int body) const;

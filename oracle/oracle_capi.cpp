@@ -101,6 +101,7 @@ int avbdo_world_clear(World *w) {
     w->bodies.clear();
     w->forces.clear();
     w->live.clear();
+    w->invalidateTree();
     return AVBDG_OK;
 }
 

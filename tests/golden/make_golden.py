@@ -1,0 +1,83 @@
+"""Generate the golden fixtures of the parity tests from the reference solver itself.
+
+Runs the reference core compiled from its own sources (oracle/_ref/libavbd_ref.so, built by
+`make -C oracle ref` on a machine that has the reference tree) on the scenes of
+godot-avbd_gb300/scenes.py and records, per scene:
+  - the FNV-1a state digest after every step (test/core_test.cpp:133-149),
+  - the sorted candidate pairs, Morton codes and (code, index) order after the first step,
+  - the live manifolds' body ids, contact counts and feature keys after the first and last step,
+  - the colouring of the last step.
+Writes tests/golden/reference_runs.json. Usage: python tests/golden/make_golden.py
+"""
+
+import ctypes
+import hashlib
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as entry  # noqa: E402
+
+# (scene builder, keyword arguments, steps recorded)
+RUNS = [
+    ("stack", {}, 300),
+    ("interleaved", {}, 300),
+    ("mixed", {}, 240),
+    ("hard_chain", {}, 120),
+    ("pyramid420", {}, 120),
+    ("pile", {"count": 300, "chain_links": 8}, 120),
+    ("lattice", {"nx": 8, "ny": 8, "nz": 4}, 90),
+]
+
+
+def sha(a):
+    return hashlib.sha256(a.tobytes()).hexdigest()
+
+
+def main():
+    pkg = entry.load_package()
+    capi, scenes = pkg.capi, pkg.scenes
+    lib = os.path.join(ROOT, "oracle", "_ref", "libavbd_ref.so")
+    ref = capi.Api(ctypes.CDLL(lib), "avbdr_")
+    out = {"generator": "tests/golden/make_golden.py", "runs": {}}
+    for name, kw, steps in RUNS:
+        sc = getattr(scenes, name)(**kw)
+        p = ref.default_params()
+        p.threads = 1
+        w = scenes.instantiate(ref, sc, params=p)
+        digests = []
+        rec = {"scene": name, "kwargs": kw, "steps": steps, "bodies": sc.n}
+        for s in range(steps):
+            scenes.advance(w, sc, 1)
+            digests.append(f"{w.digest():016x}")
+            if s == 0:
+                codes, order, pairs = w.broadphase()
+                rec["first_step"] = {
+                    "pairs_sha": sha(pairs), "pairs": int(pairs.size),
+                    "codes_sha": sha(codes), "order_sha": sha(order),
+                }
+                m = w.manifolds()
+                rec["first_step"]["manifolds_sha"] = sha(m["body_a"]) + sha(m["body_b"]) + sha(m["count"]) + \
+                    sha(m["features"])
+        m = w.manifolds()
+        col, ids = w.colours()
+        st = w.stats()
+        rec["last_step"] = {
+            "manifolds": int(m["count"].size), "contacts": int(m["count"].sum()),
+            "manifolds_sha": sha(m["body_a"]) + sha(m["body_b"]) + sha(m["count"]) + sha(m["features"]),
+            "colours_sha": sha(col) + sha(ids), "colour_groups": st.colour_groups,
+            "overflow": st.overflow_bodies,
+        }
+        rec["digests"] = digests
+        out["runs"][name] = rec
+        print(name, sc.n, "bodies", steps, "steps, last digest", digests[-1], flush=True)
+    with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,165 @@
+"""GPU parity: the sm_103a step against the reference (golden fixtures recorded from it) and the
+oracle, through the C ABI.
+
+Bar: bit-exact. Body state after every step must equal the reference's (FNV digests over
+position, orientation and both velocities), and the integer stages (candidate pairs, Morton codes,
+sorted order, manifold contact counts and feature keys, colouring) must be identical.
+"""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", ["stack", "interleaved", "mixed"])
+def test_gpu_reproduces_pinned_digests(pkg, gpu, name):
+    scenes = pkg.scenes
+    sc = getattr(scenes, name)()
+    w = scenes.instantiate(gpu, sc)
+    scenes.advance(w, sc)
+    assert w.digest() == scenes.PINNED_DIGESTS[name]
+
+
+@pytest.mark.parametrize("run", ["stack", "interleaved", "mixed", "hard_chain", "pyramid420", "pile", "lattice"])
+def test_gpu_matches_reference_every_step(pkg, gpu, golden, run):
+    scenes = pkg.scenes
+    rec = golden["runs"][run]
+    sc = getattr(scenes, rec["scene"])(**rec["kwargs"])
+    w = scenes.instantiate(gpu, sc)
+    for s in range(rec["steps"]):
+        scenes.advance(w, sc, 1)
+        assert f"{w.digest():016x}" == rec["digests"][s], f"{run}: first differing step {s + 1}"
+        if s == 0:
+            codes, order, pairs = w.broadphase()
+            fs = rec["first_step"]
+            assert pairs.size == fs["pairs"] and sha(pairs) == fs["pairs_sha"], "candidate pairs"
+            assert sha(codes) == fs["codes_sha"], "Morton codes"
+            assert sha(order) == fs["order_sha"], "sorted order"
+            m = w.manifolds()
+            assert sha(m["body_a"]) + sha(m["body_b"]) + sha(m["count"]) + sha(m["features"]) == fs["manifolds_sha"]
+    m = w.manifolds()
+    col, ids = w.colours()
+    ls = rec["last_step"]
+    assert sha(m["body_a"]) + sha(m["body_b"]) + sha(m["count"]) + sha(m["features"]) == ls["manifolds_sha"]
+    assert sha(col) + sha(ids) == ls["colours_sha"]
+    st = w.stats()
+    assert st.colour_groups == ls["colour_groups"] and st.overflow_bodies == ls["overflow"]
+
+
+def _compare_worlds(pkg, a, b, steps, check_every=1, rebuild_every=17):
+    scenes = pkg.scenes
+    for s in range(steps):
+        a.step()
+        b.step()
+        if (s + 1) % check_every == 0 or s == steps - 1:
+            for x, y, field in zip(a.state(), b.state(), ["position", "orientation", "velocity", "angular"]):
+                assert np.array_equal(x, y), f"step {s + 1}: {field} differs (max {np.max(np.abs(x - y)):g})"
+        if s % rebuild_every == 0:
+            ca, oa, pa = a.broadphase()
+            cb, ob, pb = b.broadphase()
+            assert np.array_equal(pa, pb), f"step {s + 1}: pairs"
+            assert np.array_equal(ca, cb) and np.array_equal(oa, ob), f"step {s + 1}: codes/order"
+            ma, mb = a.manifolds(), b.manifolds()
+            for key in ["body_a", "body_b", "count", "features"]:
+                assert np.array_equal(ma[key], mb[key]), f"step {s + 1}: manifold {key}"
+            for key in ["c0", "penalty", "lambda", "basis"]:
+                assert np.array_equal(ma[key], mb[key]), f"step {s + 1}: manifold {key}"
+
+
+@pytest.mark.parametrize("option", ["adaptive_beta", "stiffness_decay", "no_projection", "gs_contacts"])
+def test_gpu_matches_oracle_with_options(pkg, gpu, oracle, option):
+    scenes = pkg.scenes
+    sc = scenes.pile(count=120, chain_links=6)
+
+    def params(api):
+        p = api.default_params()
+        scenes.apply_params(p, sc.params)
+        if option == "adaptive_beta":
+            p.adaptive_beta = 1
+        elif option == "stiffness_decay":
+            p.newton_ratio = 0.5
+            p.stiffness_decay = 0.9
+        elif option == "no_projection":
+            p.position_projection = 0
+        elif option == "gs_contacts":
+            p.contact_only_overflow = 0
+        return p
+
+    a = scenes.instantiate(gpu, sc, params=params(gpu))
+    b = scenes.instantiate(oracle, sc, params=params(oracle))
+    _compare_worlds(pkg, a, b, 60)
+
+
+def test_gpu_matches_oracle_full_pile(pkg, gpu, oracle):
+    """The 1653-box mass-ratio pile with its 32-link chain, first 30 steps, every field."""
+    scenes = pkg.scenes
+    sc = scenes.pile()
+    a = scenes.instantiate(gpu, sc)
+    b = scenes.instantiate(oracle, sc)
+    _compare_worlds(pkg, a, b, 30, check_every=1)
+
+
+def test_gpu_matches_oracle_lattice_slice(pkg, gpu, oracle):
+    """A 16 x 16 x 8 slice of the large lattice (2048 cubes), 40 steps."""
+    scenes = pkg.scenes
+    sc = scenes.lattice(nx=16, ny=16, nz=8)
+    a = scenes.instantiate(gpu, sc)
+    b = scenes.instantiate(oracle, sc)
+    _compare_worlds(pkg, a, b, 40, check_every=5)
+
+
+def test_gpu_edge_cases(pkg, gpu, oracle):
+    capi, scenes = pkg.capi, pkg.scenes
+    # Empty world and a single body: stepping is a no-op / free fall, as in the reference.
+    w = pkg.world()
+    w.step()
+    assert w.stats().manifolds == 0
+    for api in (gpu, oracle):
+        pass
+    one = scenes.stack()
+    one_g = capi.World(gpu)
+    one_o = capi.World(oracle)
+    d = capi.make_body_descs(one.size[1:2], one.density[1:2], one.friction[1:2], one.position[1:2])
+    one_g.add_bodies(d)
+    one_o.add_bodies(d)
+    for _ in range(20):
+        one_g.step()
+        one_o.step()
+    for x, y in zip(one_g.state(), one_o.state()):
+        assert np.array_equal(x, y)
+    # Non-finite input is rejected at the boundary.
+    bad = capi.make_body_descs([[1, 1, 1]], [1.0], [0.5], [[0, 0, float("nan")]])
+    with pytest.raises(capi.AvbdError) as e:
+        pkg.world().add_bodies(bad)
+    assert e.value.code == capi.ERR_NONFINITE
+    # Unsupported options are reported, never approximated.
+    p = gpu.default_params()
+    p.sleep_frames = 10
+    with pytest.raises(capi.AvbdError) as e:
+        pkg.world(p)
+    assert e.value.code == capi.ERR_UNSUPPORTED
+
+
+def test_gpu_host_state_edits(pkg, gpu, oracle):
+    """Velocity edits between steps (the server integrates host forces this way)."""
+    scenes = pkg.scenes
+    sc = scenes.pyramid420()
+    a = scenes.instantiate(gpu, sc)
+    b = scenes.instantiate(oracle, sc)
+    for s in range(20):
+        a.step()
+        b.step()
+        if s == 9:
+            p, q, v, w = a.state()
+            v[1:50, 0] += 0.5
+            a.set_state(velocity=v)
+            b.set_state(velocity=v)
+    for x, y in zip(a.state(), b.state()):
+        assert np.array_equal(x, y)

@@ -1,0 +1,98 @@
+"""Pin the oracle (CPU restatement of the reference step) before trusting it as the checker.
+
+1. The reference suite's pinned digests (tools/baseline/digests.txt:1-3) must come out exactly.
+2. Per-step digests, candidate pairs, Morton codes, sorted order, manifold features and colouring
+   must equal the golden fixtures recorded from the reference itself (tests/golden/).
+3. Where the compiled reference is present, the oracle must match it step by step under
+   non-default solver options too.
+"""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", ["stack", "interleaved", "mixed"])
+def test_pinned_reference_digests(pkg, oracle, name):
+    scenes = pkg.scenes
+    sc = getattr(scenes, name)()
+    w = scenes.instantiate(oracle, sc)
+    scenes.advance(w, sc)
+    assert w.digest() == scenes.PINNED_DIGESTS[name]
+
+
+def test_golden_runs(pkg, oracle, golden):
+    scenes = pkg.scenes
+    for name, rec in golden["runs"].items():
+        sc = getattr(scenes, rec["scene"])(**rec["kwargs"])
+        p = oracle.default_params()
+        w = scenes.instantiate(oracle, sc, params=p)
+        for s in range(rec["steps"]):
+            scenes.advance(w, sc, 1)
+            assert f"{w.digest():016x}" == rec["digests"][s], f"{name}: step {s + 1} digest differs"
+            if s == 0:
+                codes, order, pairs = w.broadphase()
+                fs = rec["first_step"]
+                assert pairs.size == fs["pairs"] and sha(pairs) == fs["pairs_sha"], name
+                assert sha(codes) == fs["codes_sha"] and sha(order) == fs["order_sha"], name
+                m = w.manifolds()
+                assert sha(m["body_a"]) + sha(m["body_b"]) + sha(m["count"]) + sha(m["features"]) == \
+                    fs["manifolds_sha"], name
+        m = w.manifolds()
+        col, ids = w.colours()
+        ls = rec["last_step"]
+        assert sha(m["body_a"]) + sha(m["body_b"]) + sha(m["count"]) + sha(m["features"]) == ls["manifolds_sha"]
+        assert sha(col) + sha(ids) == ls["colours_sha"], name
+
+
+@pytest.mark.parametrize("option", ["adaptive_beta", "stiffness_decay", "no_projection", "gs_contacts"])
+def test_oracle_matches_reference_options(pkg, oracle, ref, option):
+    scenes = pkg.scenes
+    sc = scenes.pile(count=120, chain_links=6)
+
+    def params(api):
+        p = api.default_params()
+        scenes.apply_params(p, sc.params)
+        if option == "adaptive_beta":
+            p.adaptive_beta = 1
+        elif option == "stiffness_decay":
+            p.newton_ratio = 0.5
+            p.stiffness_decay = 0.9
+        elif option == "no_projection":
+            p.position_projection = 0
+        elif option == "gs_contacts":
+            p.contact_only_overflow = 0
+        p.threads = 1
+        return p
+
+    wo = scenes.instantiate(oracle, sc, params=params(oracle))
+    wr = scenes.instantiate(ref, sc, params=params(ref))
+    for s in range(90):
+        wo.step()
+        wr.step()
+        assert wo.digest() == wr.digest(), f"{option}: step {s + 1}"
+
+
+def test_oracle_matches_reference_interleaved_pile(pkg, oracle, ref):
+    scenes = pkg.scenes
+    sc = scenes.pile(count=150, chain_links=4)
+    sc.params["dt"] = float(np.float32(1.0) / np.float32(240.0))
+    wo = scenes.instantiate(oracle, sc)
+    wr = scenes.instantiate(ref, sc)
+    for s in range(60):
+        wo.step_interleaved(4, 2)
+        wr.step_interleaved(4, 2)
+        assert wo.digest() == wr.digest(), f"step {s + 1}"
+
+
+def test_oracle_rejects_unrestated_options(pkg, oracle):
+    p = oracle.default_params()
+    p.sleep_frames = 30
+    with pytest.raises(pkg.capi.AvbdError) as e:
+        pkg.capi.World(oracle, p)
+    assert e.value.code == pkg.capi.ERR_UNSUPPORTED
