@@ -1,0 +1,311 @@
+"""Benchmark of the GB300 AVBD time-step: dynamic body-steps per second at 10 solver iterations.
+
+One JSON line on rank 0. Workloads (seeded synthetic scenes, identical inputs on every arm):
+  pile       1653 boxes, edges log-uniform 0.25-2 m, densities log-uniform 100-1e4 kg/m^3, random
+             orientations, dropped on a 200 x 1 x 200 m ground, plus a 32-link hard ball-joint
+             chain (0.2 x 0.2 x 1 m links) hung from a static anchor. dt 1/60 s, 10 iterations.
+  pyramid420 two 20-row walls of unit cubes (420 boxes). dt 1/60 s, 10 iterations.
+  lattice    64 x 64 x 16 unit cubes, 5 cm gaps, 2 cm jitter, 500 m ground. dt 1/60 s, 10 iterations.
+
+--impl gpu (default): the sm_103a library. `value` times each step on the library's stream with
+CUDA events (the device is idle between steps while the host reads the step's counters), with L2
+flushed by a 512 MB write before every timed step. `e2e` runs the same workload through the C ABI
+with host buffers: every step uploads the bodies' positions, orientations and velocities from
+host memory and reads them back.
+--impl reference: the reference's CPU step on this machine's host cores (the reference compiled
+from its own sources when present here, otherwise the oracle restatement of it), all threads.
+Multi-GPU: one independent replica per rank (the path does not shard a single scene).
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as entry  # noqa: E402
+
+METRIC = "body-steps/s @10 iters"
+UNIT = "body-steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def workload(name):
+    scenes = entry.load_package().scenes
+    if name == "pile":
+        sc = scenes.pile()
+        desc = ("mass-ratio pile: 1653 boxes (edges log-uniform 0.25-2 m, densities 100-1e4 kg/m^3, random "
+                "orientations) + 32-link hard ball-joint chain, dt 1/60, 10 iterations")
+    elif name == "pyramid420":
+        sc = scenes.pyramid420()
+        desc = "two 20-row walls of 1 m cubes (420 boxes) on a static ground, dt 1/60, 10 iterations"
+    elif name == "lattice":
+        sc = scenes.lattice()
+        desc = "65,536 unit cubes on a 64x64x16 lattice (5 cm gaps, 2 cm jitter) dropped on a 500 m ground, " \
+               "dt 1/60, 10 iterations"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return sc, desc
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                maxes.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": max(maxes), "reasons": sorted(reasons),
+                "samples": len(mhz)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def manifold_pass_bytes(world, dynamic_mask, iterations):
+    """Algorithmic bytes of one dual+stamp pass over the live manifolds (the dominant kernel).
+
+    Per non-frozen manifold: body indices, basis and friction, contact count (60 B); position,
+    orientation and start-of-step pose of both bodies (128 B). Per contact: anchors, step-start
+    error, penalty and dual read (80 B), penalty and dual written (32 B). Per overflow side the
+    pass writes a 112 B block stamp on all but the last round of a step.
+    """
+    m = world.manifolds()
+    dyn_a = dynamic_mask[m["body_a"]]
+    dyn_b = dynamic_mask[m["body_b"]]
+    active = dyn_a | dyn_b
+    n_m = int(active.sum())
+    n_c = int(m["count"][active].sum())
+    sides = int(dyn_a.sum() + dyn_b.sum())
+    base = 188 * n_m + 112 * n_c
+    avg = base + 112 * sides * (iterations - 1) / iterations
+    return avg, {"manifolds": n_m, "contacts": n_c, "stamp_sides": sides}
+
+
+def run_cpu_reference(sc, steps, warmup, threads, time_budget_s=None):
+    """Time the reference CPU step (compiled reference if present here, else the oracle port)."""
+    pkg = entry.load_package()
+    capi, scenes = pkg.capi, pkg.scenes
+    ref_lib = os.path.join(ROOT, "oracle", "_ref", "libavbd_ref.so")
+    if os.path.exists(ref_lib):
+        api, kind = capi.Api(ctypes.CDLL(ref_lib), "avbdr_"), "reference"
+    else:
+        lib = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+        if not os.path.exists(lib):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+        api, kind = capi.Api(ctypes.CDLL(lib), "avbdo_"), "port"
+    p = api.default_params()
+    scenes.apply_params(p, sc.params)
+    p.threads = threads
+    w = scenes.instantiate(api, sc, params=p)
+    w.step(warmup) if warmup > 0 else None
+    done, t0 = 0, time.perf_counter()
+    per_step = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        w.step()
+        per_step.append(time.perf_counter() - t)
+        done += 1
+        if time_budget_s and time.perf_counter() - t0 > time_budget_s:
+            break
+    elapsed = sum(per_step)
+    return sc.dynamic * done / elapsed, kind, done, elapsed
+
+
+def run_gpu(args, rank, world_size):
+    import numpy as np
+    import torch
+
+    pkg = entry.load_package()
+    capi, scenes = pkg.capi, pkg.scenes
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    sc, desc = workload(args.workload)
+    gpu = pkg.gpu_api()
+    w = scenes.instantiate(gpu, sc)
+    dyn_mask = sc.density > 0
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        w.step()
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    w.take_kernel_times() if hasattr(w, "take_kernel_times") else None
+    w.set_profiling(True)
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            w.step()
+            step_ms.append(w.stats().total_ms)
+        torch.cuda.synchronize()
+    kt = w.take_kernel_times()
+    w.set_profiling(False)
+    total_ms = float(sum(step_ms))
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    body_steps = sc.dynamic * args.steps * world_size
+    value = body_steps / (total_ms / 1e3)
+
+    # End to end through the C ABI with host buffers.
+    p, q, v, av = w.state()
+    h2d = d2h = 13 * 4 * sc.n
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.set_state(position=p, orientation=q, velocity=v, angular_velocity=av)
+        w.step()
+        p, q, v, av = w.state()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world_size > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": body_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    peak, peak_kind = measured_peak_hbm()
+    bytes_per_launch, counts = manifold_pass_bytes(w, dyn_mask, 10)
+    launch_ms = kt.manifold_ms / max(kt.manifold_launches, 1)
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("manifold_pass_bytes_per_launch")
+    roofline = {"bound": "hbm", "kernel": "dualKernel (manifold dual + block stamps)", "achieved": achieved,
+                "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
+                "launch_ms": launch_ms, "counts": counts,
+                "note": "working set fits in L2 (126 MB); L2 flushed before each step, not between launches"}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+           "config": {"workload": desc, "bodies": sc.n, "dynamic_bodies": sc.dynamic, "joints": len(sc.joints),
+                      "iterations": 10, "dt": "1/60", "form": "plain per-scene step",
+                      "timed_steps": [args.warmup + 1, args.warmup + args.steps],
+                      "l2": "flushed (512 MB write) before every timed step", "parallelism": f"replicas x{world_size}"},
+           "roofline": roofline, "e2e": e2e, "gpu_launches": kt.kernel_launches,
+           "clocks": clocks.summary(),
+           "phase_ms_last_step": {k: getattr(w.stats(), k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]},
+           "kernel_ms": {"manifold_pass_per_launch": launch_ms, "body_solve_per_launch":
+                         kt.body_ms / max(kt.body_launches, 1), "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)}}
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
+        cpu_threads = os.cpu_count() or 1
+        v_cpu, kind, done, elapsed = run_cpu_reference(sc, args.steps, args.warmup, 0, time_budget_s=20.0)
+        out["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": cpu_threads, "kind": kind,
+                               "sample": f"steps {args.warmup + 1}-{args.warmup + done} of the same scene "
+                                         f"({elapsed:.1f} s of CPU step time, all {cpu_threads} threads)"}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=300)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="pile", choices=["pile", "pyramid420", "lattice"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sc, desc = workload(args.workload)
+        threads = os.cpu_count() or 1
+        v, kind, done, elapsed = run_cpu_reference(sc, args.steps, args.warmup, 0)
+        out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world_size, "steps": done,
+               "warmup": args.warmup, "ms_per_step": elapsed / max(done, 1) * 1e3, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+               "impl": "reference",
+               "config": {"workload": desc, "bodies": sc.n, "dynamic_bodies": sc.dynamic, "iterations": 10,
+                          "dt": "1/60", "form": "CPU solver step"},
+               "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                                "sample": f"steps {args.warmup + 1}-{args.warmup + done}, all {threads} threads"},
+               "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
+        return
+
+    if world_size > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    out = run_gpu(args, rank, world_size)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world_size > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

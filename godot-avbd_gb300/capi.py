@@ -96,6 +96,19 @@ class Stats(C.Structure):
     ]
 
 
+class KernelTimes(C.Structure):
+    _fields_ = [
+        ("manifold_ms", C.c_double),
+        ("manifold_launches", C.c_int),
+        ("body_ms", C.c_double),
+        ("body_launches", C.c_int),
+        ("narrow_ms", C.c_double),
+        ("narrow_launches", C.c_int),
+        ("kernel_launches", C.c_int),
+        ("steps", C.c_int),
+    ]
+
+
 class AvbdError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"AVBD call failed ({code}): {message}")
@@ -292,6 +305,18 @@ class World:
         s = Stats()
         self.api.check(self.api.world_get_stats(self.handle, C.byref(s)))
         return s
+
+    def set_profiling(self, on=True):
+        fn = getattr(self.api.lib, self.api.prefix + "world_set_profiling")
+        fn.argtypes = [C.c_void_p, C.c_int]
+        self.api.check(fn(self.handle, 1 if on else 0))
+
+    def take_kernel_times(self):
+        fn = getattr(self.api.lib, self.api.prefix + "world_take_kernel_times")
+        fn.argtypes = [C.c_void_p, C.POINTER(KernelTimes)]
+        t = KernelTimes()
+        self.api.check(fn(self.handle, C.byref(t)))
+        return t
 
     def digest(self):
         out = C.c_uint64()

@@ -205,6 +205,22 @@ int avbdg_world_digest(avbdg_world *w, uint64_t *out) {
     return guarded(w, [out](avbdg::Engine &e) { return e.digest(0, *out); });
 }
 
+int avbdg_world_set_profiling(avbdg_world *w, int enabled) {
+    return guarded(w, [=](avbdg::Engine &e) {
+        e.setProfiling(enabled != 0);
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_world_take_kernel_times(avbdg_world *w, avbdg_kernel_times *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return guarded(w, [out](avbdg::Engine &e) {
+        e.takeKernelTimes(*out);
+        return AVBDG_OK;
+    });
+}
+
 int avbdg_world_dump_broadphase(avbdg_world *w, uint64_t *codes, int32_t *order, int capN, uint64_t *pairs,
                                 int capP, int *nB, int *nP) {
     return guarded(w, [=](avbdg::Engine &e) { return e.dumpBroadphase(codes, order, capN, pairs, capP, nB, nP); });

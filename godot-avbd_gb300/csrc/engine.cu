@@ -48,6 +48,10 @@ Engine::~Engine() {
     if (stream)
         cudaStreamSynchronize(stream);
     releaseAll();
+    if (ioHost)
+        cudaFreeHost(ioHost);
+    for (cudaEvent_t e : evPool)
+        cudaEventDestroy(e);
     for (auto &e : ev)
         if (e)
             cudaEventDestroy(e);
@@ -469,7 +473,9 @@ int Engine::broadPhase(const StepParams &sp) {
 // warmstartForces + selectUpdateBodies (solver_solve.cpp:31-105, 263-424).
 int Engine::warmstartAndSelect(const StepParams &sp) {
     launchForceInit(d, sp, nForces, stream);
+    beginSpan();
     launchManifoldInit(d, sp, stream);
+    endSpan(kNarrow);
     launchManifoldCompact(d, stream);
     launchAdjacency(d, nBodies, stream);
     adjValid = true;
@@ -505,12 +511,16 @@ void Engine::runSubstep(const StepParams &sp, int rounds) {
                     launchColourPass(d, c, bodyCap, sp, stream);
                 launchStamps(d, sp, true, stream);
             }
+            beginSpan();
             launchOverflowSolve(d, bodyCap, sp, inPlace, stream);
+            endSpan(kBody);
             if (!inPlace)
                 launchOverflowApply(d, bodyCap, sp, stream);
         }
         const bool nextNewton = it + 1 < newtonRounds;
+        beginSpan();
         launchDual(d, sp, nextNewton, newton ? 1.0f : P.stiffness_decay, stream);
+        endSpan(kManifold);
         launchForceDual(d, sp, nForces, stream);
     }
     launchFinishBodies(d, nBodies, sp, stream);
@@ -524,6 +534,12 @@ int Engine::finishStep() {
     if (rc)
         return rc;
     steps++;
+    launches = launchCount() - launchBase;
+    if (profiling) {
+        collectSpans();
+        acc.kernel_launches += launches;
+        acc.steps++;
+    }
     nForces = hostCtr[C_FORCES];
     if (hostCtr[C_ERRORS]) {
         const int e = hostCtr[C_ERRORS];
@@ -544,6 +560,7 @@ int Engine::step() {
     if (nBodies == 0)
         return AVBDG_OK;
     const StepParams sp = stepParams(P.dt);
+    launchBase = launchCount();
     cudaEventRecord(ev[0], stream);
     broadPhase(sp);
     cudaEventRecord(ev[1], stream);
@@ -565,6 +582,7 @@ int Engine::stepInterleaved(int substeps, int roundsPerSubstep) {
     if (nBodies == 0)
         return AVBDG_OK;
     const StepParams sp = stepParams(P.dt * static_cast<float>(substeps));
+    launchBase = launchCount();
     cudaEventRecord(ev[0], stream);
     broadPhase(sp);
     cudaEventRecord(ev[1], stream);
@@ -592,64 +610,130 @@ int Engine::sync() {
     return AVBDG_OK;
 }
 
+int Engine::ensureIo(int count) {
+    if (count <= ioCap)
+        return AVBDG_OK;
+    const int cap = std::max(count, 2 * ioCap);
+    if (ioHost)
+        cudaFreeHost(ioHost);
+    ioHost = nullptr;
+    if (cudaMallocHost(&ioHost, sizeof(float) * 13 * static_cast<size_t>(cap)) != cudaSuccess)
+        return fail(AVBDG_ERR_CAPACITY, "pinned staging allocation failed");
+    ioDev = dalloc<float>(13 * static_cast<size_t>(cap));
+    if (!ioDev)
+        return fail(AVBDG_ERR_CAPACITY, "device staging allocation failed");
+    ioCap = cap;
+    return AVBDG_OK;
+}
+
+// One device-side pack, one copy to pinned memory, one host copy per requested field.
 int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {
     if (w < 0 || w >= worlds() || first < 0 || count < 0 || first + count > wCount[w])
         return fail(AVBDG_ERR_INVALID, "bad range");
     if (count == 0)
         return AVBDG_OK;
-    const int g0 = wBase[w] + first;
-    std::vector<float4> buf(count);
-    const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
-    const auto fetch = [&](const float4 *src, float *dst, int k) {
-        if (!dst)
-            return;
-        cudaMemcpyAsync(buf.data(), src + g0, b4, cudaMemcpyDeviceToHost, stream);
-        cudaStreamSynchronize(stream);
-        for (int i = 0; i < count; i++) {
-            dst[k * i + 0] = buf[i].x;
-            dst[k * i + 1] = buf[i].y;
-            dst[k * i + 2] = buf[i].z;
-            if (k == 4)
-                dst[k * i + 3] = buf[i].w;
-        }
-    };
-    fetch(d.x, pos, 3);
-    fetch(d.q, quat, 4);
-    fetch(d.v, vel, 3);
-    fetch(d.w, angVel, 3);
+    int rc = ensureIo(count);
+    if (rc)
+        return rc;
+    launchPackState(d, wBase[w] + first, count, ioDev, stream);
+    cudaMemcpyAsync(ioHost, ioDev, sizeof(float) * 13 * static_cast<size_t>(count), cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("getState");
+    const size_t n = static_cast<size_t>(count);
+    if (pos)
+        std::memcpy(pos, ioHost, sizeof(float) * 3 * n);
+    if (quat)
+        std::memcpy(quat, ioHost + 3 * n, sizeof(float) * 4 * n);
+    if (vel)
+        std::memcpy(vel, ioHost + 7 * n, sizeof(float) * 3 * n);
+    if (angVel)
+        std::memcpy(angVel, ioHost + 10 * n, sizeof(float) * 3 * n);
     return cudaCheck("getState");
 }
 
+// Stage the given fields in pinned memory, one copy up, one device-side unpack (packed
+// companions such as the mass in x.w are kept).
 int Engine::setState(int w, int first, int count, const float *pos, const float *quat, const float *vel,
                      const float *angVel) {
     if (w < 0 || w >= worlds() || first < 0 || count < 0 || first + count > wCount[w])
         return fail(AVBDG_ERR_INVALID, "bad range");
     if (count == 0)
         return AVBDG_OK;
-    const int g0 = wBase[w] + first;
-    std::vector<float4> buf(count);
-    const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
-    // Each field keeps its packed companion (mass in x.w, gravity in v.w).
-    const auto put = [&](float4 *dst, const float *src, int k) {
-        if (!src)
-            return;
-        cudaMemcpyAsync(buf.data(), dst + g0, b4, cudaMemcpyDeviceToHost, stream);
-        cudaStreamSynchronize(stream);
-        for (int i = 0; i < count; i++) {
-            buf[i].x = src[k * i + 0];
-            buf[i].y = src[k * i + 1];
-            buf[i].z = src[k * i + 2];
-            if (k == 4)
-                buf[i].w = src[k * i + 3];
-        }
-        cudaMemcpyAsync(dst + g0, buf.data(), b4, cudaMemcpyHostToDevice, stream);
-        cudaStreamSynchronize(stream);
-    };
-    put(d.x, pos, 3);
-    put(d.q, quat, 4);
-    put(d.v, vel, 3);
-    put(d.w, angVel, 3);
+    int rc = ensureIo(count);
+    if (rc)
+        return rc;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) // the staging buffer may still be in use
+        return cudaCheck("setState");
+    const size_t n = static_cast<size_t>(count);
+    int mask = 0;
+    for (size_t i = 0; i < 3 * n; i++)
+        if ((pos && !std::isfinite(pos[i])) || (vel && !std::isfinite(vel[i])) ||
+            (angVel && !std::isfinite(angVel[i])))
+            return fail(AVBDG_ERR_NONFINITE, "non-finite body state");
+    if (pos) {
+        std::memcpy(ioHost, pos, sizeof(float) * 3 * n);
+        mask |= 1;
+    }
+    if (quat) {
+        std::memcpy(ioHost + 3 * n, quat, sizeof(float) * 4 * n);
+        mask |= 2;
+    }
+    if (vel) {
+        std::memcpy(ioHost + 7 * n, vel, sizeof(float) * 3 * n);
+        mask |= 4;
+    }
+    if (angVel) {
+        std::memcpy(ioHost + 10 * n, angVel, sizeof(float) * 3 * n);
+        mask |= 8;
+    }
+    cudaMemcpyAsync(ioDev, ioHost, sizeof(float) * 13 * n, cudaMemcpyHostToDevice, stream);
+    launchUnpackState(d, wBase[w] + first, count, ioDev, mask, stream);
     return cudaCheck("setState");
+}
+
+int Engine::beginSpan() {
+    if (!profiling)
+        return -1;
+    while (evPool.size() < evUsed + 2) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        evPool.push_back(e);
+    }
+    cudaEventRecord(evPool[evUsed], stream);
+    spans.push_back(Span{evPool[evUsed], evPool[evUsed + 1], -1});
+    evUsed += 2;
+    return static_cast<int>(spans.size()) - 1;
+}
+
+void Engine::endSpan(int kind) {
+    if (!profiling || spans.empty())
+        return;
+    spans.back().kind = kind;
+    cudaEventRecord(spans.back().b, stream);
+}
+
+void Engine::collectSpans() {
+    for (const Span &s : spans) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, s.a, s.b);
+        if (s.kind == kManifold) {
+            acc.manifold_ms += ms;
+            acc.manifold_launches++;
+        } else if (s.kind == kBody) {
+            acc.body_ms += ms;
+            acc.body_launches++;
+        } else if (s.kind == kNarrow) {
+            acc.narrow_ms += ms;
+            acc.narrow_launches++;
+        }
+    }
+    spans.clear();
+    evUsed = 0;
+}
+
+void Engine::takeKernelTimes(avbdg_kernel_times &out) {
+    out = acc;
+    acc = avbdg_kernel_times{};
 }
 
 int Engine::stats(avbdg_stats &out) {

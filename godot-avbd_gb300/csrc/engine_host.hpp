@@ -57,6 +57,9 @@ public:
                       float *penalty, float *lambda, int *count);
     int dumpColours(int cap, uint8_t *colour, int32_t *bodyId, int *count);
 
+    void setProfiling(bool on) { profiling = on; }
+    void takeKernelTimes(avbdg_kernel_times &out);
+
     int worlds() const { return static_cast<int>(wBase.size()); }
     int worldBodies(int w) const { return wCount[w]; }
     int bodies() const { return nBodies; }
@@ -82,6 +85,26 @@ private:
     cudaEvent_t ev[5] = {};
     bool timed = false;
     std::string err;
+    // Profiling: event pairs around the hot launches of the current step.
+    bool profiling = false;
+    enum KernelKind { kManifold = 0, kBody = 1, kNarrow = 2 };
+    struct Span {
+        cudaEvent_t a, b;
+        int kind;
+    };
+    std::vector<cudaEvent_t> evPool;
+    std::vector<Span> spans;
+    size_t evUsed = 0;
+    avbdg_kernel_times acc{};
+    int launchBase = 0;
+    int beginSpan();
+    void endSpan(int kind);
+    void collectSpans();
+    // Pinned host staging for state upload/download (13 floats per body).
+    float *ioHost = nullptr;
+    float *ioDev = nullptr;
+    int ioCap = 0;
+    int ensureIo(int count);
 
     int fail(int code, const std::string &msg);
     int cudaCheck(const char *where);

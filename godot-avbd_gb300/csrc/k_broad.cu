@@ -407,45 +407,45 @@ __global__ void candTotalKernel(Dev d) {
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
 void launchAabb(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
-    aabbKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+    ++launchCount(); aabbKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
 }
 
 void launchRebuildTree(const Dev &d, int n, int nWorlds, cudaStream_t s) {
-    boundsResetKernel<<<grid(nWorlds), kThreads, 0, s>>>(d.wBounds, nWorlds);
-    boundsKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
-    mortonResetKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-    mortonKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
+    ++launchCount(); boundsResetKernel<<<grid(nWorlds), kThreads, 0, s>>>(d.wBounds, nWorlds);
+    ++launchCount(); boundsKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
+    ++launchCount(); mortonResetKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); mortonKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
     radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, n, nullptr, 0, 63, d.radixScratch, s);
     if (nWorlds > 1) {
         int bits = 1;
         while ((1 << bits) < n + 1)
             bits++;
-        worldKeyKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+        ++launchCount(); worldKeyKernel<<<grid(n), kThreads, 0, s>>>(d, n);
         radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, n, nullptr, 0, bits, d.radixScratch, s);
     }
-    leafKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-    karrasKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); leafKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); karrasKernel<<<grid(n), kThreads, 0, s>>>(d, n);
 }
 
 void launchRefit(const Dev &d, int n, cudaStream_t s) {
     cudaMemsetAsync(d.nodeFlag, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
-    refitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); refitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
 }
 
 void launchPairs(const Dev &d, int n, cudaStream_t s) {
     cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
-    traverseKernel<false><<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); traverseKernel<false><<<grid(n), kThreads, 0, s>>>(d, n);
     scanExclusive(d.pairStart, d.pairStart, d.NB + 1, nullptr, d.ctr + C_TMP, d.scanScratch, s);
-    pairTotalKernel<<<1, 1, 0, s>>>(d);
-    traverseKernel<true><<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); pairTotalKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); traverseKernel<true><<<grid(n), kThreads, 0, s>>>(d, n);
     segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, n, nullptr, d.longList, d.ctr + C_LONG, s);
 }
 
 void launchFilterAcquire(const Dev &d, cudaStream_t s) {
-    filterKernel<<<grid(d.PP), kThreads, 0, s>>>(d);
+    ++launchCount(); filterKernel<<<grid(d.PP), kThreads, 0, s>>>(d);
     scanExclusive(d.pairValid, d.mActive, d.PP, d.ctr + C_PAIRS, d.ctr + C_TMP, d.scanScratch, s);
-    acquireKernel<<<grid(d.PP), kThreads, 0, s>>>(d, d.pairValid, d.mActive);
-    candTotalKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); acquireKernel<<<grid(d.PP), kThreads, 0, s>>>(d, d.pairValid, d.mActive);
+    ++launchCount(); candTotalKernel<<<1, 1, 0, s>>>(d);
 }
 
 } // namespace avbdg

@@ -352,32 +352,32 @@ static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 void launchAdjacency(const Dev &d, int nBodies, cudaStream_t s) {
     cudaMemsetAsync(d.adjStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.adjFill, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
-    adjCountKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); adjCountKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
     scanExclusive(d.adjStart, d.adjStart, nBodies + 1, nullptr, d.ctr + C_ADJ, d.scanScratch, s);
-    adjTotalKernel<<<1, 1, 0, s>>>(d);
-    adjFillKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); adjTotalKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); adjFillKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
     segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, nBodies, nullptr, d.longList, d.ctr + C_LONG, s);
 }
 
 void launchManifoldInit(const Dev &d, const StepParams &p, cudaStream_t s) {
-    manifoldInitKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+    ++launchCount(); manifoldInitKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
 }
 
 void launchManifoldCompact(const Dev &d, cudaStream_t s) {
     scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_CAND, d.ctr + C_LIVE, d.scanScratch, s);
-    manifoldCompactKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
+    ++launchCount(); manifoldCompactKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
 }
 
 void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s) {
-    rebaseKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+    ++launchCount(); rebaseKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
 }
 
 void launchForceInit(const Dev &d, const StepParams &p, int nForces, cudaStream_t s) {
     if (nForces <= 0)
         return;
     cudaMemsetAsync(d.ctr + C_TMP, 0, sizeof(int), s);
-    forceInitKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
-    forceCompactKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); forceInitKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
+    ++launchCount(); forceCompactKernel<<<1, 1, 0, s>>>(d);
 }
 
 } // namespace avbdg

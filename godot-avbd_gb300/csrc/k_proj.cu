@@ -392,7 +392,7 @@ int brakeGridBlocks() {
 void launchProjActive(const Dev &d, int nWorlds, cudaStream_t s) {
     cudaMemsetAsync(d.wActive, 0, sizeof(int) * static_cast<size_t>(nWorlds), s);
     cudaMemsetAsync(d.ctr + C_SPEC, 0, sizeof(int), s);
-    projActiveKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); projActiveKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
 }
 
 void launchBrake(const Dev &d, int, float window, cudaStream_t s) {
@@ -401,17 +401,18 @@ void launchBrake(const Dev &d, int, float window, cudaStream_t s) {
     Dev dd = d;
     float win = window;
     void *args[] = {&dd, &win, &bar};
+    ++launchCount();
     cudaLaunchCooperativeKernel(reinterpret_cast<void *>(brakeKernel), dim3(brakeGridBlocks()), dim3(kBrakeThreads),
                                 args, 0, s);
 }
 
 void launchProjection(const Dev &d, int nBodies, int nWorlds, const StepParams &p, cudaStream_t s) {
-    projStartKernel<<<grid(nWorlds), kThreads, 0, s>>>(d, nWorlds);
+    ++launchCount(); projStartKernel<<<grid(nWorlds), kThreads, 0, s>>>(d, nWorlds);
     const float tol = smax(p.projSlop * 0.01f, 1.0e-6f);
     for (int it = 0; it < p.projIters; it++) {
-        projManifoldKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
-        projBodyKernel<<<grid(nBodies), kThreads, 0, s>>>(d, nBodies, p);
-        projCheckKernel<<<grid(nWorlds), kThreads, 0, s>>>(d, nWorlds, tol);
+        ++launchCount(); projManifoldKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+        ++launchCount(); projBodyKernel<<<grid(nBodies), kThreads, 0, s>>>(d, nBodies, p);
+        ++launchCount(); projCheckKernel<<<grid(nWorlds), kThreads, 0, s>>>(d, nWorlds, tol);
     }
 }
 

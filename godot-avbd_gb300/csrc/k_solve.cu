@@ -854,8 +854,8 @@ __global__ void colourListKernel(Dev d, int n, int contactOnlyOverflow) {
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
 void launchContactOnly(const Dev &d, int n, cudaStream_t s) {
-    contactOnlyInitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-    contactOnlyMarkKernel<<<grid(d.FF), kThreads, 0, s>>>(d);
+    ++launchCount(); contactOnlyInitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); contactOnlyMarkKernel<<<grid(d.FF), kThreads, 0, s>>>(d);
 }
 
 void launchColour(const Dev &d, int n, bool needGreedy, cudaStream_t s) {
@@ -865,7 +865,7 @@ void launchColour(const Dev &d, int n, bool needGreedy, cudaStream_t s) {
     for (int batch = 0; batch < 4096; batch++) {
         for (int r = 0; r < 16; r++) {
             cudaMemsetAsync(d.ctr + C_UNCOLOURED, 0, sizeof(int), s);
-            colourRoundKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+            ++launchCount(); colourRoundKernel<<<grid(n), kThreads, 0, s>>>(d, n);
         }
         int waiting = 0;
         cudaMemcpyAsync(&waiting, d.ctr + C_UNCOLOURED, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -877,42 +877,42 @@ void launchColour(const Dev &d, int n, bool needGreedy, cudaStream_t s) {
 
 void launchColourLists(const Dev &d, int n, int contactOnlyOverflow, cudaStream_t s) {
     cudaMemsetAsync(d.colourCount, 0, sizeof(int) * (kMaxColours + 1), s);
-    colourListKernel<<<grid(n), kThreads, 0, s>>>(d, n, contactOnlyOverflow);
+    ++launchCount(); colourListKernel<<<grid(n), kThreads, 0, s>>>(d, n, contactOnlyOverflow);
 }
 
 void launchWarmstartBodies(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
-    warmstartKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+    ++launchCount(); warmstartKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
 }
 
 void launchFinishBodies(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
-    finishKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+    ++launchCount(); finishKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
 }
 
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s) {
-    stampsKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
+    ++launchCount(); stampsKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
 }
 
 void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &p, cudaStream_t s) {
-    colourPassKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
+    ++launchCount(); colourPassKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
 }
 
 void launchOverflowSolve(const Dev &d, int capacity, const StepParams &p, bool inPlace, cudaStream_t s) {
-    overflowSolveKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p,
+    ++launchCount(); overflowSolveKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p,
                                                                                                     inPlace ? 1 : 0);
 }
 
 void launchOverflowApply(const Dev &d, int capacity, const StepParams &p, cudaStream_t s) {
-    overflowApplyKernel<<<grid(capacity), kThreads, 0, s>>>(d, p);
+    ++launchCount(); overflowApplyKernel<<<grid(capacity), kThreads, 0, s>>>(d, p);
 }
 
 void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s) {
-    dualKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, stamps ? 1 : 0, decay);
+    ++launchCount(); dualKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, stamps ? 1 : 0, decay);
 }
 
 void launchForceDual(const Dev &d, const StepParams &p, int nForces, cudaStream_t s) {
     if (nForces <= 0)
         return;
-    forceDualKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
+    ++launchCount(); forceDualKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
 }
 
 } // namespace avbdg

@@ -52,4 +52,9 @@ void launchProjection(const Dev &d, int nBodies, int nWorlds, const StepParams &
 
 int brakeGridBlocks();
 
+// ---- host state exchange (k_io.cu) ----
+// Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).
+void launchPackState(const Dev &d, int first, int count, float *buf, cudaStream_t s);
+void launchUnpackState(const Dev &d, int first, int count, const float *buf, int mask, cudaStream_t s);
+
 } // namespace avbdg

@@ -319,9 +319,9 @@ void scanExclusive(const int *in, int *out, int capacity, const int *d_n, int *d
                    cudaStream_t stream) {
     const int blocks = divUp(capacity > 0 ? capacity : 1, kScanTile);
     int *blockSums = static_cast<int *>(scratch);
-    scanReduceKernel<<<blocks, kScanThreads, 0, stream>>>(in, capacity, d_n, blockSums);
-    scanTopKernel<<<1, kTopThreads, 0, stream>>>(blockSums, blocks, d_total);
-    scanDownKernel<<<blocks, kScanThreads, 0, stream>>>(in, out, capacity, d_n, blockSums);
+    ++launchCount(); scanReduceKernel<<<blocks, kScanThreads, 0, stream>>>(in, capacity, d_n, blockSums);
+    ++launchCount(); scanTopKernel<<<1, kTopThreads, 0, stream>>>(blockSums, blocks, d_total);
+    ++launchCount(); scanDownKernel<<<blocks, kScanThreads, 0, stream>>>(in, out, capacity, d_n, blockSums);
 }
 
 void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_t *valuesAlt, int capacity,
@@ -336,9 +336,9 @@ void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_
     for (int bit = beginBit; bit < endBit; bit += 8) {
         const int bits = endBit - bit < 8 ? endBit - bit : 8;
         const uint32_t mask = (1u << bits) - 1u;
-        radixHistKernel<<<blocks, kRadixThreads, 0, stream>>>(kin, capacity, d_n, bit, mask, blocks, hist);
+        ++launchCount(); radixHistKernel<<<blocks, kRadixThreads, 0, stream>>>(kin, capacity, d_n, bit, mask, blocks, hist);
         scanExclusive(hist, hist, histN, nullptr, nullptr, scanScratch, stream);
-        radixScatterKernel<<<blocks, kRadixThreads, 0, stream>>>(kin, vin, kout, vout, capacity, d_n, bit, mask,
+        ++launchCount(); radixScatterKernel<<<blocks, kRadixThreads, 0, stream>>>(kin, vin, kout, vout, capacity, d_n, bit, mask,
                                                                  blocks, hist);
         uint64_t *tk = kin;
         kin = kout;
@@ -350,9 +350,9 @@ void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_
     }
     if (passes & 1) {
         const int grid = divUp(capacity > 0 ? capacity : 1, 256) < 1184 ? divUp(capacity > 0 ? capacity : 1, 256) : 1184;
-        copyKernel<uint64_t><<<grid, 256, 0, stream>>>(kin, keys, capacity, d_n);
+        ++launchCount(); copyKernel<uint64_t><<<grid, 256, 0, stream>>>(kin, keys, capacity, d_n);
         if (values)
-            copyKernel<uint32_t><<<grid, 256, 0, stream>>>(vin, values, capacity, d_n);
+            ++launchCount(); copyKernel<uint32_t><<<grid, 256, 0, stream>>>(vin, values, capacity, d_n);
     }
 }
 
@@ -361,13 +361,13 @@ static void segmentedSort(T *data, const int *start, int segCapacity, const int 
                           int *longCount, T *tmp, cudaStream_t stream) {
     cudaMemsetAsync(longCount, 0, sizeof(int), stream);
     const int grid = divUp(segCapacity > 0 ? segCapacity : 1, 256);
-    segSmallKernel<T><<<grid < 4096 ? grid : 4096, 256, 0, stream>>>(data, start, segCapacity, d_segments, longList,
+    ++launchCount(); segSmallKernel<T><<<grid < 4096 ? grid : 4096, 256, 0, stream>>>(data, start, segCapacity, d_segments, longList,
                                                                    longCount);
     const size_t smem = kMidSegCap * sizeof(T);
-    segMidKernel<T><<<152, kMidSegThreads, smem, stream>>>(data, start, longList, longCount);
+    ++launchCount(); segMidKernel<T><<<152, kMidSegThreads, smem, stream>>>(data, start, longList, longCount);
     if (tmp) {
-        segBigCopyKernel<T><<<kBigBlocks, 256, 0, stream>>>(data, tmp, start, longList, longCount);
-        segBigRankKernel<T><<<kBigBlocks, 256, 0, stream>>>(data, tmp, start, longList, longCount);
+        ++launchCount(); segBigCopyKernel<T><<<kBigBlocks, 256, 0, stream>>>(data, tmp, start, longList, longCount);
+        ++launchCount(); segBigRankKernel<T><<<kBigBlocks, 256, 0, stream>>>(data, tmp, start, longList, longCount);
     }
 }
 

@@ -188,6 +188,24 @@ int avbdg_world_get_stats(avbdg_world *world, avbdg_stats *out);
  * order: the reference test suite's state_digest (test/core_test.cpp:133-149). */
 int avbdg_world_digest(avbdg_world *world, uint64_t *out);
 
+/* Device time of the hot kernels, accumulated over steps while profiling is on (CUDA events on
+ * the world's stream around each launch). Diagnostics beside the reference's PhaseTimes
+ * (src/avbd/solver.h:251-275), which time the same phases on the CPU. */
+typedef struct avbdg_kernel_times {
+    double manifold_ms;   /* dual + stamp pass over manifolds (one launch per round) */
+    int manifold_launches;
+    double body_ms;       /* block-Jacobi body solve (one launch per Newton round) */
+    int body_launches;
+    double narrow_ms;     /* narrow phase + warm start (one launch per step) */
+    int narrow_launches;
+    int kernel_launches;  /* every kernel this library launched while profiling */
+    int steps;
+} avbdg_kernel_times;
+
+int avbdg_world_set_profiling(avbdg_world *world, int enabled);
+/* Read and reset the accumulated times. */
+int avbdg_world_take_kernel_times(avbdg_world *world, avbdg_kernel_times *out);
+
 /* ------------------------------------------------------------------------------------ */
 /* Parity dumps (the integer stages, for bit-exact comparison with the reference)        */
 /* ------------------------------------------------------------------------------------ */

@@ -9,6 +9,9 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace oracle {
 
@@ -1282,11 +1285,18 @@ int World::warmstartForces() {
         if (jointInitialize(f))
             kept.push_back(f);
     forces.swap(kept);
+    // Independent per manifold (the reference dispatches this loop to its pool too); the stable
+    // compaction stays serial.
+    const int nm = static_cast<int>(live.size());
+    std::vector<uint8_t> active(nm);
+#pragma omp parallel for schedule(dynamic, 64) if (parallel())
+    for (int i = 0; i < nm; i++)
+        active[i] = frozen(live[i]) || manifoldInitialize(live[i]);
     std::vector<Manifold> keptM;
     keptM.reserve(live.size());
-    for (Manifold &m : live)
-        if (frozen(m) || manifoldInitialize(m))
-            keptM.push_back(m);
+    for (int i = 0; i < nm; i++)
+        if (active[i])
+            keptM.push_back(live[i]);
     live.swap(keptM);
     buildAdjacency();
     return static_cast<int>(forces.size());
@@ -1419,6 +1429,8 @@ void World::iterate(int rounds, int forceCount) {
     for (int it = 0; it < rounds; it++) {
         const bool newton = it < newtonRounds;
         for (int c = 0; newton && c < colourCount; c++) {
+            // Bodies of one colour share no force: independent.
+#pragma omp parallel for schedule(dynamic, 16) if (parallel())
             for (int k = colourBegins[c]; k < colourBegins[c + 1]; k++) {
                 const int id = updateOrder[colourOrder[k]];
                 Body &body = bodies[id];
@@ -1439,7 +1451,10 @@ void World::iterate(int rounds, int forceCount) {
         }
         const int ovf = newton ? overflowCount : 0;
         if (ovf > 0) {
-            for (Manifold &m : live) {
+            const int nm = static_cast<int>(live.size());
+#pragma omp parallel for schedule(dynamic, 64) if (parallel())
+            for (int mi = 0; mi < nm; mi++) {
+                Manifold &m = live[mi];
                 const Body &A = bodies[m.a];
                 const Body &B = bodies[m.b];
                 const bool aIn = A.inUpdate && colour[A.updateIndex] == kOverflowColour;
@@ -1448,6 +1463,7 @@ void World::iterate(int rounds, int forceCount) {
                     continue;
                 preCompute(m);
             }
+#pragma omp parallel for schedule(dynamic, 16) if (parallel())
             for (int k = 0; k < ovf; k++) {
                 const int i = overflowOrder[k];
                 const int id = updateOrder[i];
@@ -1462,6 +1478,7 @@ void World::iterate(int rounds, int forceCount) {
                 }
                 solveDelta(blk, dLin[i], dAng[i]);
             }
+#pragma omp parallel for schedule(static) if (parallel())
             for (int k = 0; k < ovf; k++) {
                 const int i = overflowOrder[k];
                 Body &body = bodies[updateOrder[i]];
@@ -1470,13 +1487,17 @@ void World::iterate(int rounds, int forceCount) {
             }
         }
         const float decay = newton ? 1.0f : P.stiffness_decay;
-        for (Manifold &m : live) {
+        const int nm = static_cast<int>(live.size());
+#pragma omp parallel for schedule(dynamic, 64) if (parallel())
+        for (int mi = 0; mi < nm; mi++) {
+            Manifold &m = live[mi];
             if (frozen(m))
                 continue;
             if (decay < 1.0f)
                 decayPenalty(m, decay);
             manifoldUpdateDual(m);
         }
+#pragma omp parallel for schedule(static) if (parallel())
         for (int f = 0; f < forceCount; f++)
             jointUpdateDual(forces[f]);
         (void)alpha;
@@ -1484,10 +1505,13 @@ void World::iterate(int rounds, int forceCount) {
 }
 
 void World::runSubstep(int forceCount, int rounds) {
-    for (int li = 0; li < count(); li++)
+    const int n = count();
+#pragma omp parallel for schedule(static) if (parallel())
+    for (int li = 0; li < n; li++)
         warmstartBody(bodies[idAt(li)]);
     iterate(rounds, forceCount);
-    for (int li = 0; li < count(); li++)
+#pragma omp parallel for schedule(static) if (parallel())
+    for (int li = 0; li < n; li++)
         finishBody(bodies[idAt(li)]);
 }
 
@@ -1666,8 +1690,18 @@ void World::projectContacts(bool projectPositions, float brakeWindow) {
     }
 }
 
+static void setThreads(int threads) {
+#ifdef _OPENMP
+    if (threads > 1)
+        omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+}
+
 // Solver::step (solver_step.cpp:44-75).
 void World::step() {
+    setThreads(P.threads);
     collisionDt = P.dt;
     broadPhase();
     const int forceCount = warmstartForces();

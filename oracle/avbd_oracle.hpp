@@ -112,6 +112,10 @@ public:
     void stepInterleaved(int substeps, int rounds);
     uint64_t digest() const;
 
+    // Independent per-body / per-manifold loops use all host threads unless `threads` is 1 (the
+    // reference's Solver::threads convention); results do not depend on the thread count.
+    bool parallel() const { return P.threads != 1; }
+
     int count() const { return static_cast<int>(bodies.size()); }
     int listIndex(int id) const { return count() - 1 - id; }
     int idAt(int listIdx) const { return count() - 1 - listIdx; }
