@@ -24,7 +24,7 @@ NVCC_FLAGS = ARCH + [
     "-I" + os.path.join(ROOT, "include"),
 ]
 SOURCES = ["prims.cu", "k_broad.cu", "k_manifold.cu", "k_solve.cu", "k_proj.cu", "k_io.cu", "engine.cu",
-           "capi.cu"]
+           "capi.cu", "sortkeys.cu"]
 
 
 def nvcc():

@@ -46,6 +46,11 @@ int guarded(avbdg_world *w, F &&fn) {
 
 } // namespace
 
+namespace avbdg {
+// Error channel shared with the entry points defined in other translation units.
+void setLastError(const std::string &msg) { g_lastError = msg; }
+} // namespace avbdg
+
 extern "C" {
 
 const char *avbdg_last_error(void) { return g_lastError.c_str(); }

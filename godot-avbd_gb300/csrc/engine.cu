@@ -132,6 +132,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
     n.nodeParent = dalloc<int>(nb);
     n.leafParent = dalloc<int>(nb);
     n.nodeFlag = dalloc<int>(nb);
+    n.nodeMaxLp = dalloc<int>(nb);
     n.nodeMin = dalloc<float4>(nb);
     n.nodeMax = dalloc<float4>(nb);
     n.pairStart = dalloc<int>(static_cast<size_t>(nb) + 1);
@@ -232,6 +233,9 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         cudaStreamSynchronize(stream);
         for (void *p : oldAllocs)
             cudaFree(p);
+        // The device staging buffer was one of the freed allocations.
+        ioDev = nullptr;
+        ioCap = 0;
         treeValid = false;
         adjValid = false;
     }
@@ -482,6 +486,13 @@ int Engine::warmstartAndSelect(const StepParams &sp) {
     launchContactOnly(d, nBodies, stream);
     launchColour(d, nBodies, needGreedy(), stream);
     launchColourLists(d, nBodies, P.contact_only_overflow, stream);
+    std::fill(std::begin(colourSizes), std::end(colourSizes), 0);
+    if (needGreedy()) {
+        // The colouring already waited on the host; fetch the colour sizes so the round loop
+        // launches only the colours in use.
+        cudaMemcpyAsync(colourSizes, d.colourCount, sizeof(colourSizes), cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+    }
     return AVBDG_OK;
 }
 
@@ -508,7 +519,8 @@ void Engine::runSubstep(const StepParams &sp, int rounds) {
         if (newton) {
             if (colours) {
                 for (int c = 0; c < kMaxColours; c++)
-                    launchColourPass(d, c, bodyCap, sp, stream);
+                    if (colourSizes[c] > 0)
+                        launchColourPass(d, c, colourSizes[c], sp, stream);
                 launchStamps(d, sp, true, stream);
             }
             beginSpan();

@@ -94,6 +94,7 @@ struct Dev {
     uint32_t *sortV, *sortVAlt;
     int *leafBody;          // sorted position -> body
     int *nodeL, *nodeR, *nodeParent, *leafParent, *nodeFlag;
+    int *nodeMaxLp;         // largest list position in the subtree (prunes the pair walk)
     float4 *nodeMin, *nodeMax;
     // pairs
     int *pairStart;         // per list position (+1)

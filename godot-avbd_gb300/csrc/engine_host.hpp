@@ -82,6 +82,7 @@ private:
     int steps = 0;
     int launches = 0;
     int hostCtr[C_COUNT] = {};
+    int colourSizes[kMaxColours + 1] = {};
     cudaEvent_t ev[5] = {};
     bool timed = false;
     std::string err;

@@ -250,10 +250,14 @@ __global__ void refitKernel(Dev d, int n) {
             return;
         __threadfence();
         float4 a0, a1, b0, b1;
-        childBounds(d, d.nodeL[node], a0, a1);
-        childBounds(d, d.nodeR[node], b0, b1);
+        const int l = d.nodeL[node], r = d.nodeR[node];
+        childBounds(d, l, a0, a1);
+        childBounds(d, r, b0, b1);
         __stcg(&d.nodeMin[node], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f));
         __stcg(&d.nodeMax[node], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f));
+        const int ml = (l & kLeafBit) ? static_cast<int>(d.sortV[l & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[l]);
+        const int mr = (r & kLeafBit) ? static_cast<int>(d.sortV[r & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[r]);
+        __stcg(&d.nodeMaxLp[node], ml > mr ? ml : mr);
         node = d.nodeParent[node];
     }
 }
@@ -305,6 +309,8 @@ __global__ void traverseKernel(Dev d, int n) {
                         found++;
                     }
                 } else {
+                    if (d.nodeMaxLp[c] <= lpA)
+                        continue; // every leaf below was emitted by a partner with a smaller position
                     const float4 mn = d.nodeMin[c], mx = d.nodeMax[c];
                     if (overlapClosed(aMin, aMax, f3{mn.x, mn.y, mn.z}, f3{mx.x, mx.y, mx.z})) {
                         if (sp < kStack)

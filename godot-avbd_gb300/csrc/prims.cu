@@ -351,8 +351,10 @@ void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_
     if (passes & 1) {
         const int grid = divUp(capacity > 0 ? capacity : 1, 256) < 1184 ? divUp(capacity > 0 ? capacity : 1, 256) : 1184;
         ++launchCount(); copyKernel<uint64_t><<<grid, 256, 0, stream>>>(kin, keys, capacity, d_n);
-        if (values)
-            ++launchCount(); copyKernel<uint32_t><<<grid, 256, 0, stream>>>(vin, values, capacity, d_n);
+        if (values) {
+            ++launchCount();
+            copyKernel<uint32_t><<<grid, 256, 0, stream>>>(vin, values, capacity, d_n);
+        }
     }
 }
 

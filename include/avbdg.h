@@ -229,6 +229,18 @@ int avbdg_world_dump_manifolds(avbdg_world *world, int cap, int32_t *body_a, int
 int avbdg_world_dump_colours(avbdg_world *world, int cap, uint8_t *colour, int32_t *body_id,
                              int *count);
 
+/* ------------------------------------------------------------------------------------ */
+/* Standalone kernels                                                                   */
+/* ------------------------------------------------------------------------------------ */
+
+/* Sort `count` 64-bit keys held in device memory ascending and drop repeated keys, in place:
+ * the reference's candidate-pair pass radix_std::sort_with_buffer + std::unique
+ * (src/radixsort.hpp:24-83, src/avbd/solver_broadphase.cpp:136-137). Keys must be below
+ * 2^key_bits (1..64). On return d_keys[0 .. *unique_count) holds the distinct keys in order.
+ * Runs on `stream` (a cudaStream_t; NULL = the default stream) and waits for it. Scratch is
+ * allocated with cudaMalloc for the duration of the call. */
+int avbdg_sort_unique_keys(uint64_t *d_keys, int count, int key_bits, int *unique_count, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

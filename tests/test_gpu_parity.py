@@ -147,6 +147,36 @@ def test_gpu_edge_cases(pkg, gpu, oracle):
     assert e.value.code == capi.ERR_UNSUPPORTED
 
 
+def test_gpu_store_growth(pkg, gpu, oracle):
+    """A world created with the smallest store grows while bodies arrive in chunks and while its
+    pairs and manifolds outgrow their buffers; results stay identical to the oracle."""
+    capi, scenes = pkg.capi, pkg.scenes
+    sc = scenes.pyramid420()
+    p = gpu.default_params()
+    scenes.apply_params(p, sc.params)
+    a = capi.World(gpu, p, max_bodies=1, max_forces=1)
+    q = oracle.default_params()
+    scenes.apply_params(q, sc.params)
+    b = capi.World(oracle, q)
+    for lo in range(0, sc.n, 50):
+        hi = min(sc.n, lo + 50)
+        d = capi.make_body_descs(sc.size[lo:hi], sc.density[lo:hi], sc.friction[lo:hi], sc.position[lo:hi],
+                                 sc.orientation[lo:hi], sc.velocity[lo:hi])
+        a.add_bodies(d)
+        b.add_bodies(d)
+        a.step()
+        b.step()
+        pa, qa, va, wa = a.state()
+        a.set_state(velocity=va)
+        for x, y in zip(a.state(), b.state()):
+            assert np.array_equal(x, y)
+    for _ in range(20):
+        a.step()
+        b.step()
+    for x, y in zip(a.state(), b.state()):
+        assert np.array_equal(x, y)
+
+
 def test_gpu_host_state_edits(pkg, gpu, oracle):
     """Velocity edits between steps (the server integrates host forces this way)."""
     scenes = pkg.scenes
