@@ -3,6 +3,7 @@
 // src/avbd/solver_broadphase.cpp:136-137), as a GPU service over a caller-owned key buffer.
 
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "avbdg.h"
@@ -67,11 +68,89 @@ int checkArgs(uint64_t *keys, int n, int bits, int *uniqueCount) {
     return AVBDG_OK;
 }
 
+// ---- Fixed scratch for callers that cannot allocate ----------------------------------------
+//
+// Some callers of this library run where device allocation is not available to them: a host
+// that hands its physics thread a fixed memory budget and forbids further device allocations,
+// a plugin loaded into an engine whose allocator owns all device memory, or code running while
+// another component holds a stream in capture (where a cudaMalloc would break the capture).
+// They own their key buffer but cannot obtain scratch. For them the sort's scratch is this
+// one array in the library's own device image: it exists on every GPU that loads the library
+// and stays there until the process exits.
+constexpr int kStaticMaxKeys = 1 << 18; // 262,144 keys per call
+constexpr size_t kStaticScratchBytes = size_t(9) << 19; // 4.5 MiB
+static __device__ __align__(256) unsigned char g_staticSortScratch[kStaticScratchBytes];
+
+// Device address of g_staticSortScratch, per device. In host code the array's name is only a
+// host-side stand-in, so the address is looked up once per device, with that device current.
+constexpr int kMaxDevices = 64;
+static void *g_staticScratchAddr[kMaxDevices] = {};
+static std::mutex g_staticScratchMutex;
+
+int staticScratchAddress(void **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return sortFail(AVBDG_ERR_CUDA, "no current CUDA device for the static sort scratch");
+    std::lock_guard<std::mutex> lock(g_staticScratchMutex);
+    if (!g_staticScratchAddr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_staticSortScratch);
+        if (e != cudaSuccess || !p)
+            return sortFail(AVBDG_ERR_CUDA, std::string("cudaGetSymbolAddress of the static sort scratch: ") +
+                                                cudaGetErrorString(e));
+        g_staticScratchAddr[dev] = p;
+    }
+    *out = g_staticScratchAddr[dev];
+    return AVBDG_OK;
+}
+
 } // namespace
 
 } // namespace avbdg
 
 extern "C" {
+
+int avbdg_sort_unique_keys_static(uint64_t *d_keys, int count, int key_bits, int *unique_count, void *stream) {
+    using namespace avbdg;
+    int rc = checkArgs(d_keys, count, key_bits, unique_count);
+    if (rc)
+        return rc;
+    if (count > kStaticMaxKeys)
+        return sortFail(AVBDG_ERR_CAPACITY, "avbdg_sort_unique_keys_static takes at most 262144 keys per call; "
+                                            "use avbdg_sort_unique_keys for larger inputs");
+    if (count == 0) {
+        *unique_count = 0;
+        return AVBDG_OK;
+    }
+    const size_t n = static_cast<size_t>(count);
+    const size_t offAlt = 0;
+    const size_t offRadix = (offAlt + n * sizeof(uint64_t) + 255) & ~size_t(255);
+    const size_t offFlags = (offRadix + radixScratchBytes(count) + 255) & ~size_t(255);
+    const size_t offRanks = (offFlags + n * sizeof(int) + 255) & ~size_t(255);
+    const size_t offScan = (offRanks + n * sizeof(int) + 255) & ~size_t(255);
+    const size_t offCount = (offScan + scanScratchBytes(count) + 255) & ~size_t(255);
+    if (offCount + 256 > kStaticScratchBytes)
+        return sortFail(AVBDG_ERR_CAPACITY, "static sort scratch too small for this count");
+    void *addr = nullptr;
+    rc = staticScratchAddress(&addr);
+    if (rc)
+        return rc;
+    char *base = static_cast<char *>(addr);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SortScratch s{reinterpret_cast<uint64_t *>(base + offAlt), base + offRadix, reinterpret_cast<int *>(base + offFlags),
+                  reinterpret_cast<int *>(base + offRanks), base + offScan, reinterpret_cast<int *>(base + offCount)};
+    // The array keeps whatever the previous call left; the only word read before this call
+    // writes it is the result count, so it is cleared first.
+    cudaMemsetAsync(s.count, 0, sizeof(int), st);
+    enqueueSortUnique(d_keys, count, key_bits, s, st);
+    int host = 0;
+    cudaMemcpyAsync(&host, s.count, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return sortFail(AVBDG_ERR_CUDA, std::string("static sort: ") + cudaGetErrorString(e));
+    *unique_count = host;
+    return AVBDG_OK;
+}
 
 int avbdg_sort_unique_keys(uint64_t *d_keys, int count, int key_bits, int *unique_count, void *stream) {
     using namespace avbdg;

@@ -241,6 +241,18 @@ int avbdg_world_dump_colours(avbdg_world *world, int cap, uint8_t *colour, int32
  * allocated with cudaMalloc for the duration of the call. */
 int avbdg_sort_unique_keys(uint64_t *d_keys, int count, int key_bits, int *unique_count, void *stream);
 
+/* The same sort + unique for callers that cannot allocate device memory: a host that gives its
+ * physics code a fixed device budget and forbids new allocations, a plugin inside an engine whose
+ * allocator owns the device, or code that runs while a stream is being captured (a cudaMalloc
+ * there would break the capture). It allocates nothing: its scratch is a fixed 4.5 MiB array
+ * compiled into this library, present on every GPU that loads the library until the process
+ * exits. At most 262,144 keys per call; larger counts return AVBDG_ERR_CAPACITY.
+ * The first call on each device looks up the array's device address (with that device current);
+ * make that first call before any stream capture begins. All calls share the one array: calls
+ * whose GPU work overlaps (e.g. on two streams at once) race and corrupt each other's results.
+ * No counterpart in the reference (it has no GPU and no allocation constraint). */
+int avbdg_sort_unique_keys_static(uint64_t *d_keys, int count, int key_bits, int *unique_count, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
