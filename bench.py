@@ -264,14 +264,106 @@ def run_gpu(args, rank, world_size):
     return out
 
 
+BATCH_DESC = ("4096 independent worlds, dynamic body counts log-uniform in 8-512 (each a 3-20 row pyramid wall "
+              "or a random box pile with log-uniform sizes/densities, own static ground), dt 1/60, 10 iterations")
+
+
+def run_batch(args, rank, world_size):
+    """Batched form: all worlds in one device store, one launch per kernel per step; compared
+    with the plain per-scene step (one world object per scene, stepped one after another) on a
+    bounded sample of the same worlds."""
+    import numpy as np
+    import torch
+
+    pkg = entry.load_package()
+    capi, scenes = pkg.capi, pkg.scenes
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    worlds = scenes.batch(worlds=args.worlds, seed=7 + rank)
+    p = pkg.gpu_api().default_params()
+    scenes.apply_params(p, scenes.BENCH_PARAMS)
+    batch = capi.Batch(pkg.load_library(), p, max_worlds=len(worlds), max_bodies=sum(w.n for w in worlds),
+                       max_forces=max(1, sum(len(w.joints) for w in worlds)))
+    for w in worlds:
+        batch.add_scene(w)
+    dynamic = sum(w.dynamic for w in worlds)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    batch.step(args.warmup)
+    if world_size > 1:
+        torch.distributed.barrier()
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            batch.step()
+            step_ms.append(batch.stats().total_ms)
+    total_ms = float(sum(step_ms))
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = dynamic * args.steps * world_size / (total_ms / 1e3)
+    st = batch.stats()
+
+    # End to end: every step uploads all bodies' state and reads it back through the C ABI.
+    states = [batch.state(i) for i in range(len(worlds))]
+    torch.cuda.synchronize()
+    e2e_steps = max(1, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for i, (pp, qq, vv, ww) in enumerate(states):
+            batch.fn["batch_set_body_state"](batch.handle, i, 0, worlds[i].n, capi._ptr(pp, ctypes.c_float),
+                                             capi._ptr(qq, ctypes.c_float), capi._ptr(vv, ctypes.c_float),
+                                             capi._ptr(ww, ctypes.c_float))
+        batch.step()
+        states = [batch.state(i) for i in range(len(worlds))]
+    e2e_s = time.perf_counter() - t0
+    nbytes = 13 * 4 * sum(w.n for w in worlds)
+    e2e = {"value": dynamic * e2e_steps * world_size / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes, "note": "per-world state calls (4096 uploads + 4096 reads per step)"}
+
+    # Plain per-scene GPU step on a sample of the worlds, each its own avbdg_world.
+    rng = np.random.default_rng(1)
+    sample = [worlds[i] for i in rng.choice(len(worlds), size=min(args.plain_sample, len(worlds)), replace=False)]
+    gpu = pkg.gpu_api()
+    plain_body_steps, plain_s = 0, 0.0
+    for sc in sample:
+        w = scenes.instantiate(gpu, sc)
+        w.step(args.warmup)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        w.step(args.plain_steps)
+        w.sync()
+        plain_s += time.perf_counter() - t
+        plain_body_steps += sc.dynamic * args.plain_steps
+        w.close()
+    plain_value = plain_body_steps / plain_s
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+           "config": {"workload": BATCH_DESC, "worlds": len(worlds), "bodies": sum(w.n for w in worlds),
+                      "dynamic_bodies": dynamic, "iterations": 10, "dt": "1/60", "form": "batched",
+                      "l2": "flushed (512 MB write) before every timed step", "parallelism": f"replicas x{world_size}"},
+           "plain_per_scene": {"value": plain_value, "unit": UNIT, "sample_worlds": len(sample),
+                               "steps_per_world": args.plain_steps, "batched_over_plain": value / plain_value},
+           "e2e": e2e, "clocks": clocks.summary(), "counts": {"manifolds": st.manifolds, "contacts": st.contacts,
+                                                              "pairs": st.broad_pairs},
+           "phase_ms_last_step": {k: getattr(st, k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]}}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=300)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="pile", choices=["pile", "pyramid420", "lattice"])
+    ap.add_argument("--workload", default="pile", choices=["pile", "pyramid420", "lattice", "batch"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--plain-steps", type=int, default=20)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
@@ -298,7 +390,7 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    out = run_gpu(args, rank, world_size)
+    out = run_batch(args, rank, world_size) if args.workload == "batch" else run_gpu(args, rank, world_size)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world_size > 1:

@@ -109,6 +109,21 @@ class KernelTimes(C.Structure):
     ]
 
 
+class ForceDesc(C.Structure):
+    """avbdg_force_desc: kind 0 = Joint, 1 = IgnoreCollision."""
+
+    _fields_ = [
+        ("kind", C.c_int),
+        ("body_a", C.c_int),
+        ("body_b", C.c_int),
+        ("r_a", C.c_float * 3),
+        ("r_b", C.c_float * 3),
+        ("stiffness_lin", C.c_float),
+        ("stiffness_ang", C.c_float),
+        ("fracture", C.c_float),
+    ]
+
+
 class AvbdError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"AVBD call failed ({code}): {message}")
@@ -365,3 +380,96 @@ class World:
         self.api.check(self.api.world_dump_colours(self.handle, cnt.value, _ptr(col, C.c_uint8),
                                                    _ptr(ids, C.c_int32), C.byref(cnt)))
         return col, ids
+
+
+def make_force_descs(joints):
+    """Pack (a, b, rA, rB, kLin, kAng, fracture) joint tuples into an avbdg_force_desc array."""
+    descs = (ForceDesc * max(len(joints), 1))()
+    for i, (a, b, ra, rb, kl, ka, fr) in enumerate(joints):
+        d = descs[i]
+        d.kind = 0
+        d.body_a, d.body_b = int(a), int(b)
+        d.r_a[:] = list(ra)
+        d.r_b[:] = list(rb)
+        d.stiffness_lin, d.stiffness_ang, d.fracture = float(kl), float(ka), float(fr)
+    return descs
+
+
+class Batch:
+    """Many independent worlds stepped together (avbdg_batch_*, GPU library only)."""
+
+    def __init__(self, lib, params=None, max_worlds=0, max_bodies=0, max_forces=0):
+        self.lib = lib
+        self._api = Api(lib, "avbdg_")
+        p = self._api.default_params() if params is None else params
+        sig = {
+            "batch_create": ([C.POINTER(Params), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+            "batch_destroy": ([C.c_void_p]),
+            "batch_add_world": ([C.c_void_p, C.c_int, C.POINTER(BodyDesc), C.c_int, C.POINTER(ForceDesc),
+                                 C.POINTER(C.c_int)]),
+            "batch_step": ([C.c_void_p, C.c_int]),
+            "batch_sync": ([C.c_void_p]),
+            "batch_get_body_state": ([C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp]),
+            "batch_set_body_state": ([C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp]),
+            "batch_digest": ([C.c_void_p, C.c_int, _up]),
+            "batch_get_stats": ([C.c_void_p, C.POINTER(Stats)]),
+        }
+        self.fn = {}
+        for name, argtypes in sig.items():
+            f = getattr(lib, "avbdg_" + name)
+            f.argtypes = argtypes
+            f.restype = C.c_int
+            self.fn[name] = f
+        h = C.c_void_p()
+        self._api.check(self.fn["batch_create"](C.byref(p), int(max_worlds), int(max_bodies), int(max_forces),
+                                                C.byref(h)))
+        self.handle = h
+        self.sizes = []
+
+    def close(self):
+        if self.handle:
+            self.fn["batch_destroy"](self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, scene):
+        descs = make_body_descs(scene.size, scene.density, scene.friction, scene.position, scene.orientation,
+                                scene.velocity)
+        forces = make_force_descs(scene.joints)
+        out = C.c_int()
+        self._api.check(self.fn["batch_add_world"](self.handle, scene.n, descs, len(scene.joints), forces,
+                                                   C.byref(out)))
+        self.sizes.append(scene.n)
+        return out.value
+
+    def step(self, n=1):
+        self._api.check(self.fn["batch_step"](self.handle, int(n)))
+
+    def sync(self):
+        self._api.check(self.fn["batch_sync"](self.handle))
+
+    def state(self, world):
+        n = self.sizes[world]
+        p = np.zeros((n, 3), np.float32)
+        q = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        w = np.zeros((n, 3), np.float32)
+        self._api.check(self.fn["batch_get_body_state"](self.handle, world, 0, n, _ptr(p, C.c_float),
+                                                        _ptr(q, C.c_float), _ptr(v, C.c_float),
+                                                        _ptr(w, C.c_float)))
+        return p, q, v, w
+
+    def digest(self, world):
+        out = C.c_uint64()
+        self._api.check(self.fn["batch_digest"](self.handle, world, C.byref(out)))
+        return out.value
+
+    def stats(self):
+        s = Stats()
+        self._api.check(self.fn["batch_get_stats"](self.handle, C.byref(s)))
+        return s

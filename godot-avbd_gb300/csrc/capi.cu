@@ -14,6 +14,11 @@ struct avbdg_world {
     avbdg_world(const avbdg_params &p, int nb, int nf) : engine(p, nb, nf, 1) { engine.addWorld(); }
 };
 
+struct avbdg_batch {
+    avbdg::Engine engine;
+    avbdg_batch(const avbdg_params &p, int nw, int nb, int nf) : engine(p, nb, nf, nw) {}
+};
+
 namespace {
 
 thread_local std::string g_lastError;
@@ -29,10 +34,10 @@ int failWith(int rc, const char *msg) {
     return rc;
 }
 
-template <typename F>
-int guarded(avbdg_world *w, F &&fn) {
+template <typename H, typename F>
+int guarded(H *w, F &&fn) {
     if (!w)
-        return failWith(AVBDG_ERR_INVALID, "null world");
+        return failWith(AVBDG_ERR_INVALID, "null handle");
     try {
         return record(fn(w->engine), &w->engine);
     } catch (const std::bad_alloc &) {
@@ -208,6 +213,107 @@ int avbdg_world_digest(avbdg_world *w, uint64_t *out) {
     if (!out)
         return failWith(AVBDG_ERR_INVALID, "null output");
     return guarded(w, [out](avbdg::Engine &e) { return e.digest(0, *out); });
+}
+
+int avbdg_batch_create(const avbdg_params *params, int max_worlds, int max_bodies, int max_forces,
+                       avbdg_batch **out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    *out = nullptr;
+    avbdg_params p;
+    if (params)
+        p = *params;
+    else
+        avbdg_params_default(&p);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        return failWith(AVBDG_ERR_CUDA, "no CUDA device: the GPU step has no CPU fallback");
+    try {
+        avbdg_batch *b = new avbdg_batch(p, max_worlds, max_bodies, max_forces);
+        const int rc = b->engine.setParams(p);
+        if (rc != AVBDG_OK) {
+            g_lastError = b->engine.error();
+            delete b;
+            return rc;
+        }
+        *out = b;
+        return AVBDG_OK;
+    } catch (const std::bad_alloc &) {
+        return failWith(AVBDG_ERR_CAPACITY, "host allocation failed");
+    }
+}
+
+int avbdg_batch_destroy(avbdg_batch *b) {
+    delete b;
+    return AVBDG_OK;
+}
+
+int avbdg_batch_add_world(avbdg_batch *b, int nb, const avbdg_body_desc *bodies, int nf, const avbdg_force_desc *forces,
+                          int *outWorld) {
+    if (nf < 0 || (nf > 0 && !forces))
+        return failWith(AVBDG_ERR_INVALID, "bad force array");
+    return guarded(b, [=](avbdg::Engine &e) {
+        const int w = e.addWorld();
+        if (w < 0)
+            return AVBDG_ERR_CAPACITY;
+        int rc = e.addBodies(w, nb, bodies, nullptr);
+        for (int i = 0; rc == AVBDG_OK && i < nf; i++) {
+            const avbdg_force_desc &f = forces[i];
+            if (f.kind == 0)
+                rc = e.addJoint(w, f.body_a, f.body_b, f.r_a, f.r_b, f.stiffness_lin, f.stiffness_ang, f.fracture);
+            else if (f.kind == 1)
+                rc = e.addIgnore(w, f.body_a, f.body_b);
+            else
+                rc = AVBDG_ERR_UNSUPPORTED;
+        }
+        if (rc == AVBDG_OK && outWorld)
+            *outWorld = w;
+        return rc;
+    });
+}
+
+int avbdg_batch_step(avbdg_batch *b, int count) {
+    return guarded(b, [=](avbdg::Engine &e) {
+        for (int i = 0; i < count; i++) {
+            const int rc = e.step();
+            if (rc != AVBDG_OK)
+                return rc;
+        }
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_batch_sync(avbdg_batch *b) {
+    return guarded(b, [](avbdg::Engine &e) { return e.sync(); });
+}
+
+int avbdg_batch_world_count(const avbdg_batch *b, int *out) {
+    if (!b || !out)
+        return failWith(AVBDG_ERR_INVALID, "null argument");
+    *out = b->engine.worlds();
+    return AVBDG_OK;
+}
+
+int avbdg_batch_get_body_state(avbdg_batch *b, int world, int first, int count, float *p, float *q, float *v,
+                               float *av) {
+    return guarded(b, [=](avbdg::Engine &e) { return e.getState(world, first, count, p, q, v, av); });
+}
+
+int avbdg_batch_set_body_state(avbdg_batch *b, int world, int first, int count, const float *p, const float *q,
+                               const float *v, const float *av) {
+    return guarded(b, [=](avbdg::Engine &e) { return e.setState(world, first, count, p, q, v, av); });
+}
+
+int avbdg_batch_digest(avbdg_batch *b, int world, uint64_t *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return guarded(b, [=](avbdg::Engine &e) { return e.digest(world, *out); });
+}
+
+int avbdg_batch_get_stats(avbdg_batch *b, avbdg_stats *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return guarded(b, [out](avbdg::Engine &e) { return e.stats(*out); });
 }
 
 int avbdg_world_set_profiling(avbdg_world *w, int enabled) {

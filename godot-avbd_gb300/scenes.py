@@ -257,24 +257,15 @@ def small_world(rng, n_target):
     b = _Builder()
     b.box((60, 60, 1), 0.0, 0.5, (0, 0, -0.5))
     if rng.random() < 0.5:
-        remaining = n_target
-        wall = 0
-        while remaining > 0:
-            rows = int(min(20, max(3, math.ceil((math.sqrt(8 * remaining + 1) - 1) / 2))))
-            y = _f(wall * 1.5)
-            placed = 0
-            for r in range(rows):
-                cnt = rows - r
-                for k in range(cnt):
-                    if placed >= remaining:
-                        break
-                    x = (_f(k) - _f(cnt - 1) * _f(0.5)) * _f(1.01)
-                    b.box((1, 1, 1), 1.0, 0.5, (x, y, _f(0.5) + _f(r)))
-                    placed += 1
-            remaining -= placed
-            wall += 1
+        # One pyramid wall of 3-20 rows, the row count closest to the drawn size.
+        rows = int(min(20, max(3, round((math.sqrt(8 * n_target + 1) - 1) / 2))))
+        for r in range(rows):
+            cnt = rows - r
+            for k in range(cnt):
+                x = (_f(k) - _f(cnt - 1) * _f(0.5)) * _f(1.01)
+                b.box((1, 1, 1), 1.0, 0.5, (x, 0.0, _f(0.5) + _f(r)))
     else:
-        side = max(4.0, (n_target * 8.0) ** (1.0 / 3.0) * 1.6)
+        side = max(8.0, (n_target * 20.0) ** (1.0 / 3.0) * 1.5)
         _place_pile(rng, b, n_target, (-side / 2, -side / 2, 1.0), (side / 2, side / 2, 1.0 + side))
     return b.scene("world")
 

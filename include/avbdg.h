@@ -230,6 +230,44 @@ int avbdg_world_dump_colours(avbdg_world *world, int cap, uint8_t *colour, int32
                              int *count);
 
 /* ------------------------------------------------------------------------------------ */
+/* Batches: many independent worlds stepped together                                   */
+/* ------------------------------------------------------------------------------------ */
+
+/* A set of independent worlds (each one avbd::Solver, src/avbd/solver.h:50-374) that share one
+ * device store and one CUDA stream: every kernel of a step covers all worlds in one launch. Each
+ * world's result is bit-identical to stepping that world alone. All worlds share `params`
+ * (gravity is copied into each body at creation, as Rigid::Rigid does). */
+typedef struct avbdg_batch avbdg_batch;
+
+/* One force of a world (forces.hpp:58-113): kind 0 = Joint, 1 = IgnoreCollision. Body indices
+ * are creation indices within the world; body_a = -1 anchors a joint to the world point r_a. */
+typedef struct avbdg_force_desc {
+    int kind;
+    int body_a, body_b;
+    float r_a[3], r_b[3];
+    float stiffness_lin, stiffness_ang, fracture;
+} avbdg_force_desc;
+
+int avbdg_batch_create(const avbdg_params *params, int max_worlds, int max_bodies, int max_forces,
+                       avbdg_batch **out);
+int avbdg_batch_destroy(avbdg_batch *batch);
+/* Append a world with its bodies (creation order) and forces (creation order). */
+int avbdg_batch_add_world(avbdg_batch *batch, int body_count, const avbdg_body_desc *bodies,
+                          int force_count, const avbdg_force_desc *forces, int *out_world);
+/* `count` steps of every world (Solver::step each). */
+int avbdg_batch_step(avbdg_batch *batch, int count);
+int avbdg_batch_sync(avbdg_batch *batch);
+int avbdg_batch_world_count(const avbdg_batch *batch, int *out);
+int avbdg_batch_get_body_state(avbdg_batch *batch, int world, int first, int count, float *position,
+                               float *orientation, float *velocity, float *angular_velocity);
+int avbdg_batch_set_body_state(avbdg_batch *batch, int world, int first, int count,
+                               const float *position, const float *orientation,
+                               const float *velocity, const float *angular_velocity);
+int avbdg_batch_digest(avbdg_batch *batch, int world, uint64_t *out);
+/* Totals over all worlds; phase times of the last step. */
+int avbdg_batch_get_stats(avbdg_batch *batch, avbdg_stats *out);
+
+/* ------------------------------------------------------------------------------------ */
 /* Standalone kernels                                                                   */
 /* ------------------------------------------------------------------------------------ */
 
