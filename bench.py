@@ -292,12 +292,16 @@ def run_batch(args, rank, world_size):
     if world_size > 1:
         torch.distributed.barrier()
     step_ms = []
+    batch.take_kernel_times()
+    batch.set_profiling(True)
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             batch.step()
             step_ms.append(batch.stats().total_ms)
+    kt = batch.take_kernel_times()
+    batch.set_profiling(False)
     total_ms = float(sum(step_ms))
     if world_size > 1:
         t = torch.tensor([total_ms], device="cuda")
@@ -306,22 +310,41 @@ def run_batch(args, rank, world_size):
     value = dynamic * args.steps * world_size / (total_ms / 1e3)
     st = batch.stats()
 
-    # End to end: every step uploads all bodies' state and reads it back through the C ABI.
-    states = [batch.state(i) for i in range(len(worlds))]
+    # Roofline of the manifold dual + stamp pass (the per-round kernel carrying the contact state).
+    peak, peak_kind = measured_peak_hbm()
+    iters = 10
+    bytes_per_launch = 188 * st.manifolds + 112 * st.contacts + 112 * st.manifold_sides * (iters - 1) / iters
+    launch_ms = kt.manifold_ms / max(kt.manifold_launches, 1)
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_batch.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("manifold_pass_bytes_per_launch")
+    roofline = {"bound": "hbm", "kernel": "dualKernel (manifold dual + block stamps)", "achieved": achieved,
+                "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
+                "counts": {"manifolds": st.manifolds, "contacts": st.contacts, "stamp_sides": st.manifold_sides},
+                "note": "L2 flushed before each step, not between the rounds of a step"}
+
+    # End to end: every step uploads all bodies' state from host memory and reads it back, one copy
+    # each way for the whole batch, through the C ABI.
+    state = batch.state_all()
     torch.cuda.synchronize()
-    e2e_steps = max(1, args.steps // 4)
+    e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for i, (pp, qq, vv, ww) in enumerate(states):
-            batch.fn["batch_set_body_state"](batch.handle, i, 0, worlds[i].n, capi._ptr(pp, ctypes.c_float),
-                                             capi._ptr(qq, ctypes.c_float), capi._ptr(vv, ctypes.c_float),
-                                             capi._ptr(ww, ctypes.c_float))
+        batch.set_state_all(*state)
         batch.step()
-        states = [batch.state(i) for i in range(len(worlds))]
+        state = batch.state_all(state)
     e2e_s = time.perf_counter() - t0
+    if world_size > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
     nbytes = 13 * 4 * sum(w.n for w in worlds)
     e2e = {"value": dynamic * e2e_steps * world_size / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-           "d2h_bytes_per_step": nbytes, "note": "per-world state calls (4096 uploads + 4096 reads per step)"}
+           "d2h_bytes_per_step": nbytes}
 
     # Plain per-scene GPU step on a sample of the worlds, each its own avbdg_world.
     rng = np.random.default_rng(1)
@@ -347,19 +370,48 @@ def run_batch(args, rank, world_size):
                       "l2": "flushed (512 MB write) before every timed step", "parallelism": f"replicas x{world_size}"},
            "plain_per_scene": {"value": plain_value, "unit": UNIT, "sample_worlds": len(sample),
                                "steps_per_world": args.plain_steps, "batched_over_plain": value / plain_value},
-           "e2e": e2e, "clocks": clocks.summary(), "counts": {"manifolds": st.manifolds, "contacts": st.contacts,
-                                                              "pairs": st.broad_pairs},
-           "phase_ms_last_step": {k: getattr(st, k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]}}
+           "roofline": roofline, "e2e": e2e, "gpu_launches": kt.kernel_launches, "clocks": clocks.summary(),
+           "counts": {"manifolds": st.manifolds, "contacts": st.contacts, "pairs": st.broad_pairs},
+           "phase_ms_last_step": {k: getattr(st, k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]},
+           "kernel_ms": {"manifold_pass_per_launch": launch_ms,
+                         "body_solve_per_launch": kt.body_ms / max(kt.body_launches, 1),
+                         "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)}}
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
+        v_cpu, kind, done, elapsed, cores = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=20.0)
+        out["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": cores, "kind": kind,
+                               "sample": f"{done} world-steps (worlds stepped one at a time, steps "
+                                         f"{args.warmup + 1}-{args.warmup + args.steps}), {elapsed:.1f} s of CPU "
+                                         f"step time, all {cores} threads"}
     return out
+
+
+def run_cpu_batch_sample(worlds, warmup, steps, budget_s):
+    """The reference's CPU step over the batch's worlds, one world at a time with all host threads
+    (how the reference would serve them), on a bounded sample of worlds."""
+    import numpy as np
+
+    rng = np.random.default_rng(2)
+    order = rng.permutation(len(worlds))
+    body_steps, elapsed, done, kind = 0, 0.0, 0, "port"
+    cores = os.cpu_count() or 1
+    for i in order:
+        sc = worlds[i]
+        v, kind, n_done, t = run_cpu_reference(sc, steps, warmup, 0)
+        body_steps += sc.dynamic * n_done
+        elapsed += t
+        done += n_done
+        if elapsed > budget_s:
+            break
+    return body_steps / elapsed, kind, done, elapsed, cores
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
-    ap.add_argument("--warmup", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="pile", choices=["pile", "pyramid420", "lattice", "batch"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "pile", "pyramid420", "lattice"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--worlds", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=64)
@@ -367,6 +419,23 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference" and args.workload == "batch":
+        if rank != 0:
+            return
+        worlds = entry.load_package().scenes.batch(worlds=args.worlds, seed=7)
+        v, kind, done, elapsed, cores = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=60.0)
+        out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
+               "config": {"workload": BATCH_DESC, "worlds": len(worlds), "iterations": 10, "dt": "1/60",
+                          "form": "CPU solver step, worlds one at a time"},
+               "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
+                                "sample": f"{done} world-steps of randomly chosen worlds (steps {args.warmup + 1}-"
+                                          f"{args.warmup + args.steps}), {elapsed:.1f} s, all {cores} threads"},
+               "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
+        return
 
     if args.impl == "reference":
         if rank != 0:

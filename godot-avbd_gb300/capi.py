@@ -93,6 +93,9 @@ class Stats(C.Structure):
         ("solve_ms", C.c_double),
         ("finish_ms", C.c_double),
         ("total_ms", C.c_double),
+        ("manifold_sides", C.c_int),
+        ("graph_step", C.c_int),
+        ("kernel_launches", C.c_int),
     ]
 
 
@@ -468,6 +471,34 @@ class Batch:
         out = C.c_uint64()
         self._api.check(self.fn["batch_digest"](self.handle, world, C.byref(out)))
         return out.value
+
+    def state_all(self, out=None):
+        """All bodies of all worlds in world order, one device-to-host copy."""
+        n = sum(self.sizes)
+        p, q, v, w = out if out is not None else (np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32),
+                                                  np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32))
+        self._api.check(self.fn["batch_get_body_state"](self.handle, -1, 0, n, _ptr(p, C.c_float),
+                                                        _ptr(q, C.c_float), _ptr(v, C.c_float),
+                                                        _ptr(w, C.c_float)))
+        return p, q, v, w
+
+    def set_state_all(self, position=None, orientation=None, velocity=None, angular_velocity=None):
+        n = sum(self.sizes)
+        self._api.check(self.fn["batch_set_body_state"](self.handle, -1, 0, n, _ptr(position, C.c_float),
+                                                        _ptr(orientation, C.c_float), _ptr(velocity, C.c_float),
+                                                        _ptr(angular_velocity, C.c_float)))
+
+    def set_profiling(self, on=True):
+        fn = self.lib.avbdg_batch_set_profiling
+        fn.argtypes = [C.c_void_p, C.c_int]
+        self._api.check(fn(self.handle, 1 if on else 0))
+
+    def take_kernel_times(self):
+        fn = self.lib.avbdg_batch_take_kernel_times
+        fn.argtypes = [C.c_void_p, C.POINTER(KernelTimes)]
+        t = KernelTimes()
+        self._api.check(fn(self.handle, C.byref(t)))
+        return t
 
     def stats(self):
         s = Stats()

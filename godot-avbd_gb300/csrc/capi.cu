@@ -316,6 +316,22 @@ int avbdg_batch_get_stats(avbdg_batch *b, avbdg_stats *out) {
     return guarded(b, [out](avbdg::Engine &e) { return e.stats(*out); });
 }
 
+int avbdg_batch_set_profiling(avbdg_batch *b, int enabled) {
+    return guarded(b, [=](avbdg::Engine &e) {
+        e.setProfiling(enabled != 0);
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_batch_take_kernel_times(avbdg_batch *b, avbdg_kernel_times *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return guarded(b, [out](avbdg::Engine &e) {
+        e.takeKernelTimes(*out);
+        return AVBDG_OK;
+    });
+}
+
 int avbdg_world_set_profiling(avbdg_world *w, int enabled) {
     return guarded(w, [=](avbdg::Engine &e) {
         e.setProfiling(enabled != 0);

@@ -37,6 +37,9 @@ constexpr int kRefitBudget = 16; // src/avbd/bvh_broadphase.hpp:40
 } // namespace
 
 Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int maxWorlds) : P(params) {
+    const char *noGraphs = std::getenv("AVBDG_NO_GRAPHS");
+    useGraphs = !(noGraphs && noGraphs[0] == '1');
+    prepareKernels(); // attributes and occupancy queries, never during a capture
     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
     for (auto &e : ev)
         cudaEventCreate(&e);
@@ -47,6 +50,7 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
 Engine::~Engine() {
     if (stream)
         cudaStreamSynchronize(stream);
+    dropGraphs();
     releaseAll();
     if (ioHost)
         cudaFreeHost(ioHost);
@@ -89,6 +93,7 @@ void Engine::releaseAll() {
 }
 
 void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
+    dropGraphs(); // they hold the old buffers' addresses
     const Dev old = d;
     std::vector<void *> oldAllocs;
     oldAllocs.swap(allocs);
@@ -270,6 +275,7 @@ int Engine::addWorld() {
 }
 
 int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outIds) {
+    dropGraphs();
     if (w < 0 || w >= worlds() || count < 0 || (count > 0 && !descs))
         return fail(AVBDG_ERR_INVALID, "bad world or body array");
     if (w != worlds() - 1)
@@ -335,6 +341,7 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
 
 int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], float kLin, float kAng,
                      float fracture) {
+    dropGraphs();
     if (w < 0 || w >= worlds() || b < 0 || b >= wCount[w] || a < -1 || a >= wCount[w] || !rA || !rB)
         return fail(AVBDG_ERR_INVALID, "bad body index");
     int rc = ensureCapacity(nBodies, nForces + 1, worlds());
@@ -375,6 +382,7 @@ int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], 
 }
 
 int Engine::addIgnore(int w, int a, int b) {
+    dropGraphs();
     if (w < 0 || w >= worlds() || a < 0 || b < 0 || a >= wCount[w] || b >= wCount[w])
         return fail(AVBDG_ERR_INVALID, "bad body index");
     int rc = ensureCapacity(nBodies, nForces + 1, worlds());
@@ -398,6 +406,7 @@ int Engine::addIgnore(int w, int a, int b) {
 
 void Engine::clear() {
     cudaStreamSynchronize(stream);
+    dropGraphs();
     wBase.clear();
     wCount.clear();
     nBodies = nDynamic = nForces = 0;
@@ -416,6 +425,7 @@ int Engine::setParams(const avbdg_params &p) {
         return fail(AVBDG_ERR_UNSUPPORTED,
                     "contact grace, sleeping, the arm cache and the convergence probe are not on the GPU path");
     P = p;
+    dropGraphs(); // parameters are baked into captured launches
     return AVBDG_OK;
 }
 
@@ -447,31 +457,161 @@ StepParams Engine::stepParams(float collisionDt) const {
 bool Engine::needGreedy() const { return nForces > 0 || !P.contact_only_overflow; }
 
 // Solver::broadPhase (solver_broadphase.cpp:85-186).
-int Engine::broadPhase(const StepParams &sp) {
-    if (!adjValid)
+// Host decisions of one step (everything the enqueued work depends on besides device counts).
+Engine::StepPlan Engine::planStep(int mode, int substeps, int rounds) {
+    StepPlan plan;
+    plan.mode = mode;
+    plan.substeps = substeps;
+    plan.rounds = rounds;
+    plan.adjAtStart = !adjValid;
+    plan.anyTree = false;
+    for (int c : wCount)
+        plan.anyTree = plan.anyTree || c >= 2;
+    // Rebuild from fresh Morton codes when the body set changed or after kRefitBudget refits
+    // (bvh_broadphase.cpp:186-203), so the code/order dumps follow the reference's schedule.
+    plan.rebuild = plan.anyTree && (!treeValid || treeAge >= kRefitBudget);
+    if (plan.anyTree) {
+        if (plan.rebuild) {
+            treeValid = true;
+            treeAge = 0;
+        } else {
+            treeAge++;
+        }
+    }
+    adjValid = true; // the step rebuilds the adjacency after warm starting
+    plan.forces = nForces > 0;
+    plan.greedy = needGreedy();
+    return plan;
+}
+
+std::string Engine::StepPlan::key() const {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0, anyTree ? 1 : 0,
+                  rebuild ? 1 : 0, forces ? 1 : 0, greedy ? 1 : 0);
+    return buf;
+}
+
+void Engine::recordPhase(cudaEvent_t e) {
+    if (capturing)
+        cudaEventRecordWithFlags(e, stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(e, stream);
+}
+
+int Engine::broadPhase(const StepParams &sp, const StepPlan &plan) {
+    if (plan.adjAtStart)
         launchAdjacency(d, nBodies, stream);
     launchAabb(d, nBodies, sp, stream);
-    bool anyWorldTree = false;
-    for (int c : wCount)
-        anyWorldTree = anyWorldTree || c >= 2;
-    if (!anyWorldTree) {
+    if (!plan.anyTree) {
         cudaMemsetAsync(d.ctr + C_PAIRS, 0, sizeof(int), stream);
         cudaMemcpyAsync(d.ctr + C_CAND, d.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToDevice, stream);
         return AVBDG_OK;
     }
-    // Rebuild from fresh Morton codes when the body set changed or after kRefitBudget refits
-    // (bvh_broadphase.cpp:186-203), so the code/order dumps follow the reference's schedule.
-    if (!treeValid || treeAge >= kRefitBudget) {
+    if (plan.rebuild)
         launchRebuildTree(d, nBodies, worlds(), stream);
-        treeValid = true;
-        treeAge = 0;
-    } else {
-        treeAge++;
-    }
     launchRefit(d, nBodies, stream);
     launchPairs(d, nBodies, stream);
     launchFilterAcquire(d, stream);
     return AVBDG_OK;
+}
+
+// The whole step, enqueued on the stream without host round trips.
+void Engine::enqueueStep(const StepPlan &plan) {
+    if (plan.mode == 0) {
+        const StepParams sp = stepParams(P.dt);
+        broadPhase(sp, plan);
+        recordPhase(ev[1]);
+        warmstartAndSelect(sp);
+        projectContacts(sp, false, 0.0f);
+        recordPhase(ev[2]);
+        runSubstep(sp, P.iterations);
+        recordPhase(ev[3]);
+        projectContacts(sp, P.position_projection != 0, 0.0f);
+        launchRebase(d, sp, stream);
+        return;
+    }
+    const int substeps = plan.substeps;
+    const StepParams sp = stepParams(P.dt * static_cast<float>(substeps));
+    broadPhase(sp, plan);
+    recordPhase(ev[1]);
+    warmstartAndSelect(sp);
+    recordPhase(ev[2]);
+    for (int sub = 0; sub < substeps; ++sub) {
+        if (sub > 0)
+            launchRebase(d, sp, stream);
+        projectContacts(sp, false, P.dt * static_cast<float>(substeps - sub));
+        runSubstep(sp, plan.rounds);
+    }
+    recordPhase(ev[3]);
+    projectContacts(sp, P.position_projection != 0, sp.collisionDt);
+    launchRebase(d, sp, stream);
+}
+
+void Engine::dropGraphs() {
+    for (auto &kv : graphs) {
+        cudaGraphExecDestroy(kv.second.exec);
+        for (const Span &s : kv.second.spans) {
+            cudaEventDestroy(s.a);
+            cudaEventDestroy(s.b);
+        }
+    }
+    graphs.clear();
+    graphSpans = nullptr;
+}
+
+// Run the plan: from the graph cache (captured on first use), or eagerly when profiling, when
+// graphs are disabled or when a capture failed.
+int Engine::runPlan(const StepPlan &plan) {
+    launchBase = launchCount();
+    graphSpans = nullptr;
+    lastGraph = false;
+    cudaEventRecord(ev[0], stream);
+    if (useGraphs) {
+        const std::string k = plan.key() + (profiling ? "/profiled" : "");
+        auto it = graphs.find(k);
+        if (it == graphs.end()) {
+            const int before = launchCount();
+            spans.clear();
+            evUsed = 0;
+            cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+            capturing = true;
+            enqueueStep(plan);
+            capturing = false;
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(stream, &g);
+            cudaGraphExec_t exec = nullptr;
+            if (e == cudaSuccess)
+                e = cudaGraphInstantiate(&exec, g, 0);
+            if (g)
+                cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                cudaGetLastError(); // capture refused: run eagerly from now on
+                useGraphs = false;
+                graphError = cudaGetErrorString(e);
+                for (const Span &s : spans) {
+                    cudaEventDestroy(s.a);
+                    cudaEventDestroy(s.b);
+                }
+                spans.clear();
+                enqueueStep(plan);
+            } else {
+                Graph gr{exec, launchCount() - before, {}};
+                gr.spans.swap(spans);
+                it = graphs.emplace(k, std::move(gr)).first;
+            }
+        }
+        if (it != graphs.end()) {
+            cudaGraphLaunch(it->second.exec, stream);
+            launchBase = launchCount() - it->second.launches; // kernels inside the graph
+            graphSpans = &it->second.spans;
+            lastGraph = true;
+        }
+    } else {
+        enqueueStep(plan);
+    }
+    cudaEventRecord(ev[4], stream);
+    timed = true;
+    return finishStep();
 }
 
 // warmstartForces + selectUpdateBodies (solver_solve.cpp:31-105, 263-424).
@@ -482,17 +622,9 @@ int Engine::warmstartAndSelect(const StepParams &sp) {
     endSpan(kNarrow);
     launchManifoldCompact(d, stream);
     launchAdjacency(d, nBodies, stream);
-    adjValid = true;
     launchContactOnly(d, nBodies, stream);
     launchColour(d, nBodies, needGreedy(), stream);
     launchColourLists(d, nBodies, P.contact_only_overflow, stream);
-    std::fill(std::begin(colourSizes), std::end(colourSizes), 0);
-    if (needGreedy()) {
-        // The colouring already waited on the host; fetch the colour sizes so the round loop
-        // launches only the colours in use.
-        cudaMemcpyAsync(colourSizes, d.colourCount, sizeof(colourSizes), cudaMemcpyDeviceToHost, stream);
-        cudaStreamSynchronize(stream);
-    }
     return AVBDG_OK;
 }
 
@@ -512,22 +644,21 @@ void Engine::runSubstep(const StepParams &sp, int rounds) {
             std::clamp(static_cast<int>(std::ceil(P.newton_ratio * static_cast<float>(rounds))), 1, rounds);
     const bool colours = needGreedy();
     const bool inPlace = nForces == 0;
-    const int bodyCap = std::max(nDynamic, 1);
     launchStamps(d, sp, false, stream);
     for (int it = 0; it < rounds; it++) {
         const bool newton = it < newtonRounds;
         if (newton) {
             if (colours) {
+                // Each pass reads its colour's size on the device; empty colours return at once.
                 for (int c = 0; c < kMaxColours; c++)
-                    if (colourSizes[c] > 0)
-                        launchColourPass(d, c, colourSizes[c], sp, stream);
+                    launchColourPass(d, c, std::max(nDynamic, 1), sp, stream);
                 launchStamps(d, sp, true, stream);
             }
             beginSpan();
-            launchOverflowSolve(d, bodyCap, sp, inPlace, stream);
+            launchOverflowSolve(d, nBodies, sp, inPlace, stream);
             endSpan(kBody);
             if (!inPlace)
-                launchOverflowApply(d, bodyCap, sp, stream);
+                launchOverflowApply(d, nBodies, sp, stream);
         }
         const bool nextNewton = it + 1 < newtonRounds;
         beginSpan();
@@ -558,6 +689,8 @@ int Engine::finishStep() {
         cudaMemsetAsync(d.ctr + C_ERRORS, 0, sizeof(int), stream);
         if (e & kErrBrakeTimeout)
             return fail(AVBDG_ERR_TIMEOUT, "brake sweep: a bounded grid barrier gave up");
+        if (e & kErrColourTimeout)
+            return fail(AVBDG_ERR_TIMEOUT, "colouring: a bounded grid barrier gave up");
         return fail(AVBDG_ERR_CAPACITY, "a device buffer overflowed this step (state is not trustworthy)");
     }
     // Keep headroom for the next step's pairs and manifolds.
@@ -571,21 +704,7 @@ int Engine::finishStep() {
 int Engine::step() {
     if (nBodies == 0)
         return AVBDG_OK;
-    const StepParams sp = stepParams(P.dt);
-    launchBase = launchCount();
-    cudaEventRecord(ev[0], stream);
-    broadPhase(sp);
-    cudaEventRecord(ev[1], stream);
-    warmstartAndSelect(sp);
-    projectContacts(sp, false, 0.0f);
-    cudaEventRecord(ev[2], stream);
-    runSubstep(sp, P.iterations);
-    cudaEventRecord(ev[3], stream);
-    projectContacts(sp, P.position_projection != 0, 0.0f);
-    launchRebase(d, sp, stream);
-    cudaEventRecord(ev[4], stream);
-    timed = true;
-    return finishStep();
+    return runPlan(planStep(0, 1, P.iterations));
 }
 
 int Engine::stepInterleaved(int substeps, int roundsPerSubstep) {
@@ -593,27 +712,9 @@ int Engine::stepInterleaved(int substeps, int roundsPerSubstep) {
         return step();
     if (nBodies == 0)
         return AVBDG_OK;
-    const StepParams sp = stepParams(P.dt * static_cast<float>(substeps));
-    launchBase = launchCount();
-    cudaEventRecord(ev[0], stream);
-    broadPhase(sp);
-    cudaEventRecord(ev[1], stream);
-    warmstartAndSelect(sp);
-    cudaEventRecord(ev[2], stream);
     const int rounds = roundsPerSubstep > 0 ? std::max(1, roundsPerSubstep)
                                             : std::max(2, (P.iterations + substeps - 1) / substeps);
-    for (int sub = 0; sub < substeps; ++sub) {
-        if (sub > 0)
-            launchRebase(d, sp, stream);
-        projectContacts(sp, false, P.dt * static_cast<float>(substeps - sub));
-        runSubstep(sp, rounds);
-    }
-    cudaEventRecord(ev[3], stream);
-    projectContacts(sp, P.position_projection != 0, sp.collisionDt);
-    launchRebase(d, sp, stream);
-    cudaEventRecord(ev[4], stream);
-    timed = true;
-    return finishStep();
+    return runPlan(planStep(1, substeps, rounds));
 }
 
 int Engine::sync() {
@@ -639,15 +740,25 @@ int Engine::ensureIo(int count) {
 }
 
 // One device-side pack, one copy to pinned memory, one host copy per requested field.
-int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {
-    if (w < 0 || w >= worlds() || first < 0 || count < 0 || first + count > wCount[w])
+// World -1 addresses every body slot of the set in world order (one copy for all worlds).
+int Engine::slotRange(int w, int first, int count, int &g0) {
+    const int limit = w == -1 ? nBodies : (w >= 0 && w < worlds() ? wCount[w] : -1);
+    if (limit < 0 || first < 0 || count < 0 || first + count > limit)
         return fail(AVBDG_ERR_INVALID, "bad range");
+    g0 = (w == -1 ? 0 : wBase[w]) + first;
+    return AVBDG_OK;
+}
+
+int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {
+    int g0 = 0;
+    if (slotRange(w, first, count, g0))
+        return AVBDG_ERR_INVALID;
     if (count == 0)
         return AVBDG_OK;
     int rc = ensureIo(count);
     if (rc)
         return rc;
-    launchPackState(d, wBase[w] + first, count, ioDev, stream);
+    launchPackState(d, g0, count, ioDev, stream);
     cudaMemcpyAsync(ioHost, ioDev, sizeof(float) * 13 * static_cast<size_t>(count), cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess)
         return cudaCheck("getState");
@@ -667,8 +778,9 @@ int Engine::getState(int w, int first, int count, float *pos, float *quat, float
 // companions such as the mass in x.w are kept).
 int Engine::setState(int w, int first, int count, const float *pos, const float *quat, const float *vel,
                      const float *angVel) {
-    if (w < 0 || w >= worlds() || first < 0 || count < 0 || first + count > wCount[w])
-        return fail(AVBDG_ERR_INVALID, "bad range");
+    int g0 = 0;
+    if (slotRange(w, first, count, g0))
+        return AVBDG_ERR_INVALID;
     if (count == 0)
         return AVBDG_OK;
     int rc = ensureIo(count);
@@ -699,21 +811,31 @@ int Engine::setState(int w, int first, int count, const float *pos, const float 
         mask |= 8;
     }
     cudaMemcpyAsync(ioDev, ioHost, sizeof(float) * 13 * n, cudaMemcpyHostToDevice, stream);
-    launchUnpackState(d, wBase[w] + first, count, ioDev, mask, stream);
+    launchUnpackState(d, g0, count, ioDev, mask, stream);
     return cudaCheck("setState");
 }
 
+// Spans of an eager step reuse pooled events; spans captured into a graph get events of their
+// own, recorded by the graph's event nodes at every launch.
 int Engine::beginSpan() {
     if (!profiling)
         return -1;
-    while (evPool.size() < evUsed + 2) {
-        cudaEvent_t e;
-        cudaEventCreate(&e);
-        evPool.push_back(e);
+    cudaEvent_t a, b;
+    if (capturing) {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    } else {
+        while (evPool.size() < evUsed + 2) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            evPool.push_back(e);
+        }
+        a = evPool[evUsed];
+        b = evPool[evUsed + 1];
+        evUsed += 2;
     }
-    cudaEventRecord(evPool[evUsed], stream);
-    spans.push_back(Span{evPool[evUsed], evPool[evUsed + 1], -1});
-    evUsed += 2;
+    recordPhase(a);
+    spans.push_back(Span{a, b, -1});
     return static_cast<int>(spans.size()) - 1;
 }
 
@@ -721,11 +843,12 @@ void Engine::endSpan(int kind) {
     if (!profiling || spans.empty())
         return;
     spans.back().kind = kind;
-    cudaEventRecord(spans.back().b, stream);
+    recordPhase(spans.back().b);
 }
 
 void Engine::collectSpans() {
-    for (const Span &s : spans) {
+    const std::vector<Span> &list = graphSpans ? *graphSpans : spans;
+    for (const Span &s : list) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, s.a, s.b);
         if (s.kind == kManifold) {
@@ -739,8 +862,10 @@ void Engine::collectSpans() {
             acc.narrow_launches++;
         }
     }
-    spans.clear();
-    evUsed = 0;
+    if (!graphSpans) {
+        spans.clear();
+        evUsed = 0;
+    }
 }
 
 void Engine::takeKernelTimes(avbdg_kernel_times &out) {
@@ -762,6 +887,14 @@ int Engine::stats(avbdg_stats &out) {
         cudaMemcpy(counts.data(), d.live.count, sizeof(int) * counts.size(), cudaMemcpyDeviceToHost);
     for (int c : counts)
         out.contacts += c;
+    if (!counts.empty() && nBodies > 0) {
+        std::vector<int2> ab(counts.size());
+        std::vector<float4> x(static_cast<size_t>(nBodies));
+        cudaMemcpy(ab.data(), d.live.ab, sizeof(int2) * ab.size(), cudaMemcpyDeviceToHost);
+        cudaMemcpy(x.data(), d.x, sizeof(float4) * x.size(), cudaMemcpyDeviceToHost);
+        for (const int2 &m : ab)
+            out.manifold_sides += (x[m.x].w > 0.0f ? 1 : 0) + (x[m.y].w > 0.0f ? 1 : 0);
+    }
     int cc[kMaxColours + 1] = {};
     cudaMemcpy(cc, d.colourCount, sizeof(cc), cudaMemcpyDeviceToHost);
     for (int c = 0; c < kMaxColours; c++)
@@ -770,6 +903,8 @@ int Engine::stats(avbdg_stats &out) {
     out.overflow_bodies = cc[kMaxColours];
     out.update_bodies = nDynamic;
     out.steps = steps;
+    out.graph_step = lastGraph ? 1 : 0;
+    out.kernel_launches = launches;
     if (timed) {
         float t[4] = {};
         for (int i = 0; i < 4; i++)

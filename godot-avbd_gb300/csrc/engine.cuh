@@ -42,9 +42,12 @@ enum Counter {
     C_FORCES,         // live forces
     C_ADJ,            // adjacency entries
     C_LONG,           // long segments (segmented sort scratch)
-    C_SPEC,           // speculative manifolds (brake)
+    C_SPEC,           // brake candidates still pending
+    C_SPECN,          // brake candidates in specList
     C_ERRORS,         // capacity / timeout bits (kErr*)
-    C_UNCOLOURED,     // colouring rounds
+    C_UNCOLOURED,     // colouring: bodies still waiting, three rotating slots
+    C_UNCOLOURED1,
+    C_UNCOLOURED2,
     C_ONE,            // constant 1 (scan length helper)
     C_TMP,
     C_COUNT

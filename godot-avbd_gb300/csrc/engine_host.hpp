@@ -7,6 +7,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -57,7 +58,14 @@ public:
                       float *penalty, float *lambda, int *count);
     int dumpColours(int cap, uint8_t *colour, int32_t *bodyId, int *count);
 
+    // Profiling times single launches, so it runs steps eagerly (outside the graph cache).
     void setProfiling(bool on) { profiling = on; }
+    void setGraphs(bool on) {
+        useGraphs = on;
+        if (!on)
+            dropGraphs();
+    }
+    bool graphsEnabled() const { return useGraphs; }
     void takeKernelTimes(avbdg_kernel_times &out);
 
     int worlds() const { return static_cast<int>(wBase.size()); }
@@ -108,6 +116,7 @@ private:
     int ensureIo(int count);
 
     int fail(int code, const std::string &msg);
+    int slotRange(int w, int first, int count, int &g0);
     int cudaCheck(const char *where);
     void allocate(int nb, int mm, int ff, int pp, int ww);
     void releaseAll();
@@ -116,7 +125,28 @@ private:
     int ensureCapacity(int nb, int ff, int ww);
     int flushPending();
     StepParams stepParams(float collisionDt) const;
-    int broadPhase(const StepParams &sp);
+    // Host decisions of one step; the enqueued work depends on nothing else but device counts.
+    struct StepPlan {
+        int mode = 0; // 0 step, 1 interleaved
+        int substeps = 1, rounds = 0;
+        bool adjAtStart = false, anyTree = false, rebuild = false, forces = false, greedy = false;
+        std::string key() const;
+    };
+    struct Graph {
+        cudaGraphExec_t exec;
+        int launches;
+        std::vector<Span> spans; // profiling spans recorded by the graph's event nodes
+    };
+    const std::vector<Span> *graphSpans = nullptr; // spans of the graph the last step ran
+    std::map<std::string, Graph> graphs;
+    bool useGraphs = true, capturing = false, lastGraph = false;
+    std::string graphError;
+    StepPlan planStep(int mode, int substeps, int rounds);
+    void enqueueStep(const StepPlan &plan);
+    int runPlan(const StepPlan &plan);
+    void dropGraphs();
+    void recordPhase(cudaEvent_t e);
+    int broadPhase(const StepParams &sp, const StepPlan &plan);
     int warmstartAndSelect(const StepParams &sp);
     void projectContacts(const StepParams &sp, bool positions, float window);
     void runSubstep(const StepParams &sp, int rounds);

@@ -13,6 +13,7 @@
 
 #include <cooperative_groups.h>
 
+#include "grid_sync.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -22,7 +23,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kBrakeThreads = 512;
-constexpr long long kBarrierSpinLimit = 4000000; // ~0.5 s of 100 ns sleeps
 
 __device__ __forceinline__ bool movable(const Dev &d, int g) { return d.x[g].w > 0.0f; }
 
@@ -87,41 +87,17 @@ __global__ void projActiveKernel(Dev d) {
     }
     d.mSpec[m] = spec;
     d.mDone[m] = spec ? 0 : 1;
-    if (spec)
-        atomicAdd(&d.ctr[C_SPEC], 1);
+    d.mActive[m] = spec;
 }
 
-// Bounded grid barrier for a cooperative launch. Returns false (and flags a timeout) if the
-// other blocks did not arrive in time; callers then leave the kernel.
-__device__ bool gridBarrier(unsigned *bar, int *errors) {
-    __syncthreads();
-    __shared__ int ok;
-    if (threadIdx.x == 0) {
-        ok = 1;
-        volatile unsigned *vgen = bar + 1;
-        const unsigned gen = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
-            bar[0] = 0;
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long long spins = 0;
-            volatile int *verr = errors;
-            while (*vgen == gen) {
-                if (++spins > kBarrierSpinLimit || (*verr & kErrBrakeTimeout)) {
-                    atomicOr(errors, kErrBrakeTimeout);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(100);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok != 0;
+// Brake candidates in live order (the scan of their flags gives each one its slot).
+__global__ void specScatterKernel(Dev d, const int *flags, const int *rank) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m == 0)
+        d.ctr[C_SPEC] = d.ctr[C_SPECN];
+    if (m >= d.ctr[C_LIVE] || !flags[m])
+        return;
+    d.specList[rank[m]] = m;
 }
 
 // Is manifold m the earliest unfinished braking candidate on each of its movable bodies?
@@ -212,25 +188,27 @@ __device__ void brakeManifold(const Dev &d, int m, float window) {
 }
 
 __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window, unsigned *bar) {
-    const int nm = d.ctr[C_LIVE];
+    const int ns = d.ctr[C_SPECN];
     const int nf = d.ctr[C_FORCES];
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     volatile int *remaining = d.ctr + C_SPEC;
-    for (int round = 0; round <= nm; round++) {
+    for (int round = 0; round <= ns; round++) {
         if (*remaining == 0)
             break;
         // Phase 1: mark the ready manifolds (mSpec = 2).
-        for (int m = tid; m < nm; m += stride) {
+        for (int k = tid; k < ns; k += stride) {
+            const int m = d.specList[k];
             if (__ldcg(&d.mDone[m]))
                 continue;
             if (brakeReady(d, m, d.live.ab[m], nf))
                 d.mSpec[m] = 2;
         }
-        if (!gridBarrier(bar, d.ctr + C_ERRORS))
+        if (!gridBarrier(bar, d.ctr + C_ERRORS, kErrBrakeTimeout))
             return;
         // Phase 2: run them; they touch disjoint movable bodies.
-        for (int m = tid; m < nm; m += stride) {
+        for (int k = tid; k < ns; k += stride) {
+            const int m = d.specList[k];
             if (__ldcg(&d.mSpec[m]) != 2)
                 continue;
             brakeManifold(d, m, window);
@@ -238,7 +216,7 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
             __stcg(&d.mDone[m], static_cast<uint8_t>(1));
             atomicSub(d.ctr + C_SPEC, 1);
         }
-        if (!gridBarrier(bar, d.ctr + C_ERRORS))
+        if (!gridBarrier(bar, d.ctr + C_ERRORS, kErrBrakeTimeout))
             return;
     }
 }
@@ -391,8 +369,9 @@ int brakeGridBlocks() {
 
 void launchProjActive(const Dev &d, int nWorlds, cudaStream_t s) {
     cudaMemsetAsync(d.wActive, 0, sizeof(int) * static_cast<size_t>(nWorlds), s);
-    cudaMemsetAsync(d.ctr + C_SPEC, 0, sizeof(int), s);
     ++launchCount(); projActiveKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
+    scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_LIVE, d.ctr + C_SPECN, d.scanScratch, s);
+    ++launchCount(); specScatterKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
 }
 
 void launchBrake(const Dev &d, int, float window, cudaStream_t s) {

@@ -13,6 +13,7 @@
 // Coloured (Gauss-Seidel) bodies recompute their manifold terms from the current poses at every
 // touch; the reference's "first touch uses the dual's cache" rule yields the same floats.
 
+#include "grid_sync.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -666,11 +667,11 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
 
-__global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.colourCount[kOverflowColour])
+// Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
+__global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, int n, StepParams p, int inPlace) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
         return;
-    const int g = d.colourList[kOverflowColour * d.NB + k];
     Blk blk = bodyBlock(d, p, g);
     assemble<false>(d, p, g, blk);
     f3 dl, da;
@@ -685,11 +686,10 @@ __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, Step
     }
 }
 
-__global__ void overflowApplyKernel(Dev d, StepParams p) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.colourCount[kOverflowColour])
+__global__ void overflowApplyKernel(Dev d, int n, StepParams p) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
         return;
-    const int g = d.colourList[kOverflowColour * d.NB + k];
     const float4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), scale(xyz(d.dLin[g]), p.jacobiRelax)), x4.w);
     d.q[g] = f4(qintegrate(asq(d.q[g]), scale(xyz(d.dAng[g]), p.jacobiRelax)));
@@ -803,12 +803,12 @@ __device__ __forceinline__ int adjOtherSolve(const Dev &d, uint32_t seq, int x, 
     return -1;
 }
 
-// One Jones-Plassmann round with list-order priority: a body is coloured once every earlier
+// One Jones-Plassmann attempt with list-order priority: a body is coloured once every earlier
 // (lower list position) neighbour in the update set is, with the smallest colour none of them
-// uses (the sequential greedy of colourGraph, reproduced exactly).
-__global__ void colourRoundKernel(Dev d, int n) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
+// uses (the sequential greedy of colourGraph, reproduced exactly). A body still waiting counts
+// itself in *waiting.
+__device__ void colourTry(const Dev &d, int g, int *waiting) {
+    if (d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
         return;
     volatile uint8_t *col = d.colour;
     if (col[g] != kUncoloured)
@@ -822,7 +822,7 @@ __global__ void colourRoundKernel(Dev d, int n) {
             continue;
         const uint8_t c = col[h];
         if (c == kUncoloured) {
-            atomicAdd(&d.ctr[C_UNCOLOURED], 1);
+            atomicAdd(waiting, 1);
             return;
         }
         if (c < kMaxColours)
@@ -837,6 +837,28 @@ __global__ void colourRoundKernel(Dev d, int n) {
     col[g] = c;
 }
 
+constexpr int kColourThreads = 512;
+
+// All colouring rounds in one cooperative launch, rounds separated by a bounded grid barrier.
+// Round r counts waiting bodies into slot r % 3; the slot of round r + 1 is cleared during
+// round r, after every block has read it for the last time (end of round r - 2).
+__global__ void __launch_bounds__(kColourThreads) colourCoopKernel(Dev d, int n, unsigned *bar) {
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    int *slots = d.ctr + C_UNCOLOURED;
+    for (int round = 0; round <= n; round++) {
+        int *waiting = slots + (round % 3);
+        if (tid == 0)
+            slots[(round + 1) % 3] = 0;
+        for (int g = tid; g < n; g += stride)
+            colourTry(d, g, waiting);
+        if (!gridBarrier(bar, d.ctr + C_ERRORS, kErrColourTimeout))
+            return;
+        if (*reinterpret_cast<volatile int *>(waiting) == 0)
+            break;
+    }
+}
+
 __global__ void colourListKernel(Dev d, int n, int contactOnlyOverflow) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
@@ -845,8 +867,17 @@ __global__ void colourListKernel(Dev d, int n, int contactOnlyOverflow) {
     if (contactOnlyOverflow && d.contactOnly[g])
         c = kOverflowColour;
     d.colour[g] = c;
-    const int slot = atomicAdd(&d.colourCount[c], 1);
-    d.colourList[c * d.NB + slot] = g;
+    // One atomic per warp and colour (the overflow colour is counted, not listed).
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, static_cast<int>(c));
+    const int leader = __ffs(peers) - 1;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == leader)
+        base = atomicAdd(&d.colourCount[c], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    if (c < kOverflowColour)
+        d.colourList[c * d.NB + base + __popc(peers & ((1u << lane) - 1u))] = g;
 }
 
 } // namespace
@@ -858,21 +889,40 @@ void launchContactOnly(const Dev &d, int n, cudaStream_t s) {
     ++launchCount(); contactOnlyMarkKernel<<<grid(d.FF), kThreads, 0, s>>>(d);
 }
 
+static int g_colourBlocks = 0;
+
+int colourGridBlocks() {
+    if (g_colourBlocks == 0) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, colourCoopKernel, kColourThreads, 0);
+        g_colourBlocks = sms * (perSm < 1 ? 1 : (perSm > 2 ? 2 : perSm));
+        if (g_colourBlocks < 1)
+            g_colourBlocks = 1;
+    }
+    return g_colourBlocks;
+}
+
+void prepareKernels() {
+    preparePrimitives();
+    brakeGridBlocks();
+    colourGridBlocks();
+}
+
 void launchColour(const Dev &d, int n, bool needGreedy, cudaStream_t s) {
     if (!needGreedy)
         return;
-    // Rounds until no body is waiting; the host checks every 16 rounds.
-    for (int batch = 0; batch < 4096; batch++) {
-        for (int r = 0; r < 16; r++) {
-            cudaMemsetAsync(d.ctr + C_UNCOLOURED, 0, sizeof(int), s);
-            ++launchCount(); colourRoundKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-        }
-        int waiting = 0;
-        cudaMemcpyAsync(&waiting, d.ctr + C_UNCOLOURED, sizeof(int), cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        if (waiting == 0)
-            return;
-    }
+    colourGridBlocks();
+    unsigned *bar = d.barrier;
+    cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
+    cudaMemsetAsync(d.ctr + C_UNCOLOURED, 0, 3 * sizeof(int), s);
+    Dev dd = d;
+    int nn = n;
+    void *args[] = {&dd, &nn, &bar};
+    ++launchCount();
+    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(colourCoopKernel), dim3(g_colourBlocks), dim3(kColourThreads),
+                                args, 0, s);
 }
 
 void launchColourLists(const Dev &d, int n, int contactOnlyOverflow, cudaStream_t s) {
@@ -896,13 +946,15 @@ void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &
     ++launchCount(); colourPassKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
 }
 
-void launchOverflowSolve(const Dev &d, int capacity, const StepParams &p, bool inPlace, cudaStream_t s) {
-    ++launchCount(); overflowSolveKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p,
-                                                                                                    inPlace ? 1 : 0);
+void launchOverflowSolve(const Dev &d, int nBodies, const StepParams &p, bool inPlace, cudaStream_t s) {
+    ++launchCount();
+    overflowSolveKernel<<<divUp(nBodies > 0 ? nBodies : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, nBodies, p,
+                                                                                                 inPlace ? 1 : 0);
 }
 
-void launchOverflowApply(const Dev &d, int capacity, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); overflowApplyKernel<<<grid(capacity), kThreads, 0, s>>>(d, p);
+void launchOverflowApply(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s) {
+    ++launchCount();
+    overflowApplyKernel<<<grid(nBodies), kThreads, 0, s>>>(d, nBodies, p);
 }
 
 void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s) {

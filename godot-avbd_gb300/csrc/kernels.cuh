@@ -37,8 +37,9 @@ void launchFinishBodies(const Dev &d, int nBodies, const StepParams &p, cudaStre
 // also touch a coloured body (recomputed after the colour passes).
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
 void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &p, cudaStream_t s);
-void launchOverflowSolve(const Dev &d, int capacity, const StepParams &p, bool inPlace, cudaStream_t s);
-void launchOverflowApply(const Dev &d, int capacity, const StepParams &p, cudaStream_t s);
+// Block-Jacobi solve of every dynamic body in the overflow colour (walked in slot order).
+void launchOverflowSolve(const Dev &d, int nBodies, const StepParams &p, bool inPlace, cudaStream_t s);
+void launchOverflowApply(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
 // Dual pass over live manifolds; with `stamps`, also the next round's stamps of manifolds whose
 // bodies are all overflow or static. `decay` < 1 scales penalties first (dual-only rounds).
 void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s);
@@ -51,6 +52,9 @@ void launchBrake(const Dev &d, int nWorlds, float window, cudaStream_t s);
 void launchProjection(const Dev &d, int nBodies, int nWorlds, const StepParams &p, cudaStream_t s);
 
 int brakeGridBlocks();
+int colourGridBlocks();
+// Kernel attributes and cooperative grid sizes, set once before any stream capture.
+void prepareKernels();
 
 // ---- host state exchange (k_io.cu) ----
 // Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).

@@ -375,6 +375,10 @@ static void segmentedSort(T *data, const int *start, int segCapacity, const int 
 
 static bool g_smemConfigured = false;
 
+static void configureSmem();
+
+void preparePrimitives() { configureSmem(); }
+
 static void configureSmem() {
     if (g_smemConfigured)
         return;

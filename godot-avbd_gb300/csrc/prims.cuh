@@ -35,6 +35,9 @@ void segmentedSortU64(uint64_t *data, uint64_t *tmp, const int *start, int segCa
 
 inline int divUp(int a, int b) { return (a + b - 1) / b; }
 
+// Kernel attributes the primitives need (large dynamic shared memory); call before any capture.
+void preparePrimitives();
+
 // Kernels this library launched from the calling host thread (each launch site increments it).
 inline int &launchCount() {
     thread_local int count = 0;

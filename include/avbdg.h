@@ -109,6 +109,9 @@ typedef struct avbdg_stats {
     int steps;                    /* steps taken since creation */
     /* last step, milliseconds: broad, graph (warm start + colouring + brake), solve, finish */
     double broad_ms, graph_ms, solve_ms, finish_ms, total_ms;
+    int manifold_sides;           /* (manifold, side) pairs whose body moves: stamps per round */
+    int graph_step;               /* 1 if the last step ran as one CUDA graph launch */
+    int kernel_launches;          /* kernels of this library in the last step */
 } avbdg_stats;
 
 /* ------------------------------------------------------------------------------------ */
@@ -258,6 +261,8 @@ int avbdg_batch_add_world(avbdg_batch *batch, int body_count, const avbdg_body_d
 int avbdg_batch_step(avbdg_batch *batch, int count);
 int avbdg_batch_sync(avbdg_batch *batch);
 int avbdg_batch_world_count(const avbdg_batch *batch, int *out);
+/* State of bodies [first, first+count) of `world` (creation order). world = -1 addresses all
+ * bodies of all worlds, worlds in creation order, so the whole batch moves in one copy. */
 int avbdg_batch_get_body_state(avbdg_batch *batch, int world, int first, int count, float *position,
                                float *orientation, float *velocity, float *angular_velocity);
 int avbdg_batch_set_body_state(avbdg_batch *batch, int world, int first, int count,
@@ -266,6 +271,8 @@ int avbdg_batch_set_body_state(avbdg_batch *batch, int world, int first, int cou
 int avbdg_batch_digest(avbdg_batch *batch, int world, uint64_t *out);
 /* Totals over all worlds; phase times of the last step. */
 int avbdg_batch_get_stats(avbdg_batch *batch, avbdg_stats *out);
+int avbdg_batch_set_profiling(avbdg_batch *batch, int enabled);
+int avbdg_batch_take_kernel_times(avbdg_batch *batch, avbdg_kernel_times *out);
 
 /* ------------------------------------------------------------------------------------ */
 /* Standalone kernels                                                                   */

@@ -147,6 +147,24 @@ def test_gpu_edge_cases(pkg, gpu, oracle):
     assert e.value.code == capi.ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+def test_gpu_graph_and_eager_steps(pkg, gpu, golden, monkeypatch, graphs):
+    """Steps run as one captured CUDA graph by default and eagerly when graphs are disabled; both
+    must reproduce the reference's recorded runs (joints + colouring + overflow: `mixed`)."""
+    scenes = pkg.scenes
+    monkeypatch.setenv("AVBDG_NO_GRAPHS", "0" if graphs else "1")
+    for run in ["mixed", "interleaved", "pyramid420"]:
+        rec = golden["runs"][run]
+        sc = getattr(scenes, rec["scene"])(**rec["kwargs"])
+        w = scenes.instantiate(gpu, sc)
+        for s in range(min(rec["steps"], 60)):
+            scenes.advance(w, sc, 1)
+            assert f"{w.digest():016x}" == rec["digests"][s], f"{run} step {s + 1} graphs={graphs}"
+        st = w.stats()
+        assert st.graph_step == (1 if graphs else 0), f"graph capture state: {st.graph_step}"
+        assert st.kernel_launches > 0
+
+
 def test_gpu_store_growth(pkg, gpu, oracle):
     """A world created with the smallest store grows while bodies arrive in chunks and while its
     pairs and manifolds outgrow their buffers; results stay identical to the oracle."""
