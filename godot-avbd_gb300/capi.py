@@ -96,6 +96,7 @@ class Stats(C.Structure):
         ("manifold_sides", C.c_int),
         ("graph_step", C.c_int),
         ("kernel_launches", C.c_int),
+        ("block_dual", C.c_int), ("block_solve", C.c_int), ("block_narrow", C.c_int), ("block_traverse", C.c_int),
     ]
 
 
@@ -410,6 +411,7 @@ class Batch:
             "batch_destroy": ([C.c_void_p]),
             "batch_add_world": ([C.c_void_p, C.c_int, C.POINTER(BodyDesc), C.c_int, C.POINTER(ForceDesc),
                                  C.POINTER(C.c_int)]),
+            "batch_remove_worlds": ([C.c_void_p, C.c_int, _ip]),
             "batch_step": ([C.c_void_p, C.c_int]),
             "batch_sync": ([C.c_void_p]),
             "batch_get_body_state": ([C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _fp]),
@@ -449,6 +451,12 @@ class Batch:
                                                    C.byref(out)))
         self.sizes.append(scene.n)
         return out.value
+
+    def remove_worlds(self, worlds):
+        ids = np.asarray(sorted(set(int(w) for w in worlds)), np.int32)
+        self._api.check(self.fn["batch_remove_worlds"](self.handle, len(ids), _ptr(ids, C.c_int32)))
+        drop = set(ids.tolist())
+        self.sizes = [n for i, n in enumerate(self.sizes) if i not in drop]
 
     def step(self, n=1):
         self._api.check(self.fn["batch_step"](self.handle, int(n)))
@@ -504,3 +512,110 @@ class Batch:
         s = Stats()
         self._api.check(self.fn["batch_get_stats"](self.handle, C.byref(s)))
         return s
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64), ("evicted", C.c_int64),
+        ("ticks", C.c_int64),
+        ("queued", C.c_int), ("resident", C.c_int), ("resident_bodies", C.c_int), ("resident_dynamic", C.c_int),
+        ("resident_bytes", C.c_uint64), ("store_bytes", C.c_uint64), ("budget_bytes", C.c_uint64),
+        ("body_steps", C.c_double), ("busy_ms", C.c_double),
+        ("tick_p50_ms", C.c_double), ("tick_p99_ms", C.c_double), ("tick_max_ms", C.c_double),
+        ("request_p50_ms", C.c_double), ("request_p99_ms", C.c_double),
+        ("admit_ms", C.c_double), ("step_ms", C.c_double), ("retire_ms", C.c_double), ("graph_ticks", C.c_int64),
+    ]
+
+
+class Server:
+    """Served form (avbdg_server_*): scenes queued as requests, admitted under a device byte budget,
+    resident between ticks, all stepped together once per tick, retired when their steps are done."""
+
+    def __init__(self, lib, params=None, budget_bytes=120 * 10**9, max_resident=4096):
+        self.lib = lib
+        self._api = Api(lib, "avbdg_")
+        p = self._api.default_params() if params is None else params
+        sig = {
+            "server_create": [C.POINTER(Params), C.c_uint64, C.c_int, C.POINTER(C.c_void_p)],
+            "server_destroy": [C.c_void_p],
+            "server_admit": [C.c_void_p, C.c_int, C.POINTER(BodyDesc), C.c_int, C.POINTER(ForceDesc), C.c_int,
+                             C.POINTER(C.c_int64)],
+            "server_tick": [C.c_void_p, C.POINTER(C.c_int)],
+            "server_poll": [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int)],
+            "server_take_result": [C.c_void_p, C.c_int64, C.c_int, _fp, _fp, _fp, _fp],
+            "server_evict": [C.c_void_p, C.c_int64],
+            "server_get_stats": [C.c_void_p, C.POINTER(ServerStats)],
+            "server_reset_stats": [C.c_void_p],
+        }
+        self.fn = {}
+        for name, argtypes in sig.items():
+            f = getattr(lib, "avbdg_" + name)
+            f.argtypes = argtypes
+            f.restype = C.c_int
+            self.fn[name] = f
+        h = C.c_void_p()
+        self._api.check(self.fn["server_create"](C.byref(p), int(budget_bytes), int(max_resident), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.fn["server_destroy"](self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def admit(self, scene, steps, descs=None, forces=None):
+        """Queue `scene` for `steps` steps; returns the request id. Pre-packed descriptor arrays
+        (make_body_descs / make_force_descs) may be passed to keep packing out of a timed loop."""
+        if descs is None:
+            descs = make_body_descs(scene.size, scene.density, scene.friction, scene.position, scene.orientation,
+                                    scene.velocity)
+        if forces is None:
+            forces = make_force_descs(scene.joints)
+        out = C.c_int64()
+        self._api.check(self.fn["server_admit"](self.handle, scene.n, descs, len(scene.joints), forces, int(steps),
+                                                C.byref(out)))
+        return out.value
+
+    def tick(self):
+        done = C.c_int()
+        self._api.check(self.fn["server_tick"](self.handle, C.byref(done)))
+        return done.value
+
+    def poll(self):
+        rid, n = C.c_int64(), C.c_int()
+        self._api.check(self.fn["server_poll"](self.handle, C.byref(rid), C.byref(n)))
+        return rid.value, n.value
+
+    def take_result(self, request, n):
+        p = np.zeros((n, 3), np.float32)
+        q = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        w = np.zeros((n, 3), np.float32)
+        self._api.check(self.fn["server_take_result"](self.handle, int(request), n, _ptr(p, C.c_float),
+                                                      _ptr(q, C.c_float), _ptr(v, C.c_float), _ptr(w, C.c_float)))
+        return p, q, v, w
+
+    def results(self):
+        """Take every finished result: {request id: (position, orientation, velocity, angular)}."""
+        out = {}
+        while True:
+            rid, n = self.poll()
+            if rid < 0:
+                return out
+            out[rid] = self.take_result(rid, n)
+
+    def evict(self, request):
+        self._api.check(self.fn["server_evict"](self.handle, int(request)))
+
+    def stats(self):
+        s = ServerStats()
+        self._api.check(self.fn["server_get_stats"](self.handle, C.byref(s)))
+        return s
+
+    def reset_stats(self):
+        self._api.check(self.fn["server_reset_stats"](self.handle))

@@ -8,6 +8,7 @@
 
 #include "avbdg.h"
 #include "engine_host.hpp"
+#include "server.hpp"
 
 struct avbdg_world {
     avbdg::Engine engine;
@@ -19,6 +20,11 @@ struct avbdg_batch {
     avbdg_batch(const avbdg_params &p, int nw, int nb, int nf) : engine(p, nb, nf, nw) {}
 };
 
+struct avbdg_server {
+    avbdg::Server server;
+    avbdg_server(const avbdg_params &p, uint64_t budget, int maxResident) : server(p, budget, maxResident) {}
+};
+
 namespace {
 
 thread_local std::string g_lastError;
@@ -27,6 +33,8 @@ int record(int rc, const avbdg::Engine *e) {
     if (rc != AVBDG_OK && e)
         g_lastError = e->error();
     return rc;
+}
+
 }
 
 int failWith(int rc, const char *msg) {
@@ -48,6 +56,23 @@ int guarded(H *w, F &&fn) {
         return failWith(AVBDG_ERR_INVALID, "unknown error");
     }
 }
+
+template <typename F>
+int serverCall(avbdg_server *s, F &&fn) {
+    if (!s)
+        return failWith(AVBDG_ERR_INVALID, "null handle");
+    try {
+        const int rc = fn(s->server);
+        if (rc != AVBDG_OK)
+            g_lastError = s->server.error();
+        return rc;
+    } catch (const std::bad_alloc &) {
+        return failWith(AVBDG_ERR_CAPACITY, "host allocation failed");
+    } catch (const std::exception &ex) {
+        return failWith(AVBDG_ERR_INVALID, ex.what());
+    } catch (...) {
+        return failWith(AVBDG_ERR_INVALID, "unknown error");
+    }
 
 } // namespace
 
@@ -253,23 +278,30 @@ int avbdg_batch_add_world(avbdg_batch *b, int nb, const avbdg_body_desc *bodies,
     if (nf < 0 || (nf > 0 && !forces))
         return failWith(AVBDG_ERR_INVALID, "bad force array");
     return guarded(b, [=](avbdg::Engine &e) {
+        std::string why;
+        int rc = avbdg::Engine::validateBodies(nb, bodies, why);
+        if (rc == AVBDG_OK)
+            rc = avbdg::Engine::validateForces(nb, nf, forces, why);
+        if (rc != AVBDG_OK) {
+            g_lastError = why;
+            return rc;
+        }
         const int w = e.addWorld();
         if (w < 0)
             return AVBDG_ERR_CAPACITY;
-        int rc = e.addBodies(w, nb, bodies, nullptr);
-        for (int i = 0; rc == AVBDG_OK && i < nf; i++) {
-            const avbdg_force_desc &f = forces[i];
-            if (f.kind == 0)
-                rc = e.addJoint(w, f.body_a, f.body_b, f.r_a, f.r_b, f.stiffness_lin, f.stiffness_ang, f.fracture);
-            else if (f.kind == 1)
-                rc = e.addIgnore(w, f.body_a, f.body_b);
-            else
-                rc = AVBDG_ERR_UNSUPPORTED;
-        }
+        rc = e.addBodies(w, nb, bodies, nullptr);
+        if (rc == AVBDG_OK)
+            rc = e.addForces(w, nf, forces);
         if (rc == AVBDG_OK && outWorld)
             *outWorld = w;
         return rc;
     });
+}
+
+int avbdg_batch_remove_worlds(avbdg_batch *b, int count, const int *worlds) {
+    if (count < 0 || (count > 0 && !worlds))
+        return failWith(AVBDG_ERR_INVALID, "bad world list");
+    return guarded(b, [=](avbdg::Engine &e) { return e.removeWorlds(std::vector<int>(worlds, worlds + count)); });
 }
 
 int avbdg_batch_step(avbdg_batch *b, int count) {
@@ -362,6 +394,99 @@ int avbdg_world_dump_manifolds(avbdg_world *w, int cap, int32_t *ba, int32_t *bb
 
 int avbdg_world_dump_colours(avbdg_world *w, int cap, uint8_t *colour, int32_t *ids, int *count) {
     return guarded(w, [=](avbdg::Engine &e) { return e.dumpColours(cap, colour, ids, count); });
+}
+
+int avbdg_server_create(const avbdg_params *params, uint64_t budget_bytes, int max_resident, avbdg_server **out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    *out = nullptr;
+    if (budget_bytes == 0 || max_resident < 1)
+        return failWith(AVBDG_ERR_INVALID, "the budget and the resident limit must be positive");
+    avbdg_params p;
+    if (params)
+        p = *params;
+    else
+        avbdg_params_default(&p);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        return failWith(AVBDG_ERR_CUDA, "no CUDA device: the GPU step has no CPU fallback");
+    try {
+        avbdg_server *s = new avbdg_server(p, budget_bytes, max_resident);
+        const int rc = s->server.engine().setParams(p);
+        if (rc != AVBDG_OK) {
+            g_lastError = s->server.engine().error();
+            delete s;
+            return rc;
+        }
+        *out = s;
+        return AVBDG_OK;
+    } catch (const std::bad_alloc &) {
+        return failWith(AVBDG_ERR_CAPACITY, "host allocation failed");
+    }
+}
+
+int avbdg_server_destroy(avbdg_server *s) {
+    if (!s)
+        return failWith(AVBDG_ERR_INVALID, "null handle");
+    delete s;
+    return AVBDG_OK;
+}
+
+int avbdg_server_admit(avbdg_server *s, int nb, const avbdg_body_desc *bodies, int nf, const avbdg_force_desc *forces,
+                       int steps, int64_t *out) {
+    return serverCall(s, [=](avbdg::Server &srv) {
+        int64_t id = -1;
+        const int rc = srv.admit(nb, bodies, nf, forces, steps, id);
+        if (out)
+            *out = id;
+        return rc;
+    });
+}
+
+int avbdg_server_tick(avbdg_server *s, int *completed) {
+    return serverCall(s, [=](avbdg::Server &srv) {
+        int done = 0;
+        const int rc = srv.tick(done);
+        if (completed)
+            *completed = done;
+        return rc;
+    });
+}
+
+int avbdg_server_poll(avbdg_server *s, int64_t *outRequest, int *outBodies) {
+    if (!outRequest)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return serverCall(s, [=](avbdg::Server &srv) {
+        int n = 0;
+        srv.poll(*outRequest, n);
+        if (outBodies)
+            *outBodies = n;
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_server_take_result(avbdg_server *s, int64_t request, int count, float *p, float *q, float *v, float *w) {
+    return serverCall(s, [=](avbdg::Server &srv) { return srv.takeResult(request, count, p, q, v, w); });
+}
+
+int avbdg_server_evict(avbdg_server *s, int64_t request) {
+    return serverCall(s, [=](avbdg::Server &srv) { return srv.evict(request); });
+}
+
+int avbdg_server_get_stats(avbdg_server *s, avbdg_server_stats *out) {
+    if (!out)
+        return failWith(AVBDG_ERR_INVALID, "null output");
+    return serverCall(s, [=](avbdg::Server &srv) {
+        srv.stats(*out);
+        return AVBDG_OK;
+    });
+}
+
+int avbdg_server_reset_stats(avbdg_server *s) {
+    return serverCall(s, [](avbdg::Server &srv) {
+        srv.resetStats();
+        return AVBDG_OK;
+    });
 }
 
 } // extern "C"

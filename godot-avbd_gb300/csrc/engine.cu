@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "prims.cuh"
@@ -34,11 +35,124 @@ bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1])
 
 constexpr int kRefitBudget = 16; // src/avbd/bvh_broadphase.hpp:40
 
+// Every device buffer of a store, in one place: `take(ptr, count)` allocates (or counts) `count`
+// elements of ptr's type.
+template <typename Take>
+void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
+    n.NB = nb;
+    n.MM = mm;
+    n.FF = ff;
+    n.PP = pp;
+    n.WW = ww;
+    take(n.wBase, ww);
+    take(n.wCount, ww);
+    take(n.wMaxDepth, ww);
+    take(n.wStop, ww);
+    take(n.wBounds, 6 * static_cast<size_t>(ww));
+    take(n.wActive, ww);
+    take(n.wColour, ww);
+    take(n.x, nb);
+    take(n.q, nb);
+    take(n.x0, nb);
+    take(n.q0, nb);
+    take(n.xi, nb);
+    take(n.qi, nb);
+    take(n.v, nb);
+    take(n.w, nb);
+    take(n.vprev, nb);
+    take(n.size, nb);
+    take(n.moment, nb);
+    take(n.meta, nb);
+    take(n.lpToBody, nb);
+    take(n.contactOnly, nb);
+    take(n.colour, nb);
+    take(n.aabbC, nb);
+    take(n.aabbH, nb);
+    take(n.codes, nb);
+    take(n.treeCodes, nb);
+    take(n.sortK, nb);
+    take(n.sortKAlt, nb);
+    take(n.sortV, nb);
+    take(n.sortVAlt, nb);
+    take(n.leafBody, nb);
+    take(n.nodeL, nb);
+    take(n.nodeR, nb);
+    take(n.nodeParent, nb);
+    take(n.leafParent, nb);
+    take(n.nodeFlag, nb);
+    take(n.nodeMaxLp, nb);
+    take(n.nodeMin, nb);
+    take(n.nodeMax, nb);
+    take(n.pairStart, static_cast<size_t>(nb) + 1);
+    take(n.pairs, pp);
+    take(n.pairsTmp, pp);
+    const int flagsCap = std::max(pp, mm);
+    take(n.pairValid, flagsCap);
+    take(n.mActive, flagsCap);
+    for (ManifoldBuf *b : {&n.live, &n.stage}) {
+        take(b->ab, mm);
+        take(b->b0, mm);
+        take(b->b1, mm);
+        take(b->b2, mm);
+        take(b->count, mm);
+        const size_t mc = static_cast<size_t>(mm) * kMaxContacts;
+        take(b->key, mc);
+        take(b->rA, mc);
+        take(b->rB, mc);
+        take(b->C0, mc);
+        take(b->k, mc);
+        take(b->lam, mc);
+    }
+    take(n.stamps, static_cast<size_t>(mm) * 2 * kStampF4);
+    take(n.mSpec, mm);
+    take(n.mDone, mm);
+    take(n.specList, mm);
+    take(n.specPred, mm);
+    take(n.projLin, 2 * static_cast<size_t>(mm));
+    take(n.projAng, 2 * static_cast<size_t>(mm));
+    take(n.dLin, nb);
+    take(n.dAng, nb);
+    take(n.fAB, ff);
+    take(n.fRA, ff);
+    take(n.fRB, ff);
+    take(n.fC0L, ff);
+    take(n.fC0A, ff);
+    take(n.fKL, ff);
+    take(n.fKA, ff);
+    take(n.fLL, ff);
+    take(n.fLA, ff);
+    take(n.fPar, ff);
+    take(n.fKind, ff);
+    take(n.fBroken, ff);
+    take(n.fKeep, ff);
+    take(n.adjStart, static_cast<size_t>(nb) + 1);
+    take(n.adjFill, nb);
+    const size_t adjCap = 2 * (static_cast<size_t>(ff) + mm);
+    take(n.adjSeq, adjCap);
+    take(n.adjTmp, adjCap);
+    take(n.colourList, static_cast<size_t>(nb) * (kMaxColours + 1));
+    take(n.colourCount, kMaxColours + 1);
+    take(n.ctr, C_COUNT);
+    take(n.longList, static_cast<size_t>(std::max(nb, 1)) + 1);
+    const int scanCap = std::max({pp, mm, nb + 1, 2 * (ff + mm)}) + 1;
+    char *scan = nullptr, *radix = nullptr;
+    take(scan, scanScratchBytes(scanCap));
+    take(radix, radixScratchBytes(nb + 1));
+    n.scanScratch = scan;
+    n.radixScratch = radix;
+    take(n.relocInt, static_cast<size_t>(nb) + ff);
+    take(n.relocF4, std::max(nb, ff));
+    take(n.relocRemap, 2 * static_cast<size_t>(ww));
+}
+
 } // namespace
 
 Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int maxWorlds) : P(params) {
     const char *noGraphs = std::getenv("AVBDG_NO_GRAPHS");
     useGraphs = !(noGraphs && noGraphs[0] == '1');
+    const char *noTune = std::getenv("AVBDG_NO_TUNE");
+    tuneEnabled = !(noTune && noTune[0] == '1');
+    armTuning();
     prepareKernels(); // attributes and occupancy queries, never during a capture
     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
     for (auto &e : ev)
@@ -98,102 +212,10 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
     std::vector<void *> oldAllocs;
     oldAllocs.swap(allocs);
     Dev n{};
-    n.NB = nb;
-    n.MM = mm;
-    n.FF = ff;
-    n.PP = pp;
-    n.WW = ww;
-    n.wBase = dalloc<int>(ww);
-    n.wCount = dalloc<int>(ww);
-    n.wMaxDepth = dalloc<int>(ww);
-    n.wStop = dalloc<int>(ww);
-    n.wBounds = dalloc<int>(6 * static_cast<size_t>(ww));
-    n.wActive = dalloc<int>(ww);
-    n.x = dalloc<float4>(nb);
-    n.q = dalloc<float4>(nb);
-    n.x0 = dalloc<float4>(nb);
-    n.q0 = dalloc<float4>(nb);
-    n.xi = dalloc<float4>(nb);
-    n.qi = dalloc<float4>(nb);
-    n.v = dalloc<float4>(nb);
-    n.w = dalloc<float4>(nb);
-    n.vprev = dalloc<float4>(nb);
-    n.size = dalloc<float4>(nb);
-    n.moment = dalloc<float4>(nb);
-    n.meta = dalloc<int4>(nb);
-    n.lpToBody = dalloc<int>(nb);
-    n.contactOnly = dalloc<uint8_t>(nb);
-    n.colour = dalloc<uint8_t>(nb);
-    n.aabbC = dalloc<float4>(nb);
-    n.aabbH = dalloc<float4>(nb);
-    n.codes = dalloc<uint64_t>(nb);
-    n.sortK = dalloc<uint64_t>(nb);
-    n.sortKAlt = dalloc<uint64_t>(nb);
-    n.sortV = dalloc<uint32_t>(nb);
-    n.sortVAlt = dalloc<uint32_t>(nb);
-    n.leafBody = dalloc<int>(nb);
-    n.nodeL = dalloc<int>(nb);
-    n.nodeR = dalloc<int>(nb);
-    n.nodeParent = dalloc<int>(nb);
-    n.leafParent = dalloc<int>(nb);
-    n.nodeFlag = dalloc<int>(nb);
-    n.nodeMaxLp = dalloc<int>(nb);
-    n.nodeMin = dalloc<float4>(nb);
-    n.nodeMax = dalloc<float4>(nb);
-    n.pairStart = dalloc<int>(static_cast<size_t>(nb) + 1);
-    n.pairs = dalloc<uint64_t>(pp);
-    n.pairsTmp = dalloc<uint64_t>(pp);
-    const int flagsCap = std::max(pp, mm);
-    n.pairValid = dalloc<int>(flagsCap);
-    n.mActive = dalloc<int>(flagsCap);
-    for (ManifoldBuf *b : {&n.live, &n.stage}) {
-        b->ab = dalloc<int2>(mm);
-        b->b0 = dalloc<float4>(mm);
-        b->b1 = dalloc<float4>(mm);
-        b->b2 = dalloc<float4>(mm);
-        b->count = dalloc<int>(mm);
-        const size_t mc = static_cast<size_t>(mm) * kMaxContacts;
-        b->key = dalloc<int>(mc);
-        b->rA = dalloc<float4>(mc);
-        b->rB = dalloc<float4>(mc);
-        b->C0 = dalloc<float4>(mc);
-        b->k = dalloc<float4>(mc);
-        b->lam = dalloc<float4>(mc);
-    }
-    n.stamps = dalloc<float4>(static_cast<size_t>(mm) * 2 * kStampF4);
-    n.mSpec = dalloc<uint8_t>(mm);
-    n.mDone = dalloc<uint8_t>(mm);
-    n.specList = dalloc<int>(mm);
-    n.projLin = dalloc<float4>(2 * static_cast<size_t>(mm));
-    n.projAng = dalloc<float4>(2 * static_cast<size_t>(mm));
-    n.dLin = dalloc<float4>(nb);
-    n.dAng = dalloc<float4>(nb);
-    n.fAB = dalloc<int2>(ff);
-    n.fRA = dalloc<float4>(ff);
-    n.fRB = dalloc<float4>(ff);
-    n.fC0L = dalloc<float4>(ff);
-    n.fC0A = dalloc<float4>(ff);
-    n.fKL = dalloc<float4>(ff);
-    n.fKA = dalloc<float4>(ff);
-    n.fLL = dalloc<float4>(ff);
-    n.fLA = dalloc<float4>(ff);
-    n.fPar = dalloc<float4>(ff);
-    n.fKind = dalloc<int>(ff);
-    n.fBroken = dalloc<int>(ff);
-    n.fKeep = dalloc<int>(ff);
-    n.adjStart = dalloc<int>(static_cast<size_t>(nb) + 1);
-    n.adjFill = dalloc<int>(nb);
-    const size_t adjCap = 2 * (static_cast<size_t>(ff) + mm);
-    n.adjSeq = dalloc<uint32_t>(adjCap);
-    n.adjTmp = dalloc<uint32_t>(adjCap);
-    n.colourList = dalloc<int>(static_cast<size_t>(nb) * (kMaxColours + 1));
-    n.colourCount = dalloc<int>(kMaxColours + 1);
-    n.ctr = dalloc<int>(C_COUNT);
-    n.longList = dalloc<int>(static_cast<size_t>(std::max(nb, 1)) + 1);
-    const int scanCap = std::max({pp, mm, nb + 1, 2 * (ff + mm)}) + 1;
-    n.scanScratch = dalloc<char>(scanScratchBytes(scanCap));
-    n.radixScratch = dalloc<char>(radixScratchBytes(nb + 1));
-    n.barrier = dalloc<unsigned>(2);
+    layoutStore(n, nb, mm, ff, pp, ww, [this](auto *&ptr, size_t count) {
+        using T = std::remove_reference_t<decltype(*ptr)>;
+        ptr = dalloc<T>(count);
+    });
 
     if (old.NB > 0) {
         // Carry the persistent state into the new store.
@@ -243,6 +265,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         ioCap = 0;
         treeValid = false;
         adjValid = false;
+        armTuning(); // sizes changed: tune again
     }
     d = n;
     if (!wBase.empty()) {
@@ -252,14 +275,66 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
     cudaStreamSynchronize(stream);
 }
 
+size_t Engine::storeBytes(int nb, int mm, int ff, int pp, int ww) {
+    size_t total = 0;
+    Dev n{};
+    layoutStore(n, nb, mm, ff, pp, ww, [&total](auto *&ptr, size_t count) {
+        using T = std::remove_reference_t<decltype(*ptr)>;
+        total += (std::max<size_t>(count, 1) * sizeof(T) + 255) / 256 * 256; // cudaMalloc granularity
+        ptr = nullptr;
+    });
+    return total;
+}
+
 int Engine::ensureCapacity(int nb, int ff, int ww) {
     if (nb <= d.NB && ff <= d.FF && ww <= d.WW)
         return AVBDG_OK;
-    const int nnb = nb <= d.NB ? d.NB : std::max(nb, 2 * d.NB);
-    const int nff = ff <= d.FF ? d.FF : std::max(ff, 2 * d.FF);
-    const int nww = ww <= d.WW ? d.WW : std::max(ww, 2 * d.WW);
+    int nnb = nb <= d.NB ? d.NB : std::max(nb, 2 * d.NB);
+    int nff = ff <= d.FF ? d.FF : std::max(ff, 2 * d.FF);
+    int nww = ww <= d.WW ? d.WW : std::max(ww, 2 * d.WW);
+    if (!fits(nnb, std::max(d.MM, 8 * nnb), nff, std::max(d.PP, 16 * nnb), nww)) {
+        // No headroom under the byte limit: grow to exactly what is needed, or refuse.
+        nnb = std::max(nb, d.NB);
+        nff = std::max(ff, d.FF);
+        nww = std::max(ww, d.WW);
+        if (!fits(nnb, std::max(d.MM, 8 * nnb), nff, std::max(d.PP, 16 * nnb), nww))
+            return fail(AVBDG_ERR_CAPACITY, "the store would exceed its device byte limit");
+    }
     allocate(nnb, std::max(d.MM, 8 * nnb), nff, std::max(d.PP, 16 * nnb), nww);
     return cudaCheck("grow");
+}
+
+int Engine::validateBodies(int count, const avbdg_body_desc *descs, std::string &why) {
+    for (int i = 0; i < count; i++) {
+        const avbdg_body_desc &b = descs[i];
+        if (b.shape != AVBDG_SHAPE_BOX) {
+            why = "only box bodies run on the GPU path";
+            return AVBDG_ERR_UNSUPPORTED;
+        }
+        if (!finite3(b.size) || !finite3(b.position) || !finite3(b.velocity) || !finite3(b.angular_velocity) ||
+            !std::isfinite(b.density) || !std::isfinite(b.friction) || !std::isfinite(b.orientation[0]) ||
+            !std::isfinite(b.orientation[1]) || !std::isfinite(b.orientation[2]) || !std::isfinite(b.orientation[3])) {
+            why = "non-finite body description";
+            return AVBDG_ERR_NONFINITE;
+        }
+    }
+    return AVBDG_OK;
+}
+
+int Engine::validateForces(int nb, int count, const avbdg_force_desc *descs, std::string &why) {
+    for (int i = 0; i < count; i++) {
+        const avbdg_force_desc &f = descs[i];
+        if (f.kind != 0 && f.kind != 1) {
+            why = "only ball joints and ignore pairs run on the GPU path";
+            return AVBDG_ERR_UNSUPPORTED;
+        }
+        const int aMin = f.kind == 0 ? -1 : 0;
+        if (f.body_b < 0 || f.body_b >= nb || f.body_a < aMin || f.body_a >= nb) {
+            why = "bad body index";
+            return AVBDG_ERR_INVALID;
+        }
+    }
+    return AVBDG_OK;
 }
 
 int Engine::addWorld() {
@@ -267,28 +342,23 @@ int Engine::addWorld() {
         return -1;
     wBase.push_back(nBodies);
     wCount.push_back(0);
+    wDyn.push_back(0);
     const int w = worlds() - 1;
     cudaMemcpyAsync(d.wBase + w, &wBase[w], sizeof(int), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.wCount + w, &wCount[w], sizeof(int), cudaMemcpyHostToDevice, stream);
+    uploadCounts();
     cudaStreamSynchronize(stream);
     return w;
 }
 
 int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outIds) {
-    dropGraphs();
     if (w < 0 || w >= worlds() || count < 0 || (count > 0 && !descs))
         return fail(AVBDG_ERR_INVALID, "bad world or body array");
     if (w != worlds() - 1)
         return fail(AVBDG_ERR_INVALID, "only the most recently created world can receive bodies");
-    for (int i = 0; i < count; i++) {
-        const avbdg_body_desc &b = descs[i];
-        if (b.shape != AVBDG_SHAPE_BOX)
-            return fail(AVBDG_ERR_UNSUPPORTED, "only box bodies run on the GPU path");
-        if (!finite3(b.size) || !finite3(b.position) || !finite3(b.velocity) || !finite3(b.angular_velocity) ||
-            !std::isfinite(b.density) || !std::isfinite(b.friction) || !std::isfinite(b.orientation[0]) ||
-            !std::isfinite(b.orientation[1]) || !std::isfinite(b.orientation[2]) || !std::isfinite(b.orientation[3]))
-            return fail(AVBDG_ERR_NONFINITE, "non-finite body description");
-    }
+    std::string why;
+    if (const int bad = validateBodies(count, descs, why))
+        return fail(bad, why);
     if (count == 0)
         return AVBDG_OK;
     int rc = ensureCapacity(nBodies + count, nForces, worlds());
@@ -312,8 +382,10 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
         zero4[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
         if (outIds)
             outIds[i] = first - wBase[w] + i;
-        if (mass > 0.0f)
+        if (mass > 0.0f) {
             nDynamic++;
+            wDyn[w]++;
+        }
     }
     const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
     cudaMemcpyAsync(d.x + first, x.data(), b4, cudaMemcpyHostToDevice, stream);
@@ -333,6 +405,7 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
         lp[i] = wBase[w] + wCount[w] - 1 - i; // list position wBase + i holds body (base + count - 1 - i)
     cudaMemcpyAsync(d.lpToBody + wBase[w], lp.data(), sizeof(int) * lp.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.wCount + w, &wCount[w], sizeof(int), cudaMemcpyHostToDevice, stream);
+    uploadCounts();
     cudaStreamSynchronize(stream);
     treeValid = false;
     adjValid = false;
@@ -341,7 +414,6 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
 
 int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], float kLin, float kAng,
                      float fracture) {
-    dropGraphs();
     if (w < 0 || w >= worlds() || b < 0 || b >= wCount[w] || a < -1 || a >= wCount[w] || !rA || !rB)
         return fail(AVBDG_ERR_INVALID, "bad body index");
     int rc = ensureCapacity(nBodies, nForces + 1, worlds());
@@ -382,7 +454,6 @@ int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], 
 }
 
 int Engine::addIgnore(int w, int a, int b) {
-    dropGraphs();
     if (w < 0 || w >= worlds() || a < 0 || b < 0 || a >= wCount[w] || b >= wCount[w])
         return fail(AVBDG_ERR_INVALID, "bad body index");
     int rc = ensureCapacity(nBodies, nForces + 1, worlds());
@@ -404,17 +475,134 @@ int Engine::addIgnore(int w, int a, int b) {
     return cudaCheck("addIgnore");
 }
 
+// Bulk form of addJoint/addIgnore: the same records, appended in the same order, with the joints'
+// torque arms computed from one download of the world's body sizes.
+int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
+    if (w < 0 || w >= worlds() || count < 0 || (count > 0 && !descs))
+        return fail(AVBDG_ERR_INVALID, "bad world or force array");
+    if (count == 0)
+        return AVBDG_OK;
+    const int n = wCount[w];
+    std::string why;
+    if (const int bad = validateForces(n, count, descs, why))
+        return fail(bad, why);
+    int rc = ensureCapacity(nBodies, nForces + count, worlds());
+    if (rc)
+        return rc;
+    std::vector<float4> sizes(n);
+    cudaMemcpy(sizes.data(), d.size + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    std::vector<int2> ab(count);
+    std::vector<float4> ra(count), rb(count), par(count), zero(count, make_float4(0, 0, 0, 0));
+    std::vector<int> kind(count), broken(count, 0);
+    for (int i = 0; i < count; i++) {
+        const avbdg_force_desc &f = descs[i];
+        kind[i] = f.kind;
+        ab[i] = make_int2(f.body_a >= 0 ? wBase[w] + f.body_a : -1, wBase[w] + f.body_b);
+        if (f.kind == 0) {
+            // torqueArm = length2((A ? A.size : 0) + B.size) (joint.cpp:38-39), as in addJoint.
+            const float4 sa = f.body_a >= 0 ? sizes[f.body_a] : make_float4(0, 0, 0, 0);
+            const float4 sb = sizes[f.body_b];
+            const float tx = sa.x + sb.x, ty = sa.y + sb.y, tz = sa.z + sb.z;
+            const float px = tx * tx, py = ty * ty, pz = tz * tz;
+            float arm = 0.0f;
+            arm = arm + px;
+            arm = arm + py;
+            arm = arm + pz;
+            ra[i] = make_float4(f.r_a[0], f.r_a[1], f.r_a[2], 0.0f);
+            rb[i] = make_float4(f.r_b[0], f.r_b[1], f.r_b[2], 0.0f);
+            par[i] = make_float4(f.stiffness_lin, f.stiffness_ang, f.fracture, arm);
+        } else {
+            ra[i] = rb[i] = par[i] = make_float4(0, 0, 0, 0);
+        }
+    }
+    const int f0 = nForces;
+    const size_t b4 = sizeof(float4) * static_cast<size_t>(count), bi = sizeof(int) * static_cast<size_t>(count);
+    cudaMemcpyAsync(d.fAB + f0, ab.data(), sizeof(int2) * static_cast<size_t>(count), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fRA + f0, ra.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fRB + f0, rb.data(), b4, cudaMemcpyHostToDevice, stream);
+    for (float4 *arr : {d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA})
+        cudaMemcpyAsync(arr + f0, zero.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fPar + f0, par.data(), b4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fKind + f0, kind.data(), bi, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fBroken + f0, broken.data(), bi, cudaMemcpyHostToDevice, stream);
+    nForces += count;
+    cudaMemcpyAsync(d.ctr + C_FORCES, &nForces, sizeof(int), cudaMemcpyHostToDevice, stream);
+    cudaStreamSynchronize(stream);
+    adjValid = false;
+    return cudaCheck("addForces");
+}
+
+// World removal between steps: one slot map, a device move of the survivors, a stable
+// compaction of the manifold and force lists, then the new world table.
+int Engine::removeWorlds(const std::vector<int> &ids) {
+    const int nw = worlds();
+    std::vector<char> drop(nw, 0);
+    for (int w : ids) {
+        if (w < 0 || w >= nw)
+            return fail(AVBDG_ERR_INVALID, "bad world");
+        drop[w] = 1;
+    }
+    if (ids.empty())
+        return AVBDG_OK;
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("removeWorlds");
+    std::vector<int> remap(2 * static_cast<size_t>(nw)), base, count, dyn;
+    int nb = 0, ndyn = 0;
+    for (int w = 0; w < nw; w++) {
+        if (drop[w]) {
+            remap[2 * w] = -1;
+            remap[2 * w + 1] = 0;
+            continue;
+        }
+        remap[2 * w] = static_cast<int>(base.size());
+        remap[2 * w + 1] = nb;
+        base.push_back(nb);
+        count.push_back(wCount[w]);
+        dyn.push_back(wDyn[w]);
+        nb += wCount[w];
+        ndyn += wDyn[w];
+    }
+    cudaMemcpyAsync(d.relocRemap, remap.data(), sizeof(int) * remap.size(), cudaMemcpyHostToDevice, stream);
+    launchRelocateWorlds(d, nBodies, nb, nForces, d.relocRemap, stream);
+    wBase.swap(base);
+    wCount.swap(count);
+    wDyn.swap(dyn);
+    if (!wBase.empty()) {
+        cudaMemcpyAsync(d.wBase, wBase.data(), wBase.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d.wCount, wCount.data(), wCount.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
+    }
+    nBodies = nb;
+    uploadCounts();
+    launchListPositions(d, nb, stream);
+    cudaMemcpyAsync(hostCtr, d.ctr, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("removeWorlds");
+    nDynamic = ndyn;
+    nForces = hostCtr[C_FORCES];
+    treeValid = false;
+    adjValid = false;
+    return cudaCheck("removeWorlds");
+}
+
 void Engine::clear() {
     cudaStreamSynchronize(stream);
     dropGraphs();
     wBase.clear();
     wCount.clear();
+    wDyn.clear();
     nBodies = nDynamic = nForces = 0;
     cudaMemsetAsync(d.ctr, 0, sizeof(int) * C_COUNT, stream);
     cudaStreamSynchronize(stream);
     treeValid = adjValid = false;
     treeAge = 0;
     steps = 0;
+}
+
+// Body and world counts the step's kernels read from the device.
+void Engine::uploadCounts() {
+    const int counts[2] = {nBodies, worlds()};
+    static_assert(C_WORLDS == C_BODIES + 1, "counts are uploaded together");
+    cudaMemcpyAsync(d.ctr + C_BODIES, counts, sizeof(counts), cudaMemcpyHostToDevice, stream);
 }
 
 int Engine::setParams(const avbdg_params &p) {
@@ -481,13 +669,14 @@ Engine::StepPlan Engine::planStep(int mode, int substeps, int rounds) {
     adjValid = true; // the step rebuilds the adjacency after warm starting
     plan.forces = nForces > 0;
     plan.greedy = needGreedy();
+    plan.multiWorld = worlds() > 1;
     return plan;
 }
 
 std::string Engine::StepPlan::key() const {
     char buf[128];
-    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0, anyTree ? 1 : 0,
-                  rebuild ? 1 : 0, forces ? 1 : 0, greedy ? 1 : 0);
+    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0,
+                  anyTree ? 1 : 0, rebuild ? 1 : 0, forces ? 1 : 0, greedy ? 1 : 0, multiWorld ? 1 : 0);
     return buf;
 }
 
@@ -500,17 +689,19 @@ void Engine::recordPhase(cudaEvent_t e) {
 
 int Engine::broadPhase(const StepParams &sp, const StepPlan &plan) {
     if (plan.adjAtStart)
-        launchAdjacency(d, nBodies, stream);
-    launchAabb(d, nBodies, sp, stream);
+        launchAdjacency(d, stream);
+    launchAabb(d, sp, stream);
     if (!plan.anyTree) {
         cudaMemsetAsync(d.ctr + C_PAIRS, 0, sizeof(int), stream);
         cudaMemcpyAsync(d.ctr + C_CAND, d.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToDevice, stream);
         return AVBDG_OK;
     }
     if (plan.rebuild)
-        launchRebuildTree(d, nBodies, worlds(), stream);
-    launchRefit(d, nBodies, stream);
-    launchPairs(d, nBodies, stream);
+        launchRebuildTree(d, plan.multiWorld, stream);
+    launchRefit(d, stream);
+    beginSpan();
+    launchPairs(d, tuned.traverse, stream);
+    endSpan(kTraverse);
     launchFilterAcquire(d, stream);
     return AVBDG_OK;
 }
@@ -556,6 +747,7 @@ void Engine::dropGraphs() {
         }
     }
     graphs.clear();
+    planSeen.clear();
     graphSpans = nullptr;
 }
 
@@ -566,10 +758,19 @@ int Engine::runPlan(const StepPlan &plan) {
     graphSpans = nullptr;
     lastGraph = false;
     cudaEventRecord(ev[0], stream);
-    if (useGraphs) {
+    const bool trial = tuning && tuneTrial >= 0;
+    if (trial)
+        configureTrial();
+    if (useGraphs && !trial) {
         const std::string k = plan.key() + (profiling ? "/profiled" : "");
         auto it = graphs.find(k);
-        if (it == graphs.end()) {
+        // A plan runs eagerly the first time it is seen after the cache was dropped and is
+        // captured when it comes back, so plans that never recur cost no capture. Body and world
+        // counts are read on the device, so adding or removing worlds keeps the cache.
+        const bool capture = it == graphs.end() && planSeen[k]++ > 0;
+        if (it == graphs.end() && !capture) {
+            enqueueStep(plan);
+        } else if (it == graphs.end()) {
             const int before = launchCount();
             spans.clear();
             evUsed = 0;
@@ -616,30 +817,30 @@ int Engine::runPlan(const StepPlan &plan) {
 
 // warmstartForces + selectUpdateBodies (solver_solve.cpp:31-105, 263-424).
 int Engine::warmstartAndSelect(const StepParams &sp) {
-    launchForceInit(d, sp, nForces, stream);
+    launchForceInit(d, sp, nForces > 0, stream);
     beginSpan();
-    launchManifoldInit(d, sp, stream);
+    launchManifoldInit(d, sp, tuned.narrow, stream);
     endSpan(kNarrow);
     launchManifoldCompact(d, stream);
-    launchAdjacency(d, nBodies, stream);
-    launchContactOnly(d, nBodies, stream);
-    launchColour(d, nBodies, needGreedy(), stream);
-    launchColourLists(d, nBodies, P.contact_only_overflow, stream);
+    launchAdjacency(d, stream);
+    launchContactOnly(d, stream);
+    launchColour(d, needGreedy(), !P.contact_only_overflow, stream);
+    launchColourLists(d, P.contact_only_overflow, stream);
     return AVBDG_OK;
 }
 
 // Solver::projectContacts (solver_projection.cpp:67-281).
 void Engine::projectContacts(const StepParams &sp, bool positions, float window) {
-    launchProjActive(d, worlds(), stream);
+    launchProjActive(d, stream);
     if (sp.specMargin > 0.0f)
-        launchBrake(d, worlds(), window > 0.0f ? window : sp.collisionDt, stream);
+        launchBrake(d, window > 0.0f ? window : sp.collisionDt, stream);
     if (positions && sp.projIters > 0)
-        launchProjection(d, nBodies, worlds(), sp, stream);
+        launchProjection(d, sp, stream);
 }
 
 // Solver::runSubstep + iterateBody (solver_step.cpp:79-105, 195-316).
 void Engine::runSubstep(const StepParams &sp, int rounds) {
-    launchWarmstartBodies(d, nBodies, sp, stream);
+    launchWarmstartBodies(d, sp, stream);
     const int newtonRounds =
             std::clamp(static_cast<int>(std::ceil(P.newton_ratio * static_cast<float>(rounds))), 1, rounds);
     const bool colours = needGreedy();
@@ -651,22 +852,22 @@ void Engine::runSubstep(const StepParams &sp, int rounds) {
             if (colours) {
                 // Each pass reads its colour's size on the device; empty colours return at once.
                 for (int c = 0; c < kMaxColours; c++)
-                    launchColourPass(d, c, std::max(nDynamic, 1), sp, stream);
+                    launchColourPass(d, c, sp, stream);
                 launchStamps(d, sp, true, stream);
             }
             beginSpan();
-            launchOverflowSolve(d, nBodies, sp, inPlace, stream);
+            launchOverflowSolve(d, sp, inPlace, tuned.solve, stream);
             endSpan(kBody);
             if (!inPlace)
-                launchOverflowApply(d, nBodies, sp, stream);
+                launchOverflowApply(d, sp, stream);
         }
         const bool nextNewton = it + 1 < newtonRounds;
         beginSpan();
-        launchDual(d, sp, nextNewton, newton ? 1.0f : P.stiffness_decay, stream);
+        launchDual(d, sp, nextNewton, newton ? 1.0f : P.stiffness_decay, tuned.dual, stream);
         endSpan(kManifold);
-        launchForceDual(d, sp, nForces, stream);
+        launchForceDual(d, sp, nForces > 0, stream);
     }
-    launchFinishBodies(d, nBodies, sp, stream);
+    launchFinishBodies(d, sp, stream);
 }
 
 int Engine::finishStep() {
@@ -678,25 +879,37 @@ int Engine::finishStep() {
         return rc;
     steps++;
     launches = launchCount() - launchBase;
-    if (profiling) {
+    if (profiling || tuning)
         collectSpans();
+    if (profiling) {
         acc.kernel_launches += launches;
         acc.steps++;
     }
+    if (tuning)
+        finishTrial();
     nForces = hostCtr[C_FORCES];
     if (hostCtr[C_ERRORS]) {
         const int e = hostCtr[C_ERRORS];
         cudaMemsetAsync(d.ctr + C_ERRORS, 0, sizeof(int), stream);
         if (e & kErrBrakeTimeout)
-            return fail(AVBDG_ERR_TIMEOUT, "brake sweep: a bounded grid barrier gave up");
+            return fail(AVBDG_ERR_TIMEOUT, "brake sweep: a bounded wait for a preceding candidate gave up");
         if (e & kErrColourTimeout)
-            return fail(AVBDG_ERR_TIMEOUT, "colouring: a bounded grid barrier gave up");
+            return fail(AVBDG_ERR_TIMEOUT, "colouring: a bounded wait for an earlier neighbour gave up");
         return fail(AVBDG_ERR_CAPACITY, "a device buffer overflowed this step (state is not trustworthy)");
     }
     // Keep headroom for the next step's pairs and manifolds.
     if (hostCtr[C_PAIRS] * 2 > d.PP || hostCtr[C_CAND] * 2 > d.MM || hostCtr[C_ADJ] * 2 > 2 * (d.FF + d.MM)) {
-        allocate(d.NB, std::max(d.MM, 4 * hostCtr[C_CAND]), d.FF, std::max(d.PP, 4 * hostCtr[C_PAIRS]), d.WW);
-        return cudaCheck("grow");
+        int mm = std::max(d.MM, 4 * hostCtr[C_CAND]), pp = std::max(d.PP, 4 * hostCtr[C_PAIRS]);
+        if (!fits(d.NB, mm, d.FF, pp, d.WW)) {
+            mm = std::max(d.MM, 2 * hostCtr[C_CAND]);
+            pp = std::max(d.PP, 2 * hostCtr[C_PAIRS]);
+        }
+        // Under a byte limit that leaves no room, the store stays as it is; an overflow in a later
+        // step is then reported as AVBDG_ERR_CAPACITY.
+        if (fits(d.NB, mm, d.FF, pp, d.WW)) {
+            allocate(d.NB, mm, d.FF, pp, d.WW);
+            return cudaCheck("grow");
+        }
     }
     return AVBDG_OK;
 }
@@ -818,7 +1031,7 @@ int Engine::setState(int w, int first, int count, const float *pos, const float 
 // Spans of an eager step reuse pooled events; spans captured into a graph get events of their
 // own, recorded by the graph's event nodes at every launch.
 int Engine::beginSpan() {
-    if (!profiling)
+    if (!profiling && !(tuning && tuneTrial >= 0))
         return -1;
     cudaEvent_t a, b;
     if (capturing) {
@@ -840,7 +1053,7 @@ int Engine::beginSpan() {
 }
 
 void Engine::endSpan(int kind) {
-    if (!profiling || spans.empty())
+    if ((!profiling && !(tuning && tuneTrial >= 0)) || spans.empty())
         return;
     spans.back().kind = kind;
     recordPhase(spans.back().b);
@@ -848,9 +1061,17 @@ void Engine::endSpan(int kind) {
 
 void Engine::collectSpans() {
     const std::vector<Span> &list = graphSpans ? *graphSpans : spans;
+    const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
     for (const Span &s : list) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, s.a, s.b);
+        if (tuning && tuneTrial >= 0 && s.kind >= 0 && s.kind < kKinds) {
+            const int c = tuneTrial % spaces[s.kind]->count;
+            tuneMs[s.kind][c] += ms;
+            tuneN[s.kind][c]++;
+        }
+        if (!profiling)
+            continue;
         if (s.kind == kManifold) {
             acc.manifold_ms += ms;
             acc.manifold_launches++;
@@ -866,6 +1087,46 @@ void Engine::collectSpans() {
         spans.clear();
         evUsed = 0;
     }
+}
+
+void Engine::armTuning() {
+    tuning = tuneEnabled;
+    tuneTrial = -kTuneDelay;
+    std::memset(tuneMs, 0, sizeof(tuneMs));
+    std::memset(tuneN, 0, sizeof(tuneN));
+}
+
+// Trial t runs candidate t mod (number of candidates) of every tuned kernel.
+void Engine::configureTrial() {
+    tuned.dual = kTuneDual.sizes[tuneTrial % kTuneDual.count];
+    tuned.solve = kTuneSolve.sizes[tuneTrial % kTuneSolve.count];
+    tuned.narrow = kTuneNarrow.sizes[tuneTrial % kTuneNarrow.count];
+    tuned.traverse = kTuneTraverse.sizes[tuneTrial % kTuneTraverse.count];
+}
+
+void Engine::finishTrial() {
+    if (++tuneTrial < kTuneTrials)
+        return;
+    const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
+    int *picks[kKinds] = {&tuned.dual, &tuned.solve, &tuned.narrow, &tuned.traverse};
+    const Tuned defaults;
+    const int fallback[kKinds] = {defaults.dual, defaults.solve, defaults.narrow, defaults.traverse};
+    for (int k = 0; k < kKinds; k++) {
+        int best = -1;
+        double bestMs = 0.0;
+        for (int c = 0; c < spaces[k]->count; c++) {
+            if (tuneN[k][c] == 0)
+                continue;
+            const double avg = tuneMs[k][c] / tuneN[k][c];
+            if (best < 0 || avg < bestMs) {
+                best = c;
+                bestMs = avg;
+            }
+        }
+        *picks[k] = best >= 0 ? spaces[k]->sizes[best] : fallback[k];
+    }
+    tuning = false;
+    dropGraphs(); // capture again with the chosen sizes
 }
 
 void Engine::takeKernelTimes(avbdg_kernel_times &out) {
@@ -905,6 +1166,12 @@ int Engine::stats(avbdg_stats &out) {
     out.steps = steps;
     out.graph_step = lastGraph ? 1 : 0;
     out.kernel_launches = launches;
+    if (!tuning) {
+        out.block_dual = tuned.dual;
+        out.block_solve = tuned.solve;
+        out.block_narrow = tuned.narrow;
+        out.block_traverse = tuned.traverse;
+    }
     if (timed) {
         float t[4] = {};
         for (int i = 0; i < 4; i++)
@@ -956,15 +1223,23 @@ int Engine::dumpBroadphase(uint64_t *codes, int32_t *order, int capN, uint64_t *
     if ((codes || order) && n > 0) {
         std::vector<uint64_t> c(n);
         std::vector<int> l2b(n);
-        std::vector<uint32_t> sv(n);
         cudaMemcpy(c.data(), d.codes, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost);
         cudaMemcpy(l2b.data(), d.lpToBody, sizeof(int) * n, cudaMemcpyDeviceToHost);
-        cudaMemcpy(sv.data(), d.sortV, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost);
+        // The reference's order: list positions of each world sorted by (code, list position)
+        // (bvh_broadphase.cpp:87-96); the device tree is built from other codes.
+        std::vector<int32_t> sv(n);
+        for (int w = 0; w < worlds(); w++) {
+            const int b = wBase[w], e = wBase[w] + wCount[w];
+            for (int p = b; p < e; p++)
+                sv[p] = p;
+            std::stable_sort(sv.begin() + b, sv.begin() + e,
+                             [&](int32_t x, int32_t y) { return c[l2b[x]] < c[l2b[y]]; });
+        }
         for (int i = 0; i < n && i < capN; i++) {
             if (codes)
                 codes[i] = c[l2b[i]];
             if (order)
-                order[i] = static_cast<int32_t>(sv[i]);
+                order[i] = sv[i];
         }
     }
     if (pairs && np > 0)

@@ -42,12 +42,10 @@ enum Counter {
     C_FORCES,         // live forces
     C_ADJ,            // adjacency entries
     C_LONG,           // long segments (segmented sort scratch)
-    C_SPEC,           // brake candidates still pending
     C_SPECN,          // brake candidates in specList
+    C_BODIES,         // body slots in use (all worlds)
+    C_WORLDS,         // worlds
     C_ERRORS,         // capacity / timeout bits (kErr*)
-    C_UNCOLOURED,     // colouring: bodies still waiting, three rotating slots
-    C_UNCOLOURED1,
-    C_UNCOLOURED2,
     C_ONE,            // constant 1 (scan length helper)
     C_TMP,
     C_COUNT
@@ -84,6 +82,7 @@ struct Dev {
     int *wStop;             // projection: early-exit flag per world
     int *wBounds;           // Morton scene bounds per world: lo xyz, hi xyz (ordered ints)
     int *wActive;           // projection: movable manifolds per world (0 = skip the world)
+    int *wColour;           // colouring: 1 if a force touches the world (its bodies need colours)
     // bodies
     float4 *x, *q, *x0, *q0, *xi, *qi, *v, *w, *vprev;
     float4 *size, *moment;
@@ -92,7 +91,8 @@ struct Dev {
     uint8_t *contactOnly, *colour;
     float4 *aabbC, *aabbH;
     // LBVH
-    uint64_t *codes;        // per body: Morton code of the last rebuild
+    uint64_t *codes;        // per body: the reference's Morton code of the last rebuild (dumps)
+    uint64_t *treeCodes;    // per body: the code the tree is built from (true per-axis origin)
     uint64_t *sortK, *sortKAlt;
     uint32_t *sortV, *sortVAlt;
     int *leafBody;          // sorted position -> body
@@ -109,6 +109,7 @@ struct Dev {
     float4 *stamps;
     uint8_t *mSpec, *mDone; // brake
     int *specList;
+    int2 *specPred;         // brake: preceding candidate on each movable body (-1 = none)
     float4 *projLin, *projAng; // projection contributions per (manifold, side)
     float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)
     // forces (creation order; list order is descending index)
@@ -124,7 +125,10 @@ struct Dev {
     int *ctr;
     int *longList;
     void *scanScratch, *radixScratch;
-    unsigned *barrier;      // grid barrier of the cooperative brake (2 words)
+    // world removal: slot map (NB) + force ranks (FF), staging of max(NB, FF) records, world remap
+    int *relocInt;
+    float4 *relocF4;
+    int *relocRemap;        // 2 per world: new id (-1 = removed), new base slot
 };
 
 // ---- device helpers shared by the kernel files ----

@@ -15,15 +15,9 @@
 
 #include "avbdg.h"
 #include "engine.cuh"
+#include "kernels.cuh"
 
 namespace avbdg {
-
-struct HostForce {
-    int kind; // 0 joint, 1 ignore
-    int a, b; // global body indices (-1 = world)
-    float rA[3], rB[3];
-    float stiffLin, stiffAng, fracture;
-};
 
 class Engine {
 public:
@@ -38,7 +32,25 @@ public:
     int addJoint(int world, int a, int b, const float rA[3], const float rB[3], float kLin, float kAng,
                  float fracture);
     int addIgnore(int world, int a, int b);
+    // Forces of `world` in creation order (kind 0 ball joint, 1 ignore pair), one upload for all.
+    int addForces(int world, int count, const avbdg_force_desc *descs);
+    // Remove the listed worlds. The others keep their order and their results: they move down to
+    // dense body slots and are renumbered 0.. in order; their manifolds and forces are carried.
+    int removeWorlds(const std::vector<int> &ids);
     void clear();
+
+    // Checks addBodies / addForces apply before touching the store (a world of `nb` bodies).
+    static int validateBodies(int count, const avbdg_body_desc *descs, std::string &why);
+    static int validateForces(int nb, int count, const avbdg_force_desc *descs, std::string &why);
+
+    // Device bytes of a store with these capacities (bodies, manifolds, forces, pairs, worlds).
+    static size_t storeBytes(int nb, int mm, int ff, int pp, int ww);
+    // Capacities for `nb` bodies the store grows to (manifolds and pairs follow the body count).
+    static size_t storeBytesForBodies(int nb, int ff, int ww) { return storeBytes(nb, 8 * nb, ff, 16 * nb, ww); }
+    size_t reservedBytes() const { return storeBytes(d.NB, d.MM, d.FF, d.PP, d.WW); }
+    // Upper bound on the store's device bytes (0 = none): growth headroom is cut to fit, and a
+    // growth that cannot fit fails with AVBDG_ERR_CAPACITY.
+    void setByteLimit(size_t bytes) { byteLimit = bytes; }
 
     int setParams(const avbdg_params &p);
     const avbdg_params &params() const { return P; }
@@ -70,11 +82,14 @@ public:
 
     int worlds() const { return static_cast<int>(wBase.size()); }
     int worldBodies(int w) const { return wCount[w]; }
+    int worldDynamic(int w) const { return wDyn[w]; }
     int bodies() const { return nBodies; }
     int dynamicBodies() const { return nDynamic; }
+    int forces() const { return nForces; }
     cudaStream_t streamHandle() const { return stream; }
     // Kernel launches of the last step (this library's kernels only).
     int lastLaunches() const { return launches; }
+    bool lastStepWasGraph() const { return lastGraph; }
     const std::string &error() const { return err; }
 
 private:
@@ -82,11 +97,11 @@ private:
     Dev d{};
     cudaStream_t stream = nullptr;
     std::vector<void *> allocs;
-    std::vector<int> wBase, wCount;
-    std::vector<HostForce> pendingForces; // added since the last upload
+    std::vector<int> wBase, wCount, wDyn;
     int nBodies = 0, nDynamic = 0, nForces = 0;
     int treeAge = 0;
-    bool treeValid = false, adjValid = false, uploaded = false;
+    bool treeValid = false, adjValid = false;
+    size_t byteLimit = 0;
     int steps = 0;
     int launches = 0;
     int hostCtr[C_COUNT] = {};
@@ -96,7 +111,7 @@ private:
     std::string err;
     // Profiling: event pairs around the hot launches of the current step.
     bool profiling = false;
-    enum KernelKind { kManifold = 0, kBody = 1, kNarrow = 2 };
+    enum KernelKind { kManifold = 0, kBody = 1, kNarrow = 2, kTraverse = 3, kKinds = 4 };
     struct Span {
         cudaEvent_t a, b;
         int kind;
@@ -106,6 +121,21 @@ private:
     size_t evUsed = 0;
     avbdg_kernel_times acc{};
     int launchBase = 0;
+    // Autotuned block sizes (candidates in kernels.cuh). After a store is created or regrown,
+    // kTuneDelay steps run as usual, then kTuneTrials eager steps try the candidates in turn,
+    // timed by events around each tuned launch; the fastest per kernel is kept.
+    struct Tuned {
+        int dual = 256, solve = 128, narrow = 256, traverse = 256;
+    };
+    Tuned tuned;
+    static constexpr int kTuneDelay = 4, kTuneTrials = 8;
+    bool tuneEnabled = true, tuning = false;
+    int tuneTrial = 0;
+    double tuneMs[kKinds][kTuneCandidates] = {};
+    int tuneN[kKinds][kTuneCandidates] = {};
+    void armTuning();
+    void configureTrial();
+    void finishTrial();
     int beginSpan();
     void endSpan(int kind);
     void collectSpans();
@@ -123,13 +153,17 @@ private:
     template <typename T>
     T *dalloc(size_t n);
     int ensureCapacity(int nb, int ff, int ww);
-    int flushPending();
+    void uploadCounts();
+    bool fits(int nb, int mm, int ff, int pp, int ww) const {
+        return byteLimit == 0 || storeBytes(nb, mm, ff, pp, ww) <= byteLimit;
+    }
     StepParams stepParams(float collisionDt) const;
     // Host decisions of one step; the enqueued work depends on nothing else but device counts.
     struct StepPlan {
         int mode = 0; // 0 step, 1 interleaved
         int substeps = 1, rounds = 0;
         bool adjAtStart = false, anyTree = false, rebuild = false, forces = false, greedy = false;
+        bool multiWorld = false;
         std::string key() const;
     };
     struct Graph {
@@ -139,6 +173,7 @@ private:
     };
     const std::vector<Span> *graphSpans = nullptr; // spans of the graph the last step ran
     std::map<std::string, Graph> graphs;
+    std::map<std::string, int> planSeen; // plans run since the cache was dropped (capture on reuse)
     bool useGraphs = true, capturing = false, lastGraph = false;
     std::string graphError;
     StepPlan planStep(int mode, int substeps, int rounds);

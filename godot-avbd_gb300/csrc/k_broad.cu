@@ -26,7 +26,8 @@ __device__ __forceinline__ int orderedInt(float f) {
 __device__ __forceinline__ float orderedFloat(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
 
 // Swept AABB (solver_broadphase.cpp:103-122) over the tight box bound (rigid.cpp:83-106).
-__global__ void aabbKernel(Dev d, int n, StepParams p) {
+__global__ void aabbKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
         return;
@@ -52,9 +53,9 @@ __global__ void aabbKernel(Dev d, int n, StepParams p) {
 
 // ---- Morton codes (bvh_broadphase.cpp:19-36, 70-85) ----
 
-__global__ void boundsResetKernel(int *wBounds, int nWorlds) {
+__global__ void boundsResetKernel(Dev d, int *wBounds) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nWorlds)
+    if (w >= d.ctr[C_WORLDS])
         return;
     for (int k = 0; k < 3; k++) {
         wBounds[6 * w + k] = 0x7fffffff;          // lo (ordered)
@@ -62,7 +63,8 @@ __global__ void boundsResetKernel(int *wBounds, int nWorlds) {
     }
 }
 
-__global__ void boundsKernel(Dev d, int n, int *wBounds) {
+__global__ void boundsKernel(Dev d, int *wBounds) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
         return;
@@ -93,7 +95,8 @@ __device__ __forceinline__ uint32_t quantise(float v, float lo, float scaleF) {
 }
 
 // Code per body; keys/values laid out by list position for the stable (code, list index) sort.
-__global__ void mortonKernel(Dev d, int n, const int *wBounds) {
+__global__ void mortonKernel(Dev d, const int *wBounds) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
         return;
@@ -112,17 +115,23 @@ __global__ void mortonKernel(Dev d, int n, const int *wBounds) {
         e = 1.0e-6f;
     const float sc = 2097151.0f / e;
     const float4 c = d.aabbC[g];
-    // The reference quantises all three axes against lo.x (bvh_broadphase.cpp:85); kept.
-    const uint64_t code = expandBits21(quantise(c.x, lox, sc)) | (expandBits21(quantise(c.y, lox, sc)) << 1) |
-                          (expandBits21(quantise(c.z, lox, sc)) << 2);
-    d.codes[g] = code;
+    // The reference quantises all three axes against lo.x (bvh_broadphase.cpp:85): kept for the
+    // code and order dumps. Where a scene does not extend from lo.x in y and z, that clamps whole
+    // regions to one code and degrades the tree, so the tree is built from codes with each axis's
+    // own origin. The candidate pairs do not depend on the tree's shape.
+    d.codes[g] = expandBits21(quantise(c.x, lox, sc)) | (expandBits21(quantise(c.y, lox, sc)) << 1) |
+                 (expandBits21(quantise(c.z, lox, sc)) << 2);
+    const uint64_t code = expandBits21(quantise(c.x, lox, sc)) | (expandBits21(quantise(c.y, loy, sc)) << 1) |
+                          (expandBits21(quantise(c.z, loz, sc)) << 2);
+    d.treeCodes[g] = code;
     const int lp = listPos(d, g);
     d.sortK[lp] = code;
     d.sortV[lp] = static_cast<uint32_t>(lp);
 }
 
 // Slots without a body keep key ~0 and map to themselves in list-position space.
-__global__ void mortonResetKernel(Dev d, int n) {
+__global__ void mortonResetKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -132,7 +141,8 @@ __global__ void mortonResetKernel(Dev d, int n) {
 
 // Second key: the world's first slot (a free slot keys on its own position), so after the stable
 // sort world w's leaves occupy sorted positions [wBase, wBase + wCount).
-__global__ void worldKeyKernel(Dev d, int n) {
+__global__ void worldKeyKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -141,7 +151,8 @@ __global__ void worldKeyKernel(Dev d, int n) {
     d.sortK[i] = static_cast<uint64_t>(g >= 0 ? d.wBase[d.meta[g].x] : lp);
 }
 
-__global__ void leafKernel(Dev d, int n) {
+__global__ void leafKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -152,8 +163,8 @@ __global__ void leafKernel(Dev d, int n) {
 __device__ __forceinline__ int deltaKey(const Dev &d, int s, int n, int i, int j) {
     if (j < 0 || j >= n)
         return -1;
-    const uint64_t ci = d.codes[d.leafBody[s + i]];
-    const uint64_t cj = d.codes[d.leafBody[s + j]];
+    const uint64_t ci = d.treeCodes[d.leafBody[s + i]];
+    const uint64_t cj = d.treeCodes[d.leafBody[s + j]];
     if (ci != cj)
         return __clzll(static_cast<long long>(ci ^ cj));
     return 64 + __clz(static_cast<int>(d.sortV[s + i] ^ d.sortV[s + j]));
@@ -163,7 +174,8 @@ constexpr int kLeafBit = 0x40000000;
 
 // Karras (2012) radix tree: internal node i of a world spans a key range and splits at the
 // highest differing bit.
-__global__ void karrasKernel(Dev d, int n) {
+__global__ void karrasKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n)
         return;
@@ -233,7 +245,8 @@ __device__ __forceinline__ void childBounds(const Dev &d, int c, float4 &mn, flo
 }
 
 // Bottom-up refit: the second child to arrive at a node computes its bounds.
-__global__ void refitKernel(Dev d, int n) {
+__global__ void refitKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n)
         return;
@@ -269,7 +282,8 @@ __device__ __forceinline__ bool overlapClosed(f3 aMin, f3 aMax, f3 bMin, f3 bMax
 
 // Walk the world's tree with body g's box; emit partners with a larger list position.
 template <bool EMIT>
-__global__ void traverseKernel(Dev d, int n) {
+__global__ void traverseKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
         return;
@@ -412,39 +426,40 @@ __global__ void candTotalKernel(Dev d) {
 
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
-void launchAabb(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); aabbKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+void launchAabb(const Dev &d, const StepParams &p, cudaStream_t s) {
+    ++launchCount(); aabbKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
 }
 
-void launchRebuildTree(const Dev &d, int n, int nWorlds, cudaStream_t s) {
-    ++launchCount(); boundsResetKernel<<<grid(nWorlds), kThreads, 0, s>>>(d.wBounds, nWorlds);
-    ++launchCount(); boundsKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
-    ++launchCount(); mortonResetKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-    ++launchCount(); mortonKernel<<<grid(n), kThreads, 0, s>>>(d, n, d.wBounds);
-    radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, n, nullptr, 0, 63, d.radixScratch, s);
-    if (nWorlds > 1) {
-        int bits = 1;
-        while ((1 << bits) < n + 1)
+void launchRebuildTree(const Dev &d, bool multiWorld, cudaStream_t s) {
+    const int *nb = d.ctr + C_BODIES;
+    ++launchCount(); boundsResetKernel<<<grid(d.WW), kThreads, 0, s>>>(d, d.wBounds);
+    ++launchCount(); boundsKernel<<<grid(d.NB), kThreads, 0, s>>>(d, d.wBounds);
+    ++launchCount(); mortonResetKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+    ++launchCount(); mortonKernel<<<grid(d.NB), kThreads, 0, s>>>(d, d.wBounds);
+    radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, d.NB, nb, 0, 63, d.radixScratch, s);
+    if (multiWorld) {
+        int bits = 1; // world bases are below the slot capacity
+        while ((1 << bits) < d.NB + 1)
             bits++;
-        ++launchCount(); worldKeyKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-        radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, n, nullptr, 0, bits, d.radixScratch, s);
+        ++launchCount(); worldKeyKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+        radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, d.NB, nb, 0, bits, d.radixScratch, s);
     }
-    ++launchCount(); leafKernel<<<grid(n), kThreads, 0, s>>>(d, n);
-    ++launchCount(); karrasKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); leafKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+    ++launchCount(); karrasKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
 }
 
-void launchRefit(const Dev &d, int n, cudaStream_t s) {
+void launchRefit(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.nodeFlag, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
-    ++launchCount(); refitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); refitKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
 }
 
-void launchPairs(const Dev &d, int n, cudaStream_t s) {
+void launchPairs(const Dev &d, int block, cudaStream_t s) {
     cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
-    ++launchCount(); traverseKernel<false><<<grid(n), kThreads, 0, s>>>(d, n);
+    ++launchCount(); traverseKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d);
     scanExclusive(d.pairStart, d.pairStart, d.NB + 1, nullptr, d.ctr + C_TMP, d.scanScratch, s);
     ++launchCount(); pairTotalKernel<<<1, 1, 0, s>>>(d);
-    ++launchCount(); traverseKernel<true><<<grid(n), kThreads, 0, s>>>(d, n);
-    segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, n, nullptr, d.longList, d.ctr + C_LONG, s);
+    ++launchCount(); traverseKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d);
+    segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
 }
 
 void launchFilterAcquire(const Dev &d, cudaStream_t s) {

@@ -349,18 +349,19 @@ __global__ void forceCompactKernel(Dev d) {
 
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
-void launchAdjacency(const Dev &d, int nBodies, cudaStream_t s) {
+void launchAdjacency(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.adjStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.adjFill, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
     ++launchCount(); adjCountKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
-    scanExclusive(d.adjStart, d.adjStart, nBodies + 1, nullptr, d.ctr + C_ADJ, d.scanScratch, s);
+    // Slots past the last body count zero, so scanning the whole capacity gives the same starts.
+    scanExclusive(d.adjStart, d.adjStart, d.NB + 1, nullptr, d.ctr + C_ADJ, d.scanScratch, s);
     ++launchCount(); adjTotalKernel<<<1, 1, 0, s>>>(d);
     ++launchCount(); adjFillKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
-    segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, nBodies, nullptr, d.longList, d.ctr + C_LONG, s);
+    segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
 }
 
-void launchManifoldInit(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); manifoldInitKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+void launchManifoldInit(const Dev &d, const StepParams &p, int block, cudaStream_t s) {
+    ++launchCount(); manifoldInitKernel<<<divUp(d.MM, block), block, 0, s>>>(d, p);
 }
 
 void launchManifoldCompact(const Dev &d, cudaStream_t s) {
@@ -372,11 +373,11 @@ void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s) {
     ++launchCount(); rebaseKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
 }
 
-void launchForceInit(const Dev &d, const StepParams &p, int nForces, cudaStream_t s) {
-    if (nForces <= 0)
+void launchForceInit(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {
+    if (!forces)
         return;
     cudaMemsetAsync(d.ctr + C_TMP, 0, sizeof(int), s);
-    ++launchCount(); forceInitKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
+    ++launchCount(); forceInitKernel<<<grid(d.FF), kThreads, 0, s>>>(d, p);
     ++launchCount(); forceCompactKernel<<<1, 1, 0, s>>>(d);
 }
 

@@ -3,17 +3,20 @@
 // The brake is a Gauss-Seidel sweep over manifolds in live order: each braked patch updates its
 // bodies' velocities in place and later manifolds see the result. Only manifolds with an open gap
 // (some contact with positive separation at the fixed poses) can brake, so the sweep's order only
-// matters among them. A manifold runs once every earlier such manifold on one of its movable
-// bodies is done; ready manifolds never share a movable body, so each round runs them in
-// parallel and the result equals the serial sweep. Rounds are separated by a grid barrier inside
-// one cooperative launch; every wait is bounded and reports a timeout instead of hanging.
+// matters among them, and a candidate depends on exactly one earlier candidate per movable body:
+// the one just before it on that body. The sweep runs as a dataflow inside one cooperative launch:
+// every thread takes candidates in increasing live order, waits until the (at most two)
+// predecessors have published their velocities, brakes, then publishes its own. Candidates on
+// disjoint bodies proceed in parallel and every body sees its candidates in live order, so the
+// result equals the serial sweep. All threads are resident and the smallest unfinished candidate
+// can always run, so the waits end; each is still bounded and reports a timeout instead of
+// hanging.
 //
 // Projection passes are Jacobi: per-manifold patch corrections, then per-body sums in live order
 // (the adjacency order), averaged over the manifold count, with the per-world early exit.
 
 #include <cooperative_groups.h>
 
-#include "grid_sync.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -93,15 +96,21 @@ __global__ void projActiveKernel(Dev d) {
 // Brake candidates in live order (the scan of their flags gives each one its slot).
 __global__ void specScatterKernel(Dev d, const int *flags, const int *rank) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m == 0)
-        d.ctr[C_SPEC] = d.ctr[C_SPECN];
     if (m >= d.ctr[C_LIVE] || !flags[m])
         return;
     d.specList[rank[m]] = m;
 }
 
-// Is manifold m the earliest unfinished braking candidate on each of its movable bodies?
-__device__ bool brakeReady(const Dev &d, int m, int2 ab, int nf) {
+// For each candidate, the preceding candidate in live order on each of its movable bodies (-1 if
+// none), from the body's adjacency (forces first, then manifolds in live order).
+__global__ void brakePredKernel(Dev d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.ctr[C_SPECN])
+        return;
+    const int m = d.specList[k];
+    const int2 ab = d.live.ab[m];
+    const int nf = d.ctr[C_FORCES];
+    int pred[2] = {-1, -1};
     for (int side = 0; side < 2; side++) {
         const int x = side == 0 ? ab.x : ab.y;
         if (!movable(d, x))
@@ -113,12 +122,24 @@ __device__ bool brakeReady(const Dev &d, int m, int2 ab, int nf) {
             const int o = seq - nf;
             if (o >= m)
                 break;
-            if (__ldcg(&d.mSpec[o]) && !__ldcg(&d.mDone[o]))
-                return false;
+            if (d.mSpec[o])
+                pred[side] = o;
         }
     }
-    return true;
+    d.specPred[k] = make_int2(pred[0], pred[1]);
 }
+
+__device__ __forceinline__ unsigned loadAcquire(const uint8_t *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u8 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void storeRelease(uint8_t *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u8 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool published(const Dev &d, int m) { return m < 0 || loadAcquire(d.mDone + m) != 0; }
 
 // One manifold of the brake sweep (solver_projection.cpp:98-166).
 __device__ void brakeManifold(const Dev &d, int m, float window) {
@@ -187,37 +208,25 @@ __device__ void brakeManifold(const Dev &d, int m, float window) {
     }
 }
 
-__global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window, unsigned *bar) {
+constexpr long long kBrakeSpinLimit = 4000000; // ~0.3 s of 64 ns sleeps per wait
+
+__global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window) {
     const int ns = d.ctr[C_SPECN];
-    const int nf = d.ctr[C_FORCES];
     const int stride = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    volatile int *remaining = d.ctr + C_SPEC;
-    for (int round = 0; round <= ns; round++) {
-        if (*remaining == 0)
-            break;
-        // Phase 1: mark the ready manifolds (mSpec = 2).
-        for (int k = tid; k < ns; k += stride) {
-            const int m = d.specList[k];
-            if (__ldcg(&d.mDone[m]))
-                continue;
-            if (brakeReady(d, m, d.live.ab[m], nf))
-                d.mSpec[m] = 2;
+    volatile int *errors = d.ctr + C_ERRORS;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += stride) {
+        const int2 pred = d.specPred[k];
+        long long spins = 0;
+        while (!(published(d, pred.x) && published(d, pred.y))) {
+            if (++spins > kBrakeSpinLimit || (*errors & kErrBrakeTimeout)) {
+                atomicOr(d.ctr + C_ERRORS, kErrBrakeTimeout);
+                return;
+            }
+            __nanosleep(64);
         }
-        if (!gridBarrier(bar, d.ctr + C_ERRORS, kErrBrakeTimeout))
-            return;
-        // Phase 2: run them; they touch disjoint movable bodies.
-        for (int k = tid; k < ns; k += stride) {
-            const int m = d.specList[k];
-            if (__ldcg(&d.mSpec[m]) != 2)
-                continue;
-            brakeManifold(d, m, window);
-            __stcg(&d.mSpec[m], static_cast<uint8_t>(1));
-            __stcg(&d.mDone[m], static_cast<uint8_t>(1));
-            atomicSub(d.ctr + C_SPEC, 1);
-        }
-        if (!gridBarrier(bar, d.ctr + C_ERRORS, kErrBrakeTimeout))
-            return;
+        const int m = d.specList[k];
+        brakeManifold(d, m, window);
+        storeRelease(d.mDone + m, 1u); // orders this thread's velocity writes before the flag
     }
 }
 
@@ -282,7 +291,8 @@ __global__ void projManifoldKernel(Dev d, StepParams p) {
     }
 }
 
-__global__ void projBodyKernel(Dev d, int nBodies, StepParams p) {
+__global__ void projBodyKernel(Dev d, StepParams p) {
+    const int nBodies = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nBodies || d.meta[g].x < 0 || !movable(d, g))
         return;
@@ -330,7 +340,8 @@ __global__ void projBodyKernel(Dev d, int nBodies, StepParams p) {
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
 
-__global__ void projCheckKernel(Dev d, int nWorlds, float tolerance) {
+__global__ void projCheckKernel(Dev d, float tolerance) {
+    const int nWorlds = d.ctr[C_WORLDS];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nWorlds)
         return;
@@ -340,7 +351,8 @@ __global__ void projCheckKernel(Dev d, int nWorlds, float tolerance) {
 }
 
 // Worlds with no movable manifold skip the whole projection (the reference returns early).
-__global__ void projStartKernel(Dev d, int nWorlds) {
+__global__ void projStartKernel(Dev d) {
+    const int nWorlds = d.ctr[C_WORLDS];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nWorlds)
         return;
@@ -367,31 +379,30 @@ int brakeGridBlocks() {
     return g_brakeBlocks;
 }
 
-void launchProjActive(const Dev &d, int nWorlds, cudaStream_t s) {
-    cudaMemsetAsync(d.wActive, 0, sizeof(int) * static_cast<size_t>(nWorlds), s);
+void launchProjActive(const Dev &d, cudaStream_t s) {
+    cudaMemsetAsync(d.wActive, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
     ++launchCount(); projActiveKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
     scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_LIVE, d.ctr + C_SPECN, d.scanScratch, s);
     ++launchCount(); specScatterKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
 }
 
-void launchBrake(const Dev &d, int, float window, cudaStream_t s) {
-    unsigned *bar = reinterpret_cast<unsigned *>(d.barrier);
-    cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
+void launchBrake(const Dev &d, float window, cudaStream_t s) {
+    ++launchCount(); brakePredKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
     Dev dd = d;
     float win = window;
-    void *args[] = {&dd, &win, &bar};
+    void *args[] = {&dd, &win};
     ++launchCount();
     cudaLaunchCooperativeKernel(reinterpret_cast<void *>(brakeKernel), dim3(brakeGridBlocks()), dim3(kBrakeThreads),
                                 args, 0, s);
 }
 
-void launchProjection(const Dev &d, int nBodies, int nWorlds, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); projStartKernel<<<grid(nWorlds), kThreads, 0, s>>>(d, nWorlds);
+void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
+    ++launchCount(); projStartKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
     const float tol = smax(p.projSlop * 0.01f, 1.0e-6f);
     for (int it = 0; it < p.projIters; it++) {
         ++launchCount(); projManifoldKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
-        ++launchCount(); projBodyKernel<<<grid(nBodies), kThreads, 0, s>>>(d, nBodies, p);
-        ++launchCount(); projCheckKernel<<<grid(nWorlds), kThreads, 0, s>>>(d, nWorlds, tol);
+        ++launchCount(); projBodyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+        ++launchCount(); projCheckKernel<<<grid(d.WW), kThreads, 0, s>>>(d, tol);
     }
 }
 

@@ -13,7 +13,6 @@
 // Coloured (Gauss-Seidel) bodies recompute their manifold terms from the current poses at every
 // touch; the reference's "first touch uses the dual's cache" rule yields the same floats.
 
-#include "grid_sync.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -668,7 +667,8 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
 }
 
 // Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
-__global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, int n, StepParams p, int inPlace) {
+__global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
         return;
@@ -686,7 +686,8 @@ __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, int 
     }
 }
 
-__global__ void overflowApplyKernel(Dev d, int n, StepParams p) {
+__global__ void overflowApplyKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
         return;
@@ -707,7 +708,8 @@ __device__ __forceinline__ void maskLocked(int locks, f3 &v) {
 }
 
 // Solver::warmstartBody (solver_solve.cpp:109-142).
-__global__ void warmstartKernel(Dev d, int n, StepParams p) {
+__global__ void warmstartKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
         return;
@@ -745,7 +747,8 @@ __global__ void warmstartKernel(Dev d, int n, StepParams p) {
 }
 
 // Solver::finishBody (solver_solve.cpp:146-176), idle sleep disabled.
-__global__ void finishKernel(Dev d, int n, StepParams p) {
+__global__ void finishKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
         return;
@@ -766,7 +769,8 @@ __global__ void finishKernel(Dev d, int n, StepParams p) {
 
 // ---- update set and colouring (solver_solve.cpp:263-424) ----
 
-__global__ void contactOnlyInitKernel(Dev d, int n) {
+__global__ void contactOnlyInitKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
         return;
@@ -783,6 +787,7 @@ __global__ void contactOnlyMarkKernel(Dev d) {
         d.contactOnly[ab.x] = 0;
     if (ab.y >= 0)
         d.contactOnly[ab.y] = 0;
+    d.wColour[d.meta[ab.y].x] = 1;
 }
 
 __device__ __forceinline__ int adjOtherSolve(const Dev &d, uint32_t seq, int x, int nf) {
@@ -807,59 +812,68 @@ __device__ __forceinline__ int adjOtherSolve(const Dev &d, uint32_t seq, int x, 
 // (lower list position) neighbour in the update set is, with the smallest colour none of them
 // uses (the sequential greedy of colourGraph, reproduced exactly). A body still waiting counts
 // itself in *waiting.
-__device__ void colourTry(const Dev &d, int g, int *waiting) {
-    if (d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
-        return;
-    volatile uint8_t *col = d.colour;
-    if (col[g] != kUncoloured)
-        return;
-    const int nf = d.ctr[C_FORCES];
-    const int lpg = listPos(d, g);
-    unsigned used = 0;
-    for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
-        const int h = adjOtherSolve(d, d.adjSeq[e], g, nf);
-        if (h < 0 || !(d.x[h].w > 0.0f) || listPos(d, h) >= lpg)
-            continue;
-        const uint8_t c = col[h];
-        if (c == kUncoloured) {
-            atomicAdd(waiting, 1);
-            return;
-        }
-        if (c < kMaxColours)
-            used |= 1u << c;
-    }
-    uint8_t c = kOverflowColour;
-    for (int k = 0; k < kMaxColours; k++)
-        if (!(used & (1u << k))) {
-            c = static_cast<uint8_t>(k);
-            break;
-        }
-    col[g] = c;
+__device__ __forceinline__ unsigned loadColour(const uint8_t *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u8 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void publishColour(uint8_t *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u8 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 constexpr int kColourThreads = 512;
+constexpr long long kColourSpinLimit = 4000000; // ~0.3 s of 64 ns sleeps per wait
 
-// All colouring rounds in one cooperative launch, rounds separated by a bounded grid barrier.
-// Round r counts waiting bodies into slot r % 3; the slot of round r + 1 is cleared during
-// round r, after every block has read it for the last time (end of round r - 2).
-__global__ void __launch_bounds__(kColourThreads) colourCoopKernel(Dev d, int n, unsigned *bar) {
+// Greedy colouring (solver_solve.cpp:365-424) as a dataflow in one cooperative launch: bodies are
+// taken in increasing list position; each waits until its earlier dynamic neighbours have
+// published their colours, takes the smallest colour none of them has (or the overflow colour)
+// and publishes it. That is the sequential greedy assignment; the body with the smallest
+// uncoloured list position can always proceed, so the waits end (each is bounded anyway).
+// Worlds that no force touches hold only contact-only bodies, which go to the overflow colour
+// whatever their greedy colour, so they are not coloured at all (unless every body is coloured).
+__global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int everyWorld) {
+    const int n = d.ctr[C_BODIES];
+    const int nf = d.ctr[C_FORCES];
     const int stride = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    int *slots = d.ctr + C_UNCOLOURED;
-    for (int round = 0; round <= n; round++) {
-        int *waiting = slots + (round % 3);
-        if (tid == 0)
-            slots[(round + 1) % 3] = 0;
-        for (int g = tid; g < n; g += stride)
-            colourTry(d, g, waiting);
-        if (!gridBarrier(bar, d.ctr + C_ERRORS, kErrColourTimeout))
-            return;
-        if (*reinterpret_cast<volatile int *>(waiting) == 0)
-            break;
+    volatile int *errors = d.ctr + C_ERRORS;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
+        const int g = d.lpToBody[p];
+        if (g < 0 || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
+            continue;
+        if (!everyWorld && !d.wColour[d.meta[g].x]) {
+            publishColour(d.colour + g, kOverflowColour);
+            continue;
+        }
+        unsigned used = 0;
+        for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
+            const int h = adjOtherSolve(d, d.adjSeq[e], g, nf);
+            if (h < 0 || !(d.x[h].w > 0.0f) || listPos(d, h) >= p)
+                continue;
+            unsigned c;
+            long long spins = 0;
+            while ((c = loadColour(d.colour + h)) == kUncoloured) {
+                if (++spins > kColourSpinLimit || (*errors & kErrColourTimeout)) {
+                    atomicOr(d.ctr + C_ERRORS, kErrColourTimeout);
+                    return;
+                }
+                __nanosleep(64);
+            }
+            if (c < kMaxColours)
+                used |= 1u << c;
+        }
+        unsigned c = kOverflowColour;
+        for (int k = 0; k < kMaxColours; k++)
+            if (!(used & (1u << k))) {
+                c = static_cast<unsigned>(k);
+                break;
+            }
+        publishColour(d.colour + g, c);
     }
 }
 
-__global__ void colourListKernel(Dev d, int n, int contactOnlyOverflow) {
+__global__ void colourListKernel(Dev d, int contactOnlyOverflow) {
+    const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
         return;
@@ -884,8 +898,9 @@ __global__ void colourListKernel(Dev d, int n, int contactOnlyOverflow) {
 
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
-void launchContactOnly(const Dev &d, int n, cudaStream_t s) {
-    ++launchCount(); contactOnlyInitKernel<<<grid(n), kThreads, 0, s>>>(d, n);
+void launchContactOnly(const Dev &d, cudaStream_t s) {
+    cudaMemsetAsync(d.wColour, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
+    ++launchCount(); contactOnlyInitKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
     ++launchCount(); contactOnlyMarkKernel<<<grid(d.FF), kThreads, 0, s>>>(d);
 }
 
@@ -896,7 +911,7 @@ int colourGridBlocks() {
         int dev = 0, sms = 0, perSm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, colourCoopKernel, kColourThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, colourFlowKernel, kColourThreads, 0);
         g_colourBlocks = sms * (perSm < 1 ? 1 : (perSm > 2 ? 2 : perSm));
         if (g_colourBlocks < 1)
             g_colourBlocks = 1;
@@ -910,61 +925,57 @@ void prepareKernels() {
     colourGridBlocks();
 }
 
-void launchColour(const Dev &d, int n, bool needGreedy, cudaStream_t s) {
+void launchColour(const Dev &d, bool needGreedy, bool everyWorld, cudaStream_t s) {
     if (!needGreedy)
         return;
     colourGridBlocks();
-    unsigned *bar = d.barrier;
-    cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s);
-    cudaMemsetAsync(d.ctr + C_UNCOLOURED, 0, 3 * sizeof(int), s);
     Dev dd = d;
-    int nn = n;
-    void *args[] = {&dd, &nn, &bar};
+    int every = everyWorld ? 1 : 0;
+    void *args[] = {&dd, &every};
     ++launchCount();
-    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(colourCoopKernel), dim3(g_colourBlocks), dim3(kColourThreads),
+    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(colourFlowKernel), dim3(g_colourBlocks), dim3(kColourThreads),
                                 args, 0, s);
 }
 
-void launchColourLists(const Dev &d, int n, int contactOnlyOverflow, cudaStream_t s) {
+void launchColourLists(const Dev &d, int contactOnlyOverflow, cudaStream_t s) {
     cudaMemsetAsync(d.colourCount, 0, sizeof(int) * (kMaxColours + 1), s);
-    ++launchCount(); colourListKernel<<<grid(n), kThreads, 0, s>>>(d, n, contactOnlyOverflow);
+    ++launchCount(); colourListKernel<<<grid(d.NB), kThreads, 0, s>>>(d, contactOnlyOverflow);
 }
 
-void launchWarmstartBodies(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); warmstartKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+void launchWarmstartBodies(const Dev &d, const StepParams &p, cudaStream_t s) {
+    ++launchCount(); warmstartKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
 }
 
-void launchFinishBodies(const Dev &d, int n, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); finishKernel<<<grid(n), kThreads, 0, s>>>(d, n, p);
+void launchFinishBodies(const Dev &d, const StepParams &p, cudaStream_t s) {
+    ++launchCount(); finishKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
 }
 
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s) {
     ++launchCount(); stampsKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
 }
 
-void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); colourPassKernel<<<divUp(capacity > 0 ? capacity : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
+void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_t s) {
+    ++launchCount(); colourPassKernel<<<divUp(d.NB, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
 }
 
-void launchOverflowSolve(const Dev &d, int nBodies, const StepParams &p, bool inPlace, cudaStream_t s) {
+void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, int block, cudaStream_t s) {
     ++launchCount();
-    overflowSolveKernel<<<divUp(nBodies > 0 ? nBodies : 1, kSolveThreads), kSolveThreads, 0, s>>>(d, nBodies, p,
-                                                                                                 inPlace ? 1 : 0);
+    overflowSolveKernel<<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
 }
 
-void launchOverflowApply(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s) {
+void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {
     ++launchCount();
-    overflowApplyKernel<<<grid(nBodies), kThreads, 0, s>>>(d, nBodies, p);
+    overflowApplyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
 }
 
-void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s) {
-    ++launchCount(); dualKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, stamps ? 1 : 0, decay);
+void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, int block, cudaStream_t s) {
+    ++launchCount(); dualKernel<<<divUp(d.MM, block), block, 0, s>>>(d, p, stamps ? 1 : 0, decay);
 }
 
-void launchForceDual(const Dev &d, const StepParams &p, int nForces, cudaStream_t s) {
-    if (nForces <= 0)
+void launchForceDual(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {
+    if (!forces)
         return;
-    ++launchCount(); forceDualKernel<<<grid(nForces), kThreads, 0, s>>>(d, p);
+    ++launchCount(); forceDualKernel<<<grid(d.FF), kThreads, 0, s>>>(d, p);
 }
 
 } // namespace avbdg

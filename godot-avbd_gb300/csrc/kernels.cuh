@@ -5,51 +5,66 @@
 
 namespace avbdg {
 
+// Kernels with one thread per independent item take their block size from the autotuner (their
+// results do not depend on it); the candidates are the sizes each kernel's registers allow.
+constexpr int kTuneCandidates = 4;
+struct TuneSpace {
+    int sizes[kTuneCandidates];
+    int count;
+};
+constexpr TuneSpace kTuneDual{{64, 128, 256, 512}, 4};     // dualKernel (126 registers)
+constexpr TuneSpace kTuneSolve{{32, 64, 128, 0}, 3};       // overflowSolveKernel (launch bound 128)
+constexpr TuneSpace kTuneNarrow{{64, 128, 256, 512}, 4};   // manifoldInitKernel
+constexpr TuneSpace kTuneTraverse{{64, 128, 256, 512}, 4}; // traverseKernel
+
 // ---- broad phase (k_broad.cu) ----
-void launchAabb(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
-// Morton codes per body for the worlds listed as rebuilding (all worlds when `all`), then the
-// stable (world, code, list index) sort into leafBody and the Karras topology per world.
-void launchRebuildTree(const Dev &d, int nBodies, int nWorlds, cudaStream_t s);
-void launchRefit(const Dev &d, int nBodies, cudaStream_t s);
+// Body and world counts come from the device (C_BODIES, C_WORLDS); grids cover the capacities,
+// so a captured step stays valid while worlds are added or removed.
+void launchAabb(const Dev &d, const StepParams &p, cudaStream_t s);
+// Morton codes per body, the stable (code, list position) sort, with `multiWorld` a second stable
+// pass by world so each world's leaves are contiguous, then the Karras topology per world.
+void launchRebuildTree(const Dev &d, bool multiWorld, cudaStream_t s);
+void launchRefit(const Dev &d, cudaStream_t s);
 // Candidate pairs: traversal count, scan, emit, per-segment sort. Leaves the count in C_PAIRS.
-void launchPairs(const Dev &d, int nBodies, cudaStream_t s);
+void launchPairs(const Dev &d, int block, cudaStream_t s);
 // Exact filter and acquisition of new manifolds after the live ones (C_CAND = C_LIVE + new).
 void launchFilterAcquire(const Dev &d, cudaStream_t s);
 
 // ---- manifolds and adjacency (k_manifold.cu) ----
-void launchAdjacency(const Dev &d, int nBodies, cudaStream_t s);
-void launchManifoldInit(const Dev &d, const StepParams &p, cudaStream_t s);
+void launchAdjacency(const Dev &d, cudaStream_t s);
+void launchManifoldInit(const Dev &d, const StepParams &p, int block, cudaStream_t s);
 void launchManifoldCompact(const Dev &d, cudaStream_t s);
 void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s);
-void launchForceInit(const Dev &d, const StepParams &p, int nForces, cudaStream_t s);
+void launchForceInit(const Dev &d, const StepParams &p, bool forces, cudaStream_t s);
 
 // ---- update set and colouring (k_solve.cu) ----
-void launchContactOnly(const Dev &d, int nBodies, cudaStream_t s);
-// Greedy colouring of dynamic bodies in list order (when `needGreedy`), colours in d.colour.
-void launchColour(const Dev &d, int nBodies, bool needGreedy, cudaStream_t s);
+void launchContactOnly(const Dev &d, cudaStream_t s);
+// Greedy colouring of dynamic bodies in list order (when `needGreedy`), colours in d.colour;
+// unless `everyWorld`, only worlds a force touches are coloured (the rest go to overflow).
+void launchColour(const Dev &d, bool needGreedy, bool everyWorld, cudaStream_t s);
 // Contact-only bodies to the overflow colour, then per-colour body lists and counts.
-void launchColourLists(const Dev &d, int nBodies, int contactOnlyOverflow, cudaStream_t s);
+void launchColourLists(const Dev &d, int contactOnlyOverflow, cudaStream_t s);
 
 // ---- substep (k_solve.cu) ----
-void launchWarmstartBodies(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
-void launchFinishBodies(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
+void launchWarmstartBodies(const Dev &d, const StepParams &p, cudaStream_t s);
+void launchFinishBodies(const Dev &d, const StepParams &p, cudaStream_t s);
 // Stamps (precompute) of manifolds touching the overflow set; `mixedOnly` restricts to those that
 // also touch a coloured body (recomputed after the colour passes).
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
-void launchColourPass(const Dev &d, int colour, int capacity, const StepParams &p, cudaStream_t s);
+void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_t s);
 // Block-Jacobi solve of every dynamic body in the overflow colour (walked in slot order).
-void launchOverflowSolve(const Dev &d, int nBodies, const StepParams &p, bool inPlace, cudaStream_t s);
-void launchOverflowApply(const Dev &d, int nBodies, const StepParams &p, cudaStream_t s);
+void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, int block, cudaStream_t s);
+void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s);
 // Dual pass over live manifolds; with `stamps`, also the next round's stamps of manifolds whose
 // bodies are all overflow or static. `decay` < 1 scales penalties first (dual-only rounds).
-void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, cudaStream_t s);
-void launchForceDual(const Dev &d, const StepParams &p, int nForces, cudaStream_t s);
+void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, int block, cudaStream_t s);
+void launchForceDual(const Dev &d, const StepParams &p, bool forces, cudaStream_t s);
 
 // ---- projection (k_proj.cu) ----
 // projectionActive per world and the brake candidates (manifolds with an open gap).
-void launchProjActive(const Dev &d, int nWorlds, cudaStream_t s);
-void launchBrake(const Dev &d, int nWorlds, float window, cudaStream_t s);
-void launchProjection(const Dev &d, int nBodies, int nWorlds, const StepParams &p, cudaStream_t s);
+void launchProjActive(const Dev &d, cudaStream_t s);
+void launchBrake(const Dev &d, float window, cudaStream_t s);
+void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s);
 
 int brakeGridBlocks();
 int colourGridBlocks();
@@ -60,5 +75,12 @@ void prepareKernels();
 // Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).
 void launchPackState(const Dev &d, int first, int count, float *buf, cudaStream_t s);
 void launchUnpackState(const Dev &d, int first, int count, const float *buf, int mask, cudaStream_t s);
+
+// ---- world removal (k_relocate.cu) ----
+// Moves the surviving worlds' bodies down to their new bases (remap: per old world, new id or -1
+// and new base), drops the removed worlds' manifolds and forces, keeping live and force order.
+// The caller uploads the new world table afterwards and then rebuilds the list-position map.
+void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const int *remap, cudaStream_t s);
+void launchListPositions(const Dev &d, int nBodies, cudaStream_t s);
 
 } // namespace avbdg

@@ -283,6 +283,75 @@ def batch(worlds=4096, n_min=8, n_max=512, seed=7, steps=120):
     return out
 
 
+def _grid_pile(rng, b, count, z0=1.0, edge_range=(0.25, 2.0), density_range=(100.0, 1e4), friction=0.5):
+    """A pile for large requests without the per-body rejection loop: the same size, density and
+    orientation distributions as `_place_pile`, each box centred at a random point of its own cell
+    of a cubic grid (cell = the largest bounding diameter), cells filled bottom-up, so no two
+    bounding spheres overlap."""
+    sizes = np.exp(rng.uniform(math.log(edge_range[0]), math.log(edge_range[1]), (count, 3)))
+    dens = np.exp(rng.uniform(math.log(density_range[0]), math.log(density_range[1]), count))
+    quats = _random_quats(rng, count)
+    radii = 0.5 * np.linalg.norm(sizes, axis=1)
+    cell = 2.0 * float(radii.max()) + 0.05
+    side = max(2, int(math.ceil((count / 2.0) ** (1.0 / 3.0))))  # footprint side x side, ~2x as tall
+    idx = np.arange(count)
+    ij = np.stack([idx % side, (idx // side) % side, idx // (side * side)], axis=1).astype(np.float64)
+    slack = (cell / 2.0 - radii)[:, None]
+    centres = (ij + 0.5) * cell + rng.uniform(-1.0, 1.0, (count, 3)) * slack
+    centres[:, 0] -= side * cell / 2.0
+    centres[:, 1] -= side * cell / 2.0
+    centres[:, 2] += z0
+    for i in range(count):
+        b.box(sizes[i].astype(F32), dens[i], friction, centres[i].astype(F32), quats[i])
+    return side * cell
+
+
+def request_world(rng, n_target, chain_links=8):
+    """One request of the served stream, about `n_target` dynamic boxes: pyramid walls (3-20 rows,
+    as many parallel walls as the size asks for) or a pile (sizes, densities and orientations as
+    the mass-ratio pile) with a short ball-jointed chain, each on its own static ground."""
+    b = _Builder()
+    if rng.random() < 0.5:
+        rows = int(rng.integers(3, 21))
+        per_wall = rows * (rows + 1) // 2
+        walls = max(1, int(round(n_target / per_wall)))
+        extent = max(60.0, 1.6 * walls + 2.0 * rows)
+        b.box((extent, extent, 1), 0.0, 0.5, (0, 0, -0.5))
+        for wall in range(walls):
+            y = (_f(wall) - _f(walls - 1) * _f(0.5)) * _f(1.6)
+            for r in range(rows):
+                cnt = rows - r
+                for k in range(cnt):
+                    x = (_f(k) - _f(cnt - 1) * _f(0.5)) * _f(1.01)
+                    b.box((1, 1, 1), 1.0, 0.5, (x, y, _f(0.5) + _f(r)))
+    else:
+        count = max(1, n_target - chain_links)
+        b.box((400, 400, 1), 0.0, 0.5, (0, 0, -0.5))
+        width = _grid_pile(rng, b, count)
+        if chain_links > 0:
+            x0 = width / 2.0 + 4.0
+            prev = b.box((0.2, 0.2, 1.0), 0.0, 0.5, (x0, 0.0, chain_links + 4.0))
+            for i in range(chain_links):
+                link = b.box((0.2, 0.2, 1.0), 1000.0, 0.5, (x0, 0.0, _f(chain_links + 3.0) - _f(i)))
+                b.joint(prev, link, (0, 0, -0.5), (0, 0, 0.5), INF, 0.0)
+                prev = link
+    return b.scene("request")
+
+
+def request_stream(requests=200, n_min=16, n_max=16384, steps_min=60, steps_max=600, seed=11):
+    """Requests of the served workload: body counts log-uniform in [n_min, n_max], steps uniform in
+    [steps_min, steps_max]; each scene carries its step count in `steps`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(requests):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        w = request_world(rng, n)
+        w.params = dict(BENCH_PARAMS)
+        w.steps = int(rng.integers(steps_min, steps_max + 1))
+        out.append(w)
+    return out
+
+
 # ----------------------------------------------------------------------------------------------
 # Instantiation
 # ----------------------------------------------------------------------------------------------

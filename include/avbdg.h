@@ -112,6 +112,9 @@ typedef struct avbdg_stats {
     int manifold_sides;           /* (manifold, side) pairs whose body moves: stamps per round */
     int graph_step;               /* 1 if the last step ran as one CUDA graph launch */
     int kernel_launches;          /* kernels of this library in the last step */
+    /* block sizes the autotuner picked (0 while it is still trying candidates): manifold dual,
+     * overflow block solve, narrow phase, tree traversal */
+    int block_dual, block_solve, block_narrow, block_traverse;
 } avbdg_stats;
 
 /* ------------------------------------------------------------------------------------ */
@@ -257,6 +260,10 @@ int avbdg_batch_destroy(avbdg_batch *batch);
 /* Append a world with its bodies (creation order) and forces (creation order). */
 int avbdg_batch_add_world(avbdg_batch *batch, int body_count, const avbdg_body_desc *bodies,
                           int force_count, const avbdg_force_desc *forces, int *out_world);
+/* Remove `count` worlds (indices as returned by avbdg_batch_add_world). The other worlds keep
+ * their order and are renumbered 0.. in it; their state and results are unaffected (Solver::clear
+ * for the removed worlds, src/avbd/solver_step.cpp:29-40). */
+int avbdg_batch_remove_worlds(avbdg_batch *batch, int count, const int *worlds);
 /* `count` steps of every world (Solver::step each). */
 int avbdg_batch_step(avbdg_batch *batch, int count);
 int avbdg_batch_sync(avbdg_batch *batch);
@@ -273,6 +280,68 @@ int avbdg_batch_digest(avbdg_batch *batch, int world, uint64_t *out);
 int avbdg_batch_get_stats(avbdg_batch *batch, avbdg_stats *out);
 int avbdg_batch_set_profiling(avbdg_batch *batch, int enabled);
 int avbdg_batch_take_kernel_times(avbdg_batch *batch, avbdg_kernel_times *out);
+
+/* ------------------------------------------------------------------------------------ */
+/* Served form: continuous batching of scenes on one device store                        */
+/* ------------------------------------------------------------------------------------ */
+
+/* Replaces the physics server's per-space stepping loop (AVBDPhysicsServer3D::_step,
+ * src/server/avbd_physics_server3d.cpp:1396-1424, one Solver::step per active space in turn) for
+ * many scenes at once: each request is one scene (one space, _space_create :318) asking for a
+ * number of steps. Requests wait in arrival order until a slot and their device bytes fit the
+ * budget, then stay resident on the device (bodies, manifolds with their duals, forces, tree)
+ * until their steps are done; every tick advances every resident scene by one Solver::step in the
+ * same launches, so requests that arrive while others run overlap with them on the device. A
+ * scene's final state is identical to stepping it alone. Calls on one server are serialised by
+ * the caller. */
+typedef struct avbdg_server avbdg_server;
+
+typedef struct avbdg_server_stats {
+    int64_t submitted, admitted, completed, evicted; /* requests since creation */
+    int64_t ticks;                /* ticks that stepped the device, since the last reset */
+    int queued;                   /* waiting for a slot or for bytes */
+    int resident;                 /* on the device */
+    int resident_bodies;
+    int resident_dynamic;
+    uint64_t resident_bytes;      /* device bytes the resident requests are charged */
+    uint64_t store_bytes;         /* device bytes the store holds now */
+    uint64_t budget_bytes;
+    double body_steps;            /* dynamic body-steps since the last reset */
+    double busy_ms;               /* host wall time inside ticks since the last reset */
+    double tick_p50_ms, tick_p99_ms, tick_max_ms; /* per-tick wall time (admit + step + retire) */
+    double request_p50_ms, request_p99_ms;        /* admit call -> result ready */
+    /* where tick time went since the last reset: admitting, stepping, retiring (ms), and how
+     * many ticks stepped as one captured CUDA graph */
+    double admit_ms, step_ms, retire_ms;
+    int64_t graph_ticks;
+} avbdg_server_stats;
+
+/* `budget_bytes` bounds the device store (a request is charged what a store of its size needs);
+ * `max_resident` bounds the scenes on the device at once. */
+int avbdg_server_create(const avbdg_params *params, uint64_t budget_bytes, int max_resident,
+                        avbdg_server **out);
+int avbdg_server_destroy(avbdg_server *server);
+/* Queue a scene: bodies and forces in creation order (as avbdg_batch_add_world) and the number of
+ * steps it asks for (>= 1). Invalid scenes, and scenes larger than the whole budget, are refused
+ * here (AVBDG_ERR_INVALID / UNSUPPORTED / NONFINITE / CAPACITY). */
+int avbdg_server_admit(avbdg_server *server, int body_count, const avbdg_body_desc *bodies,
+                       int force_count, const avbdg_force_desc *forces, int steps,
+                       int64_t *out_request);
+/* Admit what fits, step every resident scene once, retire finished scenes (results kept on the
+ * host until taken). `completed` = requests finished by this tick. */
+int avbdg_server_tick(avbdg_server *server, int *completed);
+/* Oldest finished request whose result was not taken yet; *out_request = -1 if none. */
+int avbdg_server_poll(avbdg_server *server, int64_t *out_request, int *out_body_count);
+/* Final state of a finished request (count = its body count; NULL fields are skipped); the
+ * result is released. Layout as avbdg_world_get_body_state. */
+int avbdg_server_take_result(avbdg_server *server, int64_t request, int count, float *position,
+                             float *orientation, float *velocity, float *angular_velocity);
+/* Cancel a queued or resident request (no result), or release a finished one's result
+ * (_free_rid :292 for a space). */
+int avbdg_server_evict(avbdg_server *server, int64_t request);
+int avbdg_server_get_stats(avbdg_server *server, avbdg_server_stats *out);
+/* Restart the tick/latency/throughput window (counts of requests are kept). */
+int avbdg_server_reset_stats(avbdg_server *server);
 
 /* ------------------------------------------------------------------------------------ */
 /* Standalone kernels                                                                   */
