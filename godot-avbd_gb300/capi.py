@@ -113,8 +113,36 @@ class KernelTimes(C.Structure):
     ]
 
 
+AXIS_FREE, AXIS_LOCKED, AXIS_LIMITED = 0, 1, 2
+
+
+class JointAxis(C.Structure):
+    """avbdg_joint_axis: one degree of freedom of a generic joint."""
+
+    _fields_ = [
+        ("mode", C.c_int),
+        ("lower", C.c_float),
+        ("upper", C.c_float),
+        ("spring_stiffness", C.c_float),
+        ("spring_equilibrium", C.c_float),
+        ("spring_damping", C.c_float),
+    ]
+
+
+def make_axes(axes):
+    """Six (mode, lower, upper, spring_stiffness, spring_equilibrium, spring_damping) tuples ->
+    avbdg_joint_axis[6] (linear x, y, z, then angular x, y, z)."""
+    out = (JointAxis * 6)()
+    for i, ax in enumerate(axes):
+        out[i].mode = int(ax[0])
+        out[i].lower, out[i].upper = float(ax[1]), float(ax[2])
+        out[i].spring_stiffness, out[i].spring_equilibrium, out[i].spring_damping = (float(ax[3]), float(ax[4]),
+                                                                                     float(ax[5]))
+    return out
+
+
 class ForceDesc(C.Structure):
-    """avbdg_force_desc: kind 0 = Joint, 1 = IgnoreCollision."""
+    """avbdg_force_desc: kind 0 = Joint, 1 = IgnoreCollision, 2 = Spring, 3 = GenericJoint."""
 
     _fields_ = [
         ("kind", C.c_int),
@@ -125,6 +153,8 @@ class ForceDesc(C.Structure):
         ("stiffness_lin", C.c_float),
         ("stiffness_ang", C.c_float),
         ("fracture", C.c_float),
+        ("rest", C.c_float),
+        ("axes", JointAxis * 6),
     ]
 
 
@@ -151,6 +181,8 @@ _WORLD_FUNCS = {
     "world_add_joint": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, C.c_float, C.c_float, C.c_float,
                         C.POINTER(C.c_int)],
     "world_add_ignore_collision": [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)],
+    "world_add_spring": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, C.c_float, C.c_float, C.POINTER(C.c_int)],
+    "world_add_generic_joint": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, C.POINTER(JointAxis), C.POINTER(C.c_int)],
     "world_step": [C.c_void_p],
     "world_step_interleaved": [C.c_void_p, C.c_int, C.c_int],
     "world_step_n": [C.c_void_p, C.c_int],
@@ -287,6 +319,35 @@ class World:
         self.api.check(self.api.world_add_ignore_collision(self.handle, int(a), int(b), C.byref(out)))
         return out.value
 
+    def add_spring(self, a, b, r_a, r_b, stiffness, rest=-1.0):
+        ra = (C.c_float * 3)(*r_a)
+        rb = (C.c_float * 3)(*r_b)
+        out = C.c_int()
+        self.api.check(self.api.world_add_spring(self.handle, int(a), int(b), ra, rb, float(stiffness), float(rest),
+                                                 C.byref(out)))
+        return out.value
+
+    def add_generic_joint(self, a, b, r_a, r_b, axes):
+        ra = (C.c_float * 3)(*r_a)
+        rb = (C.c_float * 3)(*r_b)
+        out = C.c_int()
+        self.api.check(self.api.world_add_generic_joint(self.handle, int(a), int(b), ra, rb, make_axes(axes),
+                                                        C.byref(out)))
+        return out.value
+
+    def add_force(self, force):
+        """One scene force record (see scenes.Scene.joints) in creation order."""
+        if force[0] == "spring":
+            _, a, b, ra, rb, k, rest = force
+            return self.add_spring(a, b, ra, rb, k, rest)
+        if force[0] == "generic":
+            _, a, b, ra, rb, axes = force
+            return self.add_generic_joint(a, b, ra, rb, axes)
+        if force[0] == "ignore":
+            return self.add_ignore_collision(force[1], force[2])
+        a, b, ra, rb, kl, ka, fr = force
+        return self.add_joint(a, b, ra, rb, kl, ka, fr)
+
     def step(self, n=1):
         if n == 1:
             self.api.check(self.api.world_step(self.handle))
@@ -387,15 +448,30 @@ class World:
 
 
 def make_force_descs(joints):
-    """Pack (a, b, rA, rB, kLin, kAng, fracture) joint tuples into an avbdg_force_desc array."""
+    """Pack scene force records (ball-joint tuples (a, b, rA, rB, kLin, kAng, fracture), or
+    ("spring", a, b, rA, rB, k, rest), ("generic", a, b, rA, rB, axes), ("ignore", a, b)) into an
+    avbdg_force_desc array, creation order kept."""
     descs = (ForceDesc * max(len(joints), 1))()
-    for i, (a, b, ra, rb, kl, ka, fr) in enumerate(joints):
+    for i, force in enumerate(joints):
         d = descs[i]
-        d.kind = 0
+        if force[0] == "spring":
+            _, a, b, ra, rb, k, rest = force
+            d.kind, d.stiffness_lin, d.rest = 2, float(k), float(rest)
+        elif force[0] == "generic":
+            _, a, b, ra, rb, axes = force
+            d.kind = 3
+            d.axes[:] = list(make_axes(axes))
+        elif force[0] == "ignore":
+            _, a, b = force
+            ra = rb = (0.0, 0.0, 0.0)
+            d.kind = 1
+        else:
+            a, b, ra, rb, kl, ka, fr = force
+            d.kind = 0
+            d.stiffness_lin, d.stiffness_ang, d.fracture = float(kl), float(ka), float(fr)
         d.body_a, d.body_b = int(a), int(b)
         d.r_a[:] = list(ra)
         d.r_b[:] = list(rb)
-        d.stiffness_lin, d.stiffness_ang, d.fracture = float(kl), float(ka), float(fr)
     return descs
 
 

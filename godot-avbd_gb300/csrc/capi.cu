@@ -196,6 +196,46 @@ int avbdg_world_add_ignore_collision(avbdg_world *w, int a, int b, int *id) {
     });
 }
 
+int avbdg_world_add_spring(avbdg_world *w, int a, int b, const float r_a[3], const float r_b[3], float stiffness,
+                           float rest, int *id) {
+    if (!r_a || !r_b)
+        return failWith(AVBDG_ERR_INVALID, "null anchor");
+    avbdg_force_desc f{};
+    f.kind = 2;
+    f.body_a = a;
+    f.body_b = b;
+    std::memcpy(f.r_a, r_a, sizeof(f.r_a));
+    std::memcpy(f.r_b, r_b, sizeof(f.r_b));
+    f.stiffness_lin = stiffness;
+    f.rest = rest;
+    return guarded(w, [&](avbdg::Engine &e) {
+        const int rc = e.addForces(0, 1, &f);
+        if (rc == AVBDG_OK && id)
+            *id = 0;
+        return rc;
+    });
+}
+
+int avbdg_world_add_generic_joint(avbdg_world *w, int a, int b, const float r_a[3], const float r_b[3],
+                                  const avbdg_joint_axis axes[6], int *id) {
+    if (!r_a || !r_b || !axes)
+        return failWith(AVBDG_ERR_INVALID, "null anchor or axes");
+    avbdg_force_desc f{};
+    f.kind = 3;
+    f.body_a = a;
+    f.body_b = b;
+    std::memcpy(f.r_a, r_a, sizeof(f.r_a));
+    std::memcpy(f.r_b, r_b, sizeof(f.r_b));
+    for (int i = 0; i < 6; i++)
+        f.axes[i] = axes[i];
+    return guarded(w, [&](avbdg::Engine &e) {
+        const int rc = e.addForces(0, 1, &f);
+        if (rc == AVBDG_OK && id)
+            *id = 0;
+        return rc;
+    });
+}
+
 int avbdg_world_step(avbdg_world *w) {
     return guarded(w, [](avbdg::Engine &e) { return e.step(); });
 }

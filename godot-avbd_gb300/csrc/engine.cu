@@ -125,6 +125,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
     take(n.fKind, ff);
     take(n.fBroken, ff);
     take(n.fKeep, ff);
+    take(n.fExt, static_cast<size_t>(ff) * kExtF4);
     take(n.adjStart, static_cast<size_t>(nb) + 1);
     take(n.adjFill, nb);
     const size_t adjCap = 2 * (static_cast<size_t>(ff) + mm);
@@ -141,7 +142,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
     n.scanScratch = scan;
     n.radixScratch = radix;
     take(n.relocInt, static_cast<size_t>(nb) + ff);
-    take(n.relocF4, std::max(nb, ff));
+    take(n.relocF4, std::max(static_cast<size_t>(nb), static_cast<size_t>(ff) * kExtF4));
     take(n.relocRemap, 2 * static_cast<size_t>(ww));
 }
 
@@ -256,6 +257,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
                         std::make_pair(n.fLL, old.fLL), std::make_pair(n.fLA, old.fLA), std::make_pair(n.fPar, old.fPar)})
             cp(pr.first, pr.second, fCopy * sizeof(float4));
         cp(n.fKind, old.fKind, fCopy * sizeof(int));
+        cp(n.fExt, old.fExt, fCopy * kExtF4 * sizeof(float4));
         cp(n.fBroken, old.fBroken, fCopy * sizeof(int));
         cudaStreamSynchronize(stream);
         for (void *p : oldAllocs)
@@ -324,15 +326,23 @@ int Engine::validateBodies(int count, const avbdg_body_desc *descs, std::string 
 int Engine::validateForces(int nb, int count, const avbdg_force_desc *descs, std::string &why) {
     for (int i = 0; i < count; i++) {
         const avbdg_force_desc &f = descs[i];
-        if (f.kind != 0 && f.kind != 1) {
-            why = "only ball joints and ignore pairs run on the GPU path";
+        if (f.kind < 0 || f.kind > 3) {
+            why = "unknown force kind";
             return AVBDG_ERR_UNSUPPORTED;
         }
-        const int aMin = f.kind == 0 ? -1 : 0;
+        // Ball and generic joints may anchor to the world (body_a = -1); springs and ignore pairs
+        // join two bodies.
+        const int aMin = (f.kind == 0 || f.kind == 3) ? -1 : 0;
         if (f.body_b < 0 || f.body_b >= nb || f.body_a < aMin || f.body_a >= nb) {
             why = "bad body index";
             return AVBDG_ERR_INVALID;
         }
+        if (f.kind == 3)
+            for (const avbdg_joint_axis &ax : f.axes)
+                if (ax.mode < AVBDG_AXIS_FREE || ax.mode > AVBDG_AXIS_LIMITED) {
+                    why = "bad generic joint axis mode";
+                    return AVBDG_ERR_INVALID;
+                }
     }
     return AVBDG_OK;
 }
@@ -489,15 +499,48 @@ int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
     int rc = ensureCapacity(nBodies, nForces + count, worlds());
     if (rc)
         return rc;
-    std::vector<float4> sizes(n);
+    // Torque arms, spring rest lengths and generic-joint zeros read the bodies' current state.
+    std::vector<float4> sizes(n), xs(n), qs(n);
     cudaMemcpy(sizes.data(), d.size + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(xs.data(), d.x + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(qs.data(), d.q + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
     std::vector<int2> ab(count);
     std::vector<float4> ra(count), rb(count), par(count), zero(count, make_float4(0, 0, 0, 0));
+    std::vector<float4> ext(static_cast<size_t>(count) * kExtF4, make_float4(0, 0, 0, 0));
     std::vector<int> kind(count), broken(count, 0);
     for (int i = 0; i < count; i++) {
         const avbdg_force_desc &f = descs[i];
         kind[i] = f.kind;
         ab[i] = make_int2(f.body_a >= 0 ? wBase[w] + f.body_a : -1, wBase[w] + f.body_b);
+        if (f.kind == 2) {
+            // Spring::Spring (spring.cpp:16-27): rest < 0 -> the anchors' current distance.
+            const f3 rA{f.r_a[0], f.r_a[1], f.r_a[2]}, rB{f.r_b[0], f.r_b[1], f.r_b[2]};
+            float rest = f.rest;
+            if (rest < 0.0f) {
+                const f3 pA = add(xyz(xs[f.body_a]), qrot(asq(qs[f.body_a]), rA));
+                const f3 pB = add(xyz(xs[f.body_b]), qrot(asq(qs[f.body_b]), rB));
+                rest = length(sub(pA, pB));
+            }
+            ra[i] = make_float4(rA.x, rA.y, rA.z, 0.0f);
+            rb[i] = make_float4(rB.x, rB.y, rB.z, 0.0f);
+            par[i] = make_float4(f.stiffness_lin, rest, 0.0f, 0.0f);
+            continue;
+        }
+        if (f.kind == 3) {
+            // GenericJoint::GenericJoint (generic_joint.cpp:24-30): zero = B relative to A now.
+            const q4 qA = f.body_a >= 0 ? asq(qs[f.body_a]) : q4{0.0f, 0.0f, 0.0f, 1.0f};
+            float4 *e = ext.data() + static_cast<size_t>(i) * kExtF4;
+            e[0] = f4(qmul(qconj(qA), asq(qs[f.body_b])));
+            for (int k = 0; k < 6; k++) {
+                const avbdg_joint_axis &ax = f.axes[k];
+                e[1 + k] = make_float4(static_cast<float>(ax.mode), ax.lower, ax.upper, ax.spring_stiffness);
+                e[7 + k] = make_float4(ax.spring_equilibrium, ax.spring_damping, 0.0f, 0.0f);
+            }
+            ra[i] = make_float4(f.r_a[0], f.r_a[1], f.r_a[2], 0.0f);
+            rb[i] = make_float4(f.r_b[0], f.r_b[1], f.r_b[2], 0.0f);
+            par[i] = make_float4(0, 0, 0, 0);
+            continue;
+        }
         if (f.kind == 0) {
             // torqueArm = length2((A ? A.size : 0) + B.size) (joint.cpp:38-39), as in addJoint.
             const float4 sa = f.body_a >= 0 ? sizes[f.body_a] : make_float4(0, 0, 0, 0);
@@ -525,6 +568,8 @@ int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
     cudaMemcpyAsync(d.fPar + f0, par.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fKind + f0, kind.data(), bi, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fBroken + f0, broken.data(), bi, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fExt + static_cast<size_t>(f0) * kExtF4, ext.data(), sizeof(float4) * ext.size(),
+                    cudaMemcpyHostToDevice, stream);
     nForces += count;
     cudaMemcpyAsync(d.ctr + C_FORCES, &nForces, sizeof(int), cudaMemcpyHostToDevice, stream);
     cudaStreamSynchronize(stream);
@@ -856,7 +901,7 @@ void Engine::runSubstep(const StepParams &sp, int rounds) {
                 launchStamps(d, sp, true, stream);
             }
             beginSpan();
-            launchOverflowSolve(d, sp, inPlace, tuned.solve, stream);
+            launchOverflowSolve(d, sp, inPlace, nForces > 0, tuned.solve, stream);
             endSpan(kBody);
             if (!inPlace)
                 launchOverflowApply(d, sp, stream);

@@ -25,6 +25,7 @@ constexpr int kMaxColours = 8;
 constexpr uint8_t kOverflowColour = 8;
 constexpr uint8_t kUncoloured = 255;
 constexpr int kStampF4 = 7; // float4 per (manifold, side) stamp
+constexpr int kExtF4 = 16;  // float4 per force of the generic-joint record (forces.cuh)
 
 constexpr float PENALTY_MIN = 1.0f;
 constexpr float PENALTY_MAX = 10000000000.0f;
@@ -116,6 +117,7 @@ struct Dev {
     int2 *fAB;
     float4 *fRA, *fRB, *fC0L, *fC0A, *fKL, *fKA, *fLL, *fLA, *fPar; // fPar: stiffLin, stiffAng, fracture, torqueArm
     int *fKind, *fBroken, *fKeep;
+    float4 *fExt;           // generic joints: kExtF4 float4 per force (forces.cuh)
     // adjacency (dynamic bodies only): sequence numbers, forces first (list order) then manifolds
     int *adjStart, *adjFill;
     uint32_t *adjSeq, *adjTmp;
@@ -125,7 +127,8 @@ struct Dev {
     int *ctr;
     int *longList;
     void *scanScratch, *radixScratch;
-    // world removal: slot map (NB) + force ranks (FF), staging of max(NB, FF) records, world remap
+    // world removal: slot map (NB) + force ranks (FF), staging of max(NB, FF * kExtF4) records,
+    // world remap
     int *relocInt;
     float4 *relocF4;
     int *relocRemap;        // 2 per world: new id (-1 = removed), new base slot

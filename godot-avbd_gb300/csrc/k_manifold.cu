@@ -6,6 +6,7 @@
 // survivors back in order (the reference's stable compaction of `live`). Slot recycling is an
 // allocation detail of the reference that never reaches its arithmetic, so it has no equivalent.
 
+#include "forces.cuh"
 #include "kernels.cuh"
 #include "narrow.cuh"
 #include "prims.cuh"
@@ -300,7 +301,10 @@ __global__ void forceInitKernel(Dev d, StepParams p) {
     const int nf = d.ctr[C_FORCES];
     if (f >= nf)
         return;
-    if (d.fKind[f] != 0) { // IgnoreCollision: always active, no state
+    const int kind = d.fKind[f];
+    if (kind == kForceGeneric)
+        genericInit(d, p, f);
+    if (kind != kForceBall) { // IgnoreCollision, Spring, GenericJoint: never reaped
         d.fKeep[f] = 1;
         return;
     }
@@ -339,6 +343,8 @@ __global__ void forceCompactKernel(Dev d) {
             d.fPar[w] = d.fPar[f];
             d.fKind[w] = d.fKind[f];
             d.fBroken[w] = d.fBroken[f];
+            for (int k = 0; k < kExtF4; k++)
+                d.fExt[static_cast<size_t>(w) * kExtF4 + k] = d.fExt[static_cast<size_t>(f) * kExtF4 + k];
         }
         w++;
     }

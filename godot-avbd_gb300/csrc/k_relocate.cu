@@ -98,6 +98,16 @@ __global__ void compactKernel(const T *src, T *dst, const int *keep, const int *
         dst[rank[i]] = src[i];
 }
 
+// Strided records (kExtF4 float4 per force) follow their force.
+__global__ void compactExtKernel(const float4 *src, float4 *dst, const int *keep, const int *rank, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * kExtF4)
+        return;
+    const int f = i / kExtF4;
+    if (keep[f])
+        dst[static_cast<size_t>(rank[f]) * kExtF4 + i % kExtF4] = src[i];
+}
+
 // List position -> body of every world's range, from the (new) world table.
 __global__ void listPosKernel(Dev d, int n) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,7 +154,7 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
 
     // Forces: flags + exclusive rank, then a stable scatter of every field.
     if (nForces > 0) {
-        // relocF4 holds max(NB, FF) float4: room for two int2 arrays of FF entries.
+        // relocF4 holds max(NB, FF * kExtF4) float4: room for two int2 arrays of FF entries.
         int2 *abNew = reinterpret_cast<int2 *>(tmp4);
         int *rank = d.relocInt + d.NB;
         ++launchCount(); forceFlagKernel<<<grid(nForces), kThreads, 0, s>>>(d, nForces, slotMap, abNew);
@@ -157,6 +167,12 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
         int *tmpI = reinterpret_cast<int *>(tmp4);
         compactArray(d.fKind, tmpI, d.fKeep, rank, nForces, s);
         compactArray(d.fBroken, tmpI, d.fKeep, rank, nForces, s);
+        // Generic-joint records (relocF4 holds FF * kExtF4 float4).
+        float4 *extTmp = d.relocF4;
+        ++launchCount();
+        compactExtKernel<<<grid(nForces * kExtF4), kThreads, 0, s>>>(d.fExt, extTmp, d.fKeep, rank, nForces);
+        cudaMemcpyAsync(d.fExt, extTmp, sizeof(float4) * static_cast<size_t>(nForces) * kExtF4,
+                        cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(d.ctr + C_FORCES, d.ctr + C_TMP, sizeof(int), cudaMemcpyDeviceToDevice, s);
     }
 }

@@ -13,6 +13,7 @@
 // Coloured (Gauss-Seidel) bodies recompute their manifold terms from the current poses at every
 // touch; the reference's "first touch uses the dual's cache" rule yields the same floats.
 
+#include "forces.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -505,9 +506,7 @@ __device__ __forceinline__ m3 geometricStiffness(int k, f3 v) {
     return m;
 }
 
-__device__ void jointStamp(const Dev &d, const StepParams &p, int f, int body, Blk &blk) {
-    if (d.fKind[f] != 0)
-        return;
+__device__ void ballStamp(const Dev &d, const StepParams &p, int f, int body, Blk &blk) {
     const int2 ab = d.fAB[f];
     const bool isA = body == ab.x;
     const float4 par = d.fPar[f];
@@ -553,9 +552,28 @@ __device__ void jointStamp(const Dev &d, const StepParams &p, int f, int body, B
     }
 }
 
+// A non-manifold force's stamp into body `body`'s block (Force::updatePrimal by kind).
+// Not inlined: forces are rare next to manifolds, and inlining all kinds would raise the
+// register count of every body pass.
+__device__ __noinline__ void jointStamp(const Dev &d, const StepParams &p, int f, int body, Blk &blk) {
+    const int kind = d.fKind[f];
+    if (kind == kForceBall)
+        ballStamp(d, p, f, body, blk);
+    else if (kind == kForceSpring)
+        springStamp(d, f, body, blk);
+    else if (kind == kForceGeneric)
+        genericStamp(d, p, f, body, blk);
+}
+
 __global__ void forceDualKernel(Dev d, StepParams p) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= d.ctr[C_FORCES] || d.fKind[f] != 0)
+    if (f >= d.ctr[C_FORCES])
+        return;
+    if (d.fKind[f] == kForceGeneric) {
+        genericDual(d, p, f);
+        return;
+    }
+    if (d.fKind[f] != kForceBall)
         return;
     const float4 par = d.fPar[f];
     f3 kl = xyz(d.fKL[f]), ka = xyz(d.fKA[f]);
@@ -596,13 +614,16 @@ __device__ __forceinline__ int nForcesDev(const Dev &d) { return d.ctr[C_FORCES]
 
 // Assemble body g's block from its adjacency; manifold terms from stamps (Jacobi) or recomputed
 // from the current poses (Gauss-Seidel).
-template <bool RECOMPUTE>
+// Without FORCES (a store with no non-manifold force) the force branch is compiled out, so the
+// body passes keep their registers in registers.
+template <bool RECOMPUTE, bool FORCES = true>
 __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk) {
     const int nf = nForcesDev(d);
     for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
         const int seq = static_cast<int>(d.adjSeq[e]);
         if (seq < nf) {
-            jointStamp(d, p, nf - 1 - seq, g, blk);
+            if (FORCES)
+                jointStamp(d, p, nf - 1 - seq, g, blk);
             continue;
         }
         const int m = seq - nf;
@@ -667,13 +688,14 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
 }
 
 // Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
+template <bool FORCES>
 __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
         return;
     Blk blk = bodyBlock(d, p, g);
-    assemble<false>(d, p, g, blk);
+    assemble<false, FORCES>(d, p, g, blk);
     f3 dl, da;
     solveBlock(blk, dl, da);
     if (inPlace) {
@@ -958,9 +980,12 @@ void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_
     ++launchCount(); colourPassKernel<<<divUp(d.NB, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
 }
 
-void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, int block, cudaStream_t s) {
+void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s) {
     ++launchCount();
-    overflowSolveKernel<<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
+    if (forces)
+        overflowSolveKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
+    else
+        overflowSolveKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
 }
 
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {

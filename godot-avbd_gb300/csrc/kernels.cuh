@@ -53,7 +53,7 @@ void launchFinishBodies(const Dev &d, const StepParams &p, cudaStream_t s);
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
 void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_t s);
 // Block-Jacobi solve of every dynamic body in the overflow colour (walked in slot order).
-void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, int block, cudaStream_t s);
+void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s);
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s);
 // Dual pass over live manifolds; with `stamps`, also the next round's stamps of manifolds whose
 // bodies are all overflow or static. `decay` < 1 scales penalties first (dual-only rounds).

@@ -34,7 +34,9 @@ class Scene:
     position: np.ndarray      # n x 3
     orientation: np.ndarray   # n x 4 {x, y, z, w}
     velocity: np.ndarray      # n x 3
-    joints: list = field(default_factory=list)   # (a, b, rA, rB, kLin, kAng, fracture)
+    # Forces in creation order: ball joints (a, b, rA, rB, kLin, kAng, fracture),
+    # ("spring", a, b, rA, rB, k, rest), ("generic", a, b, rA, rB, six axis tuples)
+    joints: list = field(default_factory=list)
     params: dict = field(default_factory=dict)   # solver field overrides
     steps: int = 0
     substeps: int = 0          # > 1: stepInterleaved(substeps, rounds)
@@ -67,6 +69,14 @@ class _Builder:
     def joint(self, a, b, ra, rb, k_lin=INF, k_ang=0.0, fracture=INF):
         self.joints.append((a, b, tuple(float(x) for x in ra), tuple(float(x) for x in rb),
                             float(k_lin), float(k_ang), float(fracture)))
+
+    def spring(self, a, b, ra, rb, stiffness, rest=-1.0):
+        self.joints.append(("spring", a, b, tuple(float(x) for x in ra), tuple(float(x) for x in rb),
+                            float(stiffness), float(rest)))
+
+    def generic(self, a, b, ra, rb, axes):
+        self.joints.append(("generic", a, b, tuple(float(x) for x in ra), tuple(float(x) for x in rb),
+                            tuple(tuple(float(v) for v in ax) for ax in axes)))
 
     def scene(self, name, **kw):
         n = len(self.size)
@@ -141,6 +151,65 @@ def hard_chain(links=4, steps=300):
         b.joint(prev, link, (0, 0, -0.5), (0, 0, 0.5), INF, 0.0)
         prev = link
     return b.scene("hard_chain", steps=steps)
+
+
+# Axis presets of a generic joint: (mode, lower, upper, spring stiffness, equilibrium, damping).
+FREE = (0, 0.0, 0.0, 0.0, 0.0, 0.0)
+LOCK = (1, 0.0, 0.0, 0.0, 0.0, 0.0)
+
+
+def limited(lower, upper):
+    return (2, lower, upper, 0.0, 0.0, 0.0)
+
+
+def sprung(stiffness, equilibrium=0.0, damping=0.0):
+    return (0, 0.0, 0.0, stiffness, equilibrium, damping)
+
+
+def joint_zoo(steps=240):
+    """Every force kind the step supports, each in its own corner of one ground: a hinged
+    pendulum (GenericJoint, one free rotation), a vertical slider that falls to its limit, a
+    sprung-and-damped swing, a bungee (sprung linear axis) under a world anchor, a hanging chain
+    of Springs, a ball-jointed pair, an ignore pair resting inside each other, and free boxes
+    dropped onto the pendulum and the slider."""
+    b = _Builder()
+    b.box((60, 60, 1), 0.0, 0.5, (0, 0, -0.5))
+    # Hinge about x: a post, a 2 m arm pivoting at the post's top, released horizontally.
+    post = b.box((0.4, 0.4, 6), 0.0, 0.5, (-10, 0, 3))
+    arm = b.box((0.3, 2.0, 0.3), 2.0, 0.5, (-10, 1.2, 6.2))
+    b.generic(post, arm, (0, 0.2, 3.2), (0, -1.0, 0), (LOCK, LOCK, LOCK, FREE, LOCK, LOCK))
+    # Slider along z, limited to [-1.5, 0] below its start, everything else locked.
+    rail = b.box((0.5, 0.5, 0.5), 0.0, 0.5, (-4, 0, 8))
+    car = b.box((1, 1, 1), 1.0, 0.5, (-4, 0, 6))
+    b.generic(rail, car, (0, 0, -2), (0, 0, 0), (LOCK, LOCK, limited(-1.5, 0.0), LOCK, LOCK, LOCK))
+    # Swing with a sprung, damped rotation about y (equilibrium tilted) and a limited x rotation.
+    pivot = b.box((0.4, 0.4, 0.4), 0.0, 0.5, (2, 0, 7))
+    swing = b.box((0.5, 0.5, 2.0), 1.5, 0.5, (2, 0, 5.6))
+    b.generic(pivot, swing, (0, 0, -0.2), (0, 0, 1.2),
+              (LOCK, LOCK, LOCK, limited(-0.3, 0.3), sprung(40.0, 0.4, 3.0), LOCK))
+    # Bungee: world-anchored, linear z sprung, x/y locked, rotations free.
+    bob = b.box((0.6, 0.6, 0.6), 1.0, 0.5, (8, 0, 6))
+    b.generic(-1, bob, (8, 0, 9), (0, 0, 0.3), (LOCK, LOCK, sprung(60.0, 2.7, 1.5), FREE, FREE, FREE))
+    # Chain of Springs from a static hook, rest lengths from the creation pose, one explicit.
+    hook = b.box((0.3, 0.3, 0.3), 0.0, 0.5, (14, 0, 10))
+    prev = hook
+    for i in range(4):
+        link = b.box((0.4, 0.4, 0.4), 1.0, 0.5, (14, 0, _f(9.0) - _f(i) * _f(1.2)))
+        b.spring(prev, link, (0, 0, -0.15), (0, 0, 0.2), 300.0, -1.0 if i else 0.9)
+        prev = link
+    # Ball-jointed pair and an ignore pair.
+    a1 = b.box((1, 1, 1), 1.0, 0.5, (-16, 0, 3))
+    a2 = b.box((1, 1, 1), 1.0, 0.5, (-16, 0, 4.2))
+    b.joint(a1, a2, (0, 0, 0.6), (0, 0, -0.6), INF, 0.0)
+    g1 = b.box((1, 1, 1), 1.0, 0.5, (16, -8, 0.5))
+    g2 = b.box((0.6, 0.6, 0.6), 1.0, 0.5, (16, -8, 0.7))
+    b.joints.append(("ignore", g1, g2))
+    # Free boxes falling onto the pendulum arm and the slider car.
+    for i in range(4):
+        b.box((0.5, 0.5, 0.5), 1.0, 0.5, (_f(-10.0), _f(1.6), _f(8.0) + _f(i) * _f(0.8)))
+    for i in range(3):
+        b.box((0.6, 0.6, 0.6), 1.0, 0.5, (_f(-4.0), _f(0.0), _f(9.0) + _f(i) * _f(1.0)))
+    return b.scene("joint_zoo", params=dict(BENCH_PARAMS), steps=steps)
 
 
 # ----------------------------------------------------------------------------------------------
@@ -374,8 +443,8 @@ def instantiate(api, scene, world_cls=None, params=None):
     descs = capi.make_body_descs(scene.size, scene.density, scene.friction, scene.position,
                                  scene.orientation, scene.velocity)
     w.add_bodies(descs)
-    for (a, b, ra, rb, kl, ka, fr) in scene.joints:
-        w.add_joint(a, b, ra, rb, kl, ka, fr)
+    for force in scene.joints:
+        w.add_force(force)
     return w
 
 

@@ -161,6 +161,30 @@ int avbdg_world_add_joint(avbdg_world *world, int body_a, int body_b, const floa
 /* new IgnoreCollision(solver, a, b) (src/avbd/forces.hpp:103-113). */
 int avbdg_world_add_ignore_collision(avbdg_world *world, int body_a, int body_b, int *out_id);
 
+/* new Spring(solver, a, b, rA, rB, stiffness, rest) (src/avbd/forces.hpp:89-101,
+ * src/avbd/spring.cpp:16-27). Both bodies are required; rest < 0 takes the anchors' current
+ * distance. */
+int avbdg_world_add_spring(avbdg_world *world, int body_a, int body_b, const float r_a[3],
+                           const float r_b[3], float stiffness, float rest, int *out_id);
+
+/* One degree of freedom of a generic joint (JointAxis / AxisMode, src/avbd/forces.hpp:115-145). */
+#define AVBDG_AXIS_FREE 0
+#define AVBDG_AXIS_LOCKED 1
+#define AVBDG_AXIS_LIMITED 2
+typedef struct avbdg_joint_axis {
+    int mode;                     /* AVBDG_AXIS_* */
+    float lower, upper;           /* bounds of a limited axis */
+    float spring_stiffness;       /* 0 = no spring */
+    float spring_equilibrium;
+    float spring_damping;
+} avbdg_joint_axis;
+
+/* new GenericJoint(solver, a, b, rA, rB) with its six axes set (src/avbd/forces.hpp:147-190,
+ * src/avbd/generic_joint.cpp:24-30): axes[0..2] linear x/y/z, axes[3..5] angular x/y/z, in
+ * A's frame (the world's for body_a = -1). The current arrangement is the joint's zero. */
+int avbdg_world_add_generic_joint(avbdg_world *world, int body_a, int body_b, const float r_a[3],
+                                  const float r_b[3], const avbdg_joint_axis axes[6], int *out_id);
+
 /* Solver::step (src/avbd/solver_step.cpp:44-75). Enqueued on the world's stream; the state
  * accessors below synchronise. */
 int avbdg_world_step(avbdg_world *world);
@@ -248,10 +272,12 @@ typedef struct avbdg_batch avbdg_batch;
 /* One force of a world (forces.hpp:58-113): kind 0 = Joint, 1 = IgnoreCollision. Body indices
  * are creation indices within the world; body_a = -1 anchors a joint to the world point r_a. */
 typedef struct avbdg_force_desc {
-    int kind;
+    int kind;                     /* 0 ball joint, 1 ignore pair, 2 spring, 3 generic joint */
     int body_a, body_b;
     float r_a[3], r_b[3];
-    float stiffness_lin, stiffness_ang, fracture;
+    float stiffness_lin, stiffness_ang, fracture; /* ball joint; a spring's stiffness is stiffness_lin */
+    float rest;                   /* spring rest length (< 0: the anchors' distance at creation) */
+    avbdg_joint_axis axes[6];     /* generic joint */
 } avbdg_force_desc;
 
 int avbdg_batch_create(const avbdg_params *params, int max_worlds, int max_bodies, int max_forces,

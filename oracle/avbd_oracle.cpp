@@ -727,6 +727,261 @@ void World::jointUpdateDual(Force &f) {
     }
 }
 
+// Spring::Spring (spring.cpp:16-27): a negative rest length is the anchors' current distance.
+void World::addSpring(int a, int b, V3 rA, V3 rB, float stiffness, float rest) {
+    Force f;
+    f.kind = kSpring;
+    f.a = a;
+    f.b = b;
+    f.rA = rA;
+    f.rB = rB;
+    f.springK = stiffness;
+    if (rest < 0.0f) {
+        const Body &A = bodies[a], &B = bodies[b];
+        rest = length((A.x + qrot(A.q, rA)) - (B.x + qrot(B.q, rB)));
+    }
+    f.rest = rest;
+    forces.insert(forces.begin(), f);
+}
+
+// GenericJoint::GenericJoint (generic_joint.cpp:24-30): its zero is the creation arrangement.
+void World::addGeneric(int a, int b, V3 rA, V3 rB, const Axis axes[6]) {
+    Force f;
+    f.kind = kGeneric;
+    f.a = a;
+    f.b = b;
+    f.rA = rA;
+    f.rB = rB;
+    for (int i = 0; i < 6; i++)
+        f.axis[i] = axes[i];
+    f.restQ = qmul(qconj(frameOrientation(f)), bodies[b].q);
+    forces.insert(forces.begin(), f);
+}
+
+static M3 outerprod(V3 a, V3 b) { return mcols(a * b.x, a * b.y, a * b.z); }
+
+// Spring::updatePrimal (spring.cpp:31-70).
+void World::springUpdatePrimal(const Force &f, int body, Block &blk) const {
+    const Body &A = bodies[f.a], &B = bodies[f.b];
+    const V3 pA = A.x + qrot(A.q, f.rA);
+    const V3 pB = B.x + qrot(B.q, f.rB);
+    const V3 d = pA - pB;
+    const float dLen = length(d);
+    if (dLen <= 1.0e-6f)
+        return;
+    const V3 n = d / dLen;
+    const float C = dLen - f.rest;
+    const float force = f.springK * C;
+    V3 jLin, jAng;
+    if (body == f.a) {
+        const V3 r = qrot(A.q, f.rA);
+        jLin = n;
+        jAng = cross(r, n);
+    } else {
+        const V3 r = qrot(B.q, f.rB);
+        jLin = -n;
+        jAng = -cross(r, n);
+    }
+    const V3 F = jLin * force;
+    const V3 tau = jAng * force;
+    const M3 kll = outerprod(jLin, jLin) * f.springK;
+    const M3 kla = outerprod(jAng, jLin) * f.springK;
+    const M3 kaa = outerprod(jAng, jAng) * f.springK;
+    blk.lhsLin += kll;
+    blk.lhsAng += kaa;
+    blk.lhsCross += kla;
+    blk.rhsLin += F;
+    blk.rhsAng += tau;
+}
+
+static V3 unitAxis(int i) { return i == 0 ? V3{1, 0, 0} : (i == 1 ? V3{0, 1, 0} : V3{0, 0, 1}); }
+static float qcomp(Q4 q, int i) { return i == 0 ? q.x : (i == 1 ? q.y : (i == 2 ? q.z : q.w)); }
+static float v3comp(V3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+// maths.h qinv: conj(q) / qlength2(q).
+static Q4 qinvm(Q4 q) {
+    const float l = qlength2(q);
+    return Q4{-q.x / l, -q.y / l, -q.z / l, q.w / l};
+}
+
+Q4 World::frameOrientation(const Force &f) const {
+    return f.a >= 0 ? bodies[f.a].q : Q4{0.0f, 0.0f, 0.0f, 1.0f};
+}
+
+// qrot(conj(qA), anchorA - anchorB) (generic_joint.cpp:37-45, 100-104).
+V3 World::genericOffset(const Force &f) const {
+    const V3 anchorA = f.a >= 0 ? bodies[f.a].x + qrot(bodies[f.a].q, f.rA) : f.rA;
+    const Body &B = bodies[f.b];
+    const V3 anchorB = B.x + qrot(B.q, f.rB);
+    return qrot(qconj(frameOrientation(f)), anchorA - anchorB);
+}
+
+// Swing-twist measurement (generic_joint.cpp:49-98): each non-locked axis takes its twist
+// (2 atan2(v.n, w)), the locked axes read the remaining swing.
+void World::genericAngles(const Force &f, float out[3]) const {
+    const Q4 qA = frameOrientation(f);
+    const Q4 relativeNow = qmul(qconj(qA), qnormalize(bodies[f.b].q));
+    Q4 dev = qmul(qnormalize(f.restQ), qconj(relativeNow));
+    for (int i = 0; i < 3; i++) {
+        if (f.axis[3 + i].mode == kLocked)
+            continue;
+        const float proj = dot(V3{dev.x, dev.y, dev.z}, unitAxis(i));
+        const Q4 twist{dev.x * proj, dev.y * proj, dev.z * proj, dev.w};
+        if (std::sqrt(qlength2(twist)) <= 1.0e-12f) {
+            out[i] = 0.0f;
+            continue;
+        }
+        out[i] = 2.0f * std::atan2(proj, dev.w);
+        dev = qmul(qnormalize(dev), qinvm(twist));
+    }
+    for (int i = 0; i < 3; i++)
+        if (f.axis[3 + i].mode == kLocked)
+            out[i] = qcomp(dev, i) * 2.0f;
+}
+
+// GenericJoint::penaltyLimit (generic_joint.cpp:198-222).
+float World::penaltyLimit(int body, V3 axis, bool angular) const {
+    const Body &b = bodies[body];
+    float effective;
+    if (angular) {
+        const V3 local = qrot(qconj(b.q), axis);
+        effective = local.x * local.x * b.moment.x + local.y * local.y * b.moment.y + local.z * local.z * b.moment.z;
+    } else {
+        effective = b.mass;
+    }
+    if (effective <= 0.0f)
+        return PENALTY_MAX;
+    const float limit = effective * 0.25f * 0.25f / (P.dt * P.dt);
+    return smin(limit, PENALTY_MAX);
+}
+
+// GenericJoint::initialize (generic_joint.cpp:224-245).
+void World::genericInitialize(Force &f) {
+    float ang[3];
+    genericAngles(f, ang);
+    const V3 offset = genericOffset(f);
+    for (int i = 0; i < 3; i++) {
+        f.axis[i].initial = v3comp(offset, i);
+        f.axis[3 + i].initial = ang[i];
+        for (int k = 0; k < 2; k++) {
+            Axis &ax = f.axis[3 * k + i];
+            ax.lambda = ax.lambda * (P.alpha * P.gamma);
+            ax.penalty = sclamp(ax.penalty * P.gamma, PENALTY_MIN, PENALTY_MAX);
+        }
+    }
+}
+
+// axisConstraint + axisForce (generic_joint.cpp:120-168).
+static bool axisForce(const Axis &ax, float value, float alpha, float &C, float &F) {
+    if (ax.mode == kLocked) {
+        C = value;
+    } else if (ax.mode == kLimited) {
+        if (value > ax.upper)
+            C = value - ax.upper;
+        else if (value < ax.lower)
+            C = value - ax.lower;
+        else
+            return false;
+    } else {
+        return false;
+    }
+    if (ax.mode == kLocked)
+        C -= ax.initial * alpha;
+    float force = ax.penalty * C + ax.lambda;
+    if (ax.mode == kLimited)
+        force = C > 0.0f ? smax(force, 0.0f) : smin(force, 0.0f);
+    F = force;
+    return true;
+}
+
+// GenericJoint::stampAxis (generic_joint.cpp:170-196).
+static void stampAxis(Block &blk, const Axis &ax, float value, float alpha, V3 jLin, V3 jAng, float rate) {
+    float C, F;
+    if (axisForce(ax, value, alpha, C, F)) {
+        blk.lhsLin += outerprod(jLin, jLin) * ax.penalty;
+        blk.lhsAng += outerprod(jAng, jAng) * ax.penalty;
+        blk.lhsCross += outerprod(jAng, jLin) * ax.penalty;
+        blk.rhsLin += jLin * F;
+        blk.rhsAng += jAng * F;
+    }
+    if (ax.springK > 0.0f) {
+        const float Cs = value - ax.springEq;
+        const float Fs = ax.springK * Cs - ax.springDamp * rate;
+        blk.lhsLin += outerprod(jLin, jLin) * ax.springK;
+        blk.lhsAng += outerprod(jAng, jAng) * ax.springK;
+        blk.lhsCross += outerprod(jAng, jLin) * ax.springK;
+        blk.rhsLin += jLin * Fs;
+        blk.rhsAng += jAng * Fs;
+    }
+}
+
+// GenericJoint::updatePrimal (generic_joint.cpp:247-287).
+void World::genericUpdatePrimal(const Force &f, int body, Block &blk) const {
+    const Q4 qA = frameOrientation(f);
+    const Body &B = bodies[f.b];
+    const V3 rAWorld = qrot(qA, f.rA);
+    const V3 rBWorld = qrot(B.q, f.rB);
+    const V3 offset = genericOffset(f);
+    float ang[3];
+    genericAngles(f, ang);
+    const bool isA = body == f.a;
+    const float sign = isA ? 1.0f : -1.0f;
+    const V3 arm = isA ? rAWorld : rBWorld;
+    const V3 vA = f.a >= 0 ? bodies[f.a].v + cross(bodies[f.a].w, rAWorld) : V3{0, 0, 0};
+    const V3 vB = B.v + cross(B.w, rBWorld);
+    const V3 relV = vA - vB;
+    const V3 wA = f.a >= 0 ? bodies[f.a].w : V3{0, 0, 0};
+    const V3 wB = B.w;
+    for (int i = 0; i < 3; i++) {
+        const V3 axis = qrot(qA, unitAxis(i));
+        const V3 jLin = axis * sign;
+        const V3 jAng = cross(arm, jLin);
+        stampAxis(blk, f.axis[i], v3comp(offset, i), P.alpha, jLin, jAng, dot(relV, axis));
+        stampAxis(blk, f.axis[3 + i], ang[i], P.alpha, V3{0, 0, 0}, axis * sign, dot(wA - wB, axis));
+    }
+}
+
+// GenericJoint::updateDual (generic_joint.cpp:289-319).
+void World::genericUpdateDual(Force &f) {
+    float ang[3];
+    genericAngles(f, ang);
+    const V3 offset = genericOffset(f);
+    for (int i = 0; i < 3; i++) {
+        const float values[2] = {v3comp(offset, i), ang[i]};
+        const float betas[2] = {P.beta_lin, P.beta_ang};
+        for (int k = 0; k < 2; k++) {
+            Axis &ax = f.axis[3 * k + i];
+            float C, F;
+            if (!axisForce(ax, values[k], P.alpha, C, F)) {
+                if (ax.mode == kLimited)
+                    ax.lambda = 0.0f;
+                continue;
+            }
+            ax.lambda = F;
+            const V3 dir = qrot(frameOrientation(f), unitAxis(i));
+            float cap = penaltyLimit(f.b, dir, k == 1);
+            if (f.a >= 0)
+                cap = smin(cap, penaltyLimit(f.a, dir, k == 1));
+            ax.penalty = sclamp(ax.penalty + std::fabs(C) * betas[k], 0.0f, cap);
+        }
+    }
+}
+
+void World::forceUpdatePrimal(const Force &f, int body, Block &blk) const {
+    if (f.kind == kJoint)
+        jointUpdatePrimal(f, body, blk);
+    else if (f.kind == kSpring)
+        springUpdatePrimal(f, body, blk);
+    else if (f.kind == kGeneric)
+        genericUpdatePrimal(f, body, blk);
+}
+
+void World::forceUpdateDual(Force &f) {
+    if (f.kind == kJoint)
+        jointUpdateDual(f);
+    else if (f.kind == kGeneric)
+        genericUpdateDual(f);
+}
+
 // ------------------------------------------------------------------------------------------
 // Manifolds (src/avbd/manifold.cpp)
 // ------------------------------------------------------------------------------------------
@@ -1282,7 +1537,7 @@ int World::warmstartForces() {
     std::vector<Force> kept;
     kept.reserve(forces.size());
     for (Force &f : forces)
-        if (jointInitialize(f))
+        if (f.kind == kGeneric ? (genericInitialize(f), true) : jointInitialize(f))
             kept.push_back(f);
     forces.swap(kept);
     // Independent per manifold (the reference dispatches this loop to its pool too); the stable
@@ -1441,7 +1696,7 @@ void World::iterate(int rounds, int forceCount) {
                     if (ref.manifold)
                         manifoldUpdatePrimal(live[ref.index], id, blk);
                     else
-                        jointUpdatePrimal(forces[ref.index], id, blk);
+                        forceUpdatePrimal(forces[ref.index], id, blk);
                 }
                 V3 dl, da;
                 solveDelta(blk, dl, da);
@@ -1474,7 +1729,7 @@ void World::iterate(int rounds, int forceCount) {
                     if (ref.manifold)
                         stampCached(live[ref.index], id, blk);
                     else
-                        jointUpdatePrimal(forces[ref.index], id, blk);
+                        forceUpdatePrimal(forces[ref.index], id, blk);
                 }
                 solveDelta(blk, dLin[i], dAng[i]);
             }
@@ -1499,7 +1754,7 @@ void World::iterate(int rounds, int forceCount) {
         }
 #pragma omp parallel for schedule(static) if (parallel())
         for (int f = 0; f < forceCount; f++)
-            jointUpdateDual(forces[f]);
+            forceUpdateDual(forces[f]);
         (void)alpha;
     }
 }

@@ -51,15 +51,29 @@ struct Body {
     bool contactOnly = true;
 };
 
-enum ForceKind { kJoint = 0, kIgnore = 1 };
+enum ForceKind { kJoint = 0, kIgnore = 1, kSpring = 2, kGeneric = 3 };
+
+// One degree of freedom of a generic joint (JointAxis, src/avbd/forces.hpp:130-145).
+enum AxisMode { kFree = 0, kLocked = 1, kLimited = 2 };
+struct Axis {
+    int mode = kFree;
+    float lower = 0, upper = 0;
+    float springK = 0, springEq = 0, springDamp = 0;
+    float lambda = 0, penalty = 0, initial = 0;
+};
 
 struct Force {
     ForceKind kind = kJoint;
     int a = -1, b = -1; // body ids; a = -1 means the world
-    // Joint state (src/avbd/forces.hpp:58-87).
+    // Joint state (src/avbd/forces.hpp:58-87); rA/rB are also the Spring and GenericJoint anchors.
     V3 rA{}, rB{}, C0Lin{}, C0Ang{}, kLin{}, kAng{}, lamLin{}, lamAng{};
     float stiffLin = 0, stiffAng = 0, fracture = 0, torqueArm = 0;
     bool broken = false;
+    // Spring (forces.hpp:89-101).
+    float springK = 0, rest = 0;
+    // GenericJoint (forces.hpp:147-190): B relative to A at creation, linear axes 0-2, angular 3-5.
+    Q4 restQ{0, 0, 0, 1};
+    Axis axis[6];
 };
 
 struct Contact {
@@ -108,6 +122,8 @@ public:
     void invalidateTree() { treeBodies = -1; }
     void addJoint(int a, int b, V3 rA, V3 rB, float kLin, float kAng, float fracture);
     void addIgnore(int a, int b);
+    void addSpring(int a, int b, V3 rA, V3 rB, float stiffness, float rest);
+    void addGeneric(int a, int b, V3 rA, V3 rB, const Axis axes[6]);
     void step();
     void stepInterleaved(int substeps, int rounds);
     uint64_t digest() const;
@@ -159,6 +175,18 @@ private:
     bool jointInitialize(Force &f);
     void jointUpdatePrimal(const Force &f, int body, struct Block &block) const;
     void jointUpdateDual(Force &f);
+    // Spring and GenericJoint pieces (src/avbd/spring.cpp, generic_joint.cpp).
+    void springUpdatePrimal(const Force &f, int body, struct Block &block) const;
+    Q4 frameOrientation(const Force &f) const;
+    V3 genericOffset(const Force &f) const;
+    void genericAngles(const Force &f, float out[3]) const;
+    float penaltyLimit(int body, V3 axis, bool angular) const;
+    void genericInitialize(Force &f);
+    void genericUpdatePrimal(const Force &f, int body, struct Block &block) const;
+    void genericUpdateDual(Force &f);
+    // Primal and dual of any non-manifold force.
+    void forceUpdatePrimal(const Force &f, int body, struct Block &block) const;
+    void forceUpdateDual(Force &f);
 };
 
 // Box-box narrow phase with a speculative margin (src/avbd/collide.cpp:1001-1098). Exposed for

@@ -155,6 +155,37 @@ int avbdo_world_add_ignore_collision(World *w, int a, int b, int *id) {
     return AVBDG_OK;
 }
 
+int avbdo_world_add_spring(World *w, int a, int b, const float *rA, const float *rB, float stiffness, float rest,
+        int *id) {
+    if (!w || a < 0 || b < 0 || a >= w->count() || b >= w->count() || !rA || !rB)
+        return fail(AVBDG_ERR_INVALID, "bad body index");
+    w->addSpring(a, b, V3{rA[0], rA[1], rA[2]}, V3{rB[0], rB[1], rB[2]}, stiffness, rest);
+    if (id)
+        *id = 0;
+    return AVBDG_OK;
+}
+
+int avbdo_world_add_generic_joint(World *w, int a, int b, const float *rA, const float *rB,
+        const avbdg_joint_axis *axes, int *id) {
+    if (!w || b < 0 || b >= w->count() || a < -1 || a >= w->count() || !rA || !rB || !axes)
+        return fail(AVBDG_ERR_INVALID, "bad body index");
+    Axis ax[6];
+    for (int i = 0; i < 6; i++) {
+        if (axes[i].mode < 0 || axes[i].mode > 2)
+            return fail(AVBDG_ERR_INVALID, "bad axis mode");
+        ax[i].mode = axes[i].mode;
+        ax[i].lower = axes[i].lower;
+        ax[i].upper = axes[i].upper;
+        ax[i].springK = axes[i].spring_stiffness;
+        ax[i].springEq = axes[i].spring_equilibrium;
+        ax[i].springDamp = axes[i].spring_damping;
+    }
+    w->addGeneric(a, b, V3{rA[0], rA[1], rA[2]}, V3{rB[0], rB[1], rB[2]}, ax);
+    if (id)
+        *id = 0;
+    return AVBDG_OK;
+}
+
 int avbdo_world_step(World *w) {
     if (!w)
         return fail(AVBDG_ERR_INVALID, "null world");

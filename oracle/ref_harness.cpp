@@ -225,6 +225,38 @@ int avbdr_world_add_ignore_collision(RefWorld *w, int a, int b, int *id) {
     return AVBDG_OK;
 }
 
+int avbdr_world_add_spring(RefWorld *w, int a, int b, const float *rA, const float *rB, float stiffness,
+        float rest, int *id) {
+    if (!w || a < 0 || b < 0 || a >= (int)w->bodies.size() || b >= (int)w->bodies.size())
+        return fail(AVBDG_ERR_INVALID, "bad body index");
+    new Spring(&w->solver, w->bodies[a], w->bodies[b], float3{rA[0], rA[1], rA[2]}, float3{rB[0], rB[1], rB[2]},
+            stiffness, rest);
+    if (id)
+        *id = 0;
+    return AVBDG_OK;
+}
+
+int avbdr_world_add_generic_joint(RefWorld *w, int a, int b, const float *rA, const float *rB,
+        const avbdg_joint_axis *axes, int *id) {
+    if (!w || b < 0 || b >= (int)w->bodies.size() || a >= (int)w->bodies.size() || a < -1 || !axes)
+        return fail(AVBDG_ERR_INVALID, "bad body index");
+    Rigid *ba = a >= 0 ? w->bodies[a] : nullptr;
+    GenericJoint *j = new GenericJoint(&w->solver, ba, w->bodies[b], float3{rA[0], rA[1], rA[2]},
+            float3{rB[0], rB[1], rB[2]});
+    for (int i = 0; i < 6; i++) {
+        JointAxis &ax = i < 3 ? j->linear[i] : j->angular[i - 3];
+        ax.mode = static_cast<AxisMode>(axes[i].mode);
+        ax.lower = axes[i].lower;
+        ax.upper = axes[i].upper;
+        ax.springStiffness = axes[i].spring_stiffness;
+        ax.springEquilibrium = axes[i].spring_equilibrium;
+        ax.springDamping = axes[i].spring_damping;
+    }
+    if (id)
+        *id = 0;
+    return AVBDG_OK;
+}
+
 int avbdr_world_step(RefWorld *w) {
     if (!w)
         return fail(AVBDG_ERR_INVALID, "null world");

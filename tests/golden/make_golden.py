@@ -7,6 +7,9 @@ godot-avbd_gb300/scenes.py and records, per scene:
   - the sorted candidate pairs, Morton codes and (code, index) order after the first step,
   - the live manifolds' body ids, contact counts and feature keys after the first and last step,
   - the colouring of the last step.
+Scenes whose arithmetic calls the C library's atan2 (generic joints with limited or sprung
+rotations) are recorded with per-step digests plus the full pose of every body at a few steps, for
+tolerance comparisons (the GPU calls CUDA's atan2f).
 Writes tests/golden/reference_runs.json. Usage: python tests/golden/make_golden.py
 """
 
@@ -31,6 +34,12 @@ RUNS = [
     ("pyramid420", {}, 120),
     ("pile", {"count": 300, "chain_links": 8}, 120),
     ("lattice", {"nx": 8, "ny": 8, "nz": 4}, 90),
+]
+
+
+# (scene builder, keyword arguments, steps recorded, steps whose poses are stored)
+POSE_RUNS = [
+    ("joint_zoo", {}, 60, [1, 10, 20, 30, 60]),
 ]
 
 
@@ -75,6 +84,22 @@ def main():
         rec["digests"] = digests
         out["runs"][name] = rec
         print(name, sc.n, "bodies", steps, "steps, last digest", digests[-1], flush=True)
+    out["pose_runs"] = {}
+    for name, kw, steps, keep in POSE_RUNS:
+        sc = getattr(scenes, name)(**kw)
+        p = ref.default_params()
+        p.threads = 1
+        w = scenes.instantiate(ref, sc, params=p)
+        rec = {"scene": name, "kwargs": kw, "steps": steps, "bodies": sc.n, "digests": [], "poses": {}}
+        for s in range(steps):
+            scenes.advance(w, sc, 1)
+            rec["digests"].append(f"{w.digest():016x}")
+            if s + 1 in keep:
+                pos, quat, _, _ = w.state()
+                rec["poses"][str(s + 1)] = {"position": [[float(v) for v in r] for r in pos],
+                                            "orientation": [[float(v) for v in r] for r in quat]}
+        out["pose_runs"][name] = rec
+        print(name, sc.n, "bodies", steps, "steps (poses kept)", flush=True)
     with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
         json.dump(out, f, indent=1)
 

@@ -50,6 +50,24 @@ def test_golden_runs(pkg, oracle, golden):
         assert sha(col) + sha(ids) == ls["colours_sha"], name
 
 
+def test_golden_pose_runs(pkg, oracle, golden):
+    """Springs and generic joints (hinge, slider, limited and sprung rotations, world anchor): the
+    oracle calls the same C library atan2 as the reference, so every step's digest and the stored
+    poses are exact."""
+    scenes = pkg.scenes
+    for name, rec in golden["pose_runs"].items():
+        sc = getattr(scenes, rec["scene"])(**rec["kwargs"])
+        w = scenes.instantiate(oracle, sc)
+        for s in range(rec["steps"]):
+            scenes.advance(w, sc, 1)
+            assert f"{w.digest():016x}" == rec["digests"][s], f"{name}: step {s + 1} digest differs"
+            pose = rec["poses"].get(str(s + 1))
+            if pose:
+                p, q, _, _ = w.state()
+                assert np.array_equal(p, np.asarray(pose["position"], np.float32))
+                assert np.array_equal(q, np.asarray(pose["orientation"], np.float32))
+
+
 @pytest.mark.parametrize("option", ["adaptive_beta", "stiffness_decay", "no_projection", "gs_contacts"])
 def test_oracle_matches_reference_options(pkg, oracle, ref, option):
     scenes = pkg.scenes
