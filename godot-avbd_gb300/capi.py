@@ -73,6 +73,7 @@ class BodyDesc(C.Structure):
         ("collision_mask", C.c_uint32),
         ("axis_lock_linear", C.c_uint32),
         ("axis_lock_angular", C.c_uint32),
+        ("sleep_mode", C.c_uint32),
     ]
 
 
@@ -188,6 +189,7 @@ _WORLD_FUNCS = {
     "world_step_n": [C.c_void_p, C.c_int],
     "world_sync": [C.c_void_p],
     "world_get_body_state": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp, _fp],
+    "world_get_sleeping": [C.c_void_p, C.c_int, C.c_int, _bp],
     "world_set_body_state": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp, _fp],
     "world_get_stats": [C.c_void_p, C.POINTER(Stats)],
     "world_digest": [C.c_void_p, _up],
@@ -233,7 +235,7 @@ class Api:
 
 
 def make_body_descs(size, density, friction, position, orientation=None, velocity=None,
-                    angular_velocity=None):
+                    angular_velocity=None, sleep_mode=None):
     """Pack per-body arrays (n x 3 / n x 4 / n) into an avbdg_body_desc array."""
     size = np.asarray(size, np.float32).reshape(-1, 3)
     n = size.shape[0]
@@ -247,6 +249,7 @@ def make_body_descs(size, density, friction, position, orientation=None, velocit
     if angular_velocity is None:
         angular_velocity = np.zeros((n, 3), np.float32)
     angular_velocity = np.asarray(angular_velocity, np.float32).reshape(n, 3)
+    sleep_mode = np.broadcast_to(np.asarray(0 if sleep_mode is None else sleep_mode, np.int64), (n,))
     descs = (BodyDesc * n)()
     for i in range(n):
         d = descs[i]
@@ -262,7 +265,14 @@ def make_body_descs(size, density, friction, position, orientation=None, velocit
         d.collision_mask = 1
         d.axis_lock_linear = 0
         d.axis_lock_angular = 0
+        d.sleep_mode = int(sleep_mode[i])
     return descs
+
+
+def scene_body_descs(scene):
+    """avbdg_body_desc array of a scenes.Scene, creation order."""
+    return make_body_descs(scene.size, scene.density, scene.friction, scene.position, scene.orientation,
+                           scene.velocity, sleep_mode=getattr(scene, "sleep_mode", None))
 
 
 class World:
@@ -380,6 +390,11 @@ class World:
         p, q, v, w = arr(position, 3), arr(orientation, 4), arr(velocity, 3), arr(angular_velocity, 3)
         self.api.check(self.api.world_set_body_state(self.handle, 0, n, _ptr(p, C.c_float), _ptr(q, C.c_float),
                                                      _ptr(v, C.c_float), _ptr(w, C.c_float)))
+
+    def sleeping(self):
+        out = np.zeros(self.n_bodies, np.uint8)
+        self.api.check(self.api.world_get_sleeping(self.handle, 0, self.n_bodies, _ptr(out, C.c_uint8)))
+        return out
 
     def stats(self):
         s = Stats()
@@ -519,8 +534,7 @@ class Batch:
             pass
 
     def add_scene(self, scene):
-        descs = make_body_descs(scene.size, scene.density, scene.friction, scene.position, scene.orientation,
-                                scene.velocity)
+        descs = scene_body_descs(scene)
         forces = make_force_descs(scene.joints)
         out = C.c_int()
         self._api.check(self.fn["batch_add_world"](self.handle, scene.n, descs, len(scene.joints), forces,
@@ -648,8 +662,7 @@ class Server:
         """Queue `scene` for `steps` steps; returns the request id. Pre-packed descriptor arrays
         (make_body_descs / make_force_descs) may be passed to keep packing out of a timed loop."""
         if descs is None:
-            descs = make_body_descs(scene.size, scene.density, scene.friction, scene.position, scene.orientation,
-                                    scene.velocity)
+            descs = scene_body_descs(scene)
         if forces is None:
             forces = make_force_descs(scene.joints)
         out = C.c_int64()

@@ -259,6 +259,10 @@ int avbdg_world_sync(avbdg_world *w) {
     return guarded(w, [](avbdg::Engine &e) { return e.sync(); });
 }
 
+int avbdg_world_get_sleeping(avbdg_world *w, int first, int count, uint8_t *out) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.getSleeping(0, first, count, out); });
+}
+
 int avbdg_world_get_body_state(avbdg_world *w, int first, int count, float *p, float *q, float *v, float *av) {
     return guarded(w, [=](avbdg::Engine &e) { return e.getState(0, first, count, p, q, v, av); });
 }

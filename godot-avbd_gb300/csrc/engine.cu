@@ -51,6 +51,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
     take(n.wBounds, 6 * static_cast<size_t>(ww));
     take(n.wActive, ww);
     take(n.wColour, ww);
+    take(n.wSleep, 2 * static_cast<size_t>(ww));
     take(n.x, nb);
     take(n.q, nb);
     take(n.x0, nb);
@@ -63,6 +64,8 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
     take(n.size, nb);
     take(n.moment, nb);
     take(n.meta, nb);
+    take(n.sleep, nb);
+    take(n.upd, nb);
     take(n.lpToBody, nb);
     take(n.contactOnly, nb);
     take(n.colour, nb);
@@ -141,6 +144,11 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
     take(radix, radixScratchBytes(nb + 1));
     n.scanScratch = scan;
     n.radixScratch = radix;
+    take(n.sleepRank, pp);
+    take(n.sleepList, pp);
+    take(n.island, nb);
+    take(n.islandAwake, nb);
+    take(n.islandStill, nb);
     take(n.relocInt, static_cast<size_t>(nb) + ff);
     take(n.relocF4, std::max(static_cast<size_t>(nb), static_cast<size_t>(ff) * kExtF4));
     take(n.relocRemap, 2 * static_cast<size_t>(ww));
@@ -231,6 +239,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
                         std::make_pair(n.size, old.size), std::make_pair(n.moment, old.moment)})
             cp(pr.first, pr.second, nbCopy * sizeof(float4));
         cp(n.meta, old.meta, nbCopy * sizeof(int4));
+        cp(n.sleep, old.sleep, nbCopy * sizeof(int2));
         cp(n.lpToBody, old.lpToBody, nbCopy * sizeof(int));
         cp(n.codes, old.codes, nbCopy * sizeof(uint64_t));
         cp(n.ctr, old.ctr, C_COUNT * sizeof(int));
@@ -313,6 +322,10 @@ int Engine::validateBodies(int count, const avbdg_body_desc *descs, std::string 
             why = "only box bodies run on the GPU path";
             return AVBDG_ERR_UNSUPPORTED;
         }
+        if (b.sleep_mode > 2) {
+            why = "sleep_mode must be 0, 1 or 2";
+            return AVBDG_ERR_INVALID;
+        }
         if (!finite3(b.size) || !finite3(b.position) || !finite3(b.velocity) || !finite3(b.angular_velocity) ||
             !std::isfinite(b.density) || !std::isfinite(b.friction) || !std::isfinite(b.orientation[0]) ||
             !std::isfinite(b.orientation[1]) || !std::isfinite(b.orientation[2]) || !std::isfinite(b.orientation[3])) {
@@ -388,7 +401,8 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
         sz[i] = make_float4(b.size[0], b.size[1], b.size[2], radius);
         mo[i] = make_float4(moment[0], moment[1], moment[2], b.friction);
         meta[i] = make_int4(w, static_cast<int>(b.collision_layer), static_cast<int>(b.collision_mask),
-                            static_cast<int>((b.axis_lock_linear & 0xff) | ((b.axis_lock_angular & 0xff) << 8)));
+                            static_cast<int>((b.axis_lock_linear & 0xff) | ((b.axis_lock_angular & 0xff) << 8) |
+                                             ((b.sleep_mode & 0x3) << 16)));
         zero4[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
         if (outIds)
             outIds[i] = first - wBase[w] + i;
@@ -407,6 +421,7 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
     cudaMemcpyAsync(d.moment + first, mo.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.meta + first, meta.data(), sizeof(int4) * static_cast<size_t>(count), cudaMemcpyHostToDevice,
                     stream);
+    cudaMemsetAsync(d.sleep + first, 0, sizeof(int2) * static_cast<size_t>(count), stream);
     nBodies += count;
     wCount[w] += count;
     // The world's list order changed: rebuild its list-position map.
@@ -653,10 +668,10 @@ void Engine::uploadCounts() {
 int Engine::setParams(const avbdg_params &p) {
     if (p.iterations < 1 || !(p.dt > 0.0f))
         return fail(AVBDG_ERR_INVALID, "iterations must be >= 1 and dt > 0");
-    if (p.contact_grace_ticks != 0 || p.sleep_frames != 0 || p.jacobian_rebuild_distance != 0.0f ||
-        p.convergence_threshold != 0.0f)
-        return fail(AVBDG_ERR_UNSUPPORTED,
-                    "contact grace, sleeping, the arm cache and the convergence probe are not on the GPU path");
+    if (p.contact_grace_ticks != 0 || p.jacobian_rebuild_distance != 0.0f || p.convergence_threshold != 0.0f)
+        return fail(AVBDG_ERR_UNSUPPORTED, "contact grace, the arm cache and the convergence probe are not on the GPU path");
+    if (p.sleep_frames < 0)
+        return fail(AVBDG_ERR_INVALID, "sleep_frames must be >= 0");
     P = p;
     dropGraphs(); // parameters are baked into captured launches
     return AVBDG_OK;
@@ -684,6 +699,9 @@ StepParams Engine::stepParams(float collisionDt) const {
     s.adaptiveBeta = P.adaptive_beta;
     s.contactOnlyOverflow = P.contact_only_overflow;
     s.projIters = P.projection_iterations;
+    s.sleepFrames = P.sleep_frames;
+    s.sleepLin2 = P.sleep_linear_threshold * P.sleep_linear_threshold;
+    s.sleepAng2 = P.sleep_angular_threshold * P.sleep_angular_threshold;
     return s;
 }
 
@@ -748,6 +766,8 @@ int Engine::broadPhase(const StepParams &sp, const StepPlan &plan) {
     launchPairs(d, tuned.traverse, stream);
     endSpan(kTraverse);
     launchFilterAcquire(d, stream);
+    if (sp.sleepFrames > 0)
+        launchSleepWakePairs(d, stream);
     return AVBDG_OK;
 }
 
@@ -760,7 +780,7 @@ void Engine::enqueueStep(const StepPlan &plan) {
         warmstartAndSelect(sp);
         projectContacts(sp, false, 0.0f);
         recordPhase(ev[2]);
-        runSubstep(sp, P.iterations);
+        runSubstep(sp, P.iterations, true);
         recordPhase(ev[3]);
         projectContacts(sp, P.position_projection != 0, 0.0f);
         launchRebase(d, sp, stream);
@@ -776,7 +796,7 @@ void Engine::enqueueStep(const StepPlan &plan) {
         if (sub > 0)
             launchRebase(d, sp, stream);
         projectContacts(sp, false, P.dt * static_cast<float>(substeps - sub));
-        runSubstep(sp, plan.rounds);
+        runSubstep(sp, plan.rounds, sub + 1 == substeps);
     }
     recordPhase(ev[3]);
     projectContacts(sp, P.position_projection != 0, sp.collisionDt);
@@ -868,6 +888,8 @@ int Engine::warmstartAndSelect(const StepParams &sp) {
     endSpan(kNarrow);
     launchManifoldCompact(d, stream);
     launchAdjacency(d, stream);
+    if (sp.sleepFrames > 0)
+        launchSleepSelect(d, sp, stream);
     launchContactOnly(d, stream);
     launchColour(d, needGreedy(), !P.contact_only_overflow, stream);
     launchColourLists(d, P.contact_only_overflow, stream);
@@ -884,7 +906,7 @@ void Engine::projectContacts(const StepParams &sp, bool positions, float window)
 }
 
 // Solver::runSubstep + iterateBody (solver_step.cpp:79-105, 195-316).
-void Engine::runSubstep(const StepParams &sp, int rounds) {
+void Engine::runSubstep(const StepParams &sp, int rounds, bool idle) {
     launchWarmstartBodies(d, sp, stream);
     const int newtonRounds =
             std::clamp(static_cast<int>(std::ceil(P.newton_ratio * static_cast<float>(rounds))), 1, rounds);
@@ -912,7 +934,7 @@ void Engine::runSubstep(const StepParams &sp, int rounds) {
         endSpan(kManifold);
         launchForceDual(d, sp, nForces > 0, stream);
     }
-    launchFinishBodies(d, sp, stream);
+    launchFinishBodies(d, sp, idle, stream);
 }
 
 int Engine::finishStep() {
@@ -1005,6 +1027,22 @@ int Engine::slotRange(int w, int first, int count, int &g0) {
         return fail(AVBDG_ERR_INVALID, "bad range");
     g0 = (w == -1 ? 0 : wBase[w]) + first;
     return AVBDG_OK;
+}
+
+int Engine::getSleeping(int w, int first, int count, uint8_t *out) {
+    int g0 = 0;
+    if (slotRange(w, first, count, g0))
+        return AVBDG_ERR_INVALID;
+    if (count == 0)
+        return AVBDG_OK;
+    if (!out)
+        return fail(AVBDG_ERR_INVALID, "null output");
+    std::vector<int2> s(static_cast<size_t>(count));
+    sync();
+    cudaMemcpy(s.data(), d.sleep + g0, sizeof(int2) * s.size(), cudaMemcpyDeviceToHost);
+    for (int i = 0; i < count; i++)
+        out[i] = s[i].x ? 1 : 0;
+    return cudaCheck("getSleeping");
 }
 
 int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {

@@ -65,6 +65,8 @@ struct StepParams {
     float stiffnessDecay, jacobiRelax, stickDriftHeal, maxPen, specMargin;
     float projBeta, projSlop, projMaxCorr, adaptiveFloor;
     int adaptiveBeta, contactOnlyOverflow, projIters;
+    int sleepFrames;              // 0 = sleeping off
+    float sleepLin2, sleepAng2;   // squared velocity thresholds of idle detection
 };
 
 struct ManifoldBuf {
@@ -84,10 +86,13 @@ struct Dev {
     int *wBounds;           // Morton scene bounds per world: lo xyz, hi xyz (ordered ints)
     int *wActive;           // projection: movable manifolds per world (0 = skip the world)
     int *wColour;           // colouring: 1 if a force touches the world (its bodies need colours)
+    int *wSleep;            // sleep: first compacted sleeper pair and their count, per world
     // bodies
     float4 *x, *q, *x0, *q0, *xi, *qi, *v, *w, *vprev;
     float4 *size, *moment;
-    int4 *meta;             // x = world, y = layer, z = mask, w = lockLin | lockAng << 8
+    int4 *meta;             // x = world, y = layer, z = mask, w = lockLin | lockAng << 8 | sleepMode << 16
+    int2 *sleep;            // x = sleeping, y = still frames (Rigid::sleeping, stillFrames)
+    uint8_t *upd;           // this step's update set (Rigid::inUpdateSet)
     int *lpToBody;          // list position -> body
     uint8_t *contactOnly, *colour;
     float4 *aabbC, *aabbH;
@@ -127,6 +132,9 @@ struct Dev {
     int *ctr;
     int *longList;
     void *scanScratch, *radixScratch;
+    // sleep: compacted sleeper pairs (rank, list), union-find parent and island aggregates
+    int *sleepRank, *sleepList;
+    int *island, *islandAwake, *islandStill;
     // world removal: slot map (NB) + force ranks (FF), staging of max(NB, FF * kExtF4) records,
     // world remap
     int *relocInt;
@@ -144,5 +152,10 @@ __device__ __forceinline__ int listPos(const Dev &d, int g) {
     return 2 * d.wBase[w] + d.wCount[w] - 1 - g;
 }
 __device__ __forceinline__ bool isDynamic(const Dev &d, int g) { return d.x[g].w > 0.0f; }
+// Movable and not asleep (ManifoldStore::frozen's `awake`, manifold.cpp:168-172).
+__device__ __forceinline__ bool isAwake(const Dev &d, int g) { return d.x[g].w > 0.0f && d.sleep[g].x == 0; }
+// In this step's update set (solved, braked, projected).
+__device__ __forceinline__ bool inUpdate(const Dev &d, int g) { return d.upd[g] != 0; }
+constexpr uint8_t kNotUpdated = 10; // colour of a movable body outside the update set
 
 } // namespace avbdg

@@ -61,6 +61,7 @@ public:
     int sync();
 
     int getState(int world, int first, int count, float *pos, float *quat, float *vel, float *angVel);
+    int getSleeping(int world, int first, int count, uint8_t *out);
     int setState(int world, int first, int count, const float *pos, const float *quat, const float *vel,
                  const float *angVel);
     int stats(avbdg_stats &out);
@@ -184,7 +185,7 @@ private:
     int broadPhase(const StepParams &sp, const StepPlan &plan);
     int warmstartAndSelect(const StepParams &sp);
     void projectContacts(const StepParams &sp, bool positions, float window);
-    void runSubstep(const StepParams &sp, int rounds);
+    void runSubstep(const StepParams &sp, int rounds, bool idle);
     int finishStep();
     bool needGreedy() const;
 };

@@ -97,7 +97,8 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     const int2 ab = L.ab[i];
     const int a = ab.x, b = ab.y;
     const float4 xa4 = d.x[a], xb4 = d.x[b];
-    const bool awakeA = xa4.w > 0.0f, awakeB = xb4.w > 0.0f;
+    const bool dynA = xa4.w > 0.0f, dynB = xb4.w > 0.0f;
+    const bool awakeA = dynA && d.sleep[a].x == 0, awakeB = dynB && d.sleep[b].x == 0;
     const int oldN = L.count[i];
     const int base = i * kMaxContacts;
     S.ab[i] = ab;
@@ -128,8 +129,8 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     if (margin > 0.0f) {
         const float horizon = p.collisionDt;
         const float4 va4 = d.v[a], vb4 = d.v[b];
-        const float gA = awakeA ? va4.w : 0.0f;
-        const float gB = awakeB ? vb4.w : 0.0f;
+        const float gA = dynA ? va4.w : 0.0f;
+        const float gB = dynB ? vb4.w : 0.0f;
         const f3 disp = add(scale(sub(xyz(va4), xyz(vb4)), horizon), f3{0, 0, (gA - gB) * horizon * horizon});
         const float ra = d.size[a].w, rb = d.size[b].w;
         margin += length(disp) + (ra * length(xyz(d.w[a])) + rb * length(xyz(d.w[b]))) * horizon;

@@ -27,7 +27,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kBrakeThreads = 512;
 
-__device__ __forceinline__ bool movable(const Dev &d, int g) { return d.x[g].w > 0.0f; }
+// Movable and in this step's update set (solver_projection.cpp:87, 105-106, 194-195).
+__device__ __forceinline__ bool movable(const Dev &d, int g) { return d.x[g].w > 0.0f && inUpdate(d, g); }
 
 __device__ __forceinline__ float angularCompliance(f3 I, f3 axis) {
     float sum = 0.0f;
@@ -147,7 +148,7 @@ __device__ void brakeManifold(const Dev &d, int m, float window) {
     const int2 ab = L.ab[m];
     const int a = ab.x, b = ab.y;
     const float4 xa4 = d.x[a], xb4 = d.x[b];
-    const bool moveA = xa4.w > 0.0f, moveB = xb4.w > 0.0f;
+    const bool moveA = movable(d, a), moveB = movable(d, b);
     const float invMassA = moveA ? 1.0f / xa4.w : 0.0f;
     const float invMassB = moveB ? 1.0f / xb4.w : 0.0f;
     const f3 nrm = xyz(L.b0[m]);
@@ -245,7 +246,7 @@ __global__ void projManifoldKernel(Dev d, StepParams p) {
     if (d.wStop[w])
         return;
     const float4 xa4 = d.x[a], xb4 = d.x[b];
-    const bool moveA = xa4.w > 0.0f, moveB = xb4.w > 0.0f;
+    const bool moveA = movable(d, a), moveB = movable(d, b);
     const int n = L.count[m];
     if (n == 0 || (!moveA && !moveB))
         return;

@@ -142,6 +142,7 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
     float4 *tmp4 = d.relocF4;
     for (float4 *arr : {d.x, d.q, d.x0, d.q0, d.xi, d.qi, d.v, d.w, d.vprev, d.size, d.moment})
         moveArray(arr, tmp4, slotMap, nOld, nNew, s);
+    moveArray(d.sleep, reinterpret_cast<int2 *>(tmp4), slotMap, nOld, nNew, s);
     int4 *tmpMeta = reinterpret_cast<int4 *>(tmp4);
     ++launchCount(); metaScatterKernel<<<grid(nOld), kThreads, 0, s>>>(d.meta, tmpMeta, slotMap, remap, nOld);
     if (nNew > 0)

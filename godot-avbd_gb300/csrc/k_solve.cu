@@ -391,7 +391,7 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
 // Which sides of manifold m take stamps for the block-Jacobi solve, and whether a coloured body
 // touches it.
 __device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touchesColour) {
-    const bool dynA = d.x[ab.x].w > 0.0f, dynB = d.x[ab.y].w > 0.0f;
+    const bool dynA = inUpdate(d, ab.x), dynB = inUpdate(d, ab.y);
     const uint8_t ca = dynA ? d.colour[ab.x] : kUncoloured;
     const uint8_t cb = dynB ? d.colour[ab.y] : kUncoloured;
     touchesColour = (dynA && ca < kOverflowColour) || (dynB && cb < kOverflowColour);
@@ -416,8 +416,8 @@ __global__ void dualKernel(Dev d, StepParams p, int stamps, float decay) {
         return;
     const ManifoldBuf L = d.live;
     const int2 ab = L.ab[m];
-    if (!(d.x[ab.x].w > 0.0f) && !(d.x[ab.y].w > 0.0f))
-        return; // frozen
+    if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
+        return; // frozen (manifold.cpp:168-172)
     bool touches = false;
     int sides = stamps ? overflowSides(d, ab, touches) : 0;
     if (touches)
@@ -692,7 +692,7 @@ template <bool FORCES>
 __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
+    if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
         return;
     Blk blk = bodyBlock(d, p, g);
     assemble<false, FORCES>(d, p, g, blk);
@@ -711,7 +711,7 @@ __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, Step
 __global__ void overflowApplyKernel(Dev d, StepParams p) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f) || d.colour[g] != kOverflowColour)
+    if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
         return;
     const float4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), scale(xyz(d.dLin[g]), p.jacobiRelax)), x4.w);
@@ -769,7 +769,7 @@ __global__ void warmstartKernel(Dev d, StepParams p) {
 }
 
 // Solver::finishBody (solver_solve.cpp:146-176), idle sleep disabled.
-__global__ void finishKernel(Dev d, StepParams p) {
+__global__ void finishKernel(Dev d, StepParams p, int idle) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
@@ -779,12 +779,24 @@ __global__ void finishKernel(Dev d, StepParams p) {
     const float4 v4 = d.v[g];
     d.vprev[g] = f4(xyz(v4), 0.0f);
     f3 v = xyz(v4), w = xyz(d.w[g]);
-    if (x4.w > 0) {
+    const int2 s = d.sleep[g];
+    if (x4.w > 0 && !s.x) {
         v = divs(sub(xyz(x4), xyz(d.x0[g])), p.dt);
         w = divs(qdiff(asq(d.q[g]), asq(d.q0[g])), p.dt);
     }
     maskLocked(locks & 0xff, v);
     maskLocked((locks >> 8) & 0xff, w);
+    // Idle detection on the tick's last substep (sleep mode 1 only).
+    if (idle && p.sleepFrames > 0 && x4.w > 0 && !s.x && ((locks >> 16) & 0x3) == 1) {
+        const int still = (length2(v) < p.sleepLin2 && length2(w) < p.sleepAng2) ? s.y + 1 : 0;
+        if (still >= p.sleepFrames) {
+            d.sleep[g] = make_int2(1, still);
+            v = f3{0, 0, 0};
+            w = f3{0, 0, 0};
+        } else {
+            d.sleep[g] = make_int2(0, still);
+        }
+    }
     d.v[g] = f4(v, v4.w);
     d.w[g] = f4(w, 0.0f);
 }
@@ -797,7 +809,24 @@ __global__ void contactOnlyInitKernel(Dev d) {
     if (g >= n)
         return;
     d.contactOnly[g] = 1;
-    d.colour[g] = (d.meta[g].x >= 0 && d.x[g].w > 0.0f) ? kUncoloured : kOverflowColour;
+    // The update set (solver_solve.cpp:296-339): movable bodies, minus idle sleepers (mode 1) and
+    // untouched, motionless bodies that start asleep (mode 2); a mode-2 sleeper otherwise wakes.
+    const bool dyn = d.meta[g].x >= 0 && d.x[g].w > 0.0f;
+    bool update = dyn;
+    if (dyn) {
+        const int mode = (d.meta[g].w >> 16) & 0x3;
+        const int2 s = d.sleep[g];
+        if (mode == 1) {
+            update = s.x == 0;
+        } else if (mode == 2) {
+            if (!s.x && length2(xyz(d.v[g])) == 0.0f && d.adjStart[g] == d.adjStart[g + 1])
+                update = false;
+            else if (s.x)
+                d.sleep[g] = make_int2(0, s.y);
+        }
+    }
+    d.upd[g] = update ? 1 : 0;
+    d.colour[g] = update ? kUncoloured : (dyn ? kNotUpdated : kOverflowColour);
 }
 
 __global__ void contactOnlyMarkKernel(Dev d) {
@@ -861,7 +890,7 @@ __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int ev
     volatile int *errors = d.ctr + C_ERRORS;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
         const int g = d.lpToBody[p];
-        if (g < 0 || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
+        if (g < 0 || d.meta[g].x < 0 || !inUpdate(d, g))
             continue;
         if (!everyWorld && !d.wColour[d.meta[g].x]) {
             publishColour(d.colour + g, kOverflowColour);
@@ -870,7 +899,7 @@ __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int ev
         unsigned used = 0;
         for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
             const int h = adjOtherSolve(d, d.adjSeq[e], g, nf);
-            if (h < 0 || !(d.x[h].w > 0.0f) || listPos(d, h) >= p)
+            if (h < 0 || !inUpdate(d, h) || listPos(d, h) >= p)
                 continue;
             unsigned c;
             long long spins = 0;
@@ -897,7 +926,7 @@ __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int ev
 __global__ void colourListKernel(Dev d, int contactOnlyOverflow) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n || d.meta[g].x < 0 || !(d.x[g].w > 0.0f))
+    if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g))
         return;
     uint8_t c = d.colour[g];
     if (contactOnlyOverflow && d.contactOnly[g])
@@ -968,8 +997,8 @@ void launchWarmstartBodies(const Dev &d, const StepParams &p, cudaStream_t s) {
     ++launchCount(); warmstartKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
 }
 
-void launchFinishBodies(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); finishKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream_t s) {
+    ++launchCount(); finishKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p, idle ? 1 : 0);
 }
 
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s) {

@@ -47,7 +47,8 @@ void launchColourLists(const Dev &d, int contactOnlyOverflow, cudaStream_t s);
 
 // ---- substep (k_solve.cu) ----
 void launchWarmstartBodies(const Dev &d, const StepParams &p, cudaStream_t s);
-void launchFinishBodies(const Dev &d, const StepParams &p, cudaStream_t s);
+// BDF1 velocities; with `idle` (the tick's last substep) also idle detection for sleeping.
+void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream_t s);
 // Stamps (precompute) of manifolds touching the overflow set; `mixedOnly` restricts to those that
 // also touch a coloured body (recomputed after the colour passes).
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
@@ -75,6 +76,12 @@ void prepareKernels();
 // Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).
 void launchPackState(const Dev &d, int first, int count, float *buf, cudaStream_t s);
 void launchUnpackState(const Dev &d, int first, int count, const float *buf, int mask, cudaStream_t s);
+
+// ---- sleeping (k_sleep.cu; only when Solver::sleepFrames > 0) ----
+// Broad-phase wake-up over the valid pairs (after the filter), in pair order per world.
+void launchSleepWakePairs(const Dev &d, cudaStream_t s);
+// Wake pass over the adjacency, then island sleep (before the update set is chosen).
+void launchSleepSelect(const Dev &d, const StepParams &p, cudaStream_t s);
 
 // ---- world removal (k_relocate.cu) ----
 // Moves the surviving worlds' bodies down to their new bases (remap: per old world, new id or -1

@@ -41,6 +41,7 @@ class Scene:
     steps: int = 0
     substeps: int = 0          # > 1: stepInterleaved(substeps, rounds)
     rounds: int = 0
+    sleep_mode: np.ndarray = None  # n: Rigid::sleep_mode (None = 0, never sleep)
 
     @property
     def n(self):
@@ -210,6 +211,40 @@ def joint_zoo(steps=240):
     for i in range(3):
         b.box((0.6, 0.6, 0.6), 1.0, 0.5, (_f(-4.0), _f(0.0), _f(9.0) + _f(i) * _f(1.0)))
     return b.scene("joint_zoo", params=dict(BENCH_PARAMS), steps=steps)
+
+
+def sleepers(steps=300, sleep_frames=30):
+    """Idle sleep, islands and wake-ups: a pyramid wall and a hanging ball-jointed chain settle and
+    fall asleep (sleep mode 1), a box released high above them wakes the wall on impact, a box
+    that starts asleep (mode 2) floats until a falling box reaches it, and a never-sleeping
+    stack (mode 0) keeps running beside them."""
+    b = _Builder()
+    modes = []
+
+    def box(*args, mode=1, **kw):
+        modes.append(mode)
+        return b.box(*args, **kw)
+
+    box((60, 60, 1), 0.0, 0.5, (0, 0, -0.5), mode=0)
+    rows = 8
+    for r in range(rows):
+        cnt = rows - r
+        for k in range(cnt):
+            box((1, 1, 1), 1.0, 0.5, ((_f(k) - _f(cnt - 1) * _f(0.5)) * _f(1.01), 0.0, _f(0.5) + _f(r)))
+    anchor = box((0.3, 0.3, 0.3), 0.0, 0.5, (8, 0, 8), mode=0)
+    prev = anchor
+    for i in range(5):
+        link = box((0.3, 0.3, 1.0), 1.0, 0.5, (_f(8.0), 0.0, _f(7.35) - _f(i) * _f(1.0)))
+        b.joint(prev, link, (0, 0, -0.15), (0, 0, 0.5), INF, 0.0)
+        prev = link
+    box((1.5, 1.5, 1.5), 2.0, 0.5, (0.3, 0.0, 40.0))               # falls onto the wall
+    box((1, 1, 1), 1.0, 0.5, (-8, 0, 3.0), mode=2)                # starts asleep in the air
+    box((0.8, 0.8, 0.8), 1.0, 0.5, (-8, 0.1, 12.0))              # lands on it later
+    for i in range(3):                                            # never sleeps
+        box((1, 1, 1), 1.0, 0.5, (-16, 0, _f(0.5) + _f(i)), mode=0)
+    sc = b.scene("sleepers", params=dict(BENCH_PARAMS, sleep_frames=sleep_frames), steps=steps)
+    sc.sleep_mode = np.asarray(modes, np.int64)
+    return sc
 
 
 # ----------------------------------------------------------------------------------------------
@@ -440,8 +475,7 @@ def instantiate(api, scene, world_cls=None, params=None):
     p = api.default_params() if params is None else params
     apply_params(p, scene.params)
     w = world_cls(api, p, max_bodies=scene.n, max_forces=len(scene.joints))
-    descs = capi.make_body_descs(scene.size, scene.density, scene.friction, scene.position,
-                                 scene.orientation, scene.velocity)
+    descs = capi.scene_body_descs(scene)
     w.add_bodies(descs)
     for force in scene.joints:
         w.add_force(force)

@@ -93,6 +93,7 @@ typedef struct avbdg_body_desc {
     uint32_t collision_mask;
     uint32_t axis_lock_linear;    /* bits 0..2 = x/y/z */
     uint32_t axis_lock_angular;
+    uint32_t sleep_mode;          /* Rigid::sleep_mode: 0 never, 1 sleep when idle, 2 start asleep */
 } avbdg_body_desc;
 
 /* Per-step counters and phase timings (src/avbd/solver.h:160-275). */
@@ -204,6 +205,8 @@ int avbdg_world_sync(avbdg_world *world);
  * (src/avbd/types.hpp:79-88). Any pointer may be NULL. */
 int avbdg_world_get_body_state(avbdg_world *world, int first, int count, float *position,
                                float *orientation, float *velocity, float *angular_velocity);
+/* Rigid::sleeping of bodies [first, first+count) (creation order): 1 asleep, 0 awake. */
+int avbdg_world_get_sleeping(avbdg_world *world, int first, int count, uint8_t *sleeping);
 
 /* Write the same fields (host edits between steps, e.g. integrated external forces,
  * src/server/avbd_physics_server3d.cpp:1503-1528). Any pointer may be NULL. */

@@ -5,6 +5,7 @@
 #include "avbd_oracle.hpp"
 
 #include <algorithm>
+#include <climits>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -576,6 +577,7 @@ int World::addBody(const avbdg_body_desc &d) {
     b.mask = d.collision_mask;
     b.lockLin = static_cast<uint8_t>(d.axis_lock_linear);
     b.lockAng = static_cast<uint8_t>(d.axis_lock_angular);
+    b.sleepMode = static_cast<int>(d.sleep_mode);
     b.mass = b.size.x * b.size.y * b.size.z * d.density;
     b.moment = V3{(b.size.y * b.size.y + b.size.z * b.size.z) / 12.0f * b.mass,
                   (b.size.x * b.size.x + b.size.z * b.size.z) / 12.0f * b.mass,
@@ -1041,6 +1043,10 @@ bool World::manifoldInitialize(Manifold &m) {
     const Body &B = bodies[m.b];
     m.mu = std::sqrt(A.friction * B.friction);
     m.flags = 0;
+    // Grace revival (manifold.cpp:249-253): a dormant manifold re-enters with its saved contacts.
+    if (m.n == 0 && m.dormantSaved > 0)
+        m.n = m.dormantSaved;
+    const int liveCount = m.n;
     Contact nc[kMaxContacts];
     const int n = collide(A, B, nc, m.basis);
     V3 newK[kMaxContacts], newLam[kMaxContacts];
@@ -1085,6 +1091,13 @@ bool World::manifoldInitialize(Manifold &m) {
             break;
         }
     }
+    // Fresh contacts seed their penalty when grace is on (manifold.cpp:339-347).
+    if (P.contact_grace_ticks > 0) {
+        const float seed = smax(PENALTY_MIN, 0.05f * P.beta_lin);
+        for (int i = 0; i < n; i++)
+            if (prevErr[i] < 0.0f)
+                newK[i] = V3{seed, seed, seed};
+    }
     m.n = n;
     for (int i = 0; i < n; i++) {
         Contact &c = m.c[i];
@@ -1096,6 +1109,20 @@ bool World::manifoldInitialize(Manifold &m) {
         c.stick = newStick[i];
         c.betaScale = newBeta[i];
     }
+    // Grace dormancy (manifold.cpp:359-378): park without contacts, force dropped, state kept.
+    if (m.n == 0) {
+        if (P.contact_grace_ticks > 0 && m.dormantTicks < P.contact_grace_ticks) {
+            for (int i = 0; i < liveCount; i++) {
+                m.c[i].lam = V3{0, 0, 0};
+                m.c[i].stick = 0;
+            }
+            m.dormantTicks++;
+            m.dormantSaved = liveCount;
+            return false;
+        }
+        m.dormantSaved = 0;
+    }
+    m.dormantTicks = 0;
     for (int i = 0; i < n; i++) {
         Contact &c = m.c[i];
         const V3 xA = A.x + qrot(A.q, c.rA);
@@ -1516,6 +1543,16 @@ void World::broadPhase() {
             continue;
         const int ia = idAt(static_cast<int>(pairs[k] >> 32));
         const int ib = idAt(static_cast<int>(pairs[k] & 0xffffffffu));
+        // wakeSleeperPair (solver_broadphase.cpp:69-81), in pair order: a body woken by an earlier
+        // pair wakes the sleepers of later pairs.
+        Body &A = bodies[ia], &B = bodies[ib];
+        if (A.sleeping && !B.sleeping && B.mass > 0.0f) {
+            A.sleeping = false;
+            A.stillFrames = 0;
+        } else if (B.sleeping && !A.sleeping && A.mass > 0.0f) {
+            B.sleeping = false;
+            B.stillFrames = 0;
+        }
         bool exists = false;
         const int li = listIndex(ia);
         for (int r = adjStart[li]; r < adjStart[li + 1]; r++)
@@ -1550,15 +1587,90 @@ int World::warmstartForces() {
     std::vector<Manifold> keptM;
     keptM.reserve(live.size());
     for (int i = 0; i < nm; i++)
-        if (active[i])
+        if (active[i] || (P.contact_grace_ticks > 0 && live[i].dormantTicks > 0))
             keptM.push_back(live[i]);
     live.swap(keptM);
     buildAdjacency();
     return static_cast<int>(forces.size());
 }
 
-// Solver::selectUpdateBodies (solver_solve.cpp:263-361), sleep disabled.
+// Solver::islandSleep (solver_solve.cpp:179-250): sleep-enabled movable bodies joined by
+// manifolds and forces sleep together once every member passed idle detection.
+void World::islandSleep() {
+    std::vector<int> members;
+    for (int li = 0; li < count(); li++) {
+        const int id = idAt(li);
+        if (bodies[id].mass > 0 && bodies[id].sleepMode == 1)
+            members.push_back(id);
+    }
+    const int n = static_cast<int>(members.size());
+    if (n < 2)
+        return;
+    std::vector<int> parent(n), slot(bodies.size(), -1);
+    for (int i = 0; i < n; i++) {
+        parent[i] = i;
+        slot[members[i]] = i;
+    }
+    const auto find = [&parent](int x) {
+        while (parent[x] != x)
+            x = parent[x] = parent[parent[x]];
+        return x;
+    };
+    const auto join = [&](int a, int b) {
+        if (a < 0 || b < 0 || slot[a] < 0 || slot[b] < 0)
+            return;
+        parent[find(slot[a])] = find(slot[b]);
+    };
+    for (const Manifold &m : live)
+        join(m.a, m.b);
+    for (const Force &f : forces)
+        join(f.a, f.b);
+    std::vector<char> awake(n, 0);
+    std::vector<int> still(n, INT_MAX);
+    for (int i = 0; i < n; i++) {
+        const int r = find(i);
+        if (!bodies[members[i]].sleeping)
+            awake[r] = 1;
+        still[r] = std::min(still[r], bodies[members[i]].stillFrames);
+    }
+    for (int i = 0; i < n; i++) {
+        const int r = find(i);
+        if (awake[r] || still[r] < P.sleep_frames)
+            continue;
+        Body &b = bodies[members[i]];
+        if (!b.sleeping) {
+            b.sleeping = true;
+            b.v = V3{0, 0, 0};
+            b.w = V3{0, 0, 0};
+        }
+    }
+}
+
+// Solver::selectUpdateBodies (solver_solve.cpp:263-361).
 void World::selectUpdateBodies() {
+    if (P.sleep_frames > 0) {
+        // Wake a sleeper touched (manifold or force) by a moving awake body; a body woken here has
+        // zero velocity, so the order does not matter.
+        const float lin2 = P.sleep_linear_threshold * P.sleep_linear_threshold;
+        const float ang2 = P.sleep_angular_threshold * P.sleep_angular_threshold;
+        for (int li = 0; li < count(); li++) {
+            Body &b = bodies[idAt(li)];
+            if (!b.sleeping || b.sleepMode != 1)
+                continue;
+            for (int r = adjStart[li]; r < adjStart[li + 1]; r++) {
+                const int o = otherBody(adjRefs[r], idAt(li));
+                if (o < 0)
+                    continue;
+                const Body &other = bodies[o];
+                if (other.mass > 0 && !other.sleeping && (length2(other.v) > lin2 || length2(other.w) > ang2)) {
+                    b.sleeping = false;
+                    b.stillFrames = 0;
+                    break;
+                }
+            }
+        }
+        islandSleep();
+    }
     updateOrder.clear();
     for (int li = 0; li < count(); li++) {
         const int id = idAt(li);
@@ -1567,9 +1679,21 @@ void World::selectUpdateBodies() {
         b.updateIndex = -1;
         b.contactOnly = true;
         if (b.mass > 0) {
-            b.updateIndex = static_cast<int>(updateOrder.size());
-            updateOrder.push_back(id);
-            b.inUpdate = true;
+            bool update = true;
+            if (b.sleepMode == 1) {
+                if (b.sleeping)
+                    update = false;
+            } else if (b.sleepMode == 2) {
+                if (!b.sleeping && length2(b.v) == 0.0f && adjStart[li] == adjStart[li + 1])
+                    update = false;
+                else
+                    b.sleeping = false;
+            }
+            if (update) {
+                b.updateIndex = static_cast<int>(updateOrder.size());
+                updateOrder.push_back(id);
+                b.inUpdate = true;
+            }
         }
     }
     for (const Force &f : forces) {
@@ -1662,8 +1786,8 @@ void World::warmstartBody(Body &b) {
     }
 }
 
-// Solver::finishBody (solver_solve.cpp:146-176), idle sleep disabled.
-void World::finishBody(Body &b) {
+// Solver::finishBody (solver_solve.cpp:146-176).
+void World::finishBody(Body &b, bool idleDetection) {
     const float dt = P.dt;
     b.vprev = b.v;
     if (b.mass > 0 && !b.sleeping) {
@@ -1672,6 +1796,18 @@ void World::finishBody(Body &b) {
     }
     maskLocked(b.lockLin, b.v);
     maskLocked(b.lockAng, b.w);
+    if (idleDetection && P.sleep_frames > 0 && b.mass > 0 && !b.sleeping && b.sleepMode == 1) {
+        if (length2(b.v) < P.sleep_linear_threshold * P.sleep_linear_threshold &&
+            length2(b.w) < P.sleep_angular_threshold * P.sleep_angular_threshold)
+            ++b.stillFrames;
+        else
+            b.stillFrames = 0;
+        if (b.stillFrames >= P.sleep_frames) {
+            b.sleeping = true;
+            b.v = V3{0, 0, 0};
+            b.w = V3{0, 0, 0};
+        }
+    }
 }
 
 // Solver::iterateBody (solver_step.cpp:195-316) as the single-participant region.
@@ -1759,7 +1895,7 @@ void World::iterate(int rounds, int forceCount) {
     }
 }
 
-void World::runSubstep(int forceCount, int rounds) {
+void World::runSubstep(int forceCount, int rounds, bool idleDetection) {
     const int n = count();
 #pragma omp parallel for schedule(static) if (parallel())
     for (int li = 0; li < n; li++)
@@ -1767,7 +1903,7 @@ void World::runSubstep(int forceCount, int rounds) {
     iterate(rounds, forceCount);
 #pragma omp parallel for schedule(static) if (parallel())
     for (int li = 0; li < n; li++)
-        finishBody(bodies[idAt(li)]);
+        finishBody(bodies[idAt(li)], idleDetection);
 }
 
 static float angularCompliance(const Body &b, V3 axis) {
@@ -1962,7 +2098,7 @@ void World::step() {
     const int forceCount = warmstartForces();
     selectUpdateBodies();
     projectContacts(false, 0.0f);
-    runSubstep(forceCount, P.iterations);
+    runSubstep(forceCount, P.iterations, true);
     projectContacts(P.position_projection != 0, 0.0f);
     for (Manifold &m : live)
         rebase(m);
@@ -1986,7 +2122,7 @@ void World::stepInterleaved(int substeps, int roundsPerSubstep) {
             for (Manifold &m : live)
                 rebase(m);
         projectContacts(false, P.dt * (substeps - sub));
-        runSubstep(forceCount, rounds);
+        runSubstep(forceCount, rounds, sub + 1 == substeps);
     }
     projectContacts(P.position_projection != 0, collisionDt);
     for (Manifold &m : live)

@@ -45,6 +45,8 @@ struct Body {
     Q4 q{0, 0, 0, 1}, q0{0, 0, 0, 1}, qi{0, 0, 0, 1};
     V3 v{}, w{}, vprev{};
     bool sleeping = false;
+    int stillFrames = 0;
+    int sleepMode = 0; // 0 never, 1 sleep when idle, 2 start asleep (types.hpp:138)
     // Per-step bookkeeping.
     bool inUpdate = false;
     int updateIndex = -1;
@@ -92,6 +94,8 @@ struct Manifold {
     float mu = 0;
     int n = 0;
     uint8_t flags = 0;
+    // Contact grace (manifold.hpp:76-77): ticks parked without contacts, contacts kept for revival.
+    int dormantTicks = 0, dormantSaved = 0;
     Contact c[kMaxContacts];
 };
 
@@ -152,10 +156,11 @@ private:
     int warmstartForces();
     void selectUpdateBodies();
     void colourGraph();
-    void runSubstep(int forceCount, int rounds);
+    void runSubstep(int forceCount, int rounds, bool idleDetection);
     void iterate(int rounds, int forceCount);
     void warmstartBody(Body &b);
-    void finishBody(Body &b);
+    void finishBody(Body &b, bool idleDetection);
+    void islandSleep();
     void projectContacts(bool projectPositions, float window);
     void rebase(Manifold &m);
 

@@ -21,10 +21,6 @@ int fail(int code, const char *msg) {
 
 // The option set this restatement covers; anything else is reported, not approximated.
 int checkParams(const avbdg_params &p) {
-    if (p.contact_grace_ticks != 0)
-        return fail(AVBDG_ERR_UNSUPPORTED, "contact_grace_ticks > 0 is not restated");
-    if (p.sleep_frames != 0)
-        return fail(AVBDG_ERR_UNSUPPORTED, "sleep_frames > 0 is not restated");
     if (p.jacobian_rebuild_distance != 0.0f)
         return fail(AVBDG_ERR_UNSUPPORTED, "jacobian_rebuild_distance > 0 is not restated");
     if (p.convergence_threshold != 0.0f)
@@ -209,6 +205,14 @@ int avbdo_world_step_n(World *w, int count) {
 }
 
 int avbdo_world_sync(World *) { return AVBDG_OK; }
+
+int avbdo_world_get_sleeping(World *w, int first, int count, uint8_t *out) {
+    if (!w || first < 0 || count < 0 || first + count > w->count() || (count > 0 && !out))
+        return fail(AVBDG_ERR_INVALID, "bad range");
+    for (int i = 0; i < count; i++)
+        out[i] = w->bodies[first + i].sleeping ? 1 : 0;
+    return AVBDG_OK;
+}
 
 int avbdo_world_get_body_state(World *w, int first, int count, float *p, float *q, float *v, float *av) {
     if (!w || first < 0 || count < 0 || first + count > w->count())

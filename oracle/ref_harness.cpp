@@ -194,6 +194,7 @@ int avbdr_world_add_bodies(RefWorld *w, int count, const avbdg_body_desc *d, int
         r->collisionMask = b.collision_mask;
         r->axisLockLinear = static_cast<uint8_t>(b.axis_lock_linear);
         r->axisLockAngular = static_cast<uint8_t>(b.axis_lock_angular);
+        r->sleep_mode = static_cast<int>(b.sleep_mode);
         const int id = static_cast<int>(w->bodies.size());
         w->bodies.push_back(r);
         w->bodyId[r] = id;
@@ -284,6 +285,14 @@ int avbdr_world_step_n(RefWorld *w, int count) {
 }
 
 int avbdr_world_sync(RefWorld *) { return AVBDG_OK; }
+
+int avbdr_world_get_sleeping(RefWorld *w, int first, int count, uint8_t *out) {
+    if (!w || first < 0 || count < 0 || first + count > (int)w->bodies.size() || (count > 0 && !out))
+        return fail(AVBDG_ERR_INVALID, "bad range");
+    for (int i = 0; i < count; i++)
+        out[i] = w->bodies[first + i]->sleeping ? 1 : 0;
+    return AVBDG_OK;
+}
 
 int avbdr_world_get_body_state(RefWorld *w, int first, int count, float *p, float *q, float *v,
         float *av) {

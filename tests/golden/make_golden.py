@@ -8,8 +8,8 @@ godot-avbd_gb300/scenes.py and records, per scene:
   - the live manifolds' body ids, contact counts and feature keys after the first and last step,
   - the colouring of the last step.
 Scenes whose arithmetic calls the C library's atan2 (generic joints with limited or sprung
-rotations) are recorded with per-step digests plus the full pose of every body at a few steps, for
-tolerance comparisons (the GPU calls CUDA's atan2f).
+rotations), and the sleeping scene, are recorded with per-step digests plus the full pose and
+sleeping flag of every body at a few steps (pose tolerance where the GPU calls CUDA's atan2f).
 Writes tests/golden/reference_runs.json. Usage: python tests/golden/make_golden.py
 """
 
@@ -40,6 +40,7 @@ RUNS = [
 # (scene builder, keyword arguments, steps recorded, steps whose poses are stored)
 POSE_RUNS = [
     ("joint_zoo", {}, 60, [1, 10, 20, 30, 60]),
+    ("sleepers", {}, 300, [60, 150, 200, 300]),
 ]
 
 
@@ -97,7 +98,8 @@ def main():
             if s + 1 in keep:
                 pos, quat, _, _ = w.state()
                 rec["poses"][str(s + 1)] = {"position": [[float(v) for v in r] for r in pos],
-                                            "orientation": [[float(v) for v in r] for r in quat]}
+                                            "orientation": [[float(v) for v in r] for r in quat],
+                                            "sleeping": [int(v) for v in w.sleeping()]}
         out["pose_runs"][name] = rec
         print(name, sc.n, "bodies", steps, "steps (poses kept)", flush=True)
     with open(os.path.join(HERE, "reference_runs.json"), "w") as f:

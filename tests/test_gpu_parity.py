@@ -141,7 +141,7 @@ def test_gpu_edge_cases(pkg, gpu, oracle):
     assert e.value.code == capi.ERR_NONFINITE
     # Unsupported options are reported, never approximated.
     p = gpu.default_params()
-    p.sleep_frames = 10
+    p.jacobian_rebuild_distance = 0.01
     with pytest.raises(capi.AvbdError) as e:
         pkg.world(p)
     assert e.value.code == capi.ERR_UNSUPPORTED

@@ -51,9 +51,9 @@ def test_golden_runs(pkg, oracle, golden):
 
 
 def test_golden_pose_runs(pkg, oracle, golden):
-    """Springs and generic joints (hinge, slider, limited and sprung rotations, world anchor): the
-    oracle calls the same C library atan2 as the reference, so every step's digest and the stored
-    poses are exact."""
+    """Springs and generic joints (hinge, slider, limited and sprung rotations, world anchor), and
+    idle sleep with islands and wake-ups: the oracle calls the same C library atan2 as the
+    reference, so every step's digest, the stored poses and the sleeping flags are exact."""
     scenes = pkg.scenes
     for name, rec in golden["pose_runs"].items():
         sc = getattr(scenes, rec["scene"])(**rec["kwargs"])
@@ -66,6 +66,7 @@ def test_golden_pose_runs(pkg, oracle, golden):
                 p, q, _, _ = w.state()
                 assert np.array_equal(p, np.asarray(pose["position"], np.float32))
                 assert np.array_equal(q, np.asarray(pose["orientation"], np.float32))
+                assert np.array_equal(w.sleeping(), np.asarray(pose["sleeping"], np.uint8))
 
 
 @pytest.mark.parametrize("option", ["adaptive_beta", "stiffness_decay", "no_projection", "gs_contacts"])
@@ -110,7 +111,7 @@ def test_oracle_matches_reference_interleaved_pile(pkg, oracle, ref):
 
 def test_oracle_rejects_unrestated_options(pkg, oracle):
     p = oracle.default_params()
-    p.sleep_frames = 30
+    p.jacobian_rebuild_distance = 0.01
     with pytest.raises(pkg.capi.AvbdError) as e:
         pkg.capi.World(oracle, p)
     assert e.value.code == pkg.capi.ERR_UNSUPPORTED
