@@ -235,7 +235,7 @@ class Api:
 
 
 def make_body_descs(size, density, friction, position, orientation=None, velocity=None,
-                    angular_velocity=None, sleep_mode=None):
+                    angular_velocity=None, sleep_mode=None, shape=None):
     """Pack per-body arrays (n x 3 / n x 4 / n) into an avbdg_body_desc array."""
     size = np.asarray(size, np.float32).reshape(-1, 3)
     n = size.shape[0]
@@ -250,11 +250,12 @@ def make_body_descs(size, density, friction, position, orientation=None, velocit
         angular_velocity = np.zeros((n, 3), np.float32)
     angular_velocity = np.asarray(angular_velocity, np.float32).reshape(n, 3)
     sleep_mode = np.broadcast_to(np.asarray(0 if sleep_mode is None else sleep_mode, np.int64), (n,))
+    shape = np.broadcast_to(np.asarray(SHAPE_BOX if shape is None else shape, np.int64), (n,))
     descs = (BodyDesc * n)()
     for i in range(n):
         d = descs[i]
         d.size[:] = size[i].tolist()
-        d.shape = SHAPE_BOX
+        d.shape = int(shape[i])
         d.density = float(density[i])
         d.friction = float(friction[i])
         d.position[:] = position[i].tolist()
@@ -272,7 +273,8 @@ def make_body_descs(size, density, friction, position, orientation=None, velocit
 def scene_body_descs(scene):
     """avbdg_body_desc array of a scenes.Scene, creation order."""
     return make_body_descs(scene.size, scene.density, scene.friction, scene.position, scene.orientation,
-                           scene.velocity, sleep_mode=getattr(scene, "sleep_mode", None))
+                           scene.velocity, sleep_mode=getattr(scene, "sleep_mode", None),
+                           shape=getattr(scene, "shape", None))
 
 
 class World:

@@ -98,6 +98,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
         take(b->b1, mm);
         take(b->b2, mm);
         take(b->count, mm);
+        take(b->dormant, mm);
         const size_t mc = static_cast<size_t>(mm) * kMaxContacts;
         take(b->key, mc);
         take(b->rA, mc);
@@ -254,6 +255,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         cp(t.b1, s.b1, mCopy * sizeof(float4));
         cp(t.b2, s.b2, mCopy * sizeof(float4));
         cp(t.count, s.count, mCopy * sizeof(int));
+        cp(t.dormant, s.dormant, mCopy * sizeof(int2));
         const size_t cCopy = mCopy * kMaxContacts;
         cp(t.key, s.key, cCopy * sizeof(int));
         for (auto pr : {std::make_pair(t.rA, s.rA), std::make_pair(t.rB, s.rB), std::make_pair(t.C0, s.C0),
@@ -668,8 +670,10 @@ void Engine::uploadCounts() {
 int Engine::setParams(const avbdg_params &p) {
     if (p.iterations < 1 || !(p.dt > 0.0f))
         return fail(AVBDG_ERR_INVALID, "iterations must be >= 1 and dt > 0");
-    if (p.contact_grace_ticks != 0 || p.jacobian_rebuild_distance != 0.0f || p.convergence_threshold != 0.0f)
-        return fail(AVBDG_ERR_UNSUPPORTED, "contact grace, the arm cache and the convergence probe are not on the GPU path");
+    if (p.jacobian_rebuild_distance != 0.0f || p.convergence_threshold != 0.0f)
+        return fail(AVBDG_ERR_UNSUPPORTED, "the arm cache and the convergence probe are not on the GPU path");
+    if (p.contact_grace_ticks < 0)
+        return fail(AVBDG_ERR_INVALID, "contact_grace_ticks must be >= 0");
     if (p.sleep_frames < 0)
         return fail(AVBDG_ERR_INVALID, "sleep_frames must be >= 0");
     P = p;
@@ -700,6 +704,8 @@ StepParams Engine::stepParams(float collisionDt) const {
     s.contactOnlyOverflow = P.contact_only_overflow;
     s.projIters = P.projection_iterations;
     s.sleepFrames = P.sleep_frames;
+    s.graceTicks = P.contact_grace_ticks;
+    s.graceSeed = std::max(PENALTY_MIN, 0.05f * P.beta_lin);
     s.sleepLin2 = P.sleep_linear_threshold * P.sleep_linear_threshold;
     s.sleepAng2 = P.sleep_angular_threshold * P.sleep_angular_threshold;
     return s;

@@ -66,6 +66,8 @@ struct StepParams {
     float projBeta, projSlop, projMaxCorr, adaptiveFloor;
     int adaptiveBeta, contactOnlyOverflow, projIters;
     int sleepFrames;              // 0 = sleeping off
+    int graceTicks;               // Solver::contactGraceTicks (0 = off)
+    float graceSeed;              // penalty of a fresh contact under grace: max(PENALTY_MIN, 0.05 betaLin)
     float sleepLin2, sleepAng2;   // squared velocity thresholds of idle detection
 };
 
@@ -73,6 +75,7 @@ struct ManifoldBuf {
     int2 *ab;          // global body indices (a = smaller list index)
     float4 *b0, *b1, *b2;
     int *count;
+    int2 *dormant;     // contact grace: x = ticks parked, y = contacts kept for revival
     int *key;          // contacts: [m * 8 + k]
     float4 *rA, *rB, *C0, *k, *lam;
 };

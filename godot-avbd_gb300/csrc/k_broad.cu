@@ -411,6 +411,7 @@ __global__ void acquireKernel(Dev d, const int *flags, const int *rank) {
     const uint64_t key = d.pairs[k];
     d.live.ab[m] = make_int2(d.lpToBody[static_cast<int>(key >> 32)], d.lpToBody[static_cast<int>(key & 0xffffffffu)]);
     d.live.count[m] = 0;
+    d.live.dormant[m] = make_int2(0, 0);
 }
 
 __global__ void candTotalKernel(Dev d) {

@@ -99,7 +99,8 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     const float4 xa4 = d.x[a], xb4 = d.x[b];
     const bool dynA = xa4.w > 0.0f, dynB = xb4.w > 0.0f;
     const bool awakeA = dynA && d.sleep[a].x == 0, awakeB = dynB && d.sleep[b].x == 0;
-    const int oldN = L.count[i];
+    int oldN = L.count[i];
+    const int2 dorm = L.dormant[i];
     const int base = i * kMaxContacts;
     S.ab[i] = ab;
     if (!awakeA && !awakeB) {
@@ -108,7 +109,9 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
         S.b1[i] = L.b1[i];
         S.b2[i] = L.b2[i];
         S.count[i] = oldN;
-        for (int k = 0; k < oldN; k++) {
+        S.dormant[i] = dorm;
+        const int kept = oldN > 0 ? oldN : dorm.y; // a parked manifold keeps its saved contacts
+        for (int k = 0; k < kept; k++) {
             S.key[base + k] = L.key[base + k];
             S.rA[base + k] = L.rA[base + k];
             S.rB[base + k] = L.rB[base + k];
@@ -119,6 +122,9 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
         d.mActive[i] = 1;
         return;
     }
+    // Grace revival (manifold.cpp:249-253): a dormant manifold matches against its saved contacts.
+    if (oldN == 0 && dorm.y > 0)
+        oldN = dorm.y;
     const f3 xa = xyz(xa4), xb = xyz(xb4);
     const q4 qa = asq(d.q[a]), qb = asq(d.q[b]);
     const float4 ma4 = d.moment[a], mb4 = d.moment[b];
@@ -186,10 +192,36 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
             break;
         }
     }
+    // Fresh contacts seed their penalty when grace is on (manifold.cpp:339-347).
+    if (p.graceTicks > 0)
+        for (int c = 0; c < n; c++)
+            if (prevErr[c] < 0.0f)
+                newK[c] = f3{p.graceSeed, p.graceSeed, p.graceSeed};
     S.b0[i] = f4(r0, mu);
     S.b1[i] = f4(r1, 0.0f);
     S.b2[i] = f4(r2, 0.0f);
     S.count[i] = n;
+    if (n == 0) {
+        // Grace dormancy (manifold.cpp:359-378): parked, not reaped, within the grace ticks; the
+        // saved contacts keep their state except force and stick.
+        if (p.graceTicks > 0 && dorm.x < p.graceTicks) {
+            for (int j = 0; j < oldN; j++) {
+                S.key[base + j] = L.key[base + j];
+                S.rA[base + j] = L.rA[base + j];
+                S.rB[base + j] = L.rB[base + j];
+                S.C0[base + j] = L.C0[base + j];
+                S.k[base + j] = L.k[base + j];
+                S.lam[base + j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            S.dormant[i] = make_int2(dorm.x + 1, oldN);
+            d.mActive[i] = 1;
+            return;
+        }
+        S.dormant[i] = make_int2(0, 0);
+        d.mActive[i] = 0;
+        return;
+    }
+    S.dormant[i] = make_int2(0, dorm.y);
     for (int c = 0; c < n; c++) {
         const f3 rA = nc[c].rA, rB = nc[c].rB;
         const f3 pA = add(xa, qrot(qa, rA));
@@ -242,8 +274,11 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
     L.b1[r] = S.b1[i];
     L.b2[r] = S.b2[i];
     const int n = S.count[i];
+    const int2 dorm = S.dormant[i];
     L.count[r] = n;
-    for (int c = 0; c < n; c++) {
+    L.dormant[r] = dorm;
+    const int kept = n > 0 ? n : dorm.y;
+    for (int c = 0; c < kept; c++) {
         const int si = i * kMaxContacts + c, di = r * kMaxContacts + c;
         L.key[di] = S.key[si];
         L.rA[di] = S.rA[si];

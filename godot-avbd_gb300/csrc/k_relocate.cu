@@ -68,8 +68,11 @@ __global__ void manifoldRelocateKernel(Dev d, const int *slotMap) {
     S.b1[m] = L.b1[m];
     S.b2[m] = L.b2[m];
     const int cnt = L.count[m];
+    const int2 dorm = L.dormant[m];
     S.count[m] = cnt;
-    for (int c = 0; c < cnt; c++) {
+    S.dormant[m] = dorm;
+    const int kept = cnt > 0 ? cnt : dorm.y;
+    for (int c = 0; c < kept; c++) {
         const int i = m * kMaxContacts + c;
         S.key[i] = L.key[i];
         S.rA[i] = L.rA[i];

@@ -42,6 +42,7 @@ class Scene:
     substeps: int = 0          # > 1: stepInterleaved(substeps, rounds)
     rounds: int = 0
     sleep_mode: np.ndarray = None  # n: Rigid::sleep_mode (None = 0, never sleep)
+    shape: np.ndarray = None       # n: 0 box, 1 sphere (size.x = radius), 2 cylinder (size.x radius, .z height)
 
     @property
     def n(self):
@@ -56,9 +57,11 @@ class _Builder:
     def __init__(self):
         self.size, self.density, self.friction, self.position, self.orientation = [], [], [], [], []
         self.velocity = []
+        self.shapes = []
         self.joints = []
 
-    def box(self, size, density, friction, position, orientation=(0, 0, 0, 1), velocity=(0, 0, 0)):
+    def box(self, size, density, friction, position, orientation=(0, 0, 0, 1), velocity=(0, 0, 0), shape=0):
+        self.shapes.append(int(shape))
         self.size.append(np.asarray(size, F32))
         self.density.append(F32(density))
         self.friction.append(F32(friction))
@@ -79,8 +82,16 @@ class _Builder:
         self.joints.append(("generic", a, b, tuple(float(x) for x in ra), tuple(float(x) for x in rb),
                             tuple(tuple(float(v) for v in ax) for ax in axes)))
 
+    def sphere(self, radius, density, friction, position, velocity=(0, 0, 0)):
+        return self.box((radius, radius, radius), density, friction, position, velocity=velocity, shape=1)
+
+    def cylinder(self, radius, height, density, friction, position, orientation=(0, 0, 0, 1)):
+        return self.box((radius, radius, height), density, friction, position, orientation, shape=2)
+
     def scene(self, name, **kw):
         n = len(self.size)
+        if any(self.shapes):
+            kw.setdefault("shape", np.asarray(self.shapes, np.int64))
         return Scene(
             name=name,
             size=np.array(self.size, F32).reshape(n, 3),
@@ -245,6 +256,40 @@ def sleepers(steps=300, sleep_frames=30):
     sc = b.scene("sleepers", params=dict(BENCH_PARAMS, sleep_frames=sleep_frames), steps=steps)
     sc.sleep_mode = np.asarray(modes, np.int64)
     return sc
+
+
+def pile_grace(steps=240, count=250, chain_links=6, grace=4):
+    """A smaller mass-ratio pile with contact grace: manifolds whose contacts vanish for up to
+    `grace` ticks are parked with their state and revived by feature key when they touch again."""
+    sc = pile(steps=steps, count=count, chain_links=chain_links)
+    sc.name = "pile_grace"
+    sc.params = dict(sc.params, contact_grace_ticks=grace)
+    return sc
+
+
+def shape_mix(steps=240):
+    """Spheres and cylinders with boxes: a sphere pile, standing and lying cylinders, a cylinder
+    stack, spheres rolling on a tilted box ramp and against cylinders, and boxes on cylinders."""
+    b = _Builder()
+    b.box((60, 60, 1), 0.0, 0.5, (0, 0, -0.5))
+    ramp = (F32(0.0), F32(0.130526), F32(0.0), F32(0.991445))  # 15 degrees about y
+    b.box((8, 3, 0.5), 0.0, 0.5, (-10, 0, 2.0), ramp)
+    for i in range(4):
+        b.sphere(0.4, 1.0, 0.5, (_f(-12.5) + _f(i) * _f(0.9), 0.0, _f(4.0) + _f(i) * _f(0.3)))
+    for i in range(3):  # cylinder stack
+        b.cylinder(0.6, 0.8, 1.0, 0.5, (0.0, 0.0, _f(0.4) + _f(i) * _f(0.85)))
+    lying = (F32(0.707107), F32(0.0), F32(0.0), F32(0.707107))  # axis along y
+    for i in range(3):  # lying cylinders
+        b.cylinder(0.5, 2.0, 1.0, 0.5, (_f(4.0) + _f(i) * _f(1.2), 0.0, 0.5), lying)
+    b.box((2.5, 1.0, 0.3), 1.0, 0.5, (5.2, 0.0, 1.3))  # a plank across them
+    for i in range(9):  # sphere pile
+        x, y = i % 3, i // 3
+        b.sphere(0.35, 2.0, 0.5, (_f(10.0) + _f(x) * _f(0.75), _f(y) * _f(0.75), _f(0.4) + _f(i % 2) * _f(0.8)))
+    for i in range(3):  # spheres and a box dropped on the stack
+        b.sphere(0.3, 1.0, 0.5, (_f(0.1) * _f(i), 0.0, _f(4.0) + _f(i) * _f(0.8)))
+    b.box((0.7, 0.7, 0.7), 1.0, 0.5, (0.2, 0.1, 6.5))
+    b.cylinder(0.3, 1.0, 1.0, 0.5, (-3.0, 0.0, 3.0), (F32(0.258819), F32(0.0), F32(0.0), F32(0.965926)))
+    return b.scene("shape_mix", params=dict(BENCH_PARAMS), steps=steps)
 
 
 # ----------------------------------------------------------------------------------------------

@@ -303,21 +303,22 @@ struct ContactSink {
     int count = 0;
     V3 mid[kMaxContacts];
     // addContact (collide.cpp:208-233).
-    void add(V3 xA, V3 xB, int key) {
+    bool add(V3 xA, V3 xB, int key) {
         const V3 m = (xA + xB) * 0.5f;
         for (int i = 0; i < count; ++i) {
             const V3 d = m - mid[i];
             if (length2(d) < kMergeDistSq)
-                return;
+                return false;
         }
         if (count >= kMaxContacts)
-            return;
+            return false;
         Contact &c = out[count];
         c.key = key;
         c.rA = qrot(qconj(A.rot), xA - A.center);
         c.rB = qrot(qconj(B.rot), xB - B.center);
         mid[count] = m;
         ++count;
+        return true;
     }
 };
 
@@ -578,11 +579,27 @@ int World::addBody(const avbdg_body_desc &d) {
     b.lockLin = static_cast<uint8_t>(d.axis_lock_linear);
     b.lockAng = static_cast<uint8_t>(d.axis_lock_angular);
     b.sleepMode = static_cast<int>(d.sleep_mode);
-    b.mass = b.size.x * b.size.y * b.size.z * d.density;
-    b.moment = V3{(b.size.y * b.size.y + b.size.z * b.size.z) / 12.0f * b.mass,
-                  (b.size.x * b.size.x + b.size.z * b.size.z) / 12.0f * b.mass,
-                  (b.size.x * b.size.x + b.size.y * b.size.y) / 12.0f * b.mass};
-    b.radius = std::sqrt(dot(b.size * 0.5f, b.size * 0.5f));
+    // Mass properties and bounding radius per shape (rigid.cpp:34-72).
+    if (b.shape == 1) {
+        const float r = b.size.x;
+        b.mass = (4.0f / 3.0f) * 3.14159265358979f * r * r * r * d.density;
+        const float i = 0.4f * b.mass * r * r;
+        b.moment = V3{i, i, i};
+        b.radius = r;
+    } else if (b.shape == 2) {
+        const float r = b.size.x, h = b.size.z;
+        b.mass = 3.14159265358979f * r * r * h * d.density;
+        const float axial = 0.5f * b.mass * r * r;
+        const float radial = b.mass * (3.0f * r * r + h * h) / 12.0f;
+        b.moment = V3{radial, radial, axial};
+        b.radius = std::sqrt(dot(V3{r, h * 0.5f, r}, V3{r, h * 0.5f, r}));
+    } else {
+        b.mass = b.size.x * b.size.y * b.size.z * d.density;
+        b.moment = V3{(b.size.y * b.size.y + b.size.z * b.size.z) / 12.0f * b.mass,
+                      (b.size.x * b.size.x + b.size.z * b.size.z) / 12.0f * b.mass,
+                      (b.size.x * b.size.x + b.size.y * b.size.y) / 12.0f * b.mass};
+        b.radius = std::sqrt(dot(b.size * 0.5f, b.size * 0.5f));
+    }
     bodies.push_back(b);
     treeBodies = -1;
     return static_cast<int>(bodies.size()) - 1;
@@ -1025,6 +1042,354 @@ static Cone clampForce(V3 &F, float mu) {
 }
 
 // Manifold::collide (collide.cpp:1100-1120).
+// ---- Spheres and cylinders (collide.cpp:493-999): closest points, cylinder surface samples ----
+
+namespace {
+
+constexpr int kRimSamples = 8, kAxialSamples = 3;
+constexpr int kMaxCylSamples = 2 * (kRimSamples + 1) + kRimSamples * (kAxialSamples - 1);
+constexpr int kMaxCandidates = 2 * kMaxCylSamples + 8;
+constexpr uint32_t kAxisCylSample = 3, kAxisCylCorner = 4;
+
+struct Shape {
+    int type; // 0 box, 1 sphere, 2 cylinder
+    V3 center;
+    Q4 rot;
+    V3 half;
+    float radius, halfHeight;
+    V3 axis;
+};
+
+Shape makeShape(const Body &b) {
+    return Shape{b.shape, b.x, b.q, b.size * 0.5f, b.size.x, b.size.z * 0.5f, qrot(b.q, V3{0, 0, 1})};
+}
+
+// Rim directions, a coprime stride around the circle (collide.cpp:731-753).
+struct RimTrig {
+    float c[kRimSamples], s[kRimSamples];
+    RimTrig() {
+        for (int i = 0; i < kRimSamples; ++i) {
+            const int step = i * 5 % kRimSamples;
+            const float a = 6.28318530718f * (float)step / (float)kRimSamples;
+            c[i] = std::cos(a);
+            s[i] = std::sin(a);
+        }
+    }
+};
+const RimTrig &rimTrig() {
+    static const RimTrig t;
+    return t;
+}
+
+bool pointInBox(const Shape &box, V3 p, V3 &push, float &depth) {
+    const V3 local = qrot(qconj(box.rot), p - box.center);
+    float best = FLT_MAX;
+    int axis = 0;
+    float sign = 1.0f;
+    for (int i = 0; i < 3; ++i) {
+        const float d = box.half[i] - std::fabs(local[i]);
+        if (d <= 0.0f)
+            return false;
+        if (d < best) {
+            best = d;
+            axis = i;
+            sign = local[i] >= 0.0f ? 1.0f : -1.0f;
+        }
+    }
+    V3 lp{0, 0, 0};
+    lp[axis] = sign;
+    push = qrot(box.rot, lp);
+    depth = best;
+    return true;
+}
+
+bool pointNearBox(const Shape &box, V3 p, float margin, V3 &push, float &depth) {
+    const V3 local = qrot(qconj(box.rot), p - box.center);
+    bool outside = false;
+    for (int i = 0; i < 3; ++i)
+        if (std::fabs(local[i]) >= box.half[i]) {
+            outside = true;
+            break;
+        }
+    if (!outside)
+        return false;
+    const V3 cl{sclamp(local.x, -box.half.x, box.half.x), sclamp(local.y, -box.half.y, box.half.y),
+                sclamp(local.z, -box.half.z, box.half.z)};
+    const V3 d = local - cl;
+    const float gap = length(d);
+    if (gap > margin || gap <= 1.0e-9f)
+        return false;
+    push = qrot(box.rot, d / gap);
+    depth = -gap;
+    return true;
+}
+
+V3 closestPointOnCylinder(const Shape &cyl, V3 p, V3 &outward, float &distance) {
+    const V3 local = qrot(qconj(cyl.rot), p - cyl.center);
+    const float t = sclamp(local.z, -cyl.halfHeight, cyl.halfHeight);
+    const float lenSq = (0.0f + local.x * local.x) + local.y * local.y; // linalg length2 of (x, y)
+    V3 closest{0, 0, t};
+    if (lenSq > cyl.radius * cyl.radius) {
+        const float scale = cyl.radius / std::sqrt(lenSq);
+        closest.x = local.x * scale;
+        closest.y = local.y * scale;
+    } else if (lenSq > 1.0e-12f) {
+        closest.x = local.x;
+        closest.y = local.y;
+    } else {
+        closest.x = cyl.radius;
+    }
+    const V3 onCyl = qrot(cyl.rot, closest) + cyl.center;
+    const V3 d = p - onCyl;
+    distance = length(d);
+    outward = distance > 1.0e-9f ? d / distance : qrot(cyl.rot, V3{1, 0, 0});
+    return onCyl;
+}
+
+bool pointInCylinder(const Shape &cyl, V3 p, V3 &push, float &surface) {
+    const V3 local = qrot(qconj(cyl.rot), p - cyl.center);
+    const float radialSq = local.x * local.x + local.y * local.y;
+    if (radialSq >= cyl.radius * cyl.radius || std::fabs(local.z) >= cyl.halfHeight)
+        return false;
+    const float radialDepth = cyl.radius - std::sqrt(radialSq);
+    const float capDepth = cyl.halfHeight - std::fabs(local.z);
+    V3 pl{0, 0, 0};
+    if (capDepth < radialDepth) {
+        pl.z = local.z >= 0.0f ? 1.0f : -1.0f;
+        surface = capDepth;
+    } else {
+        const float len = std::sqrt(radialSq);
+        if (len > 1.0e-6f) {
+            pl.x = local.x / len;
+            pl.y = local.y / len;
+        } else {
+            pl.x = 1.0f;
+        }
+        surface = radialDepth;
+    }
+    push = qrot(cyl.rot, pl);
+    return true;
+}
+
+bool pointNearCylinder(const Shape &cyl, V3 p, float margin, V3 &push, float &depth) {
+    const V3 local = qrot(qconj(cyl.rot), p - cyl.center);
+    const float radialSq = local.x * local.x + local.y * local.y;
+    if (radialSq < cyl.radius * cyl.radius && std::fabs(local.z) < cyl.halfHeight)
+        return false;
+    V3 outward;
+    float distance;
+    closestPointOnCylinder(cyl, p, outward, distance);
+    if (distance > margin)
+        return false;
+    push = outward;
+    depth = -distance;
+    return true;
+}
+
+bool sampleInsideBox(const Shape &box, V3 p, float margin, V3 &push, float &depth) {
+    return pointInBox(box, p, push, depth) || (margin > 0.0f && pointNearBox(box, p, margin, push, depth));
+}
+
+bool sampleInsideCylinder(const Shape &cyl, V3 p, float margin, V3 &push, float &depth) {
+    return pointInCylinder(cyl, p, push, depth) || (margin > 0.0f && pointNearCylinder(cyl, p, margin, push, depth));
+}
+
+void cylinderSamples(const Shape &cyl, V3 *out, int &count) {
+    count = 0;
+    const V3 x = qrot(cyl.rot, V3{1, 0, 0});
+    const V3 y = qrot(cyl.rot, V3{0, 1, 0});
+    const RimTrig &trig = rimTrig();
+    for (int end = -1; end <= 1; end += 2) {
+        const V3 cap = cyl.center + cyl.axis * (cyl.halfHeight * (float)end);
+        out[count++] = cap;
+        for (int i = 0; i < kRimSamples; ++i)
+            out[count++] = cap + (x * trig.c[i] + y * trig.s[i]) * cyl.radius;
+    }
+    for (int ring = 1; ring < kAxialSamples; ++ring) {
+        const float t = -cyl.halfHeight + 2.0f * cyl.halfHeight * (float)ring / (float)kAxialSamples;
+        const V3 rc = cyl.center + cyl.axis * t;
+        for (int i = 0; i < kRimSamples; ++i)
+            out[count++] = rc + (x * trig.c[i] + y * trig.s[i]) * cyl.radius;
+    }
+}
+
+struct Candidate {
+    V3 xA, xB, normal;
+    float depth;
+    uint32_t feature;
+};
+
+// Deepest first, stable (equal depths keep their order); emission stops at the first contact the
+// sink refuses (collide.cpp:699-729).
+void emitRanked(const Candidate *cand, int n, ContactSink &sink) {
+    int order[kMaxCandidates];
+    for (int i = 0; i < n; ++i) {
+        int j = i;
+        while (j > 0 && cand[order[j - 1]].depth < cand[i].depth) {
+            order[j] = order[j - 1];
+            --j;
+        }
+        order[j] = i;
+    }
+    const int emit = std::min(n, kMaxContacts);
+    for (int i = 0; i < emit; ++i)
+        if (!sink.add(cand[order[i]].xA, cand[order[i]].xB, static_cast<int>(cand[order[i]].feature)))
+            break;
+}
+
+int collideSphereSphere(const Shape &a, const Shape &b, float margin, ContactSink &sink, M3 &basis) {
+    const V3 d = b.center - a.center;
+    const float distSq = length2(d);
+    const float sumPlus = a.radius + b.radius + margin;
+    if (distSq >= sumPlus * sumPlus)
+        return 0;
+    const float dist = std::sqrt(distSq);
+    const V3 n = dist > 1.0e-6f ? d / dist : V3{0, 0, 1};
+    basis = orthonormal(-n);
+    sink.add(a.center + n * a.radius, b.center - n * b.radius, 1);
+    return sink.count;
+}
+
+int collideSphereBox(const Shape &a, const Shape &b, bool sphereIsA, float margin, ContactSink &sink, M3 &basis) {
+    const Shape &sphere = sphereIsA ? a : b;
+    const Shape &box = sphereIsA ? b : a;
+    const V3 local = qrot(qconj(box.rot), sphere.center - box.center);
+    const V3 cl{sclamp(local.x, -box.half.x, box.half.x), sclamp(local.y, -box.half.y, box.half.y),
+                sclamp(local.z, -box.half.z, box.half.z)};
+    const V3 closest = qrot(box.rot, cl) + box.center;
+    const V3 d = sphere.center - closest;
+    const float distSq = length2(d);
+    const float radPlus = sphere.radius + margin;
+    if (distSq >= radPlus * radPlus)
+        return 0;
+    const float dist = std::sqrt(distSq);
+    V3 n;
+    if (dist > 1.0e-6f) {
+        n = d / dist;
+    } else {
+        float depth;
+        if (!pointInBox(box, sphere.center, n, depth))
+            return 0;
+    }
+    basis = orthonormal(-(sphereIsA ? -n : n));
+    const V3 onSphere = sphere.center - n * sphere.radius;
+    sink.add(sphereIsA ? onSphere : closest, sphereIsA ? closest : onSphere, 1);
+    return sink.count;
+}
+
+int collideSphereCylinder(const Shape &a, const Shape &b, bool sphereIsA, float margin, ContactSink &sink,
+                          M3 &basis) {
+    const Shape &sphere = sphereIsA ? a : b;
+    const Shape &cyl = sphereIsA ? b : a;
+    V3 outward;
+    float distance;
+    const V3 onCyl = closestPointOnCylinder(cyl, sphere.center, outward, distance);
+    if (distance >= sphere.radius + margin)
+        return 0;
+    basis = orthonormal(-(sphereIsA ? -outward : outward));
+    const V3 onSphere = sphere.center - outward * sphere.radius;
+    sink.add(sphereIsA ? onSphere : onCyl, sphereIsA ? onCyl : onSphere, 1);
+    return sink.count;
+}
+
+int collideCylinderBox(const Shape &a, const Shape &b, bool cylIsA, float margin, ContactSink &sink, M3 &basis) {
+    const Shape &cyl = cylIsA ? a : b;
+    const Shape &box = cylIsA ? b : a;
+    Candidate cand[kMaxCandidates];
+    int nc = 0;
+    V3 normalAB{0, 0, 0};
+    V3 samples[kMaxCylSamples];
+    int ns = 0;
+    cylinderSamples(cyl, samples, ns);
+    for (int i = 0; i < ns && nc < kMaxCandidates; ++i) {
+        V3 push;
+        float depth;
+        if (!sampleInsideBox(box, samples[i], margin, push, depth))
+            continue;
+        Candidate &c = cand[nc++];
+        c.xA = cylIsA ? samples[i] : samples[i] + push * depth;
+        c.xB = cylIsA ? samples[i] + push * depth : samples[i];
+        c.normal = cylIsA ? -push : push;
+        c.depth = depth;
+        c.feature = (kAxisCylSample << 24) | ((cylIsA ? 1u : 0u) << 20) | static_cast<uint32_t>(i);
+        normalAB += c.normal;
+    }
+    for (int corner = 0; corner < 8 && nc < kMaxCandidates; ++corner) {
+        const V3 cl{(corner & 1) ? box.half.x : -box.half.x, (corner & 2) ? box.half.y : -box.half.y,
+                    (corner & 4) ? box.half.z : -box.half.z};
+        const V3 cw = qrot(box.rot, cl) + box.center;
+        V3 push;
+        float surf;
+        if (!sampleInsideCylinder(cyl, cw, margin, push, surf))
+            continue;
+        Candidate &c = cand[nc++];
+        c.xA = cylIsA ? cw + push * surf : cw;
+        c.xB = cylIsA ? cw : cw + push * surf;
+        c.normal = cylIsA ? push : -push;
+        c.depth = surf;
+        c.feature = (kAxisCylCorner << 24) | ((cylIsA ? 0u : 1u) << 20) | static_cast<uint32_t>(corner);
+        normalAB += c.normal;
+    }
+    if (!nc)
+        return 0;
+    basis = orthonormal(-(length2(normalAB) > 1.0e-12f ? normalize(normalAB) : cyl.axis));
+    emitRanked(cand, nc, sink);
+    return sink.count;
+}
+
+int collideCylinderCylinder(const Shape &a, const Shape &b, float margin, ContactSink &sink, M3 &basis) {
+    Candidate cand[kMaxCandidates];
+    int nc = 0;
+    V3 normalAB{0, 0, 0};
+    V3 samples[kMaxCylSamples];
+    const Shape *pair[2] = {&a, &b};
+    for (int pass = 0; pass < 2; ++pass) {
+        const Shape &from = *pair[pass];
+        const Shape &into = *pair[pass == 0 ? 1 : 0];
+        const bool fromIsA = pass == 0;
+        int ns = 0;
+        cylinderSamples(from, samples, ns);
+        for (int i = 0; i < ns && nc < kMaxCandidates; ++i) {
+            V3 push;
+            float surf;
+            if (!sampleInsideCylinder(into, samples[i], margin, push, surf))
+                continue;
+            Candidate &c = cand[nc++];
+            c.xA = fromIsA ? samples[i] : samples[i] + push * surf;
+            c.xB = fromIsA ? samples[i] + push * surf : samples[i];
+            c.normal = fromIsA ? -push : push;
+            c.depth = surf;
+            c.feature = (kAxisCylSample << 24) | ((fromIsA ? 1u : 0u) << 20) | static_cast<uint32_t>(i);
+            normalAB += c.normal;
+        }
+    }
+    if (!nc)
+        return 0;
+    basis = orthonormal(-(length2(normalAB) > 1.0e-12f ? normalize(normalAB) : a.axis));
+    emitRanked(cand, nc, sink);
+    return sink.count;
+}
+
+// collideShapes' dispatch for pairs with a sphere or cylinder (collide.cpp:1001-1027).
+int collideRound(const Body &A, const Body &B, float margin, Contact *out, M3 &basis) {
+    const Shape a = makeShape(A), b = makeShape(B);
+    const Obb oa{a.center, a.rot, a.half, {}}, ob{b.center, b.rot, b.half, {}};
+    ContactSink sink{oa, ob, out, 0, {}};
+    if (a.type == 1 && b.type == 1)
+        return collideSphereSphere(a, b, margin, sink, basis);
+    if (a.type == 1 || b.type == 1) {
+        const bool sphereIsA = a.type == 1;
+        if (a.type == 2 || b.type == 2)
+            return collideSphereCylinder(a, b, sphereIsA, margin, sink, basis);
+        return collideSphereBox(a, b, sphereIsA, margin, sink, basis);
+    }
+    if (a.type == 2 && b.type == 2)
+        return collideCylinderCylinder(a, b, margin, sink, basis);
+    return collideCylinderBox(a, b, a.type == 2, margin, sink, basis);
+}
+
+} // namespace
+
 int World::collide(const Body &A, const Body &B, Contact *out, M3 &basis) const {
     float margin = P.speculative_margin;
     if (margin > 0.0f) {
@@ -1034,6 +1399,8 @@ int World::collide(const Body &A, const Body &B, Contact *out, M3 &basis) const 
         const V3 disp = (A.v - B.v) * horizon + V3{0, 0, (gA - gB) * horizon * horizon};
         margin += length(disp) + (A.radius * length(A.w) + B.radius * length(B.w)) * horizon;
     }
+    if (A.shape != 0 || B.shape != 0)
+        return collideRound(A, B, margin, out, basis);
     return collideBoxes(A.x, A.q, A.size * 0.5f, B.x, B.q, B.size * 0.5f, margin, out, basis);
 }
 
@@ -1394,7 +1761,9 @@ void World::broadPhase() {
     for (int i = 0; i < n; i++) {
         const Body &b = bodies[idAt(i)];
         const M3 rot = qmat(b.q);
-        const V3 h = b.size * 0.5f;
+        // aabbHalfExtent (rigid.cpp:83-106): sphere (r, r, r), cylinder (r, r, h/2), box size/2.
+        const V3 h = b.shape == 1 ? V3{b.size.x, b.size.x, b.size.x}
+                                  : (b.shape == 2 ? V3{b.size.x, b.size.x, b.size.z * 0.5f} : b.size * 0.5f);
         const V3 tight{(std::fabs(rot.c[0][0]) * h.x + std::fabs(rot.c[1][0]) * h.y) + std::fabs(rot.c[2][0]) * h.z,
                        (std::fabs(rot.c[0][1]) * h.x + std::fabs(rot.c[1][1]) * h.y) + std::fabs(rot.c[2][1]) * h.z,
                        (std::fabs(rot.c[0][2]) * h.x + std::fabs(rot.c[1][2]) * h.y) + std::fabs(rot.c[2][2]) * h.z};

@@ -122,8 +122,8 @@ int avbdo_world_add_bodies(World *w, int count, const avbdg_body_desc *d, int *i
     if (!w || count < 0 || (count > 0 && !d))
         return fail(AVBDG_ERR_INVALID, "bad argument");
     for (int i = 0; i < count; i++)
-        if (d[i].shape != AVBDG_SHAPE_BOX)
-            return fail(AVBDG_ERR_UNSUPPORTED, "only box bodies are restated");
+        if (d[i].shape < AVBDG_SHAPE_BOX || d[i].shape > AVBDG_SHAPE_CYLINDER)
+            return fail(AVBDG_ERR_INVALID, "unknown shape");
     for (int i = 0; i < count; i++) {
         const int id = w->addBody(d[i]);
         if (ids)

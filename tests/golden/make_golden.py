@@ -41,6 +41,7 @@ RUNS = [
 POSE_RUNS = [
     ("joint_zoo", {}, 60, [1, 10, 20, 30, 60]),
     ("sleepers", {}, 300, [60, 150, 200, 300]),
+    ("pile_grace", {}, 240, [120, 240]),
 ]
 
 

@@ -55,3 +55,37 @@ def test_gpu_sleep_in_batch(pkg, gpu):
     for x, y, field in zip(batch.state(0), plain.state(), ["position", "orientation", "velocity", "angular"]):
         assert np.array_equal(x, y), f"batched sleepers: {field}"
     batch.close()
+
+
+def test_gpu_contact_grace_matches_reference(pkg, gpu, golden):
+    """Contact grace: parked manifolds keep their state for a few ticks and revive by feature key;
+    every step's digest equals the reference's recorded run."""
+    scenes = pkg.scenes
+    rec = golden["pose_runs"]["pile_grace"]
+    sc = scenes.pile_grace()
+    w = scenes.instantiate(gpu, sc)
+    for s in range(rec["steps"]):
+        w.step()
+        assert f"{w.digest():016x}" == rec["digests"][s], f"step {s + 1}: digest differs"
+
+
+def test_gpu_contact_grace_batch_and_graphs(pkg, gpu, oracle, monkeypatch):
+    """Grace with sleeping in one batch of worlds, eager and captured steps alike."""
+    capi, scenes = pkg.capi, pkg.scenes
+    sc = scenes.pile_grace(count=120, chain_links=4)
+    sc.params = dict(sc.params, sleep_frames=20)
+    b = scenes.instantiate(oracle, sc)
+    b.step(150)
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("AVBDG_NO_GRAPHS", "0" if graphs == "1" else "1")
+        p = gpu.default_params()
+        scenes.apply_params(p, sc.params)
+        batch = capi.Batch(gpu.lib, p)
+        batch.add_scene(scenes.pyramid420())
+        batch.add_scene(sc)
+        batch.step(60)
+        batch.remove_worlds([0])
+        batch.step(90)
+        for x, y, field in zip(batch.state(0), b.state(), ["position", "orientation", "velocity", "angular"]):
+            assert np.array_equal(x, y), f"graphs={graphs}: {field}"
+        batch.close()
