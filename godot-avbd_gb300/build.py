@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
     "-I" + os.path.join(ROOT, "include"),
 ]
-SOURCES = ["prims.cu", "k_broad.cu", "k_manifold.cu", "k_solve.cu", "k_proj.cu", "k_io.cu", "k_relocate.cu", "k_sleep.cu", "engine.cu",
+SOURCES = ["prims.cu", "k_broad.cu", "k_manifold.cu", "k_solve.cu", "k_proj.cu", "k_io.cu", "k_relocate.cu", "k_sleep.cu", "k_query.cu", "engine.cu",
            "capi.cu", "server.cu", "sortkeys.cu"]
 
 

@@ -190,6 +190,8 @@ _WORLD_FUNCS = {
     "world_sync": [C.c_void_p],
     "world_get_body_state": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp, _fp],
     "world_get_sleeping": [C.c_void_p, C.c_int, C.c_int, _bp],
+    "world_pick": [C.c_void_p, C.c_int, _fp, _fp, C.c_uint32, _ip, _fp],
+    "world_collect_aabb": [C.c_void_p, _fp, _fp, C.c_uint32, C.c_int, _ip, C.POINTER(C.c_int)],
     "world_set_body_state": [C.c_void_p, C.c_int, C.c_int, _fp, _fp, _fp, _fp],
     "world_get_stats": [C.c_void_p, C.POINTER(Stats)],
     "world_digest": [C.c_void_p, _up],
@@ -392,6 +394,27 @@ class World:
         p, q, v, w = arr(position, 3), arr(orientation, 4), arr(velocity, 3), arr(angular_velocity, 3)
         self.api.check(self.api.world_set_body_state(self.handle, 0, n, _ptr(p, C.c_float), _ptr(q, C.c_float),
                                                      _ptr(v, C.c_float), _ptr(w, C.c_float)))
+
+    def pick(self, origins, dirs, mask=0xFFFFFFFF):
+        """Solver::pick for each ray: (body creation indices, -1 = no hit; hit points in body frames)."""
+        o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
+        dvec = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        n = o.shape[0]
+        body = np.zeros(n, np.int32)
+        local = np.zeros((n, 3), np.float32)
+        self.api.check(self.api.world_pick(self.handle, n, _ptr(o, C.c_float), _ptr(dvec, C.c_float), int(mask),
+                                           _ptr(body, C.c_int32), _ptr(local, C.c_float)))
+        return body, local
+
+    def collect_aabb(self, lo, hi, mask=0xFFFFFFFF):
+        """Solver::collectAABB: creation indices of bodies overlapping [lo, hi], in list order."""
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        out = np.zeros(max(self.n_bodies, 1), np.int32)
+        cnt = C.c_int()
+        self.api.check(self.api.world_collect_aabb(self.handle, _ptr(lo, C.c_float), _ptr(hi, C.c_float), int(mask),
+                                                   len(out), _ptr(out, C.c_int32), C.byref(cnt)))
+        return out[:min(cnt.value, len(out))].copy()
 
     def sleeping(self):
         out = np.zeros(self.n_bodies, np.uint8)

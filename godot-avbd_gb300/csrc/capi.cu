@@ -263,6 +263,16 @@ int avbdg_world_get_sleeping(avbdg_world *w, int first, int count, uint8_t *out)
     return guarded(w, [=](avbdg::Engine &e) { return e.getSleeping(0, first, count, out); });
 }
 
+int avbdg_world_pick(avbdg_world *w, int count, const float *origins, const float *dirs, uint32_t mask,
+                     int *out_body, float *out_local) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.pick(0, count, origins, dirs, mask, out_body, out_local); });
+}
+
+int avbdg_world_collect_aabb(avbdg_world *w, const float lo[3], const float hi[3], uint32_t mask, int capacity,
+                             int *out, int *out_count) {
+    return guarded(w, [=](avbdg::Engine &e) { return e.collectAabb(0, lo, hi, mask, capacity, out, out_count); });
+}
+
 int avbdg_world_get_body_state(avbdg_world *w, int first, int count, float *p, float *q, float *v, float *av) {
     return guarded(w, [=](avbdg::Engine &e) { return e.getState(0, first, count, p, q, v, av); });
 }

@@ -15,8 +15,32 @@ namespace avbdg {
 
 namespace {
 
-// Rigid::Rigid for boxes (src/avbd/rigid.cpp:22-72); host compiled with -ffp-contract=off.
-void boxMassProperties(const avbdg_body_desc &b, float &mass, float moment[3], float &radius) {
+// Rigid::Rigid (src/avbd/rigid.cpp:22-72) per shape; host compiled with -ffp-contract=off.
+void massProperties(const avbdg_body_desc &b, float &mass, float moment[3], float &radius) {
+    if (b.shape == AVBDG_SHAPE_SPHERE) {
+        const float r = b.size[0];
+        mass = (4.0f / 3.0f) * 3.14159265358979f * r * r * r * b.density;
+        const float i = 0.4f * mass * r * r;
+        moment[0] = moment[1] = moment[2] = i;
+        radius = r;
+        return;
+    }
+    if (b.shape == AVBDG_SHAPE_CYLINDER) {
+        const float r = b.size[0], h = b.size[2];
+        mass = 3.14159265358979f * r * r * h * b.density;
+        const float axial = 0.5f * mass * r * r;
+        const float radialM = mass * (3.0f * r * r + h * h) / 12.0f;
+        moment[0] = moment[1] = radialM;
+        moment[2] = axial;
+        const float hh = h * 0.5f;
+        const float px = r * r, py = hh * hh, pz = r * r;
+        float s = 0.0f;
+        s = s + px;
+        s = s + py;
+        s = s + pz;
+        radius = std::sqrt(s);
+        return;
+    }
     const float sx = b.size[0], sy = b.size[1], sz = b.size[2];
     mass = sx * sy * sz * b.density;
     moment[0] = (sy * sy + sz * sz) / 12.0f * mass;
@@ -320,9 +344,9 @@ int Engine::ensureCapacity(int nb, int ff, int ww) {
 int Engine::validateBodies(int count, const avbdg_body_desc *descs, std::string &why) {
     for (int i = 0; i < count; i++) {
         const avbdg_body_desc &b = descs[i];
-        if (b.shape != AVBDG_SHAPE_BOX) {
-            why = "only box bodies run on the GPU path";
-            return AVBDG_ERR_UNSUPPORTED;
+        if (b.shape < AVBDG_SHAPE_BOX || b.shape > AVBDG_SHAPE_CYLINDER) {
+            why = "unknown shape";
+            return AVBDG_ERR_INVALID;
         }
         if (b.sleep_mode > 2) {
             why = "sleep_mode must be 0, 1 or 2";
@@ -368,6 +392,7 @@ int Engine::addWorld() {
     wBase.push_back(nBodies);
     wCount.push_back(0);
     wDyn.push_back(0);
+    wRound.push_back(0);
     const int w = worlds() - 1;
     cudaMemcpyAsync(d.wBase + w, &wBase[w], sizeof(int), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.wCount + w, &wCount[w], sizeof(int), cudaMemcpyHostToDevice, stream);
@@ -395,7 +420,7 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
     for (int i = 0; i < count; i++) {
         const avbdg_body_desc &b = descs[i];
         float mass, moment[3], radius;
-        boxMassProperties(b, mass, moment, radius);
+        massProperties(b, mass, moment, radius);
         x[i] = make_float4(b.position[0], b.position[1], b.position[2], mass);
         q[i] = make_float4(b.orientation[0], b.orientation[1], b.orientation[2], b.orientation[3]);
         v[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], P.gravity);
@@ -404,13 +429,17 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
         mo[i] = make_float4(moment[0], moment[1], moment[2], b.friction);
         meta[i] = make_int4(w, static_cast<int>(b.collision_layer), static_cast<int>(b.collision_mask),
                             static_cast<int>((b.axis_lock_linear & 0xff) | ((b.axis_lock_angular & 0xff) << 8) |
-                                             ((b.sleep_mode & 0x3) << 16)));
+                                             ((b.sleep_mode & 0x3) << 16) | ((b.shape & 0x3) << 18)));
         zero4[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
         if (outIds)
             outIds[i] = first - wBase[w] + i;
         if (mass > 0.0f) {
             nDynamic++;
             wDyn[w]++;
+        }
+        if (b.shape != AVBDG_SHAPE_BOX) {
+            nRound++;
+            wRound[w]++;
         }
     }
     const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
@@ -608,8 +637,8 @@ int Engine::removeWorlds(const std::vector<int> &ids) {
         return AVBDG_OK;
     if (cudaStreamSynchronize(stream) != cudaSuccess)
         return cudaCheck("removeWorlds");
-    std::vector<int> remap(2 * static_cast<size_t>(nw)), base, count, dyn;
-    int nb = 0, ndyn = 0;
+    std::vector<int> remap(2 * static_cast<size_t>(nw)), base, count, dyn, round;
+    int nb = 0, ndyn = 0, nround = 0;
     for (int w = 0; w < nw; w++) {
         if (drop[w]) {
             remap[2 * w] = -1;
@@ -621,14 +650,17 @@ int Engine::removeWorlds(const std::vector<int> &ids) {
         base.push_back(nb);
         count.push_back(wCount[w]);
         dyn.push_back(wDyn[w]);
+        round.push_back(wRound[w]);
         nb += wCount[w];
         ndyn += wDyn[w];
+        nround += wRound[w];
     }
     cudaMemcpyAsync(d.relocRemap, remap.data(), sizeof(int) * remap.size(), cudaMemcpyHostToDevice, stream);
     launchRelocateWorlds(d, nBodies, nb, nForces, d.relocRemap, stream);
     wBase.swap(base);
     wCount.swap(count);
     wDyn.swap(dyn);
+    wRound.swap(round);
     if (!wBase.empty()) {
         cudaMemcpyAsync(d.wBase, wBase.data(), wBase.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
         cudaMemcpyAsync(d.wCount, wCount.data(), wCount.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
@@ -640,6 +672,7 @@ int Engine::removeWorlds(const std::vector<int> &ids) {
     if (cudaStreamSynchronize(stream) != cudaSuccess)
         return cudaCheck("removeWorlds");
     nDynamic = ndyn;
+    nRound = nround;
     nForces = hostCtr[C_FORCES];
     treeValid = false;
     adjValid = false;
@@ -652,7 +685,8 @@ void Engine::clear() {
     wBase.clear();
     wCount.clear();
     wDyn.clear();
-    nBodies = nDynamic = nForces = 0;
+    wRound.clear();
+    nBodies = nDynamic = nForces = nRound = 0;
     cudaMemsetAsync(d.ctr, 0, sizeof(int) * C_COUNT, stream);
     cudaStreamSynchronize(stream);
     treeValid = adjValid = false;
@@ -739,13 +773,15 @@ Engine::StepPlan Engine::planStep(int mode, int substeps, int rounds) {
     plan.forces = nForces > 0;
     plan.greedy = needGreedy();
     plan.multiWorld = worlds() > 1;
+    plan.round = nRound > 0;
     return plan;
 }
 
 std::string Engine::StepPlan::key() const {
     char buf[128];
-    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0,
-                  anyTree ? 1 : 0, rebuild ? 1 : 0, forces ? 1 : 0, greedy ? 1 : 0, multiWorld ? 1 : 0);
+    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0,
+                  anyTree ? 1 : 0, rebuild ? 1 : 0, forces ? 1 : 0, greedy ? 1 : 0, multiWorld ? 1 : 0,
+                  round ? 1 : 0);
     return buf;
 }
 
@@ -890,7 +926,7 @@ int Engine::runPlan(const StepPlan &plan) {
 int Engine::warmstartAndSelect(const StepParams &sp) {
     launchForceInit(d, sp, nForces > 0, stream);
     beginSpan();
-    launchManifoldInit(d, sp, tuned.narrow, stream);
+    launchManifoldInit(d, sp, nRound > 0, tuned.narrow, stream);
     endSpan(kNarrow);
     launchManifoldCompact(d, stream);
     launchAdjacency(d, stream);
@@ -1049,6 +1085,83 @@ int Engine::getSleeping(int w, int first, int count, uint8_t *out) {
     for (int i = 0; i < count; i++)
         out[i] = s[i].x ? 1 : 0;
     return cudaCheck("getSleeping");
+}
+
+namespace {
+
+// Device scratch of one query call, released on every path.
+struct QueryScratch {
+    std::vector<void *> ptrs;
+    ~QueryScratch() {
+        for (void *p : ptrs)
+            cudaFree(p);
+    }
+    template <typename T>
+    T *get(size_t n) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+            return nullptr;
+        ptrs.push_back(p);
+        return static_cast<T *>(p);
+    }
+};
+
+} // namespace
+
+int Engine::pick(int w, int count, const float *origins, const float *dirs, uint32_t mask, int *outBody,
+                 float *outLocal) {
+    if (w < 0 || w >= worlds() || count < 0 || (count > 0 && (!origins || !dirs || !outBody)))
+        return fail(AVBDG_ERR_INVALID, "bad pick arguments");
+    if (count == 0)
+        return AVBDG_OK;
+    std::vector<float> rays(6 * static_cast<size_t>(count));
+    for (int i = 0; i < count; i++)
+        for (int k = 0; k < 3; k++) {
+            rays[6 * i + k] = origins[3 * i + k];
+            rays[6 * i + 3 + k] = dirs[3 * i + k];
+        }
+    QueryScratch q;
+    float *dRays = q.get<float>(rays.size());
+    auto *dBest = q.get<unsigned long long>(count);
+    int *dBody = q.get<int>(count);
+    float *dLocal = q.get<float>(3 * static_cast<size_t>(count));
+    if (!dRays || !dBest || !dBody || !dLocal)
+        return fail(AVBDG_ERR_CAPACITY, "query scratch allocation failed");
+    sync();
+    cudaMemcpyAsync(dRays, rays.data(), sizeof(float) * rays.size(), cudaMemcpyHostToDevice, stream);
+    launchPick(d, wBase[w], wCount[w], dRays, count, mask, dBest, dBody, dLocal, stream);
+    std::vector<float> local(3 * static_cast<size_t>(count));
+    cudaMemcpyAsync(outBody, dBody, sizeof(int) * static_cast<size_t>(count), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(local.data(), dLocal, sizeof(float) * local.size(), cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("pick");
+    if (outLocal)
+        std::memcpy(outLocal, local.data(), sizeof(float) * local.size());
+    return cudaCheck("pick");
+}
+
+int Engine::collectAabb(int w, const float lo[3], const float hi[3], uint32_t mask, int capacity, int *out,
+                        int *outCount) {
+    if (w < 0 || w >= worlds() || !lo || !hi || capacity < 0 || (capacity > 0 && !out))
+        return fail(AVBDG_ERR_INVALID, "bad collect arguments");
+    const int n = wCount[w];
+    QueryScratch q;
+    int *flags = q.get<int>(n), *rank = q.get<int>(n), *total = q.get<int>(1), *ids = q.get<int>(n);
+    if (!flags || !rank || !total || !ids)
+        return fail(AVBDG_ERR_CAPACITY, "query scratch allocation failed");
+    sync();
+    launchCollectAabb(d, wBase[w], n, f3{lo[0], lo[1], lo[2]}, f3{hi[0], hi[1], hi[2]}, mask, flags, rank, total,
+                      d.scanScratch, n, ids, stream);
+    int found = 0;
+    cudaMemcpyAsync(&found, total, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cudaCheck("collectAabb");
+    const int k = std::min(found, capacity);
+    if (k > 0)
+        cudaMemcpy(out, ids, sizeof(int) * static_cast<size_t>(k), cudaMemcpyDeviceToHost);
+    if (outCount)
+        *outCount = found;
+    return cudaCheck("collectAabb");
 }
 
 int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {

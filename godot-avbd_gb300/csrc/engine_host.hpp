@@ -62,6 +62,11 @@ public:
 
     int getState(int world, int first, int count, float *pos, float *quat, float *vel, float *angVel);
     int getSleeping(int world, int first, int count, uint8_t *out);
+    // Solver::pick / collectAABB of one world (body ids in creation order).
+    int pick(int world, int count, const float *origins, const float *dirs, uint32_t mask, int *outBody,
+             float *outLocal);
+    int collectAabb(int world, const float lo[3], const float hi[3], uint32_t mask, int capacity, int *out,
+                    int *outCount);
     int setState(int world, int first, int count, const float *pos, const float *quat, const float *vel,
                  const float *angVel);
     int stats(avbdg_stats &out);
@@ -98,8 +103,8 @@ private:
     Dev d{};
     cudaStream_t stream = nullptr;
     std::vector<void *> allocs;
-    std::vector<int> wBase, wCount, wDyn;
-    int nBodies = 0, nDynamic = 0, nForces = 0;
+    std::vector<int> wBase, wCount, wDyn, wRound;
+    int nBodies = 0, nDynamic = 0, nForces = 0, nRound = 0; // nRound: spheres and cylinders
     int treeAge = 0;
     bool treeValid = false, adjValid = false;
     size_t byteLimit = 0;
@@ -164,7 +169,7 @@ private:
         int mode = 0; // 0 step, 1 interleaved
         int substeps = 1, rounds = 0;
         bool adjAtStart = false, anyTree = false, rebuild = false, forces = false, greedy = false;
-        bool multiWorld = false;
+        bool multiWorld = false, round = false;
         std::string key() const;
     };
     struct Graph {

@@ -35,7 +35,9 @@ __global__ void aabbKernel(Dev d, StepParams p) {
     const float4 v4 = d.v[g];
     const float4 s4 = d.size[g];
     const m3 rot = qmat(asq(d.q[g]));
-    const f3 h = scale(xyz(s4), 0.5f);
+    // aabbHalfExtent (rigid.cpp:83-106): sphere (r, r, r), cylinder (r, r, h/2), box size/2.
+    const int shape = (d.meta[g].w >> 18) & 0x3;
+    const f3 h = shape == 1 ? f3{s4.x, s4.x, s4.x} : (shape == 2 ? f3{s4.x, s4.x, s4.z * 0.5f} : scale(xyz(s4), 0.5f));
     const f3 tight{(fabsf(rot.c0.x) * h.x + fabsf(rot.c1.x) * h.y) + fabsf(rot.c2.x) * h.z,
                    (fabsf(rot.c0.y) * h.x + fabsf(rot.c1.y) * h.y) + fabsf(rot.c2.y) * h.z,
                    (fabsf(rot.c0.z) * h.x + fabsf(rot.c1.z) * h.y) + fabsf(rot.c2.z) * h.z};

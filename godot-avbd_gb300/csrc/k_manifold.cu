@@ -6,12 +6,18 @@
 // survivors back in order (the reference's stable compaction of `live`). Slot recycling is an
 // allocation detail of the reference that never reaches its arithmetic, so it has no equivalent.
 
+#include <cmath>
+
 #include "forces.cuh"
 #include "kernels.cuh"
 #include "narrow.cuh"
+#include "narrow_round.cuh"
 #include "prims.cuh"
 
 namespace avbdg {
+
+// Cylinder rim directions (narrow_round.cuh), uploaded once by prepareNarrowPhase.
+__constant__ narrow::RimTable c_rim;
 
 namespace {
 
@@ -88,6 +94,9 @@ __device__ __forceinline__ f3 basisMul(f3 r0, f3 r1, f3 r2, f3 v) {
               (r2.x * v.x + r2.y * v.y) + r2.z * v.z};
 }
 
+// ROUND: the store holds spheres or cylinders, whose sampled paths need kilobytes of local memory
+// per thread; box-only stores run the variant without them.
+template <bool ROUND>
 __global__ void manifoldInitKernel(Dev d, StepParams p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.ctr[C_CAND])
@@ -144,8 +153,12 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     NContact nc[kMaxContacts];
     m3 basis = mcols(xyz(L.b0[i]), xyz(L.b1[i]), xyz(L.b2[i])); // rows kept when the SAT fails early
     basis = transpose(basis);
-    const int n = collideBoxes(xa, qa, scale(xyz(d.size[a]), 0.5f), xb, qb, scale(xyz(d.size[b]), 0.5f), margin,
-                               nc, basis);
+    const int shapeA = (d.meta[a].w >> 18) & 0x3, shapeB = (d.meta[b].w >> 18) & 0x3;
+    const int n = (!ROUND || (shapeA == 0 && shapeB == 0))
+                          ? collideBoxes(xa, qa, scale(xyz(d.size[a]), 0.5f), xb, qb, scale(xyz(d.size[b]), 0.5f),
+                                         margin, nc, basis)
+                          : collideRound(shapeA, xa, qa, xyz(d.size[a]), shapeB, xb, qb, xyz(d.size[b]), margin,
+                                         c_rim, nc, basis);
     const f3 r0 = mrow(basis, 0), r1 = mrow(basis, 1), r2 = mrow(basis, 2);
 
     f3 newK[kMaxContacts], newLam[kMaxContacts];
@@ -391,6 +404,18 @@ __global__ void forceCompactKernel(Dev d) {
 
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
+// cos/sin of 2 pi * (5 i mod 8) / 8 with the C library, exactly as collide.cpp:739-753 builds them.
+void prepareNarrowPhase() {
+    narrow::RimTable t{};
+    for (int i = 0; i < narrow::kRimSamples; ++i) {
+        const int step = i * 5 % narrow::kRimSamples;
+        const float a = 6.28318530718f * (float)step / (float)narrow::kRimSamples;
+        t.c[i] = std::cos(a);
+        t.s[i] = std::sin(a);
+    }
+    cudaMemcpyToSymbol(c_rim, &t, sizeof(t));
+}
+
 void launchAdjacency(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.adjStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.adjFill, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
@@ -402,8 +427,12 @@ void launchAdjacency(const Dev &d, cudaStream_t s) {
     segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
 }
 
-void launchManifoldInit(const Dev &d, const StepParams &p, int block, cudaStream_t s) {
-    ++launchCount(); manifoldInitKernel<<<divUp(d.MM, block), block, 0, s>>>(d, p);
+void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block, cudaStream_t s) {
+    ++launchCount();
+    if (round)
+        manifoldInitKernel<true><<<divUp(d.MM, block), block, 0, s>>>(d, p);
+    else
+        manifoldInitKernel<false><<<divUp(d.MM, block), block, 0, s>>>(d, p);
 }
 
 void launchManifoldCompact(const Dev &d, cudaStream_t s) {

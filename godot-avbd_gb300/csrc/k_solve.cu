@@ -972,6 +972,7 @@ int colourGridBlocks() {
 
 void prepareKernels() {
     preparePrimitives();
+    prepareNarrowPhase();
     brakeGridBlocks();
     colourGridBlocks();
 }

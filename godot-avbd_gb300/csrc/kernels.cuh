@@ -32,7 +32,7 @@ void launchFilterAcquire(const Dev &d, cudaStream_t s);
 
 // ---- manifolds and adjacency (k_manifold.cu) ----
 void launchAdjacency(const Dev &d, cudaStream_t s);
-void launchManifoldInit(const Dev &d, const StepParams &p, int block, cudaStream_t s);
+void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block, cudaStream_t s);
 void launchManifoldCompact(const Dev &d, cudaStream_t s);
 void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s);
 void launchForceInit(const Dev &d, const StepParams &p, bool forces, cudaStream_t s);
@@ -68,6 +68,8 @@ void launchBrake(const Dev &d, float window, cudaStream_t s);
 void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s);
 
 int brakeGridBlocks();
+// Constant tables of the narrow phase (cylinder rim directions); before any capture.
+void prepareNarrowPhase();
 int colourGridBlocks();
 // Kernel attributes and cooperative grid sizes, set once before any stream capture.
 void prepareKernels();
@@ -82,6 +84,13 @@ void launchUnpackState(const Dev &d, int first, int count, const float *buf, int
 void launchSleepWakePairs(const Dev &d, cudaStream_t s);
 // Wake pass over the adjacency, then island sleep (before the update set is chosen).
 void launchSleepSelect(const Dev &d, const StepParams &p, cudaStream_t s);
+
+// ---- queries (k_query.cu) ----
+// Rays: 6 floats each (origin, dir). `best` holds one key per ray; results in world creation index.
+void launchPick(const Dev &d, int base, int count, const float *rays, int nRays, unsigned mask,
+                unsigned long long *best, int *outBody, float *outLocal, cudaStream_t s);
+void launchCollectAabb(const Dev &d, int base, int count, f3 lo, f3 hi, unsigned mask, int *flags, int *rank,
+                       int *total, void *scanScratch, int capacity, int *out, cudaStream_t s);
 
 // ---- world removal (k_relocate.cu) ----
 // Moves the surviving worlds' bodies down to their new bases (remap: per old world, new id or -1

@@ -91,18 +91,20 @@ struct Sink {
     int n;
     f3 mid[8];
 
-    __device__ void addc(f3 xA, f3 xB, int key) {
+    // addContact (collide.cpp:208-233): false when merged into an earlier contact or full.
+    __device__ bool addc(f3 xA, f3 xB, int key) {
         const f3 m = scale(add(xA, xB), 0.5f);
         for (int i = 0; i < n; ++i)
             if (length2(sub(m, mid[i])) < kMergeSq)
-                return;
+                return false;
         if (n >= 8)
-            return;
+            return false;
         out[n].key = key;
         out[n].rA = qrot(qconj(qA), sub(xA, cA));
         out[n].rB = qrot(qconj(qB), sub(xB, cB));
         mid[n] = m;
         ++n;
+        return true;
     }
 };
 

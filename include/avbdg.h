@@ -208,6 +208,18 @@ int avbdg_world_get_body_state(avbdg_world *world, int first, int count, float *
 /* Rigid::sleeping of bodies [first, first+count) (creation order): 1 asleep, 0 awake. */
 int avbdg_world_get_sleeping(avbdg_world *world, int first, int count, uint8_t *sleeping);
 
+/* Solver::pick (src/avbd/solver_query.cpp:24-152) for `count` rays at once: ray i starts at
+ * origins[3i..] along dirs[3i..] (not normalised; distances are in units of dir). out_body[i] is
+ * the creation index of the nearest body hit whose layer meets `mask` (-1: none; the first in list
+ * order wins a tie), out_local[3i..] the hit point in that body's frame. */
+int avbdg_world_pick(avbdg_world *world, int count, const float *origins, const float *dirs, uint32_t mask,
+                     int *out_body, float *out_local);
+/* Solver::collectAABB (src/avbd/solver_query.cpp:154-170): bodies whose tight bounds overlap
+ * [min, max] and whose layer meets `mask`, in list order (creation indices). Writes at most
+ * `capacity` ids; *out_count is the number found. */
+int avbdg_world_collect_aabb(avbdg_world *world, const float min[3], const float max[3], uint32_t mask,
+                             int capacity, int *out_bodies, int *out_count);
+
 /* Write the same fields (host edits between steps, e.g. integrated external forces,
  * src/server/avbd_physics_server3d.cpp:1503-1528). Any pointer may be NULL. */
 int avbdg_world_set_body_state(avbdg_world *world, int first, int count, const float *position,

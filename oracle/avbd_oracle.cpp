@@ -2499,6 +2499,106 @@ void World::stepInterleaved(int substeps, int roundsPerSubstep) {
     steps++;
 }
 
+static V3 localHalfExtent(const Body &b) {
+    if (b.shape == 1)
+        return V3{b.size.x, b.size.x, b.size.x};
+    if (b.shape == 2)
+        return V3{b.size.x, b.size.x, b.size.z * 0.5f};
+    return b.size * 0.5f;
+}
+
+// Solver::pick (solver_query.cpp:24-152): exact ray tests per body in list order.
+int World::pick(V3 origin, V3 dir, uint32_t mask, V3 &local) const {
+    const float eps = 1.0e-6f;
+    float bestT = std::numeric_limits<float>::infinity();
+    int best = -1;
+    V3 bestLocal{0, 0, 0};
+    for (int li = 0; li < count(); li++) {
+        const int id = idAt(li);
+        const Body &b = bodies[id];
+        if ((b.layer & mask) == 0)
+            continue;
+        const Q4 inv = qconj(b.q);
+        const V3 o = qrot(inv, origin - b.x);
+        const V3 d = qrot(inv, dir);
+        if (b.shape == 1) {
+            const float r = b.size.x;
+            const float bb = dot(o, d);
+            const float c = length2(o) - r * r;
+            const float disc = bb * bb - c;
+            if (disc < 0.0f)
+                continue;
+            const float sq = std::sqrt(disc);
+            float t = -bb - sq;
+            if (t < 0.0f)
+                t = -bb + sq;
+            if (t < 0.0f || t >= bestT)
+                continue;
+            bestT = t;
+            best = id;
+            bestLocal = o + d * t;
+            continue;
+        }
+        const V3 half = localHalfExtent(b);
+        float tEnter = 0.0f, tExit = std::numeric_limits<float>::infinity();
+        bool hit = true;
+        for (int i = 0; i < 3; ++i) {
+            if (std::fabs(d[i]) < eps) {
+                if (o[i] < -half[i] || o[i] > half[i]) {
+                    hit = false;
+                    break;
+                }
+                continue;
+            }
+            const float invD = 1.0f / d[i];
+            float t0 = (-half[i] - o[i]) * invD;
+            float t1 = (half[i] - o[i]) * invD;
+            if (t0 > t1) {
+                const float tmp = t0;
+                t0 = t1;
+                t1 = tmp;
+            }
+            tEnter = smax(tEnter, t0);
+            tExit = smin(tExit, t1);
+            if (tEnter > tExit) {
+                hit = false;
+                break;
+            }
+        }
+        if (!hit)
+            continue;
+        const float tHit = tEnter >= 0.0f ? tEnter : tExit;
+        if (tHit < 0.0f)
+            continue;
+        if (tHit < bestT) {
+            bestT = tHit;
+            best = id;
+            bestLocal = o + d * tHit;
+        }
+    }
+    if (best >= 0)
+        local = bestLocal;
+    return best;
+}
+
+// Solver::collectAABB (solver_query.cpp:154-170): tight bounds (aabbHalfExtent) about each centre.
+void World::collectAABB(V3 lo, V3 hi, uint32_t mask, std::vector<int> &out) const {
+    for (int li = 0; li < count(); li++) {
+        const int id = idAt(li);
+        const Body &b = bodies[id];
+        if ((b.layer & mask) == 0)
+            continue;
+        const M3 rot = qmat(b.q);
+        const V3 h = localHalfExtent(b);
+        const V3 wx{(std::fabs(rot.c[0][0]) * h.x + std::fabs(rot.c[1][0]) * h.y) + std::fabs(rot.c[2][0]) * h.z,
+                    (std::fabs(rot.c[0][1]) * h.x + std::fabs(rot.c[1][1]) * h.y) + std::fabs(rot.c[2][1]) * h.z,
+                    (std::fabs(rot.c[0][2]) * h.x + std::fabs(rot.c[1][2]) * h.y) + std::fabs(rot.c[2][2]) * h.z};
+        const V3 bmin = b.x - wx, bmax = b.x + wx;
+        if (!(bmin.x > hi.x || bmin.y > hi.y || bmin.z > hi.z || lo.x > bmax.x || lo.y > bmax.y || lo.z > bmax.z))
+            out.push_back(id);
+    }
+}
+
 // state_digest (test/core_test.cpp:133-149).
 uint64_t World::digest() const {
     uint64_t h = 1469598103934665603ull;

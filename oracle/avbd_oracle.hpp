@@ -130,6 +130,9 @@ public:
     void addGeneric(int a, int b, V3 rA, V3 rB, const Axis axes[6]);
     void step();
     void stepInterleaved(int substeps, int rounds);
+    // Solver::pick / collectAABB (src/avbd/solver_query.cpp): body ids, -1 = no hit.
+    int pick(V3 origin, V3 dir, uint32_t mask, V3 &local) const;
+    void collectAABB(V3 lo, V3 hi, uint32_t mask, std::vector<int> &out) const;
     uint64_t digest() const;
 
     // Independent per-body / per-manifold loops use all host threads unless `threads` is 1 (the

@@ -206,6 +206,36 @@ int avbdo_world_step_n(World *w, int count) {
 
 int avbdo_world_sync(World *) { return AVBDG_OK; }
 
+int avbdo_world_pick(World *w, int count, const float *o, const float *d, uint32_t mask, int *outBody,
+        float *outLocal) {
+    if (!w || count < 0 || (count > 0 && (!o || !d || !outBody)))
+        return fail(AVBDG_ERR_INVALID, "bad arguments");
+    for (int i = 0; i < count; i++) {
+        V3 local{0, 0, 0};
+        outBody[i] = w->pick(V3{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]}, mask,
+                local);
+        if (outLocal) {
+            outLocal[3 * i] = local.x;
+            outLocal[3 * i + 1] = local.y;
+            outLocal[3 * i + 2] = local.z;
+        }
+    }
+    return AVBDG_OK;
+}
+
+int avbdo_world_collect_aabb(World *w, const float *lo, const float *hi, uint32_t mask, int capacity, int *out,
+        int *outCount) {
+    if (!w || !lo || !hi || capacity < 0 || (capacity > 0 && !out))
+        return fail(AVBDG_ERR_INVALID, "bad arguments");
+    std::vector<int> ids;
+    w->collectAABB(V3{lo[0], lo[1], lo[2]}, V3{hi[0], hi[1], hi[2]}, mask, ids);
+    for (int i = 0; i < static_cast<int>(ids.size()) && i < capacity; i++)
+        out[i] = ids[i];
+    if (outCount)
+        *outCount = static_cast<int>(ids.size());
+    return AVBDG_OK;
+}
+
 int avbdo_world_get_sleeping(World *w, int first, int count, uint8_t *out) {
     if (!w || first < 0 || count < 0 || first + count > w->count() || (count > 0 && !out))
         return fail(AVBDG_ERR_INVALID, "bad range");

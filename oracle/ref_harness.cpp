@@ -286,6 +286,44 @@ int avbdr_world_step_n(RefWorld *w, int count) {
 
 int avbdr_world_sync(RefWorld *) { return AVBDG_OK; }
 
+static int refIndex(RefWorld *w, Rigid *r) {
+    for (int i = 0; i < (int)w->bodies.size(); i++)
+        if (w->bodies[i] == r)
+            return i;
+    return -1;
+}
+
+int avbdr_world_pick(RefWorld *w, int count, const float *o, const float *d, uint32_t mask, int *outBody,
+        float *outLocal) {
+    if (!w || count < 0 || (count > 0 && (!o || !d || !outBody)))
+        return fail(AVBDG_ERR_INVALID, "bad arguments");
+    for (int i = 0; i < count; i++) {
+        float3 local{0, 0, 0};
+        Rigid *r = w->solver.pick(float3{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, float3{d[3 * i], d[3 * i + 1], d[3 * i + 2]},
+                local, mask);
+        outBody[i] = r ? refIndex(w, r) : -1;
+        if (outLocal) {
+            outLocal[3 * i] = r ? local.x : 0.0f;
+            outLocal[3 * i + 1] = r ? local.y : 0.0f;
+            outLocal[3 * i + 2] = r ? local.z : 0.0f;
+        }
+    }
+    return AVBDG_OK;
+}
+
+int avbdr_world_collect_aabb(RefWorld *w, const float *lo, const float *hi, uint32_t mask, int capacity, int *out,
+        int *outCount) {
+    if (!w || !lo || !hi || capacity < 0 || (capacity > 0 && !out))
+        return fail(AVBDG_ERR_INVALID, "bad arguments");
+    std::vector<Rigid *> found;
+    w->solver.collectAABB(float3{lo[0], lo[1], lo[2]}, float3{hi[0], hi[1], hi[2]}, mask, found);
+    for (int i = 0; i < (int)found.size() && i < capacity; i++)
+        out[i] = refIndex(w, found[i]);
+    if (outCount)
+        *outCount = static_cast<int>(found.size());
+    return AVBDG_OK;
+}
+
 int avbdr_world_get_sleeping(RefWorld *w, int first, int count, uint8_t *out) {
     if (!w || first < 0 || count < 0 || first + count > (int)w->bodies.size() || (count > 0 && !out))
         return fail(AVBDG_ERR_INVALID, "bad range");

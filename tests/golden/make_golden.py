@@ -34,6 +34,7 @@ RUNS = [
     ("pyramid420", {}, 120),
     ("pile", {"count": 300, "chain_links": 8}, 120),
     ("lattice", {"nx": 8, "ny": 8, "nz": 4}, 90),
+    ("shape_mix", {}, 240),
 ]
 
 

@@ -79,3 +79,42 @@ def test_gpu_forces_in_batch_and_removal(pkg, gpu):
     for x, y, field in zip(batch.state(0), want, ["position", "orientation", "velocity", "angular"]):
         assert np.array_equal(x, y), f"batched joint zoo: {field}"
     batch.close()
+
+
+def test_gpu_shapes_in_batch(pkg, gpu):
+    """Spheres and cylinders batched with boxes (the round-shape narrow phase runs beside box
+    pairs in one launch) and with worlds removed: identical to the scene stepped alone."""
+    capi, scenes = pkg.capi, pkg.scenes
+    sc = scenes.shape_mix()
+    plain = scenes.instantiate(gpu, sc)
+    plain.step(80)
+    p = gpu.default_params()
+    scenes.apply_params(p, sc.params)
+    batch = capi.Batch(gpu.lib, p)
+    batch.add_scene(scenes.pyramid420())
+    batch.add_scene(sc)
+    batch.step(30)
+    batch.remove_worlds([0])
+    batch.step(50)
+    for x, y, field in zip(batch.state(0), plain.state(), ["position", "orientation", "velocity", "angular"]):
+        assert np.array_equal(x, y), f"batched shape mix: {field}"
+    batch.close()
+
+
+def test_gpu_queries_match_oracle(pkg, gpu, oracle):
+    """Ray picks (one launch for all rays) and box overlap collection on the device equal the
+    oracle's serial scans (which match the reference's; see the oracle pin tests)."""
+    scenes = pkg.scenes
+    sc = scenes.shape_mix()
+    a = scenes.instantiate(gpu, sc)
+    b = scenes.instantiate(oracle, sc)
+    a.step(40)
+    b.step(40)
+    rng = np.random.default_rng(4)
+    origins = rng.uniform([-15, -6, 1], [15, 6, 8], (256, 3)).astype(np.float32)
+    dirs = (rng.uniform([-15, -3, -1], [15, 3, 2], (256, 3)) - origins).astype(np.float32)
+    ga, la = a.pick(origins, dirs)
+    gb, lb = b.pick(origins, dirs)
+    assert np.array_equal(ga, gb) and np.array_equal(la, lb) and (ga >= 0).sum() > 40
+    for lo, hi in [((-12, -2, 0), (-8, 2, 3)), ((-1, -1, 0), (1, 1, 5)), ((-30, -30, -2), (30, 30, 10))]:
+        assert np.array_equal(a.collect_aabb(lo, hi), b.collect_aabb(lo, hi))

@@ -27,7 +27,8 @@ def test_gpu_reproduces_pinned_digests(pkg, gpu, name):
     assert w.digest() == scenes.PINNED_DIGESTS[name]
 
 
-@pytest.mark.parametrize("run", ["stack", "interleaved", "mixed", "hard_chain", "pyramid420", "pile", "lattice"])
+@pytest.mark.parametrize("run", ["stack", "interleaved", "mixed", "hard_chain", "pyramid420", "pile", "lattice",
+                                 "shape_mix"])
 def test_gpu_matches_reference_every_step(pkg, gpu, golden, run):
     scenes = pkg.scenes
     rec = golden["runs"][run]

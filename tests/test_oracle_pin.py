@@ -115,3 +115,28 @@ def test_oracle_rejects_unrestated_options(pkg, oracle):
     with pytest.raises(pkg.capi.AvbdError) as e:
         pkg.capi.World(oracle, p)
     assert e.value.code == pkg.capi.ERR_UNSUPPORTED
+
+
+def _query_rays(n=64, seed=4):
+    rng = np.random.default_rng(seed)
+    origins = rng.uniform([-15, -6, 1], [15, 6, 8], (n, 3)).astype(np.float32)
+    targets = rng.uniform([-15, -3, -1], [15, 3, 2], (n, 3)).astype(np.float32)
+    return origins, targets - origins
+
+
+def test_oracle_queries_match_reference(pkg, oracle, ref):
+    """Solver::pick and collectAABB over boxes, spheres and cylinders, after 40 steps."""
+    scenes = pkg.scenes
+    sc = scenes.shape_mix()
+    a = scenes.instantiate(oracle, sc)
+    b = scenes.instantiate(ref, sc)
+    a.step(40)
+    b.step(40)
+    origins, dirs = _query_rays()
+    ba, la = a.pick(origins, dirs)
+    bb, lb = b.pick(origins, dirs)
+    assert np.array_equal(ba, bb) and np.array_equal(la, lb) and (ba >= 0).sum() > 10
+    for lo, hi in [((-12, -2, 0), (-8, 2, 3)), ((-1, -1, 0), (1, 1, 5)), ((-30, -30, -2), (30, 30, 10))]:
+        assert np.array_equal(a.collect_aabb(lo, hi), b.collect_aabb(lo, hi))
+    box = ((-30, -30, -2), (30, 30, 10))
+    assert np.array_equal(a.collect_aabb(*box, mask=2), b.collect_aabb(*box, mask=2))
