@@ -72,3 +72,17 @@ def test_scene_generators_are_deterministic(pkg):
     assert lat.n == 33
     full = s.pile()
     assert full.dynamic == 1653 + 32 and len(full.joints) == 32
+
+
+def test_cpp_facade_compiles(tmp_path):
+    """The C++ facade (include/avbdg_solver.hpp) and a host program written against it compile
+    (linking and running need the GPU library and a device: tests/test_gpu_facade.py)."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", "-ffp-contract=off",
+                    "-I" + os.path.join(ROOT, "include"), "-c", os.path.join(ROOT, "tests", "cpp", "facade_scenes.cpp"),
+                    "-o", str(tmp_path / "facade.o")], check=True)
