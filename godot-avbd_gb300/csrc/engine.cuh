@@ -116,9 +116,9 @@ struct Dev {
     ManifoldBuf live, stage;
     int *mActive;           // then exclusive rank
     float4 *stamps;
-    uint8_t *mSpec, *mDone; // brake
+    uint8_t *mSpec, *mDone; // brake: candidate flag per manifold, done flag per candidate
     int *specList;
-    int2 *specPred;         // brake: preceding candidate on each movable body (-1 = none)
+    int2 *specPred;         // brake: candidate index of the preceding candidate on each movable body (-1 = none)
     float4 *projLin, *projAng; // projection contributions per (manifold, side)
     float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)
     // forces (creation order; list order is descending index)

@@ -275,23 +275,31 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     d.mActive[i] = n > 0 ? 1 : 0;
 }
 
+// One thread per contact slot (8 per candidate), so the copies of the contact arrays coalesce; the
+// slot-0 thread also moves the manifold's own record. Grid-stride over the candidates.
 __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.ctr[C_CAND] || !flags[i])
-        return;
+    const long long slots = static_cast<long long>(d.ctr[C_CAND]) * kMaxContacts;
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
     const ManifoldBuf L = d.live;
     const ManifoldBuf S = d.stage;
-    const int r = rank[i];
-    L.ab[r] = S.ab[i];
-    L.b0[r] = S.b0[i];
-    L.b1[r] = S.b1[i];
-    L.b2[r] = S.b2[i];
-    const int n = S.count[i];
-    const int2 dorm = S.dormant[i];
-    L.count[r] = n;
-    L.dormant[r] = dorm;
-    const int kept = n > 0 ? n : dorm.y;
-    for (int c = 0; c < kept; c++) {
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < slots; t += stride) {
+        const int i = static_cast<int>(t / kMaxContacts), c = static_cast<int>(t % kMaxContacts);
+        if (!flags[i])
+            continue;
+        const int r = rank[i];
+        const int n = S.count[i];
+        const int2 dorm = S.dormant[i];
+        if (c == 0) {
+            L.ab[r] = S.ab[i];
+            L.b0[r] = S.b0[i];
+            L.b1[r] = S.b1[i];
+            L.b2[r] = S.b2[i];
+            L.count[r] = n;
+            L.dormant[r] = dorm;
+        }
+        const int kept = n > 0 ? n : dorm.y; // a parked manifold keeps its saved contacts
+        if (c >= kept)
+            continue;
         const int si = i * kMaxContacts + c, di = r * kMaxContacts + c;
         L.key[di] = S.key[si];
         L.rA[di] = S.rA[si];
@@ -437,7 +445,10 @@ void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block
 
 void launchManifoldCompact(const Dev &d, cudaStream_t s) {
     scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_CAND, d.ctr + C_LIVE, d.scanScratch, s);
-    ++launchCount(); manifoldCompactKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
+    ++launchCount();
+    const int blocks = residentGrid(reinterpret_cast<const void *>(manifoldCompactKernel), kThreads, 0,
+                                    divUp(d.MM * kMaxContacts, kThreads));
+    manifoldCompactKernel<<<blocks, kThreads, 0, s>>>(d, d.mActive, d.pairValid);
 }
 
 void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s) {

@@ -8,9 +8,10 @@
 // every thread takes candidates in increasing live order, waits until the (at most two)
 // predecessors have published their velocities, brakes, then publishes its own. Candidates on
 // disjoint bodies proceed in parallel and every body sees its candidates in live order, so the
-// result equals the serial sweep. All threads are resident and the smallest unfinished candidate
-// can always run, so the waits end; each is still bounded and reports a timeout instead of
-// hanging.
+// result equals the serial sweep. The smallest unfinished candidate can always run, so the waits
+// end; each is still bounded and reports a timeout instead of hanging. All threads of the
+// cooperative launch are resident; everything a candidate reads but the velocities is loaded before
+// its wait, so a dependency hop costs only the flag and velocity round trips.
 //
 // Projection passes are Jacobi: per-manifold patch corrections, then per-body sums in live order
 // (the adjacency order), averaged over the manifold count, with the per-world early exit.
@@ -90,7 +91,6 @@ __global__ void projActiveKernel(Dev d) {
         }
     }
     d.mSpec[m] = spec;
-    d.mDone[m] = spec ? 0 : 1;
     d.mActive[m] = spec;
 }
 
@@ -100,11 +100,13 @@ __global__ void specScatterKernel(Dev d, const int *flags, const int *rank) {
     if (m >= d.ctr[C_LIVE] || !flags[m])
         return;
     d.specList[rank[m]] = m;
+    d.mDone[rank[m]] = 0;
 }
 
-// For each candidate, the preceding candidate in live order on each of its movable bodies (-1 if
-// none), from the body's adjacency (forces first, then manifolds in live order).
-__global__ void brakePredKernel(Dev d) {
+// For each candidate, the preceding candidate on each of its movable bodies (-1 if none), as a
+// candidate index, from the body's adjacency (forces first, then manifolds in live order); `rank`
+// is the exclusive scan of the candidate flags.
+__global__ void brakePredKernel(Dev d, const int *rank) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= d.ctr[C_SPECN])
         return;
@@ -124,7 +126,7 @@ __global__ void brakePredKernel(Dev d) {
             if (o >= m)
                 break;
             if (d.mSpec[o])
-                pred[side] = o;
+                pred[side] = rank[o];
         }
     }
     d.specPred[k] = make_int2(pred[0], pred[1]);
@@ -140,73 +142,97 @@ __device__ __forceinline__ void storeRelease(uint8_t *p, unsigned v) {
     asm volatile("st.release.gpu.global.u8 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ bool published(const Dev &d, int m) { return m < 0 || loadAcquire(d.mDone + m) != 0; }
+__device__ __forceinline__ bool published(const Dev &d, int k) { return k < 0 || loadAcquire(d.mDone + k) != 0; }
 
-// One manifold of the brake sweep (solver_projection.cpp:98-166).
-__device__ void brakeManifold(const Dev &d, int m, float window) {
+// Everything one manifold's brake reads except the velocities: loaded before its wait, so a wait
+// is followed only by the velocity reads and the arithmetic.
+struct BrakeLoad {
+    int a, b, n, locksA, locksB;
+    bool moveA, moveB;
+    float invMassA, invMassB;
+    f3 nrm, IA, IB;
+    q4 qa, qb;
+    f3 rA[kMaxContacts], rB[kMaxContacts];
+    float gap[kMaxContacts];
+};
+
+__device__ __forceinline__ void brakeLoad(const Dev &d, int m, BrakeLoad &bl) {
     const ManifoldBuf L = d.live;
     const int2 ab = L.ab[m];
-    const int a = ab.x, b = ab.y;
-    const float4 xa4 = d.x[a], xb4 = d.x[b];
-    const bool moveA = movable(d, a), moveB = movable(d, b);
-    const float invMassA = moveA ? 1.0f / xa4.w : 0.0f;
-    const float invMassB = moveB ? 1.0f / xb4.w : 0.0f;
-    const f3 nrm = xyz(L.b0[m]);
-    const q4 qa = asq(d.q[a]), qb = asq(d.q[b]);
+    bl.a = ab.x;
+    bl.b = ab.y;
+    const float4 xa4 = d.x[ab.x], xb4 = d.x[ab.y];
+    bl.moveA = movable(d, ab.x);
+    bl.moveB = movable(d, ab.y);
+    bl.invMassA = bl.moveA ? 1.0f / xa4.w : 0.0f;
+    bl.invMassB = bl.moveB ? 1.0f / xb4.w : 0.0f;
+    bl.nrm = xyz(L.b0[m]);
+    bl.qa = asq(d.q[ab.x]);
+    bl.qb = asq(d.q[ab.y]);
+    bl.IA = xyz(d.moment[ab.x]);
+    bl.IB = xyz(d.moment[ab.y]);
+    bl.locksA = d.meta[ab.x].w;
+    bl.locksB = d.meta[ab.y].w;
     const f3 xa = xyz(xa4), xb = xyz(xb4);
-    const f3 va = xyz(__ldcg(&d.v[a])), wa = xyz(__ldcg(&d.w[a]));
-    const f3 vb = xyz(__ldcg(&d.v[b])), wb = xyz(__ldcg(&d.w[b]));
+    bl.n = L.count[m];
+#pragma unroll
+    for (int k = 0; k < kMaxContacts; k++) {
+        bl.gap[k] = 0.0f;
+        if (k < bl.n) {
+            const int ci = m * kMaxContacts + k;
+            bl.rA[k] = qrot(bl.qa, xyz(L.rA[ci]));
+            bl.rB[k] = qrot(bl.qb, xyz(L.rB[ci]));
+            bl.gap[k] = dot(bl.nrm, sub(add(xa, bl.rA[k]), add(xb, bl.rB[k])));
+        }
+    }
+}
+
+// One manifold of the brake sweep (solver_projection.cpp:98-166) on velocities held by the caller;
+// false when no contact braked (velocities untouched).
+__device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, float window, f3 &va, f3 &wa, f3 &vb, f3 &wb) {
     f3 patchRA{0, 0, 0}, patchRB{0, 0, 0};
     float velErr = 0.0f;
     int braked = 0;
-    const int n = L.count[m];
-    for (int k = 0; k < n; k++) {
-        const int ci = m * kMaxContacts + k;
-        const f3 rA = qrot(qa, xyz(L.rA[ci]));
-        const f3 rB = qrot(qb, xyz(L.rB[ci]));
-        const float gap = dot(nrm, sub(add(xa, rA), add(xb, rB)));
-        if (!(gap > 0.0f))
+#pragma unroll
+    for (int k = 0; k < kMaxContacts; k++) {
+        if (k >= bl.n || !(bl.gap[k] > 0.0f))
             continue;
-        const f3 vAp = add(va, cross(wa, rA));
-        const f3 vBp = add(vb, cross(wb, rB));
-        const float vn = dot(sub(vAp, vBp), nrm);
-        const float target = -gap / window;
+        const f3 vAp = add(va, cross(wa, bl.rA[k]));
+        const f3 vBp = add(vb, cross(wb, bl.rB[k]));
+        const float vn = dot(sub(vAp, vBp), bl.nrm);
+        const float target = -bl.gap[k] / window;
         if (vn < target) {
-            patchRA = add(patchRA, rA);
-            patchRB = add(patchRB, rB);
+            patchRA = add(patchRA, bl.rA[k]);
+            patchRB = add(patchRB, bl.rB[k]);
             velErr += target - vn;
             braked++;
         }
     }
     if (braked == 0)
-        return;
+        return false;
     const float invN = 1.0f / static_cast<float>(braked);
-    const f3 IA = xyz(d.moment[a]), IB = xyz(d.moment[b]);
-    const f3 tA = moveA ? qrot(qconj(qa), cross(scale(patchRA, invN), nrm)) : f3{0, 0, 0};
-    const f3 tB = moveB ? qrot(qconj(qb), cross(scale(patchRB, invN), nrm)) : f3{0, 0, 0};
-    const float K = invMassA + invMassB + (moveA ? angularCompliance(IA, tA) : 0.0f) +
-                    (moveB ? angularCompliance(IB, tB) : 0.0f);
+    const f3 tA = bl.moveA ? qrot(qconj(bl.qa), cross(scale(patchRA, invN), bl.nrm)) : f3{0, 0, 0};
+    const f3 tB = bl.moveB ? qrot(qconj(bl.qb), cross(scale(patchRB, invN), bl.nrm)) : f3{0, 0, 0};
+    const float K = bl.invMassA + bl.invMassB + (bl.moveA ? angularCompliance(bl.IA, tA) : 0.0f) +
+                    (bl.moveB ? angularCompliance(bl.IB, tB) : 0.0f);
     const float j = velErr * invN / K;
-    if (moveA) {
-        const int locks = d.meta[a].w;
-        f3 dv = scale(nrm, invMassA * j);
-        f3 dw = scale(angularResponse(IA, qa, tA), j);
-        maskLocked(locks & 0xff, dv);
-        maskLocked((locks >> 8) & 0xff, dw);
-        const float4 v4 = __ldcg(&d.v[a]);
-        __stcg(&d.v[a], f4(add(xyz(v4), dv), v4.w));
-        __stcg(&d.w[a], f4(add(wa, dw), 0.0f));
+    if (bl.moveA) {
+        f3 dv = scale(bl.nrm, bl.invMassA * j);
+        f3 dw = scale(angularResponse(bl.IA, bl.qa, tA), j);
+        maskLocked(bl.locksA & 0xff, dv);
+        maskLocked((bl.locksA >> 8) & 0xff, dw);
+        va = add(va, dv);
+        wa = add(wa, dw);
     }
-    if (moveB) {
-        const int locks = d.meta[b].w;
-        f3 dv = scale(nrm, invMassB * j);
-        f3 dw = scale(angularResponse(IB, qb, tB), j);
-        maskLocked(locks & 0xff, dv);
-        maskLocked((locks >> 8) & 0xff, dw);
-        const float4 v4 = __ldcg(&d.v[b]);
-        __stcg(&d.v[b], f4(sub(xyz(v4), dv), v4.w));
-        __stcg(&d.w[b], f4(sub(wb, dw), 0.0f));
+    if (bl.moveB) {
+        f3 dv = scale(bl.nrm, bl.invMassB * j);
+        f3 dw = scale(angularResponse(bl.IB, bl.qb, tB), j);
+        maskLocked(bl.locksB & 0xff, dv);
+        maskLocked((bl.locksB >> 8) & 0xff, dw);
+        vb = sub(vb, dv);
+        wb = sub(wb, dw);
     }
+    return true;
 }
 
 constexpr long long kBrakeSpinLimit = 4000000; // ~0.3 s of 64 ns sleeps per wait
@@ -217,6 +243,8 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
     volatile int *errors = d.ctr + C_ERRORS;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += stride) {
         const int2 pred = d.specPred[k];
+        BrakeLoad bl;
+        brakeLoad(d, d.specList[k], bl);
         long long spins = 0;
         while (!(published(d, pred.x) && published(d, pred.y))) {
             if (++spins > kBrakeSpinLimit || (*errors & kErrBrakeTimeout)) {
@@ -225,9 +253,19 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
             }
             __nanosleep(64);
         }
-        const int m = d.specList[k];
-        brakeManifold(d, m, window);
-        storeRelease(d.mDone + m, 1u); // orders this thread's velocity writes before the flag
+        const float4 va4 = __ldcg(&d.v[bl.a]), vb4 = __ldcg(&d.v[bl.b]);
+        f3 va = xyz(va4), wa = xyz(__ldcg(&d.w[bl.a])), vb = xyz(vb4), wb = xyz(__ldcg(&d.w[bl.b]));
+        if (brakeSolve(bl, window, va, wa, vb, wb)) {
+            if (bl.moveA) {
+                __stcg(&d.v[bl.a], f4(va, va4.w));
+                __stcg(&d.w[bl.a], f4(wa, 0.0f));
+            }
+            if (bl.moveB) {
+                __stcg(&d.v[bl.b], f4(vb, vb4.w));
+                __stcg(&d.w[bl.b], f4(wb, 0.0f));
+            }
+        }
+        storeRelease(d.mDone + k, 1u); // orders this thread's velocity writes before the flag
     }
 }
 
@@ -387,8 +425,9 @@ void launchProjActive(const Dev &d, cudaStream_t s) {
     ++launchCount(); specScatterKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
 }
 
+// Runs right after launchProjActive, whose scan left each candidate's rank in d.pairValid.
 void launchBrake(const Dev &d, float window, cudaStream_t s) {
-    ++launchCount(); brakePredKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); brakePredKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.pairValid);
     Dev dd = d;
     float win = window;
     void *args[] = {&dd, &win};

@@ -270,21 +270,37 @@ struct SharedAcc {
     f3 rhsLin;
 };
 
-__device__ __forceinline__ void stampContact(const float S[6], f3 r, f3 fw, SideAcc &acc) {
+// One contact's terms of one side's stamp: the unique entries of the angular block (h00, h01, h02,
+// h11, h12, h22), the cross block r x S and the angular right-hand side r x fw.
+struct SideTerms {
+    float h[6];
+    m3 rs;
+    f3 rc;
+};
+
+__device__ __forceinline__ SideTerms sideTerms(const float S[6], f3 r, f3 fw) {
     const float s00 = S[0], s01 = S[1], s02 = S[2], s11 = S[3], s12 = S[4], s22 = S[5];
     const m3 Sm = mcols(f3{s00, s01, s02}, f3{s01, s11, s12}, f3{s02, s12, s22});
-    const m3 RS = mcols(cross(r, Sm.c0), cross(r, Sm.c1), cross(r, Sm.c2));
+    SideTerms t;
+    t.rs = mcols(cross(r, Sm.c0), cross(r, Sm.c1), cross(r, Sm.c2));
     const float rx2 = r.x * r.x, ry2 = r.y * r.y, rz2 = r.z * r.z;
     const float rxy = r.x * r.y, rxz = r.x * r.z, ryz = r.y * r.z;
-    const float h00 = s11 * rz2 - 2.0f * s12 * ryz + s22 * ry2;
-    const float h11 = s22 * rx2 - 2.0f * s02 * rxz + s00 * rz2;
-    const float h22 = s00 * ry2 - 2.0f * s01 * rxy + s11 * rx2;
-    const float h01 = s12 * rxz + s02 * ryz - s22 * rxy - s01 * rz2;
-    const float h02 = s12 * rxy + s01 * ryz - s11 * rxz - s02 * ry2;
-    const float h12 = s02 * rxy + s01 * rxz - s00 * ryz - s12 * rx2;
-    acc.ang = madd(acc.ang, mcols(f3{h00, h01, h02}, f3{h01, h11, h12}, f3{h02, h12, h22}));
-    acc.crs = madd(acc.crs, RS);
-    acc.rhsAng = add(acc.rhsAng, cross(r, fw));
+    t.h[0] = s11 * rz2 - 2.0f * s12 * ryz + s22 * ry2;
+    t.h[1] = s12 * rxz + s02 * ryz - s22 * rxy - s01 * rz2;
+    t.h[2] = s12 * rxy + s01 * ryz - s11 * rxz - s02 * ry2;
+    t.h[3] = s22 * rx2 - 2.0f * s02 * rxz + s00 * rz2;
+    t.h[4] = s02 * rxy + s01 * rxz - s00 * ryz - s12 * rx2;
+    t.h[5] = s00 * ry2 - 2.0f * s01 * rxy + s11 * rx2;
+    t.rc = cross(r, fw);
+    return t;
+}
+
+__device__ __forceinline__ void stampContact(const float S[6], f3 r, f3 fw, SideAcc &acc) {
+    const SideTerms t = sideTerms(S, r, fw);
+    const float *h = t.h;
+    acc.ang = madd(acc.ang, mcols(f3{h[0], h[1], h[2]}, f3{h[1], h[3], h[4]}, f3{h[2], h[4], h[5]}));
+    acc.crs = madd(acc.crs, t.rs);
+    acc.rhsAng = add(acc.rhsAng, t.rc);
 }
 
 __device__ __forceinline__ void stampShared(const float S[6], f3 fw, SharedAcc &acc) {
@@ -296,19 +312,6 @@ __device__ __forceinline__ void zeroAcc(SideAcc &a) {
     a.ang = mzero();
     a.crs = mzero();
     a.rhsAng = f3{0, 0, 0};
-}
-
-// Stamp record: lin (6 unique), rhsLin (signed), ang (6 unique), rhsAng (signed), cross (9).
-__device__ __forceinline__ void storeStamp(float4 *dst, const SharedAcc &sh, const SideAcc &sd, float side) {
-    const f3 rl = scale(sh.rhsLin, side);
-    const f3 ra = scale(sd.rhsAng, side);
-    dst[0] = make_float4(sh.lin.c0.x, sh.lin.c0.y, sh.lin.c0.z, sh.lin.c1.y);
-    dst[1] = make_float4(sh.lin.c1.z, sh.lin.c2.z, rl.x, rl.y);
-    dst[2] = make_float4(rl.z, sd.ang.c0.x, sd.ang.c0.y, sd.ang.c0.z);
-    dst[3] = make_float4(sd.ang.c1.y, sd.ang.c1.z, sd.ang.c2.z, ra.x);
-    dst[4] = make_float4(ra.y, ra.z, sd.crs.c0.x, sd.crs.c0.y);
-    dst[5] = make_float4(sd.crs.c0.z, sd.crs.c1.x, sd.crs.c1.y, sd.crs.c1.z);
-    dst[6] = make_float4(sd.crs.c2.x, sd.crs.c2.y, sd.crs.c2.z, 0.0f);
 }
 
 // block += stamp (full 3x3 adds, as the reference adds its accumulators).
@@ -349,6 +352,29 @@ __device__ __forceinline__ f3 contactError(const StepParams &p, f3 C0, f3 bracke
 
 enum : int { kSideA = 1, kSideB = 2 };
 
+// Which sides of manifold m take stamps for the block-Jacobi solve, and whether a coloured body
+// touches it.
+__device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touchesColour) {
+    const bool dynA = inUpdate(d, ab.x), dynB = inUpdate(d, ab.y);
+    const uint8_t ca = dynA ? d.colour[ab.x] : kUncoloured;
+    const uint8_t cb = dynB ? d.colour[ab.y] : kUncoloured;
+    touchesColour = (dynA && ca < kOverflowColour) || (dynB && cb < kOverflowColour);
+    return ((dynA && ca == kOverflowColour) ? kSideA : 0) | ((dynB && cb == kOverflowColour) ? kSideB : 0);
+}
+
+// Stamp record: lin (6 unique), rhsLin (signed), ang (6 unique), rhsAng (signed), cross (9).
+__device__ __forceinline__ void storeStamp(float4 *dst, const SharedAcc &sh, const SideAcc &sd, float side) {
+    const f3 rl = scale(sh.rhsLin, side);
+    const f3 ra = scale(sd.rhsAng, side);
+    dst[0] = make_float4(sh.lin.c0.x, sh.lin.c0.y, sh.lin.c0.z, sh.lin.c1.y);
+    dst[1] = make_float4(sh.lin.c1.z, sh.lin.c2.z, rl.x, rl.y);
+    dst[2] = make_float4(rl.z, sd.ang.c0.x, sd.ang.c0.y, sd.ang.c0.z);
+    dst[3] = make_float4(sd.ang.c1.y, sd.ang.c1.z, sd.ang.c2.z, ra.x);
+    dst[4] = make_float4(ra.y, ra.z, sd.crs.c0.x, sd.crs.c0.y);
+    dst[5] = make_float4(sd.crs.c0.z, sd.crs.c1.x, sd.crs.c1.y, sd.crs.c1.z);
+    dst[6] = make_float4(sd.crs.c2.x, sd.crs.c2.y, sd.crs.c2.z, 0.0f);
+}
+
 // Stamps of manifold m for the requested sides, from the current poses and penalties.
 __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int sides) {
     const ManifoldBuf L = d.live;
@@ -388,16 +414,6 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
         storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
 }
 
-// Which sides of manifold m take stamps for the block-Jacobi solve, and whether a coloured body
-// touches it.
-__device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touchesColour) {
-    const bool dynA = inUpdate(d, ab.x), dynB = inUpdate(d, ab.y);
-    const uint8_t ca = dynA ? d.colour[ab.x] : kUncoloured;
-    const uint8_t cb = dynB ? d.colour[ab.y] : kUncoloured;
-    touchesColour = (dynA && ca < kOverflowColour) || (dynB && cb < kOverflowColour);
-    return ((dynA && ca == kOverflowColour) ? kSideA : 0) | ((dynB && cb == kOverflowColour) ? kSideB : 0);
-}
-
 __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= d.ctr[C_LIVE])
@@ -409,72 +425,75 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
     computeStamps(d, p, m, sides);
 }
 
-// Dual pass (ManifoldStore::updateDual) and, optionally, the next round's stamps.
-__global__ void dualKernel(Dev d, StepParams p, int stamps, float decay) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= d.ctr[C_LIVE])
-        return;
+// Dual pass (ManifoldStore::updateDual, manifold.cpp:583-671) and, with STAMPS, the next round's
+// stamps (the reference's phase-A recompute of each force, manifold.cpp:655-659, from the same
+// floats). One thread per manifold, grid-stride over the live ones.
+template <bool STAMPS>
+__global__ void dualKernel(Dev d, StepParams p, float decay) {
+    const int live = d.ctr[C_LIVE];
     const ManifoldBuf L = d.live;
-    const int2 ab = L.ab[m];
-    if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
-        return; // frozen (manifold.cpp:168-172)
-    bool touches = false;
-    int sides = stamps ? overflowSides(d, ab, touches) : 0;
-    if (touches)
-        sides = 0; // recomputed after the colour passes
-    const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
-    const float4 b04 = L.b0[m];
-    const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
-    const float mu = b04.w;
-    const int n = L.count[m];
-    SharedAcc sh;
-    sh.lin = mzero();
-    sh.rhsLin = f3{0, 0, 0};
-    SideAcc sa, sb;
-    zeroAcc(sa);
-    zeroAcc(sb);
-    for (int c = 0; c < n; c++) {
-        const int ci = m * kMaxContacts + c;
-        const float4 rA4 = L.rA[ci];
-        const f3 rAw = mul(A.rot, xyz(rA4));
-        const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
-        const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
-        const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
-        f3 k = xyz(L.k[ci]);
-        if (decay < 1.0f)
-            k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
-        const float4 lam4 = L.lam[ci];
-        float stick = lam4.w;
-        f3 F = add(cmul(k, C), xyz(lam4));
-        const Cone cone = clampForce(F, mu);
-        const f3 lam = F;
-        const float beta = p.betaLin * rA4.w;
-        if (F.x < 0)
-            k.x = smin(k.x + beta * fabsf(C.x), PENALTY_MAX);
-        if (cone.scale <= cone.bounds) {
-            k.y = smin(k.y + beta * fabsf(C.y), PENALTY_MAX);
-            k.z = smin(k.z + beta * fabsf(C.z), PENALTY_MAX);
-            stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x) {
+        const int2 ab = L.ab[m];
+        if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
+            continue; // frozen (manifold.cpp:168-172)
+        bool touches = false;
+        int sides = STAMPS ? overflowSides(d, ab, touches) : 0;
+        if (touches)
+            sides = 0; // recomputed after the colour passes
+        const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
+        const float4 b04 = L.b0[m];
+        const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+        const float mu = b04.w;
+        const int n = L.count[m];
+        SharedAcc sh;
+        sh.lin = mzero();
+        sh.rhsLin = f3{0, 0, 0};
+        SideAcc sa, sb;
+        zeroAcc(sa);
+        zeroAcc(sb);
+        for (int c = 0; c < n; c++) {
+            const int ci = m * kMaxContacts + c;
+            const float4 rA4 = L.rA[ci];
+            const f3 rAw = mul(A.rot, xyz(rA4));
+            const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+            const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+            const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
+            f3 k = xyz(L.k[ci]);
+            if (decay < 1.0f)
+                k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
+            const float4 lam4 = L.lam[ci];
+            float stick = lam4.w;
+            f3 F = add(cmul(k, C), xyz(lam4));
+            const Cone cone = clampForce(F, mu);
+            const f3 lam = F;
+            const float beta = p.betaLin * rA4.w;
+            if (F.x < 0)
+                k.x = smin(k.x + beta * fabsf(C.x), PENALTY_MAX);
+            if (cone.scale <= cone.bounds) {
+                k.y = smin(k.y + beta * fabsf(C.y), PENALTY_MAX);
+                k.z = smin(k.z + beta * fabsf(C.z), PENALTY_MAX);
+                stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
+            }
+            L.k[ci] = f4(k, 0.0f);
+            L.lam[ci] = f4(lam, stick);
+            if (STAMPS && sides) {
+                f3 Fn = add(cmul(k, C), lam);
+                clampForce(Fn, mu);
+                float S[6];
+                basisHessianD(r0, r1, r2, k, S);
+                const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
+                stampShared(S, fw, sh);
+                if (sides & kSideA)
+                    stampContact(S, rAw, fw, sa);
+                if (sides & kSideB)
+                    stampContact(S, rBw, fw, sb);
+            }
         }
-        L.k[ci] = f4(k, 0.0f);
-        L.lam[ci] = f4(lam, stick);
-        if (sides) {
-            f3 Fn = add(cmul(k, C), lam);
-            clampForce(Fn, mu);
-            float S[6];
-            basisHessianD(r0, r1, r2, k, S);
-            const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
-            stampShared(S, fw, sh);
-            if (sides & kSideA)
-                stampContact(S, rAw, fw, sa);
-            if (sides & kSideB)
-                stampContact(S, rBw, fw, sb);
-        }
+        if (sides & kSideA)
+            storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
+        if (sides & kSideB)
+            storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
     }
-    if (sides & kSideA)
-        storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
-    if (sides & kSideB)
-        storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
 }
 
 // ---- joints (joint.cpp:80-230) ----
@@ -629,7 +648,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
         const int m = seq - nf;
         const int side = d.live.ab[m].x == g ? 0 : 1;
         if (RECOMPUTE) {
-            // Same floats as computeStamps for one side, summed straight into the block.
+            // Same floats as stampsKernel for one side, summed straight into the block.
             const ManifoldBuf L = d.live;
             const int2 ab = L.ab[m];
             const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
@@ -1024,7 +1043,15 @@ void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {
 }
 
 void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, int block, cudaStream_t s) {
-    ++launchCount(); dualKernel<<<divUp(d.MM, block), block, 0, s>>>(d, p, stamps ? 1 : 0, decay);
+    const int want = divUp(d.MM, block);
+    ++launchCount();
+    if (stamps) {
+        const void *fn = reinterpret_cast<const void *>(dualKernel<true>);
+        dualKernel<true><<<residentGrid(fn, block, 0, want), block, 0, s>>>(d, p, decay);
+    } else {
+        const void *fn = reinterpret_cast<const void *>(dualKernel<false>);
+        dualKernel<false><<<residentGrid(fn, block, 0, want), block, 0, s>>>(d, p, decay);
+    }
 }
 
 void launchForceDual(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {

@@ -2,6 +2,9 @@
 
 #include "prims.cuh"
 
+#include <mutex>
+#include <vector>
+
 namespace avbdg {
 
 namespace {
@@ -378,6 +381,35 @@ static bool g_smemConfigured = false;
 static void configureSmem();
 
 void preparePrimitives() { configureSmem(); }
+
+int residentGrid(const void *kernel, int block, size_t smem, int want) {
+    struct Entry {
+        int device;
+        const void *kernel;
+        int block;
+        size_t smem;
+        int blocks;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int blocks = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        for (const Entry &e : cache)
+            if (e.device == dev && e.kernel == kernel && e.block == block && e.smem == smem)
+                blocks = e.blocks;
+        if (blocks == 0) {
+            int sms = 0, perSm = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, block, smem);
+            blocks = (sms > 0 ? sms : 1) * (perSm > 0 ? perSm : 1);
+            cache.push_back(Entry{dev, kernel, block, smem, blocks});
+        }
+    }
+    return want < 1 ? 1 : (want < blocks ? want : blocks);
+}
 
 static void configureSmem() {
     if (g_smemConfigured)

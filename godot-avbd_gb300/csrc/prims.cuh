@@ -35,6 +35,11 @@ void segmentedSortU64(uint64_t *data, uint64_t *tmp, const int *start, int segCa
 
 inline int divUp(int a, int b) { return (a + b - 1) / b; }
 
+// Blocks of `block` threads (and `smem` dynamic shared bytes) of `kernel` that are resident on the
+// current device at once, capped at `want` (at least 1). Grid-stride kernels over a capacity use it so
+// that a mostly empty capacity costs no blocks. Cached per (device, kernel, block, smem).
+int residentGrid(const void *kernel, int block, size_t smem, int want);
+
 // Kernel attributes the primitives need (large dynamic shared memory); call before any capture.
 void preparePrimitives();
 
