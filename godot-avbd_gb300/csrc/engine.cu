@@ -280,11 +280,15 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         cp(t.b2, s.b2, mCopy * sizeof(float4));
         cp(t.count, s.count, mCopy * sizeof(int));
         cp(t.dormant, s.dormant, mCopy * sizeof(int2));
-        const size_t cCopy = mCopy * kMaxContacts;
-        cp(t.key, s.key, cCopy * sizeof(int));
-        for (auto pr : {std::make_pair(t.rA, s.rA), std::make_pair(t.rB, s.rB), std::make_pair(t.C0, s.C0),
-                        std::make_pair(t.k, s.k), std::make_pair(t.lam, s.lam)})
-            cp(pr.first, pr.second, cCopy * sizeof(float4));
+        // Contact arrays are slot-major: slot c of the old store (old.MM entries apart) to slot c of
+        // the new one (mm apart).
+        for (int c = 0; c < kMaxContacts; c++) {
+            const size_t so = static_cast<size_t>(c) * old.MM, sn = static_cast<size_t>(c) * mm;
+            cp(t.key + sn, s.key + so, mCopy * sizeof(int));
+            for (auto pr : {std::make_pair(t.rA, s.rA), std::make_pair(t.rB, s.rB), std::make_pair(t.C0, s.C0),
+                            std::make_pair(t.k, s.k), std::make_pair(t.lam, s.lam)})
+                cp(pr.first + sn, pr.second + so, mCopy * sizeof(float4));
+        }
         const size_t fCopy = static_cast<size_t>(std::min(old.FF, ff));
         cp(n.fAB, old.fAB, fCopy * sizeof(int2));
         for (auto pr : {std::make_pair(n.fRA, old.fRA), std::make_pair(n.fRB, old.fRB), std::make_pair(n.fC0L, old.fC0L),
@@ -1465,13 +1469,23 @@ int Engine::dumpManifolds(int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_
     std::vector<float4> C(static_cast<size_t>(k) * kMaxContacts), K(C.size()), Lm(C.size());
     cudaMemcpy(ab.data(), d.live.ab, sizeof(int2) * k, cudaMemcpyDeviceToHost);
     cudaMemcpy(cnt.data(), d.live.count, sizeof(int) * k, cudaMemcpyDeviceToHost);
-    cudaMemcpy(keys.data(), d.live.key, sizeof(int) * keys.size(), cudaMemcpyDeviceToHost);
     cudaMemcpy(b0.data(), d.live.b0, sizeof(float4) * k, cudaMemcpyDeviceToHost);
     cudaMemcpy(b1.data(), d.live.b1, sizeof(float4) * k, cudaMemcpyDeviceToHost);
     cudaMemcpy(b2.data(), d.live.b2, sizeof(float4) * k, cudaMemcpyDeviceToHost);
-    cudaMemcpy(C.data(), d.live.C0, sizeof(float4) * C.size(), cudaMemcpyDeviceToHost);
-    cudaMemcpy(K.data(), d.live.k, sizeof(float4) * C.size(), cudaMemcpyDeviceToHost);
-    cudaMemcpy(Lm.data(), d.live.lam, sizeof(float4) * C.size(), cudaMemcpyDeviceToHost);
+    // Slot-major on the device; manifold-major (8 slots per manifold) here.
+    const auto gather = [&](auto *dst, const auto *src) {
+        using T = std::remove_const_t<std::remove_reference_t<decltype(*src)>>;
+        std::vector<T> slot(static_cast<size_t>(k));
+        for (int j = 0; j < kMaxContacts; j++) {
+            cudaMemcpy(slot.data(), src + static_cast<size_t>(j) * d.MM, sizeof(T) * slot.size(), cudaMemcpyDeviceToHost);
+            for (int i = 0; i < k; i++)
+                dst[static_cast<size_t>(i) * kMaxContacts + j] = slot[static_cast<size_t>(i)];
+        }
+    };
+    gather(keys.data(), d.live.key);
+    gather(C.data(), d.live.C0);
+    gather(K.data(), d.live.k);
+    gather(Lm.data(), d.live.lam);
     const int base = wBase.empty() ? 0 : wBase[0];
     for (int i = 0; i < k; i++) {
         if (ba)

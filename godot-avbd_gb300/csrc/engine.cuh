@@ -148,6 +148,9 @@ struct Dev {
 // ---- device helpers shared by the kernel files ----
 
 __device__ __forceinline__ int bodyWorld(const Dev &d, int g) { return d.meta[g].x; }
+// Contact slot c of manifold m. The contact arrays are slot-major (MM entries per slot), so a warp
+// reading slot c of 32 consecutive manifolds reads 512 contiguous bytes.
+AVBD_HD int cslot(const Dev &d, int m, int c) { return c * d.MM + m; }
 // List position of body g: the world's bodies in list order (reverse creation) occupy
 // [wBase, wBase + wCount).
 __device__ __forceinline__ int listPos(const Dev &d, int g) {

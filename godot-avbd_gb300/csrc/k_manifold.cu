@@ -110,7 +110,6 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     const bool awakeA = dynA && d.sleep[a].x == 0, awakeB = dynB && d.sleep[b].x == 0;
     int oldN = L.count[i];
     const int2 dorm = L.dormant[i];
-    const int base = i * kMaxContacts;
     S.ab[i] = ab;
     if (!awakeA && !awakeB) {
         // Frozen: every input is parked, the state is kept verbatim.
@@ -121,12 +120,12 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
         S.dormant[i] = dorm;
         const int kept = oldN > 0 ? oldN : dorm.y; // a parked manifold keeps its saved contacts
         for (int k = 0; k < kept; k++) {
-            S.key[base + k] = L.key[base + k];
-            S.rA[base + k] = L.rA[base + k];
-            S.rB[base + k] = L.rB[base + k];
-            S.C0[base + k] = L.C0[base + k];
-            S.k[base + k] = L.k[base + k];
-            S.lam[base + k] = L.lam[base + k];
+            S.key[cslot(d, i, k)] = L.key[cslot(d, i, k)];
+            S.rA[cslot(d, i, k)] = L.rA[cslot(d, i, k)];
+            S.rB[cslot(d, i, k)] = L.rB[cslot(d, i, k)];
+            S.C0[cslot(d, i, k)] = L.C0[cslot(d, i, k)];
+            S.k[cslot(d, i, k)] = L.k[cslot(d, i, k)];
+            S.lam[cslot(d, i, k)] = L.lam[cslot(d, i, k)];
         }
         d.mActive[i] = 1;
         return;
@@ -173,15 +172,15 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     }
     for (int c = 0; c < n; c++) {
         for (int j = 0; j < oldN; j++) {
-            if (nc[c].key != L.key[base + j])
+            if (nc[c].key != L.key[cslot(d, i, j)])
                 continue;
             const f3 newRA = nc[c].rA, newRB = nc[c].rB;
-            const float4 oRA = L.rA[base + j], oRB = L.rB[base + j];
-            const float4 oLam = L.lam[base + j];
+            const float4 oRA = L.rA[cslot(d, i, j)], oRB = L.rB[cslot(d, i, j)];
+            const float4 oLam = L.lam[cslot(d, i, j)];
             nc[c].rA = xyz(oRA);
             nc[c].rB = xyz(oRB);
-            prevErr[c] = smax(0.0f, COLLISION_MARGIN - L.C0[base + j].x);
-            newK[c] = xyz(L.k[base + j]);
+            prevErr[c] = smax(0.0f, COLLISION_MARGIN - L.C0[cslot(d, i, j)].x);
+            newK[c] = xyz(L.k[cslot(d, i, j)]);
             newLam[c] = xyz(oLam);
             const int oldStick = oLam.w != 0.0f;
             newStick[c] = oldStick;
@@ -219,12 +218,12 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
         // saved contacts keep their state except force and stick.
         if (p.graceTicks > 0 && dorm.x < p.graceTicks) {
             for (int j = 0; j < oldN; j++) {
-                S.key[base + j] = L.key[base + j];
-                S.rA[base + j] = L.rA[base + j];
-                S.rB[base + j] = L.rB[base + j];
-                S.C0[base + j] = L.C0[base + j];
-                S.k[base + j] = L.k[base + j];
-                S.lam[base + j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                S.key[cslot(d, i, j)] = L.key[cslot(d, i, j)];
+                S.rA[cslot(d, i, j)] = L.rA[cslot(d, i, j)];
+                S.rB[cslot(d, i, j)] = L.rB[cslot(d, i, j)];
+                S.C0[cslot(d, i, j)] = L.C0[cslot(d, i, j)];
+                S.k[cslot(d, i, j)] = L.k[cslot(d, i, j)];
+                S.lam[cslot(d, i, j)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             }
             S.dormant[i] = make_int2(dorm.x + 1, oldN);
             d.mActive[i] = 1;
@@ -265,25 +264,26 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
         }
         lam = scale(scale(lam, p.alpha), p.gamma);
         const f3 k = lclampv(scale(newK[c], p.gamma), PENALTY_MIN, PENALTY_MAX);
-        S.key[base + c] = nc[c].key;
-        S.rA[base + c] = f4(rA, beta);
-        S.rB[base + c] = f4(rB, 0.0f);
-        S.C0[base + c] = f4(C0, 0.0f);
-        S.k[base + c] = f4(k, 0.0f);
-        S.lam[base + c] = f4(lam, stick ? 1.0f : 0.0f);
+        S.key[cslot(d, i, c)] = nc[c].key;
+        S.rA[cslot(d, i, c)] = f4(rA, beta);
+        S.rB[cslot(d, i, c)] = f4(rB, 0.0f);
+        S.C0[cslot(d, i, c)] = f4(C0, 0.0f);
+        S.k[cslot(d, i, c)] = f4(k, 0.0f);
+        S.lam[cslot(d, i, c)] = f4(lam, stick ? 1.0f : 0.0f);
     }
     d.mActive[i] = n > 0 ? 1 : 0;
 }
 
-// One thread per contact slot (8 per candidate), so the copies of the contact arrays coalesce; the
-// slot-0 thread also moves the manifold's own record. Grid-stride over the candidates.
+// One thread per contact slot (8 per candidate, slot-major like the arrays), so the copies of the
+// contact arrays coalesce; the slot-0 thread also moves the manifold's own record. Grid-stride.
 __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
-    const long long slots = static_cast<long long>(d.ctr[C_CAND]) * kMaxContacts;
+    const int cand = d.ctr[C_CAND];
+    const long long slots = static_cast<long long>(cand) * kMaxContacts;
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
     const ManifoldBuf L = d.live;
     const ManifoldBuf S = d.stage;
     for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < slots; t += stride) {
-        const int i = static_cast<int>(t / kMaxContacts), c = static_cast<int>(t % kMaxContacts);
+        const int c = static_cast<int>(t / cand), i = static_cast<int>(t % cand);
         if (!flags[i])
             continue;
         const int r = rank[i];
@@ -300,7 +300,7 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
         const int kept = n > 0 ? n : dorm.y; // a parked manifold keeps its saved contacts
         if (c >= kept)
             continue;
-        const int si = i * kMaxContacts + c, di = r * kMaxContacts + c;
+        const int si = cslot(d, i, c), di = cslot(d, r, c);
         L.key[di] = S.key[si];
         L.rA[di] = S.rA[si];
         L.rB[di] = S.rB[si];
@@ -322,7 +322,7 @@ __global__ void rebaseKernel(Dev d, StepParams p) {
     const f3 r0 = xyz(L.b0[m]), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
     const int n = L.count[m];
     for (int c = 0; c < n; c++) {
-        const int ci = m * kMaxContacts + c;
+        const int ci = cslot(d, m, c);
         const f3 pA = add(xa, qrot(qa, xyz(L.rA[ci])));
         const f3 pB = add(xb, qrot(qb, xyz(L.rB[ci])));
         f3 C0 = add(basisMul(r0, r1, r2, sub(pA, pB)), f3{COLLISION_MARGIN, 0, 0});

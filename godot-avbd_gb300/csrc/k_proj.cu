@@ -80,7 +80,7 @@ __global__ void projActiveKernel(Dev d) {
         const f3 xa = xyz(d.x[ab.x]), xb = xyz(d.x[ab.y]);
         const q4 qa = asq(d.q[ab.x]), qb = asq(d.q[ab.y]);
         for (int k = 0; k < n; k++) {
-            const int ci = m * kMaxContacts + k;
+            const int ci = cslot(d, m, k);
             const f3 rA = qrot(qa, xyz(L.rA[ci]));
             const f3 rB = qrot(qb, xyz(L.rB[ci]));
             const float gap = dot(nrm, sub(add(xa, rA), add(xb, rB)));
@@ -179,7 +179,7 @@ __device__ __forceinline__ void brakeLoad(const Dev &d, int m, BrakeLoad &bl) {
     for (int k = 0; k < kMaxContacts; k++) {
         bl.gap[k] = 0.0f;
         if (k < bl.n) {
-            const int ci = m * kMaxContacts + k;
+            const int ci = cslot(d, m, k);
             bl.rA[k] = qrot(bl.qa, xyz(L.rA[ci]));
             bl.rB[k] = qrot(bl.qb, xyz(L.rB[ci]));
             bl.gap[k] = dot(bl.nrm, sub(add(xa, bl.rA[k]), add(xb, bl.rB[k])));
@@ -298,7 +298,7 @@ __global__ void projManifoldKernel(Dev d, StepParams p) {
     float patchDepth = 0.0f;
     int corrected = 0;
     for (int k = 0; k < n; k++) {
-        const int ci = m * kMaxContacts + k;
+        const int ci = cslot(d, m, k);
         const f3 rA = mul(rotA, xyz(L.rA[ci]));
         const f3 rB = mul(rotB, xyz(L.rB[ci]));
         const float rawDepth = -dot(nrm, sub(add(xa, rA), add(xb, rB)));

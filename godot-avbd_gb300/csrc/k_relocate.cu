@@ -73,7 +73,7 @@ __global__ void manifoldRelocateKernel(Dev d, const int *slotMap) {
     S.dormant[m] = dorm;
     const int kept = cnt > 0 ? cnt : dorm.y;
     for (int c = 0; c < kept; c++) {
-        const int i = m * kMaxContacts + c;
+        const int i = cslot(d, m, c);
         S.key[i] = L.key[i];
         S.rA[i] = L.rA[i];
         S.rB[i] = L.rB[i];

@@ -391,7 +391,7 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
     zeroAcc(sa);
     zeroAcc(sb);
     for (int c = 0; c < n; c++) {
-        const int ci = m * kMaxContacts + c;
+        const int ci = cslot(d, m, c);
         const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
         const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
         const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
@@ -452,7 +452,7 @@ __global__ void dualKernel(Dev d, StepParams p, float decay) {
         zeroAcc(sa);
         zeroAcc(sb);
         for (int c = 0; c < n; c++) {
-            const int ci = m * kMaxContacts + c;
+            const int ci = cslot(d, m, c);
             const float4 rA4 = L.rA[ci];
             const f3 rAw = mul(A.rot, xyz(rA4));
             const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
@@ -661,7 +661,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             SideAcc sd;
             zeroAcc(sd);
             for (int c = 0; c < n; c++) {
-                const int ci = m * kMaxContacts + c;
+                const int ci = cslot(d, m, c);
                 const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
                 const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
                 const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));

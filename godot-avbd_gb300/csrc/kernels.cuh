@@ -12,7 +12,7 @@ struct TuneSpace {
     int sizes[kTuneCandidates];
     int count;
 };
-constexpr TuneSpace kTuneDual{{64, 128, 256, 512}, 4};     // dualKernel (thread per contact slot)
+constexpr TuneSpace kTuneDual{{64, 128, 256, 512}, 4};     // dualKernel (one thread per manifold)
 constexpr TuneSpace kTuneSolve{{32, 64, 128, 0}, 3};       // overflowSolveKernel (launch bound 128)
 constexpr TuneSpace kTuneNarrow{{64, 128, 256, 512}, 4};   // manifoldInitKernel
 constexpr TuneSpace kTuneTraverse{{64, 128, 256, 512}, 4}; // traverseKernel
