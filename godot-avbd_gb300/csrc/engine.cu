@@ -136,6 +136,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
     take(n.mDone, mm);
     take(n.specList, mm);
     take(n.specPred, mm);
+    take(n.solveFail, nb);
     take(n.projLin, 2 * static_cast<size_t>(mm));
     take(n.projAng, 2 * static_cast<size_t>(mm));
     take(n.dLin, nb);

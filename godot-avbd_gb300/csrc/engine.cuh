@@ -48,6 +48,7 @@ enum Counter {
     C_WORLDS,         // worlds
     C_ERRORS,         // capacity / timeout bits (kErr*)
     C_ONE,            // constant 1 (scan length helper)
+    C_SOLVEFAIL,      // overflow bodies whose plain LDLT failed this round (solveFail)
     C_TMP,
     C_COUNT
 };
@@ -118,6 +119,7 @@ struct Dev {
     float4 *stamps;
     uint8_t *mSpec, *mDone; // brake: candidate flag per manifold, done flag per candidate
     int *specList;
+    int *solveFail;         // overflow bodies left to the pivoted fallback this round
     int2 *specPred;         // brake: candidate index of the preceding candidate on each movable body (-1 = none)
     float4 *projLin, *projAng; // projection contributions per (manifold, side)
     float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)

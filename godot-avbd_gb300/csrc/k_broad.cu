@@ -371,8 +371,7 @@ __device__ __forceinline__ int adjOther(const Dev &d, uint32_t seq, int x, int n
 }
 
 // pairOverlaps (solver_broadphase.cpp:30-65): bounds, layer/mask, not constrained, not both static.
-__global__ void filterKernel(Dev d) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void filterAt(Dev d, int k) {
     const int np = d.ctr[C_PAIRS];
     if (k >= np)
         return;
@@ -402,8 +401,13 @@ __global__ void filterKernel(Dev d) {
     d.pairValid[k] = (bounds && layers && !constrained && !bothStatic) ? 1 : 0;
 }
 
-__global__ void acquireKernel(Dev d, const int *flags, const int *rank) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void filterKernel(Dev d) {
+    const int n = d.ctr[C_PAIRS];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        filterAt(d, k);
+}
+
+__device__ __forceinline__ void acquireAt(Dev d, const int *flags, const int *rank, int k) {
     const int np = d.ctr[C_PAIRS];
     if (k >= np || !flags[k])
         return;
@@ -414,6 +418,12 @@ __global__ void acquireKernel(Dev d, const int *flags, const int *rank) {
     d.live.ab[m] = make_int2(d.lpToBody[static_cast<int>(key >> 32)], d.lpToBody[static_cast<int>(key & 0xffffffffu)]);
     d.live.count[m] = 0;
     d.live.dormant[m] = make_int2(0, 0);
+}
+
+__global__ void acquireKernel(Dev d, const int *flags, const int *rank) {
+    const int n = d.ctr[C_PAIRS];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        acquireAt(d, flags, rank, k);
 }
 
 __global__ void candTotalKernel(Dev d) {
@@ -466,9 +476,9 @@ void launchPairs(const Dev &d, int block, cudaStream_t s) {
 }
 
 void launchFilterAcquire(const Dev &d, cudaStream_t s) {
-    ++launchCount(); filterKernel<<<grid(d.PP), kThreads, 0, s>>>(d);
+    ++launchCount(); filterKernel<<<residentGrid(filterKernel, kThreads, grid(d.PP)), kThreads, 0, s>>>(d);
     scanExclusive(d.pairValid, d.mActive, d.PP, d.ctr + C_PAIRS, d.ctr + C_TMP, d.scanScratch, s);
-    ++launchCount(); acquireKernel<<<grid(d.PP), kThreads, 0, s>>>(d, d.pairValid, d.mActive);
+    ++launchCount(); acquireKernel<<<residentGrid(acquireKernel, kThreads, grid(d.PP)), kThreads, 0, s>>>(d, d.pairValid, d.mActive);
     ++launchCount(); candTotalKernel<<<1, 1, 0, s>>>(d);
 }
 

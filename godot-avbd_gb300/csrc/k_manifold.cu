@@ -97,8 +97,7 @@ __device__ __forceinline__ f3 basisMul(f3 r0, f3 r1, f3 r2, f3 v) {
 // ROUND: the store holds spheres or cylinders, whose sampled paths need kilobytes of local memory
 // per thread; box-only stores run the variant without them.
 template <bool ROUND>
-__global__ void manifoldInitKernel(Dev d, StepParams p) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
     if (i >= d.ctr[C_CAND])
         return;
     const ManifoldBuf L = d.live;
@@ -274,6 +273,13 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
     d.mActive[i] = n > 0 ? 1 : 0;
 }
 
+template <bool ROUND>
+__global__ void manifoldInitKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_CAND];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        manifoldInitAt<ROUND>(d, p, i);
+}
+
 // One thread per contact slot (8 per candidate, slot-major like the arrays), so the copies of the
 // contact arrays coalesce; the slot-0 thread also moves the manifold's own record. Grid-stride.
 __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
@@ -311,8 +317,7 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
 }
 
 // ---- rebase (ManifoldStore::rebase, manifold.cpp:448-461) ----
-__global__ void rebaseKernel(Dev d, StepParams p) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void rebaseAt(Dev d, StepParams p, int m) {
     if (m >= d.ctr[C_LIVE])
         return;
     const ManifoldBuf L = d.live;
@@ -330,6 +335,12 @@ __global__ void rebaseKernel(Dev d, StepParams p) {
             C0.x = -p.maxPen;
         L.C0[ci] = f4(C0, 0.0f);
     }
+}
+
+__global__ void rebaseKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        rebaseAt(d, p, m);
 }
 
 // ---- forces: Joint::initialize (joint.cpp:62-78) and reaping of broken joints ----
@@ -452,7 +463,7 @@ void launchManifoldCompact(const Dev &d, cudaStream_t s) {
 }
 
 void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); rebaseKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+    ++launchCount(); rebaseKernel<<<residentGrid(rebaseKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
 }
 
 void launchForceInit(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {

@@ -65,8 +65,7 @@ __device__ __forceinline__ void maskLocked(int locks, f3 &v) {
 }
 
 // projectionActive membership and "can brake" (an open gap at the current poses).
-__global__ void projActiveKernel(Dev d) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void projActiveAt(Dev d, int m) {
     if (m >= d.ctr[C_LIVE])
         return;
     const ManifoldBuf L = d.live;
@@ -94,20 +93,30 @@ __global__ void projActiveKernel(Dev d) {
     d.mActive[m] = spec;
 }
 
+__global__ void projActiveKernel(Dev d) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        projActiveAt(d, m);
+}
+
 // Brake candidates in live order (the scan of their flags gives each one its slot).
-__global__ void specScatterKernel(Dev d, const int *flags, const int *rank) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void specScatterAt(Dev d, const int *flags, const int *rank, int m) {
     if (m >= d.ctr[C_LIVE] || !flags[m])
         return;
     d.specList[rank[m]] = m;
     d.mDone[rank[m]] = 0;
 }
 
+__global__ void specScatterKernel(Dev d, const int *flags, const int *rank) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        specScatterAt(d, flags, rank, m);
+}
+
 // For each candidate, the preceding candidate on each of its movable bodies (-1 if none), as a
 // candidate index, from the body's adjacency (forces first, then manifolds in live order); `rank`
 // is the exclusive scan of the candidate flags.
-__global__ void brakePredKernel(Dev d, const int *rank) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void brakePredAt(Dev d, const int *rank, int k) {
     if (k >= d.ctr[C_SPECN])
         return;
     const int m = d.specList[k];
@@ -130,6 +139,12 @@ __global__ void brakePredKernel(Dev d, const int *rank) {
         }
     }
     d.specPred[k] = make_int2(pred[0], pred[1]);
+}
+
+__global__ void brakePredKernel(Dev d, const int *rank) {
+    const int n = d.ctr[C_SPECN];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        brakePredAt(d, rank, k);
 }
 
 __device__ __forceinline__ unsigned loadAcquire(const uint8_t *p) {
@@ -271,8 +286,7 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
 
 // ---- positional projection (solver_projection.cpp:169-280) ----
 
-__global__ void projManifoldKernel(Dev d, StepParams p) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m) {
     if (m >= d.ctr[C_LIVE])
         return;
     const ManifoldBuf L = d.live;
@@ -328,6 +342,12 @@ __global__ void projManifoldKernel(Dev d, StepParams p) {
         d.projLin[2 * m + 1] = f4(scale(nrm, invMassB * dp), 1.0f);
         d.projAng[2 * m + 1] = f4(scale(angularResponse(IB, qb, tB), dp), 0.0f);
     }
+}
+
+__global__ void projManifoldKernel(Dev d, StepParams p) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        projManifoldAt(d, p, m);
 }
 
 __global__ void projBodyKernel(Dev d, StepParams p) {
@@ -420,14 +440,14 @@ int brakeGridBlocks() {
 
 void launchProjActive(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.wActive, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
-    ++launchCount(); projActiveKernel<<<grid(d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); projActiveKernel<<<residentGrid(projActiveKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d);
     scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_LIVE, d.ctr + C_SPECN, d.scanScratch, s);
-    ++launchCount(); specScatterKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
+    ++launchCount(); specScatterKernel<<<residentGrid(specScatterKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
 }
 
 // Runs right after launchProjActive, whose scan left each candidate's rank in d.pairValid.
 void launchBrake(const Dev &d, float window, cudaStream_t s) {
-    ++launchCount(); brakePredKernel<<<grid(d.MM), kThreads, 0, s>>>(d, d.pairValid);
+    ++launchCount(); brakePredKernel<<<residentGrid(brakePredKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, d.pairValid);
     Dev dd = d;
     float win = window;
     void *args[] = {&dd, &win};
@@ -440,7 +460,7 @@ void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
     ++launchCount(); projStartKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
     const float tol = smax(p.projSlop * 0.01f, 1.0e-6f);
     for (int it = 0; it < p.projIters; it++) {
-        ++launchCount(); projManifoldKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p);
+        ++launchCount(); projManifoldKernel<<<residentGrid(projManifoldKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
         ++launchCount(); projBodyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
         ++launchCount(); projCheckKernel<<<grid(d.WW), kThreads, 0, s>>>(d, tol);
     }

@@ -23,6 +23,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kSolveThreads = 128;
+constexpr int kFallbackBlocks = 8; // the pivoted fallback is rare: a few blocks, grid-stride
 
 struct Blk {
     m3 lin, ang, crs;
@@ -94,7 +95,7 @@ __device__ bool ldlt6(const float a[6][6], const float b[6], float x[6]) {
     return isfinite(worst) && worst < 1.0e1f;
 }
 
-__device__ __noinline__ bool ldlt6Pivoted(const float aIn[6][6], const float b[6], float x[6]) {
+__device__ __forceinline__ bool ldlt6Pivoted(const float aIn[6][6], const float b[6], float x[6]) {
     float a[6][6];
     for (int r = 0; r < 6; r++)
         for (int c = 0; c < 6; c++)
@@ -195,9 +196,8 @@ __device__ __noinline__ bool ldlt6Pivoted(const float aIn[6][6], const float b[6
     return isfinite(worst) && worst < 1.0e1f;
 }
 
-// Block::solveDelta (types.hpp:176-197) with solve()'s fallback chain.
-__device__ __forceinline__ void solveBlock(const Blk &k, f3 &dl, f3 &da) {
-    float a[6][6];
+// The 6x6 system of Block::solveDelta (types.hpp:176-197): a = [lin crs^T; crs ang], b = -rhs.
+__device__ __forceinline__ void blockSystem(const Blk &k, float a[6][6], float b[6]) {
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
@@ -207,16 +207,50 @@ __device__ __forceinline__ void solveBlock(const Blk &k, f3 &dl, f3 &da) {
             a[r + 3][c] = mat(k.crs, c, r);
             a[r][c + 3] = mat(k.crs, r, c);
         }
-    const float b[6] = {-k.rl.x, -k.rl.y, -k.rl.z, -k.ra.x, -k.ra.y, -k.ra.z};
-    float x[6];
-    if (ldlt6(a, b, x)) {
-        dl = f3{x[0], x[1], x[2]};
-        da = f3{x[3], x[4], x[5]};
+    b[0] = -k.rl.x;
+    b[1] = -k.rl.y;
+    b[2] = -k.rl.z;
+    b[3] = -k.ra.x;
+    b[4] = -k.ra.y;
+    b[5] = -k.ra.z;
+}
+
+struct Delta {
+    f3 dl, da;
+    bool ok;
+};
+
+// solve()'s pivoted fallback, out of line: the block travels by value, so the fast path's matrix
+// never needs an address and stays in registers.
+__device__ __noinline__ Delta solvePivoted(Blk k) {
+    float a[6][6], b[6], x[6];
+    blockSystem(k, a, b);
+    Delta r;
+    r.ok = ldlt6Pivoted(a, b, x);
+    r.dl = f3{x[0], x[1], x[2]};
+    r.da = f3{x[3], x[4], x[5]};
+    return r;
+}
+
+// Block::solveDelta's plain LDLT; false when solve() would fall back.
+__device__ __forceinline__ bool solveBlockFast(const Blk &k, f3 &dl, f3 &da) {
+    float a[6][6], b[6], x[6];
+    blockSystem(k, a, b);
+    if (!ldlt6(a, b, x))
+        return false;
+    dl = f3{x[0], x[1], x[2]};
+    da = f3{x[3], x[4], x[5]};
+    return true;
+}
+
+// Block::solveDelta with solve()'s fallback chain: plain LDLT, pivoted LDLT, then no step.
+__device__ __forceinline__ void solveBlock(const Blk &k, f3 &dl, f3 &da) {
+    if (solveBlockFast(k, dl, da))
         return;
-    }
-    if (ldlt6Pivoted(a, b, x)) {
-        dl = f3{x[0], x[1], x[2]};
-        da = f3{x[3], x[4], x[5]};
+    const Delta r = solvePivoted(k);
+    if (r.ok) {
+        dl = r.dl;
+        da = r.da;
         return;
     }
     dl = f3{0, 0, 0};
@@ -414,8 +448,7 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
         storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
 }
 
-__global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void stampsAt(Dev d, StepParams p, int mixedOnly, int m) {
     if (m >= d.ctr[C_LIVE])
         return;
     bool touches;
@@ -423,6 +456,12 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
     if (!sides || touches != (mixedOnly != 0))
         return;
     computeStamps(d, p, m, sides);
+}
+
+__global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        stampsAt(d, p, mixedOnly, m);
 }
 
 // Dual pass (ManifoldStore::updateDual, manifold.cpp:583-671) and, with STAMPS, the next round's
@@ -706,6 +745,18 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
 
+// An overflow body's step: in place (no forces) or into dLin/dAng for overflowApplyKernel.
+__device__ __forceinline__ void applyOverflow(const Dev &d, const StepParams &p, int g, int inPlace, f3 dl, f3 da) {
+    if (inPlace) {
+        const float4 x4 = d.x[g];
+        d.x[g] = f4(add(xyz(x4), scale(dl, p.jacobiRelax)), x4.w);
+        d.q[g] = f4(qintegrate(asq(d.q[g]), scale(da, p.jacobiRelax)));
+    } else {
+        d.dLin[g] = f4(dl, 0.0f);
+        d.dAng[g] = f4(da, 0.0f);
+    }
+}
+
 // Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
 template <bool FORCES>
 __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
@@ -716,14 +767,25 @@ __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, Step
     Blk blk = bodyBlock(d, p, g);
     assemble<false, FORCES>(d, p, g, blk);
     f3 dl, da;
-    solveBlock(blk, dl, da);
-    if (inPlace) {
-        const float4 x4 = d.x[g];
-        d.x[g] = f4(add(xyz(x4), scale(dl, p.jacobiRelax)), x4.w);
-        d.q[g] = f4(qintegrate(asq(d.q[g]), scale(da, p.jacobiRelax)));
-    } else {
-        d.dLin[g] = f4(dl, 0.0f);
-        d.dAng[g] = f4(da, 0.0f);
+    if (!solveBlockFast(blk, dl, da)) {
+        d.solveFail[atomicAdd(d.ctr + C_SOLVEFAIL, 1)] = g; // overflowFallbackKernel takes it
+        return;
+    }
+    applyOverflow(d, p, g, inPlace, dl, da);
+}
+
+// The bodies whose plain LDLT failed, through solve()'s pivoted fallback. Block-Jacobi: a block
+// reads stamps and its own pose only (with forces, updates go through dLin/dAng), so solving these
+// after the others gives the same result.
+template <bool FORCES>
+__global__ void __launch_bounds__(kSolveThreads) overflowFallbackKernel(Dev d, StepParams p, int inPlace) {
+    const int n = d.ctr[C_SOLVEFAIL];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int g = d.solveFail[i];
+        Blk blk = bodyBlock(d, p, g);
+        assemble<false, FORCES>(d, p, g, blk);
+        const Delta r = solvePivoted(blk);
+        applyOverflow(d, p, g, inPlace, r.ok ? r.dl : f3{0, 0, 0}, r.ok ? r.da : f3{0, 0, 0});
     }
 }
 
@@ -1022,7 +1084,7 @@ void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream
 }
 
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s) {
-    ++launchCount(); stampsKernel<<<grid(d.MM), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
+    ++launchCount(); stampsKernel<<<residentGrid(stampsKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
 }
 
 void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_t s) {
@@ -1030,11 +1092,15 @@ void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_
 }
 
 void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s) {
-    ++launchCount();
-    if (forces)
+    cudaMemsetAsync(d.ctr + C_SOLVEFAIL, 0, sizeof(int), s);
+    launchCount() += 2;
+    if (forces) {
         overflowSolveKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
-    else
+        overflowFallbackKernel<true><<<kFallbackBlocks, kSolveThreads, 0, s>>>(d, p, inPlace ? 1 : 0);
+    } else {
         overflowSolveKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
+        overflowFallbackKernel<false><<<kFallbackBlocks, kSolveThreads, 0, s>>>(d, p, inPlace ? 1 : 0);
+    }
 }
 
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {

@@ -39,6 +39,10 @@ inline int divUp(int a, int b) { return (a + b - 1) / b; }
 // current device at once, capped at `want` (at least 1). Grid-stride kernels over a capacity use it so
 // that a mostly empty capacity costs no blocks. Cached per (device, kernel, block, smem).
 int residentGrid(const void *kernel, int block, size_t smem, int want);
+template <typename K>
+inline int residentGrid(K *kernel, int block, int want) {
+    return residentGrid(reinterpret_cast<const void *>(kernel), block, 0, want);
+}
 
 // Kernel attributes the primitives need (large dynamic shared memory); call before any capture.
 void preparePrimitives();
