@@ -62,8 +62,9 @@ constexpr int kRefitBudget = 16; // src/avbd/bvh_broadphase.hpp:40
 // Every device buffer of a store, in one place: `take(ptr, count)` allocates (or counts) `count`
 // elements of ptr's type.
 template <typename Take>
-void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
+void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take &&take) {
     n.NB = nb;
+    n.ARM = arm ? 1 : 0;
     n.MM = mm;
     n.FF = ff;
     n.PP = pp;
@@ -130,6 +131,12 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, Take &&take) {
         take(b->C0, mc);
         take(b->k, mc);
         take(b->lam, mc);
+        const size_t am = arm ? static_cast<size_t>(mm) : 0;
+        take(b->armA, am * kMaxContacts);
+        take(b->armB, am * kMaxContacts);
+        take(b->capA, am);
+        take(b->capB, am);
+        take(b->armFlag, am);
     }
     take(n.stamps, static_cast<size_t>(mm) * 2 * kStampF4);
     take(n.mSpec, mm);
@@ -192,6 +199,7 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
     for (auto &e : ev)
         cudaEventCreate(&e);
+    armStore = P.jacobian_rebuild_distance > 0.0f;
     const int nb = std::max(maxBodies, 64);
     allocate(nb, std::max(1024, 8 * nb), std::max(maxForces, 16), std::max(4096, 16 * nb), std::max(maxWorlds, 1));
 }
@@ -247,7 +255,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
     std::vector<void *> oldAllocs;
     oldAllocs.swap(allocs);
     Dev n{};
-    layoutStore(n, nb, mm, ff, pp, ww, [this](auto *&ptr, size_t count) {
+    layoutStore(n, nb, mm, ff, pp, ww, armStore, [this](auto *&ptr, size_t count) {
         using T = std::remove_reference_t<decltype(*ptr)>;
         ptr = dalloc<T>(count);
     });
@@ -283,12 +291,22 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         cp(t.dormant, s.dormant, mCopy * sizeof(int2));
         // Contact arrays are slot-major: slot c of the old store (old.MM entries apart) to slot c of
         // the new one (mm apart).
+        const bool arms = old.ARM && n.ARM;
         for (int c = 0; c < kMaxContacts; c++) {
             const size_t so = static_cast<size_t>(c) * old.MM, sn = static_cast<size_t>(c) * mm;
             cp(t.key + sn, s.key + so, mCopy * sizeof(int));
             for (auto pr : {std::make_pair(t.rA, s.rA), std::make_pair(t.rB, s.rB), std::make_pair(t.C0, s.C0),
                             std::make_pair(t.k, s.k), std::make_pair(t.lam, s.lam)})
                 cp(pr.first + sn, pr.second + so, mCopy * sizeof(float4));
+            if (arms) {
+                cp(t.armA + sn, s.armA + so, mCopy * sizeof(float4));
+                cp(t.armB + sn, s.armB + so, mCopy * sizeof(float4));
+            }
+        }
+        if (arms) {
+            cp(t.capA, s.capA, mCopy * sizeof(float4));
+            cp(t.capB, s.capB, mCopy * sizeof(float4));
+            cp(t.armFlag, s.armFlag, mCopy * sizeof(uint8_t));
         }
         const size_t fCopy = static_cast<size_t>(std::min(old.FF, ff));
         cp(n.fAB, old.fAB, fCopy * sizeof(int2));
@@ -317,10 +335,10 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
     cudaStreamSynchronize(stream);
 }
 
-size_t Engine::storeBytes(int nb, int mm, int ff, int pp, int ww) {
+size_t Engine::storeBytes(int nb, int mm, int ff, int pp, int ww, bool arm) {
     size_t total = 0;
     Dev n{};
-    layoutStore(n, nb, mm, ff, pp, ww, [&total](auto *&ptr, size_t count) {
+    layoutStore(n, nb, mm, ff, pp, ww, arm, [&total](auto *&ptr, size_t count) {
         using T = std::remove_reference_t<decltype(*ptr)>;
         total += (std::max<size_t>(count, 1) * sizeof(T) + 255) / 256 * 256; // cudaMalloc granularity
         ptr = nullptr;
@@ -709,14 +727,24 @@ void Engine::uploadCounts() {
 int Engine::setParams(const avbdg_params &p) {
     if (p.iterations < 1 || !(p.dt > 0.0f))
         return fail(AVBDG_ERR_INVALID, "iterations must be >= 1 and dt > 0");
-    if (p.jacobian_rebuild_distance != 0.0f || p.convergence_threshold != 0.0f)
-        return fail(AVBDG_ERR_UNSUPPORTED, "the arm cache and the convergence probe are not on the GPU path");
+    if (p.convergence_threshold != 0.0f)
+        return fail(AVBDG_ERR_UNSUPPORTED, "the convergence probe is not on the GPU path");
+    if (!(p.jacobian_rebuild_distance >= 0.0f))
+        return fail(AVBDG_ERR_INVALID, "jacobian_rebuild_distance must be >= 0");
     if (p.contact_grace_ticks < 0)
         return fail(AVBDG_ERR_INVALID, "contact_grace_ticks must be >= 0");
     if (p.sleep_frames < 0)
         return fail(AVBDG_ERR_INVALID, "sleep_frames must be >= 0");
     P = p;
     dropGraphs(); // parameters are baked into captured launches
+    if (p.jacobian_rebuild_distance > 0.0f && !armStore) {
+        // The arm-cache arrays join the store (zeroed: no arms captured yet).
+        armStore = true;
+        if (d.NB > 0) {
+            allocate(d.NB, d.MM, d.FF, d.PP, d.WW);
+            return cudaCheck("arm cache");
+        }
+    }
     return AVBDG_OK;
 }
 
@@ -747,6 +775,8 @@ StepParams Engine::stepParams(float collisionDt) const {
     s.graceSeed = std::max(PENALTY_MIN, 0.05f * P.beta_lin);
     s.sleepLin2 = P.sleep_linear_threshold * P.sleep_linear_threshold;
     s.sleepAng2 = P.sleep_angular_threshold * P.sleep_angular_threshold;
+    s.armCache = P.jacobian_rebuild_distance > 0.0f && d.ARM ? 1 : 0;
+    s.armRebuild2 = P.jacobian_rebuild_distance * P.jacobian_rebuild_distance;
     return s;
 }
 
@@ -966,7 +996,7 @@ void Engine::runSubstep(const StepParams &sp, int rounds, bool idle) {
             if (colours) {
                 // Each pass reads its colour's size on the device; empty colours return at once.
                 for (int c = 0; c < kMaxColours; c++)
-                    launchColourPass(d, c, sp, stream);
+                    launchColourPass(d, c, sp, it > 0, stream);
                 launchStamps(d, sp, true, stream);
             }
             beginSpan();
@@ -1531,12 +1561,13 @@ int Engine::dumpColours(int cap, uint8_t *colour, int32_t *bodyId, int *count) {
     }
     const int n = wCount[w];
     std::vector<float4> x(n);
-    std::vector<uint8_t> col(n);
+    std::vector<uint8_t> col(n), upd(n);
     cudaMemcpy(x.data(), d.x + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
     cudaMemcpy(col.data(), d.colour + wBase[w], n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(upd.data(), d.upd + wBase[w], n, cudaMemcpyDeviceToHost);
     int u = 0;
-    for (int id = n - 1; id >= 0; id--) { // list order
-        if (!(x[id].w > 0.0f))
+    for (int id = n - 1; id >= 0; id--) { // list order, update set only (sleepers are not in it)
+        if (!(x[id].w > 0.0f) || !upd[id])
             continue;
         if (u < cap) {
             if (colour)

@@ -70,6 +70,8 @@ struct StepParams {
     int graceTicks;               // Solver::contactGraceTicks (0 = off)
     float graceSeed;              // penalty of a fresh contact under grace: max(PENALTY_MIN, 0.05 betaLin)
     float sleepLin2, sleepAng2;   // squared velocity thresholds of idle detection
+    int armCache;                 // Solver::jacobianRebuildDistance > 0
+    float armRebuild2;            // its square
 };
 
 struct ManifoldBuf {
@@ -77,12 +79,19 @@ struct ManifoldBuf {
     float4 *b0, *b1, *b2;
     int *count;
     int2 *dormant;     // contact grace: x = ticks parked, y = contacts kept for revival
-    int *key;          // contacts: [m * 8 + k]
+    int *key;          // contacts: slot-major, see cslot
     float4 *rA, *rB, *C0, *k, *lam;
+    // Arm cache (Solver::jacobianRebuildDistance, manifold.cpp:600-668): world arms (slot-major like
+    // the contacts), the first rotation columns captured with them and the kArmsCached flag.
+    // Allocated only while the cache is on (Dev::ARM).
+    float4 *armA, *armB;
+    float4 *capA, *capB;
+    uint8_t *armFlag;
 };
 
 struct Dev {
     int NB, MM, FF, PP, WW; // capacities
+    int ARM;                // 1: the arm-cache arrays of ManifoldBuf are allocated
     // worlds
     int *wBase, *wCount;    // body range
     int *wMaxDepth;         // projection: max depth bits per world (positive floats)

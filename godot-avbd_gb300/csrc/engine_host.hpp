@@ -44,10 +44,10 @@ public:
     static int validateForces(int nb, int count, const avbdg_force_desc *descs, std::string &why);
 
     // Device bytes of a store with these capacities (bodies, manifolds, forces, pairs, worlds).
-    static size_t storeBytes(int nb, int mm, int ff, int pp, int ww);
+    static size_t storeBytes(int nb, int mm, int ff, int pp, int ww, bool arm = false);
     // Capacities for `nb` bodies the store grows to (manifolds and pairs follow the body count).
     static size_t storeBytesForBodies(int nb, int ff, int ww) { return storeBytes(nb, 8 * nb, ff, 16 * nb, ww); }
-    size_t reservedBytes() const { return storeBytes(d.NB, d.MM, d.FF, d.PP, d.WW); }
+    size_t reservedBytes() const { return storeBytes(d.NB, d.MM, d.FF, d.PP, d.WW, d.ARM != 0); }
     // Upper bound on the store's device bytes (0 = none): growth headroom is cut to fit, and a
     // growth that cannot fit fails with AVBDG_ERR_CAPACITY.
     void setByteLimit(size_t bytes) { byteLimit = bytes; }
@@ -107,6 +107,7 @@ private:
     int nBodies = 0, nDynamic = 0, nForces = 0, nRound = 0; // nRound: spheres and cylinders
     int treeAge = 0;
     bool treeValid = false, adjValid = false;
+    bool armStore = false; // the store carries the arm-cache arrays (set once the cache is first on)
     size_t byteLimit = 0;
     int steps = 0;
     int launches = 0;
@@ -161,7 +162,7 @@ private:
     int ensureCapacity(int nb, int ff, int ww);
     void uploadCounts();
     bool fits(int nb, int mm, int ff, int pp, int ww) const {
-        return byteLimit == 0 || storeBytes(nb, mm, ff, pp, ww) <= byteLimit;
+        return byteLimit == 0 || storeBytes(nb, mm, ff, pp, ww, armStore) <= byteLimit;
     }
     StepParams stepParams(float collisionDt) const;
     // Host decisions of one step; the enqueued work depends on nothing else but device counts.

@@ -126,9 +126,20 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
             S.k[cslot(d, i, k)] = L.k[cslot(d, i, k)];
             S.lam[cslot(d, i, k)] = L.lam[cslot(d, i, k)];
         }
+        if (d.ARM) { // frozen manifolds keep their captured arms (initialize does not run)
+            S.armFlag[i] = L.armFlag[i];
+            S.capA[i] = L.capA[i];
+            S.capB[i] = L.capB[i];
+            for (int k = 0; k < kept; k++) {
+                S.armA[cslot(d, i, k)] = L.armA[cslot(d, i, k)];
+                S.armB[cslot(d, i, k)] = L.armB[cslot(d, i, k)];
+            }
+        }
         d.mActive[i] = 1;
         return;
     }
+    if (d.ARM)
+        S.armFlag[i] = 0; // a new contact set drops the cached arms (manifold.cpp:245-246)
     // Grace revival (manifold.cpp:249-253): a dormant manifold matches against its saved contacts.
     if (oldN == 0 && dorm.y > 0)
         oldN = dorm.y;
@@ -302,6 +313,11 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
             L.b2[r] = S.b2[i];
             L.count[r] = n;
             L.dormant[r] = dorm;
+            if (d.ARM) {
+                L.armFlag[r] = S.armFlag[i];
+                L.capA[r] = S.capA[i];
+                L.capB[r] = S.capB[i];
+            }
         }
         const int kept = n > 0 ? n : dorm.y; // a parked manifold keeps its saved contacts
         if (c >= kept)
@@ -313,6 +329,10 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
         L.C0[di] = S.C0[si];
         L.k[di] = S.k[si];
         L.lam[di] = S.lam[si];
+        if (d.ARM) {
+            L.armA[di] = S.armA[si];
+            L.armB[di] = S.armB[si];
+        }
     }
 }
 

@@ -80,6 +80,15 @@ __global__ void manifoldRelocateKernel(Dev d, const int *slotMap) {
         S.C0[i] = L.C0[i];
         S.k[i] = L.k[i];
         S.lam[i] = L.lam[i];
+        if (d.ARM) {
+            S.armA[i] = L.armA[i];
+            S.armB[i] = L.armB[i];
+        }
+    }
+    if (d.ARM) {
+        S.armFlag[m] = L.armFlag[m];
+        S.capA[m] = L.capA[m];
+        S.capB[m] = L.capB[m];
     }
 }
 

@@ -428,6 +428,10 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
         const int ci = cslot(d, m, c);
         const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
         const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+        if (p.armCache) { // preCompute refreshes the cached world arms (manifold.cpp:486-487)
+            L.armA[ci] = f4(rAw, 0.0f);
+            L.armB[ci] = f4(rBw, 0.0f);
+        }
         const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
         const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
         const f3 k = xyz(L.k[ci]);
@@ -467,8 +471,9 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
 // Dual pass (ManifoldStore::updateDual, manifold.cpp:583-671) and, with STAMPS, the next round's
 // stamps (the reference's phase-A recompute of each force, manifold.cpp:655-659, from the same
 // floats). One thread per manifold, grid-stride over the live ones.
-template <bool STAMPS>
-__global__ void dualKernel(Dev d, StepParams p, float decay) {
+// ARM: the arm cache is on (compiled out otherwise, so the common path keeps its code).
+template <bool STAMPS, bool ARM>
+__global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float decay) { // 512: largest tuned block
     const int live = d.ctr[C_LIVE];
     const ManifoldBuf L = d.live;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x) {
@@ -484,6 +489,13 @@ __global__ void dualKernel(Dev d, StepParams p, float decay) {
         const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
         const float mu = b04.w;
         const int n = L.count[m];
+        // Drift-gated arm reuse (manifold.cpp:600-608): under the rotation threshold the cached
+        // world arms stand in for the current ones.
+        bool driftUsable = false;
+        if (ARM) {
+            const f3 dA = sub(A.rot.c0, xyz(L.capA[m])), dB = sub(B.rot.c0, xyz(L.capB[m]));
+            driftUsable = L.armFlag[m] != 0 && length2(dA) <= p.armRebuild2 && length2(dB) <= p.armRebuild2;
+        }
         SharedAcc sh;
         sh.lin = mzero();
         sh.rhsLin = f3{0, 0, 0};
@@ -493,8 +505,18 @@ __global__ void dualKernel(Dev d, StepParams p, float decay) {
         for (int c = 0; c < n; c++) {
             const int ci = cslot(d, m, c);
             const float4 rA4 = L.rA[ci];
-            const f3 rAw = mul(A.rot, xyz(rA4));
-            const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+            f3 rAw, rBw;
+            if (driftUsable) {
+                rAw = xyz(L.armA[ci]);
+                rBw = xyz(L.armB[ci]);
+            } else {
+                rAw = mul(A.rot, xyz(rA4));
+                rBw = mul(B.rot, xyz(L.rB[ci]));
+                if (ARM) {
+                    L.armA[ci] = f4(rAw, 0.0f);
+                    L.armB[ci] = f4(rBw, 0.0f);
+                }
+            }
             const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
             const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
             f3 k = xyz(L.k[ci]);
@@ -516,22 +538,40 @@ __global__ void dualKernel(Dev d, StepParams p, float decay) {
             L.k[ci] = f4(k, 0.0f);
             L.lam[ci] = f4(lam, stick);
             if (STAMPS && sides) {
-                f3 Fn = add(cmul(k, C), lam);
+                // These are the next round's overflow phase A (solver_step.cpp:236-248): it always
+                // precomputes with fresh arms at this pose and stores them, whatever the dual used.
+                f3 rAs = rAw, rBs = rBw, Cs = C;
+                if (ARM) {
+                    if (driftUsable) {
+                        rAs = mul(A.rot, xyz(rA4));
+                        rBs = mul(B.rot, xyz(L.rB[ci]));
+                        const f3 bracketF = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAs)), cross(B.dAng, rBs));
+                        Cs = contactError(p, xyz(L.C0[ci]), bracketF, r0, r1, r2);
+                    }
+                    L.armA[ci] = f4(rAs, 0.0f);
+                    L.armB[ci] = f4(rBs, 0.0f);
+                }
+                f3 Fn = add(cmul(k, Cs), lam);
                 clampForce(Fn, mu);
                 float S[6];
                 basisHessianD(r0, r1, r2, k, S);
                 const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
                 stampShared(S, fw, sh);
                 if (sides & kSideA)
-                    stampContact(S, rAw, fw, sa);
+                    stampContact(S, rAs, fw, sa);
                 if (sides & kSideB)
-                    stampContact(S, rBw, fw, sb);
+                    stampContact(S, rBs, fw, sb);
             }
         }
         if (sides & kSideA)
             storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
         if (sides & kSideB)
             storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
+        if (ARM && !driftUsable) { // capture (manifold.cpp:662-667)
+            L.capA[m] = f4(A.rot.c0, 0.0f);
+            L.capB[m] = f4(B.rot.c0, 0.0f);
+            L.armFlag[m] = 1;
+        }
     }
 }
 
@@ -674,8 +714,13 @@ __device__ __forceinline__ int nForcesDev(const Dev &d) { return d.ctr[C_FORCES]
 // from the current poses (Gauss-Seidel).
 // Without FORCES (a store with no non-manifold force) the force branch is compiled out, so the
 // body passes keep their registers in registers.
+// With RECOMPUTE (coloured Gauss-Seidel, ManifoldStore::updatePrimal, manifold.cpp:572-581) and the
+// arm cache on, the first touch of a manifold after a dual pass (`armsFromDual`: rounds after the
+// first) consumes that dual's cache, so it uses the cached world arms; the other touches precompute
+// with fresh arms and store them. The first touch is the body whose partner has not been solved
+// this round (not coloured, or coloured later).
 template <bool RECOMPUTE, bool FORCES = true>
-__device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk) {
+__device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk, int armsFromDual = 0) {
     const int nf = nForcesDev(d);
     for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
         const int seq = static_cast<int>(d.adjSeq[e]);
@@ -694,6 +739,11 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             const float4 b04 = L.b0[m];
             const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
             const int n = L.count[m];
+            bool cached = false;
+            if (p.armCache && armsFromDual) {
+                const int o = side == 0 ? ab.y : ab.x;
+                cached = !(inUpdate(d, o) && d.colour[o] < d.colour[g]);
+            }
             SharedAcc sh;
             sh.lin = mzero();
             sh.rhsLin = f3{0, 0, 0};
@@ -701,8 +751,18 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             zeroAcc(sd);
             for (int c = 0; c < n; c++) {
                 const int ci = cslot(d, m, c);
-                const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
-                const f3 rBw = mul(B.rot, xyz(L.rB[ci]));
+                f3 rAw, rBw;
+                if (cached) {
+                    rAw = xyz(L.armA[ci]);
+                    rBw = xyz(L.armB[ci]);
+                } else {
+                    rAw = mul(A.rot, xyz(L.rA[ci]));
+                    rBw = mul(B.rot, xyz(L.rB[ci]));
+                    if (p.armCache) {
+                        L.armA[ci] = f4(rAw, 0.0f);
+                        L.armB[ci] = f4(rBw, 0.0f);
+                    }
+                }
                 const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
                 const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
                 const f3 k = xyz(L.k[ci]);
@@ -731,13 +791,13 @@ __device__ __forceinline__ Blk bodyBlock(const Dev &d, const StepParams &p, int 
     return makeBlock(x4.w, xyz(d.moment[g]), p.dtSq, xyz(x4), xyz(d.xi[g]), asq(d.q[g]), asq(d.qi[g]));
 }
 
-__global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepParams p, int colour) {
+__global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepParams p, int colour, int armsFromDual) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= d.colourCount[colour])
         return;
     const int g = d.colourList[colour * d.NB + k];
     Blk blk = bodyBlock(d, p, g);
-    assemble<true>(d, p, g, blk);
+    assemble<true>(d, p, g, blk, armsFromDual);
     f3 dl, da;
     solveBlock(blk, dl, da);
     const float4 x4 = d.x[g];
@@ -1087,8 +1147,9 @@ void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_
     ++launchCount(); stampsKernel<<<residentGrid(stampsKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
 }
 
-void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); colourPassKernel<<<divUp(d.NB, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour);
+void launchColourPass(const Dev &d, int colour, const StepParams &p, bool armsFromDual, cudaStream_t s) {
+    ++launchCount();
+    colourPassKernel<<<divUp(d.NB, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour, armsFromDual ? 1 : 0);
 }
 
 void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s) {
@@ -1108,16 +1169,18 @@ void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {
     overflowApplyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
 }
 
+template <bool STAMPS, bool ARM>
+static void dualLaunch(const Dev &d, const StepParams &p, float decay, int block, cudaStream_t s) {
+    const int blocks = residentGrid(dualKernel<STAMPS, ARM>, block, divUp(d.MM, block));
+    dualKernel<STAMPS, ARM><<<blocks, block, 0, s>>>(d, p, decay);
+}
+
 void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, int block, cudaStream_t s) {
-    const int want = divUp(d.MM, block);
     ++launchCount();
-    if (stamps) {
-        const void *fn = reinterpret_cast<const void *>(dualKernel<true>);
-        dualKernel<true><<<residentGrid(fn, block, 0, want), block, 0, s>>>(d, p, decay);
-    } else {
-        const void *fn = reinterpret_cast<const void *>(dualKernel<false>);
-        dualKernel<false><<<residentGrid(fn, block, 0, want), block, 0, s>>>(d, p, decay);
-    }
+    if (p.armCache)
+        stamps ? dualLaunch<true, true>(d, p, decay, block, s) : dualLaunch<false, true>(d, p, decay, block, s);
+    else
+        stamps ? dualLaunch<true, false>(d, p, decay, block, s) : dualLaunch<false, false>(d, p, decay, block, s);
 }
 
 void launchForceDual(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {

@@ -52,7 +52,8 @@ void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream
 // Stamps (precompute) of manifolds touching the overflow set; `mixedOnly` restricts to those that
 // also touch a coloured body (recomputed after the colour passes).
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
-void launchColourPass(const Dev &d, int colour, const StepParams &p, cudaStream_t s);
+// `armsFromDual`: a dual pass ran since the manifolds were (re)initialised or rebased.
+void launchColourPass(const Dev &d, int colour, const StepParams &p, bool armsFromDual, cudaStream_t s);
 // Block-Jacobi solve of every dynamic body in the overflow colour (walked in slot order).
 void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s);
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s);

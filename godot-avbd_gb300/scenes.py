@@ -267,6 +267,33 @@ def pile_grace(steps=240, count=250, chain_links=6, grace=4):
     return sc
 
 
+def arm_cache(steps=240, rebuild=0.05):
+    """The mixed scene (a jointed chain on coloured Gauss-Seidel, free boxes on block Jacobi) with
+    the drift-gated arm cache on (Solver::jacobianRebuildDistance, manifold.cpp:600-668)."""
+    sc = mixed(steps=steps)
+    sc.name = "arm_cache"
+    sc.params = dict(BENCH_PARAMS, jacobian_rebuild_distance=rebuild)
+    return sc
+
+
+def arm_cache_pile(steps=120, rebuild=0.02):
+    """A 300-box pile with jointed chains (colours and overflow in one world), arm cache on."""
+    sc = pile(steps=steps, count=300, chain_links=8)
+    sc.name = "arm_cache_pile"
+    sc.params = dict(sc.params, jacobian_rebuild_distance=rebuild)
+    return sc
+
+
+def arm_cache_sleep(steps=300, rebuild=0.05):
+    """The sleepers scene stepped with stepInterleaved(2, 5) and the arm cache on: frozen manifolds
+    keep their captured arms while parked, and the per-substep rebase keeps the cache."""
+    sc = sleepers(steps=steps)
+    sc.name = "arm_cache_sleep"
+    sc.params = dict(sc.params, jacobian_rebuild_distance=rebuild, dt=float(_f(1.0) / _f(120.0)))
+    sc.substeps, sc.rounds = 2, 5
+    return sc
+
+
 def shape_mix(steps=240):
     """Spheres and cylinders with boxes: a sphere pile, standing and lying cylinders, a cylinder
     stack, spheres rolling on a tilted box ramp and against cylinders, and boxes on cylinders."""

@@ -59,12 +59,12 @@ typedef struct avbdg_params {
     float stiffness_decay;        /* penalty decay of dual-only rounds */
     int adaptive_beta;            /* bool */
     float adaptive_beta_error_floor;
-    float convergence_threshold;  /* 0 disables the early exit */
+    float convergence_threshold;  /* 0 disables the early exit; > 0 returns AVBDG_ERR_UNSUPPORTED */
     float jacobi_relaxation;      /* overflow (block-Jacobi) combine factor */
     int contact_only_overflow;    /* bool */
     float stick_drift_heal;
     float max_penetration;
-    float jacobian_rebuild_distance;
+    float jacobian_rebuild_distance; /* > 0: drift-gated world-arm cache (manifold.cpp:600-668) */
     float speculative_margin;
     int position_projection;      /* bool */
     int projection_iterations;

@@ -19,6 +19,7 @@ namespace oracle {
 namespace {
 
 constexpr float kReleaseAbove = COLLISION_MARGIN + CONTACT_RELEASE_GAP;
+constexpr uint8_t kArmsCached = 1;
 constexpr uint8_t kPrimalCacheReady = 2;
 
 } // namespace
@@ -1622,7 +1623,8 @@ void World::manifoldUpdatePrimal(Manifold &m, int body, Block &blk) {
     m.flags = static_cast<uint8_t>(m.flags & ~kPrimalCacheReady);
 }
 
-// ManifoldStore::updateDual (manifold.cpp:583-671), arm cache disabled.
+// ManifoldStore::updateDual (manifold.cpp:583-671), with the drift-gated arm cache
+// (jacobianRebuildDistance, :600-608, 662-667).
 void World::manifoldUpdateDual(Manifold &m) {
     const Body &A = bodies[m.a];
     const Body &B = bodies[m.b];
@@ -1632,13 +1634,25 @@ void World::manifoldUpdateDual(Manifold &m) {
     const V3 dqBAng = qdiff(B.q, B.q0);
     const M3 rotA = qmat(A.q);
     const M3 rotB = qmat(B.q);
+    const bool cacheable = P.jacobian_rebuild_distance > 0.0f;
+    const float rebuild2 = P.jacobian_rebuild_distance * P.jacobian_rebuild_distance;
+    const V3 dA = rotA.c[0] - m.rotACap;
+    const V3 dB = rotB.c[0] - m.rotBCap;
+    const bool driftUsable = cacheable && (m.flags & kArmsCached) != 0 && length2(dA) <= rebuild2 &&
+                             length2(dB) <= rebuild2;
     const bool spec = P.speculative_margin > 0.0f;
     for (int i = 0; i < m.n; i++) {
         Contact &c = m.c[i];
-        const V3 rA = mul(rotA, c.rA);
-        const V3 rB = mul(rotB, c.rB);
-        c.rAW = rA;
-        c.rBW = rB;
+        V3 rA, rB;
+        if (driftUsable) {
+            rA = c.rAW;
+            rB = c.rBW;
+        } else {
+            rA = mul(rotA, c.rA);
+            rB = mul(rotB, c.rB);
+            c.rAW = rA;
+            c.rBW = rB;
+        }
         const V3 bracket = ((dqALin - dqBLin) + cross(dqAAng, rA)) - cross(dqBAng, rB);
         const V3 C = constraintError(c.C0, bracket, m.basis, 1 - P.alpha, spec);
         V3 F = cmul(c.k, C) + c.lam;
@@ -1656,6 +1670,11 @@ void World::manifoldUpdateDual(Manifold &m) {
         V3 fNext = cmul(c.k, C) + c.lam;
         clampForce(fNext, m.mu);
         c.F = fNext;
+    }
+    if (!driftUsable && cacheable) {
+        m.rotACap = rotA.c[0];
+        m.rotBCap = rotB.c[0];
+        m.flags = static_cast<uint8_t>(m.flags | kArmsCached);
     }
     m.flags = static_cast<uint8_t>(m.flags | kPrimalCacheReady);
 }

@@ -94,6 +94,9 @@ struct Manifold {
     float mu = 0;
     int n = 0;
     uint8_t flags = 0;
+    // Arm cache (manifold.hpp:79-80): first columns of the body rotations when the world arms were
+    // last captured by the dual.
+    V3 rotACap{}, rotBCap{};
     // Contact grace (manifold.hpp:76-77): ticks parked without contacts, contacts kept for revival.
     int dormantTicks = 0, dormantSaved = 0;
     Contact c[kMaxContacts];

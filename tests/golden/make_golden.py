@@ -35,6 +35,9 @@ RUNS = [
     ("pile", {"count": 300, "chain_links": 8}, 120),
     ("lattice", {"nx": 8, "ny": 8, "nz": 4}, 90),
     ("shape_mix", {}, 240),
+    ("arm_cache", {}, 240),
+    ("arm_cache_pile", {}, 120),
+    ("arm_cache_sleep", {}, 300),
 ]
 
 

@@ -28,7 +28,7 @@ def test_gpu_reproduces_pinned_digests(pkg, gpu, name):
 
 
 @pytest.mark.parametrize("run", ["stack", "interleaved", "mixed", "hard_chain", "pyramid420", "pile", "lattice",
-                                 "shape_mix"])
+                                 "shape_mix", "arm_cache", "arm_cache_pile", "arm_cache_sleep"])
 def test_gpu_matches_reference_every_step(pkg, gpu, golden, run):
     scenes = pkg.scenes
     rec = golden["runs"][run]
@@ -142,7 +142,7 @@ def test_gpu_edge_cases(pkg, gpu, oracle):
     assert e.value.code == capi.ERR_NONFINITE
     # Unsupported options are reported, never approximated.
     p = gpu.default_params()
-    p.jacobian_rebuild_distance = 0.01
+    p.convergence_threshold = 0.01
     with pytest.raises(capi.AvbdError) as e:
         pkg.world(p)
     assert e.value.code == capi.ERR_UNSUPPORTED

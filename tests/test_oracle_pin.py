@@ -111,7 +111,7 @@ def test_oracle_matches_reference_interleaved_pile(pkg, oracle, ref):
 
 def test_oracle_rejects_unrestated_options(pkg, oracle):
     p = oracle.default_params()
-    p.jacobian_rebuild_distance = 0.01
+    p.convergence_threshold = 0.01
     with pytest.raises(pkg.capi.AvbdError) as e:
         pkg.capi.World(oracle, p)
     assert e.value.code == pkg.capi.ERR_UNSUPPORTED
