@@ -727,8 +727,6 @@ void Engine::uploadCounts() {
 int Engine::setParams(const avbdg_params &p) {
     if (p.iterations < 1 || !(p.dt > 0.0f))
         return fail(AVBDG_ERR_INVALID, "iterations must be >= 1 and dt > 0");
-    if (p.convergence_threshold != 0.0f)
-        return fail(AVBDG_ERR_UNSUPPORTED, "the convergence probe is not on the GPU path");
     if (!(p.jacobian_rebuild_distance >= 0.0f))
         return fail(AVBDG_ERR_INVALID, "jacobian_rebuild_distance must be >= 0");
     if (p.contact_grace_ticks < 0)
@@ -989,8 +987,13 @@ void Engine::runSubstep(const StepParams &sp, int rounds, bool idle) {
             std::clamp(static_cast<int>(std::ceil(P.newton_ratio * static_cast<float>(rounds))), 1, rounds);
     const bool colours = needGreedy();
     const bool inPlace = nForces == 0;
+    // Convergence probe (solver_step.cpp:88, 301-314): after each round but the last, the mean
+    // step-start penetration r (a mean of positive floats, so 0 <= r <= inf) is compared with the
+    // previous probe's, starting from 0; the first probe's 0 - r < threshold holds for every
+    // threshold > 0, so a positive threshold always stops the substep after its first round.
+    const int run = (P.convergence_threshold > 0.0f && rounds > 1) ? 1 : rounds;
     launchStamps(d, sp, false, stream);
-    for (int it = 0; it < rounds; it++) {
+    for (int it = 0; it < run; it++) {
         const bool newton = it < newtonRounds;
         if (newton) {
             if (colours) {

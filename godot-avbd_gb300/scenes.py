@@ -294,6 +294,23 @@ def arm_cache_sleep(steps=300, rebuild=0.05):
     return sc
 
 
+def converge_pile(steps=120, threshold=1e-3):
+    """The 300-box jointed pile with the convergence probe on (Solver::convergenceThreshold,
+    solver_step.cpp:301-314)."""
+    sc = pile(steps=steps, count=300, chain_links=8)
+    sc.name = "converge_pile"
+    sc.params = dict(sc.params, convergence_threshold=threshold)
+    return sc
+
+
+def converge_interleaved(steps=300, threshold=1e-4):
+    """The interleaved stack (stepInterleaved(2, 3)) with the convergence probe on."""
+    sc = interleaved(steps=steps)
+    sc.name = "converge_interleaved"
+    sc.params = dict(sc.params, convergence_threshold=threshold)
+    return sc
+
+
 def shape_mix(steps=240):
     """Spheres and cylinders with boxes: a sphere pile, standing and lying cylinders, a cylinder
     stack, spheres rolling on a tilted box ramp and against cylinders, and boxes on cylinders."""

@@ -59,7 +59,7 @@ typedef struct avbdg_params {
     float stiffness_decay;        /* penalty decay of dual-only rounds */
     int adaptive_beta;            /* bool */
     float adaptive_beta_error_floor;
-    float convergence_threshold;  /* 0 disables the early exit; > 0 returns AVBDG_ERR_UNSUPPORTED */
+    float convergence_threshold;  /* 0 disables the early exit (solver_step.cpp:301-314) */
     float jacobi_relaxation;      /* overflow (block-Jacobi) combine factor */
     int contact_only_overflow;    /* bool */
     float stick_drift_heal;

@@ -2205,6 +2205,7 @@ void World::iterate(int rounds, int forceCount) {
     const int newtonRounds =
             std::clamp(static_cast<int>(std::ceil(P.newton_ratio * static_cast<float>(rounds))), 1, rounds);
     std::vector<V3> dLin(updateOrder.size()), dAng(updateOrder.size());
+    float prevResidual = 0.0f; // solver_step.cpp:88
     for (int it = 0; it < rounds; it++) {
         const bool newton = it < newtonRounds;
         for (int c = 0; newton && c < colourCount; c++) {
@@ -2280,6 +2281,28 @@ void World::iterate(int rounds, int forceCount) {
         for (int f = 0; f < forceCount; f++)
             forceUpdateDual(forces[f]);
         (void)alpha;
+        // Convergence probe (solver_step.cpp:301-314, ManifoldStore::accumulatePenetration,
+        // manifold.cpp:673-691): mean normal penetration of the step-start errors, in live order.
+        if (P.convergence_threshold > 0.0f && it + 1 < rounds) {
+            const bool spec = P.speculative_margin > 0.0f;
+            float total = 0.0f;
+            int cnt = 0;
+            for (const Manifold &m : live)
+                for (int i = 0; i < m.n; i++) {
+                    if (spec && m.c[i].C0.x > 0.0f)
+                        continue;
+                    const float pen = -m.c[i].C0.x;
+                    if (pen > 0.0f) {
+                        total += pen;
+                        cnt++;
+                    }
+                }
+            const float residual = cnt > 0 ? total / static_cast<float>(cnt) : 0.0f;
+            const bool converged = prevResidual - residual < P.convergence_threshold;
+            prevResidual = residual;
+            if (converged)
+                break;
+        }
     }
 }
 

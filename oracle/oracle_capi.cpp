@@ -21,8 +21,6 @@ int fail(int code, const char *msg) {
 
 // The option set this restatement covers; anything else is reported, not approximated.
 int checkParams(const avbdg_params &p) {
-    if (p.convergence_threshold != 0.0f)
-        return fail(AVBDG_ERR_UNSUPPORTED, "convergence_threshold > 0 is not restated");
     if (p.iterations < 1 || !(p.dt > 0.0f))
         return fail(AVBDG_ERR_INVALID, "iterations must be >= 1 and dt > 0");
     return AVBDG_OK;

@@ -38,6 +38,8 @@ RUNS = [
     ("arm_cache", {}, 240),
     ("arm_cache_pile", {}, 120),
     ("arm_cache_sleep", {}, 300),
+    ("converge_pile", {}, 120),
+    ("converge_interleaved", {}, 300),
 ]
 
 

@@ -6,6 +6,7 @@ position, orientation and both velocities), and the integer stages (candidate pa
 sorted order, manifold contact counts and feature keys, colouring) must be identical.
 """
 
+import ctypes
 import hashlib
 
 import numpy as np
@@ -28,7 +29,8 @@ def test_gpu_reproduces_pinned_digests(pkg, gpu, name):
 
 
 @pytest.mark.parametrize("run", ["stack", "interleaved", "mixed", "hard_chain", "pyramid420", "pile", "lattice",
-                                 "shape_mix", "arm_cache", "arm_cache_pile", "arm_cache_sleep"])
+                                 "shape_mix", "arm_cache", "arm_cache_pile", "arm_cache_sleep", "converge_pile",
+                                 "converge_interleaved"])
 def test_gpu_matches_reference_every_step(pkg, gpu, golden, run):
     scenes = pkg.scenes
     rec = golden["runs"][run]
@@ -140,12 +142,17 @@ def test_gpu_edge_cases(pkg, gpu, oracle):
     with pytest.raises(capi.AvbdError) as e:
         pkg.world().add_bodies(bad)
     assert e.value.code == capi.ERR_NONFINITE
-    # Unsupported options are reported, never approximated.
-    p = gpu.default_params()
-    p.convergence_threshold = 0.01
-    with pytest.raises(capi.AvbdError) as e:
-        pkg.world(p)
-    assert e.value.code == capi.ERR_UNSUPPORTED
+    # Unknown force kinds are reported, never approximated.
+    batch = capi.Batch(gpu.lib)
+    two = scenes.stack()
+    two.joints = [(1, 2, (0, 0, 0.5), (0, 0, -0.5), 1000.0, 0.0, float("inf"))]
+    descs = capi.scene_body_descs(two)
+    forces = capi.make_force_descs(two.joints)
+    forces[0].kind = 7
+    out = ctypes.c_int()
+    rc = batch.fn["batch_add_world"](batch.handle, two.n, descs, 1, forces, ctypes.byref(out))
+    assert rc == capi.ERR_UNSUPPORTED
+    batch.close()
 
 
 @pytest.mark.parametrize("graphs", [True, False])

@@ -109,12 +109,25 @@ def test_oracle_matches_reference_interleaved_pile(pkg, oracle, ref):
         assert wo.digest() == wr.digest(), f"step {s + 1}"
 
 
-def test_oracle_rejects_unrestated_options(pkg, oracle):
-    p = oracle.default_params()
-    p.convergence_threshold = 0.01
-    with pytest.raises(pkg.capi.AvbdError) as e:
-        pkg.capi.World(oracle, p)
-    assert e.value.code == pkg.capi.ERR_UNSUPPORTED
+def test_oracle_convergence_probe_stops_after_one_round(pkg, oracle, ref):
+    """The probe starts from a previous residual of 0 and the residual is a mean of positive
+    penetrations, so any positive threshold stops each substep after its first round: a run at 10
+    iterations with the probe on equals a run at 1 iteration, on the oracle and on the reference."""
+    scenes = pkg.scenes
+    sc = scenes.converge_pile(steps=0)
+    one = scenes.converge_pile(steps=0)
+    one.params = dict(one.params, convergence_threshold=0.0, iterations=1)
+    for api in (oracle, ref):
+        p = api.default_params()
+        p.threads = 1  # two thread pools in one process would oversubscribe the host
+        a = scenes.instantiate(api, sc, params=p)
+        p = api.default_params()
+        p.threads = 1
+        b = scenes.instantiate(api, one, params=p)
+        for s in range(40):
+            a.step()
+            b.step()
+            assert a.digest() == b.digest(), f"step {s + 1}"
 
 
 def _query_rays(n=64, seed=4):
