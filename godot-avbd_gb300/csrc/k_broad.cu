@@ -65,21 +65,33 @@ __global__ void boundsResetKernel(Dev d, int *wBounds) {
     }
 }
 
+// Per-world min/max of the AABB centres. Lanes of a warp reduce per world first (worlds are slot
+// ranges, so a warp mostly holds one), and one lane per world and warp does the atomics: a single
+// large world would otherwise serialise six atomics per body on six addresses.
 __global__ void boundsKernel(Dev d, int *wBounds) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n)
+    const int w = g < n ? d.meta[g].x : -1;
+    int v[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, static_cast<int>(0x80000000), static_cast<int>(0x80000000),
+                static_cast<int>(0x80000000)};
+    if (w >= 0) {
+        const float4 c = d.aabbC[g];
+        v[0] = v[3] = orderedInt(c.x);
+        v[1] = v[4] = orderedInt(c.y);
+        v[2] = v[5] = orderedInt(c.z);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, w);
+    int r[6];
+    for (int k = 0; k < 3; k++) {
+        r[k] = __reduce_min_sync(peers, v[k]);
+        r[k + 3] = __reduce_max_sync(peers, v[k + 3]);
+    }
+    if (w < 0 || (threadIdx.x & 31) != __ffs(peers) - 1)
         return;
-    const int w = d.meta[g].x;
-    if (w < 0)
-        return;
-    const float4 c = d.aabbC[g];
-    atomicMin(&wBounds[6 * w + 0], orderedInt(c.x));
-    atomicMin(&wBounds[6 * w + 1], orderedInt(c.y));
-    atomicMin(&wBounds[6 * w + 2], orderedInt(c.z));
-    atomicMax(&wBounds[6 * w + 3], orderedInt(c.x));
-    atomicMax(&wBounds[6 * w + 4], orderedInt(c.y));
-    atomicMax(&wBounds[6 * w + 5], orderedInt(c.z));
+    for (int k = 0; k < 3; k++) {
+        atomicMin(&wBounds[6 * w + k], r[k]);
+        atomicMax(&wBounds[6 * w + 3 + k], r[k + 3]);
+    }
 }
 
 __device__ __forceinline__ uint64_t expandBits21(uint32_t v) {

@@ -74,7 +74,9 @@ __device__ __forceinline__ void projActiveAt(Dev d, int m) {
     const bool active = n > 0 && (movable(d, ab.x) || movable(d, ab.y));
     uint8_t spec = 0;
     if (active) {
-        atomicAdd(&d.wActive[d.meta[ab.x].x], 1);
+        int *flag = &d.wActive[d.meta[ab.x].x]; // a flag: one store, no atomic traffic on a shared word
+        if (*flag == 0)
+            *flag = 1;
         const f3 nrm = xyz(L.b0[m]);
         const f3 xa = xyz(d.x[ab.x]), xb = xyz(d.x[ab.y]);
         const q4 qa = asq(d.q[ab.x]), qb = asq(d.q[ab.y]);
@@ -286,7 +288,9 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
 
 // ---- positional projection (solver_projection.cpp:169-280) ----
 
-__device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m) {
+// Returns the patch's mean depth bits for the world's early-exit maximum through `depthBits`
+// (left alone when the manifold corrects nothing).
+__device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &world, int &depthBits) {
     if (m >= d.ctr[C_LIVE])
         return;
     const ManifoldBuf L = d.live;
@@ -327,7 +331,8 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m) {
     if (corrected == 0)
         return;
     const float invN = 1.0f / static_cast<float>(corrected);
-    atomicMax(&d.wMaxDepth[w], __float_as_int(patchDepth * invN));
+    world = w;
+    depthBits = __float_as_int(patchDepth * invN); // positive: the bits order like the floats
     const f3 IA = xyz(d.moment[a]), IB = xyz(d.moment[b]);
     const f3 tA = moveA ? qrot(qconj(qa), cross(scale(patchRA, invN), nrm)) : f3{0, 0, 0};
     const f3 tB = moveB ? qrot(qconj(qb), cross(scale(patchRB, invN), nrm)) : f3{0, 0, 0};
@@ -344,10 +349,19 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m) {
     }
 }
 
+// Grid-stride in whole warps (every lane runs every pass), so the per-world depth maximum is
+// reduced across the warp first and one lane per world and warp does the atomic.
 __global__ void projManifoldKernel(Dev d, StepParams p) {
     const int n = d.ctr[C_LIVE];
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
-        projManifoldAt(d, p, m);
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        int world = -1, depthBits = 0;
+        projManifoldAt(d, p, base + (threadIdx.x & 31), world, depthBits);
+        const unsigned peers = __match_any_sync(0xffffffffu, world);
+        const int deepest = __reduce_max_sync(peers, depthBits);
+        if (world >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1)
+            atomicMax(&d.wMaxDepth[world], deepest);
+    }
 }
 
 __global__ void projBodyKernel(Dev d, StepParams p) {
