@@ -40,6 +40,19 @@ import __graft_entry__ as entry  # noqa: E402
 
 METRIC = "body-steps/s @10 iters"
 UNIT = "body-steps/s"
+
+
+def max_over_ranks(x, world_size):
+    """The largest value of x over all ranks: the job takes as long as its slowest rank. The tensor
+    lives where the process group's backend wants it (GPU for NCCL, host for gloo)."""
+    if world_size <= 1:
+        return x
+    import torch
+
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -210,10 +223,7 @@ def run_gpu(args, rank, world_size):
     kt = w.take_kernel_times()
     w.set_profiling(False)
     total_ms = float(sum(step_ms))
-    if world_size > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world_size)
     body_steps = sc.dynamic * args.steps * world_size
     value = body_steps / (total_ms / 1e3)
 
@@ -228,10 +238,7 @@ def run_gpu(args, rank, world_size):
         p, q, v, av = w.state()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if world_size > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world_size)
     e2e = {"value": body_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     peak, peak_kind = measured_peak_hbm()
@@ -309,10 +316,7 @@ def run_batch(args, rank, world_size):
     kt = batch.take_kernel_times()
     batch.set_profiling(False)
     total_ms = float(sum(step_ms))
-    if world_size > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world_size)
     value = dynamic * args.steps * world_size / (total_ms / 1e3)
     st = batch.stats()
 
@@ -344,10 +348,7 @@ def run_batch(args, rank, world_size):
         batch.step()
         state = batch.state_all(state)
     e2e_s = time.perf_counter() - t0
-    if world_size > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world_size)
     nbytes = 13 * 4 * sum(w.n for w in worlds)
     e2e = {"value": dynamic * e2e_steps * world_size / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes}
