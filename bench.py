@@ -391,6 +391,10 @@ def run_batch(args, rank, world_size):
                                "sample": f"{done} world-steps (worlds stepped one at a time, steps "
                                          f"{args.warmup + 1}-{args.warmup + args.steps}), {elapsed:.1f} s of CPU "
                                          f"step time, all {cores} threads"}
+        v1, kind1, done1, elapsed1, _ = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=10.0,
+                                                            threads=1)
+        out["cpu_baseline_1thread"] = {"value": v1, "unit": UNIT, "cores": 1, "kind": kind1,
+                                       "sample": f"{done1} world-steps, same sampling, {elapsed1:.1f} s, one thread"}
     return out
 
 
@@ -504,18 +508,19 @@ def run_serve(args, rank, world_size, standalone=True):
     return out
 
 
-def run_cpu_batch_sample(worlds, warmup, steps, budget_s):
+def run_cpu_batch_sample(worlds, warmup, steps, budget_s, threads=0):
     """The reference's CPU step over the batch's worlds, one world at a time with all host threads
-    (how the reference would serve them), on a bounded sample of worlds."""
+    (threads=0, how the reference would serve them) or the given count, on a bounded sample of
+    worlds."""
     import numpy as np
 
     rng = np.random.default_rng(2)
     order = rng.permutation(len(worlds))
     body_steps, elapsed, done, kind = 0, 0.0, 0, "port"
-    cores = os.cpu_count() or 1
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
     for i in order:
         sc = worlds[i]
-        v, kind, n_done, t = run_cpu_reference(sc, steps, warmup, 0)
+        v, kind, n_done, t = run_cpu_reference(sc, steps, warmup, threads)
         body_steps += sc.dynamic * n_done
         elapsed += t
         done += n_done
