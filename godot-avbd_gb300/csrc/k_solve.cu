@@ -350,7 +350,9 @@ __device__ __forceinline__ void zeroAcc(SideAcc &a) {
 
 // block += stamp (full 3x3 adds, as the reference adds its accumulators).
 __device__ __forceinline__ void addStamp(Blk &b, const float4 *src) {
-    const float4 s0 = src[0], s1 = src[1], s2 = src[2], s3 = src[3], s4 = src[4], s5 = src[5], s6 = src[6];
+    // Stamps are read-only while bodies solve: the read-only path.
+    const float4 s0 = __ldg(src), s1 = __ldg(src + 1), s2 = __ldg(src + 2), s3 = __ldg(src + 3), s4 = __ldg(src + 4),
+                 s5 = __ldg(src + 5), s6 = __ldg(src + 6);
     const m3 lin = mcols(f3{s0.x, s0.y, s0.z}, f3{s0.y, s0.w, s1.x}, f3{s0.z, s1.x, s1.y});
     const m3 ang = mcols(f3{s2.y, s2.z, s2.w}, f3{s2.z, s3.x, s3.y}, f3{s2.w, s3.y, s3.z});
     const m3 crs = mcols(f3{s4.z, s4.w, s5.x}, f3{s5.y, s5.z, s5.w}, f3{s6.x, s6.y, s6.z});
@@ -374,6 +376,18 @@ __device__ __forceinline__ Pose loadPose(const Dev &d, int g) {
     p.q = asq(d.q[g]);
     p.dLin = sub(p.x, xyz(d.x0[g]));
     p.dAng = qdiff(p.q, asq(d.q0[g]));
+    p.rot = qmat(p.q);
+    return p;
+}
+
+// loadPose through the read-only path, for kernels that write no pose.
+__device__ __forceinline__ Pose loadPoseRO(const Dev &d, int g) {
+    Pose p;
+    const float4 x4 = __ldg(&d.x[g]);
+    p.x = xyz(x4);
+    p.q = asq(__ldg(&d.q[g]));
+    p.dLin = sub(p.x, xyz(__ldg(&d.x0[g])));
+    p.dAng = qdiff(p.q, asq(__ldg(&d.q0[g])));
     p.rot = qmat(p.q);
     return p;
 }
@@ -477,18 +491,18 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
     const int live = d.ctr[C_LIVE];
     const ManifoldBuf L = d.live;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x) {
-        const int2 ab = L.ab[m];
+        const int2 ab = __ldg(&L.ab[m]);
         if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
             continue; // frozen (manifold.cpp:168-172)
         bool touches = false;
         int sides = STAMPS ? overflowSides(d, ab, touches) : 0;
         if (touches)
             sides = 0; // recomputed after the colour passes
-        const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
-        const float4 b04 = L.b0[m];
-        const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+        const Pose A = loadPoseRO(d, ab.x), B = loadPoseRO(d, ab.y);
+        const float4 b04 = __ldg(&L.b0[m]);
+        const f3 r0 = xyz(b04), r1 = xyz(__ldg(&L.b1[m])), r2 = xyz(__ldg(&L.b2[m]));
         const float mu = b04.w;
-        const int n = L.count[m];
+        const int n = __ldg(&L.count[m]);
         // Drift-gated arm reuse (manifold.cpp:600-608): under the rotation threshold the cached
         // world arms stand in for the current ones.
         bool driftUsable = false;
@@ -504,21 +518,21 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
         zeroAcc(sb);
         for (int c = 0; c < n; c++) {
             const int ci = cslot(d, m, c);
-            const float4 rA4 = L.rA[ci];
+            const float4 rA4 = __ldg(&L.rA[ci]);
             f3 rAw, rBw;
             if (driftUsable) {
                 rAw = xyz(L.armA[ci]);
                 rBw = xyz(L.armB[ci]);
             } else {
                 rAw = mul(A.rot, xyz(rA4));
-                rBw = mul(B.rot, xyz(L.rB[ci]));
+                rBw = mul(B.rot, xyz(__ldg(&L.rB[ci])));
                 if (ARM) {
                     L.armA[ci] = f4(rAw, 0.0f);
                     L.armB[ci] = f4(rBw, 0.0f);
                 }
             }
             const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
-            const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
+            const f3 C = contactError(p, xyz(__ldg(&L.C0[ci])), bracket, r0, r1, r2);
             f3 k = xyz(L.k[ci]);
             if (decay < 1.0f)
                 k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
@@ -730,7 +744,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             continue;
         }
         const int m = seq - nf;
-        const int side = d.live.ab[m].x == g ? 0 : 1;
+        const int side = __ldg(&d.live.ab[m].x) == g ? 0 : 1;
         if (RECOMPUTE) {
             // Same floats as stampsKernel for one side, summed straight into the block.
             const ManifoldBuf L = d.live;
