@@ -295,11 +295,15 @@ __device__ __forceinline__ bool overlapClosed(f3 aMin, f3 aMax, f3 bMin, f3 bMax
 }
 
 // Walk the world's tree with body g's box; emit partners with a larger list position.
+// Threads take bodies in tree (Morton) order, so a warp's walks follow nearby paths.
 template <bool EMIT>
 __global__ void traverseKernel(Dev d) {
     const int n = d.ctr[C_BODIES];
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const int g = d.leafBody[i];
+    if (g < 0)
         return;
     const int w = d.meta[g].x;
     if (w < 0)
