@@ -144,6 +144,8 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.specList, mm);
     take(n.specPred, mm);
     take(n.solveFail, nb);
+    take(n.pairStash, static_cast<size_t>(nb) * kPairStash);
+    take(n.pairSpill, nb);
     take(n.projLin, 2 * static_cast<size_t>(mm));
     take(n.projAng, 2 * static_cast<size_t>(mm));
     take(n.dLin, nb);

@@ -25,6 +25,7 @@ constexpr int kMaxColours = 8;
 constexpr uint8_t kOverflowColour = 8;
 constexpr uint8_t kUncoloured = 255;
 constexpr int kStampF4 = 7; // float4 per (manifold, side) stamp
+constexpr int kPairStash = 16; // partners kept per body by the counting walk
 constexpr int kExtF4 = 16;  // float4 per force of the generic-joint record (forces.cuh)
 
 constexpr float PENALTY_MIN = 1.0f;
@@ -49,6 +50,7 @@ enum Counter {
     C_ERRORS,         // capacity / timeout bits (kErr*)
     C_ONE,            // constant 1 (scan length helper)
     C_SOLVEFAIL,      // overflow bodies whose plain LDLT failed this round (solveFail)
+    C_PAIRSPILL,      // bodies with more broad-phase partners than the stash holds (pairSpill)
     C_TMP,
     C_COUNT
 };
@@ -129,6 +131,8 @@ struct Dev {
     uint8_t *mSpec, *mDone; // brake: candidate flag per manifold, done flag per candidate
     int *specList;
     int *solveFail;         // overflow bodies left to the pivoted fallback this round
+    int *pairStash;         // broad phase: first kPairStash partners' list positions per body list position
+    int *pairSpill;         // broad phase: bodies whose partners overflow the stash (walked again)
     int2 *specPred;         // brake: candidate index of the preceding candidate on each movable body (-1 = none)
     float4 *projLin, *projAng; // projection contributions per (manifold, side)
     float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)

@@ -294,15 +294,18 @@ __device__ __forceinline__ bool overlapClosed(f3 aMin, f3 aMax, f3 bMin, f3 bMax
              aMin.z > bMax.z);
 }
 
-// Walk the world's tree with body g's box; emit partners with a larger list position.
-// Threads take bodies in tree (Morton) order, so a warp's walks follow nearby paths.
+// Walk the world's tree with body g's box for partners with a larger list position.
+// COUNT: threads take bodies in tree (Morton) order, so a warp's walks follow nearby paths; each
+// counts its partners and keeps the first kPairStash of them, and a body with more is listed for
+// a second walk. EMIT (that second walk): the listed bodies write their partners into their
+// segments. Pair keys are (lpA << 32 | lpB); the segmented sort orders each segment afterwards.
 template <bool EMIT>
 __global__ void traverseKernel(Dev d) {
-    const int n = d.ctr[C_BODIES];
+    const int n = EMIT ? d.ctr[C_PAIRSPILL] : d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
-    const int g = d.leafBody[i];
+    const int g = EMIT ? d.pairSpill[i] : d.leafBody[i];
     if (g < 0)
         return;
     const int w = d.meta[g].x;
@@ -312,6 +315,7 @@ __global__ void traverseKernel(Dev d) {
     const int lpA = listPos(d, g);
     int out = EMIT ? d.pairStart[lpA] : 0;
     int found = 0;
+    int *stash = d.pairStash + static_cast<size_t>(lpA) * kPairStash;
     if (cnt >= 2) {
         const float4 c4 = d.aabbC[g], h4 = d.aabbH[g];
         const f3 aMin{c4.x - h4.x, c4.y - h4.y, c4.z - h4.z};
@@ -337,6 +341,8 @@ __global__ void traverseKernel(Dev d) {
                             if (out < d.PP)
                                 d.pairs[out] = (static_cast<uint64_t>(lpA) << 32) | static_cast<uint32_t>(lpB);
                             out++;
+                        } else if (found < kPairStash) {
+                            stash[found] = lpB;
                         }
                         found++;
                     }
@@ -354,8 +360,26 @@ __global__ void traverseKernel(Dev d) {
             }
         }
     }
-    if (!EMIT)
+    if (!EMIT) {
         d.pairStart[lpA] = found;
+        if (found > kPairStash)
+            d.pairSpill[atomicAdd(&d.ctr[C_PAIRSPILL], 1)] = g;
+    }
+}
+
+// Stashed partners into their body's segment (bodies with more partners are walked again).
+__global__ void pairStashKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
+    const int lpA = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lpA >= n)
+        return;
+    const int start = d.pairStart[lpA], found = d.pairStart[lpA + 1] - start;
+    if (found > kPairStash)
+        return;
+    const int *stash = d.pairStash + static_cast<size_t>(lpA) * kPairStash;
+    for (int j = 0; j < found; j++)
+        if (start + j < d.PP)
+            d.pairs[start + j] = (static_cast<uint64_t>(lpA) << 32) | static_cast<uint32_t>(stash[j]);
 }
 
 __global__ void pairTotalKernel(Dev d) {
@@ -484,9 +508,11 @@ void launchRefit(const Dev &d, cudaStream_t s) {
 
 void launchPairs(const Dev &d, int block, cudaStream_t s) {
     cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
+    cudaMemsetAsync(d.ctr + C_PAIRSPILL, 0, sizeof(int), s);
     ++launchCount(); traverseKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d);
     scanExclusive(d.pairStart, d.pairStart, d.NB + 1, nullptr, d.ctr + C_TMP, d.scanScratch, s);
     ++launchCount(); pairTotalKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); pairStashKernel<<<divUp(d.NB, kThreads), kThreads, 0, s>>>(d);
     ++launchCount(); traverseKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d);
     segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
 }
