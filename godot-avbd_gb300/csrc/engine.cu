@@ -169,6 +169,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     const size_t adjCap = 2 * (static_cast<size_t>(ff) + mm);
     take(n.adjSeq, adjCap);
     take(n.adjTmp, adjCap);
+    take(n.adjInfo, adjCap);
     take(n.colourList, static_cast<size_t>(nb) * (kMaxColours + 1));
     take(n.colourCount, kMaxColours + 1);
     take(n.ctr, C_COUNT);

@@ -144,6 +144,7 @@ struct Dev {
     // adjacency (dynamic bodies only): sequence numbers, forces first (list order) then manifolds
     int *adjStart, *adjFill;
     uint32_t *adjSeq, *adjTmp;
+    int *adjInfo;           // per adjacency entry: the other body (kNoBody: none) | side (0: body is a, 1: b) << 31
     // colouring
     int *colourList, *colourCount; // per colour c: bodies with colour c (c = 0..8)
     // scratch
@@ -175,6 +176,13 @@ __device__ __forceinline__ int listPos(const Dev &d, int g) {
 __device__ __forceinline__ bool isDynamic(const Dev &d, int g) { return d.x[g].w > 0.0f; }
 // Movable and not asleep (ManifoldStore::frozen's `awake`, manifold.cpp:168-172).
 __device__ __forceinline__ bool isAwake(const Dev &d, int g) { return d.x[g].w > 0.0f && d.sleep[g].x == 0; }
+// Adjacency entry info: the other body of the entry's force or manifold and this body's side.
+constexpr int kNoBody = 0x7fffffff;
+__device__ __forceinline__ int adjInfoOther(int v) {
+    const int o = v & 0x7fffffff;
+    return o == kNoBody ? -1 : o;
+}
+__device__ __forceinline__ int adjInfoSide(int v) { return static_cast<int>(static_cast<unsigned>(v) >> 31); }
 // In this step's update set (solved, braked, projected).
 __device__ __forceinline__ bool inUpdate(const Dev &d, int g) { return d.upd[g] != 0; }
 constexpr uint8_t kNotUpdated = 10; // colour of a movable body outside the update set

@@ -391,25 +391,6 @@ __global__ void pairTotalKernel(Dev d) {
     d.ctr[C_PAIRS] = t;
 }
 
-// The other body of adjacency entry `seq` of body x, or -1.
-__device__ __forceinline__ int adjOther(const Dev &d, uint32_t seq, int x, int nForces) {
-    int a, b;
-    if (static_cast<int>(seq) < nForces) {
-        const int2 ab = d.fAB[nForces - 1 - static_cast<int>(seq)];
-        a = ab.x;
-        b = ab.y;
-    } else {
-        const int2 ab = d.live.ab[static_cast<int>(seq) - nForces];
-        a = ab.x;
-        b = ab.y;
-    }
-    if (a == x)
-        return b;
-    if (b == x)
-        return a;
-    return -1;
-}
-
 // pairOverlaps (solver_broadphase.cpp:30-65): bounds, layer/mask, not constrained, not both static.
 __device__ __forceinline__ void filterAt(Dev d, int k) {
     const int np = d.ctr[C_PAIRS];
@@ -431,9 +412,8 @@ __device__ __forceinline__ void filterAt(Dev d, int k) {
         // The relation is symmetric; only dynamic bodies carry adjacency lists.
         const int xb = dynA ? a : b;
         const int yb = dynA ? b : a;
-        const int nf = d.ctr[C_FORCES];
         for (int e = d.adjStart[xb]; e < d.adjStart[xb + 1]; e++)
-            if (adjOther(d, d.adjSeq[e], xb, nf) == yb) {
+            if (adjInfoOther(d.adjInfo[e]) == yb) {
                 constrained = true;
                 break;
             }

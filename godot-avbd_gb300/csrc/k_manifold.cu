@@ -66,27 +66,29 @@ __global__ void adjFillKernel(Dev d) {
         d.adjSeq[d.adjStart[ab.y] + atomicAdd(&d.adjFill[ab.y], 1)] = seq;
 }
 
+// Each entry's other body and side, once per adjacency build, so the per-round passes need no
+// load of the force's or manifold's body pair to find them.
+__global__ void adjInfoKernel(Dev d) {
+    const int n = d.ctr[C_BODIES];
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n)
+        return;
+    const int nf = d.ctr[C_FORCES];
+    for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
+        const int seq = static_cast<int>(d.adjSeq[e]);
+        const int2 ab = seq < nf ? d.fAB[nf - 1 - seq] : d.live.ab[seq - nf];
+        const int side = ab.x == g ? 0 : 1;
+        const int other = side == 0 ? ab.y : ab.x;
+        d.adjInfo[e] = (other >= 0 ? other : kNoBody) | static_cast<int>(static_cast<unsigned>(side) << 31);
+    }
+}
+
 __global__ void adjTotalKernel(Dev d) {
     if (d.ctr[C_ADJ] > 2 * (d.FF + d.MM))
         atomicOr(&d.ctr[C_ERRORS], kErrAdjacency);
 }
 
 // ---- manifold initialize (ManifoldStore::initialize, manifold.cpp:237-435) ----
-
-__device__ __forceinline__ void basisHessian(f3 b0, f3 b1, f3 b2, f3 k, float S[6]) {
-    const float b0x2 = b0.x * b0.x, b0y2 = b0.y * b0.y, b0z2 = b0.z * b0.z;
-    const float b0xy = b0.x * b0.y, b0xz = b0.x * b0.z, b0yz = b0.y * b0.z;
-    const float b1x2 = b1.x * b1.x, b1y2 = b1.y * b1.y, b1z2 = b1.z * b1.z;
-    const float b1xy = b1.x * b1.y, b1xz = b1.x * b1.z, b1yz = b1.y * b1.z;
-    const float b2x2 = b2.x * b2.x, b2y2 = b2.y * b2.y, b2z2 = b2.z * b2.z;
-    const float b2xy = b2.x * b2.y, b2xz = b2.x * b2.z, b2yz = b2.y * b2.z;
-    S[0] = k.x * b0x2 + k.y * b1x2 + k.z * b2x2;
-    S[1] = k.x * b0xy + k.y * b1xy + k.z * b2xy;
-    S[2] = k.x * b0xz + k.y * b1xz + k.z * b2xz;
-    S[3] = k.x * b0y2 + k.y * b1y2 + k.z * b2y2;
-    S[4] = k.x * b0yz + k.y * b1yz + k.z * b2yz;
-    S[5] = k.x * b0z2 + k.y * b1z2 + k.z * b2z2;
-}
 
 // mul(basis, v) with the basis stored as rows.
 __device__ __forceinline__ f3 basisMul(f3 r0, f3 r1, f3 r2, f3 v) {
@@ -464,6 +466,7 @@ void launchAdjacency(const Dev &d, cudaStream_t s) {
     ++launchCount(); adjTotalKernel<<<1, 1, 0, s>>>(d);
     ++launchCount(); adjFillKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
     segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
+    ++launchCount(); adjInfoKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
 }
 
 void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block, cudaStream_t s) {

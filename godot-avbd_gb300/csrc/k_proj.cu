@@ -379,7 +379,7 @@ __global__ void projBodyKernel(Dev d, StepParams p) {
         if (seq < nf)
             continue;
         const int m = seq - nf;
-        const int side = d.live.ab[m].x == g ? 0 : 1;
+        const int side = adjInfoSide(d.adjInfo[e]);
         const float4 cl = d.projLin[2 * m + side];
         if (cl.w == 0.0f)
             continue;

@@ -27,12 +27,6 @@ int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
 __device__ __forceinline__ int sleepMode(const Dev &d, int g) { return (d.meta[g].w >> 16) & 0x3; }
 
-__device__ __forceinline__ int otherOf(const Dev &d, uint32_t seq, int x, int nf) {
-    const int2 ab = static_cast<int>(seq) < nf ? d.fAB[nf - 1 - static_cast<int>(seq)]
-                                               : d.live.ab[static_cast<int>(seq) - nf];
-    return ab.x == x ? ab.y : (ab.y == x ? ab.x : -1);
-}
-
 __device__ __forceinline__ int2 pairBodies(const Dev &d, int k) {
     const uint64_t key = d.pairs[k];
     return make_int2(d.lpToBody[static_cast<int>(key >> 32)], d.lpToBody[static_cast<int>(key & 0xffffffffu)]);
@@ -99,9 +93,8 @@ __global__ void wakeNeighboursKernel(Dev d, StepParams p) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= d.ctr[C_BODIES] || d.meta[g].x < 0 || !d.sleep[g].x || sleepMode(d, g) != 1)
         return;
-    const int nf = d.ctr[C_FORCES];
     for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
-        const int o = otherOf(d, d.adjSeq[e], g, nf);
+        const int o = adjInfoOther(d.adjInfo[e]);
         if (o < 0 || !(d.x[o].w > 0.0f) || d.sleep[o].x)
             continue;
         if (length2(xyz(d.v[o])) > p.sleepLin2 || length2(xyz(d.w[o])) > p.sleepAng2) {

@@ -744,7 +744,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             continue;
         }
         const int m = seq - nf;
-        const int side = __ldg(&d.live.ab[m].x) == g ? 0 : 1;
+        const int side = adjInfoSide(__ldg(&d.adjInfo[e]));
         if (RECOMPUTE) {
             // Same floats as stampsKernel for one side, summed straight into the block.
             const ManifoldBuf L = d.live;
@@ -996,24 +996,6 @@ __global__ void contactOnlyMarkKernel(Dev d) {
     d.wColour[d.meta[ab.y].x] = 1;
 }
 
-__device__ __forceinline__ int adjOtherSolve(const Dev &d, uint32_t seq, int x, int nf) {
-    int a, b;
-    if (static_cast<int>(seq) < nf) {
-        const int2 ab = d.fAB[nf - 1 - static_cast<int>(seq)];
-        a = ab.x;
-        b = ab.y;
-    } else {
-        const int2 ab = d.live.ab[static_cast<int>(seq) - nf];
-        a = ab.x;
-        b = ab.y;
-    }
-    if (a == x)
-        return b;
-    if (b == x)
-        return a;
-    return -1;
-}
-
 // One Jones-Plassmann attempt with list-order priority: a body is coloured once every earlier
 // (lower list position) neighbour in the update set is, with the smallest colour none of them
 // uses (the sequential greedy of colourGraph, reproduced exactly). A body still waiting counts
@@ -1040,7 +1022,6 @@ constexpr long long kColourSpinLimit = 4000000; // ~0.3 s of 64 ns sleeps per wa
 // whatever their greedy colour, so they are not coloured at all (unless every body is coloured).
 __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int everyWorld) {
     const int n = d.ctr[C_BODIES];
-    const int nf = d.ctr[C_FORCES];
     const int stride = gridDim.x * blockDim.x;
     volatile int *errors = d.ctr + C_ERRORS;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
@@ -1053,7 +1034,7 @@ __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int ev
         }
         unsigned used = 0;
         for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
-            const int h = adjOtherSolve(d, d.adjSeq[e], g, nf);
+            const int h = adjInfoOther(d.adjInfo[e]);
             if (h < 0 || !inUpdate(d, h) || listPos(d, h) >= p)
                 continue;
             unsigned c;
