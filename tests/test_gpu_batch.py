@@ -56,3 +56,34 @@ def test_batch_digests_equal_single_world_gpu(pkg, gpu):
     single.step(240)
     assert batch.digest(1) == single.digest() == scenes.PINNED_DIGESTS["mixed"]
     assert batch.digest(0) == batch.digest(2)
+
+
+def test_full_size_batch_worlds_match_alone(pkg, gpu, oracle):
+    """The bench's 4096-world batch (433k bodies) at full size: sampled worlds after 8 steps in the
+    batch equal the same worlds stepped alone, on the GPU (the largest, the smallest and a spread
+    between) and on the oracle (two of them), bit for bit."""
+    capi, scenes = pkg.capi, pkg.scenes
+    worlds = scenes.batch(worlds=4096, seed=7)
+    p = gpu.default_params()
+    scenes.apply_params(p, scenes.BENCH_PARAMS)
+    batch = capi.Batch(pkg.load_library(), p, max_worlds=len(worlds), max_bodies=sum(w.n for w in worlds),
+                       max_forces=max(1, sum(len(w.joints) for w in worlds)))
+    for w in worlds:
+        batch.add_scene(w)
+    batch.step(8)
+    sizes = np.array([w.n for w in worlds])
+    picks = sorted({int(sizes.argmax()), int(sizes.argmin()), 0, 1, 2047, 4095, 3000, 1234})
+    for i in picks:
+        sc = worlds[i]
+        sc.params = dict(scenes.BENCH_PARAMS)
+        alone = scenes.instantiate(gpu, sc)
+        alone.step(8)
+        assert batch.digest(i) == alone.digest(), f"world {i} ({sc.n} bodies)"
+    for i in (int(sizes.argmin()), 1234):
+        ref = scenes.instantiate(oracle, worlds[i])
+        ref.step(8)
+        for x, y in zip(batch.state(i), ref.state()):
+            assert np.array_equal(x, y), f"world {i} vs the oracle"
+    st = batch.stats()
+    assert st.bodies == int(sizes.sum())
+    batch.close()
