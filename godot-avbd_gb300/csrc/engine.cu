@@ -4,9 +4,16 @@
 #include "engine_host.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <type_traits>
+#include <unistd.h>
+#include <vector>
 
 #include "kernels.cuh"
 #include "prims.cuh"
@@ -1205,6 +1212,117 @@ int Engine::collectAabb(int w, const float lo[3], const float hi[3], uint32_t ma
     return cudaCheck("collectAabb");
 }
 
+namespace {
+
+// Host copies of body state between the caller's arrays and the pinned staging buffer, split over
+// the host's cores for large transfers (one core's memcpy is far slower than the link). `check`
+// also reports a non-finite value in the copied range.
+struct HostCopy {
+    float *dst;
+    const float *src;
+    size_t count;
+    bool check;
+};
+
+// A process-wide pool of copy threads, started on first use and kept (never joined: it lives
+// until the process ends), so a transfer pays no thread start-up. One caller at a time.
+class CopyPool {
+public:
+    static CopyPool &get() {
+        // A forked child has none of the parent's threads: it starts its own pool.
+        static CopyPool *pool = nullptr;
+        static pid_t owner = 0;
+        static std::mutex made;
+        std::lock_guard<std::mutex> l(made);
+        if (!pool || owner != getpid()) {
+            pool = new CopyPool(std::max(1u, std::min(16u, std::thread::hardware_concurrency())) - 1);
+            owner = getpid();
+        }
+        return *pool;
+    }
+    unsigned threads() const { return static_cast<unsigned>(workers.size()) + 1; }
+    // Runs f on every pool thread and on the caller; returns when all calls have returned.
+    void run(const std::function<void()> &f) {
+        std::lock_guard<std::mutex> one(callers);
+        {
+            std::lock_guard<std::mutex> l(mu);
+            task = &f;
+            pending = static_cast<int>(workers.size());
+            ++generation;
+        }
+        wake.notify_all();
+        f();
+        std::unique_lock<std::mutex> l(mu);
+        finished.wait(l, [&] { return pending == 0; });
+        task = nullptr;
+    }
+
+private:
+    explicit CopyPool(unsigned n) {
+        for (unsigned i = 0; i < n; i++)
+            workers.emplace_back([this] { loop(); });
+    }
+    void loop() {
+        unsigned long long seen = 0;
+        for (;;) {
+            const std::function<void()> *f = nullptr;
+            {
+                std::unique_lock<std::mutex> l(mu);
+                wake.wait(l, [&] { return generation != seen; });
+                seen = generation;
+                f = task;
+            }
+            (*f)();
+            std::lock_guard<std::mutex> l(mu);
+            if (--pending == 0)
+                finished.notify_all();
+        }
+    }
+    std::vector<std::thread> workers;
+    std::mutex mu, callers;
+    std::condition_variable wake, finished;
+    const std::function<void()> *task = nullptr;
+    unsigned long long generation = 0;
+    int pending = 0;
+};
+
+bool copyHostParallel(const std::vector<HostCopy> &jobs) {
+    size_t total = 0;
+    for (const HostCopy &j : jobs)
+        total += j.count;
+    const size_t chunk = size_t{1} << 16; // floats
+    const bool parallel = total >= 4 * chunk;
+    std::atomic<bool> finite{true};
+    std::atomic<size_t> next{0};
+    // Work items: (job, first float) pairs in order.
+    std::vector<std::pair<size_t, size_t>> items;
+    for (size_t j = 0; j < jobs.size(); j++)
+        for (size_t f = 0; f < jobs[j].count; f += chunk)
+            items.emplace_back(j, f);
+    const auto run = [&]() {
+        for (size_t i = next.fetch_add(1); i < items.size(); i = next.fetch_add(1)) {
+            const HostCopy &job = jobs[items[i].first];
+            const size_t f = items[i].second, n = std::min(chunk, job.count - f);
+            const float *src = job.src + f;
+            if (job.check) {
+                bool ok = true;
+                for (size_t k = 0; k < n; k++)
+                    ok = ok && std::isfinite(src[k]);
+                if (!ok)
+                    finite.store(false);
+            }
+            std::memcpy(job.dst + f, src, sizeof(float) * n);
+        }
+    };
+    if (parallel)
+        CopyPool::get().run(run);
+    else
+        run();
+    return finite.load();
+}
+
+} // namespace
+
 int Engine::getState(int w, int first, int count, float *pos, float *quat, float *vel, float *angVel) {
     int g0 = 0;
     if (slotRange(w, first, count, g0))
@@ -1219,14 +1337,16 @@ int Engine::getState(int w, int first, int count, float *pos, float *quat, float
     if (cudaStreamSynchronize(stream) != cudaSuccess)
         return cudaCheck("getState");
     const size_t n = static_cast<size_t>(count);
+    std::vector<HostCopy> jobs;
     if (pos)
-        std::memcpy(pos, ioHost, sizeof(float) * 3 * n);
+        jobs.push_back({pos, ioHost, 3 * n, false});
     if (quat)
-        std::memcpy(quat, ioHost + 3 * n, sizeof(float) * 4 * n);
+        jobs.push_back({quat, ioHost + 3 * n, 4 * n, false});
     if (vel)
-        std::memcpy(vel, ioHost + 7 * n, sizeof(float) * 3 * n);
+        jobs.push_back({vel, ioHost + 7 * n, 3 * n, false});
     if (angVel)
-        std::memcpy(angVel, ioHost + 10 * n, sizeof(float) * 3 * n);
+        jobs.push_back({angVel, ioHost + 10 * n, 3 * n, false});
+    copyHostParallel(jobs);
     return cudaCheck("getState");
 }
 
@@ -1246,26 +1366,26 @@ int Engine::setState(int w, int first, int count, const float *pos, const float 
         return cudaCheck("setState");
     const size_t n = static_cast<size_t>(count);
     int mask = 0;
-    for (size_t i = 0; i < 3 * n; i++)
-        if ((pos && !std::isfinite(pos[i])) || (vel && !std::isfinite(vel[i])) ||
-            (angVel && !std::isfinite(angVel[i])))
-            return fail(AVBDG_ERR_NONFINITE, "non-finite body state");
+    std::vector<HostCopy> jobs;
     if (pos) {
-        std::memcpy(ioHost, pos, sizeof(float) * 3 * n);
+        jobs.push_back({ioHost, pos, 3 * n, true});
         mask |= 1;
     }
     if (quat) {
-        std::memcpy(ioHost + 3 * n, quat, sizeof(float) * 4 * n);
+        jobs.push_back({ioHost + 3 * n, quat, 4 * n, false});
         mask |= 2;
     }
     if (vel) {
-        std::memcpy(ioHost + 7 * n, vel, sizeof(float) * 3 * n);
+        jobs.push_back({ioHost + 7 * n, vel, 3 * n, true});
         mask |= 4;
     }
     if (angVel) {
-        std::memcpy(ioHost + 10 * n, angVel, sizeof(float) * 3 * n);
+        jobs.push_back({ioHost + 10 * n, angVel, 3 * n, true});
         mask |= 8;
     }
+    // Staged and checked in one pass; nothing reaches the device when a value is not finite.
+    if (!copyHostParallel(jobs))
+        return fail(AVBDG_ERR_NONFINITE, "non-finite body state");
     cudaMemcpyAsync(ioDev, ioHost, sizeof(float) * 13 * n, cudaMemcpyHostToDevice, stream);
     launchUnpackState(d, g0, count, ioDev, mask, stream);
     return cudaCheck("setState");
