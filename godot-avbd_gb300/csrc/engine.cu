@@ -84,9 +84,6 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.wActive, ww);
     take(n.wColour, ww);
     take(n.wSleep, 2 * static_cast<size_t>(ww));
-    take(n.wManStart, ww);
-    take(n.wManCount, ww);
-    take(n.wSurv, 6 * static_cast<size_t>(ww));
     take(n.x, nb);
     take(n.q, nb);
     take(n.x0, nb);
@@ -184,7 +181,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.colourCount, kMaxColours + 1);
     take(n.ctr, C_COUNT);
     take(n.longList, static_cast<size_t>(std::max(nb, 1)) + 1);
-    const int scanCap = std::max({pp, mm, nb + 1, 2 * (ff + mm), ww}) + 1;
+    const int scanCap = std::max({pp, mm, nb + 1, 2 * (ff + mm)}) + 1;
     char *scan = nullptr, *radix = nullptr;
     take(scan, scanScratchBytes(scanCap));
     take(radix, radixScratchBytes(nb + 1));

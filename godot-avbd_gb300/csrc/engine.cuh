@@ -51,7 +51,6 @@ enum Counter {
     C_ONE,            // constant 1 (scan length helper)
     C_SOLVEFAIL,      // overflow bodies whose plain LDLT failed this round (solveFail)
     C_PAIRSPILL,      // bodies with more broad-phase partners than the stash holds (pairSpill)
-    C_SPLIT,          // compaction: candidates below this index were live before the step (the rest are new)
     C_TMP,
     C_COUNT
 };
@@ -103,8 +102,6 @@ struct Dev {
     int *wActive;           // projection: movable manifolds per world (0 = skip the world)
     int *wColour;           // colouring: 1 if a force touches the world (its bodies need colours)
     int *wSleep;            // sleep: first compacted sleeper pair and their count, per world
-    int *wManStart, *wManCount; // the world's live manifolds: [start, start + count) (live order is world-major)
-    int *wSurv;             // compaction, per world: survivors (old, new), first and last survivor rank (old, new)
     // bodies
     float4 *x, *q, *x0, *q0, *xi, *qi, *v, *w, *vprev;
     float4 *size, *moment;

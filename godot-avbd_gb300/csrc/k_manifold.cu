@@ -6,7 +6,6 @@
 // survivors back in order (the reference's stable compaction of `live`). Slot recycling is an
 // allocation detail of the reference that never reaches its arithmetic, so it has no equivalent.
 
-#include <climits>
 #include <cmath>
 
 #include "forces.cuh"
@@ -296,67 +295,6 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
 
 // One thread per contact slot (8 per candidate, slot-major like the arrays), so the copies of the
 // contact arrays coalesce; the slot-0 thread also moves the manifold's own record. Grid-stride.
-// ---- world-major compaction ----
-// The live order only matters within a world (adjacency, brake, projection and acquisition all stay
-// inside one), so the compaction keeps every world's manifolds together: world by world, and in
-// each world the surviving live manifolds in their order, then the new ones in key order (the
-// reference's append). Candidates below C_SPLIT were live (world-major already) and the new ones
-// come in key order (world-major too), so each world's survivors are one run per part.
-
-__global__ void survResetKernel(Dev d) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= d.WW)
-        return;
-    int *s = d.wSurv + 6 * w;
-    s[0] = s[1] = 0;
-    s[2] = s[3] = INT_MAX;
-    s[4] = s[5] = -1;
-}
-
-// Whole warps per pass (every lane runs every pass), so each (world, part) group of a warp is
-// reduced first and one lane does its atomics: a large world would otherwise serialise three
-// atomics per manifold on three words.
-__global__ void survStatsKernel(Dev d, const int *flags, const int *rank) {
-    const int cand = d.ctr[C_CAND], split = d.ctr[C_SPLIT];
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < cand; base += gridDim.x * blockDim.x) {
-        const int i = base + lane;
-        int key = -1, r = 0;
-        if (i < cand && flags[i]) {
-            key = 2 * d.meta[d.stage.ab[i].x].x + (i < split ? 0 : 1);
-            r = rank[i];
-        }
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        const int lo = __reduce_min_sync(peers, r), hi = __reduce_max_sync(peers, r);
-        if (key >= 0 && lane == __ffs(peers) - 1) {
-            int *s = d.wSurv + 6 * (key >> 1);
-            const int part = key & 1;
-            atomicAdd(&s[part], __popc(peers));
-            atomicMin(&s[2 + part], lo);
-            atomicMax(&s[4 + part], hi);
-        }
-    }
-}
-
-// Survivors per world, and a check that each part of a world is one run (otherwise the order
-// would not be the reference's: reported as a capacity-class error rather than used).
-__global__ void survCountKernel(Dev d) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= d.WW)
-        return;
-    const int *s = d.wSurv + 6 * w;
-    for (int part = 0; part < 2; part++)
-        if (s[part] > 0 && s[4 + part] - s[2 + part] + 1 != s[part])
-            atomicOr(&d.ctr[C_ERRORS], kErrManifolds);
-    d.wManCount[w] = w < d.ctr[C_WORLDS] ? s[0] + s[1] : 0;
-}
-
-__device__ __forceinline__ int compactTarget(const Dev &d, int i, const int *rank) {
-    const int w = d.meta[d.stage.ab[i].x].x;
-    const int *s = d.wSurv + 6 * w;
-    return i < d.ctr[C_SPLIT] ? d.wManStart[w] + (rank[i] - s[2]) : d.wManStart[w] + s[0] + (rank[i] - s[3]);
-}
-
 __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
     const int cand = d.ctr[C_CAND];
     const long long slots = static_cast<long long>(cand) * kMaxContacts;
@@ -367,7 +305,7 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
         const int c = static_cast<int>(t / cand), i = static_cast<int>(t % cand);
         if (!flags[i])
             continue;
-        const int r = compactTarget(d, i, rank);
+        const int r = rank[i];
         const int n = S.count[i];
         const int2 dorm = S.dormant[i];
         if (c == 0) {
@@ -540,13 +478,7 @@ void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block
 }
 
 void launchManifoldCompact(const Dev &d, cudaStream_t s) {
-    cudaMemcpyAsync(d.ctr + C_SPLIT, d.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToDevice, s);
     scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_CAND, d.ctr + C_LIVE, d.scanScratch, s);
-    ++launchCount(); survResetKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
-    ++launchCount();
-    survStatsKernel<<<residentGrid(survStatsKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
-    ++launchCount(); survCountKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
-    scanExclusive(d.wManCount, d.wManStart, d.WW, nullptr, nullptr, d.scanScratch, s);
     ++launchCount();
     const int blocks = residentGrid(reinterpret_cast<const void *>(manifoldCompactKernel), kThreads, 0,
                                     divUp(d.MM * kMaxContacts, kThreads));
