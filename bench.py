@@ -159,6 +159,34 @@ def manifold_pass_bytes(world, dynamic_mask, iterations):
     return avg, {"manifolds": n_m, "contacts": n_c, "stamp_sides": sides}
 
 
+PROJECTION_PASSES = 4
+
+
+def step_bytes(st, iterations=10, projection_passes=PROJECTION_PASSES):
+    """Algorithmic bytes of one whole step from that step's counters (float32 SoA, counted once).
+
+    Per round: 100 B per updated body (pose, inertial pose, mass and inertia read; pose written),
+    144 B per contact (primal and dual reads of anchors, step-start error, penalty and dual; dual
+    writes) and 304 B per manifold (basis, friction and both bodies' poses, for the primal and the
+    dual). Once a step: 56 B per body (bounds, Morton code, warm start, finish), 16 B per candidate
+    pair (keys sorted), 200 B per manifold (narrow phase), and per projection pass 152 B per
+    manifold plus 60 B per contact (passes counted at their cap; early exit can run fewer).
+    """
+    per_round = 100 * st.update_bodies + 144 * st.contacts + 304 * st.manifolds
+    once = (56 * st.bodies + 16 * st.broad_pairs + 200 * st.manifolds
+            + projection_passes * (152 * st.manifolds + 60 * st.contacts))
+    return iterations * per_round + once
+
+
+def step_roofline(total_bytes, total_ms, steps, peak, peak_kind):
+    achieved = total_bytes / (total_ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+            "frac": achieved / peak, "algorithmic_bytes_per_step": total_bytes / max(steps, 1),
+            "note": "whole step: algorithmic bytes of every timed step (its own counters) over the timed "
+                    "device time; rounds after the first read L2-resident state, so this is a lower bound "
+                    f"on DRAM-side efficiency; projection passes counted at {PROJECTION_PASSES}"}
+
+
 def run_cpu_reference(sc, steps, warmup, threads, time_budget_s=None):
     """Time the reference CPU step (compiled reference if present here, else the oracle port)."""
     pkg = entry.load_package()
@@ -213,12 +241,15 @@ def run_gpu(args, rank, world_size):
     w.take_kernel_times() if hasattr(w, "take_kernel_times") else None
     w.set_profiling(True)
     step_ms = []
+    sum_bytes = 0
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             w.step()
-            step_ms.append(w.stats().total_ms)
+            st_i = w.stats()
+            step_ms.append(st_i.total_ms)
+            sum_bytes += step_bytes(st_i)
         torch.cuda.synchronize()
     kt = w.take_kernel_times()
     w.set_profiling(False)
@@ -263,7 +294,8 @@ def run_gpu(args, rank, world_size):
                       "iterations": 10, "dt": "1/60", "form": "plain per-scene step",
                       "timed_steps": [args.warmup + 1, args.warmup + args.steps],
                       "l2": "flushed (512 MB write) before every timed step", "parallelism": f"replicas x{world_size}"},
-           "roofline": roofline, "e2e": e2e, "gpu_launches": kt.kernel_launches,
+           "roofline": roofline, "step_roofline": step_roofline(sum_bytes, total_ms, args.steps, peak, peak_kind),
+           "e2e": e2e, "gpu_launches": kt.kernel_launches,
            "clocks": clocks.summary(),
            "phase_ms_last_step": {k: getattr(w.stats(), k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]},
            "kernel_ms": {"manifold_pass_per_launch": launch_ms, "body_solve_per_launch":
@@ -307,12 +339,15 @@ def run_batch(args, rank, world_size):
     step_ms = []
     batch.take_kernel_times()
     batch.set_profiling(True)
+    sum_bytes = 0
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             batch.step()
-            step_ms.append(batch.stats().total_ms)
+            st_i = batch.stats()
+            step_ms.append(st_i.total_ms)
+            sum_bytes += step_bytes(st_i)
     kt = batch.take_kernel_times()
     batch.set_profiling(False)
     total_ms = float(sum(step_ms))
@@ -377,7 +412,8 @@ def run_batch(args, rank, world_size):
                       "l2": "flushed (512 MB write) before every timed step", "parallelism": f"replicas x{world_size}"},
            "plain_per_scene": {"value": plain_value, "unit": UNIT, "sample_worlds": len(sample),
                                "steps_per_world": args.plain_steps, "batched_over_plain": value / plain_value},
-           "roofline": roofline, "e2e": e2e, "gpu_launches": kt.kernel_launches, "clocks": clocks.summary(),
+           "roofline": roofline, "step_roofline": step_roofline(sum_bytes, total_ms, args.steps, peak, peak_kind),
+           "e2e": e2e, "gpu_launches": kt.kernel_launches, "clocks": clocks.summary(),
            "counts": {"manifolds": st.manifolds, "contacts": st.contacts, "pairs": st.broad_pairs},
            "autotuned_block_sizes": {"dualKernel": st.block_dual, "overflowSolveKernel": st.block_solve,
                                      "manifoldInitKernel": st.block_narrow, "traverseKernel": st.block_traverse},
