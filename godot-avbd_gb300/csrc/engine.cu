@@ -145,7 +145,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
         take(b->capB, am);
         take(b->armFlag, am);
     }
-    take(n.stamps, static_cast<size_t>(mm) * 2 * kStampF4);
+    take(n.stampSlot, mm);
     take(n.mSpec, mm);
     take(n.mDone, mm);
     take(n.specList, mm);
@@ -153,8 +153,6 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.solveFail, nb);
     take(n.pairStash, static_cast<size_t>(nb) * kPairStash);
     take(n.pairSpill, nb);
-    take(n.projLin, 2 * static_cast<size_t>(mm));
-    take(n.projAng, 2 * static_cast<size_t>(mm));
     take(n.dLin, nb);
     take(n.dAng, nb);
     take(n.fAB, ff);
@@ -177,6 +175,9 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.adjSeq, adjCap);
     take(n.adjTmp, adjCap);
     take(n.adjInfo, adjCap);
+    take(n.stamps, adjCap * kStampF4);
+    take(n.projLin, adjCap);
+    take(n.projAng, adjCap);
     take(n.colourList, static_cast<size_t>(nb) * (kMaxColours + 1));
     take(n.colourCount, kMaxColours + 1);
     take(n.ctr, C_COUNT);

@@ -127,14 +127,15 @@ struct Dev {
     // manifolds
     ManifoldBuf live, stage;
     int *mActive;           // then exclusive rank
-    float4 *stamps;
+    float4 *stamps;         // block stamps, one per adjacency entry (the entry of the stamped body)
+    int2 *stampSlot;        // per live manifold: the adjacency entries of its side-A and side-B stamps
     uint8_t *mSpec, *mDone; // brake: candidate flag per manifold, done flag per candidate
     int *specList;
     int *solveFail;         // overflow bodies left to the pivoted fallback this round
     int *pairStash;         // broad phase: first kPairStash partners' list positions per body list position
     int *pairSpill;         // broad phase: bodies whose partners overflow the stash (walked again)
     int2 *specPred;         // brake: candidate index of the preceding candidate on each movable body (-1 = none)
-    float4 *projLin, *projAng; // projection contributions per (manifold, side)
+    float4 *projLin, *projAng; // projection contributions, one per adjacency entry (w: side sign, 0 = none)
     float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)
     // forces (creation order; list order is descending index)
     int2 *fAB;

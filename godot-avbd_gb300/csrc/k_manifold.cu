@@ -67,7 +67,8 @@ __global__ void adjFillKernel(Dev d) {
 }
 
 // Each entry's other body and side, once per adjacency build, so the per-round passes need no
-// load of the force's or manifold's body pair to find them.
+// load of the force's or manifold's body pair to find them; and each manifold side's entry, where
+// its block stamp is stored, so a body's stamps lie contiguous in its adjacency range.
 __global__ void adjInfoKernel(Dev d) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,6 +81,8 @@ __global__ void adjInfoKernel(Dev d) {
         const int side = ab.x == g ? 0 : 1;
         const int other = side == 0 ? ab.y : ab.x;
         d.adjInfo[e] = (other >= 0 ? other : kNoBody) | static_cast<int>(static_cast<unsigned>(side) << 31);
+        if (seq >= nf)
+            reinterpret_cast<int *>(d.stampSlot)[2 * (seq - nf) + side] = e;
     }
 }
 

@@ -297,11 +297,16 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
     const int2 ab = L.ab[m];
     const int a = ab.x, b = ab.y;
     const int w = d.meta[a].x;
-    d.projLin[2 * m].w = 0.0f;
-    d.projLin[2 * m + 1].w = 0.0f;
+    // The adjacency entries of sides A and B; only bodies with mass have entries (a static side's
+    // slot is not written by the adjacency build and is not touched here).
+    const int2 slot = d.stampSlot[m];
+    const float4 xa4 = d.x[a], xb4 = d.x[b];
+    if (xa4.w > 0.0f)
+        d.projLin[slot.x].w = 0.0f;
+    if (xb4.w > 0.0f)
+        d.projLin[slot.y].w = 0.0f;
     if (d.wStop[w])
         return;
-    const float4 xa4 = d.x[a], xb4 = d.x[b];
     const bool moveA = movable(d, a), moveB = movable(d, b);
     const int n = L.count[m];
     if (n == 0 || (!moveA && !moveB))
@@ -340,12 +345,12 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
                     (moveB ? angularCompliance(IB, tB) : 0.0f);
     const float dp = p.projBeta * patchDepth * invN / K;
     if (moveA) {
-        d.projLin[2 * m] = f4(scale(nrm, invMassA * dp), 1.0f);
-        d.projAng[2 * m] = f4(scale(angularResponse(IA, qa, tA), dp), 0.0f);
+        d.projLin[slot.x] = f4(scale(nrm, invMassA * dp), 1.0f);
+        d.projAng[slot.x] = f4(scale(angularResponse(IA, qa, tA), dp), 0.0f);
     }
     if (moveB) {
-        d.projLin[2 * m + 1] = f4(scale(nrm, invMassB * dp), 1.0f);
-        d.projAng[2 * m + 1] = f4(scale(angularResponse(IB, qb, tB), dp), 0.0f);
+        d.projLin[slot.y] = f4(scale(nrm, invMassB * dp), -1.0f);
+        d.projAng[slot.y] = f4(scale(angularResponse(IB, qb, tB), dp), 0.0f);
     }
 }
 
@@ -374,18 +379,16 @@ __global__ void projBodyKernel(Dev d, StepParams p) {
     const int nf = d.ctr[C_FORCES];
     f3 sl{0, 0, 0}, sa{0, 0, 0};
     int cnt = 0;
+    // Each manifold entry holds the contribution for this body (w: +1 side A, -1 side B, 0 none).
     for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
-        const int seq = static_cast<int>(d.adjSeq[e]);
-        if (seq < nf)
+        if (nf > 0 && static_cast<int>(d.adjSeq[e]) < nf)
             continue;
-        const int m = seq - nf;
-        const int side = adjInfoSide(d.adjInfo[e]);
-        const float4 cl = d.projLin[2 * m + side];
+        const float4 cl = d.projLin[e];
         if (cl.w == 0.0f)
             continue;
-        const f3 ca = xyz(d.projAng[2 * m + side]);
+        const f3 ca = xyz(d.projAng[e]);
         cnt++;
-        if (side == 0) {
+        if (cl.w > 0.0f) {
             sl = add(sl, xyz(cl));
             sa = add(sa, ca);
         } else {

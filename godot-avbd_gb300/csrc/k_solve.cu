@@ -460,10 +460,11 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
         if (sides & kSideB)
             stampContact(S, rBw, fw, sb);
     }
+    const int2 slot = d.stampSlot[m];
     if (sides & kSideA)
-        storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
+        storeStamp(d.stamps + static_cast<size_t>(slot.x) * kStampF4, sh, sa, 1.0f);
     if (sides & kSideB)
-        storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
+        storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
 }
 
 __device__ __forceinline__ void stampsAt(Dev d, StepParams p, int mixedOnly, int m) {
@@ -577,10 +578,13 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
                     stampContact(S, rBs, fw, sb);
             }
         }
-        if (sides & kSideA)
-            storeStamp(d.stamps + static_cast<size_t>(2 * m) * kStampF4, sh, sa, 1.0f);
-        if (sides & kSideB)
-            storeStamp(d.stamps + static_cast<size_t>(2 * m + 1) * kStampF4, sh, sb, -1.0f);
+        if (sides) {
+            const int2 slot = d.stampSlot[m];
+            if (sides & kSideA)
+                storeStamp(d.stamps + static_cast<size_t>(slot.x) * kStampF4, sh, sa, 1.0f);
+            if (sides & kSideB)
+                storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
+        }
         if (ARM && !driftUsable) { // capture (manifold.cpp:662-667)
             L.capA[m] = f4(A.rot.c0, 0.0f);
             L.capB[m] = f4(B.rot.c0, 0.0f);
@@ -736,7 +740,14 @@ __device__ __forceinline__ int nForcesDev(const Dev &d) { return d.ctr[C_FORCES]
 template <bool RECOMPUTE, bool FORCES = true>
 __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk, int armsFromDual = 0) {
     const int nf = nForcesDev(d);
-    for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
+    const int e1 = d.adjStart[g + 1];
+    if (!RECOMPUTE && !FORCES && nf == 0) {
+        // Every entry is a manifold stamped for this body, stored at the entry itself.
+        for (int e = d.adjStart[g]; e < e1; e++)
+            addStamp(blk, d.stamps + static_cast<size_t>(e) * kStampF4);
+        return;
+    }
+    for (int e = d.adjStart[g]; e < e1; e++) {
         const int seq = static_cast<int>(d.adjSeq[e]);
         if (seq < nf) {
             if (FORCES)
@@ -795,7 +806,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             blk.rl = add(blk.rl, scale(sh.rhsLin, sgn));
             blk.ra = add(blk.ra, scale(sd.rhsAng, sgn));
         } else {
-            addStamp(blk, d.stamps + static_cast<size_t>(2 * m + side) * kStampF4);
+            addStamp(blk, d.stamps + static_cast<size_t>(e) * kStampF4);
         }
     }
 }
