@@ -205,6 +205,11 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     useGraphs = !(noGraphs && noGraphs[0] == '1');
     const char *noTune = std::getenv("AVBDG_NO_TUNE");
     tuneEnabled = !(noTune && noTune[0] == '1');
+    int dev = 0, hostTables = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    const char *staged = std::getenv("AVBDG_STAGED_IO");
+    directIo = hostTables == 1 && !(staged && staged[0] == '1');
     armTuning();
     prepareKernels(); // attributes and occupancy queries, never during a capture
     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
@@ -333,6 +338,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
             cudaFree(p);
         // The device staging buffer was one of the freed allocations.
         ioDev = nullptr;
+        ioFlag = nullptr;
         ioCap = 0;
         treeValid = false;
         adjValid = false;
@@ -1103,9 +1109,10 @@ int Engine::ensureIo(int count) {
     ioHost = nullptr;
     if (cudaMallocHost(&ioHost, sizeof(float) * 13 * static_cast<size_t>(cap)) != cudaSuccess)
         return fail(AVBDG_ERR_CAPACITY, "pinned staging allocation failed");
-    ioDev = dalloc<float>(13 * static_cast<size_t>(cap));
+    ioDev = dalloc<float>(13 * static_cast<size_t>(cap) + 4);
     if (!ioDev)
         return fail(AVBDG_ERR_CAPACITY, "device staging allocation failed");
+    ioFlag = reinterpret_cast<int *>(ioDev + 13 * static_cast<size_t>(cap));
     ioCap = cap;
     return AVBDG_OK;
 }
@@ -1334,10 +1341,23 @@ int Engine::getState(int w, int first, int count, float *pos, float *quat, float
     if (rc)
         return rc;
     launchPackState(d, g0, count, ioDev, stream);
-    cudaMemcpyAsync(ioHost, ioDev, sizeof(float) * 13 * static_cast<size_t>(count), cudaMemcpyDeviceToHost, stream);
+    const size_t n = static_cast<size_t>(count);
+    if (directIo) {
+        // One copy per requested field into the caller's arrays.
+        if (pos)
+            cudaMemcpyAsync(pos, ioDev, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, stream);
+        if (quat)
+            cudaMemcpyAsync(quat, ioDev + 3 * n, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, stream);
+        if (vel)
+            cudaMemcpyAsync(vel, ioDev + 7 * n, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, stream);
+        if (angVel)
+            cudaMemcpyAsync(angVel, ioDev + 10 * n, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+        return cudaCheck("getState");
+    }
+    cudaMemcpyAsync(ioHost, ioDev, sizeof(float) * 13 * n, cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess)
         return cudaCheck("getState");
-    const size_t n = static_cast<size_t>(count);
     std::vector<HostCopy> jobs;
     if (pos)
         jobs.push_back({pos, ioHost, 3 * n, false});
@@ -1363,9 +1383,32 @@ int Engine::setState(int w, int first, int count, const float *pos, const float 
     int rc = ensureIo(count);
     if (rc)
         return rc;
+    const size_t n = static_cast<size_t>(count);
+    if (directIo) {
+        // The fields go up as they are; the device checks them and unpacks only when all are
+        // finite, so nothing changes on a rejected upload.
+        const int mask = (pos ? 1 : 0) | (quat ? 2 : 0) | (vel ? 4 : 0) | (angVel ? 8 : 0);
+        cudaMemsetAsync(ioFlag, 0, sizeof(int), stream);
+        if (pos)
+            cudaMemcpyAsync(ioDev, pos, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, stream);
+        if (quat)
+            cudaMemcpyAsync(ioDev + 3 * n, quat, sizeof(float) * 4 * n, cudaMemcpyHostToDevice, stream);
+        if (vel)
+            cudaMemcpyAsync(ioDev + 7 * n, vel, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, stream);
+        if (angVel)
+            cudaMemcpyAsync(ioDev + 10 * n, angVel, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, stream);
+        launchCheckState(count, ioDev, mask, ioFlag, stream);
+        launchUnpackState(d, g0, count, ioDev, mask, ioFlag, stream);
+        int *flagHost = reinterpret_cast<int *>(ioHost);
+        cudaMemcpyAsync(flagHost, ioFlag, sizeof(int), cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess)
+            return cudaCheck("setState");
+        if (*flagHost)
+            return fail(AVBDG_ERR_NONFINITE, "non-finite body state");
+        return cudaCheck("setState");
+    }
     if (cudaStreamSynchronize(stream) != cudaSuccess) // the staging buffer may still be in use
         return cudaCheck("setState");
-    const size_t n = static_cast<size_t>(count);
     int mask = 0;
     std::vector<HostCopy> jobs;
     if (pos) {
@@ -1388,7 +1431,7 @@ int Engine::setState(int w, int first, int count, const float *pos, const float 
     if (!copyHostParallel(jobs))
         return fail(AVBDG_ERR_NONFINITE, "non-finite body state");
     cudaMemcpyAsync(ioDev, ioHost, sizeof(float) * 13 * n, cudaMemcpyHostToDevice, stream);
-    launchUnpackState(d, g0, count, ioDev, mask, stream);
+    launchUnpackState(d, g0, count, ioDev, mask, nullptr, stream);
     return cudaCheck("setState");
 }
 

@@ -149,7 +149,11 @@ private:
     // Pinned host staging for state upload/download (13 floats per body).
     float *ioHost = nullptr;
     float *ioDev = nullptr;
+    int *ioFlag = nullptr; // device: non-finite upload seen (after the 13 x ioCap floats of ioDev)
     int ioCap = 0;
+    // Body state moves straight between the caller's (pageable) arrays and the device, where the
+    // device reaches host memory through the host's page tables; else through pinned staging.
+    bool directIo = false;
     int ensureIo(int count);
 
     int fail(int code, const std::string &msg);

@@ -31,11 +31,23 @@ __global__ void packStateKernel(Dev d, int first, int count, float *out) {
     ww[3 * i + 2] = w.z;
 }
 
+// Sets *bad when an uploaded position or velocity component is not finite (orientations are taken
+// as given, as the host-side check does).
+__global__ void checkStateKernel(int count, const float *in, int mask, int *bad) {
+    const long long total = 13LL * count;
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+    for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < total; k += stride) {
+        const int field = k < 3LL * count ? 1 : (k < 7LL * count ? 2 : (k < 10LL * count ? 4 : 8));
+        if ((mask & field) && field != 2 && !isfinite(in[k]))
+            *bad = 1;
+    }
+}
+
 // Fields not in `mask` (1 pos, 2 quat, 4 vel, 8 angvel) keep their device values; the packed
-// companions (mass in x.w, gravity in v.w) are preserved.
-__global__ void unpackStateKernel(Dev d, int first, int count, const float *in, int mask) {
+// companions (mass in x.w, gravity in v.w) are preserved. With `bad` set nothing is written.
+__global__ void unpackStateKernel(Dev d, int first, int count, const float *in, int mask, const int *bad) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count)
+    if (i >= count || (bad && *bad))
         return;
     const int g = first + i;
     const float *p = in, *o = in + 3 * count, *vv = in + 7 * count, *ww = in + 10 * count;
@@ -60,9 +72,16 @@ void launchPackState(const Dev &d, int first, int count, float *out, cudaStream_
     packStateKernel<<<divUp(count > 0 ? count : 1, 256), 256, 0, s>>>(d, first, count, out);
 }
 
-void launchUnpackState(const Dev &d, int first, int count, const float *in, int mask, cudaStream_t s) {
+void launchCheckState(int count, const float *in, int mask, int *bad, cudaStream_t s) {
     ++launchCount();
-    unpackStateKernel<<<divUp(count > 0 ? count : 1, 256), 256, 0, s>>>(d, first, count, in, mask);
+    checkStateKernel<<<residentGrid(checkStateKernel, 256, divUp(13 * (count > 0 ? count : 1), 256)), 256, 0, s>>>(
+            count, in, mask, bad);
+}
+
+void launchUnpackState(const Dev &d, int first, int count, const float *in, int mask, const int *bad,
+                       cudaStream_t s) {
+    ++launchCount();
+    unpackStateKernel<<<divUp(count > 0 ? count : 1, 256), 256, 0, s>>>(d, first, count, in, mask, bad);
 }
 
 } // namespace avbdg

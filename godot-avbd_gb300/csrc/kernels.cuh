@@ -78,7 +78,9 @@ void prepareKernels();
 // ---- host state exchange (k_io.cu) ----
 // Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).
 void launchPackState(const Dev &d, int first, int count, float *buf, cudaStream_t s);
-void launchUnpackState(const Dev &d, int first, int count, const float *buf, int mask, cudaStream_t s);
+// `bad` (may be null): a device flag; when set, the unpack writes nothing.
+void launchUnpackState(const Dev &d, int first, int count, const float *buf, int mask, const int *bad, cudaStream_t s);
+void launchCheckState(int count, const float *buf, int mask, int *bad, cudaStream_t s);
 
 // ---- sleeping (k_sleep.cu; only when Solver::sleepFrames > 0) ----
 // Broad-phase wake-up over the valid pairs (after the filter), in pair order per world.
