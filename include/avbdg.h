@@ -221,7 +221,11 @@ int avbdg_world_collect_aabb(avbdg_world *world, const float min[3], const float
                              int capacity, int *out_bodies, int *out_count);
 
 /* Write the same fields (host edits between steps, e.g. integrated external forces,
- * src/server/avbd_physics_server3d.cpp:1503-1528). Any pointer may be NULL. */
+ * src/server/avbd_physics_server3d.cpp:1503-1528). Any pointer may be NULL. A non-finite
+ * position or velocity component returns AVBDG_ERR_NONFINITE and changes nothing. Returns when
+ * the arrays may be reused. Transfers go straight from the caller's arrays where the device reads
+ * host memory through the host's page tables, else through pinned staging (also forced by the
+ * environment variable AVBDG_STAGED_IO=1 when the world is created). */
 int avbdg_world_set_body_state(avbdg_world *world, int first, int count, const float *position,
                                const float *orientation, const float *velocity,
                                const float *angular_velocity);
