@@ -266,7 +266,7 @@ def run_gpu(args, rank, world_size):
     for _ in range(args.steps):
         w.set_state(position=p, orientation=q, velocity=v, angular_velocity=av)
         w.step()
-        p, q, v, av = w.state()
+        p, q, v, av = w.state(out=(p, q, v, av))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world_size)

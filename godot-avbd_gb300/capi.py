@@ -374,13 +374,20 @@ class World:
     def sync(self):
         self.api.check(self.api.world_sync(self.handle))
 
-    def state(self):
-        """(position n x 3, orientation n x 4, velocity n x 3, angular velocity n x 3), creation order."""
+    def state(self, out=None):
+        """(position n x 3, orientation n x 4, velocity n x 3, angular velocity n x 3), creation order;
+        into `out` (four float32 C-contiguous arrays of those shapes) when given."""
         n = self.n_bodies
-        p = np.zeros((n, 3), np.float32)
-        q = np.zeros((n, 4), np.float32)
-        v = np.zeros((n, 3), np.float32)
-        w = np.zeros((n, 3), np.float32)
+        if out is not None:
+            p, q, v, w = out
+            for a, k in zip(out, (3, 4, 3, 3)):
+                if a.dtype != np.float32 or a.shape != (n, k) or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError("state(out=...) wants float32 C-contiguous arrays of n x 3, 4, 3, 3")
+        else:
+            p = np.zeros((n, 3), np.float32)
+            q = np.zeros((n, 4), np.float32)
+            v = np.zeros((n, 3), np.float32)
+            w = np.zeros((n, 3), np.float32)
         self.api.check(self.api.world_get_body_state(self.handle, 0, n, _ptr(p, C.c_float), _ptr(q, C.c_float),
                                                      _ptr(v, C.c_float), _ptr(w, C.c_float)))
         return p, q, v, w

@@ -44,6 +44,8 @@ def test_world_state_round_trip_and_refusal(pkg, gpu, oracle, io_path):
     assert _equal(w.state(), ref.state())
     # A non-finite value in any checked field is refused and changes nothing.
     before = w.state()
+    into = tuple(np.empty_like(a) for a in before)
+    assert w.state(out=into) is not None and _equal(into, before)
     for field, k in (("position", 0), ("velocity", 2), ("angular_velocity", 3)):
         bad = before[k].copy()
         bad[len(bad) // 2, 1] = np.inf if k else np.nan
