@@ -348,11 +348,20 @@ __device__ __forceinline__ void zeroAcc(SideAcc &a) {
     a.rhsAng = f3{0, 0, 0};
 }
 
+// One stamp record, loaded whole before it is added.
+struct StampRec {
+    float4 s0, s1, s2, s3, s4, s5, s6;
+};
+
+// Stamps are read-only while bodies solve: the read-only path.
+__device__ __forceinline__ StampRec loadStamp(const float4 *src) {
+    return StampRec{__ldg(src), __ldg(src + 1), __ldg(src + 2), __ldg(src + 3), __ldg(src + 4), __ldg(src + 5),
+                    __ldg(src + 6)};
+}
+
 // block += stamp (full 3x3 adds, as the reference adds its accumulators).
-__device__ __forceinline__ void addStamp(Blk &b, const float4 *src) {
-    // Stamps are read-only while bodies solve: the read-only path.
-    const float4 s0 = __ldg(src), s1 = __ldg(src + 1), s2 = __ldg(src + 2), s3 = __ldg(src + 3), s4 = __ldg(src + 4),
-                 s5 = __ldg(src + 5), s6 = __ldg(src + 6);
+__device__ __forceinline__ void addStamp(Blk &b, const StampRec &r) {
+    const float4 s0 = r.s0, s1 = r.s1, s2 = r.s2, s3 = r.s3, s4 = r.s4, s5 = r.s5, s6 = r.s6;
     const m3 lin = mcols(f3{s0.x, s0.y, s0.z}, f3{s0.y, s0.w, s1.x}, f3{s0.z, s1.x, s1.y});
     const m3 ang = mcols(f3{s2.y, s2.z, s2.w}, f3{s2.z, s3.x, s3.y}, f3{s2.w, s3.y, s3.z});
     const m3 crs = mcols(f3{s4.z, s4.w, s5.x}, f3{s5.y, s5.z, s5.w}, f3{s6.x, s6.y, s6.z});
@@ -362,6 +371,8 @@ __device__ __forceinline__ void addStamp(Blk &b, const float4 *src) {
     b.rl = add(b.rl, f3{s1.z, s1.w, s2.x});
     b.ra = add(b.ra, f3{s3.w, s4.x, s4.y});
 }
+
+__device__ __forceinline__ void addStamp(Blk &b, const float4 *src) { addStamp(b, loadStamp(src)); }
 
 struct Pose {
     f3 x, dLin, dAng;
@@ -742,8 +753,16 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
     const int nf = nForcesDev(d);
     const int e1 = d.adjStart[g + 1];
     if (!RECOMPUTE && !FORCES && nf == 0) {
-        // Every entry is a manifold stamped for this body, stored at the entry itself.
-        for (int e = d.adjStart[g]; e < e1; e++)
+        // Every entry is a manifold stamped for this body, stored at the entry itself; two records
+        // are loaded before either is added (the sums keep the entry order).
+        int e = d.adjStart[g];
+        for (; e + 1 < e1; e += 2) {
+            const StampRec r0 = loadStamp(d.stamps + static_cast<size_t>(e) * kStampF4);
+            const StampRec r1 = loadStamp(d.stamps + static_cast<size_t>(e + 1) * kStampF4);
+            addStamp(blk, r0);
+            addStamp(blk, r1);
+        }
+        if (e < e1)
             addStamp(blk, d.stamps + static_cast<size_t>(e) * kStampF4);
         return;
     }
