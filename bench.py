@@ -387,6 +387,24 @@ def run_batch(args, rank, world_size):
     nbytes = 13 * 4 * sum(w.n for w in worlds)
     e2e = {"value": dynamic * e2e_steps * world_size / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes}
+    # Where an end-to-end step goes, from a few more steps after the timed ones (each part timed
+    # alone on the host clock, the step's device time from its own events).
+    split = {"upload_ms": 0.0, "step_wall_ms": 0.0, "step_device_ms": 0.0, "download_ms": 0.0}
+    split_steps = 5
+    for _ in range(split_steps):
+        t = time.perf_counter()
+        batch.set_state_all(*state)
+        t1 = time.perf_counter()
+        batch.step()
+        t2 = time.perf_counter()
+        state = batch.state_all(state)
+        t3 = time.perf_counter()
+        split["upload_ms"] += (t1 - t) * 1e3 / split_steps
+        split["step_wall_ms"] += (t2 - t1) * 1e3 / split_steps
+        split["download_ms"] += (t3 - t2) * 1e3 / split_steps
+        split["step_device_ms"] += batch.stats().total_ms / split_steps
+    e2e["ms_per_step"] = e2e_s * 1e3 / e2e_steps
+    e2e["split_after_timed_steps"] = split
 
     # Plain per-scene GPU step on a sample of the worlds, each its own avbdg_world.
     rng = np.random.default_rng(1)
