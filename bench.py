@@ -162,6 +162,18 @@ def manifold_pass_bytes(world, dynamic_mask, iterations):
 PROJECTION_PASSES = 4
 
 
+def body_solve_roofline(st, kt, peak, peak_kind):
+    """The block-Jacobi body solve (`overflowSolveKernel`): per overflow body its pose, inertial
+    pose, mass and inertia read and its pose written (96 B), plus one 112 B stamp record per
+    stamped side; counts from the last timed step, time the mean launch of the timed steps."""
+    launch_ms = kt.body_ms / max(kt.body_launches, 1)
+    nbytes = 96 * st.overflow_bodies + 112 * st.manifold_sides
+    achieved = nbytes / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": "overflowSolveKernel", "achieved": achieved, "peak": peak,
+            "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+            "algorithmic_bytes_per_launch": nbytes, "launch_ms": launch_ms}
+
+
 def step_bytes(st, iterations=10, projection_passes=PROJECTION_PASSES):
     """Algorithmic bytes of one whole step from that step's counters (float32 SoA, counted once).
 
@@ -299,7 +311,8 @@ def run_gpu(args, rank, world_size):
            "clocks": clocks.summary(),
            "phase_ms_last_step": {k: getattr(w.stats(), k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]},
            "kernel_ms": {"manifold_pass_per_launch": launch_ms, "body_solve_per_launch":
-                         kt.body_ms / max(kt.body_launches, 1), "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)}}
+                         kt.body_ms / max(kt.body_launches, 1), "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)},
+           "roofline_body_solve": body_solve_roofline(st_i, kt, peak, peak_kind)}
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         cpu_threads = os.cpu_count() or 1
         v_cpu, kind, done, elapsed = run_cpu_reference(sc, args.steps, args.warmup, 0, time_budget_s=20.0)
@@ -438,7 +451,8 @@ def run_batch(args, rank, world_size):
            "phase_ms_last_step": {k: getattr(st, k) for k in ["broad_ms", "graph_ms", "solve_ms", "finish_ms"]},
            "kernel_ms": {"manifold_pass_per_launch": launch_ms,
                          "body_solve_per_launch": kt.body_ms / max(kt.body_launches, 1),
-                         "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)}}
+                         "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)},
+           "roofline_body_solve": body_solve_roofline(st, kt, peak, peak_kind)}
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         v_cpu, kind, done, elapsed, cores = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=20.0)
         out["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": cores, "kind": kind,
