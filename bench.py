@@ -270,7 +270,12 @@ def run_gpu(args, rank, world_size):
     body_steps = sc.dynamic * args.steps * world_size
     value = body_steps / (total_ms / 1e3)
 
-    # End to end through the C ABI with host buffers.
+    # End to end through the C ABI with host buffers, on a fresh world after the same warm-up, so it
+    # covers the same steps as the device-timed value.
+    w.close()
+    w = scenes.instantiate(gpu, sc)
+    for _ in range(args.warmup):
+        w.step()
     p, q, v, av = w.state()
     h2d = d2h = 13 * 4 * sc.n
     torch.cuda.synchronize()
@@ -282,7 +287,8 @@ def run_gpu(args, rank, world_size):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world_size)
-    e2e = {"value": body_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    e2e = {"value": body_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "steps": [args.warmup + 1, args.warmup + args.steps]}
 
     peak, peak_kind = measured_peak_hbm()
     bytes_per_launch, counts = manifold_pass_bytes(w, dyn_mask, 10)
@@ -340,10 +346,14 @@ def run_batch(args, rank, world_size):
     worlds = scenes.batch(worlds=args.worlds, seed=7 + rank)
     p = pkg.gpu_api().default_params()
     scenes.apply_params(p, scenes.BENCH_PARAMS)
-    batch = capi.Batch(pkg.load_library(), p, max_worlds=len(worlds), max_bodies=sum(w.n for w in worlds),
+    def make_batch():
+        b = capi.Batch(pkg.load_library(), p, max_worlds=len(worlds), max_bodies=sum(w.n for w in worlds),
                        max_forces=max(1, sum(len(w.joints) for w in worlds)))
-    for w in worlds:
-        batch.add_scene(w)
+        for w in worlds:
+            b.add_scene(w)
+        return b
+
+    batch = make_batch()
     dynamic = sum(w.dynamic for w in worlds)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     batch.step(args.warmup)
@@ -386,7 +396,11 @@ def run_batch(args, rank, world_size):
                 "note": "L2 flushed before each step, not between the rounds of a step"}
 
     # End to end: every step uploads all bodies' state from host memory and reads it back, one copy
-    # each way for the whole batch, through the C ABI.
+    # each way for the whole batch, through the C ABI; on a fresh batch of the same worlds after the
+    # same warm-up, so it covers the same steps as the device-timed value.
+    batch.close()
+    batch = make_batch()
+    batch.step(args.warmup)
     state = batch.state_all()
     torch.cuda.synchronize()
     e2e_steps = max(1, args.steps)
@@ -417,6 +431,7 @@ def run_batch(args, rank, world_size):
         split["download_ms"] += (t3 - t2) * 1e3 / split_steps
         split["step_device_ms"] += batch.stats().total_ms / split_steps
     e2e["ms_per_step"] = e2e_s * 1e3 / e2e_steps
+    e2e["steps"] = [args.warmup + 1, args.warmup + e2e_steps]
     e2e["split_after_timed_steps"] = split
 
     # Plain per-scene GPU step on a sample of the worlds, each its own avbdg_world.
