@@ -908,13 +908,16 @@ void Engine::dropGraphs() {
     graphSpans = nullptr;
 }
 
-// Run the plan: from the graph cache (captured on first use), or eagerly when profiling, when
-// graphs are disabled or when a capture failed.
+// Run the plan: from the graph cache (a plan is captured the second time it is seen; profiled
+// plans, whose graphs carry the span events, are cached apart), or eagerly the first time, when
+// graphs are disabled, during a tuning trial or when a capture failed.
 int Engine::runPlan(const StepPlan &plan) {
     launchBase = launchCount();
     graphSpans = nullptr;
     lastGraph = false;
-    cudaEventRecord(ev[0], stream);
+    // The step's device time starts when its work is handed to the stream: after a capture and
+    // instantiation (host work the device only waits for), before an eager enqueue or a launch.
+    const auto startClock = [&] { cudaEventRecord(ev[0], stream); };
     const bool trial = tuning && tuneTrial >= 0;
     if (trial)
         configureTrial();
@@ -926,6 +929,7 @@ int Engine::runPlan(const StepPlan &plan) {
         // counts are read on the device, so adding or removing worlds keeps the cache.
         const bool capture = it == graphs.end() && planSeen[k]++ > 0;
         if (it == graphs.end() && !capture) {
+            startClock();
             enqueueStep(plan);
         } else if (it == graphs.end()) {
             const int before = launchCount();
@@ -951,6 +955,7 @@ int Engine::runPlan(const StepPlan &plan) {
                     cudaEventDestroy(s.b);
                 }
                 spans.clear();
+                startClock();
                 enqueueStep(plan);
             } else {
                 Graph gr{exec, launchCount() - before, {}};
@@ -959,12 +964,14 @@ int Engine::runPlan(const StepPlan &plan) {
             }
         }
         if (it != graphs.end()) {
+            startClock();
             cudaGraphLaunch(it->second.exec, stream);
             launchBase = launchCount() - it->second.launches; // kernels inside the graph
             graphSpans = &it->second.spans;
             lastGraph = true;
         }
     } else {
+        startClock();
         enqueueStep(plan);
     }
     cudaEventRecord(ev[4], stream);
