@@ -61,7 +61,7 @@ def test_batch_digests_equal_single_world_gpu(pkg, gpu):
 def test_full_size_batch_worlds_match_alone(pkg, gpu, oracle):
     """The bench's 4096-world batch (433k bodies) at full size: sampled worlds after 8 steps in the
     batch equal the same worlds stepped alone, on the GPU (the largest, the smallest and a spread
-    between) and on the oracle (two of them), bit for bit."""
+    between) and on the oracle (two of them), bit for bit; and again after 60 steps."""
     capi, scenes = pkg.capi, pkg.scenes
     worlds = scenes.batch(worlds=4096, seed=7)
     p = gpu.default_params()
@@ -86,4 +86,16 @@ def test_full_size_batch_worlds_match_alone(pkg, gpu, oracle):
             assert np.array_equal(x, y), f"world {i} vs the oracle"
     st = batch.stats()
     assert st.bodies == int(sizes.sum())
+    # Longer: 60 steps in all (several Morton rebuilds, the piles settling into contact).
+    batch.step(52)
+    for i in (int(sizes.argmax()), 2047, 4095):
+        sc = worlds[i]
+        alone = scenes.instantiate(gpu, sc)
+        alone.step(60)
+        assert batch.digest(i) == alone.digest(), f"world {i} ({sc.n} bodies) after 60 steps"
+    i = int(sizes.argmin())
+    ref = scenes.instantiate(oracle, worlds[i])
+    ref.step(60)
+    for x, y in zip(batch.state(i), ref.state()):
+        assert np.array_equal(x, y), f"world {i} vs the oracle after 60 steps"
     batch.close()
