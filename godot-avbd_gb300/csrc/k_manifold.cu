@@ -185,10 +185,19 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
         newBeta[c] = 1.0f;
         prevErr[c] = -1.0f;
     }
+    // The old contacts' feature keys, loaded once (registers; unused slots never match).
+    int oldKey[kMaxContacts];
+#pragma unroll
+    for (int j = 0; j < kMaxContacts; j++)
+        oldKey[j] = j < oldN ? L.key[cslot(d, i, j)] : 0;
     for (int c = 0; c < n; c++) {
-        for (int j = 0; j < oldN; j++) {
-            if (nc[c].key != L.key[cslot(d, i, j)])
-                continue;
+        // The first old contact with the same key (the reference's linear search).
+        int j = -1;
+#pragma unroll
+        for (int t = kMaxContacts - 1; t >= 0; t--)
+            if (t < oldN && oldKey[t] == nc[c].key)
+                j = t;
+        if (j >= 0) {
             const f3 newRA = nc[c].rA, newRB = nc[c].rB;
             const float4 oRA = L.rA[cslot(d, i, j)], oRB = L.rB[cslot(d, i, j)];
             const float4 oLam = L.lam[cslot(d, i, j)];
@@ -216,7 +225,6 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
                     newLam[c] = f3{newLam[c].x, 0.0f, 0.0f};
                 }
             }
-            break;
         }
     }
     // Fresh contacts seed their penalty when grace is on (manifold.cpp:339-347).
