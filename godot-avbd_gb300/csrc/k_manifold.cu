@@ -306,14 +306,16 @@ __global__ void manifoldInitKernel(Dev d, StepParams p) {
 
 // One thread per contact slot (8 per candidate, slot-major like the arrays), so the copies of the
 // contact arrays coalesce; the slot-0 thread also moves the manifold's own record. Grid-stride.
-__global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
-    const int cand = d.ctr[C_CAND];
-    const long long slots = static_cast<long long>(cand) * kMaxContacts;
-    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+// Index type T: 32-bit where the slot count fits (the usual case; its division is far cheaper).
+template <typename T>
+__device__ __forceinline__ void manifoldCompactRun(const Dev &d, const int *flags, const int *rank, int cand) {
+    const T slots = static_cast<T>(cand) * kMaxContacts;
+    const T stride = static_cast<T>(gridDim.x) * blockDim.x;
     const ManifoldBuf L = d.live;
     const ManifoldBuf S = d.stage;
-    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < slots; t += stride) {
-        const int c = static_cast<int>(t / cand), i = static_cast<int>(t % cand);
+    for (T t = static_cast<T>(blockIdx.x) * blockDim.x + threadIdx.x; t < slots; t += stride) {
+        const int c = static_cast<int>(t / static_cast<T>(cand));
+        const int i = static_cast<int>(t - static_cast<T>(c) * static_cast<T>(cand));
         if (!flags[i])
             continue;
         const int r = rank[i];
@@ -347,6 +349,16 @@ __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) 
             L.armB[di] = S.armB[si];
         }
     }
+}
+
+__global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
+    const int cand = d.ctr[C_CAND];
+    const unsigned long long span = static_cast<unsigned long long>(cand) * kMaxContacts +
+                                    static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+    if (span < 0xffffffffull)
+        manifoldCompactRun<unsigned>(d, flags, rank, cand);
+    else
+        manifoldCompactRun<unsigned long long>(d, flags, rank, cand);
 }
 
 // ---- rebase (ManifoldStore::rebase, manifold.cpp:448-461) ----
