@@ -297,6 +297,8 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
     const int2 ab = L.ab[m];
     const int a = ab.x, b = ab.y;
     const int w = d.meta[a].x;
+    if (d.wStop[w]) // a stopped world's bodies skip the body pass, which reads these entries
+        return;
     // The adjacency entries of sides A and B; only bodies with mass have entries (a static side's
     // slot is not written by the adjacency build and is not touched here).
     const int2 slot = d.stampSlot[m];
@@ -305,8 +307,6 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
         d.projLin[slot.x].w = 0.0f;
     if (xb4.w > 0.0f)
         d.projLin[slot.y].w = 0.0f;
-    if (d.wStop[w])
-        return;
     const bool moveA = movable(d, a), moveB = movable(d, b);
     const int n = L.count[m];
     if (n == 0 || (!moveA && !moveB))
