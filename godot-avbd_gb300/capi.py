@@ -438,6 +438,13 @@ class World:
         fn.argtypes = [C.c_void_p, C.c_int]
         self.api.check(fn(self.handle, 1 if on else 0))
 
+    def set_wait_limit(self, spins):
+        """Bound of the device's dataflow waits (GPU library only): 0 gives up at the first
+        unfinished predecessor, a negative value restores the default."""
+        fn = getattr(self.api.lib, self.api.prefix + "world_set_wait_limit")
+        fn.argtypes = [C.c_void_p, C.c_longlong]
+        self.api.check(fn(self.handle, int(spins)))
+
     def take_kernel_times(self):
         fn = getattr(self.api.lib, self.api.prefix + "world_take_kernel_times")
         fn.argtypes = [C.c_void_p, C.POINTER(KernelTimes)]

@@ -425,6 +425,13 @@ int avbdg_world_set_profiling(avbdg_world *w, int enabled) {
     });
 }
 
+int avbdg_world_set_wait_limit(avbdg_world *w, long long spins) {
+    return guarded(w, [=](avbdg::Engine &e) {
+        e.setWaitLimit(spins);
+        return AVBDG_OK;
+    });
+}
+
 int avbdg_world_take_kernel_times(avbdg_world *w, avbdg_kernel_times *out) {
     if (!out)
         return failWith(AVBDG_ERR_INVALID, "null output");

@@ -203,6 +203,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
 Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int maxWorlds) : P(params) {
     const char *noGraphs = std::getenv("AVBDG_NO_GRAPHS");
     useGraphs = !(noGraphs && noGraphs[0] == '1');
+    d.waitLimit = waitLimit;
     const char *noTune = std::getenv("AVBDG_NO_TUNE");
     tuneEnabled = !(noTune && noTune[0] == '1');
     int dev = 0, hostTables = 0;
@@ -344,6 +345,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         adjValid = false;
         armTuning(); // sizes changed: tune again
     }
+    n.waitLimit = waitLimit;
     d = n;
     if (!wBase.empty()) {
         cudaMemcpyAsync(d.wBase, wBase.data(), wBase.size() * sizeof(int), cudaMemcpyHostToDevice, stream);

@@ -27,6 +27,9 @@ constexpr uint8_t kUncoloured = 255;
 constexpr int kStampF4 = 7; // float4 per (manifold, side) stamp
 constexpr int kPairStash = 16; // partners kept per body by the counting walk
 constexpr int kExtF4 = 16;  // float4 per force of the generic-joint record (forces.cuh)
+// Spins (64 ns sleeps) a dataflow wait of the colouring or the brake sweep makes before it gives
+// up and reports a timeout: ~0.3 s, far beyond any real dependency hop.
+constexpr long long kDefaultWaitLimit = 4000000;
 
 constexpr float PENALTY_MIN = 1.0f;
 constexpr float PENALTY_MAX = 10000000000.0f;
@@ -94,6 +97,7 @@ struct ManifoldBuf {
 struct Dev {
     int NB, MM, FF, PP, WW; // capacities
     int ARM;                // 1: the arm-cache arrays of ManifoldBuf are allocated
+    long long waitLimit;    // spins a dataflow wait makes before it reports a timeout
     // worlds
     int *wBase, *wCount;    // body range
     int *wMaxDepth;         // projection: max depth bits per world (positive floats)

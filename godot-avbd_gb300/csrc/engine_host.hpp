@@ -84,6 +84,13 @@ public:
             dropGraphs();
     }
     bool graphsEnabled() const { return useGraphs; }
+    // Bound of the dataflow waits (colouring, brake sweep) in spins; 0 gives up at the first
+    // unfinished predecessor, a negative value restores the default.
+    void setWaitLimit(long long spins) {
+        waitLimit = spins < 0 ? kDefaultWaitLimit : spins;
+        d.waitLimit = waitLimit;
+        dropGraphs(); // the limit is part of every captured launch's arguments
+    }
     void takeKernelTimes(avbdg_kernel_times &out);
 
     int worlds() const { return static_cast<int>(wBase.size()); }
@@ -101,6 +108,7 @@ public:
 private:
     avbdg_params P;
     Dev d{};
+    long long waitLimit = kDefaultWaitLimit;
     cudaStream_t stream = nullptr;
     std::vector<void *> allocs;
     std::vector<int> wBase, wCount, wDyn, wRound;

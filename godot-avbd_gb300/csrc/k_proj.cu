@@ -252,8 +252,6 @@ __device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, float window, f3
     return true;
 }
 
-constexpr long long kBrakeSpinLimit = 4000000; // ~0.3 s of 64 ns sleeps per wait
-
 __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window) {
     const int ns = d.ctr[C_SPECN];
     const int stride = gridDim.x * blockDim.x;
@@ -264,7 +262,7 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
         brakeLoad(d, d.specList[k], bl);
         long long spins = 0;
         while (!(published(d, pred.x) && published(d, pred.y))) {
-            if (++spins > kBrakeSpinLimit || (*errors & kErrBrakeTimeout)) {
+            if (++spins > d.waitLimit || (*errors & kErrBrakeTimeout)) {
                 atomicOr(d.ctr + C_ERRORS, kErrBrakeTimeout);
                 return;
             }

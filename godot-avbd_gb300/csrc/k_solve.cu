@@ -1041,7 +1041,6 @@ __device__ __forceinline__ void publishColour(uint8_t *p, unsigned v) {
 }
 
 constexpr int kColourThreads = 512;
-constexpr long long kColourSpinLimit = 4000000; // ~0.3 s of 64 ns sleeps per wait
 
 // Greedy colouring (solver_solve.cpp:365-424) as a dataflow in one cooperative launch: bodies are
 // taken in increasing list position; each waits until its earlier dynamic neighbours have
@@ -1070,7 +1069,7 @@ __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int ev
             unsigned c;
             long long spins = 0;
             while ((c = loadColour(d.colour + h)) == kUncoloured) {
-                if (++spins > kColourSpinLimit || (*errors & kErrColourTimeout)) {
+                if (++spins > d.waitLimit || (*errors & kErrColourTimeout)) {
                     atomicOr(d.ctr + C_ERRORS, kErrColourTimeout);
                     return;
                 }
@@ -1096,6 +1095,8 @@ __global__ void colourListKernel(Dev d, int contactOnlyOverflow) {
         return;
     uint8_t c = d.colour[g];
     if (contactOnlyOverflow && d.contactOnly[g])
+        c = kOverflowColour;
+    if (c > kOverflowColour) // left uncoloured by a colouring that timed out (the step reports it)
         c = kOverflowColour;
     d.colour[g] = c;
     // One atomic per warp and colour (the overflow colour is counted, not listed).

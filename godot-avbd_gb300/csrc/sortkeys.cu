@@ -83,6 +83,9 @@ static __device__ __align__(256) unsigned char g_staticSortScratch[kStaticScratc
 
 // Device address of g_staticSortScratch, per device. In host code the array's name is only a
 // host-side stand-in, so the address is looked up once per device, with that device current.
+// The cached address lives as long as the device's primary context: cudaDeviceReset ends it
+// (with every other device object of this library on that device), and a call made after a
+// reset would use a stale address, so the library must not be used on a device after a reset.
 constexpr int kMaxDevices = 64;
 static void *g_staticScratchAddr[kMaxDevices] = {};
 static std::mutex g_staticScratchMutex;
@@ -139,15 +142,20 @@ int avbdg_sort_unique_keys_static(uint64_t *d_keys, int count, int key_bits, int
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     SortScratch s{reinterpret_cast<uint64_t *>(base + offAlt), base + offRadix, reinterpret_cast<int *>(base + offFlags),
                   reinterpret_cast<int *>(base + offRanks), base + offScan, reinterpret_cast<int *>(base + offCount)};
-    // The array keeps whatever the previous call left; the only word read before this call
-    // writes it is the result count, so it is cleared first.
+    // The array keeps whatever the previous call left. Every word this call reads is written by
+    // it first (the scan's top kernel writes the count before copyBackKernel reads it); the
+    // count is cleared as well, defensively.
     cudaMemsetAsync(s.count, 0, sizeof(int), st);
     enqueueSortUnique(d_keys, count, key_bits, s, st);
+    const cudaError_t launch = cudaPeekAtLastError();
     int host = 0;
     cudaMemcpyAsync(&host, s.count, sizeof(int), cudaMemcpyDeviceToHost, st);
     const cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess || cudaGetLastError() != cudaSuccess)
-        return sortFail(AVBDG_ERR_CUDA, std::string("static sort: ") + cudaGetErrorString(e));
+    const cudaError_t bad = e != cudaSuccess ? e : launch;
+    if (bad != cudaSuccess) {
+        cudaGetLastError(); // the error is reported through the return code
+        return sortFail(AVBDG_ERR_CUDA, std::string("static sort: ") + cudaGetErrorString(bad));
+    }
     *unique_count = host;
     return AVBDG_OK;
 }
@@ -176,12 +184,16 @@ int avbdg_sort_unique_keys(uint64_t *d_keys, int count, int key_bits, int *uniqu
     SortScratch s{reinterpret_cast<uint64_t *>(base + offAlt), base + offRadix, reinterpret_cast<int *>(base + offFlags),
                   reinterpret_cast<int *>(base + offRanks), base + offScan, reinterpret_cast<int *>(base + offCount)};
     enqueueSortUnique(d_keys, count, key_bits, s, st);
+    const cudaError_t launch = cudaPeekAtLastError();
     int host = 0;
     cudaMemcpyAsync(&host, s.count, sizeof(int), cudaMemcpyDeviceToHost, st);
     const cudaError_t e = cudaStreamSynchronize(st);
     cudaFree(base);
-    if (e != cudaSuccess || cudaGetLastError() != cudaSuccess)
-        return sortFail(AVBDG_ERR_CUDA, std::string("sort: ") + cudaGetErrorString(e));
+    const cudaError_t bad = e != cudaSuccess ? e : launch;
+    if (bad != cudaSuccess) {
+        cudaGetLastError();
+        return sortFail(AVBDG_ERR_CUDA, std::string("sort: ") + cudaGetErrorString(bad));
+    }
     *unique_count = host;
     return AVBDG_OK;
 }

@@ -357,6 +357,29 @@ def pyramid420(steps=300, rows=20, spacing=1.01):
     return b.scene("pyramid420", params=dict(BENCH_PARAMS), steps=steps)
 
 
+def pyramid_dbl(steps=600):
+    """test/core_test.cpp:1915-1925 and :1948-1962 (`--pyramid`): a 20-row wall of 1 x 1 x 0.5 m
+    boxes (density 2) on an 80 x 20 x 1 ground, and an identical wall 11.813 m above it that drops
+    onto it; the solver settings of that diagnostic (dt 1/240 stepped as stepInterleaved(4, 2) per
+    tick, 12 iterations, beta_lin 1e5, margin 0.02, arm cache 0.02, projection cap 0.1)."""
+    b = _Builder()
+    b.box((80, 20, 1), 0.0, 0.5, (0, 0, -0.5))
+    for tier in range(2):
+        for row in range(20):
+            n = 20 - row
+            z = _f(0.25) + _f(row) * _f(0.52) + _f(tier) * _f(11.813)
+            for i in range(n):
+                x = (_f(i) - _f(n - 1) * _f(0.5)) * _f(1.01)
+                b.box((1, 1, 0.5), 2.0, 0.5, (x, 0.0, z))
+    sc = b.scene("pyramid_dbl", steps=steps,
+                 params={"gravity": -9.8, "dt": float(_f(1.0) / _f(240.0)), "iterations": 12,
+                         "beta_lin": 100000.0, "speculative_margin": 0.02, "jacobian_rebuild_distance": 0.02,
+                         "position_projection": 1, "projection_max_correction": 0.1, "contact_only_overflow": 1,
+                         "sleep_frames": 30})
+    sc.substeps, sc.rounds = 4, 2
+    return sc
+
+
 def _random_quats(rng, n):
     """Uniform random unit quaternions (Shoemake's method)."""
     u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)

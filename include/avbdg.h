@@ -255,6 +255,16 @@ int avbdg_world_set_profiling(avbdg_world *world, int enabled);
 /* Read and reset the accumulated times. */
 int avbdg_world_take_kernel_times(avbdg_world *world, avbdg_kernel_times *out);
 
+/* Bound of the device's dataflow waits, in spins of ~64 ns. The greedy colouring and the
+ * speculative brake sweep run as dataflows in which a body or brake candidate waits for its
+ * predecessors (the reference runs both serially: solver_solve.cpp:365-424,
+ * solver_projection.cpp:96-167); a wait that exceeds the bound stops its kernel, and the step
+ * returns AVBDG_ERR_TIMEOUT with the world's state no longer trustworthy. The default
+ * (4,000,000 spins, ~0.3 s per wait) is never reached by a real dependency chain; a small value
+ * lets a test make a wait run out (0: give up at the first predecessor found unfinished).
+ * spins < 0 restores the default. No reference counterpart. */
+int avbdg_world_set_wait_limit(avbdg_world *world, long long spins);
+
 /* ------------------------------------------------------------------------------------ */
 /* Parity dumps (the integer stages, for bit-exact comparison with the reference)        */
 /* ------------------------------------------------------------------------------------ */
@@ -402,14 +412,21 @@ int avbdg_sort_unique_keys(uint64_t *d_keys, int count, int key_bits, int *uniqu
 
 /* The same sort + unique for callers that cannot allocate device memory: a host that gives its
  * physics code a fixed device budget and forbids new allocations, a plugin inside an engine whose
- * allocator owns the device, or code that runs while a stream is being captured (a cudaMalloc
- * there would break the capture). It allocates nothing: its scratch is a fixed 4.5 MiB array
- * compiled into this library, present on every GPU that loads the library until the process
- * exits. At most 262,144 keys per call; larger counts return AVBDG_ERR_CAPACITY.
+ * allocator owns the device, or code that runs while another component captures a stream (a
+ * cudaMalloc there would break that capture). It allocates nothing: its scratch is a fixed
+ * 4.5 MiB array compiled into this library, present on every GPU that loads the library until
+ * the process exits. At most 262,144 keys per call; larger counts return AVBDG_ERR_CAPACITY.
+ * The call itself is not capturable: it enqueues a memset, a copy of the count into host memory
+ * and waits for `stream`. So `stream` must not be a stream under capture, and while another
+ * stream is being captured it must be a non-blocking stream (not NULL, the legacy default
+ * stream, whose implicit synchronisation would invalidate that capture), and that capture must
+ * have been begun in cudaStreamCaptureModeRelaxed, or in cudaStreamCaptureModeThreadLocal by
+ * another thread (a capture in cudaStreamCaptureModeGlobal forbids this call's copy and wait).
  * The first call on each device looks up the array's device address (with that device current);
- * make that first call before any stream capture begins. All calls share the one array: calls
- * whose GPU work overlaps (e.g. on two streams at once) race and corrupt each other's results.
- * No counterpart in the reference (it has no GPU and no allocation constraint). */
+ * make that first call before any stream capture begins. The address is kept for the life of the
+ * device's context: do not call this again on a device after cudaDeviceReset. All calls share the
+ * one array: calls whose GPU work overlaps (e.g. on two streams at once) race and corrupt each
+ * other's results. No counterpart in the reference (it has no GPU and no allocation constraint). */
 int avbdg_sort_unique_keys_static(uint64_t *d_keys, int count, int key_bits, int *unique_count, void *stream);
 
 #ifdef __cplusplus

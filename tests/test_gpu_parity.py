@@ -124,8 +124,6 @@ def test_gpu_edge_cases(pkg, gpu, oracle):
     w = pkg.world()
     w.step()
     assert w.stats().manifolds == 0
-    for api in (gpu, oracle):
-        pass
     one = scenes.stack()
     one_g = capi.World(gpu)
     one_o = capi.World(oracle)

@@ -153,3 +153,42 @@ def test_oracle_queries_match_reference(pkg, oracle, ref):
         assert np.array_equal(a.collect_aabb(lo, hi), b.collect_aabb(lo, hi))
     box = ((-30, -30, -2), (30, 30, 10))
     assert np.array_equal(a.collect_aabb(*box, mask=2), b.collect_aabb(*box, mask=2))
+
+
+@pytest.fixture(scope="module")
+def full_golden():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full_runs.json")) as f:
+        return json.load(f)
+
+
+def test_statistics_pinned_to_reference_diagnostic(full_golden):
+    """The statistics code (godot-avbd_gb300/stats.py), run on the reference's own states by the
+    golden maker, reproduces the RESULT line of the reference's `core_test --pyramid`."""
+    rec = full_golden["runs"]["pyramid_dbl"]
+    diag, pen = rec["reference_diagnostic"], rec["stats"]["penetration_m"]
+    assert (round(pen["p50"], 4), round(pen["p95"], 4), round(pen["max"], 4)) == \
+        (diag["p50"], diag["p95"], diag["max"])
+    assert pen["samples"] == diag["samples"]
+    assert sum(v > 0.05 for v in rec["overlap_samples"]) == diag["over5cm"]
+
+
+@pytest.mark.parametrize("run", ["pyramid420", "pyramid_dbl"])
+def test_oracle_full_config(pkg, oracle, full_golden, run):
+    """The oracle over a full configuration: every step's digest and the long-run statistics equal
+    the reference's recorded run."""
+    from avbd_gb300 import stats
+
+    scenes = pkg.scenes
+    rec = full_golden["runs"][run]
+    sc = getattr(scenes, run)()
+    w = scenes.instantiate(oracle, sc)
+    rs = stats.RunStats(sc)
+    for s in range(rec["steps"]):
+        scenes.advance(w, sc, 1)
+        assert f"{w.digest():016x}" == rec["digests"][s], f"{run}: step {s + 1} digest differs"
+        rs.sample(s + 1, w)
+    assert rs.overlaps == rec["overlap_samples"]
+    assert rs.summary()["penetration_m"] == rec["stats"]["penetration_m"]
