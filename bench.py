@@ -7,8 +7,10 @@ One JSON line on rank 0. Workloads (seeded synthetic scenes, identical inputs on
   pyramid420 two 20-row walls of unit cubes (420 boxes). dt 1/60 s, 10 iterations.
   lattice    64 x 64 x 16 unit cubes, 5 cm gaps, 2 cm jitter, 500 m ground. dt 1/60 s, 10 iterations.
   batch      (default) 4096 independent worlds of 8-512 boxes in one store, beside the plain per-scene
-             step on a sample of them; the line also carries the served sweep (below) unless
-             --no-serve.
+             step on a sample of them; the line also carries the served sweep (below, unless
+             --no-serve), the lattice as a `lattice` sub-object (unless --no-lattice) and the
+             float32 result's error against the FP64 build of the same kernels for the pyramid,
+             pile and lattice (`fp64_error`, unless --no-fp64).
   serve      a stream of requests (16-16,384-box scenes, 60-600 steps each) arriving as Poisson
              processes at each rate of --rates, served by continuous batching under a 120 GB budget:
              throughput, p50/p99 tick and request latency, beside the plain per-scene step.
@@ -18,8 +20,16 @@ CUDA events (the device is idle between steps while the host reads the step's co
 flushed by a 512 MB write before every timed step. `e2e` runs the same workload through the C ABI
 with host buffers: every step uploads the bodies' positions, orientations and velocities from
 host memory and reads them back.
+pile / pyramid420 / lattice also run the configuration over its full length and report the
+long-run statistics (penetration distribution by true SAT depth, joint error, rest energy) beside
+the reference's recorded ones, every step's digest checked against the reference (--no-stats to
+skip; --oracle-stats adds the CPU step's own run).
+CPU baselines (batch): the reference's CPU step with one world per host thread (`cpu_baseline`,
+the fastest CPU arrangement for these worlds), worlds one after another on all threads, and one
+thread.
 --impl reference: the reference's CPU step on this machine's host cores (the reference compiled
-from its own sources when present here, otherwise the oracle restatement of it), all threads.
+from its own sources when present here, otherwise the oracle restatement of it, which runs at
+0.99x its speed), all threads; for the batch one world per host thread.
 Multi-GPU: one independent replica per rank (the path does not shard a single scene).
 """
 
@@ -162,6 +172,18 @@ def manifold_pass_bytes(world, dynamic_mask, iterations):
 PROJECTION_PASSES = 4
 
 
+def traffic_per_launch(workload, algorithmic_bytes):
+    """DRAM bytes of one dualKernel launch: the DRAM-to-algorithmic ratio an ncu capture of this
+    workload measured (profiles/traffic_<workload>.json) times this run's algorithmic bytes of a
+    launch, so the figure describes the same steps as `achieved`. None without a capture."""
+    path = os.path.join(ROOT, "profiles", f"traffic_{workload}.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        ratio = json.load(f).get("dram_over_algorithmic")
+    return None if ratio is None else ratio * algorithmic_bytes
+
+
 def body_solve_roofline(st, kt, peak, peak_kind):
     """The block-Jacobi body solve (`overflowSolveKernel`): per overflow body its pose, inertial
     pose, mass and inertia read and its pose written (96 B), plus one 112 B stamp record per
@@ -199,18 +221,32 @@ def step_roofline(total_bytes, total_ms, steps, peak, peak_kind):
                     f"on DRAM-side efficiency; projection passes counted at {PROJECTION_PASSES}"}
 
 
+# Single-thread speed of the oracle port over the compiled reference on the same batch worlds,
+# both built at -O3 (the reference's shipped level), measured where the reference tree exists
+# (x86-64; 48 random worlds of the batch, steps 6-25): the port stands in for the reference on
+# machines without its sources.
+PORT_OVER_REFERENCE = 0.99
+
+
+def cpu_reference_api():
+    """The reference CPU step: the reference compiled from its own sources if present here, else
+    the oracle port of it. Returns (api, kind)."""
+    pkg = entry.load_package()
+    capi = pkg.capi
+    ref_lib = os.path.join(ROOT, "oracle", "_ref", "libavbd_ref.so")
+    if os.path.exists(ref_lib):
+        return capi.Api(ctypes.CDLL(ref_lib), "avbdr_"), "reference"
+    lib = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+    if not os.path.exists(lib):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
+    return capi.Api(ctypes.CDLL(lib), "avbdo_"), "port"
+
+
 def run_cpu_reference(sc, steps, warmup, threads, time_budget_s=None):
     """Time the reference CPU step (compiled reference if present here, else the oracle port)."""
     pkg = entry.load_package()
-    capi, scenes = pkg.capi, pkg.scenes
-    ref_lib = os.path.join(ROOT, "oracle", "_ref", "libavbd_ref.so")
-    if os.path.exists(ref_lib):
-        api, kind = capi.Api(ctypes.CDLL(ref_lib), "avbdr_"), "reference"
-    else:
-        lib = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
-        if not os.path.exists(lib):
-            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
-        api, kind = capi.Api(ctypes.CDLL(lib), "avbdo_"), "port"
+    scenes = pkg.scenes
+    api, kind = cpu_reference_api()
     p = api.default_params()
     scenes.apply_params(p, sc.params)
     p.threads = threads
@@ -295,11 +331,7 @@ def run_gpu(args, rank, world_size):
     bytes_per_launch, counts = manifold_pass_bytes(w, dyn_mask, 10)
     launch_ms = kt.manifold_ms / max(kt.manifold_launches, 1)
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get("manifold_pass_bytes_per_launch")
+    traffic = traffic_per_launch(args.workload, bytes_per_launch)
     roofline = {"bound": "hbm", "kernel": "dualKernel (manifold dual + block stamps)", "achieved": achieved,
                 "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
@@ -326,6 +358,77 @@ def run_gpu(args, rank, world_size):
         out["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": cpu_threads, "kind": kind,
                                "sample": f"steps {args.warmup + 1}-{args.warmup + done} of the same scene "
                                          f"({elapsed:.1f} s of CPU step time, all {cpu_threads} threads)"}
+    return out
+
+
+def fp64_error_report(steps=30):
+    """Error of the float32 step, which is bit-identical to the reference's float32 solver, against
+    the FP64 build of the same kernels (libavbdg64.so): per benchmark configuration at full size,
+    the largest position (m) and rotation (rad) difference of any body after the first `steps`
+    steps. The FP64 state is read through the same float32 interface (resolution: half a float32
+    ulp of a coordinate)."""
+    pkg = entry.load_package()
+    scenes = pkg.scenes
+    from avbd_gb300 import stats
+
+    gpu, gpu64 = pkg.gpu_api(), pkg.gpu_api(fp64=True)
+    out = {"steps": steps, "against": "FP64 build of the same GPU kernels (libavbdg64.so)"}
+    for name in ("pyramid420", "pile", "lattice"):
+        sc = getattr(scenes, name)()
+        a = scenes.instantiate(gpu, sc)
+        b = scenes.instantiate(gpu64, sc)
+        scenes.advance(a, sc, steps)
+        scenes.advance(b, sc, steps)
+        pa, qa, _, _ = a.state()
+        pb, qb, _, _ = b.state()
+        dx, dq = stats.pose_difference(pa, qa, pb, qb)
+        out[name] = {"bodies": sc.n, "max_position_m": dx, "max_rotation_rad": dq}
+        a.close()
+        b.close()
+    return out
+
+
+def full_run_golden(name):
+    path = os.path.join(ROOT, "tests", "golden", "full_runs.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)["runs"].get(name)
+
+
+def long_run_stats(name, with_oracle):
+    """The configuration over its full length on the GPU, every step's state digest checked against
+    the reference's recorded run, with the long-run statistics (penetration distribution by true
+    SAT depth, joint error, rest energy) beside the reference's recorded ones and, when asked, the
+    oracle's (the CPU restatement, run here)."""
+    pkg = entry.load_package()
+    scenes = pkg.scenes
+    from avbd_gb300 import stats
+
+    rec = full_run_golden(name)
+
+    def run(api, check):
+        sc = getattr(scenes, name)()
+        w = scenes.instantiate(api, sc)
+        rs = stats.RunStats(sc)
+        mismatch = 0
+        for s in range(sc.steps):
+            scenes.advance(w, sc, 1)
+            if check and rec and f"{w.digest():016x}" != rec["digests"][s]:
+                mismatch += 1
+            rs.sample(s + 1, w)
+        w.close()
+        return rs.summary(), mismatch, sc.steps
+
+    gpu_stats, mismatch, steps = run(pkg.gpu_api(), True)
+    out = {"steps": steps, "gpu": gpu_stats}
+    if rec:
+        out["reference_recorded"] = rec["stats"]
+        out["steps_whose_digest_differs_from_reference"] = mismatch
+        out["penetration_identical_to_reference"] = gpu_stats["penetration_m"] == rec["stats"]["penetration_m"]
+    if with_oracle:
+        api, kind = cpu_reference_api()
+        out["cpu_" + kind] = run(api, False)[0]
     return out
 
 
@@ -386,11 +489,7 @@ def run_batch(args, rank, world_size):
     bytes_per_launch = 188 * st.manifolds + 112 * st.contacts + 112 * st.manifold_sides * (iters - 1) / iters
     launch_ms = kt.manifold_ms / max(kt.manifold_launches, 1)
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_batch.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get("manifold_pass_bytes_per_launch")
+    traffic = traffic_per_launch("batch", bytes_per_launch)
     roofline = {"bound": "hbm", "kernel": "dualKernel (manifold dual + block stamps)", "achieved": achieved,
                 "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
@@ -471,11 +570,18 @@ def run_batch(args, rank, world_size):
                          "narrow_per_step": kt.narrow_ms / max(kt.narrow_launches, 1)},
            "roofline_body_solve": body_solve_roofline(st, kt, peak, peak_kind)}
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
-        v_cpu, kind, done, elapsed, cores = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=20.0)
+        v_cpu, kind, done, elapsed, cores = run_cpu_parallel_worlds(worlds, args.warmup, args.steps, budget_s=20.0)
         out["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": cores, "kind": kind,
-                               "sample": f"{done} world-steps (worlds stepped one at a time, steps "
-                                         f"{args.warmup + 1}-{args.warmup + args.steps}), {elapsed:.1f} s of CPU "
-                                         f"step time, all {cores} threads"}
+                               "port_over_reference": PORT_OVER_REFERENCE if kind == "port" else None,
+                               "sample": f"{done} world-steps (one world per host thread, each solver "
+                                         f"single-threaded, steps {args.warmup + 1}-{args.warmup + args.steps}), "
+                                         f"{elapsed:.1f} s of step time per thread on {cores} threads"}
+        out["e2e_over_cpu_baseline"] = out["e2e"]["value"] / v_cpu
+        v_seq, kind_s, done_s, elapsed_s, _ = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=10.0)
+        out["cpu_baseline_one_world_at_a_time"] = {
+            "value": v_seq, "unit": UNIT, "cores": cores, "kind": kind_s,
+            "sample": f"{done_s} world-steps (worlds stepped one after another, each on all {cores} threads), "
+                      f"{elapsed_s:.1f} s"}
         v1, kind1, done1, elapsed1, _ = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=10.0,
                                                             threads=1)
         out["cpu_baseline_1thread"] = {"value": v1, "unit": UNIT, "cores": 1, "kind": kind1,
@@ -593,6 +699,50 @@ def run_serve(args, rank, world_size, standalone=True):
     return out
 
 
+def run_cpu_parallel_worlds(worlds, warmup, steps, budget_s, threads=0):
+    """The reference's CPU step over the batch's worlds with one world per host thread (each solver
+    on one thread, every core busy): how a CPU server steps many independent spaces, and the
+    fastest CPU arrangement for worlds of ~100 bodies (one world over all threads pays a barrier
+    per phase; the reference runs concurrent solvers on separate threads, test/core_test.cpp:637-658).
+    Threads take worlds in a random order from a shared queue until the wall-clock budget is
+    spent; each times its own steps, and the aggregate is the sum of the threads' rates."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+
+    scenes = entry.load_package().scenes
+    api, kind = cpu_reference_api()
+    threads = threads if threads > 0 else (os.cpu_count() or 1)
+    queue = list(np.random.default_rng(2).permutation(len(worlds)))
+    lock = threading.Lock()
+    deadline = time.perf_counter() + budget_s
+
+    def worker(_):
+        body_steps, elapsed, done = 0, 0.0, 0
+        while time.perf_counter() < deadline:
+            with lock:
+                if not queue:
+                    break
+                sc = worlds[queue.pop()]
+            p = api.default_params()
+            scenes.apply_params(p, sc.params)
+            p.threads = 1
+            w = scenes.instantiate(api, sc, params=p)
+            if warmup > 0:
+                w.step(warmup)
+            t = time.perf_counter()
+            w.step(steps)  # one C call: the GIL is released while it runs
+            elapsed += time.perf_counter() - t
+            body_steps += sc.dynamic * steps
+            done += steps
+            w.close()
+        return body_steps, elapsed, done
+
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(worker, range(threads)))
+    rate = sum(b / e for b, e, _ in res if e > 0)
+    return rate, kind, sum(r[2] for r in res), max(r[1] for r in res), threads
+
+
 def run_cpu_batch_sample(worlds, warmup, steps, budget_s, threads=0):
     """The reference's CPU step over the batch's worlds, one world at a time with all host threads
     (threads=0, how the reference would serve them) or the given count, on a bounded sample of
@@ -629,6 +779,12 @@ def main():
     ap.add_argument("--rates", type=float, nargs="+", default=[25.0, 50.0, 100.0, 400.0],
                     help="served stream arrival rates (requests/s)")
     ap.add_argument("--no-serve", action="store_true", help="batch workload without the served sweep")
+    ap.add_argument("--no-lattice", action="store_true", help="batch workload without the lattice sub-line")
+    ap.add_argument("--no-fp64", action="store_true", help="batch workload without the FP64 error figures")
+    ap.add_argument("--no-stats", action="store_true",
+                    help="pile/pyramid420/lattice without the full-length run and its long-run statistics")
+    ap.add_argument("--oracle-stats", action="store_true",
+                    help="also run the CPU reference step over the full length for its statistics")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
@@ -637,15 +793,17 @@ def main():
         if rank != 0:
             return
         worlds = entry.load_package().scenes.batch(worlds=args.worlds, seed=7)
-        v, kind, done, elapsed, cores = run_cpu_batch_sample(worlds, args.warmup, args.steps, budget_s=60.0)
+        v, kind, done, elapsed, cores = run_cpu_parallel_worlds(worlds, args.warmup, args.steps, budget_s=60.0)
         out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
                "config": {"workload": BATCH_DESC, "worlds": len(worlds), "iterations": 10, "dt": "1/60",
-                          "form": "CPU solver step, worlds one at a time"},
+                          "form": "CPU solver step, one world per host thread (each solver single-threaded)"},
                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
+                                "port_over_reference": PORT_OVER_REFERENCE if kind == "port" else None,
                                 "sample": f"{done} world-steps of randomly chosen worlds (steps {args.warmup + 1}-"
-                                          f"{args.warmup + args.steps}), {elapsed:.1f} s, all {cores} threads"},
+                                          f"{args.warmup + args.steps}), one world per thread on {cores} threads, "
+                                          f"{elapsed:.1f} s of step time per thread"},
                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out), flush=True)
         return
@@ -676,10 +834,22 @@ def main():
         out = run_batch(args, rank, world_size)
         if not args.no_serve:
             out["served"] = run_serve(args, rank, world_size, standalone=False)
+        if not args.no_lattice:
+            # The 65,536-box lattice as a plain per-scene step: its own warm-up (the cubes land in
+            # the first steps) and the same number of timed steps.
+            lat = run_gpu(argparse.Namespace(**dict(vars(args), workload="lattice", warmup=max(args.warmup, 20),
+                                                    no_cpu_baseline=True)), rank, world_size)
+            out["lattice"] = {k: lat[k] for k in ["value", "unit", "ms_per_step", "steps", "warmup", "config",
+                                                  "roofline", "roofline_body_solve", "step_roofline", "e2e",
+                                                  "gpu_launches", "kernel_ms", "clocks"]}
+        if not args.no_fp64 and rank == 0:
+            out["fp64_error"] = fp64_error_report()
     elif args.workload == "serve":
         out = run_serve(args, rank, world_size)
     else:
         out = run_gpu(args, rank, world_size)
+        if rank == 0 and not args.no_stats:
+            out["long_run_stats"] = long_run_stats(args.workload, with_oracle=args.oracle_stats)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world_size > 1:

@@ -11,8 +11,11 @@ from . import capi, scenes  # noqa: F401
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libavbdg.so")
+# The same kernels compiled with every floating-point value of the step in double precision; only
+# used to state the float32 result's rounding error.
+LIB64_PATH = os.path.join(HERE, "_build", "libavbdg64.so")
 
-_gpu = None
+_gpu = {}
 
 
 def load_library(path=LIB_PATH):
@@ -21,12 +24,11 @@ def load_library(path=LIB_PATH):
     return ctypes.CDLL(path)
 
 
-def gpu_api():
-    """The avbdg_* world API of the GPU library."""
-    global _gpu
-    if _gpu is None:
-        _gpu = capi.Api(load_library(), "avbdg_")
-    return _gpu
+def gpu_api(fp64=False):
+    """The avbdg_* world API of the GPU library (fp64=True: the FP64 build of the same kernels)."""
+    if fp64 not in _gpu:
+        _gpu[fp64] = capi.Api(load_library(LIB64_PATH if fp64 else LIB_PATH), "avbdg_")
+    return _gpu[fp64]
 
 
 def world(params=None, max_bodies=0, max_forces=0):

@@ -1,4 +1,8 @@
-"""Build the GPU library libavbdg.so (sm_103a) in-tree, one nvcc process per translation unit.
+"""Build the GPU libraries in-tree, one nvcc process per translation unit:
+
+  _build/libavbdg.so    the step in float32, bit for bit the reference's arithmetic
+  _build/libavbdg64.so  the same sources compiled with -DAVBDG_FP64: every floating-point value of
+                        the step in double precision (used to state the float32 result's error)
 
 Floating-point flags are part of the contract: the step reproduces the reference solver bit for
 bit only with no FMA contraction (device: --fmad=false; host: -ffp-contract=off) and IEEE
@@ -15,6 +19,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libavbdg.so")
+LIB64 = os.path.join(OUT, "libavbdg64.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -25,6 +30,8 @@ NVCC_FLAGS = ARCH + [
 ]
 SOURCES = ["prims.cu", "k_broad.cu", "k_manifold.cu", "k_solve.cu", "k_proj.cu", "k_io.cu", "k_relocate.cu", "k_sleep.cu", "k_query.cu", "engine.cu",
            "capi.cu", "server.cu", "sortkeys.cu"]
+# (library, object directory, extra flags)
+VARIANTS = [(LIB, OUT, []), (LIB64, os.path.join(OUT, "fp64"), ["-DAVBDG_FP64"])]
 
 
 def nvcc():
@@ -41,18 +48,23 @@ def _stale(obj, deps):
 
 
 def build(verbose=False, force=False):
-    """Compile every translation unit that changed and link libavbdg.so. Returns the library path."""
-    os.makedirs(OUT, exist_ok=True)
+    """Compile every translation unit that changed and link both libraries. Returns the float32
+    library's path."""
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h"))]
     headers.append(os.path.join(ROOT, "include", "avbdg.h"))
-    jobs = []
-    objs = []
-    for src in SOURCES:
-        s = os.path.join(CSRC, src)
-        o = os.path.join(OUT, src.replace(".cu", ".o"))
-        objs.append(o)
-        if force or _stale(o, [s] + headers):
-            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
+    jobs, links = [], []
+    for lib, objdir, extra in VARIANTS:
+        os.makedirs(objdir, exist_ok=True)
+        objs, changed = [], False
+        for src in SOURCES:
+            s = os.path.join(CSRC, src)
+            o = os.path.join(objdir, src.replace(".cu", ".o"))
+            objs.append(o)
+            if force or _stale(o, [s] + headers):
+                jobs.append([nvcc()] + NVCC_FLAGS + extra + ["-c", s, "-o", o])
+                changed = True
+        if changed or not os.path.exists(lib):
+            links.append([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
 
     def run(cmd):
         if verbose:
@@ -62,10 +74,9 @@ def build(verbose=False, force=False):
             raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
         return r
 
-    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs) + 1, os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
-    if jobs or not os.path.exists(LIB):
-        run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+        list(ex.map(run, links))
     return LIB
 
 

@@ -23,39 +23,39 @@ namespace avbdg {
 namespace {
 
 // Rigid::Rigid (src/avbd/rigid.cpp:22-72) per shape; host compiled with -ffp-contract=off.
-void massProperties(const avbdg_body_desc &b, float &mass, float moment[3], float &radius) {
+void massProperties(const avbdg_body_desc &b, real &mass, real moment[3], real &radius) {
     if (b.shape == AVBDG_SHAPE_SPHERE) {
-        const float r = b.size[0];
+        const real r = b.size[0];
         mass = (4.0f / 3.0f) * 3.14159265358979f * r * r * r * b.density;
-        const float i = 0.4f * mass * r * r;
+        const real i = 0.4f * mass * r * r;
         moment[0] = moment[1] = moment[2] = i;
         radius = r;
         return;
     }
     if (b.shape == AVBDG_SHAPE_CYLINDER) {
-        const float r = b.size[0], h = b.size[2];
+        const real r = b.size[0], h = b.size[2];
         mass = 3.14159265358979f * r * r * h * b.density;
-        const float axial = 0.5f * mass * r * r;
-        const float radialM = mass * (3.0f * r * r + h * h) / 12.0f;
+        const real axial = 0.5f * mass * r * r;
+        const real radialM = mass * (3.0f * r * r + h * h) / 12.0f;
         moment[0] = moment[1] = radialM;
         moment[2] = axial;
-        const float hh = h * 0.5f;
-        const float px = r * r, py = hh * hh, pz = r * r;
-        float s = 0.0f;
+        const real hh = h * 0.5f;
+        const real px = r * r, py = hh * hh, pz = r * r;
+        real s = 0.0f;
         s = s + px;
         s = s + py;
         s = s + pz;
         radius = std::sqrt(s);
         return;
     }
-    const float sx = b.size[0], sy = b.size[1], sz = b.size[2];
+    const real sx = b.size[0], sy = b.size[1], sz = b.size[2];
     mass = sx * sy * sz * b.density;
     moment[0] = (sy * sy + sz * sz) / 12.0f * mass;
     moment[1] = (sx * sx + sz * sz) / 12.0f * mass;
     moment[2] = (sx * sx + sy * sy) / 12.0f * mass;
-    const float hx = sx * 0.5f, hy = sy * 0.5f, hz = sz * 0.5f;
-    const float px = hx * hx, py = hy * hy, pz = hz * hz;
-    float s = 0.0f;
+    const real hx = sx * 0.5f, hy = sy * 0.5f, hz = sz * 0.5f;
+    const real px = hx * hx, py = hy * hy, pz = hz * hz;
+    real s = 0.0f;
     s = s + px;
     s = s + py;
     s = s + pz;
@@ -288,7 +288,7 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
                         std::make_pair(n.q0, old.q0), std::make_pair(n.xi, old.xi), std::make_pair(n.qi, old.qi),
                         std::make_pair(n.v, old.v), std::make_pair(n.w, old.w), std::make_pair(n.vprev, old.vprev),
                         std::make_pair(n.size, old.size), std::make_pair(n.moment, old.moment)})
-            cp(pr.first, pr.second, nbCopy * sizeof(float4));
+            cp(pr.first, pr.second, nbCopy * sizeof(real4));
         cp(n.meta, old.meta, nbCopy * sizeof(int4));
         cp(n.sleep, old.sleep, nbCopy * sizeof(int2));
         cp(n.lpToBody, old.lpToBody, nbCopy * sizeof(int));
@@ -301,9 +301,9 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         const ManifoldBuf &s = old.live;
         const ManifoldBuf &t = n.live;
         cp(t.ab, s.ab, mCopy * sizeof(int2));
-        cp(t.b0, s.b0, mCopy * sizeof(float4));
-        cp(t.b1, s.b1, mCopy * sizeof(float4));
-        cp(t.b2, s.b2, mCopy * sizeof(float4));
+        cp(t.b0, s.b0, mCopy * sizeof(real4));
+        cp(t.b1, s.b1, mCopy * sizeof(real4));
+        cp(t.b2, s.b2, mCopy * sizeof(real4));
         cp(t.count, s.count, mCopy * sizeof(int));
         cp(t.dormant, s.dormant, mCopy * sizeof(int2));
         // Contact arrays are slot-major: slot c of the old store (old.MM entries apart) to slot c of
@@ -314,15 +314,15 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
             cp(t.key + sn, s.key + so, mCopy * sizeof(int));
             for (auto pr : {std::make_pair(t.rA, s.rA), std::make_pair(t.rB, s.rB), std::make_pair(t.C0, s.C0),
                             std::make_pair(t.k, s.k), std::make_pair(t.lam, s.lam)})
-                cp(pr.first + sn, pr.second + so, mCopy * sizeof(float4));
+                cp(pr.first + sn, pr.second + so, mCopy * sizeof(real4));
             if (arms) {
-                cp(t.armA + sn, s.armA + so, mCopy * sizeof(float4));
-                cp(t.armB + sn, s.armB + so, mCopy * sizeof(float4));
+                cp(t.armA + sn, s.armA + so, mCopy * sizeof(real4));
+                cp(t.armB + sn, s.armB + so, mCopy * sizeof(real4));
             }
         }
         if (arms) {
-            cp(t.capA, s.capA, mCopy * sizeof(float4));
-            cp(t.capB, s.capB, mCopy * sizeof(float4));
+            cp(t.capA, s.capA, mCopy * sizeof(real4));
+            cp(t.capB, s.capB, mCopy * sizeof(real4));
             cp(t.armFlag, s.armFlag, mCopy * sizeof(uint8_t));
         }
         const size_t fCopy = static_cast<size_t>(std::min(old.FF, ff));
@@ -330,9 +330,9 @@ void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
         for (auto pr : {std::make_pair(n.fRA, old.fRA), std::make_pair(n.fRB, old.fRB), std::make_pair(n.fC0L, old.fC0L),
                         std::make_pair(n.fC0A, old.fC0A), std::make_pair(n.fKL, old.fKL), std::make_pair(n.fKA, old.fKA),
                         std::make_pair(n.fLL, old.fLL), std::make_pair(n.fLA, old.fLA), std::make_pair(n.fPar, old.fPar)})
-            cp(pr.first, pr.second, fCopy * sizeof(float4));
+            cp(pr.first, pr.second, fCopy * sizeof(real4));
         cp(n.fKind, old.fKind, fCopy * sizeof(int));
-        cp(n.fExt, old.fExt, fCopy * kExtF4 * sizeof(float4));
+        cp(n.fExt, old.fExt, fCopy * kExtF4 * sizeof(real4));
         cp(n.fBroken, old.fBroken, fCopy * sizeof(int));
         cudaStreamSynchronize(stream);
         for (void *p : oldAllocs)
@@ -457,22 +457,22 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
     if (rc)
         return rc;
     const int first = nBodies;
-    std::vector<float4> x(count), q(count), v(count), wv(count), sz(count), mo(count), zero4(count);
+    std::vector<real4> x(count), q(count), v(count), wv(count), sz(count), mo(count), zero4(count);
     std::vector<int4> meta(count);
     for (int i = 0; i < count; i++) {
         const avbdg_body_desc &b = descs[i];
-        float mass, moment[3], radius;
+        real mass, moment[3], radius;
         massProperties(b, mass, moment, radius);
-        x[i] = make_float4(b.position[0], b.position[1], b.position[2], mass);
-        q[i] = make_float4(b.orientation[0], b.orientation[1], b.orientation[2], b.orientation[3]);
-        v[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], P.gravity);
-        wv[i] = make_float4(b.angular_velocity[0], b.angular_velocity[1], b.angular_velocity[2], 0.0f);
-        sz[i] = make_float4(b.size[0], b.size[1], b.size[2], radius);
-        mo[i] = make_float4(moment[0], moment[1], moment[2], b.friction);
+        x[i] = mk4(b.position[0], b.position[1], b.position[2], mass);
+        q[i] = mk4(b.orientation[0], b.orientation[1], b.orientation[2], b.orientation[3]);
+        v[i] = mk4(b.velocity[0], b.velocity[1], b.velocity[2], P.gravity);
+        wv[i] = mk4(b.angular_velocity[0], b.angular_velocity[1], b.angular_velocity[2], 0.0f);
+        sz[i] = mk4(b.size[0], b.size[1], b.size[2], radius);
+        mo[i] = mk4(moment[0], moment[1], moment[2], b.friction);
         meta[i] = make_int4(w, static_cast<int>(b.collision_layer), static_cast<int>(b.collision_mask),
                             static_cast<int>((b.axis_lock_linear & 0xff) | ((b.axis_lock_angular & 0xff) << 8) |
                                              ((b.sleep_mode & 0x3) << 16) | ((b.shape & 0x3) << 18)));
-        zero4[i] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
+        zero4[i] = mk4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
         if (outIds)
             outIds[i] = first - wBase[w] + i;
         if (mass > 0.0f) {
@@ -484,7 +484,7 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
             wRound[w]++;
         }
     }
-    const size_t b4 = sizeof(float4) * static_cast<size_t>(count);
+    const size_t b4 = sizeof(real4) * static_cast<size_t>(count);
     cudaMemcpyAsync(d.x + first, x.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.q + first, q.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.v + first, v.data(), b4, cudaMemcpyHostToDevice, stream);
@@ -520,28 +520,28 @@ int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], 
     const int ga = a >= 0 ? wBase[w] + a : -1;
     const int gb = wBase[w] + b;
     // torqueArm = length2((A ? A.size : 0) + B.size) (joint.cpp:38-39), from host copies of sizes.
-    float sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
+    real sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
     if (ga >= 0)
-        cudaMemcpy(sa, d.size + ga, sizeof(float4), cudaMemcpyDeviceToHost);
-    cudaMemcpy(sb, d.size + gb, sizeof(float4), cudaMemcpyDeviceToHost);
-    const float tx = sa[0] + sb[0], ty = sa[1] + sb[1], tz = sa[2] + sb[2];
-    const float px = tx * tx, py = ty * ty, pz = tz * tz;
-    float arm = 0.0f;
+        cudaMemcpy(sa, d.size + ga, sizeof(real4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(sb, d.size + gb, sizeof(real4), cudaMemcpyDeviceToHost);
+    const real tx = sa[0] + sb[0], ty = sa[1] + sb[1], tz = sa[2] + sb[2];
+    const real px = tx * tx, py = ty * ty, pz = tz * tz;
+    real arm = 0.0f;
     arm = arm + px;
     arm = arm + py;
     arm = arm + pz;
     const int f = nForces;
     const int2 ab = make_int2(ga, gb);
-    const float4 ra = make_float4(rA[0], rA[1], rA[2], 0.0f), rb = make_float4(rB[0], rB[1], rB[2], 0.0f);
-    const float4 zero = make_float4(0, 0, 0, 0);
-    const float4 par = make_float4(kLin, kAng, fracture, arm);
+    const real4 ra = mk4(rA[0], rA[1], rA[2], 0.0f), rb = mk4(rB[0], rB[1], rB[2], 0.0f);
+    const real4 zero = mk4(0, 0, 0, 0);
+    const real4 par = mk4(kLin, kAng, fracture, arm);
     const int kind = 0, broken = 0;
     cudaMemcpyAsync(d.fAB + f, &ab, sizeof(int2), cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(d.fRA + f, &ra, sizeof(float4), cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(d.fRB + f, &rb, sizeof(float4), cudaMemcpyHostToDevice, stream);
-    for (float4 *arr : {d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA})
-        cudaMemcpyAsync(arr + f, &zero, sizeof(float4), cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(d.fPar + f, &par, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fRA + f, &ra, sizeof(real4), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fRB + f, &rb, sizeof(real4), cudaMemcpyHostToDevice, stream);
+    for (real4 *arr : {d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA})
+        cudaMemcpyAsync(arr + f, &zero, sizeof(real4), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d.fPar + f, &par, sizeof(real4), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fKind + f, &kind, sizeof(int), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fBroken + f, &broken, sizeof(int), cudaMemcpyHostToDevice, stream);
     nForces++;
@@ -560,12 +560,12 @@ int Engine::addIgnore(int w, int a, int b) {
     const int f = nForces;
     const int2 ab = make_int2(wBase[w] + a, wBase[w] + b);
     const int kind = 1, broken = 0;
-    const float4 zero = make_float4(0, 0, 0, 0);
+    const real4 zero = mk4(0, 0, 0, 0);
     cudaMemcpyAsync(d.fAB + f, &ab, sizeof(int2), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fKind + f, &kind, sizeof(int), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fBroken + f, &broken, sizeof(int), cudaMemcpyHostToDevice, stream);
-    for (float4 *arr : {d.fRA, d.fRB, d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA, d.fPar})
-        cudaMemcpyAsync(arr + f, &zero, sizeof(float4), cudaMemcpyHostToDevice, stream);
+    for (real4 *arr : {d.fRA, d.fRB, d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA, d.fPar})
+        cudaMemcpyAsync(arr + f, &zero, sizeof(real4), cudaMemcpyHostToDevice, stream);
     nForces++;
     cudaMemcpyAsync(d.ctr + C_FORCES, &nForces, sizeof(int), cudaMemcpyHostToDevice, stream);
     cudaStreamSynchronize(stream);
@@ -588,13 +588,13 @@ int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
     if (rc)
         return rc;
     // Torque arms, spring rest lengths and generic-joint zeros read the bodies' current state.
-    std::vector<float4> sizes(n), xs(n), qs(n);
-    cudaMemcpy(sizes.data(), d.size + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
-    cudaMemcpy(xs.data(), d.x + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
-    cudaMemcpy(qs.data(), d.q + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    std::vector<real4> sizes(n), xs(n), qs(n);
+    cudaMemcpy(sizes.data(), d.size + wBase[w], sizeof(real4) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(xs.data(), d.x + wBase[w], sizeof(real4) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(qs.data(), d.q + wBase[w], sizeof(real4) * n, cudaMemcpyDeviceToHost);
     std::vector<int2> ab(count);
-    std::vector<float4> ra(count), rb(count), par(count), zero(count, make_float4(0, 0, 0, 0));
-    std::vector<float4> ext(static_cast<size_t>(count) * kExtF4, make_float4(0, 0, 0, 0));
+    std::vector<real4> ra(count), rb(count), par(count), zero(count, mk4(0, 0, 0, 0));
+    std::vector<real4> ext(static_cast<size_t>(count) * kExtF4, mk4(0, 0, 0, 0));
     std::vector<int> kind(count), broken(count, 0);
     for (int i = 0; i < count; i++) {
         const avbdg_force_desc &f = descs[i];
@@ -603,60 +603,60 @@ int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
         if (f.kind == 2) {
             // Spring::Spring (spring.cpp:16-27): rest < 0 -> the anchors' current distance.
             const f3 rA{f.r_a[0], f.r_a[1], f.r_a[2]}, rB{f.r_b[0], f.r_b[1], f.r_b[2]};
-            float rest = f.rest;
+            real rest = f.rest;
             if (rest < 0.0f) {
                 const f3 pA = add(xyz(xs[f.body_a]), qrot(asq(qs[f.body_a]), rA));
                 const f3 pB = add(xyz(xs[f.body_b]), qrot(asq(qs[f.body_b]), rB));
                 rest = length(sub(pA, pB));
             }
-            ra[i] = make_float4(rA.x, rA.y, rA.z, 0.0f);
-            rb[i] = make_float4(rB.x, rB.y, rB.z, 0.0f);
-            par[i] = make_float4(f.stiffness_lin, rest, 0.0f, 0.0f);
+            ra[i] = mk4(rA.x, rA.y, rA.z, 0.0f);
+            rb[i] = mk4(rB.x, rB.y, rB.z, 0.0f);
+            par[i] = mk4(f.stiffness_lin, rest, 0.0f, 0.0f);
             continue;
         }
         if (f.kind == 3) {
             // GenericJoint::GenericJoint (generic_joint.cpp:24-30): zero = B relative to A now.
             const q4 qA = f.body_a >= 0 ? asq(qs[f.body_a]) : q4{0.0f, 0.0f, 0.0f, 1.0f};
-            float4 *e = ext.data() + static_cast<size_t>(i) * kExtF4;
+            real4 *e = ext.data() + static_cast<size_t>(i) * kExtF4;
             e[0] = f4(qmul(qconj(qA), asq(qs[f.body_b])));
             for (int k = 0; k < 6; k++) {
                 const avbdg_joint_axis &ax = f.axes[k];
-                e[1 + k] = make_float4(static_cast<float>(ax.mode), ax.lower, ax.upper, ax.spring_stiffness);
-                e[7 + k] = make_float4(ax.spring_equilibrium, ax.spring_damping, 0.0f, 0.0f);
+                e[1 + k] = mk4(static_cast<real>(ax.mode), ax.lower, ax.upper, ax.spring_stiffness);
+                e[7 + k] = mk4(ax.spring_equilibrium, ax.spring_damping, 0.0f, 0.0f);
             }
-            ra[i] = make_float4(f.r_a[0], f.r_a[1], f.r_a[2], 0.0f);
-            rb[i] = make_float4(f.r_b[0], f.r_b[1], f.r_b[2], 0.0f);
-            par[i] = make_float4(0, 0, 0, 0);
+            ra[i] = mk4(f.r_a[0], f.r_a[1], f.r_a[2], 0.0f);
+            rb[i] = mk4(f.r_b[0], f.r_b[1], f.r_b[2], 0.0f);
+            par[i] = mk4(0, 0, 0, 0);
             continue;
         }
         if (f.kind == 0) {
             // torqueArm = length2((A ? A.size : 0) + B.size) (joint.cpp:38-39), as in addJoint.
-            const float4 sa = f.body_a >= 0 ? sizes[f.body_a] : make_float4(0, 0, 0, 0);
-            const float4 sb = sizes[f.body_b];
-            const float tx = sa.x + sb.x, ty = sa.y + sb.y, tz = sa.z + sb.z;
-            const float px = tx * tx, py = ty * ty, pz = tz * tz;
-            float arm = 0.0f;
+            const real4 sa = f.body_a >= 0 ? sizes[f.body_a] : mk4(0, 0, 0, 0);
+            const real4 sb = sizes[f.body_b];
+            const real tx = sa.x + sb.x, ty = sa.y + sb.y, tz = sa.z + sb.z;
+            const real px = tx * tx, py = ty * ty, pz = tz * tz;
+            real arm = 0.0f;
             arm = arm + px;
             arm = arm + py;
             arm = arm + pz;
-            ra[i] = make_float4(f.r_a[0], f.r_a[1], f.r_a[2], 0.0f);
-            rb[i] = make_float4(f.r_b[0], f.r_b[1], f.r_b[2], 0.0f);
-            par[i] = make_float4(f.stiffness_lin, f.stiffness_ang, f.fracture, arm);
+            ra[i] = mk4(f.r_a[0], f.r_a[1], f.r_a[2], 0.0f);
+            rb[i] = mk4(f.r_b[0], f.r_b[1], f.r_b[2], 0.0f);
+            par[i] = mk4(f.stiffness_lin, f.stiffness_ang, f.fracture, arm);
         } else {
-            ra[i] = rb[i] = par[i] = make_float4(0, 0, 0, 0);
+            ra[i] = rb[i] = par[i] = mk4(0, 0, 0, 0);
         }
     }
     const int f0 = nForces;
-    const size_t b4 = sizeof(float4) * static_cast<size_t>(count), bi = sizeof(int) * static_cast<size_t>(count);
+    const size_t b4 = sizeof(real4) * static_cast<size_t>(count), bi = sizeof(int) * static_cast<size_t>(count);
     cudaMemcpyAsync(d.fAB + f0, ab.data(), sizeof(int2) * static_cast<size_t>(count), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fRA + f0, ra.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fRB + f0, rb.data(), b4, cudaMemcpyHostToDevice, stream);
-    for (float4 *arr : {d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA})
+    for (real4 *arr : {d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA})
         cudaMemcpyAsync(arr + f0, zero.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fPar + f0, par.data(), b4, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fKind + f0, kind.data(), bi, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d.fBroken + f0, broken.data(), bi, cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(d.fExt + static_cast<size_t>(f0) * kExtF4, ext.data(), sizeof(float4) * ext.size(),
+    cudaMemcpyAsync(d.fExt + static_cast<size_t>(f0) * kExtF4, ext.data(), sizeof(real4) * ext.size(),
                     cudaMemcpyHostToDevice, stream);
     nForces += count;
     cudaMemcpyAsync(d.ctr + C_FORCES, &nForces, sizeof(int), cudaMemcpyHostToDevice, stream);
@@ -765,7 +765,7 @@ int Engine::setParams(const avbdg_params &p) {
     return AVBDG_OK;
 }
 
-StepParams Engine::stepParams(float collisionDt) const {
+StepParams Engine::stepParams(real collisionDt) const {
     StepParams s{};
     s.dt = P.dt;
     s.dtSq = P.dt * P.dt;
@@ -789,7 +789,7 @@ StepParams Engine::stepParams(float collisionDt) const {
     s.projIters = P.projection_iterations;
     s.sleepFrames = P.sleep_frames;
     s.graceTicks = P.contact_grace_ticks;
-    s.graceSeed = std::max(PENALTY_MIN, 0.05f * P.beta_lin);
+    s.graceSeed = std::max(PENALTY_MIN, static_cast<real>(0.05f) * P.beta_lin);
     s.sleepLin2 = P.sleep_linear_threshold * P.sleep_linear_threshold;
     s.sleepAng2 = P.sleep_angular_threshold * P.sleep_angular_threshold;
     s.armCache = P.jacobian_rebuild_distance > 0.0f && d.ARM ? 1 : 0;
@@ -881,7 +881,7 @@ void Engine::enqueueStep(const StepPlan &plan) {
         return;
     }
     const int substeps = plan.substeps;
-    const StepParams sp = stepParams(P.dt * static_cast<float>(substeps));
+    const StepParams sp = stepParams(P.dt * static_cast<real>(substeps));
     broadPhase(sp, plan);
     recordPhase(ev[1]);
     warmstartAndSelect(sp);
@@ -889,7 +889,7 @@ void Engine::enqueueStep(const StepPlan &plan) {
     for (int sub = 0; sub < substeps; ++sub) {
         if (sub > 0)
             launchRebase(d, sp, stream);
-        projectContacts(sp, false, P.dt * static_cast<float>(substeps - sub));
+        projectContacts(sp, false, P.dt * static_cast<real>(substeps - sub));
         runSubstep(sp, plan.rounds, sub + 1 == substeps);
     }
     recordPhase(ev[3]);
@@ -998,7 +998,7 @@ int Engine::warmstartAndSelect(const StepParams &sp) {
 }
 
 // Solver::projectContacts (solver_projection.cpp:67-281).
-void Engine::projectContacts(const StepParams &sp, bool positions, float window) {
+void Engine::projectContacts(const StepParams &sp, bool positions, real window) {
     launchProjActive(d, stream);
     if (sp.specMargin > 0.0f)
         launchBrake(d, window > 0.0f ? window : sp.collisionDt, stream);
@@ -1566,9 +1566,9 @@ int Engine::stats(avbdg_stats &out) {
         out.contacts += c;
     if (!counts.empty() && nBodies > 0) {
         std::vector<int2> ab(counts.size());
-        std::vector<float4> x(static_cast<size_t>(nBodies));
+        std::vector<real4> x(static_cast<size_t>(nBodies));
         cudaMemcpy(ab.data(), d.live.ab, sizeof(int2) * ab.size(), cudaMemcpyDeviceToHost);
-        cudaMemcpy(x.data(), d.x, sizeof(float4) * x.size(), cudaMemcpyDeviceToHost);
+        cudaMemcpy(x.data(), d.x, sizeof(real4) * x.size(), cudaMemcpyDeviceToHost);
         for (const int2 &m : ab)
             out.manifold_sides += (x[m.x].w > 0.0f ? 1 : 0) + (x[m.y].w > 0.0f ? 1 : 0);
     }
@@ -1675,13 +1675,13 @@ int Engine::dumpManifolds(int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_
         return AVBDG_OK;
     std::vector<int2> ab(k);
     std::vector<int> cnt(k), keys(static_cast<size_t>(k) * kMaxContacts);
-    std::vector<float4> b0(k), b1(k), b2(k);
-    std::vector<float4> C(static_cast<size_t>(k) * kMaxContacts), K(C.size()), Lm(C.size());
+    std::vector<real4> b0(k), b1(k), b2(k);
+    std::vector<real4> C(static_cast<size_t>(k) * kMaxContacts), K(C.size()), Lm(C.size());
     cudaMemcpy(ab.data(), d.live.ab, sizeof(int2) * k, cudaMemcpyDeviceToHost);
     cudaMemcpy(cnt.data(), d.live.count, sizeof(int) * k, cudaMemcpyDeviceToHost);
-    cudaMemcpy(b0.data(), d.live.b0, sizeof(float4) * k, cudaMemcpyDeviceToHost);
-    cudaMemcpy(b1.data(), d.live.b1, sizeof(float4) * k, cudaMemcpyDeviceToHost);
-    cudaMemcpy(b2.data(), d.live.b2, sizeof(float4) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b0.data(), d.live.b0, sizeof(real4) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b1.data(), d.live.b1, sizeof(real4) * k, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b2.data(), d.live.b2, sizeof(real4) * k, cudaMemcpyDeviceToHost);
     // Slot-major on the device; manifold-major (8 slots per manifold) here.
     const auto gather = [&](auto *dst, const auto *src) {
         using T = std::remove_const_t<std::remove_reference_t<decltype(*src)>>;
@@ -1704,7 +1704,7 @@ int Engine::dumpManifolds(int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_
             bb[i] = ab[i].y - base;
         if (nc)
             nc[i] = cnt[i];
-        const float4 rows[3] = {b0[i], b1[i], b2[i]};
+        const real4 rows[3] = {b0[i], b1[i], b2[i]};
         for (int r = 0; r < 3; r++)
             if (basis) {
                 basis[9 * i + 3 * r + 0] = rows[r].x;
@@ -1716,7 +1716,7 @@ int Engine::dumpManifolds(int cap, int32_t *ba, int32_t *bb, int32_t *nc, int32_
             const size_t ci = static_cast<size_t>(i) * kMaxContacts + j;
             if (features)
                 features[8 * i + j] = on ? keys[ci] : 0;
-            const float *cv = &C[ci].x, *kv = &K[ci].x, *lv = &Lm[ci].x;
+            const real *cv = &C[ci].x, *kv = &K[ci].x, *lv = &Lm[ci].x;
             for (int e = 0; e < 3; e++) {
                 if (c0)
                     c0[24 * i + 3 * j + e] = on ? cv[e] : 0.0f;
@@ -1739,9 +1739,9 @@ int Engine::dumpColours(int cap, uint8_t *colour, int32_t *bodyId, int *count) {
         return AVBDG_OK;
     }
     const int n = wCount[w];
-    std::vector<float4> x(n);
+    std::vector<real4> x(n);
     std::vector<uint8_t> col(n), upd(n);
-    cudaMemcpy(x.data(), d.x + wBase[w], sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(x.data(), d.x + wBase[w], sizeof(real4) * n, cudaMemcpyDeviceToHost);
     cudaMemcpy(col.data(), d.colour + wBase[w], n, cudaMemcpyDeviceToHost);
     cudaMemcpy(upd.data(), d.upd + wBase[w], n, cudaMemcpyDeviceToHost);
     int u = 0;

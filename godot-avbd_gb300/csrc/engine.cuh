@@ -31,13 +31,13 @@ constexpr int kExtF4 = 16;  // float4 per force of the generic-joint record (for
 // up and reports a timeout: ~0.3 s, far beyond any real dependency hop.
 constexpr long long kDefaultWaitLimit = 4000000;
 
-constexpr float PENALTY_MIN = 1.0f;
-constexpr float PENALTY_MAX = 10000000000.0f;
-constexpr float ADAPTIVE_BETA_MAX = 64.0f;
-constexpr float COLLISION_MARGIN = 0.001f;
-constexpr float STICK_THRESH = 0.00001f;
-constexpr float CONTACT_RELEASE_GAP = 2.0e-3f;
-constexpr float kReleaseAbove = COLLISION_MARGIN + CONTACT_RELEASE_GAP;
+constexpr real PENALTY_MIN = 1.0f;
+constexpr real PENALTY_MAX = 10000000000.0f;
+constexpr real ADAPTIVE_BETA_MAX = 64.0f;
+constexpr real COLLISION_MARGIN = 0.001f;
+constexpr real STICK_THRESH = 0.00001f;
+constexpr real CONTACT_RELEASE_GAP = 2.0e-3f;
+constexpr real kReleaseAbove = COLLISION_MARGIN + CONTACT_RELEASE_GAP;
 
 // Device counters (indices into Dev::ctr).
 enum Counter {
@@ -66,31 +66,31 @@ constexpr int kErrColourTimeout = 16;
 
 // Solver fields a kernel reads (src/avbd/solver.h:54-144), with derived terms.
 struct StepParams {
-    float dt, dtSq, collisionDt;
-    float alpha, oneMinusAlpha, betaLin, betaAng, gamma;
-    float stiffnessDecay, jacobiRelax, stickDriftHeal, maxPen, specMargin;
-    float projBeta, projSlop, projMaxCorr, adaptiveFloor;
+    real dt, dtSq, collisionDt;
+    real alpha, oneMinusAlpha, betaLin, betaAng, gamma;
+    real stiffnessDecay, jacobiRelax, stickDriftHeal, maxPen, specMargin;
+    real projBeta, projSlop, projMaxCorr, adaptiveFloor;
     int adaptiveBeta, contactOnlyOverflow, projIters;
     int sleepFrames;              // 0 = sleeping off
     int graceTicks;               // Solver::contactGraceTicks (0 = off)
-    float graceSeed;              // penalty of a fresh contact under grace: max(PENALTY_MIN, 0.05 betaLin)
-    float sleepLin2, sleepAng2;   // squared velocity thresholds of idle detection
+    real graceSeed;              // penalty of a fresh contact under grace: max(PENALTY_MIN, 0.05 betaLin)
+    real sleepLin2, sleepAng2;   // squared velocity thresholds of idle detection
     int armCache;                 // Solver::jacobianRebuildDistance > 0
-    float armRebuild2;            // its square
+    real armRebuild2;            // its square
 };
 
 struct ManifoldBuf {
     int2 *ab;          // global body indices (a = smaller list index)
-    float4 *b0, *b1, *b2;
+    real4 *b0, *b1, *b2;
     int *count;
     int2 *dormant;     // contact grace: x = ticks parked, y = contacts kept for revival
     int *key;          // contacts: slot-major, see cslot
-    float4 *rA, *rB, *C0, *k, *lam;
+    real4 *rA, *rB, *C0, *k, *lam;
     // Arm cache (Solver::jacobianRebuildDistance, manifold.cpp:600-668): world arms (slot-major like
     // the contacts), the first rotation columns captured with them and the kArmsCached flag.
     // Allocated only while the cache is on (Dev::ARM).
-    float4 *armA, *armB;
-    float4 *capA, *capB;
+    real4 *armA, *armB;
+    real4 *capA, *capB;
     uint8_t *armFlag;
 };
 
@@ -107,14 +107,14 @@ struct Dev {
     int *wColour;           // colouring: 1 if a force touches the world (its bodies need colours)
     int *wSleep;            // sleep: first compacted sleeper pair and their count, per world
     // bodies
-    float4 *x, *q, *x0, *q0, *xi, *qi, *v, *w, *vprev;
-    float4 *size, *moment;
+    real4 *x, *q, *x0, *q0, *xi, *qi, *v, *w, *vprev;
+    real4 *size, *moment;
     int4 *meta;             // x = world, y = layer, z = mask, w = lockLin | lockAng << 8 | sleepMode << 16
     int2 *sleep;            // x = sleeping, y = still frames (Rigid::sleeping, stillFrames)
     uint8_t *upd;           // this step's update set (Rigid::inUpdateSet)
     int *lpToBody;          // list position -> body
     uint8_t *contactOnly, *colour;
-    float4 *aabbC, *aabbH;
+    real4 *aabbC, *aabbH;
     // LBVH
     uint64_t *codes;        // per body: the reference's Morton code of the last rebuild (dumps)
     uint64_t *treeCodes;    // per body: the code the tree is built from (true per-axis origin)
@@ -123,7 +123,7 @@ struct Dev {
     int *leafBody;          // sorted position -> body
     int *nodeL, *nodeR, *nodeParent, *leafParent, *nodeFlag;
     int *nodeMaxLp;         // largest list position in the subtree (prunes the pair walk)
-    float4 *nodeMin, *nodeMax;
+    real4 *nodeMin, *nodeMax;
     // pairs
     int *pairStart;         // per list position (+1)
     uint64_t *pairs, *pairsTmp;
@@ -131,7 +131,7 @@ struct Dev {
     // manifolds
     ManifoldBuf live, stage;
     int *mActive;           // then exclusive rank
-    float4 *stamps;         // block stamps, one per adjacency entry (the entry of the stamped body)
+    real4 *stamps;         // block stamps, one per adjacency entry (the entry of the stamped body)
     int2 *stampSlot;        // per live manifold: the adjacency entries of its side-A and side-B stamps
     uint8_t *mSpec, *mDone; // brake: candidate flag per manifold, done flag per candidate
     int *specList;
@@ -139,13 +139,13 @@ struct Dev {
     int *pairStash;         // broad phase: first kPairStash partners' list positions per body list position
     int *pairSpill;         // broad phase: bodies whose partners overflow the stash (walked again)
     int2 *specPred;         // brake: candidate index of the preceding candidate on each movable body (-1 = none)
-    float4 *projLin, *projAng; // projection contributions, one per adjacency entry (w: side sign, 0 = none)
-    float4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)
+    real4 *projLin, *projAng; // projection contributions, one per adjacency entry (w: side sign, 0 = none)
+    real4 *dLin, *dAng;       // block-Jacobi deltas per body (when applied in a separate pass)
     // forces (creation order; list order is descending index)
     int2 *fAB;
-    float4 *fRA, *fRB, *fC0L, *fC0A, *fKL, *fKA, *fLL, *fLA, *fPar; // fPar: stiffLin, stiffAng, fracture, torqueArm
+    real4 *fRA, *fRB, *fC0L, *fC0A, *fKL, *fKA, *fLL, *fLA, *fPar; // fPar: stiffLin, stiffAng, fracture, torqueArm
     int *fKind, *fBroken, *fKeep;
-    float4 *fExt;           // generic joints: kExtF4 float4 per force (forces.cuh)
+    real4 *fExt;           // generic joints: kExtF4 float4 per force (forces.cuh)
     // adjacency (dynamic bodies only): sequence numbers, forces first (list order) then manifolds
     int *adjStart, *adjFill;
     uint32_t *adjSeq, *adjTmp;
@@ -162,7 +162,7 @@ struct Dev {
     // world removal: slot map (NB) + force ranks (FF), staging of max(NB, FF * kExtF4) records,
     // world remap
     int *relocInt;
-    float4 *relocF4;
+    real4 *relocF4;
     int *relocRemap;        // 2 per world: new id (-1 = removed), new base slot
 };
 

@@ -176,7 +176,7 @@ private:
     bool fits(int nb, int mm, int ff, int pp, int ww) const {
         return byteLimit == 0 || storeBytes(nb, mm, ff, pp, ww, armStore) <= byteLimit;
     }
-    StepParams stepParams(float collisionDt) const;
+    StepParams stepParams(real collisionDt) const;
     // Host decisions of one step; the enqueued work depends on nothing else but device counts.
     struct StepPlan {
         int mode = 0; // 0 step, 1 interleaved
@@ -202,7 +202,7 @@ private:
     void recordPhase(cudaEvent_t e);
     int broadPhase(const StepParams &sp, const StepPlan &plan);
     int warmstartAndSelect(const StepParams &sp);
-    void projectContacts(const StepParams &sp, bool positions, float window);
+    void projectContacts(const StepParams &sp, bool positions, real window);
     void runSubstep(const StepParams &sp, int rounds, bool idle);
     int finishStep();
     bool needGreedy() const;

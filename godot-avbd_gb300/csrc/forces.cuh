@@ -24,18 +24,18 @@ constexpr int kAxisFree = 0, kAxisLocked = 1, kAxisLimited = 2;
 
 struct GAxis {
     int mode;
-    float lower, upper, springK, springEq, springDamp, lambda, penalty, initial;
+    real lower, upper, springK, springEq, springDamp, lambda, penalty, initial;
 };
 
 __device__ __forceinline__ GAxis loadAxis(const Dev &d, int f, int i) {
-    const float4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
-    const float4 a = e[1 + i], b = e[7 + i], c = e[13 + i / 4];
-    const float init[4] = {c.x, c.y, c.z, c.w};
+    const real4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
+    const real4 a = e[1 + i], b = e[7 + i], c = e[13 + i / 4];
+    const real init[4] = {c.x, c.y, c.z, c.w};
     return GAxis{static_cast<int>(a.x), a.y, a.z, a.w, b.x, b.y, b.z, b.w, init[i % 4]};
 }
 
 __device__ __forceinline__ f3 unitAxis(int i) { return i == 0 ? f3{1, 0, 0} : (i == 1 ? f3{0, 1, 0} : f3{0, 0, 1}); }
-__device__ __forceinline__ float qcomp(q4 q, int i) { return i == 0 ? q.x : (i == 1 ? q.y : (i == 2 ? q.z : q.w)); }
+__device__ __forceinline__ real qcomp(q4 q, int i) { return i == 0 ? q.x : (i == 1 ? q.y : (i == 2 ? q.z : q.w)); }
 
 __device__ __forceinline__ q4 frameOrientation(const Dev &d, int a) {
     return a >= 0 ? asq(d.q[a]) : q4{0.0f, 0.0f, 0.0f, 1.0f};
@@ -54,9 +54,9 @@ __device__ __forceinline__ f3 genericOffset(const Dev &d, int f) {
 
 // Angular measurement, swing-twist split (generic_joint.cpp:49-98): each non-locked axis takes its
 // twist 2 atan2(v.n, w) out of the deviation, the locked axes read the remaining swing.
-__device__ __forceinline__ void genericAngles(const Dev &d, int f, float out[3]) {
+__device__ __forceinline__ void genericAngles(const Dev &d, int f, real out[3]) {
     const int2 ab = d.fAB[f];
-    const float4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
+    const real4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
     const q4 qA = frameOrientation(d, ab.x);
     const q4 relativeNow = qmul(qconj(qA), qnormalize(asq(d.q[ab.y])));
     q4 dev = qmul(qnormalize(asq(e[0])), qconj(relativeNow));
@@ -66,14 +66,14 @@ __device__ __forceinline__ void genericAngles(const Dev &d, int f, float out[3])
     for (int i = 0; i < 3; i++) {
         if (locked[i])
             continue;
-        const float proj = dot(f3{dev.x, dev.y, dev.z}, unitAxis(i));
+        const real proj = dot(f3{dev.x, dev.y, dev.z}, unitAxis(i));
         const q4 twist{dev.x * proj, dev.y * proj, dev.z * proj, dev.w};
-        if (sqrtf(qlength2(twist)) <= 1.0e-12f) {
+        if (msqrt(qlength2(twist)) <= 1.0e-12f) {
             out[i] = 0.0f;
             continue;
         }
-        out[i] = 2.0f * atan2f(proj, dev.w);
-        const float l = qlength2(twist); // qinv(twist) = conj(twist) / |twist|^2
+        out[i] = 2.0f * matan2(proj, dev.w);
+        const real l = qlength2(twist); // qinv(twist) = conj(twist) / |twist|^2
         dev = qmul(qnormalize(dev), q4{-twist.x / l, -twist.y / l, -twist.z / l, twist.w / l});
     }
     for (int i = 0; i < 3; i++)
@@ -82,7 +82,7 @@ __device__ __forceinline__ void genericAngles(const Dev &d, int f, float out[3])
 }
 
 // axisConstraint + axisForce (generic_joint.cpp:120-168).
-__device__ __forceinline__ bool axisForce(const GAxis &ax, float value, float alpha, float &C, float &F) {
+__device__ __forceinline__ bool axisForce(const GAxis &ax, real value, real alpha, real &C, real &F) {
     if (ax.mode == kAxisLocked) {
         C = value;
     } else if (ax.mode == kAxisLimited) {
@@ -97,7 +97,7 @@ __device__ __forceinline__ bool axisForce(const GAxis &ax, float value, float al
     }
     if (ax.mode == kAxisLocked)
         C -= ax.initial * alpha;
-    float force = ax.penalty * C + ax.lambda;
+    real force = ax.penalty * C + ax.lambda;
     if (ax.mode == kAxisLimited)
         force = C > 0.0f ? smax(force, 0.0f) : smin(force, 0.0f);
     F = force;
@@ -106,9 +106,9 @@ __device__ __forceinline__ bool axisForce(const GAxis &ax, float value, float al
 
 // GenericJoint::stampAxis (generic_joint.cpp:170-196) into a block (lin, ang, cross, rhs).
 template <typename Block>
-__device__ __forceinline__ void stampAxis(Block &blk, const GAxis &ax, float value, float alpha, f3 jLin, f3 jAng,
-                                          float rate) {
-    float C, F;
+__device__ __forceinline__ void stampAxis(Block &blk, const GAxis &ax, real value, real alpha, f3 jLin, f3 jAng,
+                                          real rate) {
+    real C, F;
     if (axisForce(ax, value, alpha, C, F)) {
         blk.lin = madd(blk.lin, mscale(outerprod(jLin, jLin), ax.penalty));
         blk.ang = madd(blk.ang, mscale(outerprod(jAng, jAng), ax.penalty));
@@ -117,8 +117,8 @@ __device__ __forceinline__ void stampAxis(Block &blk, const GAxis &ax, float val
         blk.ra = add(blk.ra, scale(jAng, F));
     }
     if (ax.springK > 0.0f) {
-        const float Cs = value - ax.springEq;
-        const float Fs = ax.springK * Cs - ax.springDamp * rate;
+        const real Cs = value - ax.springEq;
+        const real Fs = ax.springK * Cs - ax.springDamp * rate;
         blk.lin = madd(blk.lin, mscale(outerprod(jLin, jLin), ax.springK));
         blk.ang = madd(blk.ang, mscale(outerprod(jAng, jAng), ax.springK));
         blk.crs = madd(blk.crs, mscale(outerprod(jAng, jLin), ax.springK));
@@ -136,10 +136,10 @@ __device__ __forceinline__ void genericStamp(const Dev &d, const StepParams &p, 
     const f3 rAWorld = qrot(qA, xyz(d.fRA[f]));
     const f3 rBWorld = qrot(qB, xyz(d.fRB[f]));
     const f3 offset = genericOffset(d, f);
-    float ang[3];
+    real ang[3];
     genericAngles(d, f, ang);
     const bool isA = body == ab.x;
-    const float sign = isA ? 1.0f : -1.0f;
+    const real sign = isA ? 1.0f : -1.0f;
     const f3 arm = isA ? rAWorld : rBWorld;
     const f3 vA = ab.x >= 0 ? add(xyz(d.v[ab.x]), cross(xyz(d.w[ab.x]), rAWorld)) : f3{0, 0, 0};
     const f3 vB = add(xyz(d.v[ab.y]), cross(xyz(d.w[ab.y]), rBWorld));
@@ -159,17 +159,17 @@ __device__ __forceinline__ void genericStamp(const Dev &d, const StepParams &p, 
 template <typename Block>
 __device__ __forceinline__ void springStamp(const Dev &d, int f, int body, Block &blk) {
     const int2 ab = d.fAB[f];
-    const float4 par = d.fPar[f];
+    const real4 par = d.fPar[f];
     const q4 qa = asq(d.q[ab.x]), qb = asq(d.q[ab.y]);
     const f3 pA = add(xyz(d.x[ab.x]), qrot(qa, xyz(d.fRA[f])));
     const f3 pB = add(xyz(d.x[ab.y]), qrot(qb, xyz(d.fRB[f])));
     const f3 dv = sub(pA, pB);
-    const float len = length(dv);
+    const real len = length(dv);
     if (len <= 1.0e-6f)
         return;
     const f3 n = divs(dv, len);
-    const float C = len - par.y;
-    const float force = par.x * C;
+    const real C = len - par.y;
+    const real force = par.x * C;
     f3 jLin, jAng;
     if (body == ab.x) {
         const f3 r = qrot(qa, xyz(d.fRA[f]));
@@ -193,8 +193,8 @@ __device__ __forceinline__ void springStamp(const Dev &d, int f, int body, Block
 }
 
 // GenericJoint::penaltyLimit (generic_joint.cpp:198-222).
-__device__ __forceinline__ float penaltyLimit(const Dev &d, const StepParams &p, int body, f3 axis, bool angular) {
-    float effective;
+__device__ __forceinline__ real penaltyLimit(const Dev &d, const StepParams &p, int body, f3 axis, bool angular) {
+    real effective;
     if (angular) {
         const f3 local = qrot(qconj(asq(d.q[body])), axis);
         const f3 mo = xyz(d.moment[body]);
@@ -204,46 +204,46 @@ __device__ __forceinline__ float penaltyLimit(const Dev &d, const StepParams &p,
     }
     if (effective <= 0.0f)
         return PENALTY_MAX;
-    const float limit = effective * 0.25f * 0.25f / (p.dt * p.dt);
+    const real limit = effective * 0.25f * 0.25f / (p.dt * p.dt);
     return smin(limit, PENALTY_MAX);
 }
 
 // GenericJoint::initialize (generic_joint.cpp:224-245).
 __device__ __forceinline__ void genericInit(const Dev &d, const StepParams &p, int f) {
-    float ang[3];
+    real ang[3];
     genericAngles(d, f, ang);
     const f3 offset = genericOffset(d, f);
-    float4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
-    float init[6];
+    real4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
+    real init[6];
     for (int i = 0; i < 3; i++) {
         init[i] = at(offset, i);
         init[3 + i] = ang[i];
     }
     for (int i = 0; i < 6; i++) {
-        float4 s = e[7 + i];
+        real4 s = e[7 + i];
         s.z = s.z * (p.alpha * p.gamma);
         s.w = sclamp(s.w * p.gamma, PENALTY_MIN, PENALTY_MAX);
         e[7 + i] = s;
     }
-    e[13] = make_float4(init[0], init[1], init[2], init[3]);
-    e[14] = make_float4(init[4], init[5], 0.0f, 0.0f);
+    e[13] = mk4(init[0], init[1], init[2], init[3]);
+    e[14] = mk4(init[4], init[5], 0.0f, 0.0f);
 }
 
 // GenericJoint::updateDual (generic_joint.cpp:289-319).
 __device__ __forceinline__ void genericDual(const Dev &d, const StepParams &p, int f) {
-    float ang[3];
+    real ang[3];
     genericAngles(d, f, ang);
     const f3 offset = genericOffset(d, f);
     const int2 ab = d.fAB[f];
-    float4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
+    real4 *e = d.fExt + static_cast<size_t>(f) * kExtF4;
     for (int i = 0; i < 3; i++) {
-        const float values[2] = {at(offset, i), ang[i]};
-        const float betas[2] = {p.betaLin, p.betaAng};
+        const real values[2] = {at(offset, i), ang[i]};
+        const real betas[2] = {p.betaLin, p.betaAng};
         for (int k = 0; k < 2; k++) {
             const int idx = 3 * k + i;
             const GAxis ax = loadAxis(d, f, idx);
-            float C, F;
-            float4 s = e[7 + idx];
+            real C, F;
+            real4 s = e[7 + idx];
             if (!axisForce(ax, values[k], p.alpha, C, F)) {
                 if (ax.mode == kAxisLimited) {
                     s.z = 0.0f;
@@ -253,10 +253,10 @@ __device__ __forceinline__ void genericDual(const Dev &d, const StepParams &p, i
             }
             s.z = F;
             const f3 dir = qrot(frameOrientation(d, ab.x), unitAxis(i));
-            float cap = penaltyLimit(d, p, ab.y, dir, k == 1);
+            real cap = penaltyLimit(d, p, ab.y, dir, k == 1);
             if (ab.x >= 0)
                 cap = smin(cap, penaltyLimit(d, p, ab.x, dir, k == 1));
-            s.w = sclamp(ax.penalty + fabsf(C) * betas[k], 0.0f, cap);
+            s.w = sclamp(ax.penalty + mabs(C) * betas[k], 0.0f, cap);
             e[7 + idx] = s;
         }
     }

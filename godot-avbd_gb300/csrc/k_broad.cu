@@ -19,11 +19,11 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kStack = 128;
 
-__device__ __forceinline__ int orderedInt(float f) {
-    const int i = __float_as_int(f);
+__device__ __forceinline__ int orderedInt(real f) {
+    const int i = fbits(f);
     return i >= 0 ? i : i ^ 0x7fffffff;
 }
-__device__ __forceinline__ float orderedFloat(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+__device__ __forceinline__ real orderedFloat(int i) { return bitsf(i >= 0 ? i : i ^ 0x7fffffff); }
 
 // Swept AABB (solver_broadphase.cpp:103-122) over the tight box bound (rigid.cpp:83-106).
 __global__ void aabbKernel(Dev d, StepParams p) {
@@ -31,22 +31,22 @@ __global__ void aabbKernel(Dev d, StepParams p) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
         return;
-    const float4 x4 = d.x[g];
-    const float4 v4 = d.v[g];
-    const float4 s4 = d.size[g];
+    const real4 x4 = d.x[g];
+    const real4 v4 = d.v[g];
+    const real4 s4 = d.size[g];
     const m3 rot = qmat(asq(d.q[g]));
     // aabbHalfExtent (rigid.cpp:83-106): sphere (r, r, r), cylinder (r, r, h/2), box size/2.
     const int shape = (d.meta[g].w >> 18) & 0x3;
     const f3 h = shape == 1 ? f3{s4.x, s4.x, s4.x} : (shape == 2 ? f3{s4.x, s4.x, s4.z * 0.5f} : scale(xyz(s4), 0.5f));
-    const f3 tight{(fabsf(rot.c0.x) * h.x + fabsf(rot.c1.x) * h.y) + fabsf(rot.c2.x) * h.z,
-                   (fabsf(rot.c0.y) * h.x + fabsf(rot.c1.y) * h.y) + fabsf(rot.c2.y) * h.z,
-                   (fabsf(rot.c0.z) * h.x + fabsf(rot.c1.z) * h.y) + fabsf(rot.c2.z) * h.z};
-    const float cdt = p.collisionDt;
+    const f3 tight{(mabs(rot.c0.x) * h.x + mabs(rot.c1.x) * h.y) + mabs(rot.c2.x) * h.z,
+                   (mabs(rot.c0.y) * h.x + mabs(rot.c1.y) * h.y) + mabs(rot.c2.y) * h.z,
+                   (mabs(rot.c0.z) * h.x + mabs(rot.c1.z) * h.y) + mabs(rot.c2.z) * h.z};
+    const real cdt = p.collisionDt;
     f3 disp = scale(xyz(v4), cdt);
     if (x4.w > 0)
         disp = add(disp, f3{0, 0, v4.w * cdt * cdt});
-    const float rotSweep = s4.w * length(xyz(d.w[g])) * cdt;
-    const float grow = rotSweep + p.specMargin;
+    const real rotSweep = s4.w * length(xyz(d.w[g])) * cdt;
+    const real grow = rotSweep + p.specMargin;
     const f3 c = add(xyz(x4), scale(disp, 0.5f));
     const f3 half = add(add(tight, scale(vabs(disp), 0.5f)), f3{grow, grow, grow});
     d.aabbC[g] = f4(c, 0.0f);
@@ -75,7 +75,7 @@ __global__ void boundsKernel(Dev d, int *wBounds) {
     int v[6] = {0x7fffffff, 0x7fffffff, 0x7fffffff, static_cast<int>(0x80000000), static_cast<int>(0x80000000),
                 static_cast<int>(0x80000000)};
     if (w >= 0) {
-        const float4 c = d.aabbC[g];
+        const real4 c = d.aabbC[g];
         v[0] = v[3] = orderedInt(c.x);
         v[1] = v[4] = orderedInt(c.y);
         v[2] = v[5] = orderedInt(c.z);
@@ -104,7 +104,7 @@ __device__ __forceinline__ uint64_t expandBits21(uint32_t v) {
     return x;
 }
 
-__device__ __forceinline__ uint32_t quantise(float v, float lo, float scaleF) {
+__device__ __forceinline__ uint32_t quantise(real v, real lo, real scaleF) {
     return static_cast<uint32_t>(sclamp((v - lo) * scaleF, 0.0f, 2097151.0f));
 }
 
@@ -115,20 +115,20 @@ __global__ void mortonKernel(Dev d, const int *wBounds) {
     if (g >= n || d.meta[g].x < 0)
         return;
     const int w = d.meta[g].x;
-    const float lox = orderedFloat(wBounds[6 * w + 0]), loy = orderedFloat(wBounds[6 * w + 1]),
+    const real lox = orderedFloat(wBounds[6 * w + 0]), loy = orderedFloat(wBounds[6 * w + 1]),
                 loz = orderedFloat(wBounds[6 * w + 2]);
-    const float hix = orderedFloat(wBounds[6 * w + 3]), hiy = orderedFloat(wBounds[6 * w + 4]),
+    const real hix = orderedFloat(wBounds[6 * w + 3]), hiy = orderedFloat(wBounds[6 * w + 4]),
                 hiz = orderedFloat(wBounds[6 * w + 5]);
     const f3 ext{hix - lox, hiy - loy, hiz - loz};
-    float e = ext.x;
+    real e = ext.x;
     if (e < ext.y)
         e = ext.y;
     if (e < ext.z)
         e = ext.z;
     if (e < 1.0e-6f)
         e = 1.0e-6f;
-    const float sc = 2097151.0f / e;
-    const float4 c = d.aabbC[g];
+    const real sc = 2097151.0f / e;
+    const real4 c = d.aabbC[g];
     // The reference quantises all three axes against lo.x (bvh_broadphase.cpp:85): kept for the
     // code and order dumps. Where a scene does not extend from lo.x in y and z, that clamps whole
     // regions to one code and degrades the tree, so the tree is built from codes with each axis's
@@ -245,13 +245,13 @@ __global__ void karrasKernel(Dev d) {
     d.nodeR[s + i] = right;
 }
 
-__device__ __forceinline__ void childBounds(const Dev &d, int c, float4 &mn, float4 &mx) {
+__device__ __forceinline__ void childBounds(const Dev &d, int c, real4 &mn, real4 &mx) {
     if (c & kLeafBit) {
         const int b = d.leafBody[c & ~kLeafBit];
-        const float4 cc = d.aabbC[b];
-        const float4 hh = d.aabbH[b];
-        mn = make_float4(cc.x - hh.x, cc.y - hh.y, cc.z - hh.z, 0.0f);
-        mx = make_float4(cc.x + hh.x, cc.y + hh.y, cc.z + hh.z, 0.0f);
+        const real4 cc = d.aabbC[b];
+        const real4 hh = d.aabbH[b];
+        mn = mk4(cc.x - hh.x, cc.y - hh.y, cc.z - hh.z, 0.0f);
+        mx = mk4(cc.x + hh.x, cc.y + hh.y, cc.z + hh.z, 0.0f);
     } else {
         mn = __ldcg(&d.nodeMin[c]);
         mx = __ldcg(&d.nodeMax[c]);
@@ -276,12 +276,12 @@ __global__ void refitKernel(Dev d) {
         if (atomicAdd(&d.nodeFlag[node], 1) == 0)
             return;
         __threadfence();
-        float4 a0, a1, b0, b1;
+        real4 a0, a1, b0, b1;
         const int l = d.nodeL[node], r = d.nodeR[node];
         childBounds(d, l, a0, a1);
         childBounds(d, r, b0, b1);
-        __stcg(&d.nodeMin[node], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f));
-        __stcg(&d.nodeMax[node], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f));
+        __stcg(&d.nodeMin[node], mk4(mmin2(a0.x, b0.x), mmin2(a0.y, b0.y), mmin2(a0.z, b0.z), 0.0f));
+        __stcg(&d.nodeMax[node], mk4(mmax2(a1.x, b1.x), mmax2(a1.y, b1.y), mmax2(a1.z, b1.z), 0.0f));
         const int ml = (l & kLeafBit) ? static_cast<int>(d.sortV[l & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[l]);
         const int mr = (r & kLeafBit) ? static_cast<int>(d.sortV[r & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[r]);
         __stcg(&d.nodeMaxLp[node], ml > mr ? ml : mr);
@@ -317,7 +317,7 @@ __global__ void traverseKernel(Dev d) {
     int found = 0;
     int *stash = d.pairStash + static_cast<size_t>(lpA) * kPairStash;
     if (cnt >= 2) {
-        const float4 c4 = d.aabbC[g], h4 = d.aabbH[g];
+        const real4 c4 = d.aabbC[g], h4 = d.aabbH[g];
         const f3 aMin{c4.x - h4.x, c4.y - h4.y, c4.z - h4.z};
         const f3 aMax{c4.x + h4.x, c4.y + h4.y, c4.z + h4.z};
         int stack[kStack];
@@ -333,7 +333,7 @@ __global__ void traverseKernel(Dev d) {
                     const int lpB = listPos(d, b);
                     if (lpB <= lpA)
                         continue;
-                    const float4 bc = d.aabbC[b], bh = d.aabbH[b];
+                    const real4 bc = d.aabbC[b], bh = d.aabbH[b];
                     const f3 bMin{bc.x - bh.x, bc.y - bh.y, bc.z - bh.z};
                     const f3 bMax{bc.x + bh.x, bc.y + bh.y, bc.z + bh.z};
                     if (overlapClosed(aMin, aMax, bMin, bMax)) {
@@ -349,7 +349,7 @@ __global__ void traverseKernel(Dev d) {
                 } else {
                     if (d.nodeMaxLp[c] <= lpA)
                         continue; // every leaf below was emitted by a partner with a smaller position
-                    const float4 mn = d.nodeMin[c], mx = d.nodeMax[c];
+                    const real4 mn = d.nodeMin[c], mx = d.nodeMax[c];
                     if (overlapClosed(aMin, aMax, f3{mn.x, mn.y, mn.z}, f3{mx.x, mx.y, mx.z})) {
                         if (sp < kStack)
                             stack[sp++] = c;
@@ -399,7 +399,7 @@ __device__ __forceinline__ void filterAt(Dev d, int k) {
     const uint64_t key = d.pairs[k];
     const int a = d.lpToBody[static_cast<int>(key >> 32)];
     const int b = d.lpToBody[static_cast<int>(key & 0xffffffffu)];
-    const float4 ac = d.aabbC[a], ah = d.aabbH[a], bc = d.aabbC[b], bh = d.aabbH[b];
+    const real4 ac = d.aabbC[a], ah = d.aabbH[a], bc = d.aabbC[b], bh = d.aabbH[b];
     const bool bounds = overlapClosed(f3{ac.x - ah.x, ac.y - ah.y, ac.z - ah.z}, f3{ac.x + ah.x, ac.y + ah.y, ac.z + ah.z},
                                       f3{bc.x - bh.x, bc.y - bh.y, bc.z - bh.z}, f3{bc.x + bh.x, bc.y + bh.y, bc.z + bh.z});
     const int4 ma = d.meta[a], mb = d.meta[b];

@@ -14,7 +14,7 @@ __global__ void packStateKernel(Dev d, int first, int count, float *out) {
     if (i >= count)
         return;
     const int g = first + i;
-    const float4 x = d.x[g], q = d.q[g], v = d.v[g], w = d.w[g];
+    const real4 x = d.x[g], q = d.q[g], v = d.v[g], w = d.w[g];
     float *p = out, *o = out + 3 * count, *vv = out + 7 * count, *ww = out + 10 * count;
     p[3 * i] = x.x;
     p[3 * i + 1] = x.y;
@@ -52,17 +52,17 @@ __global__ void unpackStateKernel(Dev d, int first, int count, const float *in, 
     const int g = first + i;
     const float *p = in, *o = in + 3 * count, *vv = in + 7 * count, *ww = in + 10 * count;
     if (mask & 1) {
-        const float4 x = d.x[g];
-        d.x[g] = make_float4(p[3 * i], p[3 * i + 1], p[3 * i + 2], x.w);
+        const real4 x = d.x[g];
+        d.x[g] = mk4(p[3 * i], p[3 * i + 1], p[3 * i + 2], x.w);
     }
     if (mask & 2)
-        d.q[g] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+        d.q[g] = mk4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
     if (mask & 4) {
-        const float4 v = d.v[g];
-        d.v[g] = make_float4(vv[3 * i], vv[3 * i + 1], vv[3 * i + 2], v.w);
+        const real4 v = d.v[g];
+        d.v[g] = mk4(vv[3 * i], vv[3 * i + 1], vv[3 * i + 2], v.w);
     }
     if (mask & 8)
-        d.w[g] = make_float4(ww[3 * i], ww[3 * i + 1], ww[3 * i + 2], 0.0f);
+        d.w[g] = mk4(ww[3 * i], ww[3 * i + 1], ww[3 * i + 2], 0.0f);
 }
 
 } // namespace

@@ -109,7 +109,7 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
     const ManifoldBuf S = d.stage;
     const int2 ab = L.ab[i];
     const int a = ab.x, b = ab.y;
-    const float4 xa4 = d.x[a], xb4 = d.x[b];
+    const real4 xa4 = d.x[a], xb4 = d.x[b];
     const bool dynA = xa4.w > 0.0f, dynB = xb4.w > 0.0f;
     const bool awakeA = dynA && d.sleep[a].x == 0, awakeB = dynB && d.sleep[b].x == 0;
     int oldN = L.count[i];
@@ -150,18 +150,18 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
         oldN = dorm.y;
     const f3 xa = xyz(xa4), xb = xyz(xb4);
     const q4 qa = asq(d.q[a]), qb = asq(d.q[b]);
-    const float4 ma4 = d.moment[a], mb4 = d.moment[b];
-    const float mu = sqrtf(ma4.w * mb4.w);
+    const real4 ma4 = d.moment[a], mb4 = d.moment[b];
+    const real mu = msqrt(ma4.w * mb4.w);
 
     // Speculative margin (Manifold::collide, collide.cpp:1100-1120).
-    float margin = p.specMargin;
+    real margin = p.specMargin;
     if (margin > 0.0f) {
-        const float horizon = p.collisionDt;
-        const float4 va4 = d.v[a], vb4 = d.v[b];
-        const float gA = dynA ? va4.w : 0.0f;
-        const float gB = dynB ? vb4.w : 0.0f;
+        const real horizon = p.collisionDt;
+        const real4 va4 = d.v[a], vb4 = d.v[b];
+        const real gA = dynA ? va4.w : 0.0f;
+        const real gB = dynB ? vb4.w : 0.0f;
         const f3 disp = add(scale(sub(xyz(va4), xyz(vb4)), horizon), f3{0, 0, (gA - gB) * horizon * horizon});
-        const float ra = d.size[a].w, rb = d.size[b].w;
+        const real ra = d.size[a].w, rb = d.size[b].w;
         margin += length(disp) + (ra * length(xyz(d.w[a])) + rb * length(xyz(d.w[b]))) * horizon;
     }
     NContact nc[kMaxContacts];
@@ -176,7 +176,7 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
     const f3 r0 = mrow(basis, 0), r1 = mrow(basis, 1), r2 = mrow(basis, 2);
 
     f3 newK[kMaxContacts], newLam[kMaxContacts];
-    float newBeta[kMaxContacts], prevErr[kMaxContacts];
+    real newBeta[kMaxContacts], prevErr[kMaxContacts];
     int newStick[kMaxContacts];
     for (int c = 0; c < kMaxContacts; c++) {
         newK[c] = f3{0, 0, 0};
@@ -199,8 +199,8 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
                 j = t;
         if (j >= 0) {
             const f3 newRA = nc[c].rA, newRB = nc[c].rB;
-            const float4 oRA = L.rA[cslot(d, i, j)], oRB = L.rB[cslot(d, i, j)];
-            const float4 oLam = L.lam[cslot(d, i, j)];
+            const real4 oRA = L.rA[cslot(d, i, j)], oRB = L.rB[cslot(d, i, j)];
+            const real4 oLam = L.lam[cslot(d, i, j)];
             nc[c].rA = xyz(oRA);
             nc[c].rB = xyz(oRB);
             prevErr[c] = smax(0.0f, COLLISION_MARGIN - L.C0[cslot(d, i, j)].x);
@@ -217,7 +217,7 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
                 const f3 oldB = add(xb, qrot(qb, xyz(oRB)));
                 const f3 nA = add(xa, qrot(qa, newRA));
                 const f3 nB = add(xb, qrot(qb, newRB));
-                const float drift = smax(length(sub(oldA, nA)), length(sub(oldB, nB)));
+                const real drift = smax(length(sub(oldA, nA)), length(sub(oldB, nB)));
                 if (drift > p.stickDriftHeal) {
                     nc[c].rA = newRA;
                     nc[c].rB = newRB;
@@ -246,7 +246,7 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
                 S.rB[cslot(d, i, j)] = L.rB[cslot(d, i, j)];
                 S.C0[cslot(d, i, j)] = L.C0[cslot(d, i, j)];
                 S.k[cslot(d, i, j)] = L.k[cslot(d, i, j)];
-                S.lam[cslot(d, i, j)] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                S.lam[cslot(d, i, j)] = mk4(0.0f, 0.0f, 0.0f, 0.0f);
             }
             S.dormant[i] = make_int2(dorm.x + 1, oldN);
             d.mActive[i] = 1;
@@ -264,11 +264,11 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
         f3 C0 = add(basisMul(r0, r1, r2, sub(pA, pB)), f3{COLLISION_MARGIN, 0, 0});
         if (C0.x < -p.maxPen)
             C0.x = -p.maxPen;
-        float beta = 1.0f;
+        real beta = 1.0f;
         if (p.adaptiveBeta && prevErr[c] >= 0.0f) {
-            const float err = smax(0.0f, COLLISION_MARGIN - C0.x);
-            const float fl = p.adaptiveFloor;
-            float sc = newBeta[c];
+            const real err = smax(0.0f, COLLISION_MARGIN - C0.x);
+            const real fl = p.adaptiveFloor;
+            real sc = newBeta[c];
             if (err <= fl)
                 sc = smax(sc * 0.5f, 1.0f);
             else if (prevErr[c] <= fl)
@@ -403,7 +403,7 @@ __device__ __forceinline__ f3 jointAngError(const Dev &d, int f) {
     return scale(qdiff(qa, asq(d.q[ab.y])), d.fPar[f].w);
 }
 
-__device__ __forceinline__ f3 warmPenalty(f3 k, float gamma, float stiffness) {
+__device__ __forceinline__ f3 warmPenalty(f3 k, real gamma, real stiffness) {
     return f3{smin(sclamp(k.x * gamma, PENALTY_MIN, PENALTY_MAX), stiffness),
               smin(sclamp(k.y * gamma, PENALTY_MIN, PENALTY_MAX), stiffness),
               smin(sclamp(k.z * gamma, PENALTY_MIN, PENALTY_MAX), stiffness)};
@@ -421,7 +421,7 @@ __global__ void forceInitKernel(Dev d, StepParams p) {
         d.fKeep[f] = 1;
         return;
     }
-    const float4 par = d.fPar[f];
+    const real4 par = d.fPar[f];
     d.fC0L[f] = f4(jointLinError(d, f), 0.0f);
     d.fC0A[f] = f4(jointAngError(d, f), 0.0f);
     d.fLL[f] = f4(scale(scale(xyz(d.fLL[f]), p.alpha), p.gamma), 0.0f);
@@ -473,7 +473,7 @@ void prepareNarrowPhase() {
     narrow::RimTable t{};
     for (int i = 0; i < narrow::kRimSamples; ++i) {
         const int step = i * 5 % narrow::kRimSamples;
-        const float a = 6.28318530718f * (float)step / (float)narrow::kRimSamples;
+        const real a = 6.28318530718f * (real)step / (real)narrow::kRimSamples;
         t.c[i] = std::cos(a);
         t.s[i] = std::sin(a);
     }

@@ -31,8 +31,8 @@ constexpr int kBrakeThreads = 512;
 // Movable and in this step's update set (solver_projection.cpp:87, 105-106, 194-195).
 __device__ __forceinline__ bool movable(const Dev &d, int g) { return d.x[g].w > 0.0f && inUpdate(d, g); }
 
-__device__ __forceinline__ float angularCompliance(f3 I, f3 axis) {
-    float sum = 0.0f;
+__device__ __forceinline__ real angularCompliance(f3 I, f3 axis) {
+    real sum = 0.0f;
     if (I.x > 0.0f)
         sum += axis.x * axis.x / I.x;
     if (I.y > 0.0f)
@@ -84,7 +84,7 @@ __device__ __forceinline__ void projActiveAt(Dev d, int m) {
             const int ci = cslot(d, m, k);
             const f3 rA = qrot(qa, xyz(L.rA[ci]));
             const f3 rB = qrot(qb, xyz(L.rB[ci]));
-            const float gap = dot(nrm, sub(add(xa, rA), add(xb, rB)));
+            const real gap = dot(nrm, sub(add(xa, rA), add(xb, rB)));
             if (gap > 0.0f) {
                 spec = 1;
                 break;
@@ -166,11 +166,11 @@ __device__ __forceinline__ bool published(const Dev &d, int k) { return k < 0 ||
 struct BrakeLoad {
     int a, b, n, locksA, locksB;
     bool moveA, moveB;
-    float invMassA, invMassB;
+    real invMassA, invMassB;
     f3 nrm, IA, IB;
     q4 qa, qb;
     f3 rA[kMaxContacts], rB[kMaxContacts];
-    float gap[kMaxContacts];
+    real gap[kMaxContacts];
 };
 
 __device__ __forceinline__ void brakeLoad(const Dev &d, int m, BrakeLoad &bl) {
@@ -178,7 +178,7 @@ __device__ __forceinline__ void brakeLoad(const Dev &d, int m, BrakeLoad &bl) {
     const int2 ab = L.ab[m];
     bl.a = ab.x;
     bl.b = ab.y;
-    const float4 xa4 = d.x[ab.x], xb4 = d.x[ab.y];
+    const real4 xa4 = d.x[ab.x], xb4 = d.x[ab.y];
     bl.moveA = movable(d, ab.x);
     bl.moveB = movable(d, ab.y);
     bl.invMassA = bl.moveA ? 1.0f / xa4.w : 0.0f;
@@ -206,9 +206,9 @@ __device__ __forceinline__ void brakeLoad(const Dev &d, int m, BrakeLoad &bl) {
 
 // One manifold of the brake sweep (solver_projection.cpp:98-166) on velocities held by the caller;
 // false when no contact braked (velocities untouched).
-__device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, float window, f3 &va, f3 &wa, f3 &vb, f3 &wb) {
+__device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, real window, f3 &va, f3 &wa, f3 &vb, f3 &wb) {
     f3 patchRA{0, 0, 0}, patchRB{0, 0, 0};
-    float velErr = 0.0f;
+    real velErr = 0.0f;
     int braked = 0;
 #pragma unroll
     for (int k = 0; k < kMaxContacts; k++) {
@@ -216,8 +216,8 @@ __device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, float window, f3
             continue;
         const f3 vAp = add(va, cross(wa, bl.rA[k]));
         const f3 vBp = add(vb, cross(wb, bl.rB[k]));
-        const float vn = dot(sub(vAp, vBp), bl.nrm);
-        const float target = -bl.gap[k] / window;
+        const real vn = dot(sub(vAp, vBp), bl.nrm);
+        const real target = -bl.gap[k] / window;
         if (vn < target) {
             patchRA = add(patchRA, bl.rA[k]);
             patchRB = add(patchRB, bl.rB[k]);
@@ -227,12 +227,12 @@ __device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, float window, f3
     }
     if (braked == 0)
         return false;
-    const float invN = 1.0f / static_cast<float>(braked);
+    const real invN = 1.0f / static_cast<real>(braked);
     const f3 tA = bl.moveA ? qrot(qconj(bl.qa), cross(scale(patchRA, invN), bl.nrm)) : f3{0, 0, 0};
     const f3 tB = bl.moveB ? qrot(qconj(bl.qb), cross(scale(patchRB, invN), bl.nrm)) : f3{0, 0, 0};
-    const float K = bl.invMassA + bl.invMassB + (bl.moveA ? angularCompliance(bl.IA, tA) : 0.0f) +
+    const real K = bl.invMassA + bl.invMassB + (bl.moveA ? angularCompliance(bl.IA, tA) : 0.0f) +
                     (bl.moveB ? angularCompliance(bl.IB, tB) : 0.0f);
-    const float j = velErr * invN / K;
+    const real j = velErr * invN / K;
     if (bl.moveA) {
         f3 dv = scale(bl.nrm, bl.invMassA * j);
         f3 dw = scale(angularResponse(bl.IA, bl.qa, tA), j);
@@ -252,7 +252,7 @@ __device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, float window, f3
     return true;
 }
 
-__global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window) {
+__global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, real window) {
     const int ns = d.ctr[C_SPECN];
     const int stride = gridDim.x * blockDim.x;
     volatile int *errors = d.ctr + C_ERRORS;
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, float window
             }
             __nanosleep(64);
         }
-        const float4 va4 = __ldcg(&d.v[bl.a]), vb4 = __ldcg(&d.v[bl.b]);
+        const real4 va4 = __ldcg(&d.v[bl.a]), vb4 = __ldcg(&d.v[bl.b]);
         f3 va = xyz(va4), wa = xyz(__ldcg(&d.w[bl.a])), vb = xyz(vb4), wb = xyz(__ldcg(&d.w[bl.b]));
         if (brakeSolve(bl, window, va, wa, vb, wb)) {
             if (bl.moveA) {
@@ -300,7 +300,7 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
     // The adjacency entries of sides A and B; only bodies with mass have entries (a static side's
     // slot is not written by the adjacency build and is not touched here).
     const int2 slot = d.stampSlot[m];
-    const float4 xa4 = d.x[a], xb4 = d.x[b];
+    const real4 xa4 = d.x[a], xb4 = d.x[b];
     if (xa4.w > 0.0f)
         d.projLin[slot.x].w = 0.0f;
     if (xb4.w > 0.0f)
@@ -309,21 +309,21 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
     const int n = L.count[m];
     if (n == 0 || (!moveA && !moveB))
         return;
-    const float invMassA = moveA ? 1.0f / xa4.w : 0.0f;
-    const float invMassB = moveB ? 1.0f / xb4.w : 0.0f;
+    const real invMassA = moveA ? 1.0f / xa4.w : 0.0f;
+    const real invMassB = moveB ? 1.0f / xb4.w : 0.0f;
     const f3 nrm = xyz(L.b0[m]);
     const q4 qa = asq(d.q[a]), qb = asq(d.q[b]);
     const f3 xa = xyz(xa4), xb = xyz(xb4);
     const m3 rotA = qmat(qa), rotB = qmat(qb);
     f3 patchRA{0, 0, 0}, patchRB{0, 0, 0};
-    float patchDepth = 0.0f;
+    real patchDepth = 0.0f;
     int corrected = 0;
     for (int k = 0; k < n; k++) {
         const int ci = cslot(d, m, k);
         const f3 rA = mul(rotA, xyz(L.rA[ci]));
         const f3 rB = mul(rotB, xyz(L.rB[ci]));
-        const float rawDepth = -dot(nrm, sub(add(xa, rA), add(xb, rB)));
-        const float depth = rawDepth - p.projSlop;
+        const real rawDepth = -dot(nrm, sub(add(xa, rA), add(xb, rB)));
+        const real depth = rawDepth - p.projSlop;
         if (depth > 0.0f) {
             patchRA = add(patchRA, rA);
             patchRB = add(patchRB, rB);
@@ -333,15 +333,15 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
     }
     if (corrected == 0)
         return;
-    const float invN = 1.0f / static_cast<float>(corrected);
+    const real invN = 1.0f / static_cast<real>(corrected);
     world = w;
-    depthBits = __float_as_int(patchDepth * invN); // positive: the bits order like the floats
+    depthBits = fbits(patchDepth * invN); // positive: the bits order like the floats
     const f3 IA = xyz(d.moment[a]), IB = xyz(d.moment[b]);
     const f3 tA = moveA ? qrot(qconj(qa), cross(scale(patchRA, invN), nrm)) : f3{0, 0, 0};
     const f3 tB = moveB ? qrot(qconj(qb), cross(scale(patchRB, invN), nrm)) : f3{0, 0, 0};
-    const float K = invMassA + invMassB + (moveA ? angularCompliance(IA, tA) : 0.0f) +
+    const real K = invMassA + invMassB + (moveA ? angularCompliance(IA, tA) : 0.0f) +
                     (moveB ? angularCompliance(IB, tB) : 0.0f);
-    const float dp = p.projBeta * patchDepth * invN / K;
+    const real dp = p.projBeta * patchDepth * invN / K;
     if (moveA) {
         d.projLin[slot.x] = f4(scale(nrm, invMassA * dp), 1.0f);
         d.projAng[slot.x] = f4(scale(angularResponse(IA, qa, tA), dp), 0.0f);
@@ -381,7 +381,7 @@ __global__ void projBodyKernel(Dev d, StepParams p) {
     for (int e = d.adjStart[g]; e < d.adjStart[g + 1]; e++) {
         if (nf > 0 && static_cast<int>(d.adjSeq[e]) < nf)
             continue;
-        const float4 cl = d.projLin[e];
+        const real4 cl = d.projLin[e];
         if (cl.w == 0.0f)
             continue;
         const f3 ca = xyz(d.projAng[e]);
@@ -394,32 +394,32 @@ __global__ void projBodyKernel(Dev d, StepParams p) {
             sa = sub(sa, ca);
         }
     }
-    const float invCount = 1.0f / static_cast<float>(cnt > 1 ? cnt : 1);
+    const real invCount = 1.0f / static_cast<real>(cnt > 1 ? cnt : 1);
     f3 dl = scale(sl, invCount);
     f3 da = scale(sa, invCount);
     const int locks = d.meta[g].w;
     maskLocked(locks & 0xff, dl);
     maskLocked((locks >> 8) & 0xff, da);
-    const float cap = p.projMaxCorr;
+    const real cap = p.projMaxCorr;
     if (cap > 0.0f) {
-        const float moved = length(dl);
+        const real moved = length(dl);
         if (moved > cap)
             dl = scale(dl, cap / moved);
-        const float turned = length(da);
+        const real turned = length(da);
         if (turned > cap)
             da = scale(da, cap / turned);
     }
-    const float4 x4 = d.x[g];
+    const real4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), dl), x4.w);
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
 
-__global__ void projCheckKernel(Dev d, float tolerance) {
+__global__ void projCheckKernel(Dev d, real tolerance) {
     const int nWorlds = d.ctr[C_WORLDS];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nWorlds)
         return;
-    if (!d.wStop[w] && __int_as_float(d.wMaxDepth[w]) <= tolerance)
+    if (!d.wStop[w] && bitsf(d.wMaxDepth[w]) <= tolerance)
         d.wStop[w] = 1;
     d.wMaxDepth[w] = 0;
 }
@@ -461,10 +461,10 @@ void launchProjActive(const Dev &d, cudaStream_t s) {
 }
 
 // Runs right after launchProjActive, whose scan left each candidate's rank in d.pairValid.
-void launchBrake(const Dev &d, float window, cudaStream_t s) {
+void launchBrake(const Dev &d, real window, cudaStream_t s) {
     ++launchCount(); brakePredKernel<<<residentGrid(brakePredKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, d.pairValid);
     Dev dd = d;
-    float win = window;
+    real win = window;
     void *args[] = {&dd, &win};
     ++launchCount();
     cudaLaunchCooperativeKernel(reinterpret_cast<void *>(brakeKernel), dim3(brakeGridBlocks()), dim3(kBrakeThreads),
@@ -473,7 +473,7 @@ void launchBrake(const Dev &d, float window, cudaStream_t s) {
 
 void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
     ++launchCount(); projStartKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
-    const float tol = smax(p.projSlop * 0.01f, 1.0e-6f);
+    const real tol = smax(p.projSlop * 0.01f, 1.0e-6f);
     for (int it = 0; it < p.projIters; it++) {
         ++launchCount(); projManifoldKernel<<<residentGrid(projManifoldKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
         ++launchCount(); projBodyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);

@@ -16,27 +16,27 @@ namespace {
 constexpr int kThreads = 256;
 
 __device__ __forceinline__ f3 localHalfExtent(const Dev &d, int g) {
-    const float4 s = d.size[g];
+    const real4 s = d.size[g];
     const int shape = (d.meta[g].w >> 18) & 0x3;
     return shape == 1 ? f3{s.x, s.x, s.x} : (shape == 2 ? f3{s.x, s.x, s.z * 0.5f} : scale(xyz(s), 0.5f));
 }
 
 // The reference's per-body ray test (solver_query.cpp:48-133): distance in units of `dir` or
 // +infinity, and the hit point in the body's frame.
-__device__ float rayTest(const Dev &d, int g, f3 origin, f3 dir, f3 &local) {
-    const float inf = __int_as_float(0x7f800000);
+__device__ real rayTest(const Dev &d, int g, f3 origin, f3 dir, f3 &local) {
+    const real inf = bitsf(0x7f800000);
     const q4 inv = qconj(asq(d.q[g]));
     const f3 o = qrot(inv, sub(origin, xyz(d.x[g])));
     const f3 dd = qrot(inv, dir);
     if (((d.meta[g].w >> 18) & 0x3) == 1) {
-        const float r = d.size[g].x;
-        const float b = dot(o, dd);
-        const float c = length2(o) - r * r;
-        const float disc = b * b - c;
+        const real r = d.size[g].x;
+        const real b = dot(o, dd);
+        const real c = length2(o) - r * r;
+        const real disc = b * b - c;
         if (disc < 0.0f)
             return inf;
-        const float sq = sqrtf(disc);
-        float t = -b - sq;
+        const real sq = msqrt(disc);
+        real t = -b - sq;
         if (t < 0.0f)
             t = -b + sq;
         if (t < 0.0f)
@@ -45,19 +45,19 @@ __device__ float rayTest(const Dev &d, int g, f3 origin, f3 dir, f3 &local) {
         return t;
     }
     const f3 half = localHalfExtent(d, g);
-    float tEnter = 0.0f, tExit = inf;
+    real tEnter = 0.0f, tExit = inf;
     for (int i = 0; i < 3; ++i) {
-        const float di = at(dd, i), oi = at(o, i), hi = at(half, i);
-        if (fabsf(di) < 1.0e-6f) {
+        const real di = at(dd, i), oi = at(o, i), hi = at(half, i);
+        if (mabs(di) < 1.0e-6f) {
             if (oi < -hi || oi > hi)
                 return inf;
             continue;
         }
-        const float invD = 1.0f / di;
-        float t0 = (-hi - oi) * invD;
-        float t1 = (hi - oi) * invD;
+        const real invD = 1.0f / di;
+        real t0 = (-hi - oi) * invD;
+        real t1 = (hi - oi) * invD;
         if (t0 > t1) {
-            const float tmp = t0;
+            const real tmp = t0;
             t0 = t1;
             t1 = tmp;
         }
@@ -66,7 +66,7 @@ __device__ float rayTest(const Dev &d, int g, f3 origin, f3 dir, f3 &local) {
         if (tEnter > tExit)
             return inf;
     }
-    const float tHit = tEnter >= 0.0f ? tEnter : tExit;
+    const real tHit = tEnter >= 0.0f ? tEnter : tExit;
     if (tHit < 0.0f)
         return inf;
     local = add(o, scale(dd, tHit));
@@ -92,10 +92,10 @@ __global__ void pickKernel(Dev d, int base, int count, const float *rays, int nR
         return;
     const float *ray = rays + 6 * r;
     f3 local;
-    const float dist = rayTest(d, g, f3{ray[0], ray[1], ray[2]}, f3{ray[3], ray[4], ray[5]}, local);
-    if (!(dist < __int_as_float(0x7f800000)))
+    const real dist = rayTest(d, g, f3{ray[0], ray[1], ray[2]}, f3{ray[3], ray[4], ray[5]}, local);
+    if (!(dist < bitsf(0x7f800000)))
         return;
-    const unsigned bits = static_cast<unsigned>(__float_as_int(dist + 0.0f));
+    const unsigned bits = static_cast<unsigned>(fbits(dist + 0.0f));
     const unsigned lp = static_cast<unsigned>(listPos(d, g) - base);
     atomicMin(best + r, (static_cast<unsigned long long>(bits) << 32) | lp);
 }
@@ -131,9 +131,9 @@ __global__ void overlapFlagKernel(Dev d, int base, int count, f3 lo, f3 hi, unsi
     if ((static_cast<unsigned>(d.meta[g].y) & mask) != 0) {
         const m3 rot = qmat(asq(d.q[g]));
         const f3 h = localHalfExtent(d, g);
-        const f3 wx{(fabsf(rot.c0.x) * h.x + fabsf(rot.c1.x) * h.y) + fabsf(rot.c2.x) * h.z,
-                    (fabsf(rot.c0.y) * h.x + fabsf(rot.c1.y) * h.y) + fabsf(rot.c2.y) * h.z,
-                    (fabsf(rot.c0.z) * h.x + fabsf(rot.c1.z) * h.y) + fabsf(rot.c2.z) * h.z};
+        const f3 wx{(mabs(rot.c0.x) * h.x + mabs(rot.c1.x) * h.y) + mabs(rot.c2.x) * h.z,
+                    (mabs(rot.c0.y) * h.x + mabs(rot.c1.y) * h.y) + mabs(rot.c2.y) * h.z,
+                    (mabs(rot.c0.z) * h.x + mabs(rot.c1.z) * h.y) + mabs(rot.c2.z) * h.z};
         const f3 c = xyz(d.x[g]);
         const f3 bmin = sub(c, wx), bmax = add(c, wx);
         hit = !(bmin.x > hi.x || bmin.y > hi.y || bmin.z > hi.z || lo.x > bmax.x || lo.y > bmax.y || lo.z > bmax.z);

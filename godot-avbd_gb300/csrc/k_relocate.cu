@@ -111,7 +111,7 @@ __global__ void compactKernel(const T *src, T *dst, const int *keep, const int *
 }
 
 // Strided records (kExtF4 float4 per force) follow their force.
-__global__ void compactExtKernel(const float4 *src, float4 *dst, const int *keep, const int *rank, int n) {
+__global__ void compactExtKernel(const real4 *src, real4 *dst, const int *keep, const int *rank, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * kExtF4)
         return;
@@ -151,8 +151,8 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
     ++launchCount(); slotMapKernel<<<grid(nOld), kThreads, 0, s>>>(d, nOld, remap, slotMap);
 
     // Bodies, through a staging array (slots only move down, so an in-place move would race).
-    float4 *tmp4 = d.relocF4;
-    for (float4 *arr : {d.x, d.q, d.x0, d.q0, d.xi, d.qi, d.v, d.w, d.vprev, d.size, d.moment})
+    real4 *tmp4 = d.relocF4;
+    for (real4 *arr : {d.x, d.q, d.x0, d.q0, d.xi, d.qi, d.v, d.w, d.vprev, d.size, d.moment})
         moveArray(arr, tmp4, slotMap, nOld, nNew, s);
     moveArray(d.sleep, reinterpret_cast<int2 *>(tmp4), slotMap, nOld, nNew, s);
     int4 *tmpMeta = reinterpret_cast<int4 *>(tmp4);
@@ -175,16 +175,16 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
         int2 *abTmp = reinterpret_cast<int2 *>(tmp4) + d.FF;
         ++launchCount(); compactKernel<int2><<<grid(nForces), kThreads, 0, s>>>(abNew, abTmp, d.fKeep, rank, nForces);
         cudaMemcpyAsync(d.fAB, abTmp, sizeof(int2) * static_cast<size_t>(nForces), cudaMemcpyDeviceToDevice, s);
-        for (float4 *arr : {d.fRA, d.fRB, d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA, d.fPar})
+        for (real4 *arr : {d.fRA, d.fRB, d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA, d.fPar})
             compactArray(arr, tmp4, d.fKeep, rank, nForces, s);
         int *tmpI = reinterpret_cast<int *>(tmp4);
         compactArray(d.fKind, tmpI, d.fKeep, rank, nForces, s);
         compactArray(d.fBroken, tmpI, d.fKeep, rank, nForces, s);
         // Generic-joint records (relocF4 holds FF * kExtF4 float4).
-        float4 *extTmp = d.relocF4;
+        real4 *extTmp = d.relocF4;
         ++launchCount();
         compactExtKernel<<<grid(nForces * kExtF4), kThreads, 0, s>>>(d.fExt, extTmp, d.fKeep, rank, nForces);
-        cudaMemcpyAsync(d.fExt, extTmp, sizeof(float4) * static_cast<size_t>(nForces) * kExtF4,
+        cudaMemcpyAsync(d.fExt, extTmp, sizeof(real4) * static_cast<size_t>(nForces) * kExtF4,
                         cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(d.ctr + C_FORCES, d.ctr + C_TMP, sizeof(int), cudaMemcpyDeviceToDevice, s);
     }

@@ -183,9 +183,9 @@ __global__ void islandApplyKernel(Dev d, StepParams p) {
     const int2 s = d.sleep[g];
     if (!s.x) {
         d.sleep[g] = make_int2(1, s.y);
-        const float4 v = d.v[g];
-        d.v[g] = make_float4(0.0f, 0.0f, 0.0f, v.w);
-        d.w[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const real4 v = d.v[g];
+        d.v[g] = mk4(0.0f, 0.0f, 0.0f, v.w);
+        d.w[g] = mk4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 

@@ -31,7 +31,7 @@ struct Blk {
 };
 
 // Block::Block (types.hpp:157-172).
-__device__ __forceinline__ Blk makeBlock(float mass, f3 moment, float dtSq, f3 x, f3 xi, q4 q, q4 qi) {
+__device__ __forceinline__ Blk makeBlock(real mass, f3 moment, real dtSq, f3 x, f3 xi, q4 q, q4 qi) {
     Blk b;
     const f3 mo = divs(f3{mass, mass, mass}, dtSq);
     b.lin = mdiag(mo.x, mo.y, mo.z);
@@ -46,12 +46,12 @@ __device__ __forceinline__ Blk makeBlock(float mass, f3 moment, float dtSq, f3 x
 
 // ---- 6x6 solves (maths.h:156-343) ----
 
-__device__ bool ldlt6(const float a[6][6], const float b[6], float x[6]) {
-    float l[6][6];
-    float dd[6];
+__device__ bool ldlt6(const real a[6][6], const real b[6], real x[6]) {
+    real l[6][6];
+    real dd[6];
 #pragma unroll
     for (int j = 0; j < 6; j++) {
-        float dj = a[j][j];
+        real dj = a[j][j];
 #pragma unroll
         for (int s = 0; s < j; s++)
             dj -= l[j][s] * l[j][s] * dd[s];
@@ -61,17 +61,17 @@ __device__ bool ldlt6(const float a[6][6], const float b[6], float x[6]) {
         l[j][j] = 1.0f;
 #pragma unroll
         for (int i = j + 1; i < 6; i++) {
-            float lij = a[i][j];
+            real lij = a[i][j];
 #pragma unroll
             for (int s = 0; s < j; s++)
                 lij -= l[i][s] * l[j][s] * dd[s];
             l[i][j] = lij / dd[j];
         }
     }
-    float z[6];
+    real z[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) {
-        float v = b[i];
+        real v = b[i];
 #pragma unroll
         for (int s = 0; s < i; s++)
             v -= l[i][s] * z[s];
@@ -82,32 +82,32 @@ __device__ bool ldlt6(const float a[6][6], const float b[6], float x[6]) {
         x[i] = z[i] / dd[i];
 #pragma unroll
     for (int i = 5; i >= 0; i--) {
-        float v = x[i];
+        real v = x[i];
 #pragma unroll
         for (int s = i + 1; s < 6; s++)
             v -= l[s][i] * x[s];
         x[i] = v;
     }
-    float worst = 0.0f;
+    real worst = 0.0f;
 #pragma unroll
     for (int i = 0; i < 6; i++)
-        worst = smax(worst, fabsf(x[i]));
+        worst = smax(worst, mabs(x[i]));
     return isfinite(worst) && worst < 1.0e1f;
 }
 
-__device__ __forceinline__ bool ldlt6Pivoted(const float aIn[6][6], const float b[6], float x[6]) {
-    float a[6][6];
+__device__ __forceinline__ bool ldlt6Pivoted(const real aIn[6][6], const real b[6], real x[6]) {
+    real a[6][6];
     for (int r = 0; r < 6; r++)
         for (int c = 0; c < 6; c++)
             a[r][c] = aIn[r][c];
-    float dd[6] = {0, 0, 0, 0, 0, 0};
+    real dd[6] = {0, 0, 0, 0, 0, 0};
     int t[6] = {0, 1, 2, 3, 4, 5};
     bool foundZero = false;
     for (int k = 0; k < 6; k++) {
         int j = k;
-        float best = fabsf(a[k][k]);
+        real best = mabs(a[k][k]);
         for (int i = k + 1; i < 6; i++) {
-            const float cand = fabsf(a[i][i]);
+            const real cand = mabs(a[i][i]);
             if (cand > best) {
                 best = cand;
                 j = i;
@@ -116,24 +116,24 @@ __device__ __forceinline__ bool ldlt6Pivoted(const float aIn[6][6], const float 
         t[k] = j;
         if (j != k) {
             for (int c = 0; c < 6; c++) {
-                const float tmp = a[k][c];
+                const real tmp = a[k][c];
                 a[k][c] = a[j][c];
                 a[j][c] = tmp;
             }
             for (int r = 0; r < 6; r++) {
-                const float tmp = a[r][k];
+                const real tmp = a[r][k];
                 a[r][k] = a[r][j];
                 a[r][j] = tmp;
             }
         }
         if (k > 0) {
-            float temp[6] = {0, 0, 0, 0, 0, 0};
+            real temp[6] = {0, 0, 0, 0, 0, 0};
             for (int i = 0; i < k; i++)
                 temp[i] = dd[i] * a[k][i];
-            float prod[6] = {0, 0, 0, 0, 0, 0};
+            real prod[6] = {0, 0, 0, 0, 0, 0};
             for (int i = 0; i < k; i++)
                 prod[i] = a[k][i] * temp[i];
-            float dotv;
+            real dotv;
             switch (k) {
             case 1: dotv = prod[0]; break;
             case 2: dotv = prod[0] + prod[1]; break;
@@ -143,13 +143,13 @@ __device__ __forceinline__ bool ldlt6Pivoted(const float aIn[6][6], const float 
             }
             a[k][k] -= dotv;
             for (int i = 0; i < k; i++) {
-                const float ti = temp[i];
+                const real ti = temp[i];
                 for (int r = k + 1; r < 6; r++)
                     a[r][k] -= a[r][i] * ti;
             }
         }
-        const float pivot = a[k][k];
-        const bool valid = fabsf(pivot) > 0.0f;
+        const real pivot = a[k][k];
+        const bool valid = mabs(pivot) > 0.0f;
         if (!valid) {
             for (int r = k + 1; r < 6; r++)
                 if (a[r][k] != 0.0f)
@@ -166,38 +166,38 @@ __device__ __forceinline__ bool ldlt6Pivoted(const float aIn[6][6], const float 
     for (int i = 0; i < 6; i++)
         x[i] = b[i];
     for (int k = 0; k < 6; k++) {
-        const float tmp = x[k];
+        const real tmp = x[k];
         x[k] = x[t[k]];
         x[t[k]] = tmp;
     }
     for (int jj = 0; jj < 5; jj++) {
-        const float v = x[jj];
+        const real v = x[jj];
         if (v != 0.0f)
             for (int i = jj + 1; i < 6; i++)
                 x[i] -= a[i][jj] * v;
     }
-    const float tolerance = 1.17549435e-38f; // FLT_MIN
+    const real tolerance = 1.17549435e-38f; // FLT_MIN
     for (int i = 0; i < 6; i++)
-        x[i] = fabsf(dd[i]) > tolerance ? x[i] / dd[i] : 0.0f;
+        x[i] = mabs(dd[i]) > tolerance ? x[i] / dd[i] : 0.0f;
     for (int jj = 5; jj >= 1; jj--) {
-        const float v = x[jj];
+        const real v = x[jj];
         if (v != 0.0f)
             for (int i = jj - 1; i >= 0; i--)
                 x[i] -= a[jj][i] * v;
     }
     for (int k = 5; k >= 0; k--) {
-        const float tmp = x[k];
+        const real tmp = x[k];
         x[k] = x[t[k]];
         x[t[k]] = tmp;
     }
-    float worst = 0.0f;
+    real worst = 0.0f;
     for (int i = 0; i < 6; i++)
-        worst = smax(worst, fabsf(x[i]));
+        worst = smax(worst, mabs(x[i]));
     return isfinite(worst) && worst < 1.0e1f;
 }
 
 // The 6x6 system of Block::solveDelta (types.hpp:176-197): a = [lin crs^T; crs ang], b = -rhs.
-__device__ __forceinline__ void blockSystem(const Blk &k, float a[6][6], float b[6]) {
+__device__ __forceinline__ void blockSystem(const Blk &k, real a[6][6], real b[6]) {
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
@@ -223,7 +223,7 @@ struct Delta {
 // solve()'s pivoted fallback, out of line: the block travels by value, so the fast path's matrix
 // never needs an address and stays in registers.
 __device__ __noinline__ Delta solvePivoted(Blk k) {
-    float a[6][6], b[6], x[6];
+    real a[6][6], b[6], x[6];
     blockSystem(k, a, b);
     Delta r;
     r.ok = ldlt6Pivoted(a, b, x);
@@ -234,7 +234,7 @@ __device__ __noinline__ Delta solvePivoted(Blk k) {
 
 // Block::solveDelta's plain LDLT; false when solve() would fall back.
 __device__ __forceinline__ bool solveBlockFast(const Blk &k, f3 &dl, f3 &da) {
-    float a[6][6], b[6], x[6];
+    real a[6][6], b[6], x[6];
     blockSystem(k, a, b);
     if (!ldlt6(a, b, x))
         return false;
@@ -259,13 +259,13 @@ __device__ __forceinline__ void solveBlock(const Blk &k, f3 &dl, f3 &da) {
 
 // ---- contact terms (manifold.cpp:196-234, 465-570, 583-671) ----
 
-__device__ __forceinline__ void basisHessianD(f3 b0, f3 b1, f3 b2, f3 k, float S[6]) {
-    const float b0x2 = b0.x * b0.x, b0y2 = b0.y * b0.y, b0z2 = b0.z * b0.z;
-    const float b0xy = b0.x * b0.y, b0xz = b0.x * b0.z, b0yz = b0.y * b0.z;
-    const float b1x2 = b1.x * b1.x, b1y2 = b1.y * b1.y, b1z2 = b1.z * b1.z;
-    const float b1xy = b1.x * b1.y, b1xz = b1.x * b1.z, b1yz = b1.y * b1.z;
-    const float b2x2 = b2.x * b2.x, b2y2 = b2.y * b2.y, b2z2 = b2.z * b2.z;
-    const float b2xy = b2.x * b2.y, b2xz = b2.x * b2.z, b2yz = b2.y * b2.z;
+__device__ __forceinline__ void basisHessianD(f3 b0, f3 b1, f3 b2, f3 k, real S[6]) {
+    const real b0x2 = b0.x * b0.x, b0y2 = b0.y * b0.y, b0z2 = b0.z * b0.z;
+    const real b0xy = b0.x * b0.y, b0xz = b0.x * b0.z, b0yz = b0.y * b0.z;
+    const real b1x2 = b1.x * b1.x, b1y2 = b1.y * b1.y, b1z2 = b1.z * b1.z;
+    const real b1xy = b1.x * b1.y, b1xz = b1.x * b1.z, b1yz = b1.y * b1.z;
+    const real b2x2 = b2.x * b2.x, b2y2 = b2.y * b2.y, b2z2 = b2.z * b2.z;
+    const real b2xy = b2.x * b2.y, b2xz = b2.x * b2.z, b2yz = b2.y * b2.z;
     S[0] = k.x * b0x2 + k.y * b1x2 + k.z * b2x2;
     S[1] = k.x * b0xy + k.y * b1xy + k.z * b2xy;
     S[2] = k.x * b0xz + k.y * b1xz + k.z * b2xz;
@@ -280,13 +280,13 @@ __device__ __forceinline__ f3 basisMulD(f3 r0, f3 r1, f3 r2, f3 v) {
 }
 
 struct Cone {
-    float bounds, scale;
+    real bounds, scale;
 };
 
-__device__ __forceinline__ Cone clampForce(f3 &F, float mu) {
+__device__ __forceinline__ Cone clampForce(f3 &F, real mu) {
     F.x = smin(F.x, 0.0f);
-    const float bounds = fabsf(F.x) * mu;
-    const float fs = length2d(F.y, F.z);
+    const real bounds = mabs(F.x) * mu;
+    const real fs = length2d(F.y, F.z);
     if (fs > bounds && fs > 0) {
         F.y = F.y * (bounds / fs);
         F.z = F.z * (bounds / fs);
@@ -307,18 +307,18 @@ struct SharedAcc {
 // One contact's terms of one side's stamp: the unique entries of the angular block (h00, h01, h02,
 // h11, h12, h22), the cross block r x S and the angular right-hand side r x fw.
 struct SideTerms {
-    float h[6];
+    real h[6];
     m3 rs;
     f3 rc;
 };
 
-__device__ __forceinline__ SideTerms sideTerms(const float S[6], f3 r, f3 fw) {
-    const float s00 = S[0], s01 = S[1], s02 = S[2], s11 = S[3], s12 = S[4], s22 = S[5];
+__device__ __forceinline__ SideTerms sideTerms(const real S[6], f3 r, f3 fw) {
+    const real s00 = S[0], s01 = S[1], s02 = S[2], s11 = S[3], s12 = S[4], s22 = S[5];
     const m3 Sm = mcols(f3{s00, s01, s02}, f3{s01, s11, s12}, f3{s02, s12, s22});
     SideTerms t;
     t.rs = mcols(cross(r, Sm.c0), cross(r, Sm.c1), cross(r, Sm.c2));
-    const float rx2 = r.x * r.x, ry2 = r.y * r.y, rz2 = r.z * r.z;
-    const float rxy = r.x * r.y, rxz = r.x * r.z, ryz = r.y * r.z;
+    const real rx2 = r.x * r.x, ry2 = r.y * r.y, rz2 = r.z * r.z;
+    const real rxy = r.x * r.y, rxz = r.x * r.z, ryz = r.y * r.z;
     t.h[0] = s11 * rz2 - 2.0f * s12 * ryz + s22 * ry2;
     t.h[1] = s12 * rxz + s02 * ryz - s22 * rxy - s01 * rz2;
     t.h[2] = s12 * rxy + s01 * ryz - s11 * rxz - s02 * ry2;
@@ -329,15 +329,15 @@ __device__ __forceinline__ SideTerms sideTerms(const float S[6], f3 r, f3 fw) {
     return t;
 }
 
-__device__ __forceinline__ void stampContact(const float S[6], f3 r, f3 fw, SideAcc &acc) {
+__device__ __forceinline__ void stampContact(const real S[6], f3 r, f3 fw, SideAcc &acc) {
     const SideTerms t = sideTerms(S, r, fw);
-    const float *h = t.h;
+    const real *h = t.h;
     acc.ang = madd(acc.ang, mcols(f3{h[0], h[1], h[2]}, f3{h[1], h[3], h[4]}, f3{h[2], h[4], h[5]}));
     acc.crs = madd(acc.crs, t.rs);
     acc.rhsAng = add(acc.rhsAng, t.rc);
 }
 
-__device__ __forceinline__ void stampShared(const float S[6], f3 fw, SharedAcc &acc) {
+__device__ __forceinline__ void stampShared(const real S[6], f3 fw, SharedAcc &acc) {
     acc.lin = madd(acc.lin, mcols(f3{S[0], S[1], S[2]}, f3{S[1], S[3], S[4]}, f3{S[2], S[4], S[5]}));
     acc.rhsLin = add(acc.rhsLin, fw);
 }
@@ -350,18 +350,18 @@ __device__ __forceinline__ void zeroAcc(SideAcc &a) {
 
 // One stamp record, loaded whole before it is added.
 struct StampRec {
-    float4 s0, s1, s2, s3, s4, s5, s6;
+    real4 s0, s1, s2, s3, s4, s5, s6;
 };
 
 // Stamps are read-only while bodies solve: the read-only path.
-__device__ __forceinline__ StampRec loadStamp(const float4 *src) {
+__device__ __forceinline__ StampRec loadStamp(const real4 *src) {
     return StampRec{__ldg(src), __ldg(src + 1), __ldg(src + 2), __ldg(src + 3), __ldg(src + 4), __ldg(src + 5),
                     __ldg(src + 6)};
 }
 
 // block += stamp (full 3x3 adds, as the reference adds its accumulators).
 __device__ __forceinline__ void addStamp(Blk &b, const StampRec &r) {
-    const float4 s0 = r.s0, s1 = r.s1, s2 = r.s2, s3 = r.s3, s4 = r.s4, s5 = r.s5, s6 = r.s6;
+    const real4 s0 = r.s0, s1 = r.s1, s2 = r.s2, s3 = r.s3, s4 = r.s4, s5 = r.s5, s6 = r.s6;
     const m3 lin = mcols(f3{s0.x, s0.y, s0.z}, f3{s0.y, s0.w, s1.x}, f3{s0.z, s1.x, s1.y});
     const m3 ang = mcols(f3{s2.y, s2.z, s2.w}, f3{s2.z, s3.x, s3.y}, f3{s2.w, s3.y, s3.z});
     const m3 crs = mcols(f3{s4.z, s4.w, s5.x}, f3{s5.y, s5.z, s5.w}, f3{s6.x, s6.y, s6.z});
@@ -372,7 +372,7 @@ __device__ __forceinline__ void addStamp(Blk &b, const StampRec &r) {
     b.ra = add(b.ra, f3{s3.w, s4.x, s4.y});
 }
 
-__device__ __forceinline__ void addStamp(Blk &b, const float4 *src) { addStamp(b, loadStamp(src)); }
+__device__ __forceinline__ void addStamp(Blk &b, const real4 *src) { addStamp(b, loadStamp(src)); }
 
 struct Pose {
     f3 x, dLin, dAng;
@@ -382,7 +382,7 @@ struct Pose {
 
 __device__ __forceinline__ Pose loadPose(const Dev &d, int g) {
     Pose p;
-    const float4 x4 = d.x[g];
+    const real4 x4 = d.x[g];
     p.x = xyz(x4);
     p.q = asq(d.q[g]);
     p.dLin = sub(p.x, xyz(d.x0[g]));
@@ -394,7 +394,7 @@ __device__ __forceinline__ Pose loadPose(const Dev &d, int g) {
 // loadPose through the read-only path, for kernels that write no pose.
 __device__ __forceinline__ Pose loadPoseRO(const Dev &d, int g) {
     Pose p;
-    const float4 x4 = __ldg(&d.x[g]);
+    const real4 x4 = __ldg(&d.x[g]);
     p.x = xyz(x4);
     p.q = asq(__ldg(&d.q[g]));
     p.dLin = sub(p.x, xyz(__ldg(&d.x0[g])));
@@ -422,16 +422,16 @@ __device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touche
 }
 
 // Stamp record: lin (6 unique), rhsLin (signed), ang (6 unique), rhsAng (signed), cross (9).
-__device__ __forceinline__ void storeStamp(float4 *dst, const SharedAcc &sh, const SideAcc &sd, float side) {
+__device__ __forceinline__ void storeStamp(real4 *dst, const SharedAcc &sh, const SideAcc &sd, real side) {
     const f3 rl = scale(sh.rhsLin, side);
     const f3 ra = scale(sd.rhsAng, side);
-    dst[0] = make_float4(sh.lin.c0.x, sh.lin.c0.y, sh.lin.c0.z, sh.lin.c1.y);
-    dst[1] = make_float4(sh.lin.c1.z, sh.lin.c2.z, rl.x, rl.y);
-    dst[2] = make_float4(rl.z, sd.ang.c0.x, sd.ang.c0.y, sd.ang.c0.z);
-    dst[3] = make_float4(sd.ang.c1.y, sd.ang.c1.z, sd.ang.c2.z, ra.x);
-    dst[4] = make_float4(ra.y, ra.z, sd.crs.c0.x, sd.crs.c0.y);
-    dst[5] = make_float4(sd.crs.c0.z, sd.crs.c1.x, sd.crs.c1.y, sd.crs.c1.z);
-    dst[6] = make_float4(sd.crs.c2.x, sd.crs.c2.y, sd.crs.c2.z, 0.0f);
+    dst[0] = mk4(sh.lin.c0.x, sh.lin.c0.y, sh.lin.c0.z, sh.lin.c1.y);
+    dst[1] = mk4(sh.lin.c1.z, sh.lin.c2.z, rl.x, rl.y);
+    dst[2] = mk4(rl.z, sd.ang.c0.x, sd.ang.c0.y, sd.ang.c0.z);
+    dst[3] = mk4(sd.ang.c1.y, sd.ang.c1.z, sd.ang.c2.z, ra.x);
+    dst[4] = mk4(ra.y, ra.z, sd.crs.c0.x, sd.crs.c0.y);
+    dst[5] = mk4(sd.crs.c0.z, sd.crs.c1.x, sd.crs.c1.y, sd.crs.c1.z);
+    dst[6] = mk4(sd.crs.c2.x, sd.crs.c2.y, sd.crs.c2.z, 0.0f);
 }
 
 // Stamps of manifold m for the requested sides, from the current poses and penalties.
@@ -439,9 +439,9 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
     const ManifoldBuf L = d.live;
     const int2 ab = L.ab[m];
     const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
-    const float4 b04 = L.b0[m];
+    const real4 b04 = L.b0[m];
     const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
-    const float mu = b04.w;
+    const real mu = b04.w;
     const int n = L.count[m];
     SharedAcc sh;
     sh.lin = mzero();
@@ -462,7 +462,7 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
         const f3 k = xyz(L.k[ci]);
         f3 F = add(cmul(k, C), xyz(L.lam[ci]));
         clampForce(F, mu);
-        float S[6];
+        real S[6];
         basisHessianD(r0, r1, r2, k, S);
         const f3 fw = add(add(scale(r0, F.x), scale(r1, F.y)), scale(r2, F.z));
         stampShared(S, fw, sh);
@@ -499,7 +499,7 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
 // floats). One thread per manifold, grid-stride over the live ones.
 // ARM: the arm cache is on (compiled out otherwise, so the common path keeps its code).
 template <bool STAMPS, bool ARM>
-__global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float decay) { // 512: largest tuned block
+__global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, real decay) { // 512: largest tuned block
     const int live = d.ctr[C_LIVE];
     const ManifoldBuf L = d.live;
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x) {
@@ -511,9 +511,9 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
         if (touches)
             sides = 0; // recomputed after the colour passes
         const Pose A = loadPoseRO(d, ab.x), B = loadPoseRO(d, ab.y);
-        const float4 b04 = __ldg(&L.b0[m]);
+        const real4 b04 = __ldg(&L.b0[m]);
         const f3 r0 = xyz(b04), r1 = xyz(__ldg(&L.b1[m])), r2 = xyz(__ldg(&L.b2[m]));
-        const float mu = b04.w;
+        const real mu = b04.w;
         const int n = __ldg(&L.count[m]);
         // Drift-gated arm reuse (manifold.cpp:600-608): under the rotation threshold the cached
         // world arms stand in for the current ones.
@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
         zeroAcc(sb);
         for (int c = 0; c < n; c++) {
             const int ci = cslot(d, m, c);
-            const float4 rA4 = __ldg(&L.rA[ci]);
+            const real4 rA4 = __ldg(&L.rA[ci]);
             f3 rAw, rBw;
             if (driftUsable) {
                 rAw = xyz(L.armA[ci]);
@@ -548,17 +548,17 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
             f3 k = xyz(L.k[ci]);
             if (decay < 1.0f)
                 k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
-            const float4 lam4 = L.lam[ci];
-            float stick = lam4.w;
+            const real4 lam4 = L.lam[ci];
+            real stick = lam4.w;
             f3 F = add(cmul(k, C), xyz(lam4));
             const Cone cone = clampForce(F, mu);
             const f3 lam = F;
-            const float beta = p.betaLin * rA4.w;
+            const real beta = p.betaLin * rA4.w;
             if (F.x < 0)
-                k.x = smin(k.x + beta * fabsf(C.x), PENALTY_MAX);
+                k.x = smin(k.x + beta * mabs(C.x), PENALTY_MAX);
             if (cone.scale <= cone.bounds) {
-                k.y = smin(k.y + beta * fabsf(C.y), PENALTY_MAX);
-                k.z = smin(k.z + beta * fabsf(C.z), PENALTY_MAX);
+                k.y = smin(k.y + beta * mabs(C.y), PENALTY_MAX);
+                k.z = smin(k.z + beta * mabs(C.z), PENALTY_MAX);
                 stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
             }
             L.k[ci] = f4(k, 0.0f);
@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, float dec
                 }
                 f3 Fn = add(cmul(k, Cs), lam);
                 clampForce(Fn, mu);
-                float S[6];
+                real S[6];
                 basisHessianD(r0, r1, r2, k, S);
                 const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
                 stampShared(S, fw, sh);
@@ -620,7 +620,7 @@ __device__ __forceinline__ f3 jointAng(const Dev &d, int f) {
 }
 
 __device__ __forceinline__ m3 geometricStiffness(int k, f3 v) {
-    const float vk = at(v, k);
+    const real vk = at(v, k);
     m3 m = mdiag(-vk, -vk, -vk);
     f3 ck = col(m, k);
     ck = f3{ck.x + v.x, ck.y + v.y, ck.z + v.z};
@@ -636,7 +636,7 @@ __device__ __forceinline__ m3 geometricStiffness(int k, f3 v) {
 __device__ void ballStamp(const Dev &d, const StepParams &p, int f, int body, Blk &blk) {
     const int2 ab = d.fAB[f];
     const bool isA = body == ab.x;
-    const float4 par = d.fPar[f];
+    const real4 par = d.fPar[f];
     const f3 kl = xyz(d.fKL[f]);
     if (length2(kl) > 0) {
         const m3 K = mdiag(kl.x, kl.y, kl.z);
@@ -702,7 +702,7 @@ __global__ void forceDualKernel(Dev d, StepParams p) {
     }
     if (d.fKind[f] != kForceBall)
         return;
-    const float4 par = d.fPar[f];
+    const real4 par = d.fPar[f];
     f3 kl = xyz(d.fKL[f]), ka = xyz(d.fKA[f]);
     f3 ll = xyz(d.fLL[f]), la = xyz(d.fLA[f]);
     if (length2(kl) > 0) {
@@ -780,7 +780,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             const ManifoldBuf L = d.live;
             const int2 ab = L.ab[m];
             const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
-            const float4 b04 = L.b0[m];
+            const real4 b04 = L.b0[m];
             const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
             const int n = L.count[m];
             bool cached = false;
@@ -812,13 +812,13 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
                 const f3 k = xyz(L.k[ci]);
                 f3 F = add(cmul(k, C), xyz(L.lam[ci]));
                 clampForce(F, b04.w);
-                float S[6];
+                real S[6];
                 basisHessianD(r0, r1, r2, k, S);
                 const f3 fw = add(add(scale(r0, F.x), scale(r1, F.y)), scale(r2, F.z));
                 stampShared(S, fw, sh);
                 stampContact(S, side == 0 ? rAw : rBw, fw, sd);
             }
-            const float sgn = side == 0 ? 1.0f : -1.0f;
+            const real sgn = side == 0 ? 1.0f : -1.0f;
             blk.lin = madd(blk.lin, sh.lin);
             blk.ang = madd(blk.ang, sd.ang);
             blk.crs = madd(blk.crs, sd.crs);
@@ -831,7 +831,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
 }
 
 __device__ __forceinline__ Blk bodyBlock(const Dev &d, const StepParams &p, int g) {
-    const float4 x4 = d.x[g];
+    const real4 x4 = d.x[g];
     return makeBlock(x4.w, xyz(d.moment[g]), p.dtSq, xyz(x4), xyz(d.xi[g]), asq(d.q[g]), asq(d.qi[g]));
 }
 
@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
     assemble<true>(d, p, g, blk, armsFromDual);
     f3 dl, da;
     solveBlock(blk, dl, da);
-    const float4 x4 = d.x[g];
+    const real4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), dl), x4.w);
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
@@ -852,7 +852,7 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
 // An overflow body's step: in place (no forces) or into dLin/dAng for overflowApplyKernel.
 __device__ __forceinline__ void applyOverflow(const Dev &d, const StepParams &p, int g, int inPlace, f3 dl, f3 da) {
     if (inPlace) {
-        const float4 x4 = d.x[g];
+        const real4 x4 = d.x[g];
         d.x[g] = f4(add(xyz(x4), scale(dl, p.jacobiRelax)), x4.w);
         d.q[g] = f4(qintegrate(asq(d.q[g]), scale(da, p.jacobiRelax)));
     } else {
@@ -898,7 +898,7 @@ __global__ void overflowApplyKernel(Dev d, StepParams p) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
         return;
-    const float4 x4 = d.x[g];
+    const real4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), scale(xyz(d.dLin[g]), p.jacobiRelax)), x4.w);
     d.q[g] = f4(qintegrate(asq(d.q[g]), scale(xyz(d.dAng[g]), p.jacobiRelax)));
 }
@@ -922,14 +922,14 @@ __global__ void warmstartKernel(Dev d, StepParams p) {
         return;
     const int locks = d.meta[g].w;
     const int lockLin = locks & 0xff, lockAng = (locks >> 8) & 0xff;
-    const float4 x4 = d.x[g];
-    const float4 v4 = d.v[g];
-    const float mass = x4.w;
+    const real4 x4 = d.x[g];
+    const real4 v4 = d.v[g];
+    const real mass = x4.w;
     f3 v = xyz(v4), w = xyz(d.w[g]);
     maskLocked(lockLin, v);
     maskLocked(lockAng, w);
-    const float dt = p.dt;
-    const float gr = (lockLin & 0x4) ? 0.0f : v4.w;
+    const real dt = p.dt;
+    const real gr = (lockLin & 0x4) ? 0.0f : v4.w;
     const f3 x = xyz(x4);
     const q4 q = asq(d.q[g]);
     f3 xi = add(x, scale(v, dt));
@@ -937,8 +937,8 @@ __global__ void warmstartKernel(Dev d, StepParams p) {
         xi = add(xi, scale(f3{0, 0, gr}, dt * dt));
     const q4 qi = qintegrate(q, scale(w, dt));
     const f3 accel = divs(sub(v, xyz(d.vprev[g])), dt);
-    const float accelExt = accel.z * copysignf(1.0f, gr);
-    float weight = sclamp(accelExt / fabsf(gr), 0.0f, 1.0f);
+    const real accelExt = accel.z * mcopysign(1.0f, gr);
+    real weight = sclamp(accelExt / mabs(gr), 0.0f, 1.0f);
     if (!isfinite(weight))
         weight = 0.0f;
     d.xi[g] = f4(xi, 0.0f);
@@ -960,8 +960,8 @@ __global__ void finishKernel(Dev d, StepParams p, int idle) {
     if (g >= n || d.meta[g].x < 0)
         return;
     const int locks = d.meta[g].w;
-    const float4 x4 = d.x[g];
-    const float4 v4 = d.v[g];
+    const real4 x4 = d.x[g];
+    const real4 v4 = d.v[g];
     d.vprev[g] = f4(xyz(v4), 0.0f);
     f3 v = xyz(v4), w = xyz(d.w[g]);
     const int2 s = d.sleep[g];
@@ -1196,12 +1196,12 @@ void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {
 }
 
 template <bool STAMPS, bool ARM>
-static void dualLaunch(const Dev &d, const StepParams &p, float decay, int block, cudaStream_t s) {
+static void dualLaunch(const Dev &d, const StepParams &p, real decay, int block, cudaStream_t s) {
     const int blocks = residentGrid(dualKernel<STAMPS, ARM>, block, divUp(d.MM, block));
     dualKernel<STAMPS, ARM><<<blocks, block, 0, s>>>(d, p, decay);
 }
 
-void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, int block, cudaStream_t s) {
+void launchDual(const Dev &d, const StepParams &p, bool stamps, real decay, int block, cudaStream_t s) {
     ++launchCount();
     if (p.armCache)
         stamps ? dualLaunch<true, true>(d, p, decay, block, s) : dualLaunch<false, true>(d, p, decay, block, s);

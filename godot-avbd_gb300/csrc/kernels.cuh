@@ -59,13 +59,13 @@ void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool f
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s);
 // Dual pass over live manifolds; with `stamps`, also the next round's stamps of manifolds whose
 // bodies are all overflow or static. `decay` < 1 scales penalties first (dual-only rounds).
-void launchDual(const Dev &d, const StepParams &p, bool stamps, float decay, int block, cudaStream_t s);
+void launchDual(const Dev &d, const StepParams &p, bool stamps, real decay, int block, cudaStream_t s);
 void launchForceDual(const Dev &d, const StepParams &p, bool forces, cudaStream_t s);
 
 // ---- projection (k_proj.cu) ----
 // projectionActive per world and the brake candidates (manifolds with an open gap).
 void launchProjActive(const Dev &d, cudaStream_t s);
-void launchBrake(const Dev &d, float window, cudaStream_t s);
+void launchBrake(const Dev &d, real window, cudaStream_t s);
 void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s);
 
 int brakeGridBlocks();

@@ -19,9 +19,9 @@ struct NContact {
 namespace narrow {
 
 constexpr int kMaxPoly = 16;
-constexpr float kSatEps = 1.0e-6f;
-constexpr float kPlaneEps = 1.0e-5f;
-constexpr float kMergeSq = 1.0e-6f;
+constexpr real kSatEps = 1.0e-6f;
+constexpr real kPlaneEps = 1.0e-5f;
+constexpr real kMergeSq = 1.0e-6f;
 enum { kFaceA = 0, kFaceB = 1, kEdge = 2 };
 
 struct Obb {
@@ -33,21 +33,21 @@ struct Obb {
 
 struct Sat {
     int type, ia, ib;
-    float sep;
+    real sep;
     f3 nAB;
     bool valid;
 };
 
-__device__ __forceinline__ float hv(const f3 &h, int i) { return at(h, i); }
+__device__ __forceinline__ real hv(const f3 &h, int i) { return at(h, i); }
 
 __device__ inline f3 support(const Obb &b, f3 dir) {
-    const float sx = dot(dir, b.ax[0]) >= 0.0f ? 1.0f : -1.0f;
-    const float sy = dot(dir, b.ax[1]) >= 0.0f ? 1.0f : -1.0f;
-    const float sz = dot(dir, b.ax[2]) >= 0.0f ? 1.0f : -1.0f;
+    const real sx = dot(dir, b.ax[0]) >= 0.0f ? 1.0f : -1.0f;
+    const real sy = dot(dir, b.ax[1]) >= 0.0f ? 1.0f : -1.0f;
+    const real sz = dot(dir, b.ax[2]) >= 0.0f ? 1.0f : -1.0f;
     return add(add(add(b.c, scale(b.ax[0], b.h.x * sx)), scale(b.ax[1], b.h.y * sy)), scale(b.ax[2], b.h.z * sz));
 }
 
-__device__ inline void faceAxes(const Obb &b, int k, f3 &u, f3 &v, float &eu, float &ev) {
+__device__ inline void faceAxes(const Obb &b, int k, f3 &u, f3 &v, real &eu, real &ev) {
     if (k == 0) {
         u = b.ax[1]; v = b.ax[2]; eu = b.h.y; ev = b.h.z;
     } else if (k == 1) {
@@ -57,21 +57,21 @@ __device__ inline void faceAxes(const Obb &b, int k, f3 &u, f3 &v, float &eu, fl
     }
 }
 
-__device__ inline int clip(const f3 *in, int inCount, f3 n, float off, f3 *out) {
+__device__ inline int clip(const f3 *in, int inCount, f3 n, real off, f3 *out) {
     if (inCount <= 0)
         return 0;
     int oc = 0;
     f3 a = in[inCount - 1];
-    float da = dot(n, a) - off;
+    real da = dot(n, a) - off;
     for (int i = 0; i < inCount; ++i) {
         const f3 b = in[i];
-        const float db = dot(n, b) - off;
+        const real db = dot(n, b) - off;
         const bool aIn = da <= kPlaneEps;
         const bool bIn = db <= kPlaneEps;
         if (aIn != bIn) {
-            float t = 0.0f;
-            const float denom = da - db;
-            if (fabsf(denom) > kSatEps)
+            real t = 0.0f;
+            const real denom = da - db;
+            if (mabs(denom) > kSatEps)
                 t = sclamp(da / denom, 0.0f, 1.0f);
             if (oc < kMaxPoly)
                 out[oc++] = add(a, scale(sub(b, a), t));
@@ -108,9 +108,9 @@ struct Sink {
     }
 };
 
-__device__ inline bool faceA(const Obb &A, const Obb &B, f3 dA, const m3 &m, int i, float margin, Sat &best) {
-    const float sep = fabsf(at(dA, i)) -
-            (((hv(A.h, i) + B.h.x * fabsf(mat(m, 0, i))) + B.h.y * fabsf(mat(m, 1, i))) + B.h.z * fabsf(mat(m, 2, i)));
+__device__ inline bool faceA(const Obb &A, const Obb &B, f3 dA, const m3 &m, int i, real margin, Sat &best) {
+    const real sep = mabs(at(dA, i)) -
+            (((hv(A.h, i) + B.h.x * mabs(mat(m, 0, i))) + B.h.y * mabs(mat(m, 1, i))) + B.h.z * mabs(mat(m, 2, i)));
     if (sep > margin)
         return false;
     if (!best.valid || sep > best.sep) {
@@ -124,9 +124,9 @@ __device__ inline bool faceA(const Obb &A, const Obb &B, f3 dA, const m3 &m, int
     return true;
 }
 
-__device__ inline bool faceB(const Obb &A, const Obb &B, f3 dB, const m3 &m, int j, float margin, Sat &best) {
-    const float sep = fabsf(at(dB, j)) -
-            (((hv(B.h, j) + A.h.x * fabsf(mat(m, j, 0))) + A.h.y * fabsf(mat(m, j, 1))) + A.h.z * fabsf(mat(m, j, 2)));
+__device__ inline bool faceB(const Obb &A, const Obb &B, f3 dB, const m3 &m, int j, real margin, Sat &best) {
+    const real sep = mabs(at(dB, j)) -
+            (((hv(B.h, j) + A.h.x * mabs(mat(m, j, 0))) + A.h.y * mabs(mat(m, j, 1))) + A.h.z * mabs(mat(m, j, 2)));
     if (sep > margin)
         return false;
     if (!best.valid || sep > best.sep) {
@@ -140,18 +140,18 @@ __device__ inline bool faceB(const Obb &A, const Obb &B, f3 dB, const m3 &m, int
     return true;
 }
 
-__device__ inline bool edge(const Obb &A, const Obb &B, f3 delta, f3 axis, const m3 &m, int i, int j, float margin,
+__device__ inline bool edge(const Obb &A, const Obb &B, f3 delta, f3 axis, const m3 &m, int i, int j, real margin,
                             Sat &best) {
-    const float lenSq = length2(axis);
+    const real lenSq = length2(axis);
     if (lenSq < kSatEps)
         return true;
-    const float invLen = 1.0f / sqrtf(lenSq);
+    const real invLen = 1.0f / msqrt(lenSq);
     const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
     const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-    const float rA = (hv(A.h, i1) * fabsf(mat(m, j, i2)) + hv(A.h, i2) * fabsf(mat(m, j, i1))) * invLen;
-    const float rB = (hv(B.h, j1) * fabsf(mat(m, j2, i)) + hv(B.h, j2) * fabsf(mat(m, j1, i))) * invLen;
-    const float sd = dot(delta, axis) * invLen;
-    const float sep = fabsf(sd) - (rA + rB);
+    const real rA = (hv(A.h, i1) * mabs(mat(m, j, i2)) + hv(A.h, i2) * mabs(mat(m, j, i1))) * invLen;
+    const real rB = (hv(B.h, j1) * mabs(mat(m, j2, i)) + hv(B.h, j2) * mabs(mat(m, j1, i))) * invLen;
+    const real sd = dot(delta, axis) * invLen;
+    const real sep = mabs(sd) - (rA + rB);
     if (sep > margin)
         return false;
     if (!best.valid || sep > best.sep) {
@@ -167,8 +167,8 @@ __device__ inline bool edge(const Obb &A, const Obb &B, f3 delta, f3 axis, const
 
 __device__ inline void supportEdge(const Obb &b, int k, f3 dir, f3 &e0, f3 &e1) {
     const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-    const float s1 = dot(dir, b.ax[k1]) >= 0.0f ? 1.0f : -1.0f;
-    const float s2 = dot(dir, b.ax[k2]) >= 0.0f ? 1.0f : -1.0f;
+    const real s1 = dot(dir, b.ax[k1]) >= 0.0f ? 1.0f : -1.0f;
+    const real s2 = dot(dir, b.ax[k2]) >= 0.0f ? 1.0f : -1.0f;
     const f3 ec = add(add(b.c, scale(b.ax[k1], hv(b.h, k1) * s1)), scale(b.ax[k2], hv(b.h, k2) * s2));
     e0 = sub(ec, scale(b.ax[k], hv(b.h, k)));
     e1 = add(ec, scale(b.ax[k], hv(b.h, k)));
@@ -178,10 +178,10 @@ __device__ inline void closestSegments(f3 p0, f3 p1, f3 q0, f3 q1, f3 &c0, f3 &c
     const f3 d1 = sub(p1, p0);
     const f3 d2 = sub(q1, q0);
     const f3 r = sub(p0, q0);
-    const float a = dot(d1, d1);
-    const float e = dot(d2, d2);
-    const float f = dot(d2, r);
-    float s = 0.0f, t = 0.0f;
+    const real a = dot(d1, d1);
+    const real e = dot(d2, d2);
+    const real f = dot(d2, r);
+    real s = 0.0f, t = 0.0f;
     if (a <= kSatEps && e <= kSatEps) {
         c0 = p0;
         c1 = q0;
@@ -190,13 +190,13 @@ __device__ inline void closestSegments(f3 p0, f3 p1, f3 q0, f3 q1, f3 &c0, f3 &c
     if (a <= kSatEps) {
         t = sclamp(f / e, 0.0f, 1.0f);
     } else {
-        const float c = dot(d1, r);
+        const real c = dot(d1, r);
         if (e <= kSatEps) {
             s = sclamp(-c / a, 0.0f, 1.0f);
         } else {
-            const float b = dot(d1, d2);
-            const float denom = a * e - b * b;
-            if (fabsf(denom) > kSatEps)
+            const real b = dot(d1, d2);
+            const real denom = a * e - b * b;
+            if (mabs(denom) > kSatEps)
                 s = sclamp((b * f - c * e) / denom, 0.0f, 1.0f);
             t = (b * s + f) / e;
             if (t < 0.0f) {
@@ -212,22 +212,22 @@ __device__ inline void closestSegments(f3 p0, f3 p1, f3 q0, f3 q1, f3 &c0, f3 &c
     c1 = add(q0, scale(d2, t));
 }
 
-__device__ inline int faceManifold(const Obb &A, const Obb &B, bool refIsA, int refAxis, f3 nAB, float margin,
+__device__ inline int faceManifold(const Obb &A, const Obb &B, bool refIsA, int refAxis, f3 nAB, real margin,
                                    NContact *out) {
     const Obb &ref = refIsA ? A : B;
     const Obb &inc = refIsA ? B : A;
     const f3 outward = refIsA ? nAB : neg(nAB);
-    const float rs = dot(outward, ref.ax[refAxis]) >= 0.0f ? 1.0f : -1.0f;
+    const real rs = dot(outward, ref.ax[refAxis]) >= 0.0f ? 1.0f : -1.0f;
     const f3 rn = scale(ref.ax[refAxis], rs);
     const f3 rc = add(ref.c, scale(rn, hv(ref.h, refAxis)));
     f3 ru, rv;
-    float reu, rev;
+    real reu, rev;
     faceAxes(ref, refAxis, ru, rv, reu, rev);
     int incAxis = 0;
     {
-        float best = -FLT_MAX;
+        real best = -FLT_MAX;
         for (int i = 0; i < 3; ++i) {
-            const float dd = fabsf(dot(inc.ax[i], rn));
+            const real dd = mabs(dot(inc.ax[i], rn));
             if (dd > best) {
                 best = dd;
                 incAxis = i;
@@ -236,11 +236,11 @@ __device__ inline int faceManifold(const Obb &A, const Obb &B, bool refIsA, int 
     }
     f3 c0[kMaxPoly], c1[kMaxPoly];
     {
-        const float sg = dot(inc.ax[incAxis], rn) > 0.0f ? -1.0f : 1.0f;
+        const real sg = dot(inc.ax[incAxis], rn) > 0.0f ? -1.0f : 1.0f;
         const f3 fn = scale(inc.ax[incAxis], sg);
         const f3 fc = add(inc.c, scale(fn, hv(inc.h, incAxis)));
         f3 u, v;
-        float eu, ev;
+        real eu, ev;
         faceAxes(inc, incAxis, u, v, eu, ev);
         c0[0] = add(add(fc, scale(u, eu)), scale(v, ev));
         c0[1] = add(sub(fc, scale(u, eu)), scale(v, ev));
@@ -272,10 +272,10 @@ __device__ inline int faceManifold(const Obb &A, const Obb &B, bool refIsA, int 
     int prefix = (refIsA ? kFaceA : kFaceB) << 24;
     prefix |= (refAxis & 0xFF) << 16;
     prefix |= (incAxis & 0xFF) << 8;
-    const float accept = smax(margin, kPlaneEps);
+    const real accept = smax(margin, kPlaneEps);
     for (int i = 0; i < cnt && sink.n < 8; ++i) {
         const f3 p = c0[i];
-        const float dist = dot(sub(p, rc), rn);
+        const real dist = dot(sub(p, rc), rn);
         if (dist > accept)
             continue;
         const f3 pr = sub(p, scale(rn, dist));
@@ -328,7 +328,7 @@ __device__ inline Obb makeObb(f3 c, q4 q, f3 h) {
 
 // Returns the contact count (0 = separated beyond the margin); `basis` is written only when the
 // SAT finds no separating axis, as in the reference.
-__device__ inline int collideBoxes(f3 ca, q4 qa, f3 ha, f3 cb, q4 qb, f3 hb, float margin, NContact *out, m3 &basis) {
+__device__ inline int collideBoxes(f3 ca, q4 qa, f3 ha, f3 cb, q4 qb, f3 hb, real margin, NContact *out, m3 &basis) {
     using namespace narrow;
     const Obb A = makeObb(ca, qa, ha);
     const Obb B = makeObb(cb, qb, hb);

@@ -22,7 +22,7 @@ constexpr unsigned kAxisCylSample = 3, kAxisCylCorner = 4;
 // Rim directions: cos/sin of 2 pi * (5 i mod 8) / 8 (collide.cpp:731-753), computed on the host
 // with the C library exactly as the reference does, then uploaded.
 struct RimTable {
-    float c[kRimSamples], s[kRimSamples];
+    real c[kRimSamples], s[kRimSamples];
 };
 
 struct RShape {
@@ -30,7 +30,7 @@ struct RShape {
     f3 center;
     q4 rot;
     f3 half;
-    float radius, halfHeight;
+    real radius, halfHeight;
     f3 axis;
 };
 
@@ -38,13 +38,13 @@ __device__ __forceinline__ RShape makeShape(int type, f3 c, q4 q, f3 size) {
     return RShape{type, c, q, scale(size, 0.5f), size.x, size.z * 0.5f, qrot(q, f3{0, 0, 1})};
 }
 
-__device__ inline bool pointInBox(const RShape &box, f3 p, f3 &push, float &depth) {
+__device__ inline bool pointInBox(const RShape &box, f3 p, f3 &push, real &depth) {
     const f3 local = qrot(qconj(box.rot), sub(p, box.center));
-    float best = FLT_MAX;
+    real best = FLT_MAX;
     int axis = 0;
-    float sign = 1.0f;
+    real sign = 1.0f;
     for (int i = 0; i < 3; ++i) {
-        const float d = at(box.half, i) - fabsf(at(local, i));
+        const real d = at(box.half, i) - mabs(at(local, i));
         if (d <= 0.0f)
             return false;
         if (d < best) {
@@ -60,11 +60,11 @@ __device__ inline bool pointInBox(const RShape &box, f3 p, f3 &push, float &dept
     return true;
 }
 
-__device__ inline bool pointNearBox(const RShape &box, f3 p, float margin, f3 &push, float &depth) {
+__device__ inline bool pointNearBox(const RShape &box, f3 p, real margin, f3 &push, real &depth) {
     const f3 local = qrot(qconj(box.rot), sub(p, box.center));
     bool outside = false;
     for (int i = 0; i < 3; ++i)
-        if (fabsf(at(local, i)) >= at(box.half, i)) {
+        if (mabs(at(local, i)) >= at(box.half, i)) {
             outside = true;
             break;
         }
@@ -73,7 +73,7 @@ __device__ inline bool pointNearBox(const RShape &box, f3 p, float margin, f3 &p
     const f3 cl{sclamp(local.x, -box.half.x, box.half.x), sclamp(local.y, -box.half.y, box.half.y),
                 sclamp(local.z, -box.half.z, box.half.z)};
     const f3 d = sub(local, cl);
-    const float gap = length(d);
+    const real gap = length(d);
     if (gap > margin || gap <= 1.0e-9f)
         return false;
     push = qrot(box.rot, divs(d, gap));
@@ -81,13 +81,13 @@ __device__ inline bool pointNearBox(const RShape &box, f3 p, float margin, f3 &p
     return true;
 }
 
-__device__ inline f3 closestOnCylinder(const RShape &cyl, f3 p, f3 &outward, float &distance) {
+__device__ inline f3 closestOnCylinder(const RShape &cyl, f3 p, f3 &outward, real &distance) {
     const f3 local = qrot(qconj(cyl.rot), sub(p, cyl.center));
-    const float t = sclamp(local.z, -cyl.halfHeight, cyl.halfHeight);
-    const float lenSq = (0.0f + local.x * local.x) + local.y * local.y; // linalg length2 of (x, y)
+    const real t = sclamp(local.z, -cyl.halfHeight, cyl.halfHeight);
+    const real lenSq = (0.0f + local.x * local.x) + local.y * local.y; // linalg length2 of (x, y)
     f3 closest{0, 0, t};
     if (lenSq > cyl.radius * cyl.radius) {
-        const float sc = cyl.radius / sqrtf(lenSq);
+        const real sc = cyl.radius / msqrt(lenSq);
         closest.x = local.x * sc;
         closest.y = local.y * sc;
     } else if (lenSq > 1.0e-12f) {
@@ -103,19 +103,19 @@ __device__ inline f3 closestOnCylinder(const RShape &cyl, f3 p, f3 &outward, flo
     return on;
 }
 
-__device__ inline bool pointInCylinder(const RShape &cyl, f3 p, f3 &push, float &surface) {
+__device__ inline bool pointInCylinder(const RShape &cyl, f3 p, f3 &push, real &surface) {
     const f3 local = qrot(qconj(cyl.rot), sub(p, cyl.center));
-    const float radialSq = local.x * local.x + local.y * local.y;
-    if (radialSq >= cyl.radius * cyl.radius || fabsf(local.z) >= cyl.halfHeight)
+    const real radialSq = local.x * local.x + local.y * local.y;
+    if (radialSq >= cyl.radius * cyl.radius || mabs(local.z) >= cyl.halfHeight)
         return false;
-    const float radialDepth = cyl.radius - sqrtf(radialSq);
-    const float capDepth = cyl.halfHeight - fabsf(local.z);
+    const real radialDepth = cyl.radius - msqrt(radialSq);
+    const real capDepth = cyl.halfHeight - mabs(local.z);
     f3 pl{0, 0, 0};
     if (capDepth < radialDepth) {
         pl.z = local.z >= 0.0f ? 1.0f : -1.0f;
         surface = capDepth;
     } else {
-        const float len = sqrtf(radialSq);
+        const real len = msqrt(radialSq);
         if (len > 1.0e-6f) {
             pl.x = local.x / len;
             pl.y = local.y / len;
@@ -128,13 +128,13 @@ __device__ inline bool pointInCylinder(const RShape &cyl, f3 p, f3 &push, float 
     return true;
 }
 
-__device__ inline bool pointNearCylinder(const RShape &cyl, f3 p, float margin, f3 &push, float &depth) {
+__device__ inline bool pointNearCylinder(const RShape &cyl, f3 p, real margin, f3 &push, real &depth) {
     const f3 local = qrot(qconj(cyl.rot), sub(p, cyl.center));
-    const float radialSq = local.x * local.x + local.y * local.y;
-    if (radialSq < cyl.radius * cyl.radius && fabsf(local.z) < cyl.halfHeight)
+    const real radialSq = local.x * local.x + local.y * local.y;
+    if (radialSq < cyl.radius * cyl.radius && mabs(local.z) < cyl.halfHeight)
         return false;
     f3 outward;
-    float distance;
+    real distance;
     closestOnCylinder(cyl, p, outward, distance);
     if (distance > margin)
         return false;
@@ -143,11 +143,11 @@ __device__ inline bool pointNearCylinder(const RShape &cyl, f3 p, float margin, 
     return true;
 }
 
-__device__ __forceinline__ bool sampleInBox(const RShape &box, f3 p, float margin, f3 &push, float &depth) {
+__device__ __forceinline__ bool sampleInBox(const RShape &box, f3 p, real margin, f3 &push, real &depth) {
     return pointInBox(box, p, push, depth) || (margin > 0.0f && pointNearBox(box, p, margin, push, depth));
 }
 
-__device__ __forceinline__ bool sampleInCylinder(const RShape &cyl, f3 p, float margin, f3 &push, float &depth) {
+__device__ __forceinline__ bool sampleInCylinder(const RShape &cyl, f3 p, real margin, f3 &push, real &depth) {
     return pointInCylinder(cyl, p, push, depth) || (margin > 0.0f && pointNearCylinder(cyl, p, margin, push, depth));
 }
 
@@ -159,20 +159,20 @@ __device__ inline f3 cylinderSample(const RShape &cyl, const RimTable &rim, int 
     if (k < capCount) {
         const int end = k < kRimSamples + 1 ? -1 : 1;
         const int j = k % (kRimSamples + 1);
-        const f3 cap = add(cyl.center, scale(cyl.axis, cyl.halfHeight * static_cast<float>(end)));
+        const f3 cap = add(cyl.center, scale(cyl.axis, cyl.halfHeight * static_cast<real>(end)));
         if (j == 0)
             return cap;
         return add(cap, scale(add(scale(x, rim.c[j - 1]), scale(y, rim.s[j - 1])), cyl.radius));
     }
     const int ring = 1 + (k - capCount) / kRimSamples, i = (k - capCount) % kRimSamples;
-    const float t = -cyl.halfHeight + 2.0f * cyl.halfHeight * static_cast<float>(ring) / static_cast<float>(kAxialSamples);
+    const real t = -cyl.halfHeight + 2.0f * cyl.halfHeight * static_cast<real>(ring) / static_cast<real>(kAxialSamples);
     const f3 rc = add(cyl.center, scale(cyl.axis, t));
     return add(rc, scale(add(scale(x, rim.c[i]), scale(y, rim.s[i])), cyl.radius));
 }
 
 struct Candidate {
     f3 xA, xB, normal;
-    float depth;
+    real depth;
     unsigned feature;
 };
 
@@ -194,20 +194,20 @@ __device__ inline void emitRanked(const Candidate *cand, int n, Sink &sink) {
             break;
 }
 
-__device__ inline int sphereSphere(const RShape &a, const RShape &b, float margin, Sink &sink, m3 &basis) {
+__device__ inline int sphereSphere(const RShape &a, const RShape &b, real margin, Sink &sink, m3 &basis) {
     const f3 d = sub(b.center, a.center);
-    const float distSq = length2(d);
-    const float sumPlus = a.radius + b.radius + margin;
+    const real distSq = length2(d);
+    const real sumPlus = a.radius + b.radius + margin;
     if (distSq >= sumPlus * sumPlus)
         return 0;
-    const float dist = sqrtf(distSq);
+    const real dist = msqrt(distSq);
     const f3 n = dist > 1.0e-6f ? divs(d, dist) : f3{0, 0, 1};
     basis = orthonormal(neg(n));
     sink.addc(add(a.center, scale(n, a.radius)), sub(b.center, scale(n, b.radius)), 1);
     return sink.n;
 }
 
-__device__ inline int sphereBox(const RShape &a, const RShape &b, bool sphereIsA, float margin, Sink &sink,
+__device__ inline int sphereBox(const RShape &a, const RShape &b, bool sphereIsA, real margin, Sink &sink,
                                 m3 &basis) {
     const RShape &sphere = sphereIsA ? a : b;
     const RShape &box = sphereIsA ? b : a;
@@ -216,16 +216,16 @@ __device__ inline int sphereBox(const RShape &a, const RShape &b, bool sphereIsA
                 sclamp(local.z, -box.half.z, box.half.z)};
     const f3 closest = add(qrot(box.rot, cl), box.center);
     const f3 d = sub(sphere.center, closest);
-    const float distSq = length2(d);
-    const float radPlus = sphere.radius + margin;
+    const real distSq = length2(d);
+    const real radPlus = sphere.radius + margin;
     if (distSq >= radPlus * radPlus)
         return 0;
-    const float dist = sqrtf(distSq);
+    const real dist = msqrt(distSq);
     f3 n;
     if (dist > 1.0e-6f) {
         n = divs(d, dist);
     } else {
-        float depth;
+        real depth;
         if (!pointInBox(box, sphere.center, n, depth))
             return 0;
     }
@@ -235,12 +235,12 @@ __device__ inline int sphereBox(const RShape &a, const RShape &b, bool sphereIsA
     return sink.n;
 }
 
-__device__ inline int sphereCylinder(const RShape &a, const RShape &b, bool sphereIsA, float margin, Sink &sink,
+__device__ inline int sphereCylinder(const RShape &a, const RShape &b, bool sphereIsA, real margin, Sink &sink,
                                      m3 &basis) {
     const RShape &sphere = sphereIsA ? a : b;
     const RShape &cyl = sphereIsA ? b : a;
     f3 outward;
-    float distance;
+    real distance;
     const f3 onCyl = closestOnCylinder(cyl, sphere.center, outward, distance);
     if (distance >= sphere.radius + margin)
         return 0;
@@ -250,7 +250,7 @@ __device__ inline int sphereCylinder(const RShape &a, const RShape &b, bool sphe
     return sink.n;
 }
 
-__device__ inline int cylinderBox(const RShape &a, const RShape &b, bool cylIsA, const RimTable &rim, float margin,
+__device__ inline int cylinderBox(const RShape &a, const RShape &b, bool cylIsA, const RimTable &rim, real margin,
                                   Sink &sink, m3 &basis) {
     const RShape &cyl = cylIsA ? a : b;
     const RShape &box = cylIsA ? b : a;
@@ -260,7 +260,7 @@ __device__ inline int cylinderBox(const RShape &a, const RShape &b, bool cylIsA,
     for (int i = 0; i < kMaxCylSamples; ++i) {
         const f3 s = cylinderSample(cyl, rim, i);
         f3 push;
-        float depth;
+        real depth;
         if (!sampleInBox(box, s, margin, push, depth))
             continue;
         Candidate &c = cand[nc++];
@@ -276,7 +276,7 @@ __device__ inline int cylinderBox(const RShape &a, const RShape &b, bool cylIsA,
                     (corner & 4) ? box.half.z : -box.half.z};
         const f3 cw = add(qrot(box.rot, cl), box.center);
         f3 push;
-        float surf;
+        real surf;
         if (!sampleInCylinder(cyl, cw, margin, push, surf))
             continue;
         Candidate &c = cand[nc++];
@@ -294,7 +294,7 @@ __device__ inline int cylinderBox(const RShape &a, const RShape &b, bool cylIsA,
     return sink.n;
 }
 
-__device__ inline int cylinderCylinder(const RShape &a, const RShape &b, const RimTable &rim, float margin, Sink &sink,
+__device__ inline int cylinderCylinder(const RShape &a, const RShape &b, const RimTable &rim, real margin, Sink &sink,
                                        m3 &basis) {
     Candidate cand[2 * kMaxCylSamples];
     int nc = 0;
@@ -306,7 +306,7 @@ __device__ inline int cylinderCylinder(const RShape &a, const RShape &b, const R
         for (int i = 0; i < kMaxCylSamples; ++i) {
             const f3 s = cylinderSample(from, rim, i);
             f3 push;
-            float surf;
+            real surf;
             if (!sampleInCylinder(into, s, margin, push, surf))
                 continue;
             Candidate &c = cand[nc++];
@@ -328,7 +328,7 @@ __device__ inline int cylinderCylinder(const RShape &a, const RShape &b, const R
 } // namespace narrow
 
 // collideShapes for a pair with a sphere or a cylinder (collide.cpp:1007-1027).
-__device__ inline int collideRound(int typeA, f3 ca, q4 qa, f3 sizeA, int typeB, f3 cb, q4 qb, f3 sizeB, float margin,
+__device__ inline int collideRound(int typeA, f3 ca, q4 qa, f3 sizeA, int typeB, f3 cb, q4 qb, f3 sizeB, real margin,
                                    const narrow::RimTable &rim, NContact *out, m3 &basis) {
     using namespace narrow;
     const RShape a = makeShape(typeA, ca, qa, sizeA), b = makeShape(typeB, cb, qb, sizeB);

@@ -226,3 +226,18 @@ class RunStats:
         if self.final is not None:
             out["rest_step"], out["rest_kinetic_energy_j"], out["rest_max_speed_mps"] = self.final
         return out
+
+
+def pose_difference(pos_a, quat_a, pos_b, quat_b):
+    """Largest position distance (m) and rotation angle (rad) between two states of the same
+    bodies, in double precision."""
+    pa = np.asarray(pos_a, np.float64)
+    pb = np.asarray(pos_b, np.float64)
+    qa = np.asarray(quat_a, np.float64)
+    qb = np.asarray(quat_b, np.float64)
+    qa = qa / np.linalg.norm(qa, axis=1, keepdims=True)
+    qb = qb / np.linalg.norm(qb, axis=1, keepdims=True)
+    c = np.clip(np.abs(np.sum(qa * qb, axis=1)), 0.0, 1.0)
+    dx = float(np.max(np.linalg.norm(pa - pb, axis=1))) if len(pa) else 0.0
+    dq = float(np.max(2.0 * np.arccos(c))) if len(qa) else 0.0
+    return dx, dq
