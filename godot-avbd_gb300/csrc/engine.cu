@@ -206,6 +206,9 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     d.waitLimit = waitLimit;
     const char *noTune = std::getenv("AVBDG_NO_TUNE");
     tuneEnabled = !(noTune && noTune[0] == '1');
+#ifdef AVBDG_FP64
+    tuneEnabled = false; // the FP64 build states an error, not a speed: default block sizes
+#endif
     int dev = 0, hostTables = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
@@ -213,6 +216,13 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     directIo = hostTables == 1 && !(staged && staged[0] == '1');
     armTuning();
     prepareKernels(); // attributes and occupancy queries, never during a capture
+    {
+        const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
+        bool (*fits[kKinds])(int) = {dualBlockFits, solveBlockFits, narrowBlockFits, traverseBlockFits};
+        for (int k = 0; k < kKinds; k++)
+            for (int c = 0; c < spaces[k]->count; c++)
+                tuneFits[k][c] = fits[k](spaces[k]->sizes[c]);
+    }
     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
     for (auto &e : ev)
         cudaEventCreate(&e);
@@ -866,35 +876,60 @@ int Engine::broadPhase(const StepParams &sp, const StepPlan &plan) {
 }
 
 // The whole step, enqueued on the stream without host round trips.
-void Engine::enqueueStep(const StepPlan &plan) {
+// A kernel whose launch fails (an invalid configuration) leaves its outputs unwritten, and the
+// kernels after it would read them; so the step stops enqueuing at the first phase boundary that
+// finds a launch error, and runPlan reports it instead of running what was enqueued as a step.
+static bool launchesOk() { return cudaPeekAtLastError() == cudaSuccess; }
+
+bool Engine::enqueueStep(const StepPlan &plan) {
     if (plan.mode == 0) {
         const StepParams sp = stepParams(P.dt);
         broadPhase(sp, plan);
         recordPhase(ev[1]);
+        if (!launchesOk())
+            return false;
         warmstartAndSelect(sp);
         projectContacts(sp, false, 0.0f);
         recordPhase(ev[2]);
+        if (!launchesOk())
+            return false;
         runSubstep(sp, P.iterations, true);
         recordPhase(ev[3]);
+        if (!launchesOk())
+            return false;
         projectContacts(sp, P.position_projection != 0, 0.0f);
         launchRebase(d, sp, stream);
-        return;
+        return launchesOk();
     }
     const int substeps = plan.substeps;
     const StepParams sp = stepParams(P.dt * static_cast<real>(substeps));
     broadPhase(sp, plan);
     recordPhase(ev[1]);
+    if (!launchesOk())
+        return false;
     warmstartAndSelect(sp);
     recordPhase(ev[2]);
     for (int sub = 0; sub < substeps; ++sub) {
+        if (!launchesOk())
+            return false;
         if (sub > 0)
             launchRebase(d, sp, stream);
         projectContacts(sp, false, P.dt * static_cast<real>(substeps - sub));
         runSubstep(sp, plan.rounds, sub + 1 == substeps);
     }
     recordPhase(ev[3]);
+    if (!launchesOk())
+        return false;
     projectContacts(sp, P.position_projection != 0, sp.collisionDt);
     launchRebase(d, sp, stream);
+    return launchesOk();
+}
+
+int Engine::launchFailure() {
+    const cudaError_t e = cudaGetLastError();
+    cudaStreamSynchronize(stream);
+    return fail(AVBDG_ERR_CUDA, std::string("step: a kernel launch failed (") + cudaGetErrorString(e) +
+                                    "); the step was stopped and the world's state is not trustworthy");
 }
 
 void Engine::dropGraphs() {
@@ -932,22 +967,31 @@ int Engine::runPlan(const StepPlan &plan) {
         const bool capture = it == graphs.end() && planSeen[k]++ > 0;
         if (it == graphs.end() && !capture) {
             startClock();
-            enqueueStep(plan);
+            if (!enqueueStep(plan))
+                return launchFailure();
         } else if (it == graphs.end()) {
             const int before = launchCount();
             spans.clear();
             evUsed = 0;
             cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
             capturing = true;
-            enqueueStep(plan);
+            const bool launched = enqueueStep(plan);
             capturing = false;
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamEndCapture(stream, &g);
             cudaGraphExec_t exec = nullptr;
-            if (e == cudaSuccess)
+            if (e == cudaSuccess && launched)
                 e = cudaGraphInstantiate(&exec, g, 0);
             if (g)
                 cudaGraphDestroy(g);
+            if (!launched) { // a launch itself failed: running the step eagerly would fail the same way
+                for (const Span &s : spans) {
+                    cudaEventDestroy(s.a);
+                    cudaEventDestroy(s.b);
+                }
+                spans.clear();
+                return launchFailure();
+            }
             if (e != cudaSuccess) {
                 cudaGetLastError(); // capture refused: run eagerly from now on
                 useGraphs = false;
@@ -958,7 +1002,8 @@ int Engine::runPlan(const StepPlan &plan) {
                 }
                 spans.clear();
                 startClock();
-                enqueueStep(plan);
+                if (!enqueueStep(plan))
+                    return launchFailure();
             } else {
                 Graph gr{exec, launchCount() - before, {}};
                 gr.spans.swap(spans);
@@ -974,7 +1019,8 @@ int Engine::runPlan(const StepPlan &plan) {
         }
     } else {
         startClock();
-        enqueueStep(plan);
+        if (!enqueueStep(plan))
+            return launchFailure();
     }
     cudaEventRecord(ev[4], stream);
     timed = true;
@@ -1020,6 +1066,8 @@ void Engine::runSubstep(const StepParams &sp, int rounds, bool idle) {
     const int run = (P.convergence_threshold > 0.0f && rounds > 1) ? 1 : rounds;
     launchStamps(d, sp, false, stream);
     for (int it = 0; it < run; it++) {
+        if (!launchesOk())
+            return; // enqueueStep reports it
         const bool newton = it < newtonRounds;
         if (newton) {
             if (colours) {
@@ -1513,11 +1561,17 @@ void Engine::armTuning() {
 }
 
 // Trial t runs candidate t mod (number of candidates) of every tuned kernel.
+// A candidate that cannot launch (too many registers for its block size) is replaced by the
+// default size for that trial and never chosen.
 void Engine::configureTrial() {
-    tuned.dual = kTuneDual.sizes[tuneTrial % kTuneDual.count];
-    tuned.solve = kTuneSolve.sizes[tuneTrial % kTuneSolve.count];
-    tuned.narrow = kTuneNarrow.sizes[tuneTrial % kTuneNarrow.count];
-    tuned.traverse = kTuneTraverse.sizes[tuneTrial % kTuneTraverse.count];
+    const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
+    int *picks[kKinds] = {&tuned.dual, &tuned.solve, &tuned.narrow, &tuned.traverse};
+    const Tuned defaults;
+    const int fallback[kKinds] = {defaults.dual, defaults.solve, defaults.narrow, defaults.traverse};
+    for (int k = 0; k < kKinds; k++) {
+        const int c = tuneTrial % spaces[k]->count;
+        *picks[k] = tuneFits[k][c] ? spaces[k]->sizes[c] : fallback[k];
+    }
 }
 
 void Engine::finishTrial() {
@@ -1531,7 +1585,7 @@ void Engine::finishTrial() {
         int best = -1;
         double bestMs = 0.0;
         for (int c = 0; c < spaces[k]->count; c++) {
-            if (tuneN[k][c] == 0)
+            if (tuneN[k][c] == 0 || !tuneFits[k][c])
                 continue;
             const double avg = tuneMs[k][c] / tuneN[k][c];
             if (best < 0 || avg < bestMs) {

@@ -148,6 +148,7 @@ private:
     int tuneTrial = 0;
     double tuneMs[kKinds][kTuneCandidates] = {};
     int tuneN[kKinds][kTuneCandidates] = {};
+    bool tuneFits[kKinds][kTuneCandidates] = {}; // the candidate can launch (occupancy >= 1 block)
     void armTuning();
     void configureTrial();
     void finishTrial();
@@ -196,7 +197,8 @@ private:
     bool useGraphs = true, capturing = false, lastGraph = false;
     std::string graphError;
     StepPlan planStep(int mode, int substeps, int rounds);
-    void enqueueStep(const StepPlan &plan);
+    bool enqueueStep(const StepPlan &plan); // false: a launch failed (the rest was not enqueued)
+    int launchFailure();
     int runPlan(const StepPlan &plan);
     void dropGraphs();
     void recordPhase(cudaEvent_t e);

@@ -486,6 +486,10 @@ void launchRefit(const Dev &d, cudaStream_t s) {
     ++launchCount(); refitKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
 }
 
+bool traverseBlockFits(int block) {
+    return blockFits(traverseKernel<false>, block) && blockFits(traverseKernel<true>, block);
+}
+
 void launchPairs(const Dev &d, int block, cudaStream_t s) {
     cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.ctr + C_PAIRSPILL, 0, sizeof(int), s);

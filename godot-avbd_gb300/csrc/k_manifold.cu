@@ -492,6 +492,10 @@ void launchAdjacency(const Dev &d, cudaStream_t s) {
     ++launchCount(); adjInfoKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
 }
 
+bool narrowBlockFits(int block) {
+    return blockFits(manifoldInitKernel<false>, block) && blockFits(manifoldInitKernel<true>, block);
+}
+
 void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block, cudaStream_t s) {
     ++launchCount();
     if (round)

@@ -1137,6 +1137,15 @@ int colourGridBlocks() {
     return g_colourBlocks;
 }
 
+bool dualBlockFits(int block) {
+    return blockFits(dualKernel<false, false>, block) && blockFits(dualKernel<true, false>, block) &&
+           blockFits(dualKernel<false, true>, block) && blockFits(dualKernel<true, true>, block);
+}
+
+bool solveBlockFits(int block) {
+    return blockFits(overflowSolveKernel<false>, block) && blockFits(overflowSolveKernel<true>, block);
+}
+
 void prepareKernels() {
     preparePrimitives();
     prepareNarrowPhase();

@@ -74,6 +74,12 @@ void prepareNarrowPhase();
 int colourGridBlocks();
 // Kernel attributes and cooperative grid sizes, set once before any stream capture.
 void prepareKernels();
+// Whether every instantiation of a tuned kernel can launch with `block` threads (the autotuner
+// only tries sizes that fit; the FP64 build uses far more registers per thread).
+bool dualBlockFits(int block);
+bool solveBlockFits(int block);
+bool narrowBlockFits(int block);
+bool traverseBlockFits(int block);
 
 // ---- host state exchange (k_io.cu) ----
 // Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).

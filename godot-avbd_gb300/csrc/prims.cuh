@@ -44,6 +44,14 @@ inline int residentGrid(K *kernel, int block, int want) {
     return residentGrid(reinterpret_cast<const void *>(kernel), block, 0, want);
 }
 
+// True when at least one block of `block` threads of `kernel` fits on an SM (registers and shared
+// memory): a launch with that block size can run.
+template <typename K>
+inline bool blockFits(K *kernel, int block) {
+    int n = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, 0) == cudaSuccess && n > 0;
+}
+
 // Kernel attributes the primitives need (large dynamic shared memory); call before any capture.
 void preparePrimitives();
 
