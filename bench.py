@@ -361,28 +361,35 @@ def run_gpu(args, rank, world_size):
     return out
 
 
-def fp64_error_report(steps=30):
+def fp64_error_report(checkpoints=(1, 10, 30)):
     """Error of the float32 step, which is bit-identical to the reference's float32 solver, against
     the FP64 build of the same kernels (libavbdg64.so): per benchmark configuration at full size,
-    the largest position (m) and rotation (rad) difference of any body after the first `steps`
-    steps. The FP64 state is read through the same float32 interface (resolution: half a float32
-    ulp of a coordinate)."""
+    after each checkpoint step, the largest and the median position difference (m) and the largest
+    rotation difference (rad) of any body. The FP64 state is read through the same float32
+    interface (resolution: half a float32 ulp of a coordinate)."""
+    import numpy as np
+
     pkg = entry.load_package()
     scenes = pkg.scenes
     from avbd_gb300 import stats
 
     gpu, gpu64 = pkg.gpu_api(), pkg.gpu_api(fp64=True)
-    out = {"steps": steps, "against": "FP64 build of the same GPU kernels (libavbdg64.so)"}
+    out = {"against": "FP64 build of the same GPU kernels (libavbdg64.so)", "steps": list(checkpoints)}
     for name in ("pyramid420", "pile", "lattice"):
         sc = getattr(scenes, name)()
         a = scenes.instantiate(gpu, sc)
         b = scenes.instantiate(gpu64, sc)
-        scenes.advance(a, sc, steps)
-        scenes.advance(b, sc, steps)
-        pa, qa, _, _ = a.state()
-        pb, qb, _, _ = b.state()
-        dx, dq = stats.pose_difference(pa, qa, pb, qb)
-        out[name] = {"bodies": sc.n, "max_position_m": dx, "max_rotation_rad": dq}
+        rec, done = {"bodies": sc.n}, 0
+        for k in checkpoints:
+            scenes.advance(a, sc, k - done)
+            scenes.advance(b, sc, k - done)
+            done = k
+            pa, qa, _, _ = a.state()
+            pb, qb, _, _ = b.state()
+            dx, dq = stats.pose_differences(pa, qa, pb, qb)
+            rec[f"step_{k}"] = {"max_position_m": float(dx.max()), "median_position_m": float(np.median(dx)),
+                                "max_rotation_rad": float(dq.max())}
+        out[name] = rec
         a.close()
         b.close()
     return out

@@ -228,8 +228,8 @@ class RunStats:
         return out
 
 
-def pose_difference(pos_a, quat_a, pos_b, quat_b):
-    """Largest position distance (m) and rotation angle (rad) between two states of the same
+def pose_differences(pos_a, quat_a, pos_b, quat_b):
+    """Per-body position distance (m) and rotation angle (rad) between two states of the same
     bodies, in double precision."""
     pa = np.asarray(pos_a, np.float64)
     pb = np.asarray(pos_b, np.float64)
@@ -238,6 +238,11 @@ def pose_difference(pos_a, quat_a, pos_b, quat_b):
     qa = qa / np.linalg.norm(qa, axis=1, keepdims=True)
     qb = qb / np.linalg.norm(qb, axis=1, keepdims=True)
     c = np.clip(np.abs(np.sum(qa * qb, axis=1)), 0.0, 1.0)
-    dx = float(np.max(np.linalg.norm(pa - pb, axis=1))) if len(pa) else 0.0
-    dq = float(np.max(2.0 * np.arccos(c))) if len(qa) else 0.0
-    return dx, dq
+    return np.linalg.norm(pa - pb, axis=1), 2.0 * np.arccos(c)
+
+
+def pose_difference(pos_a, quat_a, pos_b, quat_b):
+    """Largest position distance (m) and rotation angle (rad) between two states of the same
+    bodies, in double precision."""
+    dx, dq = pose_differences(pos_a, quat_a, pos_b, quat_b)
+    return (float(dx.max()) if dx.size else 0.0), (float(dq.max()) if dq.size else 0.0)
