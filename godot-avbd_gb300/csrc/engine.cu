@@ -84,6 +84,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.wActive, ww);
     take(n.wColour, ww);
     take(n.wSleep, 2 * static_cast<size_t>(ww));
+    take(n.gridBar, 2);
     take(n.x, nb);
     take(n.q, nb);
     take(n.x0, nb);
@@ -1071,9 +1072,8 @@ void Engine::runSubstep(const StepParams &sp, int rounds, bool idle) {
         const bool newton = it < newtonRounds;
         if (newton) {
             if (colours) {
-                // Each pass reads its colour's size on the device; empty colours return at once.
-                for (int c = 0; c < kMaxColours; c++)
-                    launchColourPass(d, c, sp, it > 0, stream);
+                // The colours in one cooperative sweep (sizes read on the device, empty colours skipped).
+                launchColourSweep(d, sp, it > 0, stream);
                 launchStamps(d, sp, true, stream);
             }
             beginSpan();
@@ -1116,6 +1116,8 @@ int Engine::finishStep() {
             return fail(AVBDG_ERR_TIMEOUT, "brake sweep: a bounded wait for a preceding candidate gave up");
         if (e & kErrColourTimeout)
             return fail(AVBDG_ERR_TIMEOUT, "colouring: a bounded wait for an earlier neighbour gave up");
+        if (e & kErrBarrierTimeout)
+            return fail(AVBDG_ERR_TIMEOUT, "colour sweep: a bounded grid barrier gave up");
         return fail(AVBDG_ERR_CAPACITY, "a device buffer overflowed this step (state is not trustworthy)");
     }
     // Keep headroom for the next step's pairs and manifolds.

@@ -63,6 +63,7 @@ constexpr int kErrManifolds = 2;
 constexpr int kErrAdjacency = 4;
 constexpr int kErrBrakeTimeout = 8;
 constexpr int kErrColourTimeout = 16;
+constexpr int kErrBarrierTimeout = 32; // a grid barrier of a cooperative sweep gave up
 
 // Solver fields a kernel reads (src/avbd/solver.h:54-144), with derived terms.
 struct StepParams {
@@ -98,6 +99,7 @@ struct Dev {
     int NB, MM, FF, PP, WW; // capacities
     int ARM;                // 1: the arm-cache arrays of ManifoldBuf are allocated
     long long waitLimit;    // spins a dataflow wait makes before it reports a timeout
+    unsigned *gridBar;      // grid barrier of the cooperative sweeps: arrivals, generation
     // worlds
     int *wBase, *wCount;    // body range
     int *wMaxDepth;         // projection: max depth bits per world (positive floats)

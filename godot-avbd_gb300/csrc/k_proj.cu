@@ -18,6 +18,7 @@
 
 #include <cooperative_groups.h>
 
+#include "gridsync.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -354,10 +355,11 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
 
 // Grid-stride in whole warps (every lane runs every pass), so the per-world depth maximum is
 // reduced across the warp first and one lane per world and warp does the atomic.
-__global__ void projManifoldKernel(Dev d, StepParams p) {
+// The manifolds' contributions of one pass, a warp per 32 manifolds: each world's deepest patch is
+// reduced across the warp (one atomic per world and warp).
+__device__ __forceinline__ void projManifoldPass(const Dev &d, const StepParams &p, int first, int stride) {
     const int n = d.ctr[C_LIVE];
-    const int stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    for (int base = first + (threadIdx.x & ~31); base < n; base += stride) {
         int world = -1, depthBits = 0;
         projManifoldAt(d, p, base + (threadIdx.x & 31), world, depthBits);
         const unsigned peers = __match_any_sync(0xffffffffu, world);
@@ -367,10 +369,9 @@ __global__ void projManifoldKernel(Dev d, StepParams p) {
     }
 }
 
-__global__ void projBodyKernel(Dev d, StepParams p) {
-    const int nBodies = d.ctr[C_BODIES];
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nBodies || d.meta[g].x < 0 || !movable(d, g))
+// One body's averaged correction of a pass: its contributions in adjacency order, capped, applied.
+__device__ __forceinline__ void projBodyAt(const Dev &d, const StepParams &p, int g) {
+    if (d.meta[g].x < 0 || !movable(d, g))
         return;
     if (d.wStop[d.meta[g].x])
         return;
@@ -414,24 +415,36 @@ __global__ void projBodyKernel(Dev d, StepParams p) {
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
 
-__global__ void projCheckKernel(Dev d, real tolerance) {
+// Solver::projectContacts's passes (solver_projection.cpp:169-280) in one cooperative launch: a
+// world with no movable manifold is stopped at once (the reference returns early); then each pass
+// computes the manifolds' contributions, averages and applies them per body, and stops the worlds
+// whose deepest patch is within tolerance, with a grid barrier between these phases (the kernel
+// boundaries of the same sequence launched separately).
+__global__ void __launch_bounds__(kThreads) projectionKernel(Dev d, StepParams p, real tolerance) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = gridDim.x * blockDim.x;
     const int nWorlds = d.ctr[C_WORLDS];
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nWorlds)
-        return;
-    if (!d.wStop[w] && bitsf(d.wMaxDepth[w]) <= tolerance)
-        d.wStop[w] = 1;
-    d.wMaxDepth[w] = 0;
-}
-
-// Worlds with no movable manifold skip the whole projection (the reference returns early).
-__global__ void projStartKernel(Dev d) {
-    const int nWorlds = d.ctr[C_WORLDS];
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nWorlds)
-        return;
-    d.wStop[w] = d.wActive[w] > 0 ? 0 : 1;
-    d.wMaxDepth[w] = 0;
+    const int nBodies = d.ctr[C_BODIES];
+    for (int w = tid; w < nWorlds; w += stride) {
+        d.wStop[w] = d.wActive[w] > 0 ? 0 : 1;
+        d.wMaxDepth[w] = 0;
+    }
+    for (int it = 0; it < p.projIters; it++) {
+        if (!gridSync(d))
+            return;
+        projManifoldPass(d, p, blockIdx.x * blockDim.x, stride);
+        if (!gridSync(d))
+            return;
+        for (int g = tid; g < nBodies; g += stride)
+            projBodyAt(d, p, g);
+        if (!gridSync(d))
+            return;
+        for (int w = tid; w < nWorlds; w += stride) {
+            if (!d.wStop[w] && bitsf(d.wMaxDepth[w]) <= tolerance)
+                d.wStop[w] = 1;
+            d.wMaxDepth[w] = 0;
+        }
+    }
 }
 
 int g_brakeBlocks = 0;
@@ -471,14 +484,32 @@ void launchBrake(const Dev &d, real window, cudaStream_t s) {
                                 args, 0, s);
 }
 
-void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); projStartKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
-    const real tol = smax(p.projSlop * 0.01f, 1.0e-6f);
-    for (int it = 0; it < p.projIters; it++) {
-        ++launchCount(); projManifoldKernel<<<residentGrid(projManifoldKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
-        ++launchCount(); projBodyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
-        ++launchCount(); projCheckKernel<<<grid(d.WW), kThreads, 0, s>>>(d, tol);
+static int g_projBlocks = 0;
+
+static int projGridMax() {
+    if (g_projBlocks == 0) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, projectionKernel, kThreads, 0);
+        g_projBlocks = sms * (perSm < 1 ? 1 : perSm);
     }
+    return g_projBlocks;
+}
+
+int projectionGridBlocks() { return projGridMax(); }
+
+void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
+    const int need = grid(d.MM > d.NB ? d.MM : d.NB);
+    const int most = projGridMax();
+    const int blocks = need < most ? need : most;
+    cudaMemsetAsync(d.gridBar, 0, sizeof(unsigned), s);
+    Dev dd = d;
+    StepParams pp = p;
+    real tol = smax(p.projSlop * 0.01f, 1.0e-6f);
+    void *args[] = {&dd, &pp, &tol};
+    ++launchCount();
+    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(projectionKernel), dim3(blocks), dim3(kThreads), args, 0, s);
 }
 
 } // namespace avbdg

@@ -14,6 +14,7 @@
 // touch; the reference's "first touch uses the dual's cache" rule yields the same floats.
 
 #include "forces.cuh"
+#include "gridsync.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
 
@@ -23,7 +24,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kSolveThreads = 128;
-constexpr int kFallbackBlocks = 8; // the pivoted fallback is rare: a few blocks, grid-stride
 
 struct Blk {
     m3 lin, ang, crs;
@@ -835,10 +835,8 @@ __device__ __forceinline__ Blk bodyBlock(const Dev &d, const StepParams &p, int 
     return makeBlock(x4.w, xyz(d.moment[g]), p.dtSq, xyz(x4), xyz(d.xi[g]), asq(d.q[g]), asq(d.qi[g]));
 }
 
-__global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepParams p, int colour, int armsFromDual) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.colourCount[colour])
-        return;
+// One coloured body's Gauss-Seidel update (solver_step.cpp:209-229).
+__device__ __forceinline__ void colourPassAt(const Dev &d, const StepParams &p, int colour, int k, int armsFromDual) {
     const int g = d.colourList[colour * d.NB + k];
     Blk blk = bodyBlock(d, p, g);
     assemble<true>(d, p, g, blk, armsFromDual);
@@ -847,6 +845,26 @@ __global__ void __launch_bounds__(kSolveThreads) colourPassKernel(Dev d, StepPar
     const real4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), dl), x4.w);
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
+}
+
+// One round's colour passes in one cooperative launch: colours in order, each a grid-stride loop
+// over its list, a grid barrier after each but the last non-empty one. Every block reads the same
+// counts (nothing writes them during the sweep), so all blocks skip the same empty colours.
+__global__ void __launch_bounds__(kSolveThreads) colourSweepKernel(Dev d, StepParams p, int armsFromDual) {
+    int last = -1;
+    for (int c = 0; c < kMaxColours; c++)
+        if (d.colourCount[c] > 0)
+            last = c;
+    const int stride = gridDim.x * blockDim.x;
+    for (int c = 0; c <= last; c++) {
+        const int cnt = d.colourCount[c];
+        if (cnt == 0)
+            continue;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += stride)
+            colourPassAt(d, p, c, k, armsFromDual);
+        if (c < last && !gridSync(d))
+            return;
+    }
 }
 
 // An overflow body's step: in place (no forces) or into dLin/dAng for overflowApplyKernel.
@@ -861,9 +879,28 @@ __device__ __forceinline__ void applyOverflow(const Dev &d, const StepParams &p,
     }
 }
 
+// solve()'s pivoted fallback for a body whose plain LDLT failed, out of line so the common path
+// keeps its registers; the kernel's parameters are grid constants, so the call passes their
+// addresses without copying them. The block is assembled again (the same floats: it reads the
+// stamps and this body's own pose, which nothing changes during the pass; with forces, poses are
+// not written during the pass at all).
+template <bool FORCES>
+__device__ __noinline__ void fallbackSolve(const Dev &d, const StepParams &p, int g, int inPlace) {
+    Blk blk = bodyBlock(d, p, g);
+    assemble<false, FORCES>(d, p, g, blk);
+    const Delta r = solvePivoted(blk);
+    applyOverflow(d, p, g, inPlace, r.ok ? r.dl : f3{0, 0, 0}, r.ok ? r.da : f3{0, 0, 0});
+}
+
 // Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
 template <bool FORCES>
-__global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, StepParams p, int inPlace) {
+#ifdef AVBDG_FP64
+#define AVBDG_SOLVE_BOUNDS __launch_bounds__(kSolveThreads)
+#else
+#define AVBDG_SOLVE_BOUNDS __launch_bounds__(kSolveThreads, 8) // 64 registers: 8 blocks an SM
+#endif
+__global__ void AVBDG_SOLVE_BOUNDS
+        overflowSolveKernel(const __grid_constant__ Dev d, const __grid_constant__ StepParams p, int inPlace) {
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
@@ -872,25 +909,10 @@ __global__ void __launch_bounds__(kSolveThreads) overflowSolveKernel(Dev d, Step
     assemble<false, FORCES>(d, p, g, blk);
     f3 dl, da;
     if (!solveBlockFast(blk, dl, da)) {
-        d.solveFail[atomicAdd(d.ctr + C_SOLVEFAIL, 1)] = g; // overflowFallbackKernel takes it
+        fallbackSolve<FORCES>(d, p, g, inPlace);
         return;
     }
     applyOverflow(d, p, g, inPlace, dl, da);
-}
-
-// The bodies whose plain LDLT failed, through solve()'s pivoted fallback. Block-Jacobi: a block
-// reads stamps and its own pose only (with forces, updates go through dLin/dAng), so solving these
-// after the others gives the same result.
-template <bool FORCES>
-__global__ void __launch_bounds__(kSolveThreads) overflowFallbackKernel(Dev d, StepParams p, int inPlace) {
-    const int n = d.ctr[C_SOLVEFAIL];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int g = d.solveFail[i];
-        Blk blk = bodyBlock(d, p, g);
-        assemble<false, FORCES>(d, p, g, blk);
-        const Delta r = solvePivoted(blk);
-        applyOverflow(d, p, g, inPlace, r.ok ? r.dl : f3{0, 0, 0}, r.ok ? r.da : f3{0, 0, 0});
-    }
 }
 
 __global__ void overflowApplyKernel(Dev d, StepParams p) {
@@ -1146,7 +1168,22 @@ bool solveBlockFits(int block) {
     return blockFits(overflowSolveKernel<false>, block) && blockFits(overflowSolveKernel<true>, block);
 }
 
+static int g_sweepBlocks = 0;
+
+static int sweepGridMax() {
+    if (g_sweepBlocks == 0) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, colourSweepKernel, kSolveThreads, 0);
+        g_sweepBlocks = sms * (perSm < 1 ? 1 : perSm);
+    }
+    return g_sweepBlocks;
+}
+
 void prepareKernels() {
+    sweepGridMax();
+    projectionGridBlocks();
     preparePrimitives();
     prepareNarrowPhase();
     brakeGridBlocks();
@@ -1182,21 +1219,25 @@ void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_
     ++launchCount(); stampsKernel<<<residentGrid(stampsKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
 }
 
-void launchColourPass(const Dev &d, int colour, const StepParams &p, bool armsFromDual, cudaStream_t s) {
+void launchColourSweep(const Dev &d, const StepParams &p, bool armsFromDual, cudaStream_t s) {
+    const int want = divUp(d.NB, kSolveThreads), most = sweepGridMax();
+    const int blocks = want < most ? want : most;
+    cudaMemsetAsync(d.gridBar, 0, sizeof(unsigned), s);
+    Dev dd = d;
+    StepParams pp = p;
+    int arms = armsFromDual ? 1 : 0;
+    void *args[] = {&dd, &pp, &arms};
     ++launchCount();
-    colourPassKernel<<<divUp(d.NB, kSolveThreads), kSolveThreads, 0, s>>>(d, p, colour, armsFromDual ? 1 : 0);
+    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(colourSweepKernel), dim3(blocks), dim3(kSolveThreads),
+                                args, 0, s);
 }
 
 void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s) {
-    cudaMemsetAsync(d.ctr + C_SOLVEFAIL, 0, sizeof(int), s);
-    launchCount() += 2;
-    if (forces) {
+    ++launchCount();
+    if (forces)
         overflowSolveKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
-        overflowFallbackKernel<true><<<kFallbackBlocks, kSolveThreads, 0, s>>>(d, p, inPlace ? 1 : 0);
-    } else {
+    else
         overflowSolveKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
-        overflowFallbackKernel<false><<<kFallbackBlocks, kSolveThreads, 0, s>>>(d, p, inPlace ? 1 : 0);
-    }
 }
 
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {

@@ -53,7 +53,8 @@ void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream
 // also touch a coloured body (recomputed after the colour passes).
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
 // `armsFromDual`: a dual pass ran since the manifolds were (re)initialised or rebased.
-void launchColourPass(const Dev &d, int colour, const StepParams &p, bool armsFromDual, cudaStream_t s);
+// One round's Gauss-Seidel colour passes, colours in order, in one cooperative launch.
+void launchColourSweep(const Dev &d, const StepParams &p, bool armsFromDual, cudaStream_t s);
 // Block-Jacobi solve of every dynamic body in the overflow colour (walked in slot order).
 void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s);
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s);
@@ -69,6 +70,7 @@ void launchBrake(const Dev &d, real window, cudaStream_t s);
 void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s);
 
 int brakeGridBlocks();
+int projectionGridBlocks();
 // Constant tables of the narrow phase (cylinder rim directions); before any capture.
 void prepareNarrowPhase();
 int colourGridBlocks();

