@@ -415,6 +415,35 @@ __device__ __forceinline__ void projBodyAt(const Dev &d, const StepParams &p, in
     d.q[g] = f4(qintegrate(asq(d.q[g]), da));
 }
 
+// The same passes as separate launches, for large stores, where every phase fills the GPU and a
+// kernel boundary costs less than a grid barrier of a resident grid.
+__global__ void projStartKernel(Dev d) {
+    const int nWorlds = d.ctr[C_WORLDS];
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nWorlds)
+        return;
+    d.wStop[w] = d.wActive[w] > 0 ? 0 : 1;
+    d.wMaxDepth[w] = 0;
+}
+
+__global__ void projManifoldKernel(Dev d, StepParams p) { projManifoldPass(d, p, blockIdx.x * blockDim.x, gridDim.x * blockDim.x); }
+
+__global__ void projBodyKernel(Dev d, StepParams p) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < d.ctr[C_BODIES])
+        projBodyAt(d, p, g);
+}
+
+__global__ void projCheckKernel(Dev d, real tolerance) {
+    const int nWorlds = d.ctr[C_WORLDS];
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nWorlds)
+        return;
+    if (!d.wStop[w] && bitsf(d.wMaxDepth[w]) <= tolerance)
+        d.wStop[w] = 1;
+    d.wMaxDepth[w] = 0;
+}
+
 // Solver::projectContacts's passes (solver_projection.cpp:169-280) in one cooperative launch: a
 // world with no movable manifold is stopped at once (the reference returns early); then each pass
 // computes the manifolds' contributions, averages and applies them per body, and stops the worlds
@@ -499,10 +528,23 @@ static int projGridMax() {
 
 int projectionGridBlocks() { return projGridMax(); }
 
+// Stores whose manifold and body capacities fit in one resident wave take the cooperative form (its
+// grid barriers cost less than kernel boundaries when each phase is a few blocks); larger stores
+// launch the phases separately.
 void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
     const int need = grid(d.MM > d.NB ? d.MM : d.NB);
     const int most = projGridMax();
-    const int blocks = need < most ? need : most;
+    if (need > most) {
+        const real tol0 = smax(p.projSlop * 0.01f, 1.0e-6f);
+        ++launchCount(); projStartKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
+        for (int it = 0; it < p.projIters; it++) {
+            ++launchCount(); projManifoldKernel<<<residentGrid(projManifoldKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
+            ++launchCount(); projBodyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+            ++launchCount(); projCheckKernel<<<grid(d.WW), kThreads, 0, s>>>(d, tol0);
+        }
+        return;
+    }
+    const int blocks = need;
     cudaMemsetAsync(d.gridBar, 0, sizeof(unsigned), s);
     Dev dd = d;
     StepParams pp = p;
