@@ -210,12 +210,6 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
 #ifdef AVBDG_FP64
     tuneEnabled = false; // the FP64 build states an error, not a speed: default block sizes
 #endif
-    // AVBDG_DUAL_LANES=1: every dual pass takes the multi-lane form (the tests check both forms).
-    const char *lanes = std::getenv("AVBDG_DUAL_LANES");
-    if (lanes && lanes[0] == '1') {
-        tuneEnabled = false;
-        tuned.dual = -128;
-    }
     int dev = 0, hostTables = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);

@@ -143,7 +143,7 @@ private:
         int dual = 256, solve = 128, narrow = 256, traverse = 256;
     };
     Tuned tuned;
-    static constexpr int kTuneDelay = 4, kTuneTrials = 10;
+    static constexpr int kTuneDelay = 4, kTuneTrials = 8;
     bool tuneEnabled = true, tuning = false;
     int tuneTrial = 0;
     double tuneMs[kKinds][kTuneCandidates] = {};

@@ -329,15 +329,12 @@ __device__ __forceinline__ SideTerms sideTerms(const real S[6], f3 r, f3 fw) {
     return t;
 }
 
-__device__ __forceinline__ void addSideTerms(const SideTerms &t, SideAcc &acc) {
+__device__ __forceinline__ void stampContact(const real S[6], f3 r, f3 fw, SideAcc &acc) {
+    const SideTerms t = sideTerms(S, r, fw);
     const real *h = t.h;
     acc.ang = madd(acc.ang, mcols(f3{h[0], h[1], h[2]}, f3{h[1], h[3], h[4]}, f3{h[2], h[4], h[5]}));
     acc.crs = madd(acc.crs, t.rs);
     acc.rhsAng = add(acc.rhsAng, t.rc);
-}
-
-__device__ __forceinline__ void stampContact(const real S[6], f3 r, f3 fw, SideAcc &acc) {
-    addSideTerms(sideTerms(S, r, fw), acc);
 }
 
 __device__ __forceinline__ void stampShared(const real S[6], f3 fw, SharedAcc &acc) {
@@ -497,68 +494,6 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
         stampsAt(d, p, mixedOnly, m);
 }
 
-// One contact's dual update (ManifoldStore::updateDual, manifold.cpp:583-671) and, with `stamp`,
-// what the next round's stamp adds for it: the unique entries S of B^T K B, the world force fw and
-// the world arms the stamp uses (the reference's phase-A recompute, manifold.cpp:655-659, always
-// with fresh arms at this pose, whatever the dual used).
-template <bool ARM>
-__device__ __forceinline__ void dualContact(const Dev &d, const StepParams &p, const ManifoldBuf &L, int ci,
-                                            const Pose &A, const Pose &B, f3 r0, f3 r1, f3 r2, real mu, real decay,
-                                            bool driftUsable, bool stamp, real S[6], f3 &fw, f3 &rAs, f3 &rBs) {
-    const real4 rA4 = __ldg(&L.rA[ci]);
-    f3 rAw, rBw;
-    if (driftUsable) {
-        rAw = xyz(L.armA[ci]);
-        rBw = xyz(L.armB[ci]);
-    } else {
-        rAw = mul(A.rot, xyz(rA4));
-        rBw = mul(B.rot, xyz(__ldg(&L.rB[ci])));
-        if (ARM) {
-            L.armA[ci] = f4(rAw, 0.0f);
-            L.armB[ci] = f4(rBw, 0.0f);
-        }
-    }
-    const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
-    const f3 C = contactError(p, xyz(__ldg(&L.C0[ci])), bracket, r0, r1, r2);
-    f3 k = xyz(L.k[ci]);
-    if (decay < 1.0f)
-        k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
-    const real4 lam4 = L.lam[ci];
-    real stick = lam4.w;
-    f3 F = add(cmul(k, C), xyz(lam4));
-    const Cone cone = clampForce(F, mu);
-    const f3 lam = F;
-    const real beta = p.betaLin * rA4.w;
-    if (F.x < 0)
-        k.x = smin(k.x + beta * mabs(C.x), PENALTY_MAX);
-    if (cone.scale <= cone.bounds) {
-        k.y = smin(k.y + beta * mabs(C.y), PENALTY_MAX);
-        k.z = smin(k.z + beta * mabs(C.z), PENALTY_MAX);
-        stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
-    }
-    L.k[ci] = f4(k, 0.0f);
-    L.lam[ci] = f4(lam, stick);
-    if (!stamp)
-        return;
-    rAs = rAw;
-    rBs = rBw;
-    f3 Cs = C;
-    if (ARM) {
-        if (driftUsable) {
-            rAs = mul(A.rot, xyz(rA4));
-            rBs = mul(B.rot, xyz(L.rB[ci]));
-            const f3 bracketF = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAs)), cross(B.dAng, rBs));
-            Cs = contactError(p, xyz(L.C0[ci]), bracketF, r0, r1, r2);
-        }
-        L.armA[ci] = f4(rAs, 0.0f);
-        L.armB[ci] = f4(rBs, 0.0f);
-    }
-    f3 Fn = add(cmul(k, Cs), lam);
-    clampForce(Fn, mu);
-    basisHessianD(r0, r1, r2, k, S);
-    fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
-}
-
 // Dual pass (ManifoldStore::updateDual, manifold.cpp:583-671) and, with STAMPS, the next round's
 // stamps (the reference's phase-A recompute of each force, manifold.cpp:655-659, from the same
 // floats). One thread per manifold, grid-stride over the live ones.
@@ -594,11 +529,59 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, real deca
         zeroAcc(sa);
         zeroAcc(sb);
         for (int c = 0; c < n; c++) {
-            real S[6];
-            f3 fw, rAs, rBs;
-            dualContact<ARM>(d, p, L, cslot(d, m, c), A, B, r0, r1, r2, mu, decay, driftUsable, STAMPS && sides, S, fw,
-                             rAs, rBs);
+            const int ci = cslot(d, m, c);
+            const real4 rA4 = __ldg(&L.rA[ci]);
+            f3 rAw, rBw;
+            if (driftUsable) {
+                rAw = xyz(L.armA[ci]);
+                rBw = xyz(L.armB[ci]);
+            } else {
+                rAw = mul(A.rot, xyz(rA4));
+                rBw = mul(B.rot, xyz(__ldg(&L.rB[ci])));
+                if (ARM) {
+                    L.armA[ci] = f4(rAw, 0.0f);
+                    L.armB[ci] = f4(rBw, 0.0f);
+                }
+            }
+            const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+            const f3 C = contactError(p, xyz(__ldg(&L.C0[ci])), bracket, r0, r1, r2);
+            f3 k = xyz(L.k[ci]);
+            if (decay < 1.0f)
+                k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
+            const real4 lam4 = L.lam[ci];
+            real stick = lam4.w;
+            f3 F = add(cmul(k, C), xyz(lam4));
+            const Cone cone = clampForce(F, mu);
+            const f3 lam = F;
+            const real beta = p.betaLin * rA4.w;
+            if (F.x < 0)
+                k.x = smin(k.x + beta * mabs(C.x), PENALTY_MAX);
+            if (cone.scale <= cone.bounds) {
+                k.y = smin(k.y + beta * mabs(C.y), PENALTY_MAX);
+                k.z = smin(k.z + beta * mabs(C.z), PENALTY_MAX);
+                stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
+            }
+            L.k[ci] = f4(k, 0.0f);
+            L.lam[ci] = f4(lam, stick);
             if (STAMPS && sides) {
+                // These are the next round's overflow phase A (solver_step.cpp:236-248): it always
+                // precomputes with fresh arms at this pose and stores them, whatever the dual used.
+                f3 rAs = rAw, rBs = rBw, Cs = C;
+                if (ARM) {
+                    if (driftUsable) {
+                        rAs = mul(A.rot, xyz(rA4));
+                        rBs = mul(B.rot, xyz(L.rB[ci]));
+                        const f3 bracketF = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAs)), cross(B.dAng, rBs));
+                        Cs = contactError(p, xyz(L.C0[ci]), bracketF, r0, r1, r2);
+                    }
+                    L.armA[ci] = f4(rAs, 0.0f);
+                    L.armB[ci] = f4(rBs, 0.0f);
+                }
+                f3 Fn = add(cmul(k, Cs), lam);
+                clampForce(Fn, mu);
+                real S[6];
+                basisHessianD(r0, r1, r2, k, S);
+                const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
                 stampShared(S, fw, sh);
                 if (sides & kSideA)
                     stampContact(S, rAs, fw, sa);
@@ -614,109 +597,6 @@ __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, real deca
                 storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
         }
         if (ARM && !driftUsable) { // capture (manifold.cpp:662-667)
-            L.capA[m] = f4(A.rot.c0, 0.0f);
-            L.capB[m] = f4(B.rot.c0, 0.0f);
-            L.armFlag[m] = 1;
-        }
-    }
-}
-
-// ---- the dual pass with several lanes per manifold ----
-//
-// For stores with too few manifolds to fill the GPU one thread each (one large world, a small world),
-// each manifold gets kDualLanes lanes of a warp: lane j updates contacts j, j + kDualLanes, ... and
-// computes their stamp terms; the group then adds the terms in contact order, exactly the sums
-// dualKernel forms one contact after another, so the results are bit-identical. The lanes share
-// the manifold's loads (each lane loads the poses itself; they are the same lines).
-constexpr int kDualLanes = 4;
-
-__device__ __forceinline__ real shflReal(unsigned mask, real v, int src) { return __shfl_sync(mask, v, src, kDualLanes); }
-
-__device__ __forceinline__ f3 shfl3(unsigned mask, f3 v, int src) {
-    return f3{shflReal(mask, v.x, src), shflReal(mask, v.y, src), shflReal(mask, v.z, src)};
-}
-
-__device__ __forceinline__ m3 shflM3(unsigned mask, const m3 &v, int src) {
-    return m3{shfl3(mask, v.c0, src), shfl3(mask, v.c1, src), shfl3(mask, v.c2, src)};
-}
-
-__device__ __forceinline__ SideTerms shflTerms(unsigned mask, const SideTerms &t, int src) {
-    SideTerms o;
-#pragma unroll
-    for (int k = 0; k < 6; k++)
-        o.h[k] = shflReal(mask, t.h[k], src);
-    o.rs = shflM3(mask, t.rs, src);
-    o.rc = shfl3(mask, t.rc, src);
-    return o;
-}
-
-template <bool STAMPS, bool ARM>
-__global__ void __launch_bounds__(256) dualLanesKernel(Dev d, StepParams p, real decay) {
-    const int live = d.ctr[C_LIVE];
-    const ManifoldBuf L = d.live;
-    const int lane = threadIdx.x & (kDualLanes - 1);
-    const unsigned group = ((1u << kDualLanes) - 1u) << ((threadIdx.x & 31) & ~(kDualLanes - 1));
-    const int perBlock = blockDim.x / kDualLanes;
-    for (int m = blockIdx.x * perBlock + threadIdx.x / kDualLanes; m < live; m += gridDim.x * perBlock) {
-        // Everything up to the contacts is uniform across the group (same manifold).
-        const int2 ab = __ldg(&L.ab[m]);
-        if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
-            continue; // frozen (manifold.cpp:168-172)
-        bool touches = false;
-        int sides = STAMPS ? overflowSides(d, ab, touches) : 0;
-        if (touches)
-            sides = 0; // recomputed after the colour passes
-        const Pose A = loadPoseRO(d, ab.x), B = loadPoseRO(d, ab.y);
-        const real4 b04 = __ldg(&L.b0[m]);
-        const f3 r0 = xyz(b04), r1 = xyz(__ldg(&L.b1[m])), r2 = xyz(__ldg(&L.b2[m]));
-        const real mu = b04.w;
-        const int n = __ldg(&L.count[m]);
-        bool driftUsable = false;
-        if (ARM) {
-            const f3 dA = sub(A.rot.c0, xyz(L.capA[m])), dB = sub(B.rot.c0, xyz(L.capB[m]));
-            driftUsable = L.armFlag[m] != 0 && length2(dA) <= p.armRebuild2 && length2(dB) <= p.armRebuild2;
-        }
-        SharedAcc sh;
-        sh.lin = mzero();
-        sh.rhsLin = f3{0, 0, 0};
-        SideAcc sa, sb;
-        zeroAcc(sa);
-        zeroAcc(sb);
-        for (int base = 0; base < n; base += kDualLanes) {
-            const int c = base + lane;
-            real S[6] = {0, 0, 0, 0, 0, 0};
-            f3 fw{0, 0, 0}, rAs{0, 0, 0}, rBs{0, 0, 0};
-            if (c < n)
-                dualContact<ARM>(d, p, L, cslot(d, m, c), A, B, r0, r1, r2, mu, decay, driftUsable, STAMPS && sides, S,
-                                 fw, rAs, rBs);
-            if (!(STAMPS && sides))
-                continue;
-            SideTerms tA{}, tB{};
-            if (c < n && (sides & kSideA))
-                tA = sideTerms(S, rAs, fw);
-            if (c < n && (sides & kSideB))
-                tB = sideTerms(S, rBs, fw);
-            const int here = n - base < kDualLanes ? n - base : kDualLanes;
-            for (int j = 0; j < here; j++) { // contact base + j, in order
-                real Sj[6];
-#pragma unroll
-                for (int k = 0; k < 6; k++)
-                    Sj[k] = shflReal(group, S[k], j);
-                stampShared(Sj, shfl3(group, fw, j), sh);
-                if (sides & kSideA)
-                    addSideTerms(shflTerms(group, tA, j), sa);
-                if (sides & kSideB)
-                    addSideTerms(shflTerms(group, tB, j), sb);
-            }
-        }
-        if (sides) {
-            const int2 slot = d.stampSlot[m];
-            if ((sides & kSideA) && lane == 0)
-                storeStamp(d.stamps + static_cast<size_t>(slot.x) * kStampF4, sh, sa, 1.0f);
-            if ((sides & kSideB) && lane == 1)
-                storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
-        }
-        if (ARM && !driftUsable && lane == 0) { // capture (manifold.cpp:662-667)
             L.capA[m] = f4(A.rot.c0, 0.0f);
             L.capB[m] = f4(B.rot.c0, 0.0f);
             L.armFlag[m] = 1;
@@ -1280,9 +1160,6 @@ int colourGridBlocks() {
 }
 
 bool dualBlockFits(int block) {
-    if (block < 0)
-        return blockFits(dualLanesKernel<false, false>, -block) && blockFits(dualLanesKernel<true, false>, -block) &&
-               blockFits(dualLanesKernel<false, true>, -block) && blockFits(dualLanesKernel<true, true>, -block);
     return blockFits(dualKernel<false, false>, block) && blockFits(dualKernel<true, false>, block) &&
            blockFits(dualKernel<false, true>, block) && blockFits(dualKernel<true, true>, block);
 }
@@ -1370,12 +1247,6 @@ void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {
 
 template <bool STAMPS, bool ARM>
 static void dualLaunch(const Dev &d, const StepParams &p, real decay, int block, cudaStream_t s) {
-    if (block < 0) {
-        const int threads = -block;
-        const int blocks = residentGrid(dualLanesKernel<STAMPS, ARM>, threads, divUp(d.MM, threads / kDualLanes));
-        dualLanesKernel<STAMPS, ARM><<<blocks, threads, 0, s>>>(d, p, decay);
-        return;
-    }
     const int blocks = residentGrid(dualKernel<STAMPS, ARM>, block, divUp(d.MM, block));
     dualKernel<STAMPS, ARM><<<blocks, block, 0, s>>>(d, p, decay);
 }

@@ -7,14 +7,12 @@ namespace avbdg {
 
 // Kernels with one thread per independent item take their block size from the autotuner (their
 // results do not depend on it); the candidates are the sizes each kernel's registers allow.
-// A negative size selects a kernel's multi-lane form with that many threads a block (several lanes
-// per item: for stores too small to fill the GPU one thread per item).
-constexpr int kTuneCandidates = 5;
+constexpr int kTuneCandidates = 4;
 struct TuneSpace {
     int sizes[kTuneCandidates];
     int count;
 };
-constexpr TuneSpace kTuneDual{{64, 128, 256, 512, -128}, 5}; // dualKernel; -128: dualLanesKernel
+constexpr TuneSpace kTuneDual{{64, 128, 256, 512}, 4};     // dualKernel (one thread per manifold)
 constexpr TuneSpace kTuneSolve{{32, 64, 128, 0}, 3};       // overflowSolveKernel (launch bound 128)
 constexpr TuneSpace kTuneNarrow{{64, 128, 256, 512}, 4};   // manifoldInitKernel
 constexpr TuneSpace kTuneTraverse{{64, 128, 256, 512}, 4}; // traverseKernel

@@ -114,8 +114,7 @@ typedef struct avbdg_stats {
     int graph_step;               /* 1 if the last step ran as one CUDA graph launch */
     int kernel_launches;          /* kernels of this library in the last step */
     /* block sizes the autotuner picked (0 while it is still trying candidates): manifold dual,
-     * overflow block solve, narrow phase, tree traversal; a negative size is a kernel's multi-lane
-     * form (several lanes per item) with that many threads a block */
+     * overflow block solve, narrow phase, tree traversal */
     int block_dual, block_solve, block_narrow, block_traverse;
 } avbdg_stats;
 
