@@ -215,8 +215,6 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
     const char *staged = std::getenv("AVBDG_STAGED_IO");
     directIo = hostTables == 1 && !(staged && staged[0] == '1');
-    const char *copyIo = std::getenv("AVBDG_COPY_IO"); // 1: copy-engine transfers instead of the kernels
-    kernelIo = directIo && !(copyIo && copyIo[0] == '1');
     armTuning();
     prepareKernels(); // attributes and occupancy queries, never during a capture
     {
@@ -1403,12 +1401,6 @@ int Engine::getState(int w, int first, int count, float *pos, float *quat, float
         return rc;
     launchPackState(d, g0, count, ioDev, stream);
     const size_t n = static_cast<size_t>(count);
-    if (kernelIo) {
-        // Written straight into the caller's arrays by a kernel (host page tables).
-        launchHostScatter(ioDev, count, pos, quat, vel, angVel, stream);
-        cudaStreamSynchronize(stream);
-        return cudaCheck("getState");
-    }
     if (directIo) {
         // One copy per requested field into the caller's arrays.
         if (pos)
@@ -1451,21 +1443,6 @@ int Engine::setState(int w, int first, int count, const float *pos, const float 
     if (rc)
         return rc;
     const size_t n = static_cast<size_t>(count);
-    if (kernelIo) {
-        // A kernel reads the caller's arrays (host page tables) into the staging buffer and flags a
-        // non-finite value; the unpack runs only when all are finite.
-        const int mask = (pos ? 1 : 0) | (quat ? 2 : 0) | (vel ? 4 : 0) | (angVel ? 8 : 0);
-        cudaMemsetAsync(ioFlag, 0, sizeof(int), stream);
-        launchHostGather(pos, quat, vel, angVel, count, mask, ioDev, ioFlag, stream);
-        launchUnpackState(d, g0, count, ioDev, mask, ioFlag, stream);
-        int *flagHost = reinterpret_cast<int *>(ioHost);
-        cudaMemcpyAsync(flagHost, ioFlag, sizeof(int), cudaMemcpyDeviceToHost, stream);
-        if (cudaStreamSynchronize(stream) != cudaSuccess)
-            return cudaCheck("setState");
-        if (*flagHost)
-            return fail(AVBDG_ERR_NONFINITE, "non-finite body state");
-        return cudaCheck("setState");
-    }
     if (directIo) {
         // The fields go up as they are; the device checks them and unpacks only when all are
         // finite, so nothing changes on a rejected upload.

@@ -162,8 +162,7 @@ private:
     int ioCap = 0;
     // Body state moves straight between the caller's (pageable) arrays and the device, where the
     // device reaches host memory through the host's page tables; else through pinned staging.
-    bool directIo = false;  // the device reads host memory through the host's page tables
-    bool kernelIo = false;  // ... and our kernels move body state to and from the caller's arrays
+    bool directIo = false;
     int ensureIo(int count);
 
     int fail(int code, const std::string &msg);

@@ -65,102 +65,7 @@ __global__ void unpackStateKernel(Dev d, int first, int count, const float *in, 
         d.w[g] = mk4(ww[3 * i], ww[3 * i + 1], ww[3 * i + 2], 0.0f);
 }
 
-// Host memory the GPU reaches through the host's page tables (NVLink-C2C on Grace): the caller's
-// four field arrays are read and written by these kernels directly, with no copy-engine transfer
-// and no staging in host memory. The 13n floats are one flat index space, [pos 3n | quat 4n |
-// vel 3n | angvel 3n]; a warp moves 128 contiguous bytes of one array, and each thread keeps
-// kHostIlp accesses in flight to cover the host round trip.
-constexpr int kHostIlp = 4;
-
-// Field (0 pos, 1 quat, 2 vel, 3 angvel) of flat index k and its offset in that field's array.
-__device__ __forceinline__ int fieldOf(long long k, long long n, long long &off) {
-    const int f = k < 3 * n ? 0 : (k < 7 * n ? 1 : (k < 10 * n ? 2 : 3));
-    const long long start[4] = {0, 3 * n, 7 * n, 10 * n};
-    off = k - start[f];
-    return f;
-}
-
-// Upload: the caller's fields into the device staging buffer, flagging a non-finite position or
-// velocity (orientations are taken as given, as the host-side check does).
-__global__ void hostGatherKernel(const float *p, const float *q, const float *v, const float *w, int count, int mask,
-                                 float *dst, int *bad) {
-    const long long n = count, total = 13LL * n;
-    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-    for (long long k0 = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k0 < total;
-         k0 += stride * kHostIlp) {
-        float val[kHostIlp];
-        int fld[kHostIlp];
-#pragma unroll
-        for (int u = 0; u < kHostIlp; u++) {
-            const long long k = k0 + u * stride;
-            val[u] = 0.0f;
-            fld[u] = 0;
-            if (k < total) {
-                long long off;
-                const int f = fieldOf(k, n, off);
-                const float *src = f == 0 ? p : (f == 1 ? q : (f == 2 ? v : w));
-                if (mask & (1 << f)) {
-                    val[u] = src[off];
-                    fld[u] = 1 << f;
-                }
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kHostIlp; u++) {
-            const long long k = k0 + u * stride;
-            if (fld[u]) {
-                dst[k] = val[u];
-                if (fld[u] != 2 && !isfinite(val[u]))
-                    *bad = 1;
-            }
-        }
-    }
-}
-
-// Download: the packed state into the caller's field arrays (a null pointer skips its field).
-__global__ void hostScatterKernel(const float *src, int count, float *p, float *q, float *v, float *w) {
-    const long long n = count, total = 13LL * n;
-    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-    for (long long k0 = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k0 < total;
-         k0 += stride * kHostIlp) {
-        float val[kHostIlp];
-#pragma unroll
-        for (int u = 0; u < kHostIlp; u++) {
-            const long long k = k0 + u * stride;
-            val[u] = k < total ? src[k] : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < kHostIlp; u++) {
-            const long long k = k0 + u * stride;
-            if (k < total) {
-                long long off;
-                const int f = fieldOf(k, n, off);
-                float *dst = f == 0 ? p : (f == 1 ? q : (f == 2 ? v : w));
-                if (dst)
-                    dst[off] = val[u];
-            }
-        }
-    }
-}
-
 } // namespace
-
-static int hostIoGrid(int count) {
-    const long long threads = 13LL * (count > 0 ? count : 1);
-    const long long blocks = (threads + 256LL * kHostIlp - 1) / (256LL * kHostIlp);
-    return static_cast<int>(blocks < 1216 ? blocks : 1216); // 8 blocks an SM at most
-}
-
-void launchHostGather(const float *p, const float *q, const float *v, const float *w, int count, int mask, float *dst,
-                      int *bad, cudaStream_t s) {
-    ++launchCount();
-    hostGatherKernel<<<hostIoGrid(count), 256, 0, s>>>(p, q, v, w, count, mask, dst, bad);
-}
-
-void launchHostScatter(const float *src, int count, float *p, float *q, float *v, float *w, cudaStream_t s) {
-    ++launchCount();
-    hostScatterKernel<<<hostIoGrid(count), 256, 0, s>>>(src, count, p, q, v, w);
-}
 
 void launchPackState(const Dev &d, int first, int count, float *out, cudaStream_t s) {
     ++launchCount();

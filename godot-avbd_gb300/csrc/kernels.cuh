@@ -86,12 +86,6 @@ bool traverseBlockFits(int block);
 // ---- host state exchange (k_io.cu) ----
 // Layout of `buf`: [pos 3n | quat 4n | vel 3n | angvel 3n] for bodies [first, first + n).
 void launchPackState(const Dev &d, int first, int count, float *buf, cudaStream_t s);
-// Between the caller's host arrays (reached through the host's page tables) and `buf`: the fields
-// in `mask` (1 pos, 2 quat, 4 vel, 8 angvel) up, with *bad set on a non-finite position or
-// velocity; or all non-null fields down.
-void launchHostGather(const float *p, const float *q, const float *v, const float *w, int count, int mask, float *buf,
-                      int *bad, cudaStream_t s);
-void launchHostScatter(const float *buf, int count, float *p, float *q, float *v, float *w, cudaStream_t s);
 // `bad` (may be null): a device flag; when set, the unpack writes nothing.
 void launchUnpackState(const Dev &d, int first, int count, const float *buf, int mask, const int *bad, cudaStream_t s);
 void launchCheckState(int count, const float *buf, int mask, int *bad, cudaStream_t s);

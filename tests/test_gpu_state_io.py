@@ -1,9 +1,8 @@
-"""Body state exchange through the C ABI on its three transfer paths: kernels that read and write the
-caller's arrays directly (hosts whose GPU reaches host memory through the host's page tables, the
-default there), copy-engine transfers between the caller's arrays and the device
-(`AVBDG_COPY_IO=1`), and pinned staging (`AVBDG_STAGED_IO=1`, every other host). Either way a state
-written back is stepped exactly like the oracle's, and an upload holding a non-finite position or
-velocity is refused with nothing changed (`Rigid` public fields, src/avbd/types.hpp:79-88)."""
+"""Body state exchange through the C ABI on both transfer paths: straight between the caller's
+arrays and the device (hosts whose GPU reads host memory through the host's page tables) and
+through pinned staging (`AVBDG_STAGED_IO=1`, every other host). Either way a state written back
+is stepped exactly like the oracle's, and an upload holding a non-finite position or velocity is
+refused with nothing changed (`Rigid` public fields, src/avbd/types.hpp:79-88)."""
 
 import numpy as np
 import pytest
@@ -11,14 +10,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=["kernel", "copy", "staged"])
+@pytest.fixture(params=["direct", "staged"])
 def io_path(request, monkeypatch):
-    monkeypatch.delenv("AVBDG_STAGED_IO", raising=False)
-    monkeypatch.delenv("AVBDG_COPY_IO", raising=False)
     if request.param == "staged":
         monkeypatch.setenv("AVBDG_STAGED_IO", "1")
-    elif request.param == "copy":
-        monkeypatch.setenv("AVBDG_COPY_IO", "1")
+    else:
+        monkeypatch.delenv("AVBDG_STAGED_IO", raising=False)
     return request.param
 
 
