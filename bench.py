@@ -612,6 +612,7 @@ def serve_stream(capi, lib, params, reqs, packed, rate, seed, budget):
     arrivals -= arrivals[0]
     n, nxt, finished, peak_resident = len(reqs), 0, 0, 0
     arriving = None  # (seconds, body-steps) when the last request arrived
+    trace = []  # after each tick: (seconds, body-steps so far, requests in flight)
     t0 = time.perf_counter()
     while finished < n:
         now = time.perf_counter() - t0
@@ -627,10 +628,22 @@ def serve_stream(capi, lib, params, reqs, packed, rate, seed, budget):
         finished += srv.tick()
         srv.results()
         peak_resident = max(peak_resident, nxt - finished)
+        trace.append((time.perf_counter() - t0, srv.stats().body_steps, nxt - finished))
     wall = time.perf_counter() - t0
     st = srv.stats()
+    # Steady state: the ticks during which at least 80 % of the peak number of requests were in
+    # flight (the ramp while requests arrive and the drain at the end are left out).
+    steady_steps = steady_s = 0.0
+    prev_t, prev_b = 0.0, 0.0
+    for t, b, flight in trace:
+        if flight >= 0.8 * peak_resident:
+            steady_steps += b - prev_b
+            steady_s += t - prev_t
+        prev_t, prev_b = t, b
     out = {"rate_per_s": rate, "requests": n, "body_steps_per_s": st.body_steps / wall, "wall_s": wall,
            "body_steps_per_s_while_arriving": arriving[1] / arriving[0] if arriving and arriving[0] > 0 else None,
+           "body_steps_per_s_steady": steady_steps / steady_s if steady_s > 0 else None,
+           "steady_share_of_wall": steady_s / wall if wall > 0 else None,
            "ticks": st.ticks, "tick_p50_ms": st.tick_p50_ms, "tick_p99_ms": st.tick_p99_ms,
            "tick_max_ms": st.tick_max_ms, "request_p50_ms": st.request_p50_ms, "request_p99_ms": st.request_p99_ms,
            "peak_in_flight": peak_resident, "busy_s": st.busy_ms / 1e3,
@@ -683,6 +696,7 @@ def run_serve(args, rank, world_size, standalone=True):
     plain = plain_stream_sample(pkg, reqs, args.plain_sample, 3, args.plain_steps)
     total_work = sum(r.dynamic * r.steps for r in reqs)
     served = {"value": best["body_steps_per_s"], "unit": UNIT, "rate_per_s": best["rate_per_s"],
+              "steady_value": best["body_steps_per_s_steady"], "steady_share_of_wall": best["steady_share_of_wall"],
               "tick_p50_ms": best["tick_p50_ms"], "tick_p99_ms": best["tick_p99_ms"],
               "request_p50_ms": best["request_p50_ms"], "request_p99_ms": best["request_p99_ms"],
               "served_over_plain": best["body_steps_per_s"] / plain["value"], "plain_per_scene": plain,
