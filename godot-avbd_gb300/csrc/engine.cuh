@@ -25,7 +25,7 @@ constexpr int kMaxColours = 8;
 constexpr uint8_t kOverflowColour = 8;
 constexpr uint8_t kUncoloured = 255;
 constexpr int kStampF4 = 7; // float4 per (manifold, side) stamp
-constexpr int kPairStash = 16; // partners kept per body by the counting walk
+constexpr int kPairStash = 64; // partners kept per body by the counting walk
 constexpr int kExtF4 = 16;  // float4 per force of the generic-joint record (forces.cuh)
 // Spins (64 ns sleeps) a dataflow wait of the colouring or the brake sweep makes before it gives
 // up and reports a timeout: ~0.3 s, far beyond any real dependency hop.
