@@ -330,7 +330,7 @@ def run_gpu(args, rank, world_size):
     peak, peak_kind = measured_peak_hbm()
     bytes_per_launch, counts = manifold_pass_bytes(w, dyn_mask, 10)
     launch_ms = kt.manifold_ms / max(kt.manifold_launches, 1)
-    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
     traffic = traffic_per_launch(args.workload, bytes_per_launch)
     roofline = {"bound": "hbm", "kernel": "dualKernel (manifold dual + block stamps)", "achieved": achieved,
                 "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -495,7 +495,7 @@ def run_batch(args, rank, world_size):
     iters = 10
     bytes_per_launch = 188 * st.manifolds + 112 * st.contacts + 112 * st.manifold_sides * (iters - 1) / iters
     launch_ms = kt.manifold_ms / max(kt.manifold_launches, 1)
-    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
     traffic = traffic_per_launch("batch", bytes_per_launch)
     roofline = {"bound": "hbm", "kernel": "dualKernel (manifold dual + block stamps)", "achieved": achieved,
                 "peak": peak, "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

@@ -85,6 +85,12 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.wColour, ww);
     take(n.wSleep, 2 * static_cast<size_t>(ww));
     take(n.gridBar, 2);
+    take(n.wManStart, static_cast<size_t>(ww) + 1);
+    take(n.wManFill, ww);
+    take(n.qPre, 2 * (static_cast<size_t>(ww) + 1));
+    take(n.qStage, ww);
+    take(n.qDone, ww);
+    take(n.qTicket, 1);
     take(n.x, nb);
     take(n.q, nb);
     take(n.x0, nb);
@@ -147,6 +153,7 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
         take(b->armFlag, am);
     }
     take(n.stampSlot, mm);
+    take(n.wManList, mm);
     take(n.mSpec, mm);
     take(n.mDone, mm);
     take(n.specList, mm);
@@ -205,6 +212,8 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     const char *noGraphs = std::getenv("AVBDG_NO_GRAPHS");
     useGraphs = !(noGraphs && noGraphs[0] == '1');
     d.waitLimit = waitLimit;
+    const char *queue = std::getenv("AVBDG_QUEUE");
+    roundQueue = queue && queue[0] == '1';
     const char *noTune = std::getenv("AVBDG_NO_TUNE");
     tuneEnabled = !(noTune && noTune[0] == '1');
 #ifdef AVBDG_FP64
@@ -1066,6 +1075,21 @@ void Engine::runSubstep(const StepParams &sp, int rounds, bool idle) {
     // threshold > 0, so a positive threshold always stops the substep after its first round.
     const int run = (P.convergence_threshold > 0.0f && rounds > 1) ? 1 : rounds;
     launchStamps(d, sp, false, stream);
+    if (roundQueue && !colours && nForces == 0 && run <= kMaxQueueRounds) {
+        QueueRounds qr{};
+        qr.rounds = run;
+        for (int it = 0; it < run; it++) {
+            const bool newton = it < newtonRounds;
+            if (newton)
+                qr.newtonMask |= 1u << it;
+            if (it + 1 < newtonRounds)
+                qr.stampMask |= 1u << it;
+            qr.decay[it] = newton ? 1.0f : P.stiffness_decay;
+        }
+        launchRoundQueue(d, sp, qr, stream);
+        launchFinishBodies(d, sp, idle, stream);
+        return;
+    }
     for (int it = 0; it < run; it++) {
         if (!launchesOk())
             return; // enqueueStep reports it
@@ -1118,6 +1142,8 @@ int Engine::finishStep() {
             return fail(AVBDG_ERR_TIMEOUT, "colouring: a bounded wait for an earlier neighbour gave up");
         if (e & kErrBarrierTimeout)
             return fail(AVBDG_ERR_TIMEOUT, "colour sweep: a bounded grid barrier gave up");
+        if (e & kErrQueueTimeout)
+            return fail(AVBDG_ERR_TIMEOUT, "round queue: a tile's bounded wait for its world gave up");
         return fail(AVBDG_ERR_CAPACITY, "a device buffer overflowed this step (state is not trustworthy)");
     }
     // Keep headroom for the next step's pairs and manifolds.

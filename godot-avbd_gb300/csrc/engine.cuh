@@ -54,6 +54,8 @@ enum Counter {
     C_ONE,            // constant 1 (scan length helper)
     C_SOLVEFAIL,      // overflow bodies whose plain LDLT failed this round (solveFail)
     C_PAIRSPILL,      // bodies with more broad-phase partners than the stash holds (pairSpill)
+    C_QSOLVE,         // round-loop queue: solve tiles a round (all worlds)
+    C_QDUAL,          // round-loop queue: dual tiles a round (all worlds)
     C_TMP,
     C_COUNT
 };
@@ -64,6 +66,7 @@ constexpr int kErrAdjacency = 4;
 constexpr int kErrBrakeTimeout = 8;
 constexpr int kErrColourTimeout = 16;
 constexpr int kErrBarrierTimeout = 32; // a grid barrier of a cooperative sweep gave up
+constexpr int kErrQueueTimeout = 64;   // a tile of the round-loop queue waited too long for its world
 
 // Solver fields a kernel reads (src/avbd/solver.h:54-144), with derived terms.
 struct StepParams {
@@ -100,6 +103,12 @@ struct Dev {
     int ARM;                // 1: the arm-cache arrays of ManifoldBuf are allocated
     long long waitLimit;    // spins a dataflow wait makes before it reports a timeout
     unsigned *gridBar;      // grid barrier of the cooperative sweeps: arrivals, generation
+    // Round-loop tile queue (k_queue.cu): each world's live manifolds grouped together (wManStart,
+    // wManList), the prefix sums of the worlds' solve and dual chunk counts (qPre: WW + 1 each), and
+    // per world the phases completed (qStage) and the chunks of the current phase done (qDone).
+    int *wManStart, *wManFill, *wManList;
+    int *qPre, *qStage, *qDone;
+    unsigned *qTicket;
     // worlds
     int *wBase, *wCount;    // body range
     int *wMaxDepth;         // projection: max depth bits per world (positive floats)

@@ -162,6 +162,7 @@ private:
     int ioCap = 0;
     // Body state moves straight between the caller's (pageable) arrays and the device, where the
     // device reaches host memory through the host's page tables; else through pinned staging.
+    bool roundQueue = false; // AVBDG_QUEUE=1: the round loop as one tile-queue launch where it applies
     bool directIo = false;
     int ensureIo(int count);
 

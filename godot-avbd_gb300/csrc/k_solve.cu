@@ -24,6 +24,9 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kSolveThreads = 128;
+constexpr int kQueueThreads = 128; // items per round-queue tile
+
+__device__ __forceinline__ int divUpDev(int a, int b) { return (a + b - 1) / b; }
 
 struct Blk {
     m3 lin, ang, crs;
@@ -372,6 +375,16 @@ __device__ __forceinline__ void addStamp(Blk &b, const StampRec &r) {
     b.ra = add(b.ra, f3{s3.w, s4.x, s4.y});
 }
 
+// The same record through ordinary (coherent) loads, for a kernel that also writes the stamps.
+__device__ __forceinline__ StampRec loadStampCoherent(const real4 *src) {
+    return StampRec{src[0], src[1], src[2], src[3], src[4], src[5], src[6]};
+}
+
+template <bool RO = true>
+__device__ __forceinline__ StampRec loadStampAs(const real4 *src) {
+    return RO ? loadStamp(src) : loadStampCoherent(src);
+}
+
 __device__ __forceinline__ void addStamp(Blk &b, const real4 *src) { addStamp(b, loadStamp(src)); }
 
 struct Pose {
@@ -498,110 +511,118 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
 // stamps (the reference's phase-A recompute of each force, manifold.cpp:655-659, from the same
 // floats). One thread per manifold, grid-stride over the live ones.
 // ARM: the arm cache is on (compiled out otherwise, so the common path keeps its code).
+// One manifold's dual pass (and, with STAMPS, its next-round stamps): the body of dualKernel's loop,
+// also run by the tile queue of the round loop.
+// RO: poses are read-only for the whole launch (read-only cache path); false inside the round-loop
+// tile queue, which writes them in the same launch.
+template <bool STAMPS, bool ARM, bool RO = true>
+__device__ __forceinline__ void dualAt(const Dev &d, const StepParams &p, real decay, int m) {
+    const ManifoldBuf L = d.live;
+    const int2 ab = __ldg(&L.ab[m]);
+    if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
+        return; // frozen (manifold.cpp:168-172)
+    bool touches = false;
+    int sides = STAMPS ? overflowSides(d, ab, touches) : 0;
+    if (touches)
+        sides = 0; // recomputed after the colour passes
+    const Pose A = RO ? loadPoseRO(d, ab.x) : loadPose(d, ab.x), B = RO ? loadPoseRO(d, ab.y) : loadPose(d, ab.y);
+    const real4 b04 = __ldg(&L.b0[m]);
+    const f3 r0 = xyz(b04), r1 = xyz(__ldg(&L.b1[m])), r2 = xyz(__ldg(&L.b2[m]));
+    const real mu = b04.w;
+    const int n = __ldg(&L.count[m]);
+    // Drift-gated arm reuse (manifold.cpp:600-608): under the rotation threshold the cached
+    // world arms stand in for the current ones.
+    bool driftUsable = false;
+    if (ARM) {
+        const f3 dA = sub(A.rot.c0, xyz(L.capA[m])), dB = sub(B.rot.c0, xyz(L.capB[m]));
+        driftUsable = L.armFlag[m] != 0 && length2(dA) <= p.armRebuild2 && length2(dB) <= p.armRebuild2;
+    }
+    SharedAcc sh;
+    sh.lin = mzero();
+    sh.rhsLin = f3{0, 0, 0};
+    SideAcc sa, sb;
+    zeroAcc(sa);
+    zeroAcc(sb);
+    for (int c = 0; c < n; c++) {
+        const int ci = cslot(d, m, c);
+        const real4 rA4 = __ldg(&L.rA[ci]);
+        f3 rAw, rBw;
+        if (driftUsable) {
+            rAw = xyz(L.armA[ci]);
+            rBw = xyz(L.armB[ci]);
+        } else {
+            rAw = mul(A.rot, xyz(rA4));
+            rBw = mul(B.rot, xyz(__ldg(&L.rB[ci])));
+            if (ARM) {
+                L.armA[ci] = f4(rAw, 0.0f);
+                L.armB[ci] = f4(rBw, 0.0f);
+            }
+        }
+        const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+        const f3 C = contactError(p, xyz(__ldg(&L.C0[ci])), bracket, r0, r1, r2);
+        f3 k = xyz(L.k[ci]);
+        if (decay < 1.0f)
+            k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
+        const real4 lam4 = L.lam[ci];
+        real stick = lam4.w;
+        f3 F = add(cmul(k, C), xyz(lam4));
+        const Cone cone = clampForce(F, mu);
+        const f3 lam = F;
+        const real beta = p.betaLin * rA4.w;
+        if (F.x < 0)
+            k.x = smin(k.x + beta * mabs(C.x), PENALTY_MAX);
+        if (cone.scale <= cone.bounds) {
+            k.y = smin(k.y + beta * mabs(C.y), PENALTY_MAX);
+            k.z = smin(k.z + beta * mabs(C.z), PENALTY_MAX);
+            stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
+        }
+        L.k[ci] = f4(k, 0.0f);
+        L.lam[ci] = f4(lam, stick);
+        if (STAMPS && sides) {
+            // These are the next round's overflow phase A (solver_step.cpp:236-248): it always
+            // precomputes with fresh arms at this pose and stores them, whatever the dual used.
+            f3 rAs = rAw, rBs = rBw, Cs = C;
+            if (ARM) {
+                if (driftUsable) {
+                    rAs = mul(A.rot, xyz(rA4));
+                    rBs = mul(B.rot, xyz(L.rB[ci]));
+                    const f3 bracketF = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAs)), cross(B.dAng, rBs));
+                    Cs = contactError(p, xyz(L.C0[ci]), bracketF, r0, r1, r2);
+                }
+                L.armA[ci] = f4(rAs, 0.0f);
+                L.armB[ci] = f4(rBs, 0.0f);
+            }
+            f3 Fn = add(cmul(k, Cs), lam);
+            clampForce(Fn, mu);
+            real S[6];
+            basisHessianD(r0, r1, r2, k, S);
+            const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
+            stampShared(S, fw, sh);
+            if (sides & kSideA)
+                stampContact(S, rAs, fw, sa);
+            if (sides & kSideB)
+                stampContact(S, rBs, fw, sb);
+        }
+    }
+    if (sides) {
+        const int2 slot = d.stampSlot[m];
+        if (sides & kSideA)
+            storeStamp(d.stamps + static_cast<size_t>(slot.x) * kStampF4, sh, sa, 1.0f);
+        if (sides & kSideB)
+            storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
+    }
+    if (ARM && !driftUsable) { // capture (manifold.cpp:662-667)
+        L.capA[m] = f4(A.rot.c0, 0.0f);
+        L.capB[m] = f4(B.rot.c0, 0.0f);
+        L.armFlag[m] = 1;
+    }
+}
+
 template <bool STAMPS, bool ARM>
 __global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, real decay) { // 512: largest tuned block
     const int live = d.ctr[C_LIVE];
-    const ManifoldBuf L = d.live;
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x) {
-        const int2 ab = __ldg(&L.ab[m]);
-        if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
-            continue; // frozen (manifold.cpp:168-172)
-        bool touches = false;
-        int sides = STAMPS ? overflowSides(d, ab, touches) : 0;
-        if (touches)
-            sides = 0; // recomputed after the colour passes
-        const Pose A = loadPoseRO(d, ab.x), B = loadPoseRO(d, ab.y);
-        const real4 b04 = __ldg(&L.b0[m]);
-        const f3 r0 = xyz(b04), r1 = xyz(__ldg(&L.b1[m])), r2 = xyz(__ldg(&L.b2[m]));
-        const real mu = b04.w;
-        const int n = __ldg(&L.count[m]);
-        // Drift-gated arm reuse (manifold.cpp:600-608): under the rotation threshold the cached
-        // world arms stand in for the current ones.
-        bool driftUsable = false;
-        if (ARM) {
-            const f3 dA = sub(A.rot.c0, xyz(L.capA[m])), dB = sub(B.rot.c0, xyz(L.capB[m]));
-            driftUsable = L.armFlag[m] != 0 && length2(dA) <= p.armRebuild2 && length2(dB) <= p.armRebuild2;
-        }
-        SharedAcc sh;
-        sh.lin = mzero();
-        sh.rhsLin = f3{0, 0, 0};
-        SideAcc sa, sb;
-        zeroAcc(sa);
-        zeroAcc(sb);
-        for (int c = 0; c < n; c++) {
-            const int ci = cslot(d, m, c);
-            const real4 rA4 = __ldg(&L.rA[ci]);
-            f3 rAw, rBw;
-            if (driftUsable) {
-                rAw = xyz(L.armA[ci]);
-                rBw = xyz(L.armB[ci]);
-            } else {
-                rAw = mul(A.rot, xyz(rA4));
-                rBw = mul(B.rot, xyz(__ldg(&L.rB[ci])));
-                if (ARM) {
-                    L.armA[ci] = f4(rAw, 0.0f);
-                    L.armB[ci] = f4(rBw, 0.0f);
-                }
-            }
-            const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
-            const f3 C = contactError(p, xyz(__ldg(&L.C0[ci])), bracket, r0, r1, r2);
-            f3 k = xyz(L.k[ci]);
-            if (decay < 1.0f)
-                k = lclampv(scale(k, decay), PENALTY_MIN, PENALTY_MAX);
-            const real4 lam4 = L.lam[ci];
-            real stick = lam4.w;
-            f3 F = add(cmul(k, C), xyz(lam4));
-            const Cone cone = clampForce(F, mu);
-            const f3 lam = F;
-            const real beta = p.betaLin * rA4.w;
-            if (F.x < 0)
-                k.x = smin(k.x + beta * mabs(C.x), PENALTY_MAX);
-            if (cone.scale <= cone.bounds) {
-                k.y = smin(k.y + beta * mabs(C.y), PENALTY_MAX);
-                k.z = smin(k.z + beta * mabs(C.z), PENALTY_MAX);
-                stick = length2d(C.y, C.z) < STICK_THRESH ? 1.0f : 0.0f;
-            }
-            L.k[ci] = f4(k, 0.0f);
-            L.lam[ci] = f4(lam, stick);
-            if (STAMPS && sides) {
-                // These are the next round's overflow phase A (solver_step.cpp:236-248): it always
-                // precomputes with fresh arms at this pose and stores them, whatever the dual used.
-                f3 rAs = rAw, rBs = rBw, Cs = C;
-                if (ARM) {
-                    if (driftUsable) {
-                        rAs = mul(A.rot, xyz(rA4));
-                        rBs = mul(B.rot, xyz(L.rB[ci]));
-                        const f3 bracketF = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAs)), cross(B.dAng, rBs));
-                        Cs = contactError(p, xyz(L.C0[ci]), bracketF, r0, r1, r2);
-                    }
-                    L.armA[ci] = f4(rAs, 0.0f);
-                    L.armB[ci] = f4(rBs, 0.0f);
-                }
-                f3 Fn = add(cmul(k, Cs), lam);
-                clampForce(Fn, mu);
-                real S[6];
-                basisHessianD(r0, r1, r2, k, S);
-                const f3 fw = add(add(scale(r0, Fn.x), scale(r1, Fn.y)), scale(r2, Fn.z));
-                stampShared(S, fw, sh);
-                if (sides & kSideA)
-                    stampContact(S, rAs, fw, sa);
-                if (sides & kSideB)
-                    stampContact(S, rBs, fw, sb);
-            }
-        }
-        if (sides) {
-            const int2 slot = d.stampSlot[m];
-            if (sides & kSideA)
-                storeStamp(d.stamps + static_cast<size_t>(slot.x) * kStampF4, sh, sa, 1.0f);
-            if (sides & kSideB)
-                storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
-        }
-        if (ARM && !driftUsable) { // capture (manifold.cpp:662-667)
-            L.capA[m] = f4(A.rot.c0, 0.0f);
-            L.capB[m] = f4(B.rot.c0, 0.0f);
-            L.armFlag[m] = 1;
-        }
-    }
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x)
+        dualAt<STAMPS, ARM>(d, p, decay, m);
 }
 
 // ---- joints (joint.cpp:80-230) ----
@@ -748,7 +769,9 @@ __device__ __forceinline__ int nForcesDev(const Dev &d) { return d.ctr[C_FORCES]
 // first) consumes that dual's cache, so it uses the cached world arms; the other touches precompute
 // with fresh arms and store them. The first touch is the body whose partner has not been solved
 // this round (not coloured, or coloured later).
-template <bool RECOMPUTE, bool FORCES = true>
+// RO: the stamps are read-only for the whole launch (read-only cache path); false inside the
+// round-loop tile queue, which writes them in the same launch.
+template <bool RECOMPUTE, bool FORCES = true, bool RO = true>
 __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk, int armsFromDual = 0) {
     const int nf = nForcesDev(d);
     const int e1 = d.adjStart[g + 1];
@@ -757,13 +780,13 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
         // are loaded before either is added (the sums keep the entry order).
         int e = d.adjStart[g];
         for (; e + 1 < e1; e += 2) {
-            const StampRec r0 = loadStamp(d.stamps + static_cast<size_t>(e) * kStampF4);
-            const StampRec r1 = loadStamp(d.stamps + static_cast<size_t>(e + 1) * kStampF4);
+            const StampRec r0 = loadStampAs<RO>(d.stamps + static_cast<size_t>(e) * kStampF4);
+            const StampRec r1 = loadStampAs<RO>(d.stamps + static_cast<size_t>(e + 1) * kStampF4);
             addStamp(blk, r0);
             addStamp(blk, r1);
         }
         if (e < e1)
-            addStamp(blk, d.stamps + static_cast<size_t>(e) * kStampF4);
+            addStamp(blk, loadStampAs<RO>(d.stamps + static_cast<size_t>(e) * kStampF4));
         return;
     }
     for (int e = d.adjStart[g]; e < e1; e++) {
@@ -825,7 +848,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
             blk.rl = add(blk.rl, scale(sh.rhsLin, sgn));
             blk.ra = add(blk.ra, scale(sd.rhsAng, sgn));
         } else {
-            addStamp(blk, d.stamps + static_cast<size_t>(e) * kStampF4);
+            addStamp(blk, loadStampAs<RO>(d.stamps + static_cast<size_t>(e) * kStampF4));
         }
     }
 }
@@ -892,27 +915,161 @@ __device__ __noinline__ void fallbackSolve(const Dev &d, const StepParams &p, in
     applyOverflow(d, p, g, inPlace, r.ok ? r.dl : f3{0, 0, 0}, r.ok ? r.da : f3{0, 0, 0});
 }
 
-// Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
-template <bool FORCES>
-#ifdef AVBDG_FP64
-#define AVBDG_SOLVE_BOUNDS __launch_bounds__(kSolveThreads)
-#else
-#define AVBDG_SOLVE_BOUNDS __launch_bounds__(kSolveThreads, 8) // 64 registers: 8 blocks an SM
-#endif
-__global__ void AVBDG_SOLVE_BOUNDS
-        overflowSolveKernel(const __grid_constant__ Dev d, const __grid_constant__ StepParams p, int inPlace) {
-    const int n = d.ctr[C_BODIES];
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
+// One overflow body's block-Jacobi solve (the body of overflowSolveKernel), also run by the
+// round-loop tile queue (RO false there: the stamps are written in the same launch).
+template <bool FORCES, bool RO = true>
+__device__ __forceinline__ void solveAt(const Dev &d, const StepParams &p, int g, int inPlace) {
+    if (d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
         return;
     Blk blk = bodyBlock(d, p, g);
-    assemble<false, FORCES>(d, p, g, blk);
+    assemble<false, FORCES, RO>(d, p, g, blk);
     f3 dl, da;
     if (!solveBlockFast(blk, dl, da)) {
         fallbackSolve<FORCES>(d, p, g, inPlace);
         return;
     }
     applyOverflow(d, p, g, inPlace, dl, da);
+}
+
+#ifdef AVBDG_FP64
+#define AVBDG_SOLVE_BOUNDS __launch_bounds__(kSolveThreads)
+#else
+#define AVBDG_SOLVE_BOUNDS __launch_bounds__(kSolveThreads, 8) // 64 registers: 8 blocks an SM
+#endif
+// Overflow bodies are walked in slot order (coalesced body loads); the overflow colour has no list.
+template <bool FORCES>
+__global__ void AVBDG_SOLVE_BOUNDS
+        overflowSolveKernel(const __grid_constant__ Dev d, const __grid_constant__ StepParams p, int inPlace) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < d.ctr[C_BODIES])
+        solveAt<FORCES>(d, p, g, inPlace);
+}
+
+// ---- the round loop as one persistent launch over a tile queue ----
+//
+// In a store without forces or coloured bodies, round r's body solve in world w needs only the
+// stamps round r-1's dual wrote for w, and round r's dual needs only that round's solves in w;
+// worlds never read each other. One launch runs all the rounds: tiles (round, phase, world, chunk)
+// are handed out in that order by one counter, a tile waits (bounded by waitLimit) until its world
+// has completed the previous phase, runs one item per thread and counts itself done; the last
+// chunk of a phase advances the world's stage. Every tile a tile waits for was handed out earlier
+// to a block that is running (cooperative launch), so the waits end. Worlds move through their
+// rounds independently instead of every world waiting at each kernel boundary. The per-item work
+// is the separate kernels' (solveAt, dualAt, with coherent loads), so the results are the same.
+__device__ __forceinline__ int worldOfTile(const int *pre, int nWorlds, int t) {
+    int lo = 0, hi = nWorlds - 1; // the largest w with pre[w] <= t (every world has a chunk)
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool ARM>
+__global__ void __launch_bounds__(kQueueThreads, 4) roundQueueKernel(Dev d, StepParams p, QueueRounds qr) {
+    __shared__ int sTile, sOk;
+    const int nWorlds = d.ctr[C_WORLDS];
+    const int ts = d.ctr[C_QSOLVE], td = d.ctr[C_QDUAL];
+    const int perRound = ts + td;
+    const int total = qr.rounds * perRound;
+    const int *sPre = d.qPre, *dPre = d.qPre + (d.WW + 1);
+    volatile int *errors = d.ctr + C_ERRORS;
+    for (;;) {
+        if (threadIdx.x == 0)
+            sTile = static_cast<int>(atomicAdd(d.qTicket, 1u));
+        __syncthreads();
+        const int t = sTile;
+        __syncthreads();
+        if (t >= total)
+            return;
+        const int r = t / perRound;
+        int u = t - r * perRound;
+        const bool solve = u < ts;
+        if (!solve)
+            u -= ts;
+        const int *pre = solve ? sPre : dPre;
+        const int w = worldOfTile(pre, nWorlds, u);
+        const int chunk = u - pre[w];
+        const int q = 2 * r + (solve ? 0 : 1); // phases of world w completed before this tile may run
+        if (threadIdx.x == 0) {
+            sOk = 1;
+            long long spins = 0;
+            while (static_cast<int>(ldAcquireU32(reinterpret_cast<const unsigned *>(d.qStage + w))) < q) {
+                if (++spins > d.waitLimit || (*errors & kErrQueueTimeout)) {
+                    atomicOr(d.ctr + C_ERRORS, kErrQueueTimeout);
+                    sOk = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (!sOk)
+            return;
+        if (solve) {
+            const int g = d.wBase[w] + chunk * kQueueThreads + threadIdx.x;
+            if (((qr.newtonMask >> r) & 1u) && g < d.wBase[w] + d.wCount[w])
+                solveAt<false, false>(d, p, g, 1);
+        } else {
+            const int k = d.wManStart[w] + chunk * kQueueThreads + threadIdx.x;
+            if (k < d.wManStart[w + 1]) {
+                const int m = d.wManList[k];
+                if ((qr.stampMask >> r) & 1u)
+                    dualAt<true, ARM, false>(d, p, qr.decay[r], m);
+                else
+                    dualAt<false, ARM, false>(d, p, qr.decay[r], m);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence(); // the tile's writes before its count
+            if (atomicAdd(d.qDone + w, 1) + 1 == pre[w + 1] - pre[w]) {
+                d.qDone[w] = 0;
+                __threadfence();
+                stReleaseU32(reinterpret_cast<unsigned *>(d.qStage + w), static_cast<unsigned>(q + 1));
+            }
+        }
+    }
+}
+
+// Each live manifold into its world's group (the order inside a group does not matter: every
+// manifold's dual reads and writes only its own state and its bodies' stamp entries).
+__global__ void worldManCountKernel(Dev d) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        atomicAdd(&d.wManStart[d.meta[d.live.ab[m].x].x], 1);
+}
+
+__global__ void worldManFillKernel(Dev d) {
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        const int w = d.meta[d.live.ab[m].x].x;
+        d.wManList[d.wManStart[w] + atomicAdd(&d.wManFill[w], 1)] = m;
+    }
+}
+
+// Chunks of each world's solve and dual phases (at least one each, so every phase of every world
+// has a tile that advances its stage), zero past the last world; the stages start at zero.
+__global__ void queueChunksKernel(Dev d) {
+    const int nWorlds = d.ctr[C_WORLDS];
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w > d.WW)
+        return;
+    int cs = 0, cd = 0;
+    if (w < nWorlds) {
+        cs = divUpDev(d.wCount[w], kQueueThreads);
+        cd = divUpDev(d.wManStart[w + 1] - d.wManStart[w], kQueueThreads);
+        cs = cs > 0 ? cs : 1;
+        cd = cd > 0 ? cd : 1;
+        d.qStage[w] = 0;
+        d.qDone[w] = 0;
+    }
+    d.qPre[w] = cs;
+    d.qPre[d.WW + 1 + w] = cd;
 }
 
 __global__ void overflowApplyKernel(Dev d, StepParams p) {
@@ -1137,6 +1294,7 @@ __global__ void colourListKernel(Dev d, int contactOnlyOverflow) {
 } // namespace
 
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
+static int queueGridMax();
 
 void launchContactOnly(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.wColour, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
@@ -1183,6 +1341,7 @@ static int sweepGridMax() {
 
 void prepareKernels() {
     sweepGridMax();
+    queueGridMax();
     projectionGridBlocks();
     preparePrimitives();
     prepareNarrowPhase();
@@ -1238,6 +1397,42 @@ void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool f
         overflowSolveKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
     else
         overflowSolveKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
+}
+
+static int g_queueBlocks = 0;
+
+static int queueGridMax() {
+    if (g_queueBlocks == 0) {
+        int dev = 0, sms = 0, perSm = 0, perSmArm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, roundQueueKernel<false>, kQueueThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmArm, roundQueueKernel<true>, kQueueThreads, 0);
+        perSm = perSm < perSmArm ? perSm : perSmArm;
+        g_queueBlocks = sms * (perSm < 1 ? 1 : perSm);
+    }
+    return g_queueBlocks;
+}
+
+void launchRoundQueue(const Dev &d, const StepParams &p, const QueueRounds &qr, cudaStream_t s) {
+    const int cap = static_cast<int>(static_cast<size_t>(d.WW) + 1);
+    cudaMemsetAsync(d.wManStart, 0, sizeof(int) * static_cast<size_t>(cap), s);
+    cudaMemsetAsync(d.wManFill, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
+    ++launchCount(); worldManCountKernel<<<residentGrid(worldManCountKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d);
+    scanExclusive(d.wManStart, d.wManStart, cap, nullptr, nullptr, d.scanScratch, s);
+    ++launchCount(); worldManFillKernel<<<residentGrid(worldManFillKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d);
+    ++launchCount(); queueChunksKernel<<<divUp(cap, kThreads), kThreads, 0, s>>>(d);
+    scanExclusive(d.qPre, d.qPre, cap, nullptr, d.ctr + C_QSOLVE, d.scanScratch, s);
+    scanExclusive(d.qPre + cap, d.qPre + cap, cap, nullptr, d.ctr + C_QDUAL, d.scanScratch, s);
+    cudaMemsetAsync(d.qTicket, 0, sizeof(unsigned), s);
+    Dev dd = d;
+    StepParams pp = p;
+    QueueRounds q = qr;
+    void *args[] = {&dd, &pp, &q};
+    ++launchCount();
+    cudaLaunchCooperativeKernel(p.armCache ? reinterpret_cast<void *>(roundQueueKernel<true>)
+                                           : reinterpret_cast<void *>(roundQueueKernel<false>),
+                                dim3(queueGridMax()), dim3(kQueueThreads), args, 0, s);
 }
 
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {

@@ -53,6 +53,17 @@ void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream
 // also touch a coloured body (recomputed after the colour passes).
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s);
 // `armsFromDual`: a dual pass ran since the manifolds were (re)initialised or rebased.
+// The rounds of a substep for a store without forces or coloured bodies, as one persistent launch
+// over a (round, phase, world, chunk) tile queue; per round: Newton (solve) or not, stamps written
+// by its dual or not, and the stiffness decay of its dual.
+constexpr int kMaxQueueRounds = 32;
+struct QueueRounds {
+    int rounds;
+    unsigned newtonMask, stampMask;
+    real decay[kMaxQueueRounds];
+};
+void launchRoundQueue(const Dev &d, const StepParams &p, const QueueRounds &qr, cudaStream_t s);
+
 // One round's Gauss-Seidel colour passes, colours in order, in one cooperative launch.
 void launchColourSweep(const Dev &d, const StepParams &p, bool armsFromDual, cudaStream_t s);
 // Block-Jacobi solve of every dynamic body in the overflow colour (walked in slot order).
