@@ -907,10 +907,10 @@ __device__ __forceinline__ void applyOverflow(const Dev &d, const StepParams &p,
 // addresses without copying them. The block is assembled again (the same floats: it reads the
 // stamps and this body's own pose, which nothing changes during the pass; with forces, poses are
 // not written during the pass at all).
-template <bool FORCES>
+template <bool FORCES, bool RO = true>
 __device__ __noinline__ void fallbackSolve(const Dev &d, const StepParams &p, int g, int inPlace) {
     Blk blk = bodyBlock(d, p, g);
-    assemble<false, FORCES>(d, p, g, blk);
+    assemble<false, FORCES, RO>(d, p, g, blk);
     const Delta r = solvePivoted(blk);
     applyOverflow(d, p, g, inPlace, r.ok ? r.dl : f3{0, 0, 0}, r.ok ? r.da : f3{0, 0, 0});
 }
@@ -925,7 +925,7 @@ __device__ __forceinline__ void solveAt(const Dev &d, const StepParams &p, int g
     assemble<false, FORCES, RO>(d, p, g, blk);
     f3 dl, da;
     if (!solveBlockFast(blk, dl, da)) {
-        fallbackSolve<FORCES>(d, p, g, inPlace);
+        fallbackSolve<FORCES, RO>(d, p, g, inPlace);
         return;
     }
     applyOverflow(d, p, g, inPlace, dl, da);
