@@ -245,14 +245,7 @@ int avbdg_world_step_interleaved(avbdg_world *w, int substeps, int rounds) {
 }
 
 int avbdg_world_step_n(avbdg_world *w, int count) {
-    return guarded(w, [=](avbdg::Engine &e) {
-        for (int i = 0; i < count; i++) {
-            const int rc = e.step();
-            if (rc != AVBDG_OK)
-                return rc;
-        }
-        return AVBDG_OK;
-    });
+    return guarded(w, [=](avbdg::Engine &e) { return e.stepMany(count, 1, 0); });
 }
 
 int avbdg_world_sync(avbdg_world *w) {
@@ -359,14 +352,7 @@ int avbdg_batch_remove_worlds(avbdg_batch *b, int count, const int *worlds) {
 }
 
 int avbdg_batch_step(avbdg_batch *b, int count) {
-    return guarded(b, [=](avbdg::Engine &e) {
-        for (int i = 0; i < count; i++) {
-            const int rc = e.step();
-            if (rc != AVBDG_OK)
-                return rc;
-        }
-        return AVBDG_OK;
-    });
+    return guarded(b, [=](avbdg::Engine &e) { return e.stepMany(count, 1, 0); });
 }
 
 int avbdg_batch_sync(avbdg_batch *b) {

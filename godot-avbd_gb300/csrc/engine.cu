@@ -248,6 +248,11 @@ Engine::~Engine() {
     releaseAll();
     if (ioHost)
         cudaFreeHost(ioHost);
+    if (ctrRing)
+        cudaFreeHost(ctrRing);
+    for (cudaEvent_t e : ctrEvent)
+        if (e)
+            cudaEventDestroy(e);
     for (cudaEvent_t e : evPool)
         cudaEventDestroy(e);
     for (auto &e : ev)
@@ -287,6 +292,7 @@ void Engine::releaseAll() {
 }
 
 void Engine::allocate(int nb, int mm, int ff, int pp, int ww) {
+    ctrFresh = false;
     dropGraphs(); // they hold the old buffers' addresses
     const Dev old = d;
     std::vector<void *> oldAllocs;
@@ -449,6 +455,7 @@ int Engine::validateForces(int nb, int count, const avbdg_force_desc *descs, std
 }
 
 int Engine::addWorld() {
+    ctrFresh = false;
     if (ensureCapacity(nBodies, nForces, worlds() + 1))
         return -1;
     wBase.push_back(nBodies);
@@ -464,6 +471,7 @@ int Engine::addWorld() {
 }
 
 int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outIds) {
+    ctrFresh = false;
     if (w < 0 || w >= worlds() || count < 0 || (count > 0 && !descs))
         return fail(AVBDG_ERR_INVALID, "bad world or body array");
     if (w != worlds() - 1)
@@ -532,6 +540,7 @@ int Engine::addBodies(int w, int count, const avbdg_body_desc *descs, int *outId
 
 int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], float kLin, float kAng,
                      float fracture) {
+    ctrFresh = false;
     if (w < 0 || w >= worlds() || b < 0 || b >= wCount[w] || a < -1 || a >= wCount[w] || !rA || !rB)
         return fail(AVBDG_ERR_INVALID, "bad body index");
     int rc = ensureCapacity(nBodies, nForces + 1, worlds());
@@ -572,6 +581,7 @@ int Engine::addJoint(int w, int a, int b, const float rA[3], const float rB[3], 
 }
 
 int Engine::addIgnore(int w, int a, int b) {
+    ctrFresh = false;
     if (w < 0 || w >= worlds() || a < 0 || b < 0 || a >= wCount[w] || b >= wCount[w])
         return fail(AVBDG_ERR_INVALID, "bad body index");
     int rc = ensureCapacity(nBodies, nForces + 1, worlds());
@@ -596,6 +606,7 @@ int Engine::addIgnore(int w, int a, int b) {
 // Bulk form of addJoint/addIgnore: the same records, appended in the same order, with the joints'
 // torque arms computed from one download of the world's body sizes.
 int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
+    ctrFresh = false;
     if (w < 0 || w >= worlds() || count < 0 || (count > 0 && !descs))
         return fail(AVBDG_ERR_INVALID, "bad world or force array");
     if (count == 0)
@@ -688,6 +699,7 @@ int Engine::addForces(int w, int count, const avbdg_force_desc *descs) {
 // World removal between steps: one slot map, a device move of the survivors, a stable
 // compaction of the manifold and force lists, then the new world table.
 int Engine::removeWorlds(const std::vector<int> &ids) {
+    ctrFresh = false;
     const int nw = worlds();
     std::vector<char> drop(nw, 0);
     for (int w : ids) {
@@ -742,6 +754,7 @@ int Engine::removeWorlds(const std::vector<int> &ids) {
 }
 
 void Engine::clear() {
+    ctrFresh = false;
     cudaStreamSynchronize(stream);
     dropGraphs();
     wBase.clear();
@@ -955,10 +968,10 @@ void Engine::dropGraphs() {
     graphSpans = nullptr;
 }
 
-// Run the plan: from the graph cache (a plan is captured the second time it is seen; profiled
+// Enqueue the plan: from the graph cache (a plan is captured the second time it is seen; profiled
 // plans, whose graphs carry the span events, are cached apart), or eagerly the first time, when
 // graphs are disabled, during a tuning trial or when a capture failed.
-int Engine::runPlan(const StepPlan &plan) {
+int Engine::enqueuePlan(const StepPlan &plan) {
     launchBase = launchCount();
     graphSpans = nullptr;
     lastGraph = false;
@@ -1034,7 +1047,12 @@ int Engine::runPlan(const StepPlan &plan) {
     }
     cudaEventRecord(ev[4], stream);
     timed = true;
-    return finishStep();
+    return AVBDG_OK;
+}
+
+int Engine::runPlan(const StepPlan &plan) {
+    const int rc = enqueuePlan(plan);
+    return rc ? rc : finishStep();
 }
 
 // warmstartForces + selectUpdateBodies (solver_solve.cpp:31-105, 263-424).
@@ -1122,8 +1140,14 @@ int Engine::finishStep() {
     int rc = cudaCheck("step");
     if (rc)
         return rc;
-    steps++;
     launches = launchCount() - launchBase;
+    return processCounters();
+}
+
+// The host's part of a finished step: its counters are in hostCtr.
+int Engine::processCounters() {
+    steps++;
+    ctrFresh = true;
     if (profiling || tuning)
         collectSpans();
     if (profiling) {
@@ -1167,6 +1191,93 @@ int Engine::step() {
     if (nBodies == 0)
         return AVBDG_OK;
     return runPlan(planStep(0, 1, P.iterations));
+}
+
+// Every buffer a step fills has at least 4x headroom over the last checked step's counts, so the
+// next step cannot overflow unless its counts more than quadruple.
+bool Engine::roomy() const {
+    return ctrFresh && hostCtr[C_PAIRS] * 4 <= d.PP && hostCtr[C_CAND] * 4 <= d.MM &&
+           hostCtr[C_ADJ] * 4 <= 2 * (d.FF + d.MM);
+}
+
+// Waits for the queued step whose counters go to ring slot `slot` and checks them as finishStep does.
+int Engine::finishQueued(int slot) {
+    if (cudaEventSynchronize(ctrEvent[slot]) != cudaSuccess)
+        return cudaCheck("step");
+    const int rc = cudaCheck("step");
+    if (rc)
+        return rc;
+    std::memcpy(hostCtr, ctrRing + slot * C_COUNT, sizeof(int) * C_COUNT);
+    launches = ctrLaunches[slot];
+    // An error or a growth replaces or resets buffers the step queued after this one still uses:
+    // let that step finish first.
+    const bool grow = hostCtr[C_PAIRS] * 2 > d.PP || hostCtr[C_CAND] * 2 > d.MM || hostCtr[C_ADJ] * 2 > 2 * (d.FF + d.MM);
+    if (grow || hostCtr[C_ERRORS])
+        cudaStreamSynchronize(stream);
+    return processCounters();
+}
+
+// Steps `count` times. Without profiling or tuning, and while the last checked counters leave 4x
+// headroom (roomy), step i is enqueued before step i-1's counters are read back: the host waits
+// for the step before the one it just queued, so the device runs the steps back to back instead
+// of idling while the host checks each one. Every step's counters are still checked in order;
+// when a check finds an error the queued step is drained and the error returned (the state is
+// then not trustworthy, as after a failed step), and when the headroom is short the next step
+// waits for the check, which grows the store as step() does.
+int Engine::stepMany(int count, int substeps, int rounds) {
+    if (nBodies == 0 || count <= 0)
+        return AVBDG_OK;
+    const auto plan = [&] {
+        if (substeps <= 1)
+            return planStep(0, 1, P.iterations);
+        const int r = rounds > 0 ? std::max(1, rounds) : std::max(2, (P.iterations + substeps - 1) / substeps);
+        return planStep(1, substeps, r);
+    };
+    if (!ctrRing) {
+        if (cudaMallocHost(&ctrRing, sizeof(int) * 2 * C_COUNT) != cudaSuccess)
+            return fail(AVBDG_ERR_CAPACITY, "pinned counter allocation failed");
+        for (cudaEvent_t &e : ctrEvent)
+            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    }
+    int queued = -1; // ring slot of the step whose counters are not checked yet
+    for (int i = 0; i < count; i++) {
+        if (profiling || tuning) {
+            if (queued >= 0) {
+                const int rc = finishQueued(queued);
+                queued = -1;
+                if (rc)
+                    return rc;
+            }
+            const int rc = runPlan(plan());
+            if (rc)
+                return rc;
+            continue;
+        }
+        if (queued >= 0 && !roomy()) {
+            const int rc = finishQueued(queued);
+            queued = -1;
+            if (rc)
+                return rc;
+        }
+        const int slot = i & 1;
+        int rc = enqueuePlan(plan());
+        if (rc) {
+            cudaStreamSynchronize(stream);
+            return rc;
+        }
+        ctrLaunches[slot] = launchCount() - launchBase;
+        cudaMemcpyAsync(ctrRing + slot * C_COUNT, d.ctr, sizeof(int) * C_COUNT, cudaMemcpyDeviceToHost, stream);
+        cudaEventRecord(ctrEvent[slot], stream);
+        if (queued >= 0) {
+            rc = finishQueued(queued);
+            if (rc) {
+                cudaStreamSynchronize(stream);
+                return rc;
+            }
+        }
+        queued = slot;
+    }
+    return queued >= 0 ? finishQueued(queued) : AVBDG_OK;
 }
 
 int Engine::stepInterleaved(int substeps, int roundsPerSubstep) {

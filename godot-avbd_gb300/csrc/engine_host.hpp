@@ -58,6 +58,9 @@ public:
     // Enqueue one step of every world (Solver::step / Solver::stepInterleaved).
     int step();
     int stepInterleaved(int substeps, int rounds);
+    // `count` steps (substeps > 1: stepInterleaved(substeps, rounds)), queued back to back while the
+    // store has room; each step's counters are still checked in order.
+    int stepMany(int count, int substeps, int rounds);
     int sync();
 
     int getState(int world, int first, int count, float *pos, float *quat, float *vel, float *angVel);
@@ -120,6 +123,16 @@ private:
     int steps = 0;
     int launches = 0;
     int hostCtr[C_COUNT] = {};
+    // stepMany: counters of queued steps come back through a two-slot pinned ring, each slot with
+    // the event that marks its copy; ctrFresh is true when hostCtr holds a step of the current
+    // store (cleared whenever the store or its contents change).
+    int *ctrRing = nullptr;
+    cudaEvent_t ctrEvent[2] = {nullptr, nullptr};
+    int ctrLaunches[2] = {0, 0};
+    bool ctrFresh = false;
+    int processCounters();
+    int finishQueued(int slot);
+    bool roomy() const;
     int colourSizes[kMaxColours + 1] = {};
     cudaEvent_t ev[5] = {};
     bool timed = false;
@@ -200,6 +213,7 @@ private:
     StepPlan planStep(int mode, int substeps, int rounds);
     bool enqueueStep(const StepPlan &plan); // false: a launch failed (the rest was not enqueued)
     int launchFailure();
+    int enqueuePlan(const StepPlan &plan);
     int runPlan(const StepPlan &plan);
     void dropGraphs();
     void recordPhase(cudaEvent_t e);

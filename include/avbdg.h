@@ -194,7 +194,9 @@ int avbdg_world_step(avbdg_world *world);
  * substep dt, as in the reference. */
 int avbdg_world_step_interleaved(avbdg_world *world, int substeps, int rounds_per_substep);
 
-/* Run `count` plain steps back to back (one call, no host round trip between steps). */
+/* Run `count` plain steps. While every buffer a step fills has at least 4x headroom, the next step
+ * is queued before the previous one's counters are read back, so the device runs the steps back to
+ * back; every step's counters (errors, forces, growth) are still checked in order. */
 int avbdg_world_step_n(avbdg_world *world, int count);
 
 /* Wait for every queued step of this world. */
@@ -319,7 +321,7 @@ int avbdg_batch_add_world(avbdg_batch *batch, int body_count, const avbdg_body_d
  * their order and are renumbered 0.. in it; their state and results are unaffected (Solver::clear
  * for the removed worlds, src/avbd/solver_step.cpp:29-40). */
 int avbdg_batch_remove_worlds(avbdg_batch *batch, int count, const int *worlds);
-/* `count` steps of every world (Solver::step each). */
+/* `count` steps of every world (Solver::step each), queued back to back as avbdg_world_step_n. */
 int avbdg_batch_step(avbdg_batch *batch, int count);
 int avbdg_batch_sync(avbdg_batch *batch);
 int avbdg_batch_world_count(const avbdg_batch *batch, int *out);

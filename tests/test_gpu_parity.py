@@ -217,3 +217,26 @@ def test_gpu_host_state_edits(pkg, gpu, oracle):
             b.set_state(velocity=v)
     for x, y in zip(a.state(), b.state()):
         assert np.array_equal(x, y)
+
+
+def test_gpu_queued_steps_with_growth(pkg, gpu, oracle, golden):
+    """step(n) queues each step before the previous one's counters come back (they are checked one
+    step behind, in order). A world created with the smallest store grows in its first steps and
+    still equals the oracle, and a long run equals the reference's recorded digest."""
+    capi, scenes = pkg.capi, pkg.scenes
+    sc = scenes.pile(count=300, chain_links=8)
+    p = gpu.default_params()
+    scenes.apply_params(p, sc.params)
+    a = capi.World(gpu, p, max_bodies=1, max_forces=1)
+    a.add_bodies(capi.scene_body_descs(sc))
+    for force in sc.joints:
+        a.add_force(force)
+    b = scenes.instantiate(oracle, sc)
+    a.step(60)
+    b.step(60)
+    for x, y in zip(a.state(), b.state()):
+        assert np.array_equal(x, y)
+    rec = golden["runs"]["pile"]
+    w = scenes.instantiate(gpu, scenes.pile(**rec["kwargs"]))
+    w.step(rec["steps"])
+    assert f"{w.digest():016x}" == rec["digests"][-1]
