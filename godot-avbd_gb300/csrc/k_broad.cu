@@ -27,6 +27,8 @@ __device__ __forceinline__ real orderedFloat(int i) { return bitsf(i >= 0 ? i : 
 
 // Swept AABB (solver_broadphase.cpp:103-122) over the tight box bound (rigid.cpp:83-106).
 __global__ void aabbKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
@@ -56,6 +58,8 @@ __global__ void aabbKernel(Dev d, StepParams p) {
 // ---- Morton codes (bvh_broadphase.cpp:19-36, 70-85) ----
 
 __global__ void boundsResetKernel(Dev d, int *wBounds) {
+    pdlWait();
+    pdlTrigger();
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= d.ctr[C_WORLDS])
         return;
@@ -69,6 +73,8 @@ __global__ void boundsResetKernel(Dev d, int *wBounds) {
 // ranges, so a warp mostly holds one), and one lane per world and warp does the atomics: a single
 // large world would otherwise serialise six atomics per body on six addresses.
 __global__ void boundsKernel(Dev d, int *wBounds) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int w = g < n ? d.meta[g].x : -1;
@@ -110,6 +116,8 @@ __device__ __forceinline__ uint32_t quantise(real v, real lo, real scaleF) {
 
 // Code per body; keys/values laid out by list position for the stable (code, list index) sort.
 __global__ void mortonKernel(Dev d, const int *wBounds) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
@@ -145,6 +153,8 @@ __global__ void mortonKernel(Dev d, const int *wBounds) {
 
 // Slots without a body keep key ~0 and map to themselves in list-position space.
 __global__ void mortonResetKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -156,6 +166,8 @@ __global__ void mortonResetKernel(Dev d) {
 // Second key: the world's first slot (a free slot keys on its own position), so after the stable
 // sort world w's leaves occupy sorted positions [wBase, wBase + wCount).
 __global__ void worldKeyKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -166,6 +178,8 @@ __global__ void worldKeyKernel(Dev d) {
 }
 
 __global__ void leafKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -189,6 +203,8 @@ constexpr int kLeafBit = 0x40000000;
 // Karras (2012) radix tree: internal node i of a world spans a key range and splits at the
 // highest differing bit.
 __global__ void karrasKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n)
@@ -260,6 +276,8 @@ __device__ __forceinline__ void childBounds(const Dev &d, int c, real4 &mn, real
 
 // Bottom-up refit: the second child to arrive at a node computes its bounds.
 __global__ void refitKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n)
@@ -301,6 +319,8 @@ __device__ __forceinline__ bool overlapClosed(f3 aMin, f3 aMax, f3 bMin, f3 bMax
 // segments. Pair keys are (lpA << 32 | lpB); the segmented sort orders each segment afterwards.
 template <bool EMIT>
 __global__ void traverseKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = EMIT ? d.ctr[C_PAIRSPILL] : d.ctr[C_BODIES];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -369,6 +389,8 @@ __global__ void traverseKernel(Dev d) {
 
 // Stashed partners into their body's segment (bodies with more partners are walked again).
 __global__ void pairStashKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int lpA = blockIdx.x * blockDim.x + threadIdx.x;
     if (lpA >= n)
@@ -383,6 +405,8 @@ __global__ void pairStashKernel(Dev d) {
 }
 
 __global__ void pairTotalKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     int t = d.ctr[C_TMP];
     if (t > d.PP) {
         atomicOr(&d.ctr[C_ERRORS], kErrPairs);
@@ -422,6 +446,8 @@ __device__ __forceinline__ void filterAt(Dev d, int k) {
 }
 
 __global__ void filterKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_PAIRS];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         filterAt(d, k);
@@ -441,12 +467,16 @@ __device__ __forceinline__ void acquireAt(Dev d, const int *flags, const int *ra
 }
 
 __global__ void acquireKernel(Dev d, const int *flags, const int *rank) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_PAIRS];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         acquireAt(d, flags, rank, k);
 }
 
 __global__ void candTotalKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     int c = d.ctr[C_LIVE] + d.ctr[C_TMP];
     if (c > d.MM) {
         atomicOr(&d.ctr[C_ERRORS], kErrManifolds);
@@ -460,30 +490,30 @@ __global__ void candTotalKernel(Dev d) {
 static int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
 void launchAabb(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); aabbKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+    ++launchCount(); launchK(aabbKernel, grid(d.NB), kThreads, 0, s, d, p);
 }
 
 void launchRebuildTree(const Dev &d, bool multiWorld, cudaStream_t s) {
     const int *nb = d.ctr + C_BODIES;
-    ++launchCount(); boundsResetKernel<<<grid(d.WW), kThreads, 0, s>>>(d, d.wBounds);
-    ++launchCount(); boundsKernel<<<grid(d.NB), kThreads, 0, s>>>(d, d.wBounds);
-    ++launchCount(); mortonResetKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
-    ++launchCount(); mortonKernel<<<grid(d.NB), kThreads, 0, s>>>(d, d.wBounds);
+    ++launchCount(); launchK(boundsResetKernel, grid(d.WW), kThreads, 0, s, d, d.wBounds);
+    ++launchCount(); launchK(boundsKernel, grid(d.NB), kThreads, 0, s, d, d.wBounds);
+    ++launchCount(); launchK(mortonResetKernel, grid(d.NB), kThreads, 0, s, d);
+    ++launchCount(); launchK(mortonKernel, grid(d.NB), kThreads, 0, s, d, d.wBounds);
     radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, d.NB, nb, 0, 63, d.radixScratch, s);
     if (multiWorld) {
         int bits = 1; // world bases are below the slot capacity
         while ((1 << bits) < d.NB + 1)
             bits++;
-        ++launchCount(); worldKeyKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+        ++launchCount(); launchK(worldKeyKernel, grid(d.NB), kThreads, 0, s, d);
         radixSortPairs(d.sortK, d.sortV, d.sortKAlt, d.sortVAlt, d.NB, nb, 0, bits, d.radixScratch, s);
     }
-    ++launchCount(); leafKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
-    ++launchCount(); karrasKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(leafKernel, grid(d.NB), kThreads, 0, s, d);
+    ++launchCount(); launchK(karrasKernel, grid(d.NB), kThreads, 0, s, d);
 }
 
 void launchRefit(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.nodeFlag, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
-    ++launchCount(); refitKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(refitKernel, grid(d.NB), kThreads, 0, s, d);
 }
 
 bool traverseBlockFits(int block) {
@@ -493,19 +523,19 @@ bool traverseBlockFits(int block) {
 void launchPairs(const Dev &d, int block, cudaStream_t s) {
     cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.ctr + C_PAIRSPILL, 0, sizeof(int), s);
-    ++launchCount(); traverseKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d);
+    ++launchCount(); launchK(traverseKernel<false>, divUp(d.NB, block), block, 0, s, d);
     scanExclusive(d.pairStart, d.pairStart, d.NB + 1, nullptr, d.ctr + C_TMP, d.scanScratch, s);
-    ++launchCount(); pairTotalKernel<<<1, 1, 0, s>>>(d);
-    ++launchCount(); pairStashKernel<<<divUp(d.NB, kThreads), kThreads, 0, s>>>(d);
-    ++launchCount(); traverseKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d);
+    ++launchCount(); launchK(pairTotalKernel, 1, 1, 0, s, d);
+    ++launchCount(); launchK(pairStashKernel, divUp(d.NB, kThreads), kThreads, 0, s, d);
+    ++launchCount(); launchK(traverseKernel<true>, divUp(d.NB, block), block, 0, s, d);
     segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
 }
 
 void launchFilterAcquire(const Dev &d, cudaStream_t s) {
-    ++launchCount(); filterKernel<<<residentGrid(filterKernel, kThreads, grid(d.PP)), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(filterKernel, residentGrid(filterKernel, kThreads, grid(d.PP)), kThreads, 0, s, d);
     scanExclusive(d.pairValid, d.mActive, d.PP, d.ctr + C_PAIRS, d.ctr + C_TMP, d.scanScratch, s);
-    ++launchCount(); acquireKernel<<<residentGrid(acquireKernel, kThreads, grid(d.PP)), kThreads, 0, s>>>(d, d.pairValid, d.mActive);
-    ++launchCount(); candTotalKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); launchK(acquireKernel, residentGrid(acquireKernel, kThreads, grid(d.PP)), kThreads, 0, s, d, d.pairValid, d.mActive);
+    ++launchCount(); launchK(candTotalKernel, 1, 1, 0, s, d);
 }
 
 } // namespace avbdg

@@ -10,6 +10,8 @@ namespace avbdg {
 namespace {
 
 __global__ void packStateKernel(Dev d, int first, int count, float *out) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count)
         return;
@@ -34,6 +36,8 @@ __global__ void packStateKernel(Dev d, int first, int count, float *out) {
 // Sets *bad when an uploaded position or velocity component is not finite (orientations are taken
 // as given, as the host-side check does).
 __global__ void checkStateKernel(int count, const float *in, int mask, int *bad) {
+    pdlWait();
+    pdlTrigger();
     const long long total = 13LL * count;
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
     for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < total; k += stride) {
@@ -46,6 +50,8 @@ __global__ void checkStateKernel(int count, const float *in, int mask, int *bad)
 // Fields not in `mask` (1 pos, 2 quat, 4 vel, 8 angvel) keep their device values; the packed
 // companions (mass in x.w, gravity in v.w) are preserved. With `bad` set nothing is written.
 __global__ void unpackStateKernel(Dev d, int first, int count, const float *in, int mask, const int *bad) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count || (bad && *bad))
         return;
@@ -69,19 +75,19 @@ __global__ void unpackStateKernel(Dev d, int first, int count, const float *in, 
 
 void launchPackState(const Dev &d, int first, int count, float *out, cudaStream_t s) {
     ++launchCount();
-    packStateKernel<<<divUp(count > 0 ? count : 1, 256), 256, 0, s>>>(d, first, count, out);
+    launchK(packStateKernel, divUp(count > 0 ? count : 1, 256), 256, 0, s, d, first, count, out);
 }
 
 void launchCheckState(int count, const float *in, int mask, int *bad, cudaStream_t s) {
     ++launchCount();
-    checkStateKernel<<<residentGrid(checkStateKernel, 256, divUp(13 * (count > 0 ? count : 1), 256)), 256, 0, s>>>(
+    launchK(checkStateKernel, residentGrid(checkStateKernel, 256, divUp(13 * (count > 0 ? count : 1), 256)), 256, 0, s, 
             count, in, mask, bad);
 }
 
 void launchUnpackState(const Dev &d, int first, int count, const float *in, int mask, const int *bad,
                        cudaStream_t s) {
     ++launchCount();
-    unpackStateKernel<<<divUp(count > 0 ? count : 1, 256), 256, 0, s>>>(d, first, count, in, mask, bad);
+    launchK(unpackStateKernel, divUp(count > 0 ? count : 1, 256), 256, 0, s, d, first, count, in, mask, bad);
 }
 
 } // namespace avbdg

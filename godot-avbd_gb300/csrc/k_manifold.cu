@@ -29,6 +29,8 @@ constexpr int kThreads = 256;
 // a pair query always has a dynamic side.
 
 __global__ void adjCountKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int nf = d.ctr[C_FORCES];
     const int nm = d.ctr[C_LIVE];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -46,6 +48,8 @@ __global__ void adjCountKernel(Dev d) {
 }
 
 __global__ void adjFillKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int nf = d.ctr[C_FORCES];
     const int nm = d.ctr[C_LIVE];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -70,6 +74,8 @@ __global__ void adjFillKernel(Dev d) {
 // load of the force's or manifold's body pair to find them; and each manifold side's entry, where
 // its block stamp is stored, so a body's stamps lie contiguous in its adjacency range.
 __global__ void adjInfoKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
@@ -87,6 +93,8 @@ __global__ void adjInfoKernel(Dev d) {
 }
 
 __global__ void adjTotalKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     if (d.ctr[C_ADJ] > 2 * (d.FF + d.MM))
         atomicOr(&d.ctr[C_ERRORS], kErrAdjacency);
 }
@@ -299,6 +307,8 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
 
 template <bool ROUND>
 __global__ void manifoldInitKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_CAND];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         manifoldInitAt<ROUND>(d, p, i);
@@ -352,6 +362,8 @@ __device__ __forceinline__ void manifoldCompactRun(const Dev &d, const int *flag
 }
 
 __global__ void manifoldCompactKernel(Dev d, const int *flags, const int *rank) {
+    pdlWait();
+    pdlTrigger();
     const int cand = d.ctr[C_CAND];
     const unsigned long long span = static_cast<unsigned long long>(cand) * kMaxContacts +
                                     static_cast<unsigned long long>(gridDim.x) * blockDim.x;
@@ -383,6 +395,8 @@ __device__ __forceinline__ void rebaseAt(Dev d, StepParams p, int m) {
 }
 
 __global__ void rebaseKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
         rebaseAt(d, p, m);
@@ -410,6 +424,8 @@ __device__ __forceinline__ f3 warmPenalty(f3 k, real gamma, real stiffness) {
 }
 
 __global__ void forceInitKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     const int nf = d.ctr[C_FORCES];
     if (f >= nf)
@@ -436,6 +452,8 @@ __global__ void forceInitKernel(Dev d, StepParams p) {
 
 // Stable in-place compaction of the force list (reaping is rare; one thread walks it in order).
 __global__ void forceCompactKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     if (!d.ctr[C_TMP])
         return;
     const int nf = d.ctr[C_FORCES];
@@ -483,13 +501,13 @@ void prepareNarrowPhase() {
 void launchAdjacency(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.adjStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.adjFill, 0, sizeof(int) * static_cast<size_t>(d.NB), s);
-    ++launchCount(); adjCountKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(adjCountKernel, grid(d.FF + d.MM), kThreads, 0, s, d);
     // Slots past the last body count zero, so scanning the whole capacity gives the same starts.
     scanExclusive(d.adjStart, d.adjStart, d.NB + 1, nullptr, d.ctr + C_ADJ, d.scanScratch, s);
-    ++launchCount(); adjTotalKernel<<<1, 1, 0, s>>>(d);
-    ++launchCount(); adjFillKernel<<<grid(d.FF + d.MM), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(adjTotalKernel, 1, 1, 0, s, d);
+    ++launchCount(); launchK(adjFillKernel, grid(d.FF + d.MM), kThreads, 0, s, d);
     segmentedSortU32(d.adjSeq, d.adjTmp, d.adjStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
-    ++launchCount(); adjInfoKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(adjInfoKernel, grid(d.NB), kThreads, 0, s, d);
 }
 
 bool narrowBlockFits(int block) {
@@ -499,9 +517,9 @@ bool narrowBlockFits(int block) {
 void launchManifoldInit(const Dev &d, const StepParams &p, bool round, int block, cudaStream_t s) {
     ++launchCount();
     if (round)
-        manifoldInitKernel<true><<<divUp(d.MM, block), block, 0, s>>>(d, p);
+        launchK(manifoldInitKernel<true>, divUp(d.MM, block), block, 0, s, d, p);
     else
-        manifoldInitKernel<false><<<divUp(d.MM, block), block, 0, s>>>(d, p);
+        launchK(manifoldInitKernel<false>, divUp(d.MM, block), block, 0, s, d, p);
 }
 
 void launchManifoldCompact(const Dev &d, cudaStream_t s) {
@@ -509,19 +527,19 @@ void launchManifoldCompact(const Dev &d, cudaStream_t s) {
     ++launchCount();
     const int blocks = residentGrid(reinterpret_cast<const void *>(manifoldCompactKernel), kThreads, 0,
                                     divUp(d.MM * kMaxContacts, kThreads));
-    manifoldCompactKernel<<<blocks, kThreads, 0, s>>>(d, d.mActive, d.pairValid);
+    launchK(manifoldCompactKernel, blocks, kThreads, 0, s, d, d.mActive, d.pairValid);
 }
 
 void launchRebase(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); rebaseKernel<<<residentGrid(rebaseKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
+    ++launchCount(); launchK(rebaseKernel, residentGrid(rebaseKernel, kThreads, grid(d.MM)), kThreads, 0, s, d, p);
 }
 
 void launchForceInit(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {
     if (!forces)
         return;
     cudaMemsetAsync(d.ctr + C_TMP, 0, sizeof(int), s);
-    ++launchCount(); forceInitKernel<<<grid(d.FF), kThreads, 0, s>>>(d, p);
-    ++launchCount(); forceCompactKernel<<<1, 1, 0, s>>>(d);
+    ++launchCount(); launchK(forceInitKernel, grid(d.FF), kThreads, 0, s, d, p);
+    ++launchCount(); launchK(forceCompactKernel, 1, 1, 0, s, d);
 }
 
 } // namespace avbdg

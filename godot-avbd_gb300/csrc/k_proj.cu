@@ -97,6 +97,8 @@ __device__ __forceinline__ void projActiveAt(Dev d, int m) {
 }
 
 __global__ void projActiveKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
         projActiveAt(d, m);
@@ -111,6 +113,8 @@ __device__ __forceinline__ void specScatterAt(Dev d, const int *flags, const int
 }
 
 __global__ void specScatterKernel(Dev d, const int *flags, const int *rank) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
         specScatterAt(d, flags, rank, m);
@@ -145,6 +149,8 @@ __device__ __forceinline__ void brakePredAt(Dev d, const int *rank, int k) {
 }
 
 __global__ void brakePredKernel(Dev d, const int *rank) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_SPECN];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         brakePredAt(d, rank, k);
@@ -254,6 +260,8 @@ __device__ __forceinline__ bool brakeSolve(const BrakeLoad &bl, real window, f3 
 }
 
 __global__ void __launch_bounds__(kBrakeThreads) brakeKernel(Dev d, real window) {
+    pdlWait();
+    pdlTrigger();
     const int ns = d.ctr[C_SPECN];
     const int stride = gridDim.x * blockDim.x;
     volatile int *errors = d.ctr + C_ERRORS;
@@ -418,6 +426,8 @@ __device__ __forceinline__ void projBodyAt(const Dev &d, const StepParams &p, in
 // The same passes as separate launches, for large stores, where every phase fills the GPU and a
 // kernel boundary costs less than a grid barrier of a resident grid.
 __global__ void projStartKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int nWorlds = d.ctr[C_WORLDS];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nWorlds)
@@ -426,15 +436,19 @@ __global__ void projStartKernel(Dev d) {
     d.wMaxDepth[w] = 0;
 }
 
-__global__ void projManifoldKernel(Dev d, StepParams p) { projManifoldPass(d, p, blockIdx.x * blockDim.x, gridDim.x * blockDim.x); }
+__global__ void projManifoldKernel(Dev d, StepParams p) { pdlWait(); pdlTrigger(); projManifoldPass(d, p, blockIdx.x * blockDim.x, gridDim.x * blockDim.x); }
 
 __global__ void projBodyKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g < d.ctr[C_BODIES])
         projBodyAt(d, p, g);
 }
 
 __global__ void projCheckKernel(Dev d, real tolerance) {
+    pdlWait();
+    pdlTrigger();
     const int nWorlds = d.ctr[C_WORLDS];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nWorlds)
@@ -450,6 +464,8 @@ __global__ void projCheckKernel(Dev d, real tolerance) {
 // whose deepest patch is within tolerance, with a grid barrier between these phases (the kernel
 // boundaries of the same sequence launched separately).
 __global__ void __launch_bounds__(kThreads) projectionKernel(Dev d, StepParams p, real tolerance) {
+    pdlWait();
+    pdlTrigger();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int stride = gridDim.x * blockDim.x;
     const int nWorlds = d.ctr[C_WORLDS];
@@ -497,14 +513,14 @@ int brakeGridBlocks() {
 
 void launchProjActive(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.wActive, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
-    ++launchCount(); projActiveKernel<<<residentGrid(projActiveKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(projActiveKernel, residentGrid(projActiveKernel, kThreads, grid(d.MM)), kThreads, 0, s, d);
     scanExclusive(d.mActive, d.pairValid, d.MM, d.ctr + C_LIVE, d.ctr + C_SPECN, d.scanScratch, s);
-    ++launchCount(); specScatterKernel<<<residentGrid(specScatterKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, d.mActive, d.pairValid);
+    ++launchCount(); launchK(specScatterKernel, residentGrid(specScatterKernel, kThreads, grid(d.MM)), kThreads, 0, s, d, d.mActive, d.pairValid);
 }
 
 // Runs right after launchProjActive, whose scan left each candidate's rank in d.pairValid.
 void launchBrake(const Dev &d, real window, cudaStream_t s) {
-    ++launchCount(); brakePredKernel<<<residentGrid(brakePredKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, d.pairValid);
+    ++launchCount(); launchK(brakePredKernel, residentGrid(brakePredKernel, kThreads, grid(d.MM)), kThreads, 0, s, d, d.pairValid);
     Dev dd = d;
     real win = window;
     void *args[] = {&dd, &win};
@@ -536,11 +552,11 @@ void launchProjection(const Dev &d, const StepParams &p, cudaStream_t s) {
     const int most = projGridMax();
     if (need > most) {
         const real tol0 = smax(p.projSlop * 0.01f, 1.0e-6f);
-        ++launchCount(); projStartKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
+        ++launchCount(); launchK(projStartKernel, grid(d.WW), kThreads, 0, s, d);
         for (int it = 0; it < p.projIters; it++) {
-            ++launchCount(); projManifoldKernel<<<residentGrid(projManifoldKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p);
-            ++launchCount(); projBodyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
-            ++launchCount(); projCheckKernel<<<grid(d.WW), kThreads, 0, s>>>(d, tol0);
+            ++launchCount(); launchK(projManifoldKernel, residentGrid(projManifoldKernel, kThreads, grid(d.MM)), kThreads, 0, s, d, p);
+            ++launchCount(); launchK(projBodyKernel, grid(d.NB), kThreads, 0, s, d, p);
+            ++launchCount(); launchK(projCheckKernel, grid(d.WW), kThreads, 0, s, d, tol0);
         }
         return;
     }

@@ -74,6 +74,8 @@ __device__ real rayTest(const Dev &d, int g, f3 origin, f3 dir, f3 &local) {
 }
 
 __global__ void pickResetKernel(unsigned long long *best, int rays) {
+    pdlWait();
+    pdlTrigger();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < rays)
         best[r] = ~0ull;
@@ -83,6 +85,8 @@ __global__ void pickResetKernel(unsigned long long *best, int rays) {
 // (-0 counts as +0, as the reference's comparisons do).
 __global__ void pickKernel(Dev d, int base, int count, const float *rays, int nRays, unsigned mask,
                            unsigned long long *best) {
+    pdlWait();
+    pdlTrigger();
     const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= static_cast<long long>(nRays) * count)
         return;
@@ -102,6 +106,8 @@ __global__ void pickKernel(Dev d, int base, int count, const float *rays, int nR
 
 __global__ void pickResultKernel(Dev d, int base, int count, const float *rays, int nRays,
                                  const unsigned long long *best, int *outBody, float *outLocal) {
+    pdlWait();
+    pdlTrigger();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nRays)
         return;
@@ -123,6 +129,8 @@ __global__ void pickResultKernel(Dev d, int base, int count, const float *rays, 
 
 // Overlap flag per list position of the world (collectAABB's test, solver_query.cpp:154-170).
 __global__ void overlapFlagKernel(Dev d, int base, int count, f3 lo, f3 hi, unsigned mask, int *flags) {
+    pdlWait();
+    pdlTrigger();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= count)
         return;
@@ -143,6 +151,8 @@ __global__ void overlapFlagKernel(Dev d, int base, int count, f3 lo, f3 hi, unsi
 
 __global__ void overlapScatterKernel(int base, int count, const int *flags, const int *rank, int capacity,
                                      int *out) {
+    pdlWait();
+    pdlTrigger();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= count || !flags[p])
         return;
@@ -154,25 +164,25 @@ __global__ void overlapScatterKernel(int base, int count, const int *flags, cons
 
 void launchPick(const Dev &d, int base, int count, const float *rays, int nRays, unsigned mask,
                 unsigned long long *best, int *outBody, float *outLocal, cudaStream_t s) {
-    ++launchCount(); pickResetKernel<<<divUp(nRays > 0 ? nRays : 1, kThreads), kThreads, 0, s>>>(best, nRays);
+    ++launchCount(); launchK(pickResetKernel, divUp(nRays > 0 ? nRays : 1, kThreads), kThreads, 0, s, best, nRays);
     const long long pairs = static_cast<long long>(nRays) * count;
     if (pairs > 0) {
         ++launchCount();
-        pickKernel<<<static_cast<unsigned>((pairs + kThreads - 1) / kThreads), kThreads, 0, s>>>(d, base, count, rays,
+        launchK(pickKernel, static_cast<unsigned>((pairs + kThreads - 1) / kThreads), kThreads, 0, s, d, base, count, rays,
                                                                                               nRays, mask, best);
     }
     ++launchCount();
-    pickResultKernel<<<divUp(nRays > 0 ? nRays : 1, kThreads), kThreads, 0, s>>>(d, base, count, rays, nRays, best,
+    launchK(pickResultKernel, divUp(nRays > 0 ? nRays : 1, kThreads), kThreads, 0, s, d, base, count, rays, nRays, best,
                                                                                  outBody, outLocal);
 }
 
 void launchCollectAabb(const Dev &d, int base, int count, f3 lo, f3 hi, unsigned mask, int *flags, int *rank,
                        int *total, void *scanScratch, int capacity, int *out, cudaStream_t s) {
     ++launchCount();
-    overlapFlagKernel<<<divUp(count > 0 ? count : 1, kThreads), kThreads, 0, s>>>(d, base, count, lo, hi, mask, flags);
+    launchK(overlapFlagKernel, divUp(count > 0 ? count : 1, kThreads), kThreads, 0, s, d, base, count, lo, hi, mask, flags);
     scanExclusive(flags, rank, count, nullptr, total, scanScratch, s);
     ++launchCount();
-    overlapScatterKernel<<<divUp(count > 0 ? count : 1, kThreads), kThreads, 0, s>>>(base, count, flags, rank, capacity,
+    launchK(overlapScatterKernel, divUp(count > 0 ? count : 1, kThreads), kThreads, 0, s, base, count, flags, rank, capacity,
                                                                                     out);
 }
 

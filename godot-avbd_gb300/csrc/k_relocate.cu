@@ -20,6 +20,8 @@ int grid(int n) { return divUp(n > 0 ? n : 1, kThreads); }
 
 // remap[2w] = new world id (-1 = removed), remap[2w + 1] = new base slot.
 __global__ void slotMapKernel(Dev d, int n, const int *remap, int *slotMap) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
         return;
@@ -30,6 +32,8 @@ __global__ void slotMapKernel(Dev d, int n, const int *remap, int *slotMap) {
 
 template <typename T>
 __global__ void scatterKernel(const T *src, T *dst, const int *slotMap, int n) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
         return;
@@ -39,6 +43,8 @@ __global__ void scatterKernel(const T *src, T *dst, const int *slotMap, int n) {
 }
 
 __global__ void metaScatterKernel(const int4 *src, int4 *dst, const int *slotMap, const int *remap, int n) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
         return;
@@ -53,6 +59,8 @@ __global__ void metaScatterKernel(const int4 *src, int4 *dst, const int *slotMap
 // Live manifolds -> stage with rewritten bodies; mActive marks the survivors for the stable
 // compaction back into live order.
 __global__ void manifoldRelocateKernel(Dev d, const int *slotMap) {
+    pdlWait();
+    pdlTrigger();
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= d.ctr[C_CAND])
         return;
@@ -94,6 +102,8 @@ __global__ void manifoldRelocateKernel(Dev d, const int *slotMap) {
 
 // Force b is always a body of the force's world (a may be the static world anchor, -1).
 __global__ void forceFlagKernel(Dev d, int nf, const int *slotMap, int2 *abOut) {
+    pdlWait();
+    pdlTrigger();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf)
         return;
@@ -105,6 +115,8 @@ __global__ void forceFlagKernel(Dev d, int nf, const int *slotMap, int2 *abOut) 
 
 template <typename T>
 __global__ void compactKernel(const T *src, T *dst, const int *keep, const int *rank, int n) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && keep[i])
         dst[rank[i]] = src[i];
@@ -112,6 +124,8 @@ __global__ void compactKernel(const T *src, T *dst, const int *keep, const int *
 
 // Strided records (kExtF4 float4 per force) follow their force.
 __global__ void compactExtKernel(const real4 *src, real4 *dst, const int *keep, const int *rank, int n) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * kExtF4)
         return;
@@ -122,6 +136,8 @@ __global__ void compactExtKernel(const real4 *src, real4 *dst, const int *keep, 
 
 // List position -> body of every world's range, from the (new) world table.
 __global__ void listPosKernel(Dev d, int n) {
+    pdlWait();
+    pdlTrigger();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n)
         return;
@@ -131,7 +147,7 @@ __global__ void listPosKernel(Dev d, int n) {
 
 template <typename T>
 void moveArray(T *arr, T *tmp, const int *slotMap, int nOld, int nNew, cudaStream_t s) {
-    ++launchCount(); scatterKernel<T><<<grid(nOld), kThreads, 0, s>>>(arr, tmp, slotMap, nOld);
+    ++launchCount(); launchK(scatterKernel<T>, grid(nOld), kThreads, 0, s, arr, tmp, slotMap, nOld);
     if (nNew > 0)
         cudaMemcpyAsync(arr, tmp, sizeof(T) * static_cast<size_t>(nNew), cudaMemcpyDeviceToDevice, s);
 }
@@ -140,7 +156,7 @@ void moveArray(T *arr, T *tmp, const int *slotMap, int nOld, int nNew, cudaStrea
 // needs no host read of the surviving count.
 template <typename T>
 void compactArray(T *arr, T *tmp, const int *keep, const int *rank, int n, cudaStream_t s) {
-    ++launchCount(); compactKernel<T><<<grid(n), kThreads, 0, s>>>(arr, tmp, keep, rank, n);
+    ++launchCount(); launchK(compactKernel<T>, grid(n), kThreads, 0, s, arr, tmp, keep, rank, n);
     cudaMemcpyAsync(arr, tmp, sizeof(T) * static_cast<size_t>(n), cudaMemcpyDeviceToDevice, s);
 }
 
@@ -148,7 +164,7 @@ void compactArray(T *arr, T *tmp, const int *keep, const int *rank, int n, cudaS
 
 void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const int *remap, cudaStream_t s) {
     int *slotMap = d.relocInt;
-    ++launchCount(); slotMapKernel<<<grid(nOld), kThreads, 0, s>>>(d, nOld, remap, slotMap);
+    ++launchCount(); launchK(slotMapKernel, grid(nOld), kThreads, 0, s, d, nOld, remap, slotMap);
 
     // Bodies, through a staging array (slots only move down, so an in-place move would race).
     real4 *tmp4 = d.relocF4;
@@ -156,13 +172,13 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
         moveArray(arr, tmp4, slotMap, nOld, nNew, s);
     moveArray(d.sleep, reinterpret_cast<int2 *>(tmp4), slotMap, nOld, nNew, s);
     int4 *tmpMeta = reinterpret_cast<int4 *>(tmp4);
-    ++launchCount(); metaScatterKernel<<<grid(nOld), kThreads, 0, s>>>(d.meta, tmpMeta, slotMap, remap, nOld);
+    ++launchCount(); launchK(metaScatterKernel, grid(nOld), kThreads, 0, s, d.meta, tmpMeta, slotMap, remap, nOld);
     if (nNew > 0)
         cudaMemcpyAsync(d.meta, tmpMeta, sizeof(int4) * static_cast<size_t>(nNew), cudaMemcpyDeviceToDevice, s);
 
     // Live manifolds: stage with new body slots, then the step's stable compaction into live.
     cudaMemcpyAsync(d.ctr + C_CAND, d.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToDevice, s);
-    ++launchCount(); manifoldRelocateKernel<<<grid(d.MM), kThreads, 0, s>>>(d, slotMap);
+    ++launchCount(); launchK(manifoldRelocateKernel, grid(d.MM), kThreads, 0, s, d, slotMap);
     launchManifoldCompact(d, s);
 
     // Forces: flags + exclusive rank, then a stable scatter of every field.
@@ -170,10 +186,10 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
         // relocF4 holds max(NB, FF * kExtF4) float4: room for two int2 arrays of FF entries.
         int2 *abNew = reinterpret_cast<int2 *>(tmp4);
         int *rank = d.relocInt + d.NB;
-        ++launchCount(); forceFlagKernel<<<grid(nForces), kThreads, 0, s>>>(d, nForces, slotMap, abNew);
+        ++launchCount(); launchK(forceFlagKernel, grid(nForces), kThreads, 0, s, d, nForces, slotMap, abNew);
         scanExclusive(d.fKeep, rank, d.FF, d.ctr + C_FORCES, d.ctr + C_TMP, d.scanScratch, s);
         int2 *abTmp = reinterpret_cast<int2 *>(tmp4) + d.FF;
-        ++launchCount(); compactKernel<int2><<<grid(nForces), kThreads, 0, s>>>(abNew, abTmp, d.fKeep, rank, nForces);
+        ++launchCount(); launchK(compactKernel<int2>, grid(nForces), kThreads, 0, s, abNew, abTmp, d.fKeep, rank, nForces);
         cudaMemcpyAsync(d.fAB, abTmp, sizeof(int2) * static_cast<size_t>(nForces), cudaMemcpyDeviceToDevice, s);
         for (real4 *arr : {d.fRA, d.fRB, d.fC0L, d.fC0A, d.fKL, d.fKA, d.fLL, d.fLA, d.fPar})
             compactArray(arr, tmp4, d.fKeep, rank, nForces, s);
@@ -183,7 +199,7 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
         // Generic-joint records (relocF4 holds FF * kExtF4 float4).
         real4 *extTmp = d.relocF4;
         ++launchCount();
-        compactExtKernel<<<grid(nForces * kExtF4), kThreads, 0, s>>>(d.fExt, extTmp, d.fKeep, rank, nForces);
+        launchK(compactExtKernel, grid(nForces * kExtF4), kThreads, 0, s, d.fExt, extTmp, d.fKeep, rank, nForces);
         cudaMemcpyAsync(d.fExt, extTmp, sizeof(real4) * static_cast<size_t>(nForces) * kExtF4,
                         cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(d.ctr + C_FORCES, d.ctr + C_TMP, sizeof(int), cudaMemcpyDeviceToDevice, s);
@@ -192,7 +208,7 @@ void launchRelocateWorlds(const Dev &d, int nOld, int nNew, int nForces, const i
 
 void launchListPositions(const Dev &d, int nBodies, cudaStream_t s) {
     if (nBodies > 0) {
-        ++launchCount(); listPosKernel<<<grid(nBodies), kThreads, 0, s>>>(d, nBodies);
+        ++launchCount(); launchK(listPosKernel, grid(nBodies), kThreads, 0, s, d, nBodies);
     }
 }
 

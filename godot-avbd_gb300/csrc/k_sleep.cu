@@ -35,6 +35,8 @@ __device__ __forceinline__ int2 pairBodies(const Dev &d, int k) {
 // ---- broad-phase wake-up ----
 
 __global__ void wakeResetKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= d.ctr[C_WORLDS])
         return;
@@ -50,6 +52,8 @@ __device__ __forceinline__ bool touchesSleeper(const Dev &d, int k, int2 &ab) {
 }
 
 __global__ void wakeFlagKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= d.ctr[C_PAIRS])
         return;
@@ -58,6 +62,8 @@ __global__ void wakeFlagKernel(Dev d) {
 }
 
 __global__ void wakeScatterKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= d.ctr[C_PAIRS])
         return;
@@ -73,6 +79,8 @@ __global__ void wakeScatterKernel(Dev d) {
 
 // wakeSleeperPair over one world's compacted pairs, in key order.
 __global__ void wakeWalkKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= d.ctr[C_WORLDS])
         return;
@@ -90,6 +98,8 @@ __global__ void wakeWalkKernel(Dev d) {
 // ---- wake pass over the adjacency ----
 
 __global__ void wakeNeighboursKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= d.ctr[C_BODIES] || d.meta[g].x < 0 || !d.sleep[g].x || sleepMode(d, g) != 1)
         return;
@@ -111,6 +121,8 @@ __device__ __forceinline__ bool islandMember(const Dev &d, int g) {
 }
 
 __global__ void islandInitKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= d.ctr[C_BODIES])
         return;
@@ -151,6 +163,8 @@ __device__ __forceinline__ void unite(const Dev &d, int a, int b) {
 }
 
 __global__ void islandUnionKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nm = d.ctr[C_LIVE], nf = d.ctr[C_FORCES];
     if (i < nm) {
@@ -163,6 +177,8 @@ __global__ void islandUnionKernel(Dev d) {
 }
 
 __global__ void islandAggregateKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= d.ctr[C_BODIES] || d.island[g] < 0)
         return;
@@ -174,6 +190,8 @@ __global__ void islandAggregateKernel(Dev d) {
 }
 
 __global__ void islandApplyKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= d.ctr[C_BODIES] || d.island[g] < 0)
         return;
@@ -192,19 +210,19 @@ __global__ void islandApplyKernel(Dev d, StepParams p) {
 } // namespace
 
 void launchSleepWakePairs(const Dev &d, cudaStream_t s) {
-    ++launchCount(); wakeResetKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
-    ++launchCount(); wakeFlagKernel<<<grid(d.PP), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(wakeResetKernel, grid(d.WW), kThreads, 0, s, d);
+    ++launchCount(); launchK(wakeFlagKernel, grid(d.PP), kThreads, 0, s, d);
     scanExclusive(d.sleepRank, d.sleepRank, d.PP, d.ctr + C_PAIRS, nullptr, d.scanScratch, s);
-    ++launchCount(); wakeScatterKernel<<<grid(d.PP), kThreads, 0, s>>>(d);
-    ++launchCount(); wakeWalkKernel<<<grid(d.WW), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(wakeScatterKernel, grid(d.PP), kThreads, 0, s, d);
+    ++launchCount(); launchK(wakeWalkKernel, grid(d.WW), kThreads, 0, s, d);
 }
 
 void launchSleepSelect(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); wakeNeighboursKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
-    ++launchCount(); islandInitKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
-    ++launchCount(); islandUnionKernel<<<grid(d.MM + d.FF), kThreads, 0, s>>>(d);
-    ++launchCount(); islandAggregateKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
-    ++launchCount(); islandApplyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+    ++launchCount(); launchK(wakeNeighboursKernel, grid(d.NB), kThreads, 0, s, d, p);
+    ++launchCount(); launchK(islandInitKernel, grid(d.NB), kThreads, 0, s, d);
+    ++launchCount(); launchK(islandUnionKernel, grid(d.MM + d.FF), kThreads, 0, s, d);
+    ++launchCount(); launchK(islandAggregateKernel, grid(d.NB), kThreads, 0, s, d);
+    ++launchCount(); launchK(islandApplyKernel, grid(d.NB), kThreads, 0, s, d, p);
 }
 
 } // namespace avbdg

@@ -502,6 +502,8 @@ __device__ __forceinline__ void stampsAt(Dev d, StepParams p, int mixedOnly, int
 }
 
 __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
         stampsAt(d, p, mixedOnly, m);
@@ -619,7 +621,7 @@ __device__ __forceinline__ void dualAt(const Dev &d, const StepParams &p, real d
 }
 
 template <bool STAMPS, bool ARM>
-__global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, real decay) { // 512: largest tuned block
+__global__ void __launch_bounds__(512) dualKernel(Dev d, StepParams p, real decay) { pdlWait(); pdlTrigger(); // 512: largest tuned block
     const int live = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < live; m += gridDim.x * blockDim.x)
         dualAt<STAMPS, ARM>(d, p, decay, m);
@@ -714,6 +716,8 @@ __device__ __noinline__ void jointStamp(const Dev &d, const StepParams &p, int f
 }
 
 __global__ void forceDualKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= d.ctr[C_FORCES])
         return;
@@ -874,6 +878,8 @@ __device__ __forceinline__ void colourPassAt(const Dev &d, const StepParams &p, 
 // over its list, a grid barrier after each but the last non-empty one. Every block reads the same
 // counts (nothing writes them during the sweep), so all blocks skip the same empty colours.
 __global__ void __launch_bounds__(kSolveThreads) colourSweepKernel(Dev d, StepParams p, int armsFromDual) {
+    pdlWait();
+    pdlTrigger();
     int last = -1;
     for (int c = 0; c < kMaxColours; c++)
         if (d.colourCount[c] > 0)
@@ -940,6 +946,8 @@ __device__ __forceinline__ void solveAt(const Dev &d, const StepParams &p, int g
 template <bool FORCES>
 __global__ void AVBDG_SOLVE_BOUNDS
         overflowSolveKernel(const __grid_constant__ Dev d, const __grid_constant__ StepParams p, int inPlace) {
+    pdlWait();
+    pdlTrigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g < d.ctr[C_BODIES])
         solveAt<FORCES>(d, p, g, inPlace);
@@ -970,6 +978,8 @@ __device__ __forceinline__ int worldOfTile(const int *pre, int nWorlds, int t) {
 
 template <bool ARM>
 __global__ void __launch_bounds__(kQueueThreads, 4) roundQueueKernel(Dev d, StepParams p, QueueRounds qr) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int sTile, sOk;
     const int nWorlds = d.ctr[C_WORLDS];
     const int ts = d.ctr[C_QSOLVE], td = d.ctr[C_QDUAL];
@@ -1039,12 +1049,16 @@ __global__ void __launch_bounds__(kQueueThreads, 4) roundQueueKernel(Dev d, Step
 // Each live manifold into its world's group (the order inside a group does not matter: every
 // manifold's dual reads and writes only its own state and its bodies' stamp entries).
 __global__ void worldManCountKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
         atomicAdd(&d.wManStart[d.meta[d.live.ab[m].x].x], 1);
 }
 
 __global__ void worldManFillKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_LIVE];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
         const int w = d.meta[d.live.ab[m].x].x;
@@ -1055,6 +1069,8 @@ __global__ void worldManFillKernel(Dev d) {
 // Chunks of each world's solve and dual phases (at least one each, so every phase of every world
 // has a tile that advances its stage), zero past the last world; the stages start at zero.
 __global__ void queueChunksKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int nWorlds = d.ctr[C_WORLDS];
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w > d.WW)
@@ -1073,6 +1089,8 @@ __global__ void queueChunksKernel(Dev d) {
 }
 
 __global__ void overflowApplyKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
@@ -1095,6 +1113,8 @@ __device__ __forceinline__ void maskLocked(int locks, f3 &v) {
 
 // Solver::warmstartBody (solver_solve.cpp:109-142).
 __global__ void warmstartKernel(Dev d, StepParams p) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
@@ -1134,6 +1154,8 @@ __global__ void warmstartKernel(Dev d, StepParams p) {
 
 // Solver::finishBody (solver_solve.cpp:146-176), idle sleep disabled.
 __global__ void finishKernel(Dev d, StepParams p, int idle) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0)
@@ -1168,6 +1190,8 @@ __global__ void finishKernel(Dev d, StepParams p, int idle) {
 // ---- update set and colouring (solver_solve.cpp:263-424) ----
 
 __global__ void contactOnlyInitKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n)
@@ -1194,6 +1218,8 @@ __global__ void contactOnlyInitKernel(Dev d) {
 }
 
 __global__ void contactOnlyMarkKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= d.ctr[C_FORCES])
         return;
@@ -1229,6 +1255,8 @@ constexpr int kColourThreads = 512;
 // Worlds that no force touches hold only contact-only bodies, which go to the overflow colour
 // whatever their greedy colour, so they are not coloured at all (unless every body is coloured).
 __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int everyWorld) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int stride = gridDim.x * blockDim.x;
     volatile int *errors = d.ctr + C_ERRORS;
@@ -1268,6 +1296,8 @@ __global__ void __launch_bounds__(kColourThreads) colourFlowKernel(Dev d, int ev
 }
 
 __global__ void colourListKernel(Dev d, int contactOnlyOverflow) {
+    pdlWait();
+    pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g))
@@ -1298,8 +1328,8 @@ static int queueGridMax();
 
 void launchContactOnly(const Dev &d, cudaStream_t s) {
     cudaMemsetAsync(d.wColour, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
-    ++launchCount(); contactOnlyInitKernel<<<grid(d.NB), kThreads, 0, s>>>(d);
-    ++launchCount(); contactOnlyMarkKernel<<<grid(d.FF), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(contactOnlyInitKernel, grid(d.NB), kThreads, 0, s, d);
+    ++launchCount(); launchK(contactOnlyMarkKernel, grid(d.FF), kThreads, 0, s, d);
 }
 
 static int g_colourBlocks = 0;
@@ -1363,19 +1393,19 @@ void launchColour(const Dev &d, bool needGreedy, bool everyWorld, cudaStream_t s
 
 void launchColourLists(const Dev &d, int contactOnlyOverflow, cudaStream_t s) {
     cudaMemsetAsync(d.colourCount, 0, sizeof(int) * (kMaxColours + 1), s);
-    ++launchCount(); colourListKernel<<<grid(d.NB), kThreads, 0, s>>>(d, contactOnlyOverflow);
+    ++launchCount(); launchK(colourListKernel, grid(d.NB), kThreads, 0, s, d, contactOnlyOverflow);
 }
 
 void launchWarmstartBodies(const Dev &d, const StepParams &p, cudaStream_t s) {
-    ++launchCount(); warmstartKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+    ++launchCount(); launchK(warmstartKernel, grid(d.NB), kThreads, 0, s, d, p);
 }
 
 void launchFinishBodies(const Dev &d, const StepParams &p, bool idle, cudaStream_t s) {
-    ++launchCount(); finishKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p, idle ? 1 : 0);
+    ++launchCount(); launchK(finishKernel, grid(d.NB), kThreads, 0, s, d, p, idle ? 1 : 0);
 }
 
 void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_t s) {
-    ++launchCount(); stampsKernel<<<residentGrid(stampsKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d, p, mixedOnly ? 1 : 0);
+    ++launchCount(); launchK(stampsKernel, residentGrid(stampsKernel, kThreads, grid(d.MM)), kThreads, 0, s, d, p, mixedOnly ? 1 : 0);
 }
 
 void launchColourSweep(const Dev &d, const StepParams &p, bool armsFromDual, cudaStream_t s) {
@@ -1394,9 +1424,9 @@ void launchColourSweep(const Dev &d, const StepParams &p, bool armsFromDual, cud
 void launchOverflowSolve(const Dev &d, const StepParams &p, bool inPlace, bool forces, int block, cudaStream_t s) {
     ++launchCount();
     if (forces)
-        overflowSolveKernel<true><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
+        launchK(overflowSolveKernel<true>, divUp(d.NB, block), block, 0, s, d, p, inPlace ? 1 : 0);
     else
-        overflowSolveKernel<false><<<divUp(d.NB, block), block, 0, s>>>(d, p, inPlace ? 1 : 0);
+        launchK(overflowSolveKernel<false>, divUp(d.NB, block), block, 0, s, d, p, inPlace ? 1 : 0);
 }
 
 static int g_queueBlocks = 0;
@@ -1418,10 +1448,10 @@ void launchRoundQueue(const Dev &d, const StepParams &p, const QueueRounds &qr, 
     const int cap = static_cast<int>(static_cast<size_t>(d.WW) + 1);
     cudaMemsetAsync(d.wManStart, 0, sizeof(int) * static_cast<size_t>(cap), s);
     cudaMemsetAsync(d.wManFill, 0, sizeof(int) * static_cast<size_t>(d.WW), s);
-    ++launchCount(); worldManCountKernel<<<residentGrid(worldManCountKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(worldManCountKernel, residentGrid(worldManCountKernel, kThreads, grid(d.MM)), kThreads, 0, s, d);
     scanExclusive(d.wManStart, d.wManStart, cap, nullptr, nullptr, d.scanScratch, s);
-    ++launchCount(); worldManFillKernel<<<residentGrid(worldManFillKernel, kThreads, grid(d.MM)), kThreads, 0, s>>>(d);
-    ++launchCount(); queueChunksKernel<<<divUp(cap, kThreads), kThreads, 0, s>>>(d);
+    ++launchCount(); launchK(worldManFillKernel, residentGrid(worldManFillKernel, kThreads, grid(d.MM)), kThreads, 0, s, d);
+    ++launchCount(); launchK(queueChunksKernel, divUp(cap, kThreads), kThreads, 0, s, d);
     scanExclusive(d.qPre, d.qPre, cap, nullptr, d.ctr + C_QSOLVE, d.scanScratch, s);
     scanExclusive(d.qPre + cap, d.qPre + cap, cap, nullptr, d.ctr + C_QDUAL, d.scanScratch, s);
     cudaMemsetAsync(d.qTicket, 0, sizeof(unsigned), s);
@@ -1437,13 +1467,13 @@ void launchRoundQueue(const Dev &d, const StepParams &p, const QueueRounds &qr, 
 
 void launchOverflowApply(const Dev &d, const StepParams &p, cudaStream_t s) {
     ++launchCount();
-    overflowApplyKernel<<<grid(d.NB), kThreads, 0, s>>>(d, p);
+    launchK(overflowApplyKernel, grid(d.NB), kThreads, 0, s, d, p);
 }
 
 template <bool STAMPS, bool ARM>
 static void dualLaunch(const Dev &d, const StepParams &p, real decay, int block, cudaStream_t s) {
     const int blocks = residentGrid(dualKernel<STAMPS, ARM>, block, divUp(d.MM, block));
-    dualKernel<STAMPS, ARM><<<blocks, block, 0, s>>>(d, p, decay);
+    launchK(dualKernel<STAMPS, ARM>, blocks, block, 0, s, d, p, decay);
 }
 
 void launchDual(const Dev &d, const StepParams &p, bool stamps, real decay, int block, cudaStream_t s) {
@@ -1457,7 +1487,7 @@ void launchDual(const Dev &d, const StepParams &p, bool stamps, real decay, int 
 void launchForceDual(const Dev &d, const StepParams &p, bool forces, cudaStream_t s) {
     if (!forces)
         return;
-    ++launchCount(); forceDualKernel<<<grid(d.FF), kThreads, 0, s>>>(d, p);
+    ++launchCount(); launchK(forceDualKernel, grid(d.FF), kThreads, 0, s, d, p);
 }
 
 } // namespace avbdg

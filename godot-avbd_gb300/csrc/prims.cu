@@ -61,6 +61,8 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int *smemWarp, int &tot
 }
 
 __global__ void scanReduceKernel(const int *in, int capacity, const int *d_n, int *blockSums) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int warpSums[kScanThreads / 32];
     const int n = loadCount(d_n, capacity);
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -78,6 +80,8 @@ __global__ void scanReduceKernel(const int *in, int capacity, const int *d_n, in
 }
 
 __global__ void scanTopKernel(int *blockSums, int numBlocks, int *d_total) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int warpSums[kTopThreads / 32];
     const int per = (numBlocks + kTopThreads - 1) / kTopThreads;
     const int first = threadIdx.x * per;
@@ -105,6 +109,8 @@ __global__ void scanTopKernel(int *blockSums, int numBlocks, int *d_total) {
 // write, so `in` may alias `out`), exactly the prefixes the three-launch form writes.
 __global__ void __launch_bounds__(kSmallThreads) scanSmallKernel(const int *in, int *out, int capacity,
                                                                  const int *d_n, int *d_total) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int warpSums[kSmallThreads / 32];
     const int n = loadCount(d_n, capacity);
     const int base = threadIdx.x * kSmallItems;
@@ -130,6 +136,8 @@ __global__ void __launch_bounds__(kSmallThreads) scanSmallKernel(const int *in, 
 }
 
 __global__ void scanDownKernel(const int *in, int *out, int capacity, const int *d_n, const int *blockSums) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int warpSums[kScanThreads / 32];
     const int n = loadCount(d_n, capacity);
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
@@ -163,6 +171,8 @@ constexpr int kRadixBins = 256;
 
 __global__ void radixHistKernel(const uint64_t *keys, int capacity, const int *d_n, int shift, uint32_t mask,
                                 int numBlocks, int *hist) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int h[kRadixBins];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -180,6 +190,8 @@ __global__ void radixHistKernel(const uint64_t *keys, int capacity, const int *d
 __global__ void radixScatterKernel(const uint64_t *keysIn, const uint32_t *valsIn, uint64_t *keysOut,
                                    uint32_t *valsOut, int capacity, const int *d_n, int shift, uint32_t mask,
                                    int numBlocks, const int *offsets) {
+    pdlWait();
+    pdlTrigger();
     __shared__ int running[kRadixBins];
     __shared__ int warpCount[kRadixThreads / 32][kRadixBins];
     __shared__ int roundTotal[kRadixBins];
@@ -232,6 +244,8 @@ __global__ void radixScatterKernel(const uint64_t *keysIn, const uint32_t *valsI
 
 template <typename T>
 __global__ void copyKernel(const T *src, T *dst, int capacity, const int *d_n) {
+    pdlWait();
+    pdlTrigger();
     const int n = loadCount(d_n, capacity);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         dst[i] = src[i];
@@ -250,6 +264,8 @@ constexpr int kBigTile = 2048;
 template <typename T>
 __global__ void segSmallKernel(T *data, const int *start, int segCapacity, const int *d_segments, int *longList,
                                int *longCount) {
+    pdlWait();
+    pdlTrigger();
     const int ns = loadCount(d_segments, segCapacity);
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         const int b = start[s], e = start[s + 1];
@@ -274,6 +290,8 @@ __global__ void segSmallKernel(T *data, const int *start, int segCapacity, const
 
 template <typename T>
 __global__ void segMidKernel(T *data, const int *start, const int *longList, const int *longCount) {
+    pdlWait();
+    pdlTrigger();
     extern __shared__ unsigned char smemRaw[];
     T *buf = reinterpret_cast<T *>(smemRaw);
     const int nl = *longCount;
@@ -298,6 +316,8 @@ __global__ void segMidKernel(T *data, const int *start, const int *longList, con
 
 template <typename T>
 __global__ void segBigCopyKernel(const T *data, T *tmp, const int *start, const int *longList, const int *longCount) {
+    pdlWait();
+    pdlTrigger();
     const int nl = *longCount;
     for (int k = 0; k < nl; k++) {
         const int s = longList[k];
@@ -311,6 +331,8 @@ __global__ void segBigCopyKernel(const T *data, T *tmp, const int *start, const 
 
 template <typename T>
 __global__ void segBigRankKernel(T *data, const T *tmp, const int *start, const int *longList, const int *longCount) {
+    pdlWait();
+    pdlTrigger();
     __shared__ T tile[kBigTile];
     const int nl = *longCount;
     for (int k = 0; k < nl; k++) {
@@ -354,14 +376,14 @@ size_t radixScratchBytes(int capacity) {
 void scanExclusive(const int *in, int *out, int capacity, const int *d_n, int *d_total, void *scratch,
                    cudaStream_t stream) {
     if (capacity <= kSmallScanCap) {
-        ++launchCount(); scanSmallKernel<<<1, kSmallThreads, 0, stream>>>(in, out, capacity, d_n, d_total);
+        ++launchCount(); launchK(scanSmallKernel, 1, kSmallThreads, 0, stream, in, out, capacity, d_n, d_total);
         return;
     }
     const int blocks = divUp(capacity > 0 ? capacity : 1, kScanTile);
     int *blockSums = static_cast<int *>(scratch);
-    ++launchCount(); scanReduceKernel<<<blocks, kScanThreads, 0, stream>>>(in, capacity, d_n, blockSums);
-    ++launchCount(); scanTopKernel<<<1, kTopThreads, 0, stream>>>(blockSums, blocks, d_total);
-    ++launchCount(); scanDownKernel<<<blocks, kScanThreads, 0, stream>>>(in, out, capacity, d_n, blockSums);
+    ++launchCount(); launchK(scanReduceKernel, blocks, kScanThreads, 0, stream, in, capacity, d_n, blockSums);
+    ++launchCount(); launchK(scanTopKernel, 1, kTopThreads, 0, stream, blockSums, blocks, d_total);
+    ++launchCount(); launchK(scanDownKernel, blocks, kScanThreads, 0, stream, in, out, capacity, d_n, blockSums);
 }
 
 void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_t *valuesAlt, int capacity,
@@ -376,9 +398,9 @@ void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_
     for (int bit = beginBit; bit < endBit; bit += 8) {
         const int bits = endBit - bit < 8 ? endBit - bit : 8;
         const uint32_t mask = (1u << bits) - 1u;
-        ++launchCount(); radixHistKernel<<<blocks, kRadixThreads, 0, stream>>>(kin, capacity, d_n, bit, mask, blocks, hist);
+        ++launchCount(); launchK(radixHistKernel, blocks, kRadixThreads, 0, stream, kin, capacity, d_n, bit, mask, blocks, hist);
         scanExclusive(hist, hist, histN, nullptr, nullptr, scanScratch, stream);
-        ++launchCount(); radixScatterKernel<<<blocks, kRadixThreads, 0, stream>>>(kin, vin, kout, vout, capacity, d_n, bit, mask,
+        ++launchCount(); launchK(radixScatterKernel, blocks, kRadixThreads, 0, stream, kin, vin, kout, vout, capacity, d_n, bit, mask,
                                                                  blocks, hist);
         uint64_t *tk = kin;
         kin = kout;
@@ -390,10 +412,10 @@ void radixSortPairs(uint64_t *keys, uint32_t *values, uint64_t *keysAlt, uint32_
     }
     if (passes & 1) {
         const int grid = divUp(capacity > 0 ? capacity : 1, 256) < 1184 ? divUp(capacity > 0 ? capacity : 1, 256) : 1184;
-        ++launchCount(); copyKernel<uint64_t><<<grid, 256, 0, stream>>>(kin, keys, capacity, d_n);
+        ++launchCount(); launchK(copyKernel<uint64_t>, grid, 256, 0, stream, kin, keys, capacity, d_n);
         if (values) {
             ++launchCount();
-            copyKernel<uint32_t><<<grid, 256, 0, stream>>>(vin, values, capacity, d_n);
+            launchK(copyKernel<uint32_t>, grid, 256, 0, stream, vin, values, capacity, d_n);
         }
     }
 }
@@ -403,13 +425,13 @@ static void segmentedSort(T *data, const int *start, int segCapacity, const int 
                           int *longCount, T *tmp, cudaStream_t stream) {
     cudaMemsetAsync(longCount, 0, sizeof(int), stream);
     const int grid = divUp(segCapacity > 0 ? segCapacity : 1, 256);
-    ++launchCount(); segSmallKernel<T><<<grid < 4096 ? grid : 4096, 256, 0, stream>>>(data, start, segCapacity, d_segments, longList,
+    ++launchCount(); launchK(segSmallKernel<T>, grid < 4096 ? grid : 4096, 256, 0, stream, data, start, segCapacity, d_segments, longList,
                                                                    longCount);
     const size_t smem = kMidSegCap * sizeof(T);
-    ++launchCount(); segMidKernel<T><<<152, kMidSegThreads, smem, stream>>>(data, start, longList, longCount);
+    ++launchCount(); launchK(segMidKernel<T>, 152, kMidSegThreads, smem, stream, data, start, longList, longCount);
     if (tmp) {
-        ++launchCount(); segBigCopyKernel<T><<<kBigBlocks, 256, 0, stream>>>(data, tmp, start, longList, longCount);
-        ++launchCount(); segBigRankKernel<T><<<kBigBlocks, 256, 0, stream>>>(data, tmp, start, longList, longCount);
+        ++launchCount(); launchK(segBigCopyKernel<T>, kBigBlocks, 256, 0, stream, data, tmp, start, longList, longCount);
+        ++launchCount(); launchK(segBigRankKernel<T>, kBigBlocks, 256, 0, stream, data, tmp, start, longList, longCount);
     }
 }
 

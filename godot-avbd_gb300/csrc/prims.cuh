@@ -6,9 +6,48 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstdlib>
+#include <utility>
 #include <cuda_runtime.h>
 
 namespace avbdg {
+
+// Programmatic dependent launch. The step is a chain of dependent kernels, most of them a few
+// microseconds long on small stores, so the gap between one kernel's drain and the next one's
+// start is a large part of a step. Every kernel of the library is launched with the programmatic
+// stream serialization attribute (launchK) and begins with pdlWait() then pdlTrigger(): the next
+// kernel's blocks may be scheduled as soon as every block of the current one has started, and each
+// waits in pdlWait() until the kernel before it has completed and its writes are visible. So no
+// kernel touches memory before its predecessor is done: the order of the step is unchanged.
+// (In a kernel launched without the attribute both are no-ops.)
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// AVBDG_NO_PDL=1: plain stream order between kernels (read once per process).
+inline bool pdlEnabled() {
+    static const bool on = [] {
+        const char *v = std::getenv("AVBDG_NO_PDL");
+        return !(v && v[0] == '1');
+    }();
+    return on;
+}
+
+// kernel<<<grid, block, smem, stream>>>(args...) with the programmatic serialization attribute.
+template <typename... KArgs, typename... Args>
+inline void launchK(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                    Args &&...args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdlEnabled() ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Scratch sizes the primitives need for `capacity` elements.
 size_t scanScratchBytes(int capacity);

@@ -21,18 +21,24 @@ int sortFail(int code, const std::string &msg) {
 }
 
 __global__ void uniqueFlagKernel(const uint64_t *keys, int n, int *flags) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n)
         flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
 }
 
 __global__ void uniqueScatterKernel(const uint64_t *keys, int n, const int *flags, const int *rank, uint64_t *out) {
+    pdlWait();
+    pdlTrigger();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && flags[i])
         out[rank[i]] = keys[i];
 }
 
 __global__ void copyBackKernel(const uint64_t *src, uint64_t *dst, const int *count) {
+    pdlWait();
+    pdlTrigger();
     const int n = *count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         dst[i] = src[i];
@@ -52,10 +58,10 @@ struct SortScratch {
 void enqueueSortUnique(uint64_t *keys, int n, int bits, const SortScratch &s, cudaStream_t stream) {
     radixSortPairs(keys, nullptr, s.keysAlt, nullptr, n, nullptr, 0, bits, s.radix, stream);
     const int grid = divUp(n, 256);
-    uniqueFlagKernel<<<grid, 256, 0, stream>>>(keys, n, s.flags);
+    launchK(uniqueFlagKernel, grid, 256, 0, stream, keys, n, s.flags);
     scanExclusive(s.flags, s.ranks, n, nullptr, s.count, s.scan, stream);
-    uniqueScatterKernel<<<grid, 256, 0, stream>>>(keys, n, s.flags, s.ranks, s.keysAlt);
-    copyBackKernel<<<grid < 1184 ? grid : 1184, 256, 0, stream>>>(s.keysAlt, keys, s.count);
+    launchK(uniqueScatterKernel, grid, 256, 0, stream, keys, n, s.flags, s.ranks, s.keysAlt);
+    launchK(copyBackKernel, grid < 1184 ? grid : 1184, 256, 0, stream, s.keysAlt, keys, s.count);
 }
 
 int checkArgs(uint64_t *keys, int n, int bits, int *uniqueCount) {
