@@ -764,6 +764,13 @@ __global__ void forceDualKernel(Dev d, StepParams p) {
 
 __device__ __forceinline__ int nForcesDev(const Dev &d) { return d.ctr[C_FORCES]; }
 
+// Body g has a force (joint or spring) among its adjacency entries; forces come first in a body's
+// entries, so its first entry decides.
+__device__ __forceinline__ bool bodyHasForce(const Dev &d, int g, int nf) {
+    const int e0 = d.adjStart[g];
+    return nf > 0 && e0 < d.adjStart[g + 1] && static_cast<int>(d.adjSeq[e0]) < nf;
+}
+
 // Assemble body g's block from its adjacency; manifold terms from stamps (Jacobi) or recomputed
 // from the current poses (Gauss-Seidel).
 // Without FORCES (a store with no non-manifold force) the force branch is compiled out, so the
@@ -779,7 +786,7 @@ template <bool RECOMPUTE, bool FORCES = true, bool RO = true>
 __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int g, Blk &blk, int armsFromDual = 0) {
     const int nf = nForcesDev(d);
     const int e1 = d.adjStart[g + 1];
-    if (!RECOMPUTE && !FORCES && nf == 0) {
+    if (!RECOMPUTE && !bodyHasForce(d, g, nf)) {
         // Every entry is a manifold stamped for this body, stored at the entry itself; two records
         // are loaded before either is added (the sums keep the entry order).
         int e = d.adjStart[g];
@@ -896,7 +903,8 @@ __global__ void __launch_bounds__(kSolveThreads) colourSweepKernel(Dev d, StepPa
     }
 }
 
-// An overflow body's step: in place (no forces) or into dLin/dAng for overflowApplyKernel.
+// An overflow body's step: in place, or (a body with a force, in a store with forces) into
+// dLin/dAng for overflowApplyKernel.
 __device__ __forceinline__ void applyOverflow(const Dev &d, const StepParams &p, int g, int inPlace, f3 dl, f3 da) {
     if (inPlace) {
         const real4 x4 = d.x[g];
@@ -911,8 +919,8 @@ __device__ __forceinline__ void applyOverflow(const Dev &d, const StepParams &p,
 // solve()'s pivoted fallback for a body whose plain LDLT failed, out of line so the common path
 // keeps its registers; the kernel's parameters are grid constants, so the call passes their
 // addresses without copying them. The block is assembled again (the same floats: it reads the
-// stamps and this body's own pose, which nothing changes during the pass; with forces, poses are
-// not written during the pass at all).
+// stamps, this body's own pose, which it has not written yet, and for a body with a force its
+// partners' poses, which defer their updates to the apply pass).
 template <bool FORCES, bool RO = true>
 __device__ __noinline__ void fallbackSolve(const Dev &d, const StepParams &p, int g, int inPlace) {
     Blk blk = bodyBlock(d, p, g);
@@ -923,10 +931,16 @@ __device__ __noinline__ void fallbackSolve(const Dev &d, const StepParams &p, in
 
 // One overflow body's block-Jacobi solve (the body of overflowSolveKernel), also run by the
 // round-loop tile queue (RO false there: the stamps are written in the same launch).
+// inPlace 0 (a store with forces): a body with a force of its own leaves its update to the apply
+// pass, because its force terms read its partners' poses, which must stay at the round's start
+// (every partner has the same force, so it defers too); any other body reads only its own pose and
+// its stamps, so it updates in place with the same floats.
 template <bool FORCES, bool RO = true>
 __device__ __forceinline__ void solveAt(const Dev &d, const StepParams &p, int g, int inPlace) {
     if (d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
         return;
+    if (!inPlace && !bodyHasForce(d, g, nForcesDev(d)))
+        inPlace = 1;
     Blk blk = bodyBlock(d, p, g);
     assemble<false, FORCES, RO>(d, p, g, blk);
     f3 dl, da;
@@ -1093,8 +1107,9 @@ __global__ void overflowApplyKernel(Dev d, StepParams p) {
     pdlTrigger();
     const int n = d.ctr[C_BODIES];
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
-        return;
+    if (g >= n || d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour ||
+        !bodyHasForce(d, g, nForcesDev(d)))
+        return; // bodies without a force were updated in place by the solve
     const real4 x4 = d.x[g];
     d.x[g] = f4(add(xyz(x4), scale(xyz(d.dLin[g]), p.jacobiRelax)), x4.w);
     d.q[g] = f4(qintegrate(asq(d.q[g]), scale(xyz(d.dAng[g]), p.jacobiRelax)));
@@ -1409,7 +1424,10 @@ void launchStamps(const Dev &d, const StepParams &p, bool mixedOnly, cudaStream_
 }
 
 void launchColourSweep(const Dev &d, const StepParams &p, bool armsFromDual, cudaStream_t s) {
-    const int want = divUp(d.NB, kSolveThreads), most = sweepGridMax();
+    // With contact-only bodies in the overflow colour, a coloured body has a force of its own and a
+    // force touches at most two bodies, so the grid (and its barrier) scales with the forces.
+    const int bound = p.contactOnlyOverflow && d.FF < d.NB / 2 ? 2 * d.FF : d.NB;
+    const int want = divUp(bound > 0 ? bound : 1, kSolveThreads), most = sweepGridMax();
     const int blocks = want < most ? want : most;
     cudaMemsetAsync(d.gridBar, 0, sizeof(unsigned), s);
     Dev dd = d;
