@@ -771,6 +771,59 @@ __device__ __forceinline__ bool bodyHasForce(const Dev &d, int g, int nf) {
     return nf > 0 && e0 < d.adjStart[g + 1] && static_cast<int>(d.adjSeq[e0]) < nf;
 }
 
+// One side of manifold m recomputed for coloured body g from the current poses (the same floats
+// as stampsKernel for that side, with the arms the colour pass may reuse), as a stamp record. The
+// record's adds (addStamp) are the ones of summing the side's accumulators into the block: its
+// symmetric blocks are summed entry by entry in the same order on both sides of the diagonal, so
+// their unique entries carry every value, and its right-hand sides are stored already signed.
+__device__ __forceinline__ StampRec recomputeSide(const Dev &d, const StepParams &p, int g, int m, int side,
+                                                  int armsFromDual) {
+    const ManifoldBuf L = d.live;
+    const int2 ab = L.ab[m];
+    const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
+    const real4 b04 = L.b0[m];
+    const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
+    const int n = L.count[m];
+    bool cached = false;
+    if (p.armCache && armsFromDual) {
+        const int o = side == 0 ? ab.y : ab.x;
+        cached = !(inUpdate(d, o) && d.colour[o] < d.colour[g]);
+    }
+    SharedAcc sh;
+    sh.lin = mzero();
+    sh.rhsLin = f3{0, 0, 0};
+    SideAcc sd;
+    zeroAcc(sd);
+    for (int c = 0; c < n; c++) {
+        const int ci = cslot(d, m, c);
+        f3 rAw, rBw;
+        if (cached) {
+            rAw = xyz(L.armA[ci]);
+            rBw = xyz(L.armB[ci]);
+        } else {
+            rAw = mul(A.rot, xyz(L.rA[ci]));
+            rBw = mul(B.rot, xyz(L.rB[ci]));
+            if (p.armCache) {
+                L.armA[ci] = f4(rAw, 0.0f);
+                L.armB[ci] = f4(rBw, 0.0f);
+            }
+        }
+        const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
+        const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
+        const f3 k = xyz(L.k[ci]);
+        f3 F = add(cmul(k, C), xyz(L.lam[ci]));
+        clampForce(F, b04.w);
+        real S[6];
+        basisHessianD(r0, r1, r2, k, S);
+        const f3 fw = add(add(scale(r0, F.x), scale(r1, F.y)), scale(r2, F.z));
+        stampShared(S, fw, sh);
+        stampContact(S, side == 0 ? rAw : rBw, fw, sd);
+    }
+    real4 rec[kStampF4];
+    storeStamp(rec, sh, sd, side == 0 ? 1.0f : -1.0f);
+    return StampRec{rec[0], rec[1], rec[2], rec[3], rec[4], rec[5], rec[6]};
+}
+
 // Assemble body g's block from its adjacency; manifold terms from stamps (Jacobi) or recomputed
 // from the current poses (Gauss-Seidel).
 // Without FORCES (a store with no non-manifold force) the force branch is compiled out, so the
@@ -810,54 +863,7 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
         const int m = seq - nf;
         const int side = adjInfoSide(__ldg(&d.adjInfo[e]));
         if (RECOMPUTE) {
-            // Same floats as stampsKernel for one side, summed straight into the block.
-            const ManifoldBuf L = d.live;
-            const int2 ab = L.ab[m];
-            const Pose A = loadPose(d, ab.x), B = loadPose(d, ab.y);
-            const real4 b04 = L.b0[m];
-            const f3 r0 = xyz(b04), r1 = xyz(L.b1[m]), r2 = xyz(L.b2[m]);
-            const int n = L.count[m];
-            bool cached = false;
-            if (p.armCache && armsFromDual) {
-                const int o = side == 0 ? ab.y : ab.x;
-                cached = !(inUpdate(d, o) && d.colour[o] < d.colour[g]);
-            }
-            SharedAcc sh;
-            sh.lin = mzero();
-            sh.rhsLin = f3{0, 0, 0};
-            SideAcc sd;
-            zeroAcc(sd);
-            for (int c = 0; c < n; c++) {
-                const int ci = cslot(d, m, c);
-                f3 rAw, rBw;
-                if (cached) {
-                    rAw = xyz(L.armA[ci]);
-                    rBw = xyz(L.armB[ci]);
-                } else {
-                    rAw = mul(A.rot, xyz(L.rA[ci]));
-                    rBw = mul(B.rot, xyz(L.rB[ci]));
-                    if (p.armCache) {
-                        L.armA[ci] = f4(rAw, 0.0f);
-                        L.armB[ci] = f4(rBw, 0.0f);
-                    }
-                }
-                const f3 bracket = sub(add(sub(A.dLin, B.dLin), cross(A.dAng, rAw)), cross(B.dAng, rBw));
-                const f3 C = contactError(p, xyz(L.C0[ci]), bracket, r0, r1, r2);
-                const f3 k = xyz(L.k[ci]);
-                f3 F = add(cmul(k, C), xyz(L.lam[ci]));
-                clampForce(F, b04.w);
-                real S[6];
-                basisHessianD(r0, r1, r2, k, S);
-                const f3 fw = add(add(scale(r0, F.x), scale(r1, F.y)), scale(r2, F.z));
-                stampShared(S, fw, sh);
-                stampContact(S, side == 0 ? rAw : rBw, fw, sd);
-            }
-            const real sgn = side == 0 ? 1.0f : -1.0f;
-            blk.lin = madd(blk.lin, sh.lin);
-            blk.ang = madd(blk.ang, sd.ang);
-            blk.crs = madd(blk.crs, sd.crs);
-            blk.rl = add(blk.rl, scale(sh.rhsLin, sgn));
-            blk.ra = add(blk.ra, scale(sd.rhsAng, sgn));
+            addStamp(blk, recomputeSide(d, p, g, m, side, armsFromDual));
         } else {
             addStamp(blk, loadStampAs<RO>(d.stamps + static_cast<size_t>(e) * kStampF4));
         }
