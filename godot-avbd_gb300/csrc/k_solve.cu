@@ -297,13 +297,28 @@ __device__ __forceinline__ Cone clampForce(f3 &F, real mu) {
     return Cone{bounds, fs};
 }
 
+// A symmetric 3x3 sum kept as its unique entries (00, 01, 02, 11, 12, 22). Every term added to it
+// is symmetric, so the full matrix's two off-diagonal copies would take the same adds in the same
+// order; the stamp record stores only these six.
+struct Sym3 {
+    real v[6];
+};
+
+__device__ __forceinline__ Sym3 symZero() { return Sym3{{0, 0, 0, 0, 0, 0}}; }
+
+__device__ __forceinline__ void symAdd(Sym3 &a, const real t[6]) {
+    for (int i = 0; i < 6; i++)
+        a.v[i] = a.v[i] + t[i];
+}
+
 // Per-side accumulators of stampCached.
 struct SideAcc {
-    m3 ang, crs;
+    Sym3 ang;
+    m3 crs;
     f3 rhsAng;
 };
 struct SharedAcc {
-    m3 lin;
+    Sym3 lin;
     f3 rhsLin;
 };
 
@@ -335,18 +350,18 @@ __device__ __forceinline__ SideTerms sideTerms(const real S[6], f3 r, f3 fw) {
 __device__ __forceinline__ void stampContact(const real S[6], f3 r, f3 fw, SideAcc &acc) {
     const SideTerms t = sideTerms(S, r, fw);
     const real *h = t.h;
-    acc.ang = madd(acc.ang, mcols(f3{h[0], h[1], h[2]}, f3{h[1], h[3], h[4]}, f3{h[2], h[4], h[5]}));
+    symAdd(acc.ang, h);
     acc.crs = madd(acc.crs, t.rs);
     acc.rhsAng = add(acc.rhsAng, t.rc);
 }
 
 __device__ __forceinline__ void stampShared(const real S[6], f3 fw, SharedAcc &acc) {
-    acc.lin = madd(acc.lin, mcols(f3{S[0], S[1], S[2]}, f3{S[1], S[3], S[4]}, f3{S[2], S[4], S[5]}));
+    symAdd(acc.lin, S);
     acc.rhsLin = add(acc.rhsLin, fw);
 }
 
 __device__ __forceinline__ void zeroAcc(SideAcc &a) {
-    a.ang = mzero();
+    a.ang = symZero();
     a.crs = mzero();
     a.rhsAng = f3{0, 0, 0};
 }
@@ -438,10 +453,10 @@ __device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touche
 __device__ __forceinline__ void storeStamp(real4 *dst, const SharedAcc &sh, const SideAcc &sd, real side) {
     const f3 rl = scale(sh.rhsLin, side);
     const f3 ra = scale(sd.rhsAng, side);
-    dst[0] = mk4(sh.lin.c0.x, sh.lin.c0.y, sh.lin.c0.z, sh.lin.c1.y);
-    dst[1] = mk4(sh.lin.c1.z, sh.lin.c2.z, rl.x, rl.y);
-    dst[2] = mk4(rl.z, sd.ang.c0.x, sd.ang.c0.y, sd.ang.c0.z);
-    dst[3] = mk4(sd.ang.c1.y, sd.ang.c1.z, sd.ang.c2.z, ra.x);
+    dst[0] = mk4(sh.lin.v[0], sh.lin.v[1], sh.lin.v[2], sh.lin.v[3]);
+    dst[1] = mk4(sh.lin.v[4], sh.lin.v[5], rl.x, rl.y);
+    dst[2] = mk4(rl.z, sd.ang.v[0], sd.ang.v[1], sd.ang.v[2]);
+    dst[3] = mk4(sd.ang.v[3], sd.ang.v[4], sd.ang.v[5], ra.x);
     dst[4] = mk4(ra.y, ra.z, sd.crs.c0.x, sd.crs.c0.y);
     dst[5] = mk4(sd.crs.c0.z, sd.crs.c1.x, sd.crs.c1.y, sd.crs.c1.z);
     dst[6] = mk4(sd.crs.c2.x, sd.crs.c2.y, sd.crs.c2.z, 0.0f);
@@ -457,7 +472,7 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
     const real mu = b04.w;
     const int n = L.count[m];
     SharedAcc sh;
-    sh.lin = mzero();
+    sh.lin = symZero();
     sh.rhsLin = f3{0, 0, 0};
     SideAcc sa, sb;
     zeroAcc(sa);
@@ -540,7 +555,7 @@ __device__ __forceinline__ void dualAt(const Dev &d, const StepParams &p, real d
         driftUsable = L.armFlag[m] != 0 && length2(dA) <= p.armRebuild2 && length2(dB) <= p.armRebuild2;
     }
     SharedAcc sh;
-    sh.lin = mzero();
+    sh.lin = symZero();
     sh.rhsLin = f3{0, 0, 0};
     SideAcc sa, sb;
     zeroAcc(sa);
@@ -790,7 +805,7 @@ __device__ __forceinline__ StampRec recomputeSide(const Dev &d, const StepParams
         cached = !(inUpdate(d, o) && d.colour[o] < d.colour[g]);
     }
     SharedAcc sh;
-    sh.lin = mzero();
+    sh.lin = symZero();
     sh.rhsLin = f3{0, 0, 0};
     SideAcc sd;
     zeroAcc(sd);
