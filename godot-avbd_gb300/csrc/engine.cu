@@ -229,9 +229,16 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     {
         const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
         bool (*fits[kKinds])(int) = {dualBlockFits, solveBlockFits, narrowBlockFits, traverseBlockFits};
-        for (int k = 0; k < kKinds; k++)
+        int *base[kKinds] = {&tunedBase.dual, &tunedBase.solve, &tunedBase.narrow, &tunedBase.traverse};
+        for (int k = 0; k < kKinds; k++) {
             for (int c = 0; c < spaces[k]->count; c++)
                 tuneFits[k][c] = fits[k](spaces[k]->sizes[c]);
+            if (!fits[k](*base[k])) // a default above the kernel's launch bounds or registers
+                for (int c = 0; c < spaces[k]->count; c++)
+                    if (tuneFits[k][c])
+                        *base[k] = spaces[k]->sizes[c];
+        }
+        tuned = tunedBase;
     }
     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
     for (auto &e : ev)
@@ -1705,8 +1712,7 @@ void Engine::armTuning() {
 void Engine::configureTrial() {
     const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
     int *picks[kKinds] = {&tuned.dual, &tuned.solve, &tuned.narrow, &tuned.traverse};
-    const Tuned defaults;
-    const int fallback[kKinds] = {defaults.dual, defaults.solve, defaults.narrow, defaults.traverse};
+    const int fallback[kKinds] = {tunedBase.dual, tunedBase.solve, tunedBase.narrow, tunedBase.traverse};
     for (int k = 0; k < kKinds; k++) {
         const int c = tuneTrial % spaces[k]->count;
         *picks[k] = tuneFits[k][c] ? spaces[k]->sizes[c] : fallback[k];
@@ -1718,8 +1724,7 @@ void Engine::finishTrial() {
         return;
     const TuneSpace *spaces[kKinds] = {&kTuneDual, &kTuneSolve, &kTuneNarrow, &kTuneTraverse};
     int *picks[kKinds] = {&tuned.dual, &tuned.solve, &tuned.narrow, &tuned.traverse};
-    const Tuned defaults;
-    const int fallback[kKinds] = {defaults.dual, defaults.solve, defaults.narrow, defaults.traverse};
+    const int fallback[kKinds] = {tunedBase.dual, tunedBase.solve, tunedBase.narrow, tunedBase.traverse};
     for (int k = 0; k < kKinds; k++) {
         int best = -1;
         double bestMs = 0.0;

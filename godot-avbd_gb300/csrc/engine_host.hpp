@@ -156,6 +156,7 @@ private:
         int dual = 256, solve = 128, narrow = 256, traverse = 256;
     };
     Tuned tuned;
+    Tuned tunedBase; // the default sizes, each replaced by the largest candidate that launches if it does not
     static constexpr int kTuneDelay = 4, kTuneTrials = 8;
     bool tuneEnabled = true, tuning = false;
     int tuneTrial = 0;

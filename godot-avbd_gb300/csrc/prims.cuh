@@ -83,12 +83,20 @@ inline int residentGrid(K *kernel, int block, int want) {
     return residentGrid(reinterpret_cast<const void *>(kernel), block, 0, want);
 }
 
-// True when at least one block of `block` threads of `kernel` fits on an SM (registers and shared
-// memory): a launch with that block size can run.
+// True when a launch of `kernel` with `block` threads can run: the block is within the kernel's
+// launch bounds (its maxThreadsPerBlock, which the occupancy query does not check) and at least one
+// such block fits on an SM (registers and shared memory). A failed query's error is cleared here, so
+// the launch checks of a later step do not take it for a failed launch.
 template <typename K>
 inline bool blockFits(K *kernel, int block) {
+    cudaFuncAttributes attr{};
     int n = 0;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, 0) == cudaSuccess && n > 0;
+    if (cudaFuncGetAttributes(&attr, kernel) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return block <= attr.maxThreadsPerBlock && n > 0;
 }
 
 // Kernel attributes the primitives need (large dynamic shared memory); call before any capture.
