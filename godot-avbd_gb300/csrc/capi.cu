@@ -459,9 +459,9 @@ int avbdg_server_create(const avbdg_params *params, uint64_t budget_bytes, int m
         return failWith(AVBDG_ERR_CUDA, "no CUDA device: the GPU step has no CPU fallback");
     try {
         avbdg_server *s = new avbdg_server(p, budget_bytes, max_resident);
-        const int rc = s->server.engine().setParams(p);
+        const int rc = s->server.setParams(p);
         if (rc != AVBDG_OK) {
-            g_lastError = s->server.engine().error();
+            g_lastError = s->server.error();
             delete s;
             return rc;
         }

@@ -760,6 +760,17 @@ int Engine::removeWorlds(const std::vector<int> &ids) {
     return cudaCheck("removeWorlds");
 }
 
+int Engine::shrinkEmpty() {
+    if (!wBase.empty() || nBodies != 0)
+        return AVBDG_OK;
+    constexpr int nb = 64;
+    if (d.NB <= nb)
+        return AVBDG_OK;
+    clear();
+    allocate(nb, 8 * nb, std::min(d.FF, 64), 16 * nb, d.WW);
+    return cudaCheck("shrink");
+}
+
 void Engine::clear() {
     ctrFresh = false;
     cudaStreamSynchronize(stream);
@@ -1198,6 +1209,24 @@ int Engine::step() {
     if (nBodies == 0)
         return AVBDG_OK;
     return runPlan(planStep(0, 1, P.iterations));
+}
+
+int Engine::stepEnqueue() {
+    stepPending = false;
+    if (nBodies == 0)
+        return AVBDG_OK;
+    const int rc = enqueuePlan(planStep(0, 1, P.iterations));
+    pendingLaunches = launchCount() - launchBase;
+    stepPending = rc == AVBDG_OK;
+    return rc;
+}
+
+int Engine::stepFinish() {
+    if (!stepPending)
+        return AVBDG_OK;
+    stepPending = false;
+    launchBase = launchCount() - pendingLaunches; // launches of other stores in between are not this step's
+    return finishStep();
 }
 
 // Every buffer a step fills has at least 4x headroom over the last checked step's counts, so the

@@ -38,6 +38,9 @@ public:
     // dense body slots and are renumbered 0.. in order; their manifolds and forces are carried.
     int removeWorlds(const std::vector<int> &ids);
     void clear();
+    // A store with no worlds gives its device memory back down to the smallest capacities (64
+    // bodies); the next worlds grow it again. No effect on a store that holds worlds.
+    int shrinkEmpty();
 
     // Checks addBodies / addForces apply before touching the store (a world of `nb` bodies).
     static int validateBodies(int count, const avbdg_body_desc *descs, std::string &why);
@@ -57,6 +60,11 @@ public:
 
     // Enqueue one step of every world (Solver::step / Solver::stepInterleaved).
     int step();
+    // step() in two halves, for a caller that steps several stores at once on their own streams:
+    // stepEnqueue hands the step to this store's stream, stepFinish waits for it and checks its
+    // counters (growing the store as step() does). Nothing may change the store in between.
+    int stepEnqueue();
+    int stepFinish();
     int stepInterleaved(int substeps, int rounds);
     // `count` steps (substeps > 1: stepInterleaved(substeps, rounds)), queued back to back while the
     // store has room; each step's counters are still checked in order.
@@ -177,6 +185,8 @@ private:
     // Body state moves straight between the caller's (pageable) arrays and the device, where the
     // device reaches host memory through the host's page tables; else through pinned staging.
     bool roundQueue = false; // AVBDG_QUEUE=1: the round loop as one tile-queue launch where it applies
+    bool stepPending = false; // stepEnqueue ran, stepFinish has not
+    int pendingLaunches = 0;  // kernels the pending step launched
     bool directIo = false;
     int ensureIo(int count);
 

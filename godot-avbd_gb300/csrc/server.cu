@@ -1,5 +1,5 @@
 // Served form (host side): request queue, admission under a device byte budget, per-tick stepping
-// of every resident scene, retirement. See server.hpp.
+// of every resident scene in two stores (lanes), retirement. See server.hpp.
 
 #include "server.hpp"
 
@@ -37,10 +37,40 @@ int initialBodies(uint64_t budget, int worlds) {
 } // namespace
 
 Server::Server(const avbdg_params &params, uint64_t budgetBytes, int maxResidentScenes)
-    : eng(params, initialBodies(budgetBytes, std::max(1, std::min(maxResidentScenes, 1024))), 64,
-          std::max(1, std::min(maxResidentScenes, 1024))),
-      budget(budgetBytes), maxResident(std::max(1, maxResidentScenes)) {
-    eng.setByteLimit(budget);
+    : budget(budgetBytes), maxResident(std::max(1, maxResidentScenes)) {
+    const int worlds = std::max(1, std::min(maxResidentScenes, 1024));
+    // Each lane starts at no more than a sixteenth of the budget, so either one can grow to nearly
+    // all of it when its scenes need it.
+    const int nb = initialBodies(budgetBytes / 16, worlds);
+    for (auto &lane : lanes)
+        lane = std::make_unique<Lane>(params, nb, 64, worlds);
+    for (int l = 0; l < kLanes; l++)
+        limitLane(l);
+}
+
+int Server::setParams(const avbdg_params &p) {
+    for (auto &lane : lanes) {
+        const int rc = lane->eng.setParams(p);
+        if (rc != AVBDG_OK)
+            return engineFail(lane->eng, rc);
+    }
+    return AVBDG_OK;
+}
+
+int Server::residentCount() const {
+    int n = 0;
+    for (const auto &lane : lanes)
+        n += static_cast<int>(lane->resident.size());
+    return n;
+}
+
+void Server::limitLane(int lane) {
+    uint64_t other = 0;
+    for (int l = 0; l < kLanes; l++)
+        if (l != lane)
+            other += lanes[l]->eng.reservedBytes();
+    // A limit of 0 would mean none: a lane left no room keeps a one-byte limit (no growth).
+    lanes[lane]->eng.setByteLimit(budget > other + 1 ? budget - other : 1);
 }
 
 int Server::admit(int nb, const avbdg_body_desc *bodies, int nf, const avbdg_force_desc *forces, int steps,
@@ -70,27 +100,46 @@ int Server::admit(int nb, const avbdg_body_desc *bodies, int nf, const avbdg_for
     return AVBDG_OK;
 }
 
-// Arrival order, no overtaking: the head waits until a slot and its bytes are free.
+// Arrival order, no overtaking: the head waits until a slot and its bytes are free. A scene with
+// forces goes to lane 1, any other to lane 0. When the head's lane cannot grow because the other
+// lane's store holds the bytes and no scene, that store is shrunk and the head tried once more.
 int Server::admitQueued() {
+    bool shrunk = false;
     while (!queue.empty()) {
         Pending &p = queue.front();
-        if (static_cast<int>(resident.size()) >= maxResident || residentBytes + p.bytes > budget)
+        if (residentCount() >= maxResident || residentBytes + p.bytes > budget)
             break;
-        const int w = eng.addWorld();
-        if (w < 0)
-            break; // the store cannot grow now; retry next tick
-        int rc = eng.addBodies(w, static_cast<int>(p.bodies.size()), p.bodies.data(), nullptr);
+        const int l = p.forces.empty() ? 0 : 1;
+        Lane &lane = *lanes[l];
+        Lane &other = *lanes[1 - l];
+        const auto retry = [&] {
+            if (shrunk || !other.resident.empty())
+                return false;
+            shrunk = true;
+            return other.eng.shrinkEmpty() == AVBDG_OK;
+        };
+        limitLane(l);
+        const int w = lane.eng.addWorld();
+        if (w < 0) { // the store cannot grow now
+            if (retry())
+                continue;
+            break; // retry next tick
+        }
+        int rc = lane.eng.addBodies(w, static_cast<int>(p.bodies.size()), p.bodies.data(), nullptr);
         if (rc == AVBDG_OK)
-            rc = eng.addForces(w, static_cast<int>(p.forces.size()), p.forces.data());
+            rc = lane.eng.addForces(w, static_cast<int>(p.forces.size()), p.forces.data());
         if (rc != AVBDG_OK) {
-            const std::string why = eng.error();
-            eng.removeWorlds({w});
-            if (rc == AVBDG_ERR_CAPACITY)
-                break; // the byte limit bit before the budget estimate did; retry next tick
+            const std::string why = lane.eng.error();
+            lane.eng.removeWorlds({w});
+            if (rc == AVBDG_ERR_CAPACITY) { // the byte limit bit before the budget estimate did
+                if (retry())
+                    continue;
+                break; // retry next tick
+            }
             return fail(rc, why);
         }
-        resident.push_back(Resident{p.id, p.steps, static_cast<int>(p.bodies.size()), eng.worldDynamic(w), p.bytes,
-                                    p.submitted});
+        lane.resident.push_back(Resident{p.id, p.steps, static_cast<int>(p.bodies.size()), lane.eng.worldDynamic(w),
+                                         p.bytes, p.submitted});
         residentBytes += p.bytes;
         admitted++;
         queue.pop_front();
@@ -105,46 +154,73 @@ int Server::tick(int &completedNow) {
     int rc = admitQueued();
     if (rc != AVBDG_OK)
         return rc;
-    if (resident.empty())
+    if (residentCount() == 0)
         return AVBDG_OK; // nothing on the device: not a tick
     const Clock::time_point t1 = Clock::now();
-    rc = eng.step();
-    if (rc != AVBDG_OK)
-        return rc;
+    // Every lane's step goes to its stream before any is waited for; a lane's counters are then
+    // checked (and its store grown) one lane after the other.
+    bool stepped[kLanes] = {};
+    int failed = AVBDG_OK;
+    for (int l = 0; l < kLanes && failed == AVBDG_OK; l++) {
+        if (lanes[l]->resident.empty())
+            continue;
+        rc = lanes[l]->eng.stepEnqueue();
+        if (rc != AVBDG_OK)
+            failed = engineFail(lanes[l]->eng, rc);
+        else
+            stepped[l] = true;
+    }
+    for (int l = 0; l < kLanes; l++) {
+        if (!stepped[l])
+            continue;
+        limitLane(l);
+        rc = lanes[l]->eng.stepFinish(); // a lane enqueued before a failure is still finished
+        if (rc != AVBDG_OK && failed == AVBDG_OK)
+            failed = engineFail(lanes[l]->eng, rc);
+    }
+    if (failed != AVBDG_OK)
+        return failed;
     const Clock::time_point t2 = Clock::now();
-    graphTicks += eng.lastStepWasGraph() ? 1 : 0;
-    double dyn = 0.0;
-    std::vector<int> done;
-    for (size_t i = 0; i < resident.size(); i++) {
-        dyn += resident[i].dynamic;
-        if (--resident[i].stepsLeft <= 0)
-            done.push_back(static_cast<int>(i));
+    bool allGraphs = true;
+    for (int l = 0; l < kLanes; l++)
+        if (stepped[l])
+            allGraphs = allGraphs && lanes[l]->eng.lastStepWasGraph();
+    graphTicks += allGraphs ? 1 : 0;
+    for (auto &lanePtr : lanes) {
+        Lane &lane = *lanePtr;
+        double dyn = 0.0;
+        std::vector<int> done;
+        for (size_t i = 0; i < lane.resident.size(); i++) {
+            dyn += lane.resident[i].dynamic;
+            if (--lane.resident[i].stepsLeft <= 0)
+                done.push_back(static_cast<int>(i));
+        }
+        bodySteps += dyn;
+        for (int w : done) {
+            const Resident &r = lane.resident[w];
+            Result res;
+            res.bodies = r.bodies;
+            const size_t n = static_cast<size_t>(r.bodies);
+            res.state.resize(13 * n);
+            float *s = res.state.data();
+            rc = lane.eng.getState(w, 0, r.bodies, s, s + 3 * n, s + 7 * n, s + 10 * n);
+            if (rc != AVBDG_OK)
+                return engineFail(lane.eng, rc);
+            results.emplace(r.id, std::move(res));
+            ready.push_back(r.id);
+            requestMs.push_back(static_cast<float>(msSince(r.submitted)));
+            residentBytes -= r.bytes;
+            completed++;
+        }
+        if (!done.empty()) {
+            rc = lane.eng.removeWorlds(done);
+            if (rc != AVBDG_OK)
+                return engineFail(lane.eng, rc);
+            for (auto it = done.rbegin(); it != done.rend(); ++it)
+                lane.resident.erase(lane.resident.begin() + *it);
+        }
+        completedNow += static_cast<int>(done.size());
     }
-    bodySteps += dyn;
-    for (int w : done) {
-        const Resident &r = resident[w];
-        Result res;
-        res.bodies = r.bodies;
-        const size_t n = static_cast<size_t>(r.bodies);
-        res.state.resize(13 * n);
-        float *s = res.state.data();
-        rc = eng.getState(w, 0, r.bodies, s, s + 3 * n, s + 7 * n, s + 10 * n);
-        if (rc != AVBDG_OK)
-            return rc;
-        results.emplace(r.id, std::move(res));
-        ready.push_back(r.id);
-        requestMs.push_back(static_cast<float>(msSince(r.submitted)));
-        residentBytes -= r.bytes;
-        completed++;
-    }
-    if (!done.empty()) {
-        rc = eng.removeWorlds(done);
-        if (rc != AVBDG_OK)
-            return rc;
-        for (auto it = done.rbegin(); it != done.rend(); ++it)
-            resident.erase(resident.begin() + *it);
-    }
-    completedNow = static_cast<int>(done.size());
     const double ms = msSince(t0);
     admitMs += std::chrono::duration<double, std::milli>(t1 - t0).count();
     stepMs += std::chrono::duration<double, std::milli>(t2 - t1).count();
@@ -197,16 +273,19 @@ int Server::evict(int64_t id) {
             evicted++;
             return AVBDG_OK;
         }
-    for (size_t i = 0; i < resident.size(); i++)
-        if (resident[i].id == id) {
-            const int rc = eng.removeWorlds({static_cast<int>(i)});
-            if (rc != AVBDG_OK)
-                return rc;
-            residentBytes -= resident[i].bytes;
-            resident.erase(resident.begin() + static_cast<long>(i));
-            evicted++;
-            return AVBDG_OK;
-        }
+    for (auto &lanePtr : lanes) {
+        Lane &lane = *lanePtr;
+        for (size_t i = 0; i < lane.resident.size(); i++)
+            if (lane.resident[i].id == id) {
+                const int rc = lane.eng.removeWorlds({static_cast<int>(i)});
+                if (rc != AVBDG_OK)
+                    return engineFail(lane.eng, rc);
+                residentBytes -= lane.resident[i].bytes;
+                lane.resident.erase(lane.resident.begin() + static_cast<long>(i));
+                evicted++;
+                return AVBDG_OK;
+            }
+    }
     if (results.erase(id)) {
         ready.erase(std::remove(ready.begin(), ready.end(), id), ready.end());
         return AVBDG_OK;
@@ -222,13 +301,15 @@ void Server::stats(avbdg_server_stats &out) const {
     out.evicted = evicted;
     out.ticks = ticks;
     out.queued = static_cast<int>(queue.size());
-    out.resident = static_cast<int>(resident.size());
-    for (const Resident &r : resident) {
-        out.resident_bodies += r.bodies;
-        out.resident_dynamic += r.dynamic;
+    out.resident = residentCount();
+    for (const auto &lane : lanes) {
+        for (const Resident &r : lane->resident) {
+            out.resident_bodies += r.bodies;
+            out.resident_dynamic += r.dynamic;
+        }
+        out.store_bytes += lane->eng.reservedBytes();
     }
     out.resident_bytes = residentBytes;
-    out.store_bytes = eng.reservedBytes();
     out.budget_bytes = budget;
     out.body_steps = bodySteps;
     out.busy_ms = busyMs;

@@ -10,14 +10,20 @@
 //     tree resident between ticks;
 //   * advances every resident scene by one Solver::step per tick, all of them in the same launches;
 //   * downloads a scene's final state when its steps are done and removes it from the store.
-// A scene's results are the same as stepping it alone: worlds in one store share no state, and
-// removal keeps every survivor's live and force order.
+// Scenes without forces and scenes with joints or springs are kept in two stores (lanes), each
+// with its own CUDA stream: a store holding any force takes the coloured Gauss-Seidel passes, the
+// deferred Jacobi update and the force duals for every body in it, and its dataflow sweeps wait
+// along the longest chains, so the contact-only scenes step apart from them, and a tick hands both
+// stores' steps to the device before it waits for either. A scene's results are the same as
+// stepping it alone: worlds in one store share no state, and removal keeps every survivor's live
+// and force order.
 #pragma once
 
 #include <chrono>
 #include <cstdint>
 #include <deque>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -29,6 +35,8 @@ namespace avbdg {
 class Server {
 public:
     Server(const avbdg_params &params, uint64_t budgetBytes, int maxResident);
+    // Solver parameters of every lane.
+    int setParams(const avbdg_params &p);
 
     // Queue a scene (bodies and forces in creation order) for `steps` steps. Rejected at once when
     // it is invalid or could never fit the budget.
@@ -44,8 +52,7 @@ public:
     void stats(avbdg_server_stats &out) const;
     void resetStats();
 
-    Engine &engine() { return eng; }
-    const std::string &error() const { return err.empty() ? eng.error() : err; }
+    const std::string &error() const { return err; }
 
 private:
     using Clock = std::chrono::steady_clock;
@@ -73,12 +80,26 @@ private:
         return code;
     }
     int admitQueued();
+    // An engine call failed: keep its message and pass its code on.
+    int engineFail(const Engine &e, int code) {
+        err = e.error();
+        return code;
+    }
+    int residentCount() const;
+    // A lane may grow up to the budget less what the other lane's store holds now.
+    void limitLane(int lane);
 
-    Engine eng;
+    // Lane 0: scenes without forces; lane 1: scenes with forces.
+    static constexpr int kLanes = 2;
+    struct Lane {
+        Engine eng;
+        std::vector<Resident> resident; // in the store's world order
+        Lane(const avbdg_params &params, int bodies, int forces, int worlds) : eng(params, bodies, forces, worlds) {}
+    };
+    std::unique_ptr<Lane> lanes[kLanes];
     uint64_t budget;
     int maxResident;
     std::deque<Pending> queue;
-    std::vector<Resident> resident; // in the store's world order
     std::map<int64_t, Result> results;
     std::deque<int64_t> ready;
     uint64_t residentBytes = 0;
