@@ -67,6 +67,8 @@ def test_gpu_served_same_alone_and_in_mix(pkg, gpu):
     steps = [25, 40, 10, 30, 35, 12, 20]
     arrive = [0, 0, 3, 5, 5, 11, 17]  # tick at which each request is submitted
     reqs = _requests(pkg, sizes, steps)
+    # Jointed and contact-only scenes: both of the server's stores run.
+    assert {bool(r.joints) for r in reqs} == {True, False}
     p = gpu.default_params()
     pkg.scenes.apply_params(p, pkg.scenes.BENCH_PARAMS)
     srv = capi.Server(gpu.lib, p, budget_bytes=8 * 10**9, max_resident=64)
@@ -96,6 +98,9 @@ def test_gpu_server_budget_and_eviction(pkg, gpu):
     evicted request leaves the others exact; a scene larger than the budget is refused."""
     capi = pkg.capi
     reqs = _requests(pkg, [1500, 1200, 1000, 900], [6, 5, 4, 8], seed=3)
+    # The first scene has no joints and the next ones do: the jointed store can only grow once the
+    # contact-only store, emptied, gives its bytes back.
+    assert not reqs[0].joints and reqs[1].joints
     p = gpu.default_params()
     pkg.scenes.apply_params(p, pkg.scenes.BENCH_PARAMS)
     # The device bytes a request is charged, read from a server that admits the largest one.
