@@ -532,15 +532,42 @@ __global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
 // also run by the tile queue of the round loop.
 // RO: poses are read-only for the whole launch (read-only cache path); false inside the round-loop
 // tile queue, which writes them in the same launch.
+// The flags of a manifold's two bodies the dual reads before its poses (awake: mass and not
+// asleep; in the update set; colour), loaded together: each is a word or a byte of a valid body, so
+// none waits for another to decide whether it is needed.
+struct PairFlags {
+    bool awakeA, awakeB;
+    int sides;    // overflow sides that take stamps (kSideA | kSideB)
+    bool touches; // a coloured body touches the manifold
+};
+
+template <bool STAMPS>
+__device__ __forceinline__ PairFlags loadPairFlags(const Dev &d, int2 ab) {
+    const real wA = d.x[ab.x].w, wB = d.x[ab.y].w;
+    const int sA = d.sleep[ab.x].x, sB = d.sleep[ab.y].x;
+    PairFlags f;
+    f.awakeA = (wA > 0.0f) & (sA == 0);
+    f.awakeB = (wB > 0.0f) & (sB == 0);
+    f.sides = 0;
+    f.touches = false;
+    if (STAMPS) { // overflowSides, with the colour read whether or not the body is in the set
+        const bool dynA = d.upd[ab.x] != 0, dynB = d.upd[ab.y] != 0;
+        const uint8_t cA = d.colour[ab.x], cB = d.colour[ab.y];
+        f.touches = (dynA & (cA < kOverflowColour)) | (dynB & (cB < kOverflowColour));
+        f.sides = ((dynA & (cA == kOverflowColour)) ? kSideA : 0) | ((dynB & (cB == kOverflowColour)) ? kSideB : 0);
+    }
+    return f;
+}
+
 template <bool STAMPS, bool ARM, bool RO = true>
 __device__ __forceinline__ void dualAt(const Dev &d, const StepParams &p, real decay, int m) {
     const ManifoldBuf L = d.live;
     const int2 ab = __ldg(&L.ab[m]);
-    if (!isAwake(d, ab.x) && !isAwake(d, ab.y))
+    const PairFlags flags = loadPairFlags<STAMPS>(d, ab);
+    if (!flags.awakeA && !flags.awakeB)
         return; // frozen (manifold.cpp:168-172)
-    bool touches = false;
-    int sides = STAMPS ? overflowSides(d, ab, touches) : 0;
-    if (touches)
+    int sides = flags.sides;
+    if (flags.touches)
         sides = 0; // recomputed after the colour passes
     const Pose A = RO ? loadPoseRO(d, ab.x) : loadPose(d, ab.x), B = RO ? loadPoseRO(d, ab.y) : loadPose(d, ab.y);
     const real4 b04 = __ldg(&L.b0[m]);
@@ -958,7 +985,11 @@ __device__ __noinline__ void fallbackSolve(const Dev &d, const StepParams &p, in
 // its stamps, so it updates in place with the same floats.
 template <bool FORCES, bool RO = true>
 __device__ __forceinline__ void solveAt(const Dev &d, const StepParams &p, int g, int inPlace) {
-    if (d.meta[g].x < 0 || !inUpdate(d, g) || d.colour[g] != kOverflowColour)
+    // The three checks' loads go out together (non-short-circuit: all three are valid reads).
+    const int world = d.meta[g].x;
+    const bool updated = d.upd[g] != 0;
+    const uint8_t colour = d.colour[g];
+    if ((world < 0) | !updated | (colour != kOverflowColour))
         return;
     if (!inPlace && !bodyHasForce(d, g, nForcesDev(d)))
         inPlace = 1;
