@@ -20,17 +20,20 @@ __device__ __forceinline__ void stReleaseU32(unsigned *p, unsigned v) {
 // they set kErrBarrierTimeout and the barrier returns false; every block then leaves the kernel,
 // and the step reports the timeout). The arrival count must be zero when the launch starts (the
 // launchers clear it). Writes before the barrier are visible to every block after it.
-__device__ __forceinline__ bool gridSync(const Dev &d) {
+// `participants`: the blocks that take part (blocks 0 .. participants-1; the others have left the
+// kernel and never call it); the whole grid by default.
+__device__ __forceinline__ bool gridSync(const Dev &d, unsigned participants = 0) {
     __shared__ int ok;
     __syncthreads();
-    if (gridDim.x == 1)
+    const unsigned blocks = participants ? participants : gridDim.x;
+    if (blocks == 1)
         return true; // one block: the block barrier orders its own global writes
     if (threadIdx.x == 0) {
         ok = 1;
         volatile int *errors = d.ctr + C_ERRORS;
         const unsigned gen = ldAcquireU32(d.gridBar + 1);
         __threadfence(); // this block's writes before its arrival
-        if (atomicAdd(d.gridBar, 1u) + 1u == gridDim.x) {
+        if (atomicAdd(d.gridBar, 1u) + 1u == blocks) {
             d.gridBar[0] = 0;
             __threadfence();
             stReleaseU32(d.gridBar + 1, gen + 1u);

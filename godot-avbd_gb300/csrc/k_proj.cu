@@ -466,23 +466,30 @@ __global__ void projCheckKernel(Dev d, real tolerance) {
 __global__ void __launch_bounds__(kThreads) projectionKernel(Dev d, StepParams p, real tolerance) {
     pdlWait();
     pdlTrigger();
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int stride = gridDim.x * blockDim.x;
     const int nWorlds = d.ctr[C_WORLDS];
     const int nBodies = d.ctr[C_BODIES];
+    // The grid is sized by the store's capacities; only the blocks this step's counts need take
+    // part (every block reads the same counts, which nothing changes during the launch), so a
+    // small store's barriers are a block barrier.
+    const int items = max(max(d.ctr[C_LIVE], nBodies), nWorlds);
+    const unsigned active = static_cast<unsigned>(min(static_cast<int>(gridDim.x), max(1, (items + kThreads - 1) / kThreads)));
+    if (blockIdx.x >= active)
+        return;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int stride = static_cast<int>(active) * blockDim.x;
     for (int w = tid; w < nWorlds; w += stride) {
         d.wStop[w] = d.wActive[w] > 0 ? 0 : 1;
         d.wMaxDepth[w] = 0;
     }
     for (int it = 0; it < p.projIters; it++) {
-        if (!gridSync(d))
+        if (!gridSync(d, active))
             return;
         projManifoldPass(d, p, blockIdx.x * blockDim.x, stride);
-        if (!gridSync(d))
+        if (!gridSync(d, active))
             return;
         for (int g = tid; g < nBodies; g += stride)
             projBodyAt(d, p, g);
-        if (!gridSync(d))
+        if (!gridSync(d, active))
             return;
         for (int w = tid; w < nWorlds; w += stride) {
             if (!d.wStop[w] && bitsf(d.wMaxDepth[w]) <= tolerance)
