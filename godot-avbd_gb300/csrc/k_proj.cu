@@ -531,9 +531,11 @@ void launchBrake(const Dev &d, real window, cudaStream_t s) {
     Dev dd = d;
     real win = window;
     void *args[] = {&dd, &win};
+    // No more blocks than the store's manifolds can fill (the list is a subset of them).
+    const int want = divUp(d.MM > 0 ? d.MM : 1, kBrakeThreads), most = brakeGridBlocks();
     ++launchCount();
-    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(brakeKernel), dim3(brakeGridBlocks()), dim3(kBrakeThreads),
-                                args, 0, s);
+    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(brakeKernel), dim3(want < most ? want : most),
+                                dim3(kBrakeThreads), args, 0, s);
 }
 
 static int g_projBlocks = 0;

@@ -1449,13 +1449,14 @@ void prepareKernels() {
 void launchColour(const Dev &d, bool needGreedy, bool everyWorld, cudaStream_t s) {
     if (!needGreedy)
         return;
-    colourGridBlocks();
+    // No more blocks than the store's bodies can fill.
+    const int want = divUp(d.NB > 0 ? d.NB : 1, kColourThreads), most = colourGridBlocks();
     Dev dd = d;
     int every = everyWorld ? 1 : 0;
     void *args[] = {&dd, &every};
     ++launchCount();
-    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(colourFlowKernel), dim3(g_colourBlocks), dim3(kColourThreads),
-                                args, 0, s);
+    cudaLaunchCooperativeKernel(reinterpret_cast<void *>(colourFlowKernel), dim3(want < most ? want : most),
+                                dim3(kColourThreads), args, 0, s);
 }
 
 void launchColourLists(const Dev &d, int contactOnlyOverflow, cudaStream_t s) {
