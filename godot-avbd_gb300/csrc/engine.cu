@@ -859,8 +859,11 @@ Engine::StepPlan Engine::planStep(int mode, int substeps, int rounds) {
     plan.rounds = rounds;
     plan.adjAtStart = !adjValid;
     plan.anyTree = false;
-    for (int c : wCount)
+    plan.brute = true;
+    for (int c : wCount) {
         plan.anyTree = plan.anyTree || c >= 2;
+        plan.brute = plan.brute && c <= kBruteMaxBodies;
+    }
     // Rebuild from fresh Morton codes when the body set changed or after kRefitBudget refits
     // (bvh_broadphase.cpp:186-203), so the code/order dumps follow the reference's schedule.
     plan.rebuild = plan.anyTree && (!treeValid || treeAge >= kRefitBudget);
@@ -882,9 +885,9 @@ Engine::StepPlan Engine::planStep(int mode, int substeps, int rounds) {
 
 std::string Engine::StepPlan::key() const {
     char buf[128];
-    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0,
+    std::snprintf(buf, sizeof(buf), "%d/%d/%d/%d%d%d%d%d%d%d%d", mode, substeps, rounds, adjAtStart ? 1 : 0,
                   anyTree ? 1 : 0, rebuild ? 1 : 0, forces ? 1 : 0, greedy ? 1 : 0, multiWorld ? 1 : 0,
-                  round ? 1 : 0);
+                  round ? 1 : 0, brute ? 1 : 0);
     return buf;
 }
 
@@ -904,11 +907,14 @@ int Engine::broadPhase(const StepParams &sp, const StepPlan &plan) {
         cudaMemcpyAsync(d.ctr + C_CAND, d.ctr + C_LIVE, sizeof(int), cudaMemcpyDeviceToDevice, stream);
         return AVBDG_OK;
     }
+    // The tree is rebuilt on the reference's schedule either way (its codes and order are dumped);
+    // the all-pairs test needs no bounds, so only the tree walk refits it.
     if (plan.rebuild)
         launchRebuildTree(d, plan.multiWorld, stream);
-    launchRefit(d, stream);
+    if (!plan.brute)
+        launchRefit(d, stream);
     beginSpan();
-    launchPairs(d, tuned.traverse, stream);
+    launchPairs(d, tuned.traverse, plan.brute, stream);
     endSpan(kTraverse);
     launchFilterAcquire(d, stream);
     if (sp.sleepFrames > 0)

@@ -166,6 +166,9 @@ private:
     Tuned tuned;
     Tuned tunedBase; // the default sizes, each replaced by the largest candidate that launches if it does not
     static constexpr int kTuneDelay = 4, kTuneTrials = 8;
+    // Largest world whose candidate pairs come from the all-pairs test: each body of it walks up to
+    // this many candidates, which costs less than refitting and walking the tree below this size.
+    static constexpr int kBruteMaxBodies = 512;
     bool tuneEnabled = true, tuning = false;
     int tuneTrial = 0;
     double tuneMs[kKinds][kTuneCandidates] = {};
@@ -209,6 +212,7 @@ private:
         int substeps = 1, rounds = 0;
         bool adjAtStart = false, anyTree = false, rebuild = false, forces = false, greedy = false;
         bool multiWorld = false, round = false;
+        bool brute = false; // pairs by the all-pairs test within each world instead of the tree
         std::string key() const;
     };
     struct Graph {

@@ -387,6 +387,58 @@ __global__ void traverseKernel(Dev d) {
     }
 }
 
+// The same partner search without the tree, for stores whose worlds are all small: body g tests
+// every body of its world with a larger list position (a smaller slot: lp = 2 base + count - 1 -
+// slot) with the traversal's own closed-box test, and hands on the same count, stash and spill list
+// (EMIT: the same second pass for bodies with more than kPairStash partners), so the pair set and
+// everything after it are the traversal's. Threads take bodies in slot order; the threads of one
+// world read the same candidate on each iteration (one broadcast load).
+template <bool EMIT>
+__global__ void bruteKernel(Dev d) {
+    pdlWait();
+    pdlTrigger();
+    const int n = EMIT ? d.ctr[C_PAIRSPILL] : d.ctr[C_BODIES];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const int g = EMIT ? d.pairSpill[i] : i;
+    const int w = d.meta[g].x;
+    if (w < 0)
+        return;
+    const int base = d.wBase[w], cnt = d.wCount[w];
+    const int lpA = 2 * base + cnt - 1 - g;
+    int out = EMIT ? d.pairStart[lpA] : 0;
+    int found = 0;
+    int *stash = d.pairStash + static_cast<size_t>(lpA) * kPairStash;
+    if (cnt >= 2) {
+        const real4 c4 = d.aabbC[g], h4 = d.aabbH[g];
+        const f3 aMin{c4.x - h4.x, c4.y - h4.y, c4.z - h4.z};
+        const f3 aMax{c4.x + h4.x, c4.y + h4.y, c4.z + h4.z};
+#pragma unroll 4
+        for (int b = base; b < g; b++) {
+            const real4 bc = d.aabbC[b], bh = d.aabbH[b];
+            const f3 bMin{bc.x - bh.x, bc.y - bh.y, bc.z - bh.z};
+            const f3 bMax{bc.x + bh.x, bc.y + bh.y, bc.z + bh.z};
+            if (overlapClosed(aMin, aMax, bMin, bMax)) {
+                const int lpB = 2 * base + cnt - 1 - b;
+                if (EMIT) {
+                    if (out < d.PP)
+                        d.pairs[out] = (static_cast<uint64_t>(lpA) << 32) | static_cast<uint32_t>(lpB);
+                    out++;
+                } else if (found < kPairStash) {
+                    stash[found] = lpB;
+                }
+                found++;
+            }
+        }
+    }
+    if (!EMIT) {
+        d.pairStart[lpA] = found;
+        if (found > kPairStash)
+            d.pairSpill[atomicAdd(&d.ctr[C_PAIRSPILL], 1)] = g;
+    }
+}
+
 // Stashed partners into their body's segment (bodies with more partners are walked again).
 __global__ void pairStashKernel(Dev d) {
     pdlWait();
@@ -517,17 +569,26 @@ void launchRefit(const Dev &d, cudaStream_t s) {
 }
 
 bool traverseBlockFits(int block) {
-    return blockFits(traverseKernel<false>, block) && blockFits(traverseKernel<true>, block);
+    return blockFits(traverseKernel<false>, block) && blockFits(traverseKernel<true>, block) &&
+           blockFits(bruteKernel<false>, block) && blockFits(bruteKernel<true>, block);
 }
 
-void launchPairs(const Dev &d, int block, cudaStream_t s) {
+void launchPairs(const Dev &d, int block, bool brute, cudaStream_t s) {
     cudaMemsetAsync(d.pairStart, 0, sizeof(int) * static_cast<size_t>(d.NB + 1), s);
     cudaMemsetAsync(d.ctr + C_PAIRSPILL, 0, sizeof(int), s);
-    ++launchCount(); launchK(traverseKernel<false>, divUp(d.NB, block), block, 0, s, d);
+    ++launchCount();
+    if (brute)
+        launchK(bruteKernel<false>, divUp(d.NB, block), block, 0, s, d);
+    else
+        launchK(traverseKernel<false>, divUp(d.NB, block), block, 0, s, d);
     scanExclusive(d.pairStart, d.pairStart, d.NB + 1, nullptr, d.ctr + C_TMP, d.scanScratch, s);
     ++launchCount(); launchK(pairTotalKernel, 1, 1, 0, s, d);
     ++launchCount(); launchK(pairStashKernel, divUp(d.NB, kThreads), kThreads, 0, s, d);
-    ++launchCount(); launchK(traverseKernel<true>, divUp(d.NB, block), block, 0, s, d);
+    ++launchCount();
+    if (brute)
+        launchK(bruteKernel<true>, divUp(d.NB, block), block, 0, s, d);
+    else
+        launchK(traverseKernel<true>, divUp(d.NB, block), block, 0, s, d);
     segmentedSortU64(d.pairs, d.pairsTmp, d.pairStart, d.NB, d.ctr + C_BODIES, d.longList, d.ctr + C_LONG, s);
 }
 

@@ -26,7 +26,9 @@ void launchAabb(const Dev &d, const StepParams &p, cudaStream_t s);
 void launchRebuildTree(const Dev &d, bool multiWorld, cudaStream_t s);
 void launchRefit(const Dev &d, cudaStream_t s);
 // Candidate pairs: traversal count, scan, emit, per-segment sort. Leaves the count in C_PAIRS.
-void launchPairs(const Dev &d, int block, cudaStream_t s);
+// `brute`: every world of the store is small, and each body tests its world's bodies directly
+// (the same pair set; the tree's bounds are not needed).
+void launchPairs(const Dev &d, int block, bool brute, cudaStream_t s);
 // Exact filter and acquisition of new manifolds after the live ones (C_CAND = C_LIVE + new).
 void launchFilterAcquire(const Dev &d, cudaStream_t s);
 
