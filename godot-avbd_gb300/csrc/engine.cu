@@ -125,6 +125,8 @@ void layoutStore(Dev &n, int nb, int mm, int ff, int pp, int ww, bool arm, Take 
     take(n.nodeMaxLp, nb);
     take(n.nodeMin, nb);
     take(n.nodeMax, nb);
+    take(n.nodeKids, 4 * static_cast<size_t>(nb));
+    take(n.nodeLink, nb);
     take(n.pairStart, static_cast<size_t>(nb) + 1);
     take(n.pairs, pp);
     take(n.pairsTmp, pp);

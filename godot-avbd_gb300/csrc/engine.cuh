@@ -135,6 +135,11 @@ struct Dev {
     int *nodeL, *nodeR, *nodeParent, *leafParent, *nodeFlag;
     int *nodeMaxLp;         // largest list position in the subtree (prunes the pair walk)
     real4 *nodeMin, *nodeMax;
+    // What the pair walk reads at an internal node, written by the refit in one place: its
+    // children's boxes (left min, left max, right min, right max) and (left, right, largest list
+    // position under the left child, under the right child; a leaf's own position).
+    real4 *nodeKids;
+    int4 *nodeLink;
     // pairs
     int *pairStart;         // per list position (+1)
     uint64_t *pairs, *pairsTmp;

@@ -303,6 +303,12 @@ __global__ void refitKernel(Dev d) {
         const int ml = (l & kLeafBit) ? static_cast<int>(d.sortV[l & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[l]);
         const int mr = (r & kLeafBit) ? static_cast<int>(d.sortV[r & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[r]);
         __stcg(&d.nodeMaxLp[node], ml > mr ? ml : mr);
+        real4 *kids = d.nodeKids + 4 * static_cast<size_t>(node);
+        __stcg(kids, a0);
+        __stcg(kids + 1, a1);
+        __stcg(kids + 2, b0);
+        __stcg(kids + 3, b1);
+        __stcg(&d.nodeLink[node], make_int4(l, r, ml, mr));
         node = d.nodeParent[node];
     }
 }
@@ -345,17 +351,22 @@ __global__ void traverseKernel(Dev d) {
         stack[sp++] = d.wBase[w];
         while (sp > 0) {
             const int node = stack[--sp];
-            const int kids[2] = {d.nodeL[node], d.nodeR[node]};
+            // One visit reads the node's record: both children, their boxes and list positions
+            // (a leaf's box is c -/+ h of its body, the floats the test below used to compute).
+            const int4 link = d.nodeLink[node];
+            const real4 *kidBox = d.nodeKids + 4 * static_cast<size_t>(node);
+            const real4 boxes[4] = {kidBox[0], kidBox[1], kidBox[2], kidBox[3]};
+            const int kids[2] = {link.x, link.y};
+            const int kidLp[2] = {link.z, link.w};
             for (int k = 0; k < 2; k++) {
                 const int c = kids[k];
+                const real4 mn = boxes[2 * k], mx = boxes[2 * k + 1];
                 if (c & kLeafBit) {
-                    const int b = d.leafBody[c & ~kLeafBit];
-                    const int lpB = listPos(d, b);
+                    const int lpB = kidLp[k];
                     if (lpB <= lpA)
                         continue;
-                    const real4 bc = d.aabbC[b], bh = d.aabbH[b];
-                    const f3 bMin{bc.x - bh.x, bc.y - bh.y, bc.z - bh.z};
-                    const f3 bMax{bc.x + bh.x, bc.y + bh.y, bc.z + bh.z};
+                    const f3 bMin{mn.x, mn.y, mn.z};
+                    const f3 bMax{mx.x, mx.y, mx.z};
                     if (overlapClosed(aMin, aMax, bMin, bMax)) {
                         if (EMIT) {
                             if (out < d.PP)
@@ -367,9 +378,8 @@ __global__ void traverseKernel(Dev d) {
                         found++;
                     }
                 } else {
-                    if (d.nodeMaxLp[c] <= lpA)
+                    if (kidLp[k] <= lpA)
                         continue; // every leaf below was emitted by a partner with a smaller position
-                    const real4 mn = d.nodeMin[c], mx = d.nodeMax[c];
                     if (overlapClosed(aMin, aMax, f3{mn.x, mn.y, mn.z}, f3{mx.x, mx.y, mx.z})) {
                         if (sp < kStack)
                             stack[sp++] = c;

@@ -379,9 +379,13 @@ __device__ __forceinline__ void projManifoldPass(const Dev &d, const StepParams 
 
 // One body's averaged correction of a pass: its contributions in adjacency order, capped, applied.
 __device__ __forceinline__ void projBodyAt(const Dev &d, const StepParams &p, int g) {
-    if (d.meta[g].x < 0 || !movable(d, g))
+    // The checks' loads go out together (valid reads of body g), then its world's stop flag.
+    const int world = d.meta[g].x;
+    const real mass = d.x[g].w;
+    const bool updated = inUpdate(d, g);
+    if ((world < 0) | !((mass > 0.0f) & updated))
         return;
-    if (d.wStop[d.meta[g].x])
+    if (d.wStop[world])
         return;
     const int nf = d.ctr[C_FORCES];
     f3 sl{0, 0, 0}, sa{0, 0, 0};

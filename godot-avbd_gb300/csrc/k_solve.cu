@@ -439,16 +439,6 @@ __device__ __forceinline__ f3 contactError(const StepParams &p, f3 C0, f3 bracke
 
 enum : int { kSideA = 1, kSideB = 2 };
 
-// Which sides of manifold m take stamps for the block-Jacobi solve, and whether a coloured body
-// touches it.
-__device__ __forceinline__ int overflowSides(const Dev &d, int2 ab, bool &touchesColour) {
-    const bool dynA = inUpdate(d, ab.x), dynB = inUpdate(d, ab.y);
-    const uint8_t ca = dynA ? d.colour[ab.x] : kUncoloured;
-    const uint8_t cb = dynB ? d.colour[ab.y] : kUncoloured;
-    touchesColour = (dynA && ca < kOverflowColour) || (dynB && cb < kOverflowColour);
-    return ((dynA && ca == kOverflowColour) ? kSideA : 0) | ((dynB && cb == kOverflowColour) ? kSideB : 0);
-}
-
 // Stamp record: lin (6 unique), rhsLin (signed), ang (6 unique), rhsAng (signed), cross (9).
 __device__ __forceinline__ void storeStamp(real4 *dst, const SharedAcc &sh, const SideAcc &sd, real side) {
     const f3 rl = scale(sh.rhsLin, side);
@@ -506,32 +496,6 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
         storeStamp(d.stamps + static_cast<size_t>(slot.y) * kStampF4, sh, sb, -1.0f);
 }
 
-__device__ __forceinline__ void stampsAt(Dev d, StepParams p, int mixedOnly, int m) {
-    if (m >= d.ctr[C_LIVE])
-        return;
-    bool touches;
-    const int sides = overflowSides(d, d.live.ab[m], touches);
-    if (!sides || touches != (mixedOnly != 0))
-        return;
-    computeStamps(d, p, m, sides);
-}
-
-__global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
-    pdlWait();
-    pdlTrigger();
-    const int n = d.ctr[C_LIVE];
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
-        stampsAt(d, p, mixedOnly, m);
-}
-
-// Dual pass (ManifoldStore::updateDual, manifold.cpp:583-671) and, with STAMPS, the next round's
-// stamps (the reference's phase-A recompute of each force, manifold.cpp:655-659, from the same
-// floats). One thread per manifold, grid-stride over the live ones.
-// ARM: the arm cache is on (compiled out otherwise, so the common path keeps its code).
-// One manifold's dual pass (and, with STAMPS, its next-round stamps): the body of dualKernel's loop,
-// also run by the tile queue of the round loop.
-// RO: poses are read-only for the whole launch (read-only cache path); false inside the round-loop
-// tile queue, which writes them in the same launch.
 // The flags of a manifold's two bodies the dual reads before its poses (awake: mass and not
 // asleep; in the update set; colour), loaded together: each is a word or a byte of a valid body, so
 // none waits for another to decide whether it is needed.
@@ -550,7 +514,8 @@ __device__ __forceinline__ PairFlags loadPairFlags(const Dev &d, int2 ab) {
     f.awakeB = (wB > 0.0f) & (sB == 0);
     f.sides = 0;
     f.touches = false;
-    if (STAMPS) { // overflowSides, with the colour read whether or not the body is in the set
+    if (STAMPS) { // overflow sides take stamps; a coloured side means the colour passes recompute it
+        // (the colour is read whether or not the body is in the update set, and used only if it is)
         const bool dynA = d.upd[ab.x] != 0, dynB = d.upd[ab.y] != 0;
         const uint8_t cA = d.colour[ab.x], cB = d.colour[ab.y];
         f.touches = (dynA & (cA < kOverflowColour)) | (dynB & (cB < kOverflowColour));
@@ -559,6 +524,31 @@ __device__ __forceinline__ PairFlags loadPairFlags(const Dev &d, int2 ab) {
     return f;
 }
 
+__device__ __forceinline__ void stampsAt(Dev d, StepParams p, int mixedOnly, int m) {
+    if (m >= d.ctr[C_LIVE])
+        return;
+    const PairFlags flags = loadPairFlags<true>(d, d.live.ab[m]); // the awake fields are not used here
+    if (!flags.sides || flags.touches != (mixedOnly != 0))
+        return;
+    computeStamps(d, p, m, flags.sides);
+}
+
+__global__ void stampsKernel(Dev d, StepParams p, int mixedOnly) {
+    pdlWait();
+    pdlTrigger();
+    const int n = d.ctr[C_LIVE];
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x)
+        stampsAt(d, p, mixedOnly, m);
+}
+
+// Dual pass (ManifoldStore::updateDual, manifold.cpp:583-671) and, with STAMPS, the next round's
+// stamps (the reference's phase-A recompute of each force, manifold.cpp:655-659, from the same
+// floats). One thread per manifold, grid-stride over the live ones.
+// ARM: the arm cache is on (compiled out otherwise, so the common path keeps its code).
+// One manifold's dual pass (and, with STAMPS, its next-round stamps): the body of dualKernel's loop,
+// also run by the tile queue of the round loop.
+// RO: poses are read-only for the whole launch (read-only cache path); false inside the round-loop
+// tile queue, which writes them in the same launch.
 template <bool STAMPS, bool ARM, bool RO = true>
 __device__ __forceinline__ void dualAt(const Dev &d, const StepParams &p, real decay, int m) {
     const ManifoldBuf L = d.live;
