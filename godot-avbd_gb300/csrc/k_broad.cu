@@ -274,6 +274,15 @@ __device__ __forceinline__ void childBounds(const Dev &d, int c, real4 &mn, real
     }
 }
 
+// Arrival count at a node, acquire-release at GPU scope: it releases this thread's earlier bound
+// writes to the node's other child thread and acquires that thread's, in one instruction instead of
+// a fence on each side of a relaxed add.
+__device__ __forceinline__ int arriveAcqRel(int *flag) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(flag) : "memory");
+    return old;
+}
+
 // Bottom-up refit: the second child to arrive at a node computes its bounds.
 __global__ void refitKernel(Dev d) {
     pdlWait();
@@ -290,10 +299,8 @@ __global__ void refitKernel(Dev d) {
         return;
     int node = d.leafParent[p];
     while (node >= 0) {
-        __threadfence();
-        if (atomicAdd(&d.nodeFlag[node], 1) == 0)
+        if (arriveAcqRel(&d.nodeFlag[node]) == 0)
             return;
-        __threadfence();
         real4 a0, a1, b0, b1;
         const int l = d.nodeL[node], r = d.nodeR[node];
         childBounds(d, l, a0, a1);
