@@ -283,7 +283,10 @@ __device__ __forceinline__ int arriveAcqRel(int *flag) {
     return old;
 }
 
-// Bottom-up refit: the second child to arrive at a node computes its bounds.
+// Bottom-up refit: the second child to arrive at a node computes its bounds. The arriving thread
+// carries the box and largest list position of the child it comes from (the values it stored, or a
+// leaf's c -/+ h) and loads only the other child's; the node's topology is read with the arrival.
+// The bounds are combined as (left, right) in the same order as always.
 __global__ void refitKernel(Dev d) {
     pdlWait();
     pdlTrigger();
@@ -297,18 +300,27 @@ __global__ void refitKernel(Dev d) {
     const int w = d.meta[g].x;
     if (d.wCount[w] < 2)
         return;
+    int child = p | kLeafBit;
+    real4 cMin, cMax;
+    childBounds(d, child, cMin, cMax);
+    int cLp = static_cast<int>(d.sortV[p]);
     int node = d.leafParent[p];
     while (node >= 0) {
+        const int l = d.nodeL[node], r = d.nodeR[node], parent = d.nodeParent[node];
         if (arriveAcqRel(&d.nodeFlag[node]) == 0)
             return;
-        real4 a0, a1, b0, b1;
-        const int l = d.nodeL[node], r = d.nodeR[node];
-        childBounds(d, l, a0, a1);
-        childBounds(d, r, b0, b1);
-        __stcg(&d.nodeMin[node], mk4(mmin2(a0.x, b0.x), mmin2(a0.y, b0.y), mmin2(a0.z, b0.z), 0.0f));
-        __stcg(&d.nodeMax[node], mk4(mmax2(a1.x, b1.x), mmax2(a1.y, b1.y), mmax2(a1.z, b1.z), 0.0f));
-        const int ml = (l & kLeafBit) ? static_cast<int>(d.sortV[l & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[l]);
-        const int mr = (r & kLeafBit) ? static_cast<int>(d.sortV[r & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[r]);
+        const bool fromLeft = l == child;
+        const int other = fromLeft ? r : l;
+        real4 oMin, oMax;
+        childBounds(d, other, oMin, oMax);
+        const int oLp = (other & kLeafBit) ? static_cast<int>(d.sortV[other & ~kLeafBit]) : __ldcg(&d.nodeMaxLp[other]);
+        const real4 a0 = fromLeft ? cMin : oMin, a1 = fromLeft ? cMax : oMax;
+        const real4 b0 = fromLeft ? oMin : cMin, b1 = fromLeft ? oMax : cMax;
+        const int ml = fromLeft ? cLp : oLp, mr = fromLeft ? oLp : cLp;
+        const real4 nMin = mk4(mmin2(a0.x, b0.x), mmin2(a0.y, b0.y), mmin2(a0.z, b0.z), 0.0f);
+        const real4 nMax = mk4(mmax2(a1.x, b1.x), mmax2(a1.y, b1.y), mmax2(a1.z, b1.z), 0.0f);
+        __stcg(&d.nodeMin[node], nMin);
+        __stcg(&d.nodeMax[node], nMax);
         __stcg(&d.nodeMaxLp[node], ml > mr ? ml : mr);
         real4 *kids = d.nodeKids + 4 * static_cast<size_t>(node);
         __stcg(kids, a0);
@@ -316,7 +328,11 @@ __global__ void refitKernel(Dev d) {
         __stcg(kids + 2, b0);
         __stcg(kids + 3, b1);
         __stcg(&d.nodeLink[node], make_int4(l, r, ml, mr));
-        node = d.nodeParent[node];
+        child = node;
+        cMin = nMin;
+        cMax = nMax;
+        cLp = ml > mr ? ml : mr;
+        node = parent;
     }
 }
 
