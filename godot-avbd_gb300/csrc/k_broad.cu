@@ -371,9 +371,10 @@ __global__ void traverseKernel(Dev d) {
         const f3 aMax{c4.x + h4.x, c4.y + h4.y, c4.z + h4.z};
         int stack[kStack];
         int sp = 0;
-        stack[sp++] = d.wBase[w];
-        while (sp > 0) {
-            const int node = stack[--sp];
+        // The next node to visit stays in a register; only a second child to visit goes on the stack.
+        int node = d.wBase[w];
+        while (node >= 0) {
+            int next = -1;
             // One visit reads the node's record: both children, their boxes and list positions
             // (a leaf's box is c -/+ h of its body, the floats the test below used to compute).
             const int4 link = d.nodeLink[node];
@@ -404,13 +405,16 @@ __global__ void traverseKernel(Dev d) {
                     if (kidLp[k] <= lpA)
                         continue; // every leaf below was emitted by a partner with a smaller position
                     if (overlapClosed(aMin, aMax, f3{mn.x, mn.y, mn.z}, f3{mx.x, mx.y, mx.z})) {
-                        if (sp < kStack)
+                        if (next < 0)
+                            next = c;
+                        else if (sp < kStack)
                             stack[sp++] = c;
                         else
                             atomicOr(&d.ctr[C_ERRORS], kErrPairs);
                     }
                 }
             }
+            node = next >= 0 ? next : (sp > 0 ? stack[--sp] : -1);
         }
     }
     if (!EMIT) {

@@ -118,8 +118,9 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
     const int2 ab = L.ab[i];
     const int a = ab.x, b = ab.y;
     const real4 xa4 = d.x[a], xb4 = d.x[b];
+    const int sleepA = d.sleep[a].x, sleepB = d.sleep[b].x; // loaded with the poses, not after them
     const bool dynA = xa4.w > 0.0f, dynB = xb4.w > 0.0f;
-    const bool awakeA = dynA && d.sleep[a].x == 0, awakeB = dynB && d.sleep[b].x == 0;
+    const bool awakeA = dynA & (sleepA == 0), awakeB = dynB & (sleepB == 0);
     int oldN = L.count[i];
     const int2 dorm = L.dormant[i];
     S.ab[i] = ab;
