@@ -216,6 +216,8 @@ Engine::Engine(const avbdg_params &params, int maxBodies, int maxForces, int max
     d.waitLimit = waitLimit;
     const char *queue = std::getenv("AVBDG_QUEUE");
     roundQueue = queue && queue[0] == '1';
+    const char *noBrute = std::getenv("AVBDG_NO_BRUTE");
+    bruteAllowed = !(noBrute && noBrute[0] == '1');
     const char *noTune = std::getenv("AVBDG_NO_TUNE");
     tuneEnabled = !(noTune && noTune[0] == '1');
 #ifdef AVBDG_FP64
@@ -861,7 +863,7 @@ Engine::StepPlan Engine::planStep(int mode, int substeps, int rounds) {
     plan.rounds = rounds;
     plan.adjAtStart = !adjValid;
     plan.anyTree = false;
-    plan.brute = true;
+    plan.brute = bruteAllowed;
     for (int c : wCount) {
         plan.anyTree = plan.anyTree || c >= 2;
         plan.brute = plan.brute && c <= kBruteMaxBodies;

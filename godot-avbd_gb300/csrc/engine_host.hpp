@@ -188,6 +188,7 @@ private:
     // Body state moves straight between the caller's (pageable) arrays and the device, where the
     // device reaches host memory through the host's page tables; else through pinned staging.
     bool roundQueue = false; // AVBDG_QUEUE=1: the round loop as one tile-queue launch where it applies
+    bool bruteAllowed = true; // AVBDG_NO_BRUTE=1: candidate pairs always from the tree walk
     bool stepPending = false; // stepEnqueue ran, stepFinish has not
     int pendingLaunches = 0;  // kernels the pending step launched
     bool directIo = false;

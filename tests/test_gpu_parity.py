@@ -28,10 +28,14 @@ def test_gpu_reproduces_pinned_digests(pkg, gpu, name):
     assert w.digest() == scenes.PINNED_DIGESTS[name]
 
 
+# Candidate pairs come from the all-pairs test within each world for stores of small worlds (every
+# recorded run here) and from the tree walk otherwise; both paths are run against every recording.
+@pytest.mark.parametrize("pair_path", ["direct", "tree"])
 @pytest.mark.parametrize("run", ["stack", "interleaved", "mixed", "hard_chain", "pyramid420", "pile", "lattice",
                                  "shape_mix", "arm_cache", "arm_cache_pile", "arm_cache_sleep", "converge_pile",
                                  "converge_interleaved"])
-def test_gpu_matches_reference_every_step(pkg, gpu, golden, run):
+def test_gpu_matches_reference_every_step(pkg, gpu, golden, monkeypatch, run, pair_path):
+    monkeypatch.setenv("AVBDG_NO_BRUTE", "1" if pair_path == "tree" else "0")
     scenes = pkg.scenes
     rec = golden["runs"][run]
     sc = getattr(scenes, rec["scene"])(**rec["kwargs"])
