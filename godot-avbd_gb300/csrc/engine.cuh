@@ -196,7 +196,6 @@ __device__ __forceinline__ int listPos(const Dev &d, int g) {
 }
 __device__ __forceinline__ bool isDynamic(const Dev &d, int g) { return d.x[g].w > 0.0f; }
 // Movable and not asleep (ManifoldStore::frozen's `awake`, manifold.cpp:168-172).
-__device__ __forceinline__ bool isAwake(const Dev &d, int g) { return d.x[g].w > 0.0f && d.sleep[g].x == 0; }
 // Adjacency entry info: the other body of the entry's force or manifold and this body's side.
 constexpr int kNoBody = 0x7fffffff;
 __device__ __forceinline__ int adjInfoOther(int v) {
