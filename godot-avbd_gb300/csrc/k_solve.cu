@@ -577,6 +577,15 @@ __device__ __forceinline__ void dualAt(const Dev &d, const StepParams &p, real d
     SideAcc sa, sb;
     zeroAcc(sa);
     zeroAcc(sb);
+    // The later contacts' inputs are requested now; the loop below reads them in order.
+    for (int c = 1; c < n; c++) {
+        const int ci = cslot(d, m, c);
+        prefetchL1(&L.rA[ci]);
+        prefetchL1(&L.rB[ci]);
+        prefetchL1(&L.C0[ci]);
+        prefetchL1(&L.k[ci]);
+        prefetchL1(&L.lam[ci]);
+    }
     for (int c = 0; c < n; c++) {
         const int ci = cslot(d, m, c);
         const real4 rA4 = __ldg(&L.rA[ci]);
@@ -873,8 +882,13 @@ __device__ __forceinline__ void assemble(const Dev &d, const StepParams &p, int 
     const int e1 = d.adjStart[g + 1];
     if (!RECOMPUTE && !bodyHasForce(d, g, nf)) {
         // Every entry is a manifold stamped for this body, stored at the entry itself; two records
-        // are loaded before either is added (the sums keep the entry order).
+        // are loaded before either is added (the sums keep the entry order), and the records after
+        // the first pair are requested before any of them.
         int e = d.adjStart[g];
+        for (int f = e + 2; f < e1; f++) {
+            prefetchL1(d.stamps + static_cast<size_t>(f) * kStampF4);
+            prefetchL1(d.stamps + static_cast<size_t>(f) * kStampF4 + kStampF4 - 1);
+        }
         for (; e + 1 < e1; e += 2) {
             const StampRec r0 = loadStampAs<RO>(d.stamps + static_cast<size_t>(e) * kStampF4);
             const StampRec r1 = loadStampAs<RO>(d.stamps + static_cast<size_t>(e + 1) * kStampF4);

@@ -23,6 +23,10 @@ namespace avbdg {
 __device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdlTrigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// A hint that the line holding `p` will be read soon: it is fetched toward this SM's L1 without
+// holding a register or waiting, and the value read later is unchanged.
+__device__ __forceinline__ void prefetchL1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 // AVBDG_NO_PDL=1: plain stream order between kernels (read once per process).
 inline bool pdlEnabled() {
     static const bool on = [] {
