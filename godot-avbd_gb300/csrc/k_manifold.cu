@@ -157,6 +157,16 @@ __device__ __forceinline__ void manifoldInitAt(Dev d, StepParams p, int i) {
     // Grace revival (manifold.cpp:249-253): a dormant manifold matches against its saved contacts.
     if (oldN == 0 && dorm.y > 0)
         oldN = dorm.y;
+    // The old contacts are read after the separating-axis test; their lines are requested now.
+    for (int j = 0; j < oldN; j++) {
+        const int cj = cslot(d, i, j);
+        prefetchL1(&L.key[cj]);
+        prefetchL1(&L.rA[cj]);
+        prefetchL1(&L.rB[cj]);
+        prefetchL1(&L.C0[cj]);
+        prefetchL1(&L.k[cj]);
+        prefetchL1(&L.lam[cj]);
+    }
     const f3 xa = xyz(xa4), xb = xyz(xb4);
     const q4 qa = asq(d.q[a]), qb = asq(d.q[b]);
     const real4 ma4 = d.moment[a], mb4 = d.moment[b];

@@ -327,6 +327,10 @@ __device__ __forceinline__ void projManifoldAt(Dev d, StepParams p, int m, int &
     f3 patchRA{0, 0, 0}, patchRB{0, 0, 0};
     real patchDepth = 0.0f;
     int corrected = 0;
+    for (int k = 1; k < n; k++) { // the later contacts' arms, requested before the in-order loop
+        prefetchL1(&L.rA[cslot(d, m, k)]);
+        prefetchL1(&L.rB[cslot(d, m, k)]);
+    }
     for (int k = 0; k < n; k++) {
         const int ci = cslot(d, m, k);
         const f3 rA = mul(rotA, xyz(L.rA[ci]));

@@ -467,6 +467,14 @@ __device__ void computeStamps(const Dev &d, const StepParams &p, int m, int side
     SideAcc sa, sb;
     zeroAcc(sa);
     zeroAcc(sb);
+    for (int c = 1; c < n; c++) { // the later contacts' lines, requested before the in-order loop
+        const int ci = cslot(d, m, c);
+        prefetchL1(&L.rA[ci]);
+        prefetchL1(&L.rB[ci]);
+        prefetchL1(&L.C0[ci]);
+        prefetchL1(&L.k[ci]);
+        prefetchL1(&L.lam[ci]);
+    }
     for (int c = 0; c < n; c++) {
         const int ci = cslot(d, m, c);
         const f3 rAw = mul(A.rot, xyz(L.rA[ci]));
